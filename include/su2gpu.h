@@ -1,0 +1,218 @@
+/* su2gpu.h -- C ABI of libsu2gpu, the GB300 (sm_103a) implementation of the
+ * su2higgs checkerboard lattice update sweep.
+ *
+ * Every entry point returns an int status (SU2GPU_OK = 0, negative on error)
+ * instead of exiting, and takes plain pointers and sizes.  Field arrays on
+ * the host side are FP64, array-of-structures, in the reference's layout site
+ * order (EVEN sites first, each parity in lexicographic order with x fastest):
+ * exactly the field blocks of the reference's binary lattice file
+ * (src/checkpoint.c:101-115 of su2higgs).  On the device the context keeps
+ * them resident as parity-split structure-of-arrays (FP64, or FP32 in the
+ * precision form).
+ *
+ * Reference entry points replaced (su2higgs, src/):
+ *   update_lattice()           update.c:270      -> su2gpu_update_lattice
+ *   measure() volume sums      measure.c:71-243  -> su2gpu_measure
+ *   grad_flow()                gradflow.c:46     -> su2gpu_grad_flow
+ *   calc_orderparam()          multicanonical.c:709 -> su2gpu_calc_orderparam
+ *   init_last_max()            multicanonical.c:826 -> su2gpu_muca_init_last_max
+ *   load_lattice()/setfields() field upload      -> su2gpu_upload_fields
+ *   save_lattice() field download                -> su2gpu_download_fields
+ */
+#ifndef SU2GPU_H
+#define SU2GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define SU2GPU_OK 0
+#define SU2GPU_ERR_INVALID (-1)     /* bad argument / unsupported configuration */
+#define SU2GPU_ERR_CUDA (-2)        /* CUDA runtime error */
+#define SU2GPU_ERR_NOMEM (-3)       /* device allocation failed */
+#define SU2GPU_ERR_UNSUPPORTED (-4) /* valid for the reference, not implemented on the GPU */
+#define SU2GPU_ERR_KERNEL (-5)      /* a kernel flagged an error (loop cap, bad state) */
+#define SU2GPU_ERR_CAPACITY (-6)    /* request does not fit (serving admission) */
+
+/* ---- field content bits (the reference's compile-time -D flags, Makefile:3-16) ---- */
+#define SU2GPU_HIGGS1 0x01   /* -DNHIGGS=1 */
+#define SU2GPU_HIGGS2 0x02   /* -DNHIGGS=2 */
+#define SU2GPU_TRIPLET 0x04  /* -DTRIPLET */
+#define SU2GPU_SINGLET 0x08  /* -DSINGLET */
+#define SU2GPU_U1 0x10       /* -DU1 */
+#define SU2GPU_GRADFLOW 0x20 /* -DGRADFLOW */
+
+/* ---- update algorithms (generic/stddefs.h:47-49) ---- */
+#define SU2GPU_METROPOLIS 1
+#define SU2GPU_HEATBATH 2
+#define SU2GPU_OVERRELAX 3
+
+/* ---- multicanonical order parameters and modes (stddefs.h:57-65) ---- */
+#define SU2GPU_PHISQ 1
+#define SU2GPU_SIGMASQ 2
+#define SU2GPU_PHI2MINUSSIGMA2 3
+#define SU2GPU_PHI2SQ 4
+#define SU2GPU_MUCA_READONLY 0
+#define SU2GPU_MUCA_FAST 1
+#define SU2GPU_MUCA_SLOW 2
+
+/* Simulation parameters: the action couplings and update recipe of the
+ * reference's params struct (su2.h:76-181), plus the field content and the
+ * device precision.  Field names follow the reference. */
+typedef struct {
+  int32_t dim;                 /* only 3 is supported on the GPU */
+  int32_t L[4];
+  int32_t content;             /* SU2GPU_* content bits */
+  int32_t precision;           /* 64 (plain FP64 path) or 32 (FP32 fields, FP64 reductions) */
+  int32_t algorithm_su2link;   /* HEATBATH or METROPOLIS */
+  int32_t algorithm_u1link;    /* METROPOLIS */
+  int32_t algorithm_su2doublet;/* OVERRELAX or METROPOLIS */
+  int32_t algorithm_su2triplet;/* OVERRELAX or METROPOLIS */
+  int32_t algorithm_singlet;   /* OVERRELAX or METROPOLIS */
+  int32_t update_links;
+  int32_t scalar_sweeps;
+  int32_t update_su2doublet;
+  int32_t update_su2triplet;
+  int32_t update_singlet;
+  int32_t reunitarize_interval;/* FP32 form: renormalise links every n sweeps (0 = never) */
+  int32_t reserved;
+  double betasu2;
+  double msq_phi, lambda_phi;            /* doublet */
+  double msq_triplet, a2, b4;            /* triplet */
+  double betau1, r_u1;                   /* U(1) */
+  double b1_s, msq_s, b3_s, b4_s, a1_s, a2_s; /* singlet */
+  double msq_phi2, m12sq_re, m12sq_im;   /* second doublet (NHIGGS == 2) */
+  double lam2, lam3, lam4, lam5_re, lam5_im, lam6_re, lam6_im, lam7_re, lam7_im;
+} su2gpu_params;
+
+/* Accept/reject counters (su2.h:208-231), int64 each. */
+enum {
+  SU2GPU_C_TOTAL_SU2LINK = 0, SU2GPU_C_ACC_SU2LINK = 1,
+  SU2GPU_C_TOTAL_U1LINK = 2, SU2GPU_C_ACC_U1LINK = 3,
+  SU2GPU_C_TOTAL_DOUBLET = 4,      /* +higgs_id (2 entries) */
+  SU2GPU_C_ACC_DOUBLET = 6,        /* +higgs_id */
+  SU2GPU_C_TOTAL_OR_DOUBLET = 8,   /* +higgs_id */
+  SU2GPU_C_ACC_OR_DOUBLET = 10,    /* +higgs_id */
+  SU2GPU_C_TOTAL_TRIPLET = 12, SU2GPU_C_ACC_TRIPLET = 13,
+  SU2GPU_C_TOTAL_OR_TRIPLET = 14, SU2GPU_C_ACC_OR_TRIPLET = 15,
+  SU2GPU_C_TOTAL_SINGLET = 16, SU2GPU_C_ACC_SINGLET = 17,
+  SU2GPU_C_TOTAL_OR_SINGLET = 18, SU2GPU_C_ACC_OR_SINGLET = 19,
+  SU2GPU_C_TOTAL_MUCA = 20, SU2GPU_C_ACC_MUCA = 21,
+  SU2GPU_C_KP_CAP = 22,            /* heatbath loop-cap fallbacks (heatbath.c:64-68) */
+  SU2GPU_C_POLY_FALLBACK = 23,     /* polysolve3 multi-root fallbacks (overrelax.c:26-32) */
+  SU2GPU_NCOUNTERS = 24
+};
+
+/* Volume sums of measure() (measure.c:110-233), before the division by the
+ * volume that the row writer applies; mag_charge_abs is before the division
+ * by 2*pi*sqrt(beta). */
+enum {
+  SU2GPU_M_ACTION = 0, SU2GPU_M_WILSON = 1, SU2GPU_M_U1WILSON = 2,
+  SU2GPU_M_COV_PHI = 3,   /* +3*higgs_id: covariant, phi2, phi4 */
+  SU2GPU_M_PHI2 = 4, SU2GPU_M_PHI4 = 5,
+  SU2GPU_M_PHI12_RE = 9, SU2GPU_M_PHI12_IM = 10,
+  SU2GPU_M_HOP_SIGMA = 11, SU2GPU_M_SIGMA2 = 12, SU2GPU_M_SIGMA4 = 13, SU2GPU_M_PHI2SIGMA2 = 14,
+  SU2GPU_M_MAGCHARGE = 15, SU2GPU_M_MAGCHARGE_ABS = 16,
+  SU2GPU_M_S_COV = 17, SU2GPU_M_S1 = 18, SU2GPU_M_S2 = 19, SU2GPU_M_S3 = 20, SU2GPU_M_S4 = 21,
+  SU2GPU_M_SPHI2 = 22, SU2GPU_M_S2PHI2 = 23,
+  SU2GPU_NMEAS = 24
+};
+
+/* Multicanonical weight (su2.h:235-274).  Arrays are host memory with
+ * bins+2 entries (the two virtual bins included). */
+typedef struct {
+  int32_t orderparam;
+  int32_t mode;
+  int32_t do_acceptance;
+  int32_t checks_per_sweep;
+  int32_t bins;
+  int32_t muca_count;
+  int32_t update_interval;
+  int32_t last_max;
+  double param_value[2];
+  double min, max, wrk_min, wrk_max, delta;
+  double* pos;
+  double* W;
+  double* slope;
+  double* b;
+  int32_t* hits;
+  int64_t* gsum;   /* SLOW mode only */
+  int64_t* nsum;   /* SLOW mode only */
+  double* hgram;   /* SLOW mode only */
+} su2gpu_weight;
+
+typedef struct su2gpu_ctx su2gpu_ctx;
+
+/* Library / device information. */
+int su2gpu_version(void);
+int su2gpu_device_info(int* sm_count, int* cc_major, int* cc_minor, int64_t* free_bytes);
+
+/* Create a device-resident lattice for one chain.  Fields start cold
+ * (links = 1, scalars 0) until uploaded.  Replaces layout()/alloc_fields()
+ * (layout.c:657-704 serial, alloc.c:103). */
+int su2gpu_create(const su2gpu_params* p, su2gpu_ctx** out);
+int su2gpu_destroy(su2gpu_ctx* ctx);
+/* Bytes of device memory a context with these parameters needs. */
+int64_t su2gpu_footprint_bytes(const su2gpu_params* p);
+
+/* Neighbour / coordinate / parity tables of the layout (layout.c:657-756,
+ * 826-922): next, prev, coords are [V*dim] int64, parity [V] int32.
+ * Computed on the device from the closed form of the reference's EVEN-first
+ * order and copied back. */
+int su2gpu_layout_tables(su2gpu_ctx* ctx, int64_t* next, int64_t* prev, int64_t* coords, int32_t* parity);
+
+/* Field transfer (FP64 AoS host arrays in layout order; NULL for absent
+ * fields).  link: V*dim*4, u1: V*dim, doublet: V*4, triplet: V*3, singlet: V. */
+int su2gpu_upload_fields(su2gpu_ctx* ctx, const double* link, const double* u1, const double* doublet0,
+                         const double* doublet1, const double* triplet, const double* singlet);
+int su2gpu_download_fields(su2gpu_ctx* ctx, double* link, double* u1, double* doublet0,
+                           double* doublet1, double* triplet, double* singlet);
+
+/* Random stream: Philox4x32-10, key = seed, counter = (site, pass<<16|block,
+ * sweep, chain). */
+int su2gpu_set_seed(su2gpu_ctx* ctx, uint64_t seed, uint32_t chain);
+
+/* One full sweep, update.c:270-430 order; `sweep` is the counter word of the
+ * random stream for this call.  Counters accumulate on the device. */
+int su2gpu_update_lattice(su2gpu_ctx* ctx, uint32_t sweep);
+/* n sweeps back to back (sweep, sweep+1, ...), optionally through a captured
+ * CUDA graph of one sweep. */
+int su2gpu_run_sweeps(su2gpu_ctx* ctx, uint32_t first_sweep, int32_t nsweeps, int32_t use_graph);
+int su2gpu_get_counters(su2gpu_ctx* ctx, int64_t* counters /* SU2GPU_NCOUNTERS */);
+int su2gpu_reset_counters(su2gpu_ctx* ctx);
+
+/* measure() volume sums (SU2GPU_NMEAS doubles, FP64 accumulation). */
+int su2gpu_measure(su2gpu_ctx* ctx, double* sums);
+
+/* Multicanonical weight: copy host weight state to the device / back. */
+int su2gpu_muca_set(su2gpu_ctx* ctx, const su2gpu_weight* w);
+int su2gpu_muca_get(su2gpu_ctx* ctx, su2gpu_weight* w);
+/* calc_orderparam(par) (multicanonical.c:709): recompute the parity
+ * contribution on the device, store it, return the total in *value. */
+int su2gpu_calc_orderparam(su2gpu_ctx* ctx, int32_t parity, double* value);
+int su2gpu_muca_init_last_max(su2gpu_ctx* ctx);
+
+/* grad_flow() (gradflow.c:46-173) on a device copy of the fields: Euler
+ * Wilson flow of the SU(2) links (and triplet), measuring every meas_interval
+ * steps.  rows[k*(1+SU2GPU_NMEAS)] = flow time, followed by the sums.
+ * Returns the number of rows in *nrows (at most maxrows). */
+int su2gpu_grad_flow(su2gpu_ctx* ctx, double t_max, double dt, int32_t meas_interval,
+                     double* rows, int32_t maxrows, int32_t* nrows);
+
+/* Drop-in form of update_lattice() with host buffers: upload the host
+ * fields, run one sweep, download them again (the reference mutates its host
+ * arrays in place, su2.h:184-185). */
+int su2gpu_update_lattice_host(su2gpu_ctx* ctx, uint32_t sweep, double* link, double* u1, double* doublet0,
+                               double* doublet1, double* triplet, double* singlet);
+
+/* Last CUDA / kernel error as text. */
+const char* su2gpu_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
