@@ -78,7 +78,7 @@ typedef struct {
   int32_t update_su2triplet;
   int32_t update_singlet;
   int32_t reunitarize_interval;/* FP32 form: renormalise links every n sweeps (0 = never) */
-  int32_t reserved;
+  int32_t reserved[2];         /* keeps the doubles 8-byte aligned without padding */
   double betasu2;
   double msq_phi, lambda_phi;            /* doublet */
   double msq_triplet, a2, b4;            /* triplet */
@@ -207,6 +207,16 @@ int su2gpu_grad_flow(su2gpu_ctx* ctx, double t_max, double dt, int32_t meas_inte
  * arrays in place, su2.h:184-185). */
 int su2gpu_update_lattice_host(su2gpu_ctx* ctx, uint32_t sweep, double* link, double* u1, double* doublet0,
                                double* doublet1, double* triplet, double* singlet);
+
+/* Number of multicanonical weight recursions done on the device (FAST/SLOW
+ * modes); the host rewrites the weight file when it changes, as save_weight()
+ * does after each update (multicanonical.c:426-441). */
+int su2gpu_muca_weight_updates(su2gpu_ctx* ctx, int32_t* n);
+
+/* The uniform the kernels draw as the `draw`-th number of `site` in `pass`
+ * of sweep `sweep` (the Philox stream, evaluated on the host). */
+double su2gpu_stream_uniform(uint64_t seed, uint32_t site, uint32_t pass, uint32_t draw, uint32_t sweep,
+                             uint32_t chain);
 
 /* Last CUDA / kernel error as text. */
 const char* su2gpu_last_error(void);

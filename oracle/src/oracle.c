@@ -1448,3 +1448,18 @@ int orc_grad_flow(orc_ctx* c, double t_max, double dt, int meas_interval, double
   *nrows = nr;
   return nr;
 }
+
+/* ------------------------------------------------------------------ */
+/* random stream probes (tests)                                        */
+/* ------------------------------------------------------------------ */
+void orc_philox_raw(const uint32_t* ctr, const uint32_t* key, uint32_t* out) { orc_philox4x32_10(ctr, key, out); }
+
+double orc_stream_uniform_at(uint64_t seed, uint32_t site, uint32_t pass, uint32_t draw, uint32_t sweep,
+                             uint32_t chain) {
+  orc_stream s;
+  orc_stream_init(&s, seed, sweep, chain);
+  orc_stream_at(&s, site, pass);
+  double u = 0.0;
+  for (uint32_t k = 0; k <= draw; k++) u = orc_stream_uniform(&s);
+  return u;
+}

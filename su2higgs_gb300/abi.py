@@ -87,7 +87,7 @@ class Params(ctypes.Structure):
         ("update_su2triplet", ctypes.c_int32),
         ("update_singlet", ctypes.c_int32),
         ("reunitarize_interval", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 2),
         ("betasu2", ctypes.c_double),
         ("msq_phi", ctypes.c_double),
         ("lambda_phi", ctypes.c_double),

@@ -1,0 +1,297 @@
+// su2_common.cuh -- device building blocks of libsu2gpu: lattice geometry in
+// the reference's EVEN-first site order, the Philox4x32-10 stream, quaternion
+// algebra and the parity-split structure-of-arrays field views.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace su2 {
+
+// ---------------------------------------------------------------------------
+// field content bits (same values as SU2GPU_* in include/su2gpu.h)
+// ---------------------------------------------------------------------------
+enum : int { C_H1 = 0x01, C_H2 = 0x02, C_T = 0x04, C_S = 0x08, C_U1 = 0x10 };
+constexpr int C_GENERIC = -1;  // content read from the runtime mask
+enum : int { ALG_METRO = 1, ALG_HEATBATH = 2, ALG_OR = 3 };
+
+#define SU2_HAS(CC, rt, bit) (((CC) == ::su2::C_GENERIC) ? (((rt) & (bit)) != 0) : (((CC) & (bit)) != 0))
+
+// ---------------------------------------------------------------------------
+// geometry.  Site index of (x,y,z): the reference orders sites
+// lexicographically (x fastest, layout.c:945-972) and then moves EVEN sites
+// first, keeping the order inside each parity (paritymap, layout.c:826-851).
+// With L0 even this is  idx = parity*V/2 + n/2,  n = x + L0*(y + L1*z).
+// ---------------------------------------------------------------------------
+struct Geom {
+  int L[3];
+  int hL0;        // L0 / 2
+  int64_t V;      // sites
+  int64_t half;   // sites per parity
+};
+
+__host__ __device__ inline int64_t site_index(const Geom& g, int x, int y, int z) {
+  int64_t n = (int64_t)x + (int64_t)g.L[0] * ((int64_t)y + (int64_t)g.L[1] * z);
+  return (int64_t)((x + y + z) & 1) * g.half + (n >> 1);
+}
+
+// coordinates of the t-th site of a parity
+__host__ __device__ inline void site_coords(const Geom& g, int parity, int64_t t, int* c) {
+  int64_t r = t / g.hL0;
+  int k = (int)(t - r * g.hL0);
+  int y = (int)(r % g.L[1]);
+  int z = (int)(r / g.L[1]);
+  c[0] = 2 * k + ((parity + y + z) & 1);
+  c[1] = y;
+  c[2] = z;
+}
+
+// index of the site at c + s1*e_d1 + s2*e_d2 (periodic)
+__host__ __device__ inline int64_t shifted(const Geom& g, const int* c, int d1, int s1, int d2 = 0, int s2 = 0) {
+  int x[3] = {c[0], c[1], c[2]};
+  x[d1] += s1;
+  x[d2] += s2;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    if (x[d] >= g.L[d]) x[d] -= g.L[d];
+    if (x[d] < 0) x[d] += g.L[d];
+  }
+  return site_index(g, x[0], x[1], x[2]);
+}
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon et al., SC'11).  key = seed, counter =
+// (site, pass<<16 | block, sweep, chain); draw 2b / 2b+1 are the two 64-bit
+// halves of block b, converted as (x >> 11) * 2^-53 for FP64 (the conversion
+// of the reference's dran(), generic/mersenne.c:147-150) or (x >> 40) * 2^-24
+// for FP32.
+// ---------------------------------------------------------------------------
+constexpr uint32_t GLOBAL_SITE = 0xffffffffu;
+
+__host__ __device__ inline uint32_t mulhi32(uint32_t a, uint32_t b) {
+#ifdef __CUDA_ARCH__
+  return __umulhi(a, b);
+#else
+  return (uint32_t)(((uint64_t)a * (uint64_t)b) >> 32);
+#endif
+}
+
+__host__ __device__ inline void philox4x32_10(uint32_t& c0, uint32_t& c1, uint32_t& c2, uint32_t& c3, uint32_t k0,
+                                              uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    if (r) {
+      k0 += 0x9E3779B9u;
+      k1 += 0xBB67AE85u;
+    }
+    uint32_t hi0 = mulhi32(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+    uint32_t hi1 = mulhi32(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+    uint32_t n0 = hi1 ^ c1 ^ k0;
+    uint32_t n2 = hi0 ^ c3 ^ k1;
+    c0 = n0;
+    c1 = lo1;
+    c2 = n2;
+    c3 = lo0;
+  }
+}
+
+struct RngKey {
+  uint32_t k0, k1;
+  uint32_t chain;
+  const uint32_t* sweep;  // device word holding the current sweep number
+};
+
+template <typename R>
+__host__ __device__ inline R u64_to_uniform(uint64_t x);
+template <>
+__host__ __device__ inline double u64_to_uniform<double>(uint64_t x) {
+  return (double)(x >> 11) * (1.0 / 9007199254740992.0);
+}
+template <>
+__host__ __device__ inline float u64_to_uniform<float>(uint64_t x) {
+  return (float)(uint32_t)(x >> 40) * (1.0f / 16777216.0f);
+}
+
+// per-site stream: uniforms are consumed strictly in order
+template <typename R>
+struct SiteRng {
+  uint32_t k0, k1, site, pass_hi, sweep, chain, draw;
+  uint64_t w1;
+  __device__ SiteRng(const RngKey& k, uint32_t sweep_, uint32_t site_, uint32_t pass)
+      : k0(k.k0), k1(k.k1), site(site_), pass_hi(pass << 16), sweep(sweep_), chain(k.chain), draw(0), w1(0) {}
+  __device__ inline R uni() {
+    uint32_t d = draw++;
+    if (d & 1u) return u64_to_uniform<R>(w1);
+    uint32_t c0 = site, c1 = pass_hi | ((d >> 1) & 0xffffu), c2 = sweep, c3 = chain;
+    philox4x32_10(c0, c1, c2, c3, k0, k1);
+    w1 = ((uint64_t)c2 << 32) | c3;
+    return u64_to_uniform<R>(((uint64_t)c0 << 32) | c1);
+  }
+};
+
+// first uniform of block `block` of a stream position (host and device)
+__host__ __device__ inline double philox_uniform53(uint32_t k0, uint32_t k1, uint32_t site, uint32_t pass,
+                                                   uint32_t block, uint32_t sweep, uint32_t chain, int half) {
+  uint32_t c0 = site, c1 = (pass << 16) | (block & 0xffffu), c2 = sweep, c3 = chain;
+  philox4x32_10(c0, c1, c2, c3, k0, k1);
+  uint64_t x = half ? (((uint64_t)c2 << 32) | c3) : (((uint64_t)c0 << 32) | c1);
+  return u64_to_uniform<double>(x);
+}
+
+// ---------------------------------------------------------------------------
+// math overloads
+// ---------------------------------------------------------------------------
+__device__ inline double msqrt(double x) { return sqrt(x); }
+__device__ inline float msqrt(float x) { return sqrtf(x); }
+__device__ inline double mlog(double x) { return log(x); }
+__device__ inline float mlog(float x) { return logf(x); }
+__device__ inline double mexp(double x) { return exp(x); }
+__device__ inline float mexp(float x) { return expf(x); }
+__device__ inline double mcos(double x) { return cos(x); }
+__device__ inline float mcos(float x) { return cosf(x); }
+__device__ inline double msin(double x) { return sin(x); }
+__device__ inline float msin(float x) { return sinf(x); }
+__device__ inline double mcbrt(double x) { return cbrt(x); }
+__device__ inline float mcbrt(float x) { return cbrtf(x); }
+__device__ inline double matan2(double y, double x) { return atan2(y, x); }
+__device__ inline float matan2(float y, float x) { return atan2f(y, x); }
+__device__ inline double mabs(double x) { return fabs(x); }
+__device__ inline float mabs(float x) { return fabsf(x); }
+
+// ---------------------------------------------------------------------------
+// storage types and quaternions.  q = (a, b, c, d) is a + i(b s1 + c s2 + d s3)
+// (su2u1.c:7-31); qmul is the product of the reference's su2rot().
+// ---------------------------------------------------------------------------
+struct __align__(32) D4 { double x, y, z, w; };
+struct __align__(16) F4 { float x, y, z, w; };
+template <typename R> struct V4T;
+template <> struct V4T<double> { using T = D4; };
+template <> struct V4T<float> { using T = F4; };
+template <typename R> using V4 = typename V4T<R>::T;
+
+template <typename R>
+struct Q {
+  R a, b, c, d;
+};
+
+template <typename R>
+__device__ inline Q<R> ld4(const V4<R>* p, int64_t i) {
+  V4<R> v = p[i];
+  return Q<R>{v.x, v.y, v.z, v.w};
+}
+template <typename R>
+__device__ inline void st4(V4<R>* p, int64_t i, const Q<R>& q) {
+  V4<R> v;
+  v.x = q.a;
+  v.y = q.b;
+  v.z = q.c;
+  v.w = q.d;
+  p[i] = v;
+}
+
+template <typename R>
+__device__ inline Q<R> qmul(const Q<R>& x, const Q<R>& y) {
+  Q<R> r;
+  r.a = x.a * y.a - x.b * y.b - x.c * y.c - x.d * y.d;
+  r.b = x.a * y.b + y.a * x.b - (x.c * y.d - x.d * y.c);
+  r.c = x.a * y.c + y.a * x.c - (x.d * y.b - x.b * y.d);
+  r.d = x.a * y.d + y.a * x.d - (x.b * y.c - x.c * y.b);
+  return r;
+}
+template <typename R>
+__device__ inline Q<R> qdag(const Q<R>& x) {
+  return Q<R>{x.a, -x.b, -x.c, -x.d};
+}
+template <typename R>
+__device__ inline Q<R> qadd(const Q<R>& x, const Q<R>& y) {
+  return Q<R>{x.a + y.a, x.b + y.b, x.c + y.c, x.d + y.d};
+}
+template <typename R>
+__device__ inline Q<R> qscale(const Q<R>& x, R s) {
+  return Q<R>{x.a * s, x.b * s, x.c * s, x.d * s};
+}
+template <typename R>
+__device__ inline R qsq(const Q<R>& x) {
+  return x.a * x.a + x.b * x.b + x.c * x.c + x.d * x.d;
+}
+// scalar part of x*y
+template <typename R>
+__device__ inline R qdot0(const Q<R>& x, const Q<R>& y) {
+  return x.a * y.a - x.b * y.b - x.c * y.c - x.d * y.d;
+}
+// e^{-i alpha sigma_3}
+template <typename R>
+__device__ inline Q<R> u1phase(R alpha) {
+  return Q<R>{mcos(alpha), (R)0, (R)0, -msin(alpha)};
+}
+
+template <typename R>
+struct V3 {
+  R x, y, z;
+};
+// vec(u (0,b) u^dagger): the adjoint rotation of a triplet by a link
+template <typename R>
+__device__ inline V3<R> qrot(const Q<R>& u, const V3<R>& b) {
+  Q<R> vb{(R)0, b.x, b.y, b.z};
+  Q<R> o = qmul(qmul(u, vb), qdag(u));
+  return V3<R>{o.b, o.c, o.d};
+}
+template <typename R>
+__device__ inline R dot3(const V3<R>& a, const V3<R>& b) {
+  return a.x * b.x + a.y * b.y + a.z * b.z;
+}
+
+// ---------------------------------------------------------------------------
+// device field views: parity-split SoA.  link[d][i], u1[d][i], phi[h][i],
+// trip[k][i] (three planes), sing[i]; i is the EVEN-first site index.
+// ---------------------------------------------------------------------------
+template <typename R>
+struct Fields {
+  V4<R>* link[3];
+  R* u1[3];
+  V4<R>* phi[2];
+  R* trip[3];
+  R* sing;
+};
+
+template <typename R>
+__device__ inline V3<R> ld3(const Fields<R>& f, int64_t i) {
+  return V3<R>{f.trip[0][i], f.trip[1][i], f.trip[2][i]};
+}
+template <typename R>
+__device__ inline void st3(const Fields<R>& f, int64_t i, const V3<R>& v) {
+  f.trip[0][i] = v.x;
+  f.trip[1][i] = v.y;
+  f.trip[2][i] = v.z;
+}
+
+// couplings (reference params, su2.h:76-181)
+struct Coup {
+  double beta, msq, lam;
+  double msqT, a2, b4;
+  double betau1, r_u1;
+  double b1s, msqs, b3s, b4s, a1s, a2s;
+  double msq2, m12re, m12im, lam2, lam3, lam4, lam5re, lam5im, lam6re, lam6im, lam7re, lam7im;
+  int content;
+  int alg_link, alg_u1, alg_d, alg_t, alg_s;
+};
+
+// device multicanonical state (weight struct, su2.h:235-274)
+struct MucaDev {
+  int orderparam, mode, do_acceptance, checks_per_sweep, bins, muca_count, update_interval, last_max;
+  double param_value[2];
+  double min, max, wrk_min, wrk_max, delta;
+  double* pos;
+  double* W;
+  double* slope;
+  double* b;
+  int* hits;
+  long long* gsum;
+  long long* nsum;
+  double* hgram;
+  double* wold;  // scratch of the slow recursion
+  int last_accept;
+  int weight_updates;  // number of weight recursions done (host saves the file)
+};
+
+}  // namespace su2

@@ -1,0 +1,80 @@
+// su2_inst.cu -- one instantiation of the sweep kernels.  Compiled several
+// times with -DSU2_R=<double|float> -DSU2_CC=<content mask or -1>
+// -DSU2_OPS=<table name>; the generic units also carry the content-free
+// kernels (-DSU2_WITH_PREC=<table name>) and, for FP64, the non-template ones.
+#include "su2_kernels.cuh"
+#include "su2_ops.h"
+
+namespace su2 {
+
+using R = SU2_R;
+constexpr int CCI = SU2_CC;
+
+static void l_link(const void* f, const PassArgs& a, unsigned nb, cudaStream_t st) {
+  k_link<R, CCI><<<nb, BLOCK, 0, st>>>(*(const Fields<R>*)f, a);
+}
+static void l_u1(const void* f, const PassArgs& a, unsigned nb, cudaStream_t st) {
+  k_u1<R, CCI><<<nb, BLOCK, 0, st>>>(*(const Fields<R>*)f, a);
+}
+static void l_scalar(int field, const void* f, const PassArgs& a, unsigned nb, cudaStream_t st) {
+  const Fields<R>& F = *(const Fields<R>*)f;
+  if (field == 0) k_scalar<R, CCI, 0><<<nb, BLOCK, 0, st>>>(F, a);
+  else if (field == 1) k_scalar<R, CCI, 1><<<nb, BLOCK, 0, st>>>(F, a);
+  else k_scalar<R, CCI, 2><<<nb, BLOCK, 0, st>>>(F, a);
+}
+static void l_measure(const void* f, const Geom& g, const Coup& cp, const double* alpha, double* partials,
+                      unsigned nb, cudaStream_t st) {
+  k_measure<R, CCI><<<nb, BLOCK, 0, st>>>(*(const Fields<R>*)f, g, cp, alpha, partials);
+}
+static void l_flow(const void* fin, const void* fout, const Geom& g, const Coup& cp, double dt,
+                   unsigned long long* fz, unsigned nb, cudaStream_t st) {
+  k_flow<R, CCI><<<nb, BLOCK, 0, st>>>(*(const Fields<R>*)fin, *(const Fields<R>*)fout, g, cp, (R)dt, fz);
+}
+
+const Ops SU2_OPS = {sizeof(R) == 8 ? 64 : 32, CCI, l_link, l_u1, l_scalar, l_measure, l_flow};
+
+#ifdef SU2_WITH_PREC
+static unsigned nblk(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
+static void p_orderparam(const void* f, const Geom& g, int parity, int op, double* partials, unsigned nb,
+                         cudaStream_t st) {
+  k_orderparam<R><<<nb, BLOCK, 0, st>>>(*(const Fields<R>*)f, g, parity, op, partials);
+}
+static void p_restore(int field, const void* f, const MucaDev* m, const void* backup, int h, int64_t lo, int64_t hi,
+                      cudaStream_t st) {
+  if (hi <= lo) return;
+  unsigned nb = nblk(hi - lo, 256);
+  if (field == 0) k_muca_restore<R, 0><<<nb, 256, 0, st>>>(*(const Fields<R>*)f, m, backup, h, lo, hi);
+  else k_muca_restore<R, 1><<<nb, 256, 0, st>>>(*(const Fields<R>*)f, m, backup, h, lo, hi);
+}
+static void p_alpha(const void* f, const Geom& g, const Coup& cp, double* alpha, cudaStream_t st) {
+  k_alpha<R><<<nblk(g.V, BLOCK), BLOCK, 0, st>>>(*(const Fields<R>*)f, g, cp, alpha);
+}
+static void p_import(const void* f, int64_t V, int kind, int h, const double* src, cudaStream_t st) {
+  k_import<R><<<nblk(V * 3, 256), 256, 0, st>>>(*(const Fields<R>*)f, V, kind, h, src);
+}
+static void p_export(const void* f, int64_t V, int kind, int h, double* dst, cudaStream_t st) {
+  k_export<R><<<nblk(V * 3, 256), 256, 0, st>>>(*(const Fields<R>*)f, V, kind, h, dst);
+}
+static void p_reunit(const void* f, int64_t V, const uint32_t* sweep, int interval, cudaStream_t st) {
+  k_reunitarize<R><<<nblk(V * 3, 256), 256, 0, st>>>(*(const Fields<R>*)f, V, sweep, interval);
+}
+static void p_fixup(const void* fin, const void* fout, const Geom& g, const unsigned long long* fz, cudaStream_t st) {
+  k_flow_fixup<R><<<nblk(g.V * 3, 256), 256, 0, st>>>(*(const Fields<R>*)fin, *(const Fields<R>*)fout, g, fz);
+}
+const PrecOps SU2_WITH_PREC = {p_orderparam, p_restore, p_alpha, p_import, p_export, p_reunit, p_fixup};
+#endif
+
+#ifdef SU2_WITH_GLOBAL
+void launch_muca_decide(MucaDev* w, const double* partials, int np, double vol, int parity, const RngKey& rk,
+                        uint32_t pass, uint32_t check, unsigned long long* ctr, cudaStream_t st) {
+  k_muca_decide<<<1, 256, 0, st>>>(w, partials, np, vol, parity, rk, pass, check, ctr);
+}
+void launch_muca_set_param(MucaDev* w, const double* partials, int np, double vol, int parity, cudaStream_t st) {
+  k_muca_set_param<<<1, 256, 0, st>>>(w, partials, np, vol, parity);
+}
+void launch_reduce_partials(const double* partials, int np, double* out, cudaStream_t st) {
+  k_reduce_partials<<<1, 256, 0, st>>>(partials, np, out);
+}
+#endif
+
+}  // namespace su2

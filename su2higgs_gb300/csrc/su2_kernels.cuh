@@ -1,0 +1,1373 @@
+// su2_kernels.cuh -- device kernels of the checkerboard update sweep, the
+// measurement reductions and the gradient flow, templated on the field
+// precision R (double: plain FP64 path, float: precision form with FP64
+// reductions) and on the field content CC (a compile-time content mask, or
+// C_GENERIC to read it at run time).
+//
+// One thread owns one site of the parity being updated.  Sites of one parity
+// never read each other's updated field (checkerboard), so a half-sweep is
+// one launch, exactly as the reference's sequential site loop over that
+// parity (update.c:35-259).
+#pragma once
+
+#include "su2_common.cuh"
+
+namespace su2 {
+
+#define HAS(bit) SU2_HAS(CC, cp.content, bit)
+#define NHIGGS (HAS(C_H2) ? 2 : (HAS(C_H1) ? 1 : 0))
+
+constexpr int BLOCK = 128;
+constexpr int NSUMS = 24;
+
+// ---------------------------------------------------------------------------
+// reductions
+// ---------------------------------------------------------------------------
+__device__ inline void warp_count(unsigned long long* ctr, int v) {
+  // every lane of the warp reaches this call (no early returns in kernels)
+  int s = __reduce_add_sync(0xffffffffu, v);
+  if ((threadIdx.x & 31) == 0 && s) atomicAdd(ctr, (unsigned long long)s);
+}
+
+// sum of v over the block, result valid in thread 0; blockDim.x <= 1024
+__device__ inline double block_sum(double v) {
+  __shared__ double sm[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sm[w] = v;
+  __syncthreads();
+  int nw = (blockDim.x + 31) >> 5;
+  if (w == 0) {
+    v = lane < nw ? sm[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  }
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// SU(2) gauge part
+// ---------------------------------------------------------------------------
+// su2staple_wilson (staples.c:84-115)
+template <typename R>
+__device__ inline Q<R> wilson_staple(const Fields<R>& f, const Geom& g, const int* c, int64_t i, int mu) {
+  Q<R> tot{(R)0, (R)0, (R)0, (R)0};
+  int64_t xp = shifted(g, c, mu, 1);
+#pragma unroll
+  for (int nu = 0; nu < 3; nu++) {
+    if (nu == mu) continue;
+    int64_t xn = shifted(g, c, nu, 1);
+    int64_t xpm = shifted(g, c, mu, 1, nu, -1);
+    int64_t xm = shifted(g, c, nu, -1);
+    Q<R> up = qmul(qmul(ld4<R>(f.link[nu], xp), qdag(ld4<R>(f.link[mu], xn))), qdag(ld4<R>(f.link[nu], i)));
+    tot = qadd(tot, up);
+    Q<R> lo = qmul(qmul(qdag(ld4<R>(f.link[nu], xpm)), qdag(ld4<R>(f.link[mu], xm))), ld4<R>(f.link[nu], xm));
+    tot = qadd(tot, lo);
+  }
+  return tot;
+}
+
+// hopping_triplet_forward (su2u1.c:605-617): -Sigma(x) . R(U_mu(x)) Sigma(x+mu)
+template <typename R>
+__device__ inline R hop_triplet_fwd_u(const Fields<R>& f, const Geom& g, const int* c, int64_t i, int mu,
+                                      const Q<R>& U) {
+  V3<R> r = qrot(U, ld3(f, shifted(g, c, mu, 1)));
+  return -dot3(ld3(f, i), r);
+}
+
+// su2link_staple (staples.c:134-193)
+template <typename R, int CC>
+__device__ inline Q<R> link_staple(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+                                   int mu) {
+  Q<R> V = qscale(wilson_staple(f, g, c, i, mu), (R)(-0.5 * cp.beta));
+  const int nh = NHIGGS;
+  if (nh > 0) {
+    int64_t xp = shifted(g, c, mu, 1);
+    for (int h = 0; h < nh; h++) {
+      Q<R> nphi = ld4<R>(f.phi[h], xp);
+      if (HAS(C_U1)) nphi = qmul(nphi, u1phase(f.u1[mu][i]));
+      Q<R> t = qmul(nphi, qdag(ld4<R>(f.phi[h], i)));
+      V.a -= (R)0.5 * t.a;
+      V.b -= (R)0.5 * t.b;
+      V.c -= (R)0.5 * t.c;
+      V.d -= (R)0.5 * t.d;
+    }
+  }
+  return V;
+}
+
+// su2ptrace (su2u1.c:108-116) at site x (index i, coords c)
+template <typename R>
+__device__ inline R ptrace(const Fields<R>& f, const Geom& g, const int* c, int64_t i, int mu, int nu) {
+  Q<R> s = qmul(qmul(ld4<R>(f.link[mu], i), ld4<R>(f.link[nu], shifted(g, c, mu, 1))),
+                qdag(ld4<R>(f.link[mu], shifted(g, c, nu, 1))));
+  return (R)2 * qdot0(s, qdag(ld4<R>(f.link[nu], i)));
+}
+
+// ---------------------------------------------------------------------------
+// doublet
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ inline R doubletsq(const Q<R>& a) {
+  return (R)0.5 * (a.a * a.a + a.b * a.b + a.c * a.c + a.d * a.d);
+}
+template <typename R>
+__device__ inline R tripletsq(const V3<R>& a) {
+  return (R)0.5 * (a.x * a.x + a.y * a.y + a.z * a.z);
+}
+
+// hopping_trace(_su2u1) (su2u1.c:388-418): Re Tr Phi1^+ U Phi2 e^{-i a s3}
+template <typename R, int CC>
+__device__ inline R hop_trace(const Coup& cp, const Q<R>& p1, const Q<R>& u, const Q<R>& p2, R alpha) {
+  Q<R> t = qmul(u, p2);
+  if (HAS(C_U1)) t = qmul(t, u1phase(alpha));
+  return qdot0(qdag(p1), t);
+}
+template <typename R, int CC>
+__device__ inline R hop_doublet_fwd(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+                                    int mu, int h) {
+  R al = HAS(C_U1) ? f.u1[mu][i] : (R)0;
+  return -hop_trace<R, CC>(cp, ld4<R>(f.phi[h], i), ld4<R>(f.link[mu], i), ld4<R>(f.phi[h], shifted(g, c, mu, 1)), al);
+}
+template <typename R, int CC>
+__device__ inline R hop_doublet_bwd(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+                                    int mu, int h) {
+  int64_t pm = shifted(g, c, mu, -1);
+  R al = HAS(C_U1) ? f.u1[mu][pm] : (R)0;
+  return -hop_trace<R, CC>(cp, ld4<R>(f.phi[h], pm), ld4<R>(f.link[mu], pm), ld4<R>(f.phi[h], i), al);
+}
+template <typename R, int CC>
+__device__ inline R covariant_doublet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+                                      int h) {
+  R tot = 0, mod = doubletsq(ld4<R>(f.phi[h], i));
+#pragma unroll
+  for (int d = 0; d < 3; d++) tot += (R)2 * mod + hop_doublet_fwd<R, CC>(f, g, cp, c, i, d, h);
+  return tot;
+}
+
+// potential_singlet (su2u1.c:708-723)
+template <typename R, int CC>
+__device__ inline R potential_singlet(const Fields<R>& f, const Coup& cp, int64_t i) {
+  R S = f.sing[i];
+  R pot = (R)cp.b1s * S + (R)0.5 * (R)cp.msqs * S * S + (R)(1.0 / 3.0) * (R)cp.b3s * S * S * S +
+          (R)0.25 * (R)cp.b4s * S * S * S * S;
+  if (NHIGGS == 1) {
+    R mod = doubletsq(ld4<R>(f.phi[0], i));
+    pot += (R)0.5 * (R)cp.a1s * S * mod + (R)0.5 * (R)cp.a2s * S * S * mod;
+  }
+  return pot;
+}
+
+// higgspotential (su2u1.c:528-572)
+template <typename R, int CC>
+__device__ inline R higgspotential(const Fields<R>& f, const Coup& cp, int64_t i) {
+  R pot = 0, mod = 0;
+  const int nh = NHIGGS;
+  if (nh > 0) {
+    Q<R> h1 = ld4<R>(f.phi[0], i);
+    mod = doubletsq(h1);
+    pot += (R)cp.msq * mod + (R)cp.lam * mod * mod;
+    if (nh == 2) {
+      Q<R> h2 = ld4<R>(f.phi[1], i);
+      R f11 = mod, f22 = doubletsq(h2);
+      R Re = (R)0.5 * (h1.a * h2.a + h1.b * h2.b + h1.c * h2.c + h1.d * h2.d);
+      R Im = (R)0.5 * (h1.d * h2.a + h1.c * h2.b - h1.b * h2.c - h1.a * h2.d);
+      pot += (R)cp.msq2 * f22 + (R)cp.m12re * Re - (R)cp.m12im * Im + (R)cp.lam2 * f22 * f22 +
+             (R)cp.lam3 * f11 * f22 + (R)cp.lam4 * (Re * Re + Im * Im) + (R)cp.lam5re * (Re * Re - Im * Im) -
+             (R)2 * (R)cp.lam5im * Re * Im + f11 * ((R)cp.lam6re * Re - (R)cp.lam6im * Im) +
+             f22 * ((R)cp.lam7re * Re + (R)cp.lam7im * Im);
+    }
+  }
+  if (HAS(C_T)) {
+    R mt = tripletsq(ld3(f, i));
+    pot += (R)cp.msqT * mt + (R)cp.b4 * mt * mt;
+    if (nh > 0) pot += (R)cp.a2 * mod * mt;
+  }
+  if (HAS(C_S)) pot += potential_singlet<R, CC>(f, cp, i);
+  return pot;
+}
+
+// localact_doublet (su2u1.c:495-510)
+template <typename R, int CC>
+__device__ inline R localact_doublet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+                                     int h) {
+  R tot = covariant_doublet<R, CC>(f, g, cp, c, i, h);
+#pragma unroll
+  for (int d = 0; d < 3; d++) tot += hop_doublet_bwd<R, CC>(f, g, cp, c, i, d, h);
+  tot += higgspotential<R, CC>(f, cp, i);
+  return tot;
+}
+
+// staple_doublet (staples.c:243-302)
+template <typename R, int CC>
+__device__ inline Q<R> staple_doublet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+                                      int h) {
+  Q<R> res{(R)0, (R)0, (R)0, (R)0};
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    int64_t xp = shifted(g, c, d, 1), xm = shifted(g, c, d, -1);
+    Q<R> w = qmul(ld4<R>(f.link[d], i), ld4<R>(f.phi[h], xp));
+    if (HAS(C_U1)) w = qmul(w, u1phase(f.u1[d][i]));
+    res.a -= w.a; res.b -= w.b; res.c -= w.c; res.d -= w.d;
+    w = qmul(qdag(ld4<R>(f.link[d], xm)), ld4<R>(f.phi[h], xm));
+    if (HAS(C_U1)) w = qmul(w, qdag(u1phase(f.u1[d][xm])));
+    res.a -= w.a; res.b -= w.b; res.c -= w.c; res.d -= w.d;
+  }
+  return res;
+}
+
+// ---------------------------------------------------------------------------
+// triplet
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ inline R hop_triplet_fwd(const Fields<R>& f, const Geom& g, const int* c, int64_t i, int mu) {
+  return hop_triplet_fwd_u(f, g, c, i, mu, ld4<R>(f.link[mu], i));
+}
+// hopping_triplet_backward (su2u1.c:623-637)
+template <typename R>
+__device__ inline R hop_triplet_bwd(const Fields<R>& f, const Geom& g, const int* c, int64_t i, int mu) {
+  int64_t pm = shifted(g, c, mu, -1);
+  V3<R> r = qrot(ld4<R>(f.link[mu], pm), ld3(f, i));
+  return -dot3(ld3(f, pm), r);
+}
+template <typename R>
+__device__ inline R covariant_triplet(const Fields<R>& f, const Geom& g, const int* c, int64_t i) {
+  R tot = 0, mod = tripletsq(ld3(f, i));
+#pragma unroll
+  for (int d = 0; d < 3; d++) tot += (R)2 * mod + hop_triplet_fwd(f, g, c, i, d);
+  return tot;
+}
+// localact_triplet (su2u1.c:657-679)
+template <typename R, int CC>
+__device__ inline R localact_triplet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i) {
+  R tot = covariant_triplet(f, g, c, i);
+#pragma unroll
+  for (int d = 0; d < 3; d++) tot += hop_triplet_bwd(f, g, c, i, d);
+  R mod = tripletsq(ld3(f, i));
+  tot += (R)cp.msqT * mod + (R)cp.b4 * mod * mod;
+  if (NHIGGS > 0) tot += (R)cp.a2 * doubletsq(ld4<R>(f.phi[0], i)) * mod;
+  return tot;
+}
+
+// localact_su2link (su2u1.c:166-198)
+template <typename R, int CC>
+__device__ inline R localact_su2link(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+                                     int mu) {
+  R tot = 0;
+#pragma unroll
+  for (int nu = 0; nu < 3; nu++) {
+    if (nu == mu) continue;
+    tot += ((R)1 - (R)0.5 * ptrace(f, g, c, i, mu, nu));
+    int cm[3] = {c[0], c[1], c[2]};
+    cm[nu] = cm[nu] == 0 ? g.L[nu] - 1 : cm[nu] - 1;
+    tot += ((R)1 - (R)0.5 * ptrace(f, g, cm, shifted(g, c, nu, -1), mu, nu));
+  }
+  tot *= (R)cp.beta;
+  for (int h = 0; h < NHIGGS; h++) tot += hop_doublet_fwd<R, CC>(f, g, cp, c, i, mu, h);
+  if (HAS(C_T)) tot += hop_triplet_fwd(f, g, c, i, mu);
+  return tot;
+}
+
+// ---------------------------------------------------------------------------
+// U(1)
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ inline R u1ptrace(const Fields<R>& f, const Geom& g, const int* c, int64_t i, int d1, int d2) {
+  return f.u1[d1][i] + f.u1[d2][shifted(g, c, d1, 1)] - f.u1[d1][shifted(g, c, d2, 1)] - f.u1[d2][i];
+}
+// local_u1wilson (su2u1.c:316-328)
+template <typename R>
+__device__ inline R local_u1wilson(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i) {
+  R res = 0;
+#pragma unroll
+  for (int d1 = 0; d1 < 3; d1++)
+#pragma unroll
+    for (int d2 = 0; d2 < d1; d2++) res += ((R)1 - mcos((R)cp.r_u1 * u1ptrace(f, g, c, i, d2, d1)));
+  return (R)cp.betau1 * res;
+}
+// localact_u1link (su2u1.c:336-354)
+template <typename R, int CC>
+__device__ inline R localact_u1link(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+                                    int mu) {
+  R tot = 0;
+#pragma unroll
+  for (int nu = 0; nu < 3; nu++) {
+    if (nu == mu) continue;
+    tot += ((R)1 - mcos((R)cp.r_u1 * u1ptrace(f, g, c, i, mu, nu)));
+    int cm[3] = {c[0], c[1], c[2]};
+    cm[nu] = cm[nu] == 0 ? g.L[nu] - 1 : cm[nu] - 1;
+    tot += ((R)1 - mcos((R)cp.r_u1 * u1ptrace(f, g, cm, shifted(g, c, nu, -1), mu, nu)));
+  }
+  tot *= (R)cp.betau1;
+  for (int h = 0; h < NHIGGS; h++) tot += hop_doublet_fwd<R, CC>(f, g, cp, c, i, mu, h);
+  return tot;
+}
+
+// ---------------------------------------------------------------------------
+// real root of a x^3 + b x^2 + c x + d (polysolve3, overrelax.c:14-34).
+// FP64: Cardano's formula in double (the reference uses long double; the
+// difference is a rounding effect, far below 1e-12 for these cubics).
+// FP32: the same formula followed by two Newton steps on the cubic, which is
+// well conditioned near its root even where Cardano's form is not.
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ inline R polysolve3(R a, R b, R c, R d, int* fallback) {
+  R discr = (R)18 * a * b * c * d - (R)4 * b * b * b * d + b * b * c * c - (R)4 * a * c * c * c - (R)27 * a * a * d * d;
+  R del1 = (R)2 * b * b * b - (R)9 * a * b * c + (R)27 * a * a * d;
+  R x;
+  if (discr < (R)0) {
+    R A = (R)0.5 * (del1 + a * msqrt((R)(-27) * discr));
+    A = mcbrt(A);
+    x = -(b + A + (b * b - (R)3 * a * c) / A) / ((R)3 * a);
+    if (sizeof(R) == 4) {
+#pragma unroll
+      for (int it = 0; it < 2; it++) {
+        R fx = ((a * x + b) * x + c) * x + d;
+        R dfx = ((R)3 * a * x + (R)2 * b) * x + c;
+        x -= fx / dfx;
+      }
+    }
+  } else {
+    x = b / a;
+    *fallback = 1;
+  }
+  return x;
+}
+
+// ---------------------------------------------------------------------------
+// local updates
+// ---------------------------------------------------------------------------
+// heatbath_su2link (heatbath.c:15-124): Kennedy-Pendleton; the uniforms are
+// drawn in the reference's order (4 per trial, 3 per sphere trial, 1 for the
+// triplet accept/reject).
+template <typename R, int CC>
+__device__ inline int heatbath(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i, int mu,
+                               SiteRng<R>& rng, int* kpcap, int* err) {
+  Q<R> old{};
+  R oldact = 0;
+  if (HAS(C_T)) {
+    old = ld4<R>(f.link[mu], i);
+    oldact = hop_triplet_fwd_u(f, g, c, i, mu, old);
+  }
+  Q<R> V = link_staple<R, CC>(f, g, cp, c, i, mu);
+  R a = msqrt(qsq(V));
+  V = qscale(V, (R)-1 / a);
+  a *= (R)2;
+  R a0, r1, r2, r3, d;
+  int loop = 1;
+  const R twopi = (R)(2 * 3.14159265358979323846);
+  do {
+    r1 = -mlog((R)1 - rng.uni()) / a;
+    r2 = -mlog((R)1 - rng.uni()) / a;
+    r3 = mcos(twopi * rng.uni());
+    r3 *= r3;
+    d = r1 * r3 + r2;
+    r3 = (R)1 - rng.uni();
+    loop++;
+  } while (r3 * r3 > (R)1 - (R)0.5 * d && loop <= 200);
+  R rad;
+  if (loop > 200) {
+    a0 = (R)1e-9;
+    *kpcap = 1;
+    rad = (R)1 - a0 * a0;
+  } else {
+    a0 = (R)1 - d;
+    // FP32: 1 - a0^2 = d (2 - d) without the cancellation near a0 = 1
+    rad = sizeof(R) == 8 ? (R)1 - a0 * a0 : d * ((R)2 - d);
+  }
+  if (rad < (R)0) return 0;
+  rad = msqrt(rad);
+  d = 2;
+  int it = 0;
+  while (d > (R)1 || d == (R)0) {
+    r1 = (R)2 * rng.uni() - (R)1;
+    r2 = (R)2 * rng.uni() - (R)1;
+    r3 = (R)2 * rng.uni() - (R)1;
+    d = r1 * r1 + r2 * r2 + r3 * r3;
+    if (++it > 4096) {  // probability (1 - pi/6)^4096: never; guards a NaN state
+      *err = 1;
+      return 0;
+    }
+  }
+  d = msqrt(d);
+  Q<R> nl{a0, r1 * (rad / d), r2 * (rad / d), r3 * (rad / d)};
+  Q<R> U = qmul(nl, qdag(V));
+  st4<R>(f.link[mu], i, U);
+  if (HAS(C_T)) {
+    R diff = oldact - hop_triplet_fwd_u(f, g, c, i, mu, U);
+    if (rng.uni() < mexp(diff)) return 1;
+    st4<R>(f.link[mu], i, old);
+    return 0;
+  }
+  return 1;
+}
+
+// Metropolis decision (metropolis.c:15-167)
+template <typename R>
+__device__ inline int metro_accept(R diff, SiteRng<R>& rng) {
+  if (diff < (R)0) return 1;
+  if (diff > (R)0 && mexp(-diff) > rng.uni()) return 1;
+  return 0;
+}
+
+// metro_su2link (metropolis.c:15-41) with random_su2link (init.c:43-58)
+template <typename R, int CC>
+__device__ inline int metro_link(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i, int mu,
+                                 SiteRng<R>& rng) {
+  Q<R> old = ld4<R>(f.link[mu], i);
+  R a0 = localact_su2link<R, CC>(f, g, cp, c, i, mu);
+  Q<R> u;
+  u.a = (R)10 * (rng.uni() - (R)0.5);
+  u.b = (R)1 * (rng.uni() - (R)0.5);
+  u.c = (R)1 * (rng.uni() - (R)0.5);
+  u.d = (R)1 * (rng.uni() - (R)0.5);
+  R n = msqrt(u.a * u.a + u.b * u.b + u.c * u.c + u.d * u.d);
+  u = Q<R>{u.a / n, u.b / n, u.c / n, u.d / n};
+  st4<R>(f.link[mu], i, qmul(old, u));
+  R a1 = localact_su2link<R, CC>(f, g, cp, c, i, mu);
+  if (metro_accept(a1 - a0, rng)) return 1;
+  st4<R>(f.link[mu], i, old);
+  return 0;
+}
+
+// metro_u1link (metropolis.c:48-70)
+template <typename R, int CC>
+__device__ inline int metro_u1(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i, int mu,
+                               SiteRng<R>& rng) {
+  R old = f.u1[mu][i];
+  R a0 = localact_u1link<R, CC>(f, g, cp, c, i, mu);
+  f.u1[mu][i] = old + (R)0.95 * (rng.uni() - (R)0.5);
+  R a1 = localact_u1link<R, CC>(f, g, cp, c, i, mu);
+  if (metro_accept(a1 - a0, rng)) return 1;
+  f.u1[mu][i] = old;
+  return 0;
+}
+
+// metro_doublet (metropolis.c:77-106)
+template <typename R, int CC>
+__device__ inline int metro_doublet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+                                    int h, SiteRng<R>& rng) {
+  Q<R> old = ld4<R>(f.phi[h], i);
+  R a0 = localact_doublet<R, CC>(f, g, cp, c, i, h);
+  Q<R> nw = old;
+  nw.a += (R)1 * (rng.uni() - (R)0.5);
+  nw.b += (R)1 * (rng.uni() - (R)0.5);
+  nw.c += (R)1 * (rng.uni() - (R)0.5);
+  nw.d += (R)1 * (rng.uni() - (R)0.5);
+  st4<R>(f.phi[h], i, nw);
+  R a1 = localact_doublet<R, CC>(f, g, cp, c, i, h);
+  if (metro_accept(a1 - a0, rng)) return 1;
+  st4<R>(f.phi[h], i, old);
+  return 0;
+}
+
+// overrelax_doublet (overrelax.c:54-128)
+template <typename R, int CC>
+__device__ inline int overrelax_doublet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+                                        SiteRng<R>& rng, int* fallback) {
+  Q<R> s = staple_doublet<R, CC>(f, g, cp, c, i, 0);
+  Q<R> p = ld4<R>(f.phi[0], i);
+  R F = msqrt(s.a * s.a + s.b * s.b + s.c * s.c + s.d * s.d);
+  R X = (p.a * s.a + p.b * s.b + p.c * s.c + p.d * s.d) / F;
+  R y0 = p.a - X * s.a / F, y1 = p.b - X * s.b / F, y2 = p.c - X * s.c / F, y3 = p.d - X * s.d / F;
+  R Ysq = y0 * y0 + y1 * y1 + y2 * y2 + y3 * y3;
+  R B = (R)0.5 * (R)cp.msq + (R)3;
+  if (HAS(C_T)) B += (R)0.5 * (R)cp.a2 * tripletsq(ld3(f, i));
+  if (HAS(C_S)) {
+    R S = f.sing[i];
+    B += (R)0.25 * (R)cp.a1s * S + (R)0.25 * (R)cp.a2s * S * S;
+  }
+  R C = (R)0.25 * (R)cp.lam;
+  R cc = B + (R)2 * Ysq * C;
+  R newX = polysolve3<R>(C, C * X, cc + C * X * X, F + cc * X + C * X * X * X, fallback);
+  R dV = F + (R)2 * B * X + (R)4 * C * (X * X * X + Ysq * X);
+  R dVn = F + (R)2 * B * newX + (R)4 * C * (newX * newX * newX + Ysq * newX);
+  if (mabs(dV / dVn) >= rng.uni()) {
+    R k = (newX + X);
+    st4<R>(f.phi[0], i, Q<R>{-p.a + k * s.a / F, -p.b + k * s.b / F, -p.c + k * s.c / F, -p.d + k * s.d / F});
+    return 1;
+  }
+  return 0;
+}
+
+// overrelax_higgs2 (overrelax.c:295-417)
+template <typename R, int CC>
+__device__ inline int overrelax_higgs2(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+                                       int h, SiteRng<R>& rng, int* fallback) {
+  Q<R> s = staple_doublet<R, CC>(f, g, cp, c, i, h);
+  Q<R> fv = ld4<R>(f.phi[h], i);
+  Q<R> H;
+  R l67re, l67im, lore, loim, lam12, msq;
+  int sign;
+  if (h == 0) {
+    H = ld4<R>(f.phi[1], i);
+    sign = -1;
+    lam12 = cp.lam; msq = cp.msq;
+    l67re = cp.lam7re; l67im = cp.lam7im; lore = cp.lam6re; loim = -cp.lam6im;
+  } else {
+    H = ld4<R>(f.phi[0], i);
+    sign = 1;
+    lam12 = cp.lam2; msq = cp.msq2;
+    l67re = cp.lam6re; l67im = -cp.lam6im; lore = cp.lam7re; loim = cp.lam7im;
+  }
+  R Hv[4] = {H.a, H.b, H.c, H.d};
+  R G[4] = {sign * Hv[3], sign * Hv[2], -(R)sign * Hv[1], -(R)sign * Hv[0]};
+  R Hsq = doubletsq(H);
+  R sv[4] = {s.a, s.b, s.c, s.d}, fr[4] = {fv.a, fv.b, fv.c, fv.d};
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    sv[k] += (R)0.5 * ((R)cp.m12re + Hsq * l67re) * Hv[k];
+    sv[k] += (R)0.5 * (-(R)cp.m12im + Hsq * l67im) * G[k];
+    sv[k] = -sv[k];
+  }
+  R F = msqrt(sv[0] * sv[0] + sv[1] * sv[1] + sv[2] * sv[2] + sv[3] * sv[3]);
+  R X = 0;
+#pragma unroll
+  for (int k = 0; k < 4; k++) { sv[k] /= F; X += fr[k] * sv[k]; }
+  R Y[4], Ysq = 0;
+#pragma unroll
+  for (int k = 0; k < 4; k++) { Y[k] = fr[k] - X * sv[k]; Ysq += Y[k] * Y[k]; }
+  R Hf = 0, Gf = 0, HY = 0, GY = 0;
+#pragma unroll
+  for (int k = 0; k < 4; k++) { Hf += Hv[k] * sv[k]; Gf += G[k] * sv[k]; HY += Hv[k] * Y[k]; GY += G[k] * Y[k]; }
+  R b4 = (R)0.25 * lam12;
+  R b3 = (R)0.25 * (Hf * lore + Gf * loim);
+  R b2 = (R)0.5 * msq + (R)3 + (R)0.5 * Ysq * lam12 + (R)0.25 * (HY * lore + GY * loim);
+  R b1 = -F + (R)0.25 * Ysq * (Hf * lore + Gf * loim);
+  b2 += (R)0.5 * Hsq * (R)cp.lam3 + (R)0.25 * (R)cp.lam4 * (Hf * Hf + Gf * Gf) +
+        (R)0.25 * (R)cp.lam5re * (Hf * Hf - Gf * Gf) - (R)0.5 * (R)cp.lam5im * Gf * Hf;
+  b1 += (R)0.5 * Hf * (HY * (R)cp.lam4 + HY * (R)cp.lam5re - GY * (R)cp.lam5im) +
+        (R)0.5 * Gf * (GY * (R)cp.lam4 - GY * (R)cp.lam5re - HY * (R)cp.lam5im);
+  R Xn = polysolve3<R>(b4, b3 + b4 * X, b2 + b3 * X + b4 * X * X, b1 + b2 * X + b3 * X * X + b4 * X * X * X, fallback);
+  R dV = (R)4 * b4 * X * X * X + (R)3 * b3 * X * X + (R)2 * b2 * X + b1;
+  R dVn = (R)4 * b4 * Xn * Xn * Xn + (R)3 * b3 * Xn * Xn + (R)2 * b2 * Xn + b1;
+  if (mabs(dV / dVn) >= rng.uni()) {
+    st4<R>(f.phi[h], i, Q<R>{fr[0] + sv[0] * (Xn - X), fr[1] + sv[1] * (Xn - X), fr[2] + sv[2] * (Xn - X),
+                             fr[3] + sv[3] * (Xn - X)});
+    return 1;
+  }
+  return 0;
+}
+
+// overrelax_triplet (overrelax.c:137-236); no portal term in B (the
+// reference's "#ifdef HIGGS" there is never defined)
+template <typename R, int CC>
+__device__ inline int overrelax_triplet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+                                        SiteRng<R>& rng, int* fallback) {
+  V3<R> s{(R)0, (R)0, (R)0};
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    int64_t xp = shifted(g, c, d, 1), xm = shifted(g, c, d, -1);
+    V3<R> r = qrot(ld4<R>(f.link[d], i), ld3(f, xp));
+    s.x -= r.x; s.y -= r.y; s.z -= r.z;
+    r = qrot(qdag(ld4<R>(f.link[d], xm)), ld3(f, xm));
+    s.x -= r.x; s.y -= r.y; s.z -= r.z;
+  }
+  V3<R> t = ld3(f, i);
+  R F = msqrt(s.x * s.x + s.y * s.y + s.z * s.z);
+  R X = (t.x * s.x + t.y * s.y + t.z * s.z) / F;
+  R y0 = t.x - X * s.x / F, y1 = t.y - X * s.y / F, y2 = t.z - X * s.z / F;
+  R Ysq = y0 * y0 + y1 * y1 + y2 * y2;
+  R B = (R)0.5 * (R)cp.msqT + (R)3;
+  R C = (R)0.25 * (R)cp.b4;
+  R cc = B + (R)2 * Ysq * C;
+  R newX = polysolve3<R>(C, C * X, cc + C * X * X, F + cc * X + C * X * X * X, fallback);
+  R dV = F + (R)2 * B * X + (R)4 * C * (X * X * X + Ysq * X);
+  R dVn = F + (R)2 * B * newX + (R)4 * C * (newX * newX * newX + Ysq * newX);
+  if (mabs(dV / dVn) >= rng.uni()) {
+    R k = newX + X;
+    st3(f, i, V3<R>{-t.x + k * s.x / F, -t.y + k * s.y / F, -t.z + k * s.z / F});
+    return 1;
+  }
+  return 0;
+}
+
+// metro_triplet (metropolis.c:113-143)
+template <typename R, int CC>
+__device__ inline int metro_triplet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+                                    SiteRng<R>& rng) {
+  V3<R> old = ld3(f, i);
+  R a0 = localact_triplet<R, CC>(f, g, cp, c, i);
+  V3<R> nw = old;
+  nw.x += (R)1 * (rng.uni() - (R)0.5);
+  nw.y += (R)1 * (rng.uni() - (R)0.5);
+  nw.z += (R)1 * (rng.uni() - (R)0.5);
+  st3(f, i, nw);
+  R a1 = localact_triplet<R, CC>(f, g, cp, c, i);
+  if (metro_accept(a1 - a0, rng)) return 1;
+  st3(f, i, old);
+  return 0;
+}
+
+// localact_singlet (su2u1.c:688-705)
+template <typename R, int CC>
+__device__ inline R localact_singlet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i) {
+  R S = f.sing[i], res = (R)3 * S * S;
+#pragma unroll
+  for (int d = 0; d < 3; d++) res -= S * (f.sing[shifted(g, c, d, 1)] + f.sing[shifted(g, c, d, -1)]);
+  res += potential_singlet<R, CC>(f, cp, i);
+  return res;
+}
+
+// overrelax_singlet (overrelax.c:243-285)
+template <typename R, int CC>
+__device__ inline int overrelax_singlet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+                                        SiteRng<R>& rng, int* fallback) {
+  R S = f.sing[i];
+  R c1 = (R)cp.b1s;
+#pragma unroll
+  for (int d = 0; d < 3; d++) c1 -= (f.sing[shifted(g, c, d, 1)] + f.sing[shifted(g, c, d, -1)]);
+  R c2 = (R)3 + (R)0.5 * (R)cp.msqs;
+  R c3 = (R)(1.0 / 3.0) * (R)cp.b3s;
+  R c4 = (R)0.25 * (R)cp.b4s;
+  if (NHIGGS == 1) {
+    R phisq = doubletsq(ld4<R>(f.phi[0], i));
+    c1 += (R)0.5 * (R)cp.a1s * phisq;
+    c2 += (R)0.5 * (R)cp.a2s * phisq;
+  }
+  R d0 = c1 + c2 * S + c3 * S * S + c4 * S * S * S;
+  R d1 = c2 + c3 * S + c4 * S * S;
+  R d2 = c3 + c4 * S;
+  R Y = polysolve3<R>(c4, d2, d1, d0, fallback);
+  R dV = c1 + (R)2 * c2 * S + (R)3 * c3 * S * S + (R)4 * c4 * S * S * S;
+  R dVn = c1 + (R)2 * c2 * Y + (R)3 * c3 * Y * Y + (R)4 * c4 * Y * Y * Y;
+  if (mabs(dV / dVn) >= rng.uni()) {
+    f.sing[i] = Y;
+    return 1;
+  }
+  return 0;
+}
+
+// metro_singlet (metropolis.c:148-167)
+template <typename R, int CC>
+__device__ inline int metro_singlet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+                                    SiteRng<R>& rng) {
+  R old = f.sing[i];
+  R a0 = localact_singlet<R, CC>(f, g, cp, c, i);
+  f.sing[i] = old + (R)1 * (rng.uni() - (R)0.5);
+  R a1 = localact_singlet<R, CC>(f, g, cp, c, i);
+  if (metro_accept(a1 - a0, rng)) return 1;
+  f.sing[i] = old;
+  return 0;
+}
+
+// order-parameter contribution of one site (calc_orderparam, multicanonical.c:709-751)
+template <typename R>
+__device__ inline double orderparam_site(const Fields<R>& f, int op, int64_t i) {
+  switch (op) {
+    case 2: return (double)tripletsq(ld3(f, i));
+    case 3: return (double)doubletsq(ld4<R>(f.phi[0], i)) - (double)tripletsq(ld3(f, i));
+    case 1: return (double)doubletsq(ld4<R>(f.phi[0], i));
+    case 4: return (double)doubletsq(ld4<R>(f.phi[1], i));
+  }
+  return 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// half-sweep kernels
+// ---------------------------------------------------------------------------
+struct PassArgs {
+  Geom g;
+  Coup cp;
+  RngKey rk;
+  int parity;
+  int sub;      // direction for links, doublet index for doublets
+  int alg;      // algorithm (links) or forced Metropolis flag (scalars)
+  uint32_t pass;
+  int64_t t_lo, t_hi;       // site range inside the parity
+  void* backup;             // multicanonical backup of the updated field (or null)
+  int op;                   // order parameter to reduce (0: none)
+  double* partials;         // per-block order-parameter sums (or null)
+  unsigned long long* ctr;  // device counters
+  int* err;                 // device error flag
+};
+
+template <typename R, int CC>
+__global__ void __launch_bounds__(BLOCK) k_link(Fields<R> f, PassArgs a) {
+  const Coup& cp = a.cp;
+  int64_t t = a.t_lo + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int acc = 0, cap = 0, err = 0;
+  if (t < a.t_hi) {
+    int c[3];
+    site_coords(a.g, a.parity, t, c);
+    int64_t i = a.parity * a.g.half + t;
+    SiteRng<R> rng(a.rk, *a.rk.sweep, (uint32_t)i, a.pass);
+    if (a.alg == ALG_HEATBATH) acc = heatbath<R, CC>(f, a.g, cp, c, i, a.sub, rng, &cap, &err);
+    else acc = metro_link<R, CC>(f, a.g, cp, c, i, a.sub, rng);
+  }
+  warp_count(a.ctr + 1, acc);
+  warp_count(a.ctr + 22, cap);
+  if (err) atomicOr(a.err, 1);
+}
+
+template <typename R, int CC>
+__global__ void __launch_bounds__(BLOCK) k_u1(Fields<R> f, PassArgs a) {
+  const Coup& cp = a.cp;
+  int64_t t = a.t_lo + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int acc = 0;
+  if (t < a.t_hi) {
+    int c[3];
+    site_coords(a.g, a.parity, t, c);
+    int64_t i = a.parity * a.g.half + t;
+    SiteRng<R> rng(a.rk, *a.rk.sweep, (uint32_t)i, a.pass);
+    acc = metro_u1<R, CC>(f, a.g, cp, c, i, a.sub, rng);
+  }
+  warp_count(a.ctr + 3, acc);
+}
+
+// one parity (or a contiguous block of it) of one doublet / the triplet /
+// the singlet; optional multicanonical backup of the old values and block
+// sums of the order parameter over the new ones
+template <typename R, int CC, int FIELD>
+__global__ void __launch_bounds__(BLOCK) k_scalar(Fields<R> f, PassArgs a) {
+  const Coup& cp = a.cp;
+  int64_t t = a.t_lo + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int acc = 0, fb = 0;
+  double opv = 0.0;
+  bool orr = false;
+  if (t < a.t_hi) {
+    int c[3];
+    site_coords(a.g, a.parity, t, c);
+    int64_t i = a.parity * a.g.half + t;
+    SiteRng<R> rng(a.rk, *a.rk.sweep, (uint32_t)i, a.pass);
+    if (FIELD == 0) {
+      const int h = a.sub;
+      if (a.backup) ((V4<R>*)a.backup)[i] = f.phi[h][i];
+      orr = cp.alg_d == ALG_OR && !a.alg;
+      if (orr) acc = NHIGGS == 2 ? overrelax_higgs2<R, CC>(f, a.g, cp, c, i, h, rng, &fb)
+                                 : overrelax_doublet<R, CC>(f, a.g, cp, c, i, rng, &fb);
+      else acc = metro_doublet<R, CC>(f, a.g, cp, c, i, h, rng);
+    } else if (FIELD == 1) {
+      if (a.backup) {
+        R* b = (R*)a.backup;
+        b[3 * i] = f.trip[0][i]; b[3 * i + 1] = f.trip[1][i]; b[3 * i + 2] = f.trip[2][i];
+      }
+      orr = cp.alg_t == ALG_OR && !a.alg;
+      if (orr) acc = overrelax_triplet<R, CC>(f, a.g, cp, c, i, rng, &fb);
+      else acc = metro_triplet<R, CC>(f, a.g, cp, c, i, rng);
+    } else {
+      orr = cp.alg_s == ALG_OR && !a.alg;
+      if (orr) acc = overrelax_singlet<R, CC>(f, a.g, cp, c, i, rng, &fb);
+      else acc = metro_singlet<R, CC>(f, a.g, cp, c, i, rng);
+    }
+    if (a.partials) opv = orderparam_site<R>(f, a.op, i);
+  }
+  // counters: doublet OR/Metropolis (+h), triplet, singlet
+  int base_or = FIELD == 0 ? 10 + a.sub : (FIELD == 1 ? 15 : 19);
+  int base_mt = FIELD == 0 ? 6 + a.sub : (FIELD == 1 ? 13 : 17);
+  bool any_or = (FIELD == 0 ? cp.alg_d : (FIELD == 1 ? cp.alg_t : cp.alg_s)) == ALG_OR && !a.alg;
+  warp_count(a.ctr + (any_or ? base_or : base_mt), acc);
+  warp_count(a.ctr + 23, fb);
+  if (a.partials) {
+    double s = block_sum(opv);
+    if (threadIdx.x == 0) a.partials[blockIdx.x] = s;
+  }
+}
+
+// order parameter of a whole parity (calc_orderparam)
+template <typename R>
+__global__ void __launch_bounds__(BLOCK) k_orderparam(Fields<R> f, Geom g, int parity, int op, double* partials) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double v = 0.0;
+  if (t < g.half) v = orderparam_site<R>(f, op, parity * g.half + t);
+  double s = block_sum(v);
+  if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+// restore a block of the parity from the backup if the last check rejected
+template <typename R, int FIELD>
+__global__ void k_muca_restore(Fields<R> f, const MucaDev* m, const void* backup, int h, int64_t lo, int64_t hi) {
+  if (m->last_accept) return;
+  int64_t i = lo + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= hi) return;
+  if (FIELD == 0) {
+    f.phi[h][i] = ((const V4<R>*)backup)[i];
+  } else {
+    const R* b = (const R*)backup;
+    f.trip[0][i] = b[3 * i]; f.trip[1][i] = b[3 * i + 1]; f.trip[2][i] = b[3 * i + 2];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// multicanonical decision (multicanonical.c:337-704, update.c:13-30), one block
+// ---------------------------------------------------------------------------
+__device__ inline void muca_linearize(MucaDev* w) {
+  w->slope[0] = 0;
+  w->slope[w->bins + 1] = 0;
+  w->b[0] = w->W[0];
+  w->b[w->bins + 1] = w->W[w->bins + 1];
+  for (int i = 1; i < w->bins + 1; i++) {
+    w->slope[i] = (w->W[i + 1] - w->W[i]) / (w->pos[i + 1] - w->pos[i]);
+    w->b[i] = w->W[i] - w->slope[i] * w->pos[i];
+  }
+}
+__device__ inline int muca_whichbin(const MucaDev* w, double val) {
+  if (val < w->min) return 0;
+  if (val >= w->max) return w->bins + 1;
+  int bmin = 1, bmax = w->bins;
+  while (bmin <= bmax) {
+    int bin = bmin + (bmax - bmin) / 2;
+    double cur = w->pos[bin], nxt = w->pos[bin + 1];
+    if ((val < nxt && val > cur) || (fabs(val - cur) < 1e-12)) return bin;
+    if (val > cur) bmin = bin + 1;
+    else bmax = bin - 1;
+  }
+  return w->bins;
+}
+__device__ inline double muca_get_weight(const MucaDev* w, double val) {
+  if (val >= w->max) return w->b[w->bins + 1];
+  if (val < w->min) return w->b[0];
+  int bin = muca_whichbin(w, val);
+  if (bin >= w->bins + 1) return w->b[w->bins + 1];
+  return w->b[bin] + w->slope[bin] * val;
+}
+__device__ inline void muca_accumulate(MucaDev* w, double val) {
+  int bin = muca_whichbin(w, val);
+  if (bin == 0) {
+    double dmin = w->pos[2] - w->pos[1];
+    if (val < w->pos[1] - 0.5 * dmin) return;
+    bin += 1;
+  } else if (bin < w->bins + 1) {
+    if (val - w->pos[bin] > w->pos[bin + 1] - val) bin = bin + 1;
+  } else {
+    double dmax = w->pos[w->bins + 1] - w->pos[w->bins];
+    if (val > w->pos[w->bins + 1] + 0.5 * dmax) return;
+  }
+  if (w->mode == 1) {
+    w->hits[bin] += 5;
+    if (bin > 1) w->hits[bin - 1] += 3;
+    if (bin > 2) w->hits[bin - 2] += 1;
+    if (bin < w->bins) w->hits[bin + 1] += 3;
+    if (bin < w->bins - 1) w->hits[bin + 2] += 1;
+  } else if (w->mode == 2) {
+    w->hits[bin]++;
+    w->hgram[bin] += exp(muca_get_weight(w, val));
+  }
+}
+__device__ inline void muca_update_fast(MucaDev* w) {
+  int first = -1;
+  double delta = 0.0;
+  for (int i = 0; i < w->bins + 2; i++) {
+    if (w->pos[i] >= w->wrk_min && w->wrk_max >= w->pos[i]) {
+      if (first < 0) first = i;
+      delta = (w->hits[i] - w->hits[first]) * w->delta / ((double)w->bins);
+      w->W[i] += delta;
+    } else if (w->wrk_max < w->pos[i]) {
+      w->W[i] += delta;
+    }
+  }
+  w->W[0] = w->W[1];
+  w->W[w->bins + 1] = w->W[w->bins];
+  muca_linearize(w);
+  int tunnel = 0;
+  if (w->last_max && w->hits[1] > 0) { w->last_max = 0; tunnel = 1; }
+  else if (!w->last_max && w->hits[w->bins] > 0) { w->last_max = 1; tunnel = 1; }
+  if (tunnel) w->delta /= 1.5;
+  for (int i = 0; i < w->bins + 2; i++) w->hits[i] = 0;
+}
+__device__ inline void muca_update_slow(MucaDev* w) {
+  int n = w->bins + 2;
+  double* wold = w->wold;
+  for (int i = 0; i < n; i++) wold[i] = w->W[i];
+  double dmin = w->pos[2] - w->pos[1];
+  w->hgram[1] /= dmin;
+  for (int i = 2; i < w->bins + 1; i++) w->hgram[i] /= (w->pos[i + 1] - w->pos[i - 1]);
+  int first = -1, last = -1, hits_min = 8;
+  for (int i = 1; i < w->bins + 1; i++) {
+    if (w->pos[i] >= w->wrk_min && w->wrk_max >= w->pos[i]) {
+      if (first < 0) { first = i; continue; }
+      w->nsum[i] += w->hits[i];
+      int gg = 0;
+      if (w->hits[i] >= hits_min && w->hits[i - 1] >= hits_min) {
+        gg = w->hits[i] + w->hits[i - 1];
+      } else {
+        w->W[i] = wold[i] - wold[i - 1] + w->W[i - 1];
+        continue;
+      }
+      long long gsum_new = w->gsum[i] + gg;
+      double ln = w->hgram[i - 1] / w->hgram[i];
+      ln = -1.0 * gg * log(ln);
+      w->W[i] = w->W[i - 1] + ((wold[i] - wold[i - 1]) * w->gsum[i] + ln) / ((double)gsum_new);
+      w->gsum[i] = gsum_new;
+    } else if (w->wrk_max < w->pos[i]) {
+      if (last < 0) last = i - 1;
+      w->W[i] += w->W[last] - wold[last];
+    }
+  }
+  for (int i = 0; i < n; i++) { w->hits[i] = 0; w->hgram[i] = 0.0; }
+  w->W[0] = w->W[1];
+  w->W[w->bins + 1] = w->W[w->bins];
+  for (int i = 0; i < n; i++) wold[i] = w->W[i];
+  double corr = 0.0;
+  if (first < 1) {  // no bin inside the work range: nothing to overcorrect
+    muca_linearize(w);
+    return;
+  }
+  if (first == 1) dmin = w->pos[first + 1] - w->pos[first];
+  else dmin = w->pos[first + 1] - w->pos[first - 1];
+  for (int i = first + 1; i < w->bins + 1; i++) {
+    if (i <= last) {
+      double diff1 = w->pos[i + 1] - w->pos[i - 1];
+      corr = 2.0 * log((dmin / diff1) * w->nsum[i] / w->nsum[first]);
+    }
+    w->W[i] += corr;
+  }
+  w->W[0] = w->W[1];
+  w->W[w->bins + 1] = w->W[w->bins];
+  muca_linearize(w);
+  for (int i = 0; i < n; i++) w->W[i] = wold[i];
+}
+
+#ifdef SU2_WITH_GLOBAL
+// muca_check (update.c:13-30): total of the parity sums, weight difference,
+// global draw (site 0xffffffff, block = check), accept/reject, hits and
+// weight recursion.  Partial sums are added in a fixed order.
+__global__ void k_muca_decide(MucaDev* w, const double* partials, int np, double vol, int parity, RngKey rk,
+                              uint32_t pass, uint32_t check, unsigned long long* ctr) {
+  __shared__ double red[256];
+  double v = 0.0;
+  for (int k = threadIdx.x; k < np; k += blockDim.x) v += partials[k];
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int s = blockDim.x >> 1; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x != 0) return;
+  double tot = red[0] / vol;
+  double old = w->param_value[0] + w->param_value[1];
+  w->param_value[parity] = tot;
+  double nw = tot + w->param_value[1 - parity];
+  double Wn = muca_get_weight(w, nw), Wo = muca_get_weight(w, old);
+  double u = philox_uniform53(rk.k0, rk.k1, GLOBAL_SITE, pass, check, *rk.sweep, rk.chain, 0);
+  int accept = exp(-(Wn - Wo)) > u ? 1 : 0;
+  if (w->mode != 0) {
+    double val = accept ? nw : old;
+    muca_accumulate(w, val);
+    w->muca_count++;
+    if (w->muca_count % w->update_interval == 0) {
+      if (w->mode == 1) muca_update_fast(w);
+      else if (w->mode == 2) muca_update_slow(w);
+      w->muca_count = 0;
+      w->weight_updates++;
+    }
+  }
+  if (!accept) w->param_value[parity] = old - w->param_value[1 - parity];
+  w->last_accept = accept;
+  ctr[20] += 1;
+  ctr[21] += accept;
+}
+
+// calc_orderparam for the host API: store the parity sum
+__global__ void k_muca_set_param(MucaDev* w, const double* partials, int np, double vol, int parity) {
+  __shared__ double red[256];
+  double v = 0.0;
+  for (int k = threadIdx.x; k < np; k += blockDim.x) v += partials[k];
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int s = blockDim.x >> 1; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) w->param_value[parity] = red[0] / vol;
+}
+
+#endif  // SU2_WITH_GLOBAL
+
+// ---------------------------------------------------------------------------
+// measurements (measure.c:71-243)
+// ---------------------------------------------------------------------------
+// complex 2x2 matrices for the projected U(1) links (magfield.c:32-184)
+template <typename R>
+struct CM {
+  R re[4], im[4];
+};
+template <typename R>
+__device__ inline CM<R> cm_mul(const CM<R>& a, const CM<R>& b) {
+  CM<R> t;
+#pragma unroll
+  for (int i = 0; i < 2; i++)
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      R sr = 0, si = 0;
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        R ar = a.re[2 * i + k], ai = a.im[2 * i + k], br = b.re[2 * k + j], bi = b.im[2 * k + j];
+        sr += ar * br - ai * bi;
+        si += ar * bi + ai * br;
+      }
+      t.re[2 * i + j] = sr;
+      t.im[2 * i + j] = si;
+    }
+  return t;
+}
+template <typename R>
+__device__ inline CM<R> cm_dag(const CM<R>& a) {
+  CM<R> t;
+#pragma unroll
+  for (int i = 0; i < 2; i++)
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      t.re[2 * i + j] = a.re[2 * j + i];
+      t.im[2 * i + j] = -a.im[2 * j + i];
+    }
+  return t;
+}
+// projector() / project_u1(): Pi(x) U_mu(x) Pi(x+mu), Pi = (1 + n.sigma)/2
+template <typename R>
+__device__ inline CM<R> proj_mat(const V3<R>& a) {
+  R m = msqrt(a.x * a.x + a.y * a.y + a.z * a.z);
+  R n1 = a.x / m, n2 = a.y / m, n3 = a.z / m;
+  CM<R> P;
+  P.re[0] = (R)0.5 * ((R)1 + n3); P.im[0] = 0;
+  P.re[1] = (R)0.5 * n1;          P.im[1] = (R)-0.5 * n2;
+  P.re[2] = (R)0.5 * n1;          P.im[2] = (R)0.5 * n2;
+  P.re[3] = (R)0.5 * ((R)1 - n3); P.im[3] = 0;
+  return P;
+}
+template <typename R>
+__device__ inline CM<R> project_u1(const Fields<R>& f, const Geom& g, const int* c, int64_t i, int d) {
+  Q<R> u = ld4<R>(f.link[d], i);
+  CM<R> U;
+  U.re[0] = u.a; U.im[0] = u.d;
+  U.re[1] = u.c; U.im[1] = u.b;
+  U.re[2] = -u.c; U.im[2] = u.b;
+  U.re[3] = u.a; U.im[3] = -u.d;
+  return cm_mul(cm_mul(proj_mat(ld3(f, i)), U), proj_mat(ld3(f, shifted(g, c, d, 1))));
+}
+// alpha_proj (magfield.c:189-216)
+template <typename R>
+__device__ inline R alpha_proj(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i, int d1,
+                               int d2) {
+  int c1[3] = {c[0], c[1], c[2]}, c2[3] = {c[0], c[1], c[2]};
+  c1[d1] = c1[d1] + 1 == g.L[d1] ? 0 : c1[d1] + 1;
+  c2[d2] = c2[d2] + 1 == g.L[d2] ? 0 : c2[d2] + 1;
+  CM<R> u1 = project_u1(f, g, c, i, d1);
+  CM<R> u2 = project_u1(f, g, c1, shifted(g, c, d1, 1), d2);
+  CM<R> u3 = project_u1(f, g, c2, shifted(g, c, d2, 1), d1);
+  CM<R> u4 = project_u1(f, g, c, i, d2);
+  CM<R> t = cm_mul(cm_mul(cm_mul(u1, u2), cm_dag(u3)), cm_dag(u4));
+  R a = matan2(t.im[0] + t.im[3], t.re[0] + t.re[3]);
+  return a * msqrt((R)cp.beta);
+}
+
+// alpha(x; 0,1), alpha(x; 0,2), alpha(x; 1,2) for every site
+template <typename R>
+__global__ void __launch_bounds__(BLOCK) k_alpha(Fields<R> f, Geom g, Coup cp, double* alpha) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.V) return;
+  int parity = t >= g.half;
+  int64_t tp = t - parity * g.half;
+  int c[3];
+  site_coords(g, parity, tp, c);
+  alpha[t] = (double)alpha_proj(f, g, cp, c, t, 0, 1);
+  alpha[g.V + t] = (double)alpha_proj(f, g, cp, c, t, 0, 2);
+  alpha[2 * g.V + t] = (double)alpha_proj(f, g, cp, c, t, 1, 2);
+}
+
+// per-site terms of measure() summed over the block into partials[block][NSUMS]
+template <typename R, int CC>
+__global__ void __launch_bounds__(BLOCK) k_measure(Fields<R> f, Geom g, Coup cp, const double* alpha,
+                                                   double* partials) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double m[NSUMS];
+#pragma unroll
+  for (int k = 0; k < NSUMS; k++) m[k] = 0.0;
+  if (t < g.V) {
+    int parity = t >= g.half;
+    int64_t i = t;
+    int c[3];
+    site_coords(g, parity, t - parity * g.half, c);
+    // local_su2wilson (su2u1.c:143-157)
+    R wl = 0;
+    wl += ((R)1 - (R)0.5 * ptrace(f, g, c, i, 0, 1));
+    wl += ((R)1 - (R)0.5 * ptrace(f, g, c, i, 0, 2));
+    wl += ((R)1 - (R)0.5 * ptrace(f, g, c, i, 1, 2));
+    wl = (R)cp.beta * wl;
+    double act = (double)wl;
+    m[1] = (double)wl;
+    if (HAS(C_U1)) {
+      R u1w = local_u1wilson(f, g, cp, c, i);
+      act += (double)u1w;
+      m[2] = (double)u1w;
+    }
+    act += (double)higgspotential<R, CC>(f, cp, i);
+    const int nh = NHIGGS;
+    for (int h = 0; h < nh; h++) {
+      R mod = doubletsq(ld4<R>(f.phi[h], i));
+      R cov = covariant_doublet<R, CC>(f, g, cp, c, i, h);
+      act += (double)cov;
+      m[3 + 3 * h] = (double)cov;
+      m[4 + 3 * h] = (double)mod;
+      m[5 + 3 * h] = (double)(mod * mod);
+    }
+    if (HAS(C_T)) {
+      R covt = covariant_triplet(f, g, c, i);
+      act += (double)covt;
+      V3<R> tr = ld3(f, i);
+      R tm = tripletsq(tr);
+      if (nh > 0) m[14] = (double)(doubletsq(ld4<R>(f.phi[0], i)) * tm);
+      m[12] = (double)tm;
+      m[13] = (double)(tm * tm);
+      R hs = 0;
+#pragma unroll
+      for (int d = 0; d < 3; d++) hs += hop_triplet_fwd(f, g, c, i, d);
+      m[11] = (double)hs;
+      // magcharge_cube (magfield.c:262-280) from the alpha planes
+      const int64_t V = g.V;
+      double q = 0.0;
+      {
+        int64_t n0 = shifted(g, c, 0, 1), n1 = shifted(g, c, 1, 1), n2 = shifted(g, c, 2, 1);
+        double B1 = alpha[2 * V + i], B2 = alpha[2 * V + n0];
+        q += B2 - B1;
+        B1 = -alpha[V + i];
+        B2 = -alpha[V + n1];
+        q += B2 - B1;
+        B1 = alpha[i];
+        B2 = alpha[n2];
+        q += B2 - B1;
+      }
+      m[15] = q;
+      m[16] = fabs(q);
+    }
+    if (nh == 2) {
+      Q<R> h1 = ld4<R>(f.phi[0], i), h2 = ld4<R>(f.phi[1], i);
+      m[9] = (double)((R)0.5 * (h1.a * h2.a + h1.b * h2.b + h1.c * h2.c + h1.d * h2.d));
+      m[10] = (double)((R)0.5 * (h1.d * h2.a + h1.c * h2.b - h1.b * h2.c - h1.a * h2.d));
+    }
+    if (HAS(C_S)) {
+      R S = f.sing[i];
+      R kin = (R)3 * S * S;
+      R scov = 0;
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        R Sn = f.sing[shifted(g, c, d, 1)];
+        kin -= S * Sn;
+        scov += S * S - S * Sn;
+      }
+      act += (double)kin;
+      m[17] = (double)scov;
+      m[18] = (double)S;
+      m[19] = (double)(S * S);
+      m[20] = (double)(S * S * S);
+      m[21] = (double)(S * S * S * S);
+      if (nh == 1) {
+        R mod = doubletsq(ld4<R>(f.phi[0], i));
+        m[22] = (double)(mod * S);
+        m[23] = (double)(mod * S * S);
+      }
+    }
+    m[0] = act;
+  }
+  __shared__ double sm[BLOCK / 32][NSUMS];
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NSUMS; k++) {
+    double v = m[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sm[w][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < NSUMS) {
+    double v = 0.0;
+#pragma unroll
+    for (int ww = 0; ww < BLOCK / 32; ww++) v += sm[ww][threadIdx.x];
+    partials[(int64_t)blockIdx.x * NSUMS + threadIdx.x] = v;
+  }
+}
+
+#ifdef SU2_WITH_GLOBAL
+// fixed-order sum of partials[np][NSUMS] -> out[NSUMS]; one block of 256
+__global__ void k_reduce_partials(const double* partials, int np, double* out) {
+  __shared__ double red[256];
+  for (int k = 0; k < NSUMS; k++) {
+    double v = 0.0;
+    for (int b = threadIdx.x; b < np; b += blockDim.x) v += partials[(int64_t)b * NSUMS + k];
+    red[threadIdx.x] = v;
+    __syncthreads();
+    for (int s = blockDim.x >> 1; s > 0; s >>= 1) {
+      if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[k] = red[0];
+    __syncthreads();
+  }
+}
+
+#endif  // SU2_WITH_GLOBAL
+
+// ---------------------------------------------------------------------------
+// gradient flow (gradflow.c:190-414): forces from `in`, Euler step into `out`
+// ---------------------------------------------------------------------------
+template <typename R, int CC>
+__global__ void __launch_bounds__(BLOCK) k_flow(Fields<R> in, Fields<R> out, Geom g, Coup cp, R dt,
+                                                unsigned long long* first_zero) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.V) return;
+  int parity = t >= g.half;
+  int64_t i = t;
+  int c[3];
+  site_coords(g, parity, t - parity * g.half, c);
+#pragma unroll
+  for (int mu = 0; mu < 3; mu++) {
+    // grad_force_link (gradflow.c:190-258)
+    Q<R> s = qscale(wilson_staple(in, g, c, i, mu), (R)(-cp.beta / 8.0));
+    Q<R> U = ld4<R>(in.link[mu], i);
+    if (HAS(C_T)) {
+      V3<R> a1 = ld3(in, i), a2 = ld3(in, shifted(g, c, mu, 1));
+      Q<R> r = qmul(qmul(Q<R>{(R)0, a2.x, a2.y, a2.z}, qdag(U)), Q<R>{(R)0, a1.x, a1.y, a1.z});
+      s.a -= (-r.a) / (R)4;
+      s.b -= (-r.b) / (R)4;
+      s.c -= (-r.c) / (R)4;
+      s.d -= (-r.d) / (R)4;
+    }
+    Q<R> m = qmul(U, s);
+    R fz[3] = {(R)2 * m.b, (R)2 * m.c, (R)2 * m.d};
+    R z[3], mod = 0;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      fz[a] *= (R)(4.0 / cp.beta);
+      z[a] = dt * fz[a];
+      mod += z[a] * z[a];
+    }
+    // flow_gauge (gradflow.c:361-401)
+    if (mod <= (R)0) {
+      atomicMin(first_zero, (unsigned long long)(i * 3 + mu));
+      st4<R>(out.link[mu], i, U);
+      continue;
+    }
+    mod = msqrt(mod);
+    R sm = msin(mod);
+    Q<R> u{mcos(mod), sm * z[0] / mod, sm * z[1] / mod, sm * z[2] / mod};
+    st4<R>(out.link[mu], i, qmul(u, U));
+  }
+  if (HAS(C_T)) {
+    // grad_force_triplet (gradflow.c:267-330) and flow_triplet (405-414)
+    R res[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      V3<R> r = qrot(ld4<R>(in.link[d], i), ld3(in, shifted(g, c, d, 1)));
+      res[0] -= r.x; res[1] -= r.y; res[2] -= r.z;
+      int64_t xm = shifted(g, c, d, -1);
+      r = qrot(qdag(ld4<R>(in.link[d], xm)), ld3(in, xm));
+      res[0] -= r.x; res[1] -= r.y; res[2] -= r.z;
+    }
+    V3<R> tr = ld3(in, i);
+    R tv[3] = {tr.x, tr.y, tr.z};
+    R ts = tripletsq(tr);
+    R hm = NHIGGS > 0 ? doubletsq(ld4<R>(in.phi[0], i)) : (R)0;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      res[a] += ((R)6 + (R)cp.msqT + (R)2 * (R)cp.b4 * ts) * tv[a];
+      if (NHIGGS > 0) res[a] += (R)cp.a2 * hm * tv[a];
+    }
+    st3(out, i, V3<R>{tv[0] + dt * (-res[0]), tv[1] + dt * (-res[1]), tv[2] + dt * (-res[2])});
+  }
+}
+
+// links at or after the first zero-force link keep their value (the
+// reference's early return in flow_gauge)
+template <typename R>
+__global__ void k_flow_fixup(Fields<R> in, Fields<R> out, Geom g, const unsigned long long* first_zero) {
+  unsigned long long fz = *first_zero;
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.V * 3 || (unsigned long long)t < fz) return;
+  int64_t i = t / 3;
+  int mu = (int)(t - i * 3);
+  out.link[mu][i] = in.link[mu][i];
+}
+
+// ---------------------------------------------------------------------------
+// transfers, tables, reunitarisation
+// ---------------------------------------------------------------------------
+// host AoS FP64 (lattice-file order) <-> device SoA
+template <typename R>
+__global__ void k_import(Fields<R> f, int64_t V, int kind, int h, const double* src) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  switch (kind) {
+    case 0:  // links [V][3][4]
+      if (t < V * 3) {
+        int64_t i = t / 3;
+        int d = (int)(t - i * 3);
+        const double* s = src + t * 4;
+        st4<R>(f.link[d], i, Q<R>{(R)s[0], (R)s[1], (R)s[2], (R)s[3]});
+      }
+      break;
+    case 1:  // u1 [V][3]
+      if (t < V * 3) {
+        int64_t i = t / 3;
+        f.u1[t - i * 3][i] = (R)src[t];
+      }
+      break;
+    case 2:  // doublet [V][4]
+      if (t < V) {
+        const double* s = src + t * 4;
+        st4<R>(f.phi[h], t, Q<R>{(R)s[0], (R)s[1], (R)s[2], (R)s[3]});
+      }
+      break;
+    case 3:  // triplet [V][3]
+      if (t < V) st3(f, t, V3<R>{(R)src[3 * t], (R)src[3 * t + 1], (R)src[3 * t + 2]});
+      break;
+    case 4:  // singlet [V]
+      if (t < V) f.sing[t] = (R)src[t];
+      break;
+  }
+}
+template <typename R>
+__global__ void k_export(Fields<R> f, int64_t V, int kind, int h, double* dst) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  switch (kind) {
+    case 0:
+      if (t < V * 3) {
+        int64_t i = t / 3;
+        int d = (int)(t - i * 3);
+        Q<R> q = ld4<R>(f.link[d], i);
+        double* s = dst + t * 4;
+        s[0] = q.a; s[1] = q.b; s[2] = q.c; s[3] = q.d;
+      }
+      break;
+    case 1:
+      if (t < V * 3) {
+        int64_t i = t / 3;
+        dst[t] = f.u1[t - i * 3][i];
+      }
+      break;
+    case 2:
+      if (t < V) {
+        Q<R> q = ld4<R>(f.phi[h], t);
+        double* s = dst + t * 4;
+        s[0] = q.a; s[1] = q.b; s[2] = q.c; s[3] = q.d;
+      }
+      break;
+    case 3:
+      if (t < V) {
+        V3<R> v = ld3(f, t);
+        dst[3 * t] = v.x; dst[3 * t + 1] = v.y; dst[3 * t + 2] = v.z;
+      }
+      break;
+    case 4:
+      if (t < V) dst[t] = f.sing[t];
+      break;
+  }
+}
+
+// renormalise every link to unit norm (FP32 form, every `interval` sweeps)
+template <typename R>
+__global__ void k_reunitarize(Fields<R> f, int64_t V, const uint32_t* sweep, int interval) {
+  if (interval <= 0 || (*sweep % (uint32_t)interval) != (uint32_t)(interval - 1)) return;
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= V * 3) return;
+  int64_t i = t / 3;
+  int d = (int)(t - i * 3);
+  Q<R> q = ld4<R>(f.link[d], i);
+  R n = (R)1 / msqrt(qsq(q));
+  st4<R>(f.link[d], i, qscale(q, n));
+}
+
+#undef HAS
+#undef NHIGGS
+
+}  // namespace su2

@@ -1,0 +1,49 @@
+// su2_ops.h -- host-visible launcher tables of the kernel instantiations.
+// Each (precision, content) instantiation unit (su2_inst.cu compiled with
+// SU2_R / SU2_CC) fills one Ops table; the per-precision kernels that do not
+// depend on the content live in a PrecOps table.
+#pragma once
+
+#include "su2_common.cuh"
+
+namespace su2 {
+
+struct PassArgs;
+
+struct Ops {
+  int prec;     // 64 or 32
+  int content;  // C_GENERIC or a content mask
+  void (*link)(const void* f, const PassArgs& a, unsigned nblocks, cudaStream_t st);
+  void (*u1)(const void* f, const PassArgs& a, unsigned nblocks, cudaStream_t st);
+  void (*scalar)(int field, const void* f, const PassArgs& a, unsigned nblocks, cudaStream_t st);
+  void (*measure)(const void* f, const Geom& g, const Coup& cp, const double* alpha, double* partials,
+                  unsigned nblocks, cudaStream_t st);
+  void (*flow)(const void* fin, const void* fout, const Geom& g, const Coup& cp, double dt,
+               unsigned long long* first_zero, unsigned nblocks, cudaStream_t st);
+};
+
+struct PrecOps {
+  void (*orderparam)(const void* f, const Geom& g, int parity, int op, double* partials, unsigned nblocks,
+                     cudaStream_t st);
+  void (*restore)(int field, const void* f, const MucaDev* m, const void* backup, int h, int64_t lo, int64_t hi,
+                  cudaStream_t st);
+  void (*alpha)(const void* f, const Geom& g, const Coup& cp, double* alpha, cudaStream_t st);
+  void (*import)(const void* f, int64_t V, int kind, int h, const double* src, cudaStream_t st);
+  void (*exportf)(const void* f, int64_t V, int kind, int h, double* dst, cudaStream_t st);
+  void (*reunitarize)(const void* f, int64_t V, const uint32_t* sweep, int interval, cudaStream_t st);
+  void (*flow_fixup)(const void* fin, const void* fout, const Geom& g, const unsigned long long* fz,
+                     cudaStream_t st);
+};
+
+// instantiations (su2_inst.cu)
+extern const Ops ops_f64_generic, ops_f64_fund, ops_f64_adj, ops_f64_su2u1s;
+extern const Ops ops_f32_generic, ops_f32_fund, ops_f32_adj, ops_f32_su2u1s;
+extern const PrecOps precops_f64, precops_f32;
+
+// non-template kernels (su2_inst.cu, generic FP64 unit)
+void launch_muca_decide(MucaDev* w, const double* partials, int np, double vol, int parity, const RngKey& rk,
+                        uint32_t pass, uint32_t check, unsigned long long* ctr, cudaStream_t st);
+void launch_muca_set_param(MucaDev* w, const double* partials, int np, double vol, int parity, cudaStream_t st);
+void launch_reduce_partials(const double* partials, int np, double* out, cudaStream_t st);
+
+}  // namespace su2

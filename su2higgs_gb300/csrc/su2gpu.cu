@@ -1,0 +1,865 @@
+// su2gpu.cu -- the C ABI of libsu2gpu (include/su2gpu.h): device-resident
+// lattice contexts, the half-sweep sequence of the reference's
+// update_lattice() (update.c:270-430), multicanonical global checks decided
+// on the device, measurements, gradient flow and CUDA-graph replay.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstddef>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "../../include/su2gpu.h"
+#include "su2_kernels.cuh"
+#include "su2_ops.h"
+
+using namespace su2;
+
+// ---------------------------------------------------------------------------
+// error reporting
+// ---------------------------------------------------------------------------
+static thread_local char g_err[512] = "";
+static void set_err(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+#define CK(call)                                                                     \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess) {                                                         \
+      set_err("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return SU2GPU_ERR_CUDA;                                                        \
+    }                                                                                \
+  } while (0)
+#define CKL()                                                                        \
+  do {                                                                               \
+    cudaError_t e_ = cudaGetLastError();                                             \
+    if (e_ != cudaSuccess) {                                                         \
+      set_err("kernel launch failed: %s (%s:%d)", cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return SU2GPU_ERR_CUDA;                                                        \
+    }                                                                                \
+  } while (0)
+
+static unsigned nblk(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
+
+__global__ void k_set_u32(uint32_t* p, uint32_t v) { *p = v; }
+__global__ void k_inc_u32(uint32_t* p) { *p += 1u; }
+__global__ void k_fill_u64(unsigned long long* p, unsigned long long v) { *p = v; }
+
+// layout tables (layout.c:657-756 serial order) from the closed form
+__global__ void k_layout_tables(Geom g, int64_t* next, int64_t* prev, int64_t* coords, int32_t* parity) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.V) return;
+  int par = i >= g.half;
+  int c[3];
+  site_coords(g, par, i - par * g.half, c);
+  for (int d = 0; d < 3; d++) {
+    next[i * 3 + d] = shifted(g, c, d, 1);
+    prev[i * 3 + d] = shifted(g, c, d, -1);
+    coords[i * 3 + d] = c[d];
+  }
+  parity[i] = par;
+}
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+struct DevBuf {
+  void* p = nullptr;
+  size_t n = 0;
+  int ensure(size_t bytes) {
+    if (bytes <= n) return 0;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) {
+      set_err("cudaMalloc(%zu) failed", bytes);
+      return SU2GPU_ERR_NOMEM;
+    }
+    n = bytes;
+    return 0;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+struct su2gpu_ctx {
+  su2gpu_params p;
+  int prec, nh, has_t, has_s, has_u1;
+  Geom g;
+  Coup cp;
+  const Ops* ops;
+  const PrecOps* pops;
+  cudaStream_t st = nullptr;
+  DevBuf fields, stage, ctrbuf, partials, sums, alpha, backup, muca, flow, rows;
+  Fields<double> f64{};
+  Fields<float> f32{};
+  unsigned long long* d_ctr = nullptr;  // [24] counters (accepted + muca)
+  int* d_err = nullptr;
+  uint32_t* d_sweep = nullptr;
+  unsigned long long* d_fz = nullptr;
+  int64_t host_tot[SU2GPU_NCOUNTERS] = {0};
+  uint64_t seed = 0;
+  uint32_t chain = 0;
+  // multicanonical
+  bool muca_on = false;
+  int muca_bins = 0;
+  MucaDev* d_muca = nullptr;
+  int muca_orderparam = 0, muca_cps = 1, muca_do_acc = 0;
+  // graph of one sweep
+  cudaGraphExec_t gexec = nullptr;
+  int64_t graph_tot[SU2GPU_NCOUNTERS] = {0};
+
+  const void* F() const { return prec == 64 ? (const void*)&f64 : (const void*)&f32; }
+  size_t rsize() const { return prec == 64 ? 8 : 4; }
+  size_t v4size() const { return prec == 64 ? 32 : 16; }
+};
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static int valid_params(const su2gpu_params* p) {
+  if (!p) return 0;
+  if (p->dim != 3) { set_err("only dim 3 is supported on the GPU (got %d)", p->dim); return 0; }
+  for (int d = 0; d < 3; d++)
+    if (p->L[d] < 2 || (p->L[d] & 1)) { set_err("L%d = %d: side lengths must be even and >= 2", d + 1, p->L[d]); return 0; }
+  if (p->precision != 64 && p->precision != 32) { set_err("precision must be 64 or 32"); return 0; }
+  int c = p->content;
+  if ((c & SU2GPU_HIGGS1) && (c & SU2GPU_HIGGS2)) { set_err("HIGGS1 and HIGGS2 are exclusive"); return 0; }
+  if ((c & SU2GPU_HIGGS2) && (c & (SU2GPU_TRIPLET | SU2GPU_SINGLET))) {
+    set_err("two doublets with a triplet or singlet are not implemented (as in the reference)");
+    return 0;
+  }
+  if (p->algorithm_su2link != SU2GPU_HEATBATH && p->algorithm_su2link != SU2GPU_METROPOLIS) {
+    set_err("algorithm_su2link must be heatbath or metropolis"); return 0;
+  }
+  return 1;
+}
+
+static size_t field_bytes(const su2gpu_params* p, int64_t V) {
+  size_t r = p->precision == 64 ? 8 : 4, v4 = 4 * r;
+  int nh = (p->content & SU2GPU_HIGGS2) ? 2 : ((p->content & SU2GPU_HIGGS1) ? 1 : 0);
+  size_t b = 3 * align256(V * v4);
+  if (p->content & SU2GPU_U1) b += 3 * align256(V * r);
+  b += nh * align256(V * v4);
+  if (p->content & SU2GPU_TRIPLET) b += 3 * align256(V * r);
+  if (p->content & SU2GPU_SINGLET) b += align256(V * r);
+  return b;
+}
+
+template <typename R>
+static void carve(Fields<R>& f, char* base, const su2gpu_params* p, int64_t V) {
+  size_t r = sizeof(R), v4 = 4 * r, off = 0;
+  int nh = (p->content & SU2GPU_HIGGS2) ? 2 : ((p->content & SU2GPU_HIGGS1) ? 1 : 0);
+  memset(&f, 0, sizeof(f));
+  for (int d = 0; d < 3; d++) { f.link[d] = (V4<R>*)(base + off); off += align256(V * v4); }
+  if (p->content & SU2GPU_U1)
+    for (int d = 0; d < 3; d++) { f.u1[d] = (R*)(base + off); off += align256(V * r); }
+  for (int h = 0; h < nh; h++) { f.phi[h] = (V4<R>*)(base + off); off += align256(V * v4); }
+  if (p->content & SU2GPU_TRIPLET)
+    for (int k = 0; k < 3; k++) { f.trip[k] = (R*)(base + off); off += align256(V * r); }
+  if (p->content & SU2GPU_SINGLET) { f.sing = (R*)(base + off); off += align256(V * r); }
+}
+
+static Coup make_coup(const su2gpu_params* p) {
+  Coup c;
+  c.beta = p->betasu2; c.msq = p->msq_phi; c.lam = p->lambda_phi;
+  c.msqT = p->msq_triplet; c.a2 = p->a2; c.b4 = p->b4;
+  c.betau1 = p->betau1; c.r_u1 = p->r_u1;
+  c.b1s = p->b1_s; c.msqs = p->msq_s; c.b3s = p->b3_s; c.b4s = p->b4_s; c.a1s = p->a1_s; c.a2s = p->a2_s;
+  c.msq2 = p->msq_phi2; c.m12re = p->m12sq_re; c.m12im = p->m12sq_im;
+  c.lam2 = p->lam2; c.lam3 = p->lam3; c.lam4 = p->lam4; c.lam5re = p->lam5_re; c.lam5im = p->lam5_im;
+  c.lam6re = p->lam6_re; c.lam6im = p->lam6_im; c.lam7re = p->lam7_re; c.lam7im = p->lam7_im;
+  c.content = p->content & 0x1f;
+  c.alg_link = p->algorithm_su2link; c.alg_u1 = p->algorithm_u1link; c.alg_d = p->algorithm_su2doublet;
+  c.alg_t = p->algorithm_su2triplet; c.alg_s = p->algorithm_singlet;
+  return c;
+}
+
+static const Ops* pick_ops(int prec, int content) {
+  int c = content & 0x1f;
+  if (prec == 64) {
+    if (c == C_H1) return &ops_f64_fund;
+    if (c == C_T) return &ops_f64_adj;
+    if (c == (C_H1 | C_S | C_U1)) return &ops_f64_su2u1s;
+    return &ops_f64_generic;
+  }
+  if (c == C_H1) return &ops_f32_fund;
+  if (c == C_T) return &ops_f32_adj;
+  if (c == (C_H1 | C_S | C_U1)) return &ops_f32_su2u1s;
+  return &ops_f32_generic;
+}
+
+extern "C" {
+
+int su2gpu_version(void) { return 10000; }
+
+const char* su2gpu_last_error(void) { return g_err; }
+
+int su2gpu_device_info(int* sm_count, int* cc_major, int* cc_minor, int64_t* free_bytes) {
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  cudaDeviceProp pr;
+  CK(cudaGetDeviceProperties(&pr, dev));
+  if (sm_count) *sm_count = pr.multiProcessorCount;
+  if (cc_major) *cc_major = pr.major;
+  if (cc_minor) *cc_minor = pr.minor;
+  if (free_bytes) {
+    size_t fr = 0, tot = 0;
+    CK(cudaMemGetInfo(&fr, &tot));
+    *free_bytes = (int64_t)fr;
+  }
+  return SU2GPU_OK;
+}
+
+int64_t su2gpu_footprint_bytes(const su2gpu_params* p) {
+  if (!valid_params(p)) return -1;
+  int64_t V = (int64_t)p->L[0] * p->L[1] * p->L[2];
+  size_t b = field_bytes(p, V);
+  b += align256((size_t)(V / BLOCK + 2) * NSUMS * 8);        // partials
+  b += 4096;                                                 // counters, flags, sums
+  if (p->content & SU2GPU_TRIPLET) b += align256(3 * V * 8);  // alpha planes
+  return (int64_t)b;
+}
+
+int su2gpu_create(const su2gpu_params* p, su2gpu_ctx** out) {
+  if (!out) return SU2GPU_ERR_INVALID;
+  *out = nullptr;
+  if (!valid_params(p)) return SU2GPU_ERR_INVALID;
+  su2gpu_ctx* c = new su2gpu_ctx();
+  c->p = *p;
+  c->prec = p->precision;
+  c->nh = (p->content & SU2GPU_HIGGS2) ? 2 : ((p->content & SU2GPU_HIGGS1) ? 1 : 0);
+  c->has_t = !!(p->content & SU2GPU_TRIPLET);
+  c->has_s = !!(p->content & SU2GPU_SINGLET);
+  c->has_u1 = !!(p->content & SU2GPU_U1);
+  for (int d = 0; d < 3; d++) c->g.L[d] = p->L[d];
+  c->g.hL0 = p->L[0] / 2;
+  c->g.V = (int64_t)p->L[0] * p->L[1] * p->L[2];
+  c->g.half = c->g.V / 2;
+  c->cp = make_coup(p);
+  c->ops = pick_ops(c->prec, p->content);
+  c->pops = c->prec == 64 ? &precops_f64 : &precops_f32;
+  int rc;
+  if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) {
+    set_err("cudaStreamCreate failed");
+    delete c;
+    return SU2GPU_ERR_CUDA;
+  }
+  int64_t V = c->g.V;
+  if ((rc = c->fields.ensure(field_bytes(p, V))) ||
+      (rc = c->ctrbuf.ensure(4096)) ||
+      (rc = c->partials.ensure((size_t)(nblk(V, BLOCK) + 2) * NSUMS * 8)) ||
+      (rc = c->sums.ensure(NSUMS * 8))) {
+    su2gpu_destroy(c);
+    return rc;
+  }
+  if (c->prec == 64) carve(c->f64, (char*)c->fields.p, p, V);
+  else carve(c->f32, (char*)c->fields.p, p, V);
+  c->d_ctr = (unsigned long long*)c->ctrbuf.p;
+  c->d_err = (int*)((char*)c->ctrbuf.p + 512);
+  c->d_sweep = (uint32_t*)((char*)c->ctrbuf.p + 1024);
+  c->d_fz = (unsigned long long*)((char*)c->ctrbuf.p + 1536);
+  if (cudaMemsetAsync(c->fields.p, 0, c->fields.n, c->st) != cudaSuccess ||
+      cudaMemsetAsync(c->ctrbuf.p, 0, c->ctrbuf.n, c->st) != cudaSuccess) {
+    set_err("cudaMemset failed");
+    su2gpu_destroy(c);
+    return SU2GPU_ERR_CUDA;
+  }
+  // cold links: unit quaternions (setsu2, init.c:18-28)
+  {
+    std::vector<double> one((size_t)V * 12, 0.0);
+    for (int64_t k = 0; k < V * 3; k++) one[(size_t)k * 4] = 1.0;
+    if ((rc = c->stage.ensure((size_t)V * 12 * 8))) { su2gpu_destroy(c); return rc; }
+    if (cudaMemcpyAsync(c->stage.p, one.data(), (size_t)V * 12 * 8, cudaMemcpyHostToDevice, c->st) != cudaSuccess) {
+      set_err("cold-start upload failed");
+      su2gpu_destroy(c);
+      return SU2GPU_ERR_CUDA;
+    }
+    c->pops->import(c->F(), V, 0, 0, (const double*)c->stage.p, c->st);
+    if (cudaStreamSynchronize(c->st) != cudaSuccess) {
+      set_err("cold start failed: %s", cudaGetErrorString(cudaGetLastError()));
+      su2gpu_destroy(c);
+      return SU2GPU_ERR_CUDA;
+    }
+  }
+  *out = c;
+  return SU2GPU_OK;
+}
+
+int su2gpu_destroy(su2gpu_ctx* c) {
+  if (!c) return SU2GPU_OK;
+  if (c->st) cudaStreamSynchronize(c->st);
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  c->fields.release(); c->stage.release(); c->ctrbuf.release(); c->partials.release(); c->sums.release();
+  c->alpha.release(); c->backup.release(); c->muca.release(); c->flow.release(); c->rows.release();
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+  return SU2GPU_OK;
+}
+
+int su2gpu_layout_tables(su2gpu_ctx* c, int64_t* next, int64_t* prev, int64_t* coords, int32_t* parity) {
+  if (!c) return SU2GPU_ERR_INVALID;
+  int64_t V = c->g.V;
+  DevBuf t;
+  int rc = t.ensure((size_t)V * (3 * 8 * 3 + 4));
+  if (rc) return rc;
+  int64_t* dn = (int64_t*)t.p;
+  int64_t* dp = dn + V * 3;
+  int64_t* dc = dp + V * 3;
+  int32_t* dpar = (int32_t*)(dc + V * 3);
+  k_layout_tables<<<nblk(V, 256), 256, 0, c->st>>>(c->g, dn, dp, dc, dpar);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && next) e = cudaMemcpyAsync(next, dn, V * 24, cudaMemcpyDeviceToHost, c->st);
+  if (e == cudaSuccess && prev) e = cudaMemcpyAsync(prev, dp, V * 24, cudaMemcpyDeviceToHost, c->st);
+  if (e == cudaSuccess && coords) e = cudaMemcpyAsync(coords, dc, V * 24, cudaMemcpyDeviceToHost, c->st);
+  if (e == cudaSuccess && parity) e = cudaMemcpyAsync(parity, dpar, V * 4, cudaMemcpyDeviceToHost, c->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  t.release();
+  if (e != cudaSuccess) { set_err("layout tables: %s", cudaGetErrorString(e)); return SU2GPU_ERR_CUDA; }
+  return SU2GPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// field transfer
+// ---------------------------------------------------------------------------
+static int transfer(su2gpu_ctx* c, int upload, double* link, double* u1, double* d0, double* d1, double* trip,
+                    double* sing) {
+  int64_t V = c->g.V;
+  int rc = c->stage.ensure((size_t)V * 12 * 8);
+  if (rc) return rc;
+  double* st = (double*)c->stage.p;
+  struct Item { double* h; int kind, h_id; size_t n; bool present; };
+  Item items[] = {
+      {link, 0, 0, (size_t)V * 12, true},
+      {u1, 1, 0, (size_t)V * 3, (bool)c->has_u1},
+      {d0, 2, 0, (size_t)V * 4, c->nh > 0},
+      {d1, 2, 1, (size_t)V * 4, c->nh > 1},
+      {trip, 3, 0, (size_t)V * 3, (bool)c->has_t},
+      {sing, 4, 0, (size_t)V, (bool)c->has_s},
+  };
+  for (const Item& it : items) {
+    if (!it.present || !it.h) continue;
+    if (upload) {
+      CK(cudaMemcpyAsync(st, it.h, it.n * 8, cudaMemcpyHostToDevice, c->st));
+      c->pops->import(c->F(), V, it.kind, it.h_id, st, c->st);
+      CKL();
+    } else {
+      c->pops->exportf(c->F(), V, it.kind, it.h_id, st, c->st);
+      CKL();
+      CK(cudaMemcpyAsync(it.h, st, it.n * 8, cudaMemcpyDeviceToHost, c->st));
+    }
+    CK(cudaStreamSynchronize(c->st));
+  }
+  return SU2GPU_OK;
+}
+
+int su2gpu_upload_fields(su2gpu_ctx* c, const double* link, const double* u1, const double* d0, const double* d1,
+                         const double* trip, const double* sing) {
+  if (!c) return SU2GPU_ERR_INVALID;
+  return transfer(c, 1, (double*)link, (double*)u1, (double*)d0, (double*)d1, (double*)trip, (double*)sing);
+}
+
+int su2gpu_download_fields(su2gpu_ctx* c, double* link, double* u1, double* d0, double* d1, double* trip,
+                           double* sing) {
+  if (!c) return SU2GPU_ERR_INVALID;
+  return transfer(c, 0, link, u1, d0, d1, trip, sing);
+}
+
+int su2gpu_set_seed(su2gpu_ctx* c, uint64_t seed, uint32_t chain) {
+  if (!c) return SU2GPU_ERR_INVALID;
+  c->seed = seed;
+  c->chain = chain;
+  if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
+  return SU2GPU_OK;
+}
+
+double su2gpu_stream_uniform(uint64_t seed, uint32_t site, uint32_t pass, uint32_t draw, uint32_t sweep,
+                             uint32_t chain) {
+  return philox_uniform53((uint32_t)seed, (uint32_t)(seed >> 32), site, pass, draw >> 1, sweep, chain, draw & 1);
+}
+
+// ---------------------------------------------------------------------------
+// one sweep: update_lattice (update.c:270-430), non-random order
+// ---------------------------------------------------------------------------
+static int scalar_pass(su2gpu_ctx* c, const PassArgs& base, int field, int h, int par, int metro, uint32_t pass,
+                       int64_t* tot) {
+  const int64_t N = c->g.half;
+  int alg = field == 0 ? c->p.algorithm_su2doublet : (field == 1 ? c->p.algorithm_su2triplet : c->p.algorithm_singlet);
+  bool orr = alg == SU2GPU_OVERRELAX && !metro;
+  int tot_idx = field == 0 ? (orr ? SU2GPU_C_TOTAL_OR_DOUBLET : SU2GPU_C_TOTAL_DOUBLET) + h
+                           : (field == 1 ? (orr ? SU2GPU_C_TOTAL_OR_TRIPLET : SU2GPU_C_TOTAL_TRIPLET)
+                                         : (orr ? SU2GPU_C_TOTAL_OR_SINGLET : SU2GPU_C_TOTAL_SINGLET));
+  tot[tot_idx] += N;
+  PassArgs a = base;
+  a.parity = par;
+  a.sub = h;
+  a.alg = metro;
+  a.pass = pass;
+  int op = c->muca_orderparam;
+  bool do_muca = c->muca_on && c->muca_do_acc && field != 2 &&
+                 ((field == 0 && ((h == 0 && (op == SU2GPU_PHISQ || op == SU2GPU_PHI2MINUSSIGMA2)) ||
+                                  (h == 1 && op == SU2GPU_PHI2SQ))) ||
+                  (field == 1 && (op == SU2GPU_SIGMASQ || op == SU2GPU_PHI2MINUSSIGMA2)));
+  if (!do_muca) {
+    a.t_lo = 0;
+    a.t_hi = N;
+    c->ops->scalar(field, c->F(), a, nblk(N, BLOCK), c->st);
+    CKL();
+    return SU2GPU_OK;
+  }
+  // checkerboard_sweep_su2doublet/_su2triplet (update.c:82-229): global
+  // checks after every `interval` sites, a final one if the blocks do not
+  // add up; the fields of the checked block are restored on reject
+  const int cps = c->muca_cps;
+  int64_t interval = N / cps;
+  if (interval <= 0) interval = 1;
+  int64_t m = N / interval;
+  bool fused = (m == 1 && interval == N);
+  double* partials = (double*)c->partials.p;
+  const double vol = (double)c->g.V;
+  uint32_t check = 0;
+  RngKey rk = base.rk;
+  a.backup = c->backup.p;
+  a.op = op;
+  for (int64_t k = 0; k < m; k++) {
+    a.t_lo = k * interval;
+    a.t_hi = (k + 1) * interval;
+    a.partials = fused ? partials : nullptr;
+    unsigned nb = nblk(a.t_hi - a.t_lo, BLOCK);
+    c->ops->scalar(field, c->F(), a, nb, c->st);
+    CKL();
+    unsigned np = nb;
+    if (!fused) {
+      np = nblk(N, BLOCK);
+      c->pops->orderparam(c->F(), c->g, par, op, partials, np, c->st);
+      CKL();
+    }
+    launch_muca_decide(c->d_muca, partials, (int)np, vol, par, rk, pass, check++, c->d_ctr, c->st);
+    CKL();
+    c->pops->restore(field, c->F(), c->d_muca, c->backup.p, h, par * N + a.t_lo, par * N + a.t_hi, c->st);
+    CKL();
+  }
+  if (N % cps != 0) {
+    int64_t lo = m * interval, hi = N, rlo = lo, rhi = hi;
+    if (lo < hi) {
+      a.t_lo = lo;
+      a.t_hi = hi;
+      a.partials = nullptr;
+      c->ops->scalar(field, c->F(), a, nblk(hi - lo, BLOCK), c->st);
+      CKL();
+    } else {
+      // nothing left to update: a reject reverts the last block, whose
+      // backup the reference did not refresh after its final check
+      rlo = (m - 1) * interval;
+      rhi = m * interval;
+    }
+    unsigned np = nblk(N, BLOCK);
+    c->pops->orderparam(c->F(), c->g, par, op, partials, np, c->st);
+    CKL();
+    launch_muca_decide(c->d_muca, partials, (int)np, vol, par, rk, pass, check++, c->d_ctr, c->st);
+    CKL();
+    c->pops->restore(field, c->F(), c->d_muca, c->backup.p, h, par * N + rlo, par * N + rhi, c->st);
+    CKL();
+  }
+  return SU2GPU_OK;
+}
+
+static int enqueue_sweep(su2gpu_ctx* c, int64_t* tot) {
+  const su2gpu_params& p = c->p;
+  const int64_t N = c->g.half;
+  PassArgs base;
+  memset(&base, 0, sizeof(base));
+  base.g = c->g;
+  base.cp = c->cp;
+  base.rk = RngKey{(uint32_t)c->seed, (uint32_t)(c->seed >> 32), c->chain, c->d_sweep};
+  base.ctr = c->d_ctr;
+  base.err = c->d_err;
+  uint32_t pass = 0;
+  int rc;
+  for (int k = 0; k < p.update_links; k++) {
+    for (int mu = 0; mu < 3; mu++)
+      for (int par = 0; par <= 1; par++) {
+        PassArgs a = base;
+        a.parity = par; a.sub = mu; a.alg = p.algorithm_su2link; a.pass = pass++; a.t_lo = 0; a.t_hi = N;
+        c->ops->link(c->F(), a, nblk(N, BLOCK), c->st);
+        CKL();
+        tot[SU2GPU_C_TOTAL_SU2LINK] += N;
+      }
+    if (c->has_u1)
+      for (int mu = 0; mu < 3; mu++)
+        for (int par = 0; par <= 1; par++) {
+          PassArgs a = base;
+          a.parity = par; a.sub = mu; a.pass = pass++; a.t_lo = 0; a.t_hi = N;
+          c->ops->u1(c->F(), a, nblk(N, BLOCK), c->st);
+          CKL();
+          tot[SU2GPU_C_TOTAL_U1LINK] += N;
+        }
+  }
+  int nsweeps = p.scalar_sweeps + 1;
+  for (int s = 0; s < nsweeps; s++) {
+    if (c->nh > 0)
+      for (int k = 0; k < p.update_su2doublet; k++) {
+        int force = 0;
+        if (s >= nsweeps - 1) {
+          if (p.algorithm_su2doublet == SU2GPU_OVERRELAX) force = 1;
+          else continue;
+        }
+        for (int h = 0; h < c->nh; h++)
+          for (int par = 0; par <= 1; par++)
+            if ((rc = scalar_pass(c, base, 0, h, par, force, pass++, tot))) return rc;
+      }
+    if (c->has_t)
+      for (int k = 0; k < p.update_su2triplet; k++) {
+        int force = 0;
+        if (s >= nsweeps - 1) {
+          if (p.algorithm_su2triplet == SU2GPU_OVERRELAX) force = 1;
+          else continue;
+        }
+        for (int par = 0; par <= 1; par++)
+          if ((rc = scalar_pass(c, base, 1, 0, par, force, pass++, tot))) return rc;
+      }
+    if (c->has_s)
+      for (int k = 0; k < p.update_singlet; k++) {
+        int force = 0;
+        if (s >= nsweeps - 1) {
+          if (p.algorithm_singlet == SU2GPU_OVERRELAX) force = 1;
+          else continue;
+        }
+        for (int par = 0; par <= 1; par++)
+          if ((rc = scalar_pass(c, base, 2, 0, par, force, pass++, tot))) return rc;
+      }
+  }
+  if (c->prec == 32 && p.reunitarize_interval > 0) {
+    c->pops->reunitarize(c->F(), c->g.V, c->d_sweep, p.reunitarize_interval, c->st);
+    CKL();
+  }
+  return SU2GPU_OK;
+}
+
+static int check_device_error(su2gpu_ctx* c) {
+  int herr = 0;
+  CK(cudaMemcpyAsync(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (herr) {
+    set_err("a kernel reported an invalid state (sphere sampling did not terminate: NaN fields?)");
+    return SU2GPU_ERR_KERNEL;
+  }
+  return SU2GPU_OK;
+}
+
+int su2gpu_update_lattice(su2gpu_ctx* c, uint32_t sweep) {
+  if (!c) return SU2GPU_ERR_INVALID;
+  k_set_u32<<<1, 1, 0, c->st>>>(c->d_sweep, sweep);
+  CKL();
+  int rc = enqueue_sweep(c, c->host_tot);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->st));
+  return SU2GPU_OK;
+}
+
+int su2gpu_run_sweeps(su2gpu_ctx* c, uint32_t first_sweep, int32_t nsweeps, int32_t use_graph) {
+  if (!c || nsweeps < 0) return SU2GPU_ERR_INVALID;
+  k_set_u32<<<1, 1, 0, c->st>>>(c->d_sweep, first_sweep);
+  CKL();
+  if (use_graph) {
+    if (!c->gexec) {
+      int64_t tot[SU2GPU_NCOUNTERS] = {0};
+      cudaGraph_t graph;
+      CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+      int rc = enqueue_sweep(c, tot);
+      k_inc_u32<<<1, 1, 0, c->st>>>(c->d_sweep);
+      cudaError_t e = cudaStreamEndCapture(c->st, &graph);
+      if (rc) return rc;
+      if (e != cudaSuccess) { set_err("graph capture: %s", cudaGetErrorString(e)); return SU2GPU_ERR_CUDA; }
+      e = cudaGraphInstantiate(&c->gexec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (e != cudaSuccess) { set_err("graph instantiate: %s", cudaGetErrorString(e)); return SU2GPU_ERR_CUDA; }
+      memcpy(c->graph_tot, tot, sizeof(tot));
+    }
+    for (int s = 0; s < nsweeps; s++) {
+      CK(cudaGraphLaunch(c->gexec, c->st));
+      for (int k = 0; k < SU2GPU_NCOUNTERS; k++) c->host_tot[k] += c->graph_tot[k];
+    }
+  } else {
+    for (int s = 0; s < nsweeps; s++) {
+      int rc = enqueue_sweep(c, c->host_tot);
+      if (rc) return rc;
+      k_inc_u32<<<1, 1, 0, c->st>>>(c->d_sweep);
+      CKL();
+    }
+  }
+  CK(cudaStreamSynchronize(c->st));
+  return SU2GPU_OK;
+}
+
+int su2gpu_get_counters(su2gpu_ctx* c, int64_t* out) {
+  if (!c || !out) return SU2GPU_ERR_INVALID;
+  unsigned long long d[SU2GPU_NCOUNTERS];
+  CK(cudaMemcpyAsync(d, c->d_ctr, sizeof(d), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  for (int k = 0; k < SU2GPU_NCOUNTERS; k++) out[k] = (int64_t)d[k] + c->host_tot[k];
+  return check_device_error(c);
+}
+
+int su2gpu_reset_counters(su2gpu_ctx* c) {
+  if (!c) return SU2GPU_ERR_INVALID;
+  CK(cudaMemsetAsync(c->d_ctr, 0, SU2GPU_NCOUNTERS * 8, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  memset(c->host_tot, 0, sizeof(c->host_tot));
+  return SU2GPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// measurements
+// ---------------------------------------------------------------------------
+static int enqueue_measure(su2gpu_ctx* c, const void* F, const Coup& cp, double* out) {
+  int64_t V = c->g.V;
+  if (c->has_t) {
+    int rc = c->alpha.ensure((size_t)V * 3 * 8);
+    if (rc) return rc;
+    c->pops->alpha(F, c->g, cp, (double*)c->alpha.p, c->st);
+    CKL();
+  }
+  unsigned nb = nblk(V, BLOCK);
+  c->ops->measure(F, c->g, cp, (const double*)c->alpha.p, (double*)c->partials.p, nb, c->st);
+  CKL();
+  launch_reduce_partials((const double*)c->partials.p, (int)nb, out, c->st);
+  CKL();
+  return SU2GPU_OK;
+}
+
+int su2gpu_measure(su2gpu_ctx* c, double* sums) {
+  if (!c || !sums) return SU2GPU_ERR_INVALID;
+  int rc = enqueue_measure(c, c->F(), c->cp, (double*)c->sums.p);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(sums, c->sums.p, NSUMS * 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return SU2GPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// multicanonical state
+// ---------------------------------------------------------------------------
+int su2gpu_muca_set(su2gpu_ctx* c, const su2gpu_weight* w) {
+  if (!c || !w || w->bins <= 0) return SU2GPU_ERR_INVALID;
+  if (w->checks_per_sweep <= 0 || w->update_interval <= 0) { set_err("checks_per_sweep and update_interval must be > 0"); return SU2GPU_ERR_INVALID; }
+  int n = w->bins + 2;
+  size_t arr = align256((size_t)n * 8);
+  int rc = c->muca.ensure(align256(sizeof(MucaDev)) + 9 * arr);
+  if (rc) return rc;
+  char* base = (char*)c->muca.p;
+  MucaDev m;
+  memset(&m, 0, sizeof(m));
+  m.orderparam = w->orderparam; m.mode = w->mode; m.do_acceptance = w->do_acceptance;
+  m.checks_per_sweep = w->checks_per_sweep; m.bins = w->bins; m.muca_count = w->muca_count;
+  m.update_interval = w->update_interval; m.last_max = w->last_max;
+  m.param_value[0] = w->param_value[0]; m.param_value[1] = w->param_value[1];
+  m.min = w->min; m.max = w->max; m.wrk_min = w->wrk_min; m.wrk_max = w->wrk_max; m.delta = w->delta;
+  size_t off = align256(sizeof(MucaDev));
+  m.pos = (double*)(base + off); off += arr;
+  m.W = (double*)(base + off); off += arr;
+  m.slope = (double*)(base + off); off += arr;
+  m.b = (double*)(base + off); off += arr;
+  m.hits = (int*)(base + off); off += arr;
+  m.gsum = (long long*)(base + off); off += arr;
+  m.nsum = (long long*)(base + off); off += arr;
+  m.hgram = (double*)(base + off); off += arr;
+  m.wold = (double*)(base + off); off += arr;
+  CK(cudaMemcpyAsync(base, &m, sizeof(m), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(m.pos, w->pos, n * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(m.W, w->W, n * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(m.slope, w->slope, n * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(m.b, w->b, n * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(m.hits, w->hits, n * 4, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemsetAsync(m.gsum, 0, arr * 3, c->st));
+  if (w->gsum) CK(cudaMemcpyAsync(m.gsum, w->gsum, n * 8, cudaMemcpyHostToDevice, c->st));
+  if (w->nsum) CK(cudaMemcpyAsync(m.nsum, w->nsum, n * 8, cudaMemcpyHostToDevice, c->st));
+  if (w->hgram) CK(cudaMemcpyAsync(m.hgram, w->hgram, n * 8, cudaMemcpyHostToDevice, c->st));
+  size_t bu = c->prec == 64 ? 32 : 16;
+  if ((rc = c->backup.ensure((size_t)c->g.V * bu))) return rc;
+  CK(cudaStreamSynchronize(c->st));
+  c->d_muca = (MucaDev*)base;
+  c->muca_on = true;
+  c->muca_bins = w->bins;
+  c->muca_orderparam = w->orderparam;
+  c->muca_cps = w->checks_per_sweep;
+  c->muca_do_acc = w->do_acceptance;
+  if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
+  return SU2GPU_OK;
+}
+
+int su2gpu_muca_get(su2gpu_ctx* c, su2gpu_weight* w) {
+  if (!c || !w || !c->muca_on) return SU2GPU_ERR_INVALID;
+  MucaDev m;
+  CK(cudaMemcpyAsync(&m, c->d_muca, sizeof(m), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  int n = m.bins + 2;
+  w->orderparam = m.orderparam; w->mode = m.mode; w->do_acceptance = m.do_acceptance;
+  w->checks_per_sweep = m.checks_per_sweep; w->bins = m.bins; w->muca_count = m.muca_count;
+  w->update_interval = m.update_interval; w->last_max = m.last_max;
+  w->param_value[0] = m.param_value[0]; w->param_value[1] = m.param_value[1];
+  w->min = m.min; w->max = m.max; w->wrk_min = m.wrk_min; w->wrk_max = m.wrk_max; w->delta = m.delta;
+  if (w->pos) CK(cudaMemcpyAsync(w->pos, m.pos, n * 8, cudaMemcpyDeviceToHost, c->st));
+  if (w->W) CK(cudaMemcpyAsync(w->W, m.W, n * 8, cudaMemcpyDeviceToHost, c->st));
+  if (w->slope) CK(cudaMemcpyAsync(w->slope, m.slope, n * 8, cudaMemcpyDeviceToHost, c->st));
+  if (w->b) CK(cudaMemcpyAsync(w->b, m.b, n * 8, cudaMemcpyDeviceToHost, c->st));
+  if (w->hits) CK(cudaMemcpyAsync(w->hits, m.hits, n * 4, cudaMemcpyDeviceToHost, c->st));
+  if (w->gsum) CK(cudaMemcpyAsync(w->gsum, m.gsum, n * 8, cudaMemcpyDeviceToHost, c->st));
+  if (w->nsum) CK(cudaMemcpyAsync(w->nsum, m.nsum, n * 8, cudaMemcpyDeviceToHost, c->st));
+  if (w->hgram) CK(cudaMemcpyAsync(w->hgram, m.hgram, n * 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return SU2GPU_OK;
+}
+
+// number of weight recursions done on the device so far (the host rewrites
+// the weight file when it changes, as save_weight() does after each update)
+int su2gpu_muca_weight_updates(su2gpu_ctx* c, int32_t* n) {
+  if (!c || !n || !c->muca_on) return SU2GPU_ERR_INVALID;
+  MucaDev m;
+  CK(cudaMemcpyAsync(&m, c->d_muca, sizeof(m), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  *n = m.weight_updates;
+  return SU2GPU_OK;
+}
+
+int su2gpu_calc_orderparam(su2gpu_ctx* c, int32_t parity, double* value) {
+  if (!c || !c->muca_on || (parity != 0 && parity != 1)) return SU2GPU_ERR_INVALID;
+  unsigned np = nblk(c->g.half, BLOCK);
+  c->pops->orderparam(c->F(), c->g, parity, c->muca_orderparam, (double*)c->partials.p, np, c->st);
+  CKL();
+  launch_muca_set_param(c->d_muca, (const double*)c->partials.p, (int)np, (double)c->g.V, parity, c->st);
+  CKL();
+  MucaDev m;
+  CK(cudaMemcpyAsync(&m, c->d_muca, sizeof(m), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (value) *value = m.param_value[parity] + m.param_value[1 - parity];
+  return SU2GPU_OK;
+}
+
+// init_last_max (multicanonical.c:826-831)
+int su2gpu_muca_init_last_max(su2gpu_ctx* c) {
+  if (!c || !c->muca_on) return SU2GPU_ERR_INVALID;
+  MucaDev m;
+  CK(cudaMemcpyAsync(&m, c->d_muca, sizeof(m), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  double val = m.param_value[0] + m.param_value[1];
+  int lm = (fabs(val - m.wrk_min) >= fabs(val - m.wrk_max));
+  CK(cudaMemcpyAsync((char*)c->d_muca + offsetof(MucaDev, last_max), &lm, sizeof(int), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return SU2GPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// gradient flow (gradflow.c:46-173)
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+// remove_counterterms (gradflow.c:424-459): the triplet's tree-level mass
+static double triplet_tree_mass(const su2gpu_params* p) {
+  const double Sigma = 3.17591153625, zeta = 0.08849, delta = 1.942130, rho = -0.313964;
+  const double k1 = 0.958382, k2 = 0.25 * Sigma * Sigma - 0.5 * delta - 0.25, k3 = 0.751498, k4 = 1.204295;
+  double gsq = 4.0 / p->betasu2, RGscale = gsq, b4 = p->b4;
+  double ct = -(4.0 * gsq + 5.0 * b4) * Sigma / (4.0 * M_PI);
+  ct += -1.0 / (16.0 * M_PI * M_PI) *
+        ((20.0 * b4 * gsq - 10.0 * b4 * b4) * (log(6.0 / (RGscale)) + zeta) + 20.0 * b4 * gsq * (0.25 * Sigma * Sigma - delta) +
+         2.0 * gsq * gsq * (1.25 * Sigma * Sigma + M_PI / 3.0 * Sigma - 6.0 * delta - 6.0 * rho + 4.0 * k1 - k2 - k3 - 3.0 * k4));
+  return p->msq_triplet - ct;
+}
+
+template <typename R>
+static int flow_impl(su2gpu_ctx* c, Fields<R>& main, double t_max, double dt, int32_t mi, double* rows,
+                     int32_t maxrows, int32_t* nrows) {
+  int64_t V = c->g.V;
+  size_t lb = align256((size_t)V * sizeof(V4<R>)), tb = align256((size_t)V * sizeof(R));
+  size_t per = 3 * lb + (c->has_t ? 3 * tb : 0);
+  int rc = c->flow.ensure(2 * per);
+  if (rc) return rc;
+  Fields<R> A = main, B = main;
+  char* base = (char*)c->flow.p;
+  for (int d = 0; d < 3; d++) {
+    A.link[d] = (V4<R>*)(base + d * lb);
+    B.link[d] = (V4<R>*)(base + per + d * lb);
+    CK(cudaMemcpyAsync(A.link[d], main.link[d], V * sizeof(V4<R>), cudaMemcpyDeviceToDevice, c->st));
+  }
+  if (c->has_t)
+    for (int k = 0; k < 3; k++) {
+      A.trip[k] = (R*)(base + 3 * lb + k * tb);
+      B.trip[k] = (R*)(base + per + 3 * lb + k * tb);
+      CK(cudaMemcpyAsync(A.trip[k], main.trip[k], V * sizeof(R), cudaMemcpyDeviceToDevice, c->st));
+    }
+  Coup cp = c->cp;
+  if (c->has_t) cp.msqT = triplet_tree_mass(&c->p);
+  const int W = 1 + NSUMS;
+  // rows buffered on the device: one copy back at the end
+  int64_t cap = maxrows > 0 ? maxrows : 1;
+  if ((rc = c->rows.ensure((size_t)cap * NSUMS * 8))) return rc;
+  double* drows = (double*)c->rows.p;
+  std::vector<double> times;
+  int nr = 0;
+  double t = 0.0;
+  auto meas = [&](double tt) -> int {
+    if (nr >= maxrows) return SU2GPU_OK;
+    int r = enqueue_measure(c, &A, cp, drows + (size_t)nr * NSUMS);
+    if (r) return r;
+    times.push_back(tt);
+    nr++;
+    return SU2GPU_OK;
+  };
+  if ((rc = meas(t))) return rc;
+  int iter = 1;
+  unsigned nb = nblk(V, BLOCK);
+  while (t < t_max) {
+    if (t + dt > t_max) dt = t_max - t;
+    k_fill_u64<<<1, 1, 0, c->st>>>(c->d_fz, ~0ull);
+    c->ops->flow(&A, &B, c->g, cp, dt, c->d_fz, nb, c->st);
+    CKL();
+    c->pops->flow_fixup(&A, &B, c->g, c->d_fz, c->st);
+    CKL();
+    std::swap(A, B);
+    t += dt;
+    if (iter % mi == 0)
+      if ((rc = meas(t))) return rc;
+    iter++;
+  }
+  if ((iter - 1) % mi != 0)
+    if ((rc = meas(t))) return rc;
+  std::vector<double> h((size_t)nr * NSUMS);
+  if (nr) CK(cudaMemcpyAsync(h.data(), drows, (size_t)nr * NSUMS * 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  for (int r = 0; r < nr; r++) {
+    rows[(size_t)r * W] = times[r];
+    memcpy(rows + (size_t)r * W + 1, h.data() + (size_t)r * NSUMS, NSUMS * 8);
+  }
+  *nrows = nr;
+  return SU2GPU_OK;
+}
+
+extern "C" {
+
+int su2gpu_grad_flow(su2gpu_ctx* c, double t_max, double dt, int32_t meas_interval, double* rows, int32_t maxrows,
+                     int32_t* nrows) {
+  if (!c || !rows || !nrows || meas_interval <= 0 || dt <= 0) return SU2GPU_ERR_INVALID;
+  if (c->prec == 64) return flow_impl<double>(c, c->f64, t_max, dt, meas_interval, rows, maxrows, nrows);
+  return flow_impl<float>(c, c->f32, t_max, dt, meas_interval, rows, maxrows, nrows);
+}
+
+// ---------------------------------------------------------------------------
+// drop-in update_lattice with host buffers
+// ---------------------------------------------------------------------------
+int su2gpu_update_lattice_host(su2gpu_ctx* c, uint32_t sweep, double* link, double* u1, double* d0, double* d1,
+                               double* trip, double* sing) {
+  int rc = su2gpu_upload_fields(c, link, u1, d0, d1, trip, sing);
+  if (rc) return rc;
+  if ((rc = su2gpu_update_lattice(c, sweep))) return rc;
+  return su2gpu_download_fields(c, link, u1, d0, d1, trip, sing);
+}
+
+}  // extern "C"

@@ -1,0 +1,201 @@
+"""Python binding of libsu2gpu (include/su2gpu.h) through ctypes.
+
+`Lattice` mirrors the reference's per-lattice entry points: update_lattice()
+(update.c:270), measure() sums (measure.c:71), grad_flow() (gradflow.c:46),
+calc_orderparam() (multicanonical.c:709) and the field transfer that stands in
+for load_lattice()/save_lattice() (checkpoint.c:84-214).  Host field arrays are
+FP64, array-of-structures, in the reference's EVEN-first site order.
+
+There is no CPU fallback: every call goes to the CUDA library, and a missing
+library or device raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import abi
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libsu2gpu.so")
+
+_lib = None
+
+
+class SU2GPUError(RuntimeError):
+    pass
+
+
+def lib():
+    """The loaded libsu2gpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise SU2GPUError(f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, i32, u32, u64, i64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int64
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.su2gpu_last_error.restype = ctypes.c_char_p
+        L.su2gpu_create.argtypes = [ctypes.POINTER(abi.Params), ctypes.POINTER(vp)]
+        L.su2gpu_destroy.argtypes = [vp]
+        L.su2gpu_footprint_bytes.restype = i64
+        L.su2gpu_footprint_bytes.argtypes = [ctypes.POINTER(abi.Params)]
+        L.su2gpu_layout_tables.argtypes = [vp, vp, vp, vp, vp]
+        L.su2gpu_upload_fields.argtypes = [vp] + [vp] * 6
+        L.su2gpu_download_fields.argtypes = [vp] + [vp] * 6
+        L.su2gpu_set_seed.argtypes = [vp, u64, u32]
+        L.su2gpu_update_lattice.argtypes = [vp, u32]
+        L.su2gpu_run_sweeps.argtypes = [vp, u32, i32, i32]
+        L.su2gpu_get_counters.argtypes = [vp, vp]
+        L.su2gpu_reset_counters.argtypes = [vp]
+        L.su2gpu_measure.argtypes = [vp, vp]
+        L.su2gpu_muca_set.argtypes = [vp, ctypes.POINTER(abi.Weight)]
+        L.su2gpu_muca_get.argtypes = [vp, ctypes.POINTER(abi.Weight)]
+        L.su2gpu_muca_weight_updates.argtypes = [vp, ctypes.POINTER(i32)]
+        L.su2gpu_calc_orderparam.argtypes = [vp, i32, dp]
+        L.su2gpu_muca_init_last_max.argtypes = [vp]
+        L.su2gpu_grad_flow.argtypes = [vp, ctypes.c_double, ctypes.c_double, i32, vp, i32, ctypes.POINTER(i32)]
+        L.su2gpu_update_lattice_host.argtypes = [vp, u32] + [vp] * 6
+        L.su2gpu_stream_uniform.restype = ctypes.c_double
+        L.su2gpu_stream_uniform.argtypes = [u64, u32, u32, u32, u32, u32]
+        L.su2gpu_device_info.argtypes = [ctypes.POINTER(ctypes.c_int)] * 3 + [ctypes.POINTER(i64)]
+        _lib = L
+    return _lib
+
+
+def check(rc):
+    if rc != abi.OK:
+        raise SU2GPUError(f"libsu2gpu error {rc}: {lib().su2gpu_last_error().decode()}")
+    return rc
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+FIELD_NAMES = ("link", "u1", "d0", "d1", "trip", "sing")
+
+
+class Lattice:
+    """One device-resident chain (a su2gpu context)."""
+
+    def __init__(self, params, seed=0, chain=0):
+        self.params = params
+        self.V = params.sites()
+        self._h = ctypes.c_void_p()
+        check(lib().su2gpu_create(ctypes.byref(params), ctypes.byref(self._h)))
+        check(lib().su2gpu_set_seed(self._h, seed, chain))
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().su2gpu_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def shapes(self):
+        p, V = self.params, self.V
+        nh = p.nhiggs()
+        return {
+            "link": (V, 3, 4),
+            "u1": (V, 3) if p.content & abi.U1 else None,
+            "d0": (V, 4) if nh > 0 else None,
+            "d1": (V, 4) if nh > 1 else None,
+            "trip": (V, 3) if p.content & abi.TRIPLET else None,
+            "sing": (V,) if p.content & abi.SINGLET else None,
+        }
+
+    def upload(self, **fields):
+        arrs = []
+        for n in FIELD_NAMES:
+            a = fields.get(n)
+            arrs.append(None if a is None else np.ascontiguousarray(a, dtype=np.float64))
+        check(lib().su2gpu_upload_fields(self._h, *[_p(a) for a in arrs]))
+
+    def download(self):
+        out = {}
+        for n, shp in self.shapes().items():
+            out[n] = None if shp is None else np.zeros(shp)
+        check(lib().su2gpu_download_fields(self._h, *[_p(out[n]) for n in FIELD_NAMES]))
+        return out
+
+    def set_seed(self, seed, chain=0):
+        check(lib().su2gpu_set_seed(self._h, seed, chain))
+
+    def update_lattice(self, sweep):
+        check(lib().su2gpu_update_lattice(self._h, sweep))
+
+    def run_sweeps(self, first_sweep, n, graph=True):
+        check(lib().su2gpu_run_sweeps(self._h, first_sweep, n, 1 if graph else 0))
+
+    def counters(self):
+        c = np.zeros(abi.NCOUNTERS, np.int64)
+        check(lib().su2gpu_get_counters(self._h, _p(c)))
+        return c
+
+    def reset_counters(self):
+        check(lib().su2gpu_reset_counters(self._h))
+
+    def measure(self):
+        m = np.zeros(abi.NMEAS)
+        check(lib().su2gpu_measure(self._h, _p(m)))
+        return m
+
+    def layout_tables(self):
+        V = self.V
+        nx, pv, co = (np.zeros(V * 3, np.int64) for _ in range(3))
+        par = np.zeros(V, np.int32)
+        check(lib().su2gpu_layout_tables(self._h, _p(nx), _p(pv), _p(co), _p(par)))
+        return nx.reshape(V, 3), pv.reshape(V, 3), co.reshape(V, 3), par
+
+    def muca_set(self, weight_struct):
+        check(lib().su2gpu_muca_set(self._h, ctypes.byref(weight_struct)))
+
+    def muca_get(self, weight_struct):
+        check(lib().su2gpu_muca_get(self._h, ctypes.byref(weight_struct)))
+
+    def muca_weight_updates(self):
+        n = ctypes.c_int32(0)
+        check(lib().su2gpu_muca_weight_updates(self._h, ctypes.byref(n)))
+        return n.value
+
+    def calc_orderparam(self, parity):
+        v = ctypes.c_double(0)
+        check(lib().su2gpu_calc_orderparam(self._h, parity, ctypes.byref(v)))
+        return v.value
+
+    def muca_init_last_max(self):
+        check(lib().su2gpu_muca_init_last_max(self._h))
+
+    def grad_flow(self, t_max, dt, meas_interval, maxrows=None):
+        if maxrows is None:
+            maxrows = int(t_max / dt) // meas_interval + 4
+        rows = np.zeros((maxrows, 1 + abi.NMEAS))
+        n = ctypes.c_int32(0)
+        check(lib().su2gpu_grad_flow(self._h, t_max, dt, meas_interval, _p(rows), maxrows, ctypes.byref(n)))
+        return rows[: n.value].copy()
+
+    def update_lattice_host(self, sweep, fields):
+        """Drop-in update_lattice(): host arrays in, updated host arrays out."""
+        arrs = [fields.get(n) for n in FIELD_NAMES]
+        check(lib().su2gpu_update_lattice_host(self._h, sweep, *[_p(a) for a in arrs]))
+
+
+def stream_uniform(seed, site, pass_, draw, sweep, chain=0):
+    """The uniform the kernels draw (host evaluation of the Philox stream)."""
+    return lib().su2gpu_stream_uniform(seed, site, pass_, draw, sweep, chain)
+
+
+def device_info():
+    sm, ma, mi = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    fr = ctypes.c_int64()
+    check(lib().su2gpu_device_info(ctypes.byref(sm), ctypes.byref(ma), ctypes.byref(mi), ctypes.byref(fr)))
+    return dict(sm_count=sm.value, cc=(ma.value, mi.value), free_bytes=fr.value)

@@ -57,7 +57,8 @@ def fields_dict(f, prefix):
 
 
 def param_dict(p):
-    return {"p_" + name: np.array(getattr(p, name) if name != "L" else list(p.L)) for name, _ in abi.Params._fields_}
+    return {"p_" + name: np.array(getattr(p, name) if name != "L" else list(p.L)) for name, _ in abi.Params._fields_
+            if name != "reserved"}
 
 
 def gen_layout():

@@ -21,6 +21,8 @@ def names(prefix):
 def params_of(d):
     p = abi.Params()
     for name, _ in abi.Params._fields_:
+        if name == "reserved":
+            continue
         v = d["p_" + name]
         if name == "L":
             for k, x in enumerate(v):
