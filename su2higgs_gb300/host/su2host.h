@@ -1,0 +1,69 @@
+/* su2host.h -- the C host of bin/su2: config reader, lattice/weight files,
+ * labels/measure writers.  Mirrors the reference's host-side behaviour
+ * (parameters.c, checkpoint.c, multicanonical.c file I/O, measure.c output)
+ * so that `bin/su2 config` is a drop-in for the reference binary; all field
+ * updates and volume sums run on the GPU through libsu2gpu. */
+#ifndef SU2HOST_H
+#define SU2HOST_H
+
+#include <stdint.h>
+#include <stdio.h>
+
+#include "../../include/su2gpu.h"
+
+/* run settings read from the config (params, parameters.c:157-338) */
+typedef struct {
+  su2gpu_params p;
+  int nhiggs, triplet, singlet, u1, gradflow;
+  int reset;
+  long iterations, checkpoint, n_thermalize, interval;
+  char resultsfile[200];
+  char latticefile[200];
+  int run_checks, do_local_meas, multicanonical;
+  double phi0, sigma0, singlet0;
+  /* gradient flow */
+  int do_flow, flow_interval, flow_meas_interval;
+  double flow_dt, flow_t_max;
+  /* additions of this implementation (optional keys) */
+  uint64_t seed;
+  int have_seed;
+  int use_graph;
+} host_params;
+
+/* multicanonical settings (get_weight_parameters, parameters.c:344-402) */
+typedef struct {
+  char weightfile[200];
+  int mode, checks_per_sweep, bins, orderparam;
+  double min, max, delta;
+} host_muca;
+
+/* config.c */
+int cfg_open(const char* fname, FILE** f);
+int cfg_find(FILE* f, const char* label, char* result); /* 1 found, 0 not */
+int cfg_get_int(FILE* f, const char* label);
+long cfg_get_long(FILE* f, const char* label);
+double cfg_get_double(FILE* f, const char* label);
+void cfg_get_string(FILE* f, const char* label, char* result);
+int cfg_get_algorithm(FILE* f, const char* label);
+int cfg_optional_string(const char* fname, const char* label, char* result);
+void read_parameters(const char* fname, host_params* hp);
+void read_weight_parameters(const char* fname, const host_params* hp, host_muca* hm);
+void read_updated_parameters(const char* fname, host_params* hp);
+void print_parameters(const host_params* hp);
+void die(int code);
+
+/* files.c */
+int64_t field_count(const host_params* hp, int which); /* doubles per field array */
+int save_lattice(const char* fname, const host_params* hp, long iter, double total_time, double comms_time,
+                 double* const* arrays);
+int load_lattice(const char* fname, const host_params* hp, long* iter, double* total_time, double* comms_time,
+                 double** arrays);
+void print_labels(const host_params* hp);
+void write_measure_row(FILE* f, const host_params* hp, const double* sums, const su2gpu_weight* w, int have_muca);
+int load_weight(su2gpu_weight* w, host_muca* hm);
+void save_weight(const su2gpu_weight* w);
+void linearize_weight(su2gpu_weight* w);
+double get_weight(const su2gpu_weight* w, double val);
+void print_acceptance(const host_params* hp, const int64_t* c);
+
+#endif
