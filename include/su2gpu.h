@@ -218,6 +218,25 @@ int su2gpu_muca_weight_updates(su2gpu_ctx* ctx, int32_t* n);
 double su2gpu_stream_uniform(uint64_t seed, uint32_t site, uint32_t pass, uint32_t draw, uint32_t sweep,
                              uint32_t chain);
 
+/* ---- execution control (asynchronous use, profiling) ---- */
+/* Run on the caller's CUDA stream (a cudaStream_t passed as void*; NULL
+ * returns to the context's own stream).  Graphs are still captured on the
+ * context's own stream and launched on this one. */
+int su2gpu_set_stream(su2gpu_ctx* ctx, void* cuda_stream);
+/* su2gpu_run_sweeps without the final synchronisation. */
+int su2gpu_enqueue_sweeps(su2gpu_ctx* ctx, uint32_t first_sweep, int32_t nsweeps, int32_t use_graph);
+/* su2gpu_measure into a device buffer of SU2GPU_NMEAS doubles, no synchronisation. */
+int su2gpu_enqueue_measure(su2gpu_ctx* ctx, double* device_sums);
+/* Kernel launches of one sweep (nodes of its graph). */
+int su2gpu_launches_per_sweep(su2gpu_ctx* ctx, int32_t* n);
+/* One sweep with CUDA events around every pass: kinds[k] = 0 link, 1 U(1),
+ * 2 doublet, 3 triplet, 4 singlet, 5 reunitarisation; ms[k] its duration. */
+int su2gpu_profile_sweep(su2gpu_ctx* ctx, uint32_t sweep, int32_t max_passes, int32_t* kinds, float* ms,
+                         int32_t* npasses);
+/* Page-lock host memory for the host-buffer entry points. */
+int su2gpu_host_register(void* ptr, int64_t bytes);
+int su2gpu_host_unregister(void* ptr);
+
 /* Last CUDA / kernel error as text. */
 const char* su2gpu_last_error(void);
 

@@ -98,7 +98,11 @@ struct su2gpu_ctx {
   Coup cp;
   const Ops* ops;
   const PrecOps* pops;
-  cudaStream_t st = nullptr;
+  cudaStream_t st = nullptr;      // execution stream (the caller's, or own_st)
+  cudaStream_t own_st = nullptr;  // the context's own stream; graphs are captured on it
+  int launches = 0;               // kernel launches enqueued by the last sweep
+  std::vector<cudaEvent_t>* prof = nullptr;  // per-pass events while profiling
+  std::vector<int>* prof_kind = nullptr;
   DevBuf fields, stage, ctrbuf, partials, sums, alpha, backup, muca, flow, rows;
   Fields<double> f64{};
   Fields<float> f32{};
@@ -248,11 +252,12 @@ int su2gpu_create(const su2gpu_params* p, su2gpu_ctx** out) {
   c->ops = pick_ops(c->prec, p->content);
   c->pops = c->prec == 64 ? &precops_f64 : &precops_f32;
   int rc;
-  if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&c->own_st, cudaStreamNonBlocking) != cudaSuccess) {
     set_err("cudaStreamCreate failed");
     delete c;
     return SU2GPU_ERR_CUDA;
   }
+  c->st = c->own_st;
   int64_t V = c->g.V;
   if ((rc = c->fields.ensure(field_bytes(p, V))) ||
       (rc = c->ctrbuf.ensure(4096)) ||
@@ -297,10 +302,11 @@ int su2gpu_create(const su2gpu_params* p, su2gpu_ctx** out) {
 int su2gpu_destroy(su2gpu_ctx* c) {
   if (!c) return SU2GPU_OK;
   if (c->st) cudaStreamSynchronize(c->st);
+  if (c->own_st) cudaStreamSynchronize(c->own_st);
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   c->fields.release(); c->stage.release(); c->ctrbuf.release(); c->partials.release(); c->sums.release();
   c->alpha.release(); c->backup.release(); c->muca.release(); c->flow.release(); c->rows.release();
-  if (c->st) cudaStreamDestroy(c->st);
+  if (c->own_st) cudaStreamDestroy(c->own_st);
   delete c;
   return SU2GPU_OK;
 }
@@ -389,6 +395,15 @@ double su2gpu_stream_uniform(uint64_t seed, uint32_t site, uint32_t pass, uint32
 // ---------------------------------------------------------------------------
 // one sweep: update_lattice (update.c:270-430), non-random order
 // ---------------------------------------------------------------------------
+static void mark(su2gpu_ctx* c, int kind) {
+  if (!c->prof) return;
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  cudaEventRecord(e, c->st);
+  c->prof->push_back(e);
+  c->prof_kind->push_back(kind);
+}
+
 static int scalar_pass(su2gpu_ctx* c, const PassArgs& base, int field, int h, int par, int metro, uint32_t pass,
                        int64_t* tot) {
   const int64_t N = c->g.half;
@@ -408,10 +423,12 @@ static int scalar_pass(su2gpu_ctx* c, const PassArgs& base, int field, int h, in
                  ((field == 0 && ((h == 0 && (op == SU2GPU_PHISQ || op == SU2GPU_PHI2MINUSSIGMA2)) ||
                                   (h == 1 && op == SU2GPU_PHI2SQ))) ||
                   (field == 1 && (op == SU2GPU_SIGMASQ || op == SU2GPU_PHI2MINUSSIGMA2)));
+  mark(c, 2 + field);
   if (!do_muca) {
     a.t_lo = 0;
     a.t_hi = N;
     c->ops->scalar(field, c->F(), a, nblk(N, BLOCK), c->st);
+    c->launches++;
     CKL();
     return SU2GPU_OK;
   }
@@ -440,11 +457,13 @@ static int scalar_pass(su2gpu_ctx* c, const PassArgs& base, int field, int h, in
     if (!fused) {
       np = nblk(N, BLOCK);
       c->pops->orderparam(c->F(), c->g, par, op, partials, np, c->st);
+      c->launches++;
       CKL();
     }
     launch_muca_decide(c->d_muca, partials, (int)np, vol, par, rk, pass, check++, c->d_ctr, c->st);
     CKL();
     c->pops->restore(field, c->F(), c->d_muca, c->backup.p, h, par * N + a.t_lo, par * N + a.t_hi, c->st);
+    c->launches += 3;
     CKL();
   }
   if (N % cps != 0) {
@@ -454,6 +473,7 @@ static int scalar_pass(su2gpu_ctx* c, const PassArgs& base, int field, int h, in
       a.t_hi = hi;
       a.partials = nullptr;
       c->ops->scalar(field, c->F(), a, nblk(hi - lo, BLOCK), c->st);
+      c->launches++;
       CKL();
     } else {
       // nothing left to update: a reject reverts the last block, whose
@@ -467,6 +487,7 @@ static int scalar_pass(su2gpu_ctx* c, const PassArgs& base, int field, int h, in
     launch_muca_decide(c->d_muca, partials, (int)np, vol, par, rk, pass, check++, c->d_ctr, c->st);
     CKL();
     c->pops->restore(field, c->F(), c->d_muca, c->backup.p, h, par * N + rlo, par * N + rhi, c->st);
+    c->launches += 3;
     CKL();
   }
   return SU2GPU_OK;
@@ -474,6 +495,7 @@ static int scalar_pass(su2gpu_ctx* c, const PassArgs& base, int field, int h, in
 
 static int enqueue_sweep(su2gpu_ctx* c, int64_t* tot) {
   const su2gpu_params& p = c->p;
+  c->launches = 0;
   const int64_t N = c->g.half;
   PassArgs base;
   memset(&base, 0, sizeof(base));
@@ -489,7 +511,9 @@ static int enqueue_sweep(su2gpu_ctx* c, int64_t* tot) {
       for (int par = 0; par <= 1; par++) {
         PassArgs a = base;
         a.parity = par; a.sub = mu; a.alg = p.algorithm_su2link; a.pass = pass++; a.t_lo = 0; a.t_hi = N;
+        mark(c, 0);
         c->ops->link(c->F(), a, nblk(N, BLOCK), c->st);
+        c->launches++;
         CKL();
         tot[SU2GPU_C_TOTAL_SU2LINK] += N;
       }
@@ -498,7 +522,9 @@ static int enqueue_sweep(su2gpu_ctx* c, int64_t* tot) {
         for (int par = 0; par <= 1; par++) {
           PassArgs a = base;
           a.parity = par; a.sub = mu; a.pass = pass++; a.t_lo = 0; a.t_hi = N;
+          mark(c, 1);
           c->ops->u1(c->F(), a, nblk(N, BLOCK), c->st);
+          c->launches++;
           CKL();
           tot[SU2GPU_C_TOTAL_U1LINK] += N;
         }
@@ -538,9 +564,12 @@ static int enqueue_sweep(su2gpu_ctx* c, int64_t* tot) {
       }
   }
   if (c->prec == 32 && p.reunitarize_interval > 0) {
+    mark(c, 5);
     c->pops->reunitarize(c->F(), c->g.V, c->d_sweep, p.reunitarize_interval, c->st);
+    c->launches++;
     CKL();
   }
+  mark(c, -1);
   return SU2GPU_OK;
 }
 
@@ -565,24 +594,28 @@ int su2gpu_update_lattice(su2gpu_ctx* c, uint32_t sweep) {
   return SU2GPU_OK;
 }
 
-int su2gpu_run_sweeps(su2gpu_ctx* c, uint32_t first_sweep, int32_t nsweeps, int32_t use_graph) {
-  if (!c || nsweeps < 0) return SU2GPU_ERR_INVALID;
+static int enqueue_sweeps(su2gpu_ctx* c, uint32_t first_sweep, int32_t nsweeps, int32_t use_graph) {
   k_set_u32<<<1, 1, 0, c->st>>>(c->d_sweep, first_sweep);
   CKL();
   if (use_graph) {
     if (!c->gexec) {
       int64_t tot[SU2GPU_NCOUNTERS] = {0};
       cudaGraph_t graph;
+      cudaStream_t exec = c->st;
+      CK(cudaStreamSynchronize(exec));
+      c->st = c->own_st;
       CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
       int rc = enqueue_sweep(c, tot);
       k_inc_u32<<<1, 1, 0, c->st>>>(c->d_sweep);
       cudaError_t e = cudaStreamEndCapture(c->st, &graph);
+      c->st = exec;
       if (rc) return rc;
       if (e != cudaSuccess) { set_err("graph capture: %s", cudaGetErrorString(e)); return SU2GPU_ERR_CUDA; }
       e = cudaGraphInstantiate(&c->gexec, graph, 0);
       cudaGraphDestroy(graph);
       if (e != cudaSuccess) { set_err("graph instantiate: %s", cudaGetErrorString(e)); return SU2GPU_ERR_CUDA; }
       memcpy(c->graph_tot, tot, sizeof(tot));
+      c->launches += 1;
     }
     for (int s = 0; s < nsweeps; s++) {
       CK(cudaGraphLaunch(c->gexec, c->st));
@@ -596,7 +629,84 @@ int su2gpu_run_sweeps(su2gpu_ctx* c, uint32_t first_sweep, int32_t nsweeps, int3
       CKL();
     }
   }
+  return SU2GPU_OK;
+}
+
+int su2gpu_run_sweeps(su2gpu_ctx* c, uint32_t first_sweep, int32_t nsweeps, int32_t use_graph) {
+  if (!c || nsweeps < 0) return SU2GPU_ERR_INVALID;
+  int rc = enqueue_sweeps(c, first_sweep, nsweeps, use_graph);
+  if (rc) return rc;
   CK(cudaStreamSynchronize(c->st));
+  return SU2GPU_OK;
+}
+
+int su2gpu_enqueue_sweeps(su2gpu_ctx* c, uint32_t first_sweep, int32_t nsweeps, int32_t use_graph) {
+  if (!c || nsweeps < 0) return SU2GPU_ERR_INVALID;
+  return enqueue_sweeps(c, first_sweep, nsweeps, use_graph);
+}
+
+int su2gpu_set_stream(su2gpu_ctx* c, void* stream) {
+  if (!c) return SU2GPU_ERR_INVALID;
+  CK(cudaStreamSynchronize(c->st));
+  c->st = stream ? (cudaStream_t)stream : c->own_st;
+  return SU2GPU_OK;
+}
+
+int su2gpu_launches_per_sweep(su2gpu_ctx* c, int32_t* n) {
+  if (!c || !n) return SU2GPU_ERR_INVALID;
+  int64_t tot[SU2GPU_NCOUNTERS] = {0};
+  // count by enqueueing nothing: replay the bookkeeping of one sweep on a
+  // capture that is discarded
+  cudaGraph_t graph;
+  cudaStream_t exec = c->st;
+  CK(cudaStreamSynchronize(exec));
+  c->st = c->own_st;
+  CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_sweep(c, tot);
+  cudaError_t e = cudaStreamEndCapture(c->st, &graph);
+  c->st = exec;
+  if (rc) return rc;
+  if (e != cudaSuccess) { set_err("capture: %s", cudaGetErrorString(e)); return SU2GPU_ERR_CUDA; }
+  size_t nodes = 0;
+  cudaGraphGetNodes(graph, nullptr, &nodes);
+  cudaGraphDestroy(graph);
+  *n = (int32_t)nodes;
+  return SU2GPU_OK;
+}
+
+// one sweep with an event before every pass: kinds[k] (0 link, 1 U(1),
+// 2 doublet, 3 triplet, 4 singlet, 5 reunitarisation) and its duration ms[k]
+int su2gpu_profile_sweep(su2gpu_ctx* c, uint32_t sweep, int32_t maxp, int32_t* kinds, float* ms, int32_t* npasses) {
+  if (!c || !kinds || !ms || !npasses) return SU2GPU_ERR_INVALID;
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> kd;
+  k_set_u32<<<1, 1, 0, c->st>>>(c->d_sweep, sweep);
+  c->prof = &ev;
+  c->prof_kind = &kd;
+  int rc = enqueue_sweep(c, c->host_tot);
+  c->prof = nullptr;
+  c->prof_kind = nullptr;
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->st));
+  int n = 0;
+  for (size_t k = 0; k + 1 < ev.size() && n < maxp; k++, n++) {
+    kinds[n] = kd[k];
+    cudaEventElapsedTime(&ms[n], ev[k], ev[k + 1]);
+  }
+  for (cudaEvent_t e : ev) cudaEventDestroy(e);
+  *npasses = n;
+  return SU2GPU_OK;
+}
+
+int su2gpu_host_register(void* p, int64_t bytes) {
+  if (!p || bytes <= 0) return SU2GPU_ERR_INVALID;
+  CK(cudaHostRegister(p, (size_t)bytes, cudaHostRegisterDefault));
+  return SU2GPU_OK;
+}
+
+int su2gpu_host_unregister(void* p) {
+  if (!p) return SU2GPU_ERR_INVALID;
+  CK(cudaHostUnregister(p));
   return SU2GPU_OK;
 }
 
@@ -634,6 +744,11 @@ static int enqueue_measure(su2gpu_ctx* c, const void* F, const Coup& cp, double*
   launch_reduce_partials((const double*)c->partials.p, (int)nb, out, c->st);
   CKL();
   return SU2GPU_OK;
+}
+
+int su2gpu_enqueue_measure(su2gpu_ctx* c, double* dev_sums) {
+  if (!c || !dev_sums) return SU2GPU_ERR_INVALID;
+  return enqueue_measure(c, c->F(), c->cp, dev_sums);
 }
 
 int su2gpu_measure(su2gpu_ctx* c, double* sums) {

@@ -59,6 +59,13 @@ def lib():
         L.su2gpu_stream_uniform.restype = ctypes.c_double
         L.su2gpu_stream_uniform.argtypes = [u64, u32, u32, u32, u32, u32]
         L.su2gpu_device_info.argtypes = [ctypes.POINTER(ctypes.c_int)] * 3 + [ctypes.POINTER(i64)]
+        L.su2gpu_set_stream.argtypes = [vp, vp]
+        L.su2gpu_enqueue_sweeps.argtypes = [vp, u32, i32, i32]
+        L.su2gpu_enqueue_measure.argtypes = [vp, vp]
+        L.su2gpu_launches_per_sweep.argtypes = [vp, ctypes.POINTER(i32)]
+        L.su2gpu_profile_sweep.argtypes = [vp, u32, i32, vp, vp, ctypes.POINTER(i32)]
+        L.su2gpu_host_register.argtypes = [vp, i64]
+        L.su2gpu_host_unregister.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -183,6 +190,29 @@ class Lattice:
         check(lib().su2gpu_grad_flow(self._h, t_max, dt, meas_interval, _p(rows), maxrows, ctypes.byref(n)))
         return rows[: n.value].copy()
 
+    def set_stream(self, stream_ptr):
+        """Run on a caller's CUDA stream (an int cudaStream_t, e.g.
+        torch.cuda.current_stream().cuda_stream); 0/None = own stream."""
+        check(lib().su2gpu_set_stream(self._h, ctypes.c_void_p(stream_ptr or None)))
+
+    def enqueue_sweeps(self, first_sweep, n, graph=True):
+        check(lib().su2gpu_enqueue_sweeps(self._h, first_sweep, n, 1 if graph else 0))
+
+    def enqueue_measure(self, device_ptr):
+        check(lib().su2gpu_enqueue_measure(self._h, ctypes.c_void_p(device_ptr)))
+
+    def launches_per_sweep(self):
+        n = ctypes.c_int32(0)
+        check(lib().su2gpu_launches_per_sweep(self._h, ctypes.byref(n)))
+        return n.value
+
+    def profile_sweep(self, sweep, maxp=4096):
+        kinds = np.zeros(maxp, np.int32)
+        ms = np.zeros(maxp, np.float32)
+        n = ctypes.c_int32(0)
+        check(lib().su2gpu_profile_sweep(self._h, sweep, maxp, _p(kinds), _p(ms), ctypes.byref(n)))
+        return kinds[: n.value].copy(), ms[: n.value].astype(np.float64)
+
     def update_lattice_host(self, sweep, fields):
         """Drop-in update_lattice(): host arrays in, updated host arrays out."""
         arrs = [fields.get(n) for n in FIELD_NAMES]
@@ -192,6 +222,15 @@ class Lattice:
 def stream_uniform(seed, site, pass_, draw, sweep, chain=0):
     """The uniform the kernels draw (host evaluation of the Philox stream)."""
     return lib().su2gpu_stream_uniform(seed, site, pass_, draw, sweep, chain)
+
+
+def host_register(arr):
+    """Page-lock a numpy array for the host-buffer entry points."""
+    check(lib().su2gpu_host_register(_p(arr), arr.nbytes))
+
+
+def host_unregister(arr):
+    check(lib().su2gpu_host_unregister(_p(arr)))
 
 
 def device_info():
