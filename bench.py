@@ -47,6 +47,7 @@ WORKLOADS = {
     "fund64_f32": ("fund", (64, 64, 64), 32),
     "fund64_f64": ("fund", (64, 64, 64), 64),
     "fund16_f64": ("fund", (16, 16, 16), 64),
+    "fund160_f32": ("fund", (160, 160, 160), 32),
 }
 
 # Compulsory device traffic per lattice site, in reals, for one launch of each
