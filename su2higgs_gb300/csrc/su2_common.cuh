@@ -25,38 +25,42 @@ enum : int { ALG_METRO = 1, ALG_HEATBATH = 2, ALG_OR = 3 };
 // ---------------------------------------------------------------------------
 struct Geom {
   int L[3];
-  int hL0;        // L0 / 2
-  int64_t V;      // sites
-  int64_t half;   // sites per parity
+  int hL0;   // L0 / 2
+  int V;     // sites (< 2^31)
+  int half;  // sites per parity
 };
 
-__host__ __device__ inline int64_t site_index(const Geom& g, int x, int y, int z) {
-  int64_t n = (int64_t)x + (int64_t)g.L[0] * ((int64_t)y + (int64_t)g.L[1] * z);
-  return (int64_t)((x + y + z) & 1) * g.half + (n >> 1);
+__host__ __device__ inline int site_index(const Geom& g, int x, int y, int z) {
+  int n = x + g.L[0] * (y + g.L[1] * z);
+  return ((x + y + z) & 1) * g.half + (n >> 1);
 }
 
 // coordinates of the t-th site of a parity
-__host__ __device__ inline void site_coords(const Geom& g, int parity, int64_t t, int* c) {
-  int64_t r = t / g.hL0;
-  int k = (int)(t - r * g.hL0);
-  int y = (int)(r % g.L[1]);
-  int z = (int)(r / g.L[1]);
-  c[0] = 2 * k + ((parity + y + z) & 1);
+__host__ __device__ inline void site_coords(const Geom& g, int parity, int t, int* c) {
+  unsigned r = (unsigned)t / (unsigned)g.hL0;
+  int k = t - (int)r * g.hL0;
+  unsigned z = r / (unsigned)g.L[1];
+  int y = (int)(r - z * (unsigned)g.L[1]);
+  c[0] = 2 * k + ((parity + y + (int)z) & 1);
   c[1] = y;
-  c[2] = z;
+  c[2] = (int)z;
 }
 
-// index of the site at c + s1*e_d1 + s2*e_d2 (periodic)
-__host__ __device__ inline int64_t shifted(const Geom& g, const int* c, int d1, int s1, int d2 = 0, int s2 = 0) {
-  int x[3] = {c[0], c[1], c[2]};
-  x[d1] += s1;
-  x[d2] += s2;
-#pragma unroll
-  for (int d = 0; d < 3; d++) {
-    if (x[d] >= g.L[d]) x[d] -= g.L[d];
-    if (x[d] < 0) x[d] += g.L[d];
-  }
-  return site_index(g, x[0], x[1], x[2]);
+__host__ __device__ inline int wrap(int v, int L) { return v >= L ? v - L : (v < 0 ? v + L : v); }
+
+// index of the site at c + s1*e_d1 + s2*e_d2 (periodic, |s| <= 1); written
+// with selects so that runtime directions never index an array
+__host__ __device__ inline int shifted(const Geom& g, const int* c, int d1, int s1, int d2 = 0, int s2 = 0) {
+  int x = wrap(c[0] + (d1 == 0 ? s1 : 0) + (d2 == 0 ? s2 : 0), g.L[0]);
+  int y = wrap(c[1] + (d1 == 1 ? s1 : 0) + (d2 == 1 ? s2 : 0), g.L[1]);
+  int z = wrap(c[2] + (d1 == 2 ? s1 : 0) + (d2 == 2 ? s2 : 0), g.L[2]);
+  return site_index(g, x, y, z);
+}
+// coordinates of c + s*e_d
+__host__ __device__ inline void shift_coords(const Geom& g, const int* c, int d, int s, int* o) {
+  o[0] = wrap(c[0] + (d == 0 ? s : 0), g.L[0]);
+  o[1] = wrap(c[1] + (d == 1 ? s : 0), g.L[1]);
+  o[2] = wrap(c[2] + (d == 2 ? s : 0), g.L[2]);
 }
 
 // ---------------------------------------------------------------------------
@@ -149,6 +153,10 @@ __device__ inline double mexp(double x) { return exp(x); }
 __device__ inline float mexp(float x) { return expf(x); }
 __device__ inline double mcos(double x) { return cos(x); }
 __device__ inline float mcos(float x) { return cosf(x); }
+// cos(2 pi u) for u in [0,1): FP64 keeps the reference's cos(2*M_PI*u)
+// (heatbath.c:56); FP32 uses cospi, which needs no argument reduction
+__device__ inline double mcos2pi(double u) { return cos(2 * 3.14159265358979323846 * u); }
+__device__ inline float mcos2pi(float u) { return cospif(2.0f * u); }
 __device__ inline double msin(double x) { return sin(x); }
 __device__ inline float msin(float x) { return sinf(x); }
 __device__ inline double mcbrt(double x) { return cbrt(x); }
@@ -175,12 +183,12 @@ struct Q {
 };
 
 template <typename R>
-__device__ inline Q<R> ld4(const V4<R>* p, int64_t i) {
+__device__ inline Q<R> ld4(const V4<R>* p, int i) {
   V4<R> v = p[i];
   return Q<R>{v.x, v.y, v.z, v.w};
 }
 template <typename R>
-__device__ inline void st4(V4<R>* p, int64_t i, const Q<R>& q) {
+__device__ inline void st4(V4<R>* p, int i, const Q<R>& q) {
   V4<R> v;
   v.x = q.a;
   v.y = q.b;
@@ -254,12 +262,26 @@ struct Fields {
   R* sing;
 };
 
+// field pointers by a runtime direction / doublet index, chosen with selects
 template <typename R>
-__device__ inline V3<R> ld3(const Fields<R>& f, int64_t i) {
+__device__ inline V4<R>* lk(const Fields<R>& f, int d) {
+  return d == 0 ? f.link[0] : (d == 1 ? f.link[1] : f.link[2]);
+}
+template <typename R>
+__device__ inline R* a1p(const Fields<R>& f, int d) {
+  return d == 0 ? f.u1[0] : (d == 1 ? f.u1[1] : f.u1[2]);
+}
+template <typename R>
+__device__ inline V4<R>* php(const Fields<R>& f, int h) {
+  return h == 0 ? f.phi[0] : f.phi[1];
+}
+
+template <typename R>
+__device__ inline V3<R> ld3(const Fields<R>& f, int i) {
   return V3<R>{f.trip[0][i], f.trip[1][i], f.trip[2][i]};
 }
 template <typename R>
-__device__ inline void st3(const Fields<R>& f, int64_t i, const V3<R>& v) {
+__device__ inline void st3(const Fields<R>& f, int i, const V3<R>& v) {
   f.trip[0][i] = v.x;
   f.trip[1][i] = v.y;
   f.trip[2][i] = v.z;

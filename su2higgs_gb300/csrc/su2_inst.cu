@@ -73,7 +73,7 @@ void launch_muca_set_param(MucaDev* w, const double* partials, int np, double vo
   k_muca_set_param<<<1, 256, 0, st>>>(w, partials, np, vol, parity);
 }
 void launch_reduce_partials(const double* partials, int np, double* out, cudaStream_t st) {
-  k_reduce_partials<<<1, 256, 0, st>>>(partials, np, out);
+  k_reduce_partials<<<NSUMS, 256, 0, st>>>(partials, np, out);
 }
 #endif
 

@@ -18,6 +18,12 @@ namespace su2 {
 #define NHIGGS (HAS(C_H2) ? 2 : (HAS(C_H1) ? 1 : 0))
 
 constexpr int BLOCK = 128;
+// resident blocks per SM asked of the compiler: 8 x 128 threads caps FP32
+// kernels at 64 registers (half occupancy); FP64 ones at 128
+template <typename R>
+struct MinBlocks {
+  static constexpr int value = sizeof(R) == 4 ? 8 : 4;
+};
 constexpr int NSUMS = 24;
 
 // ---------------------------------------------------------------------------
@@ -52,18 +58,18 @@ __device__ inline double block_sum(double v) {
 // ---------------------------------------------------------------------------
 // su2staple_wilson (staples.c:84-115)
 template <typename R>
-__device__ inline Q<R> wilson_staple(const Fields<R>& f, const Geom& g, const int* c, int64_t i, int mu) {
+__device__ inline Q<R> wilson_staple(const Fields<R>& f, const Geom& g, const int* c, int i, int mu) {
   Q<R> tot{(R)0, (R)0, (R)0, (R)0};
-  int64_t xp = shifted(g, c, mu, 1);
+  int xp = shifted(g, c, mu, 1);
 #pragma unroll
   for (int nu = 0; nu < 3; nu++) {
     if (nu == mu) continue;
-    int64_t xn = shifted(g, c, nu, 1);
-    int64_t xpm = shifted(g, c, mu, 1, nu, -1);
-    int64_t xm = shifted(g, c, nu, -1);
-    Q<R> up = qmul(qmul(ld4<R>(f.link[nu], xp), qdag(ld4<R>(f.link[mu], xn))), qdag(ld4<R>(f.link[nu], i)));
+    int xn = shifted(g, c, nu, 1);
+    int xpm = shifted(g, c, mu, 1, nu, -1);
+    int xm = shifted(g, c, nu, -1);
+    Q<R> up = qmul(qmul(ld4<R>(lk(f, nu), xp), qdag(ld4<R>(lk(f, mu), xn))), qdag(ld4<R>(lk(f, nu), i)));
     tot = qadd(tot, up);
-    Q<R> lo = qmul(qmul(qdag(ld4<R>(f.link[nu], xpm)), qdag(ld4<R>(f.link[mu], xm))), ld4<R>(f.link[nu], xm));
+    Q<R> lo = qmul(qmul(qdag(ld4<R>(lk(f, nu), xpm)), qdag(ld4<R>(lk(f, mu), xm))), ld4<R>(lk(f, nu), xm));
     tot = qadd(tot, lo);
   }
   return tot;
@@ -71,7 +77,7 @@ __device__ inline Q<R> wilson_staple(const Fields<R>& f, const Geom& g, const in
 
 // hopping_triplet_forward (su2u1.c:605-617): -Sigma(x) . R(U_mu(x)) Sigma(x+mu)
 template <typename R>
-__device__ inline R hop_triplet_fwd_u(const Fields<R>& f, const Geom& g, const int* c, int64_t i, int mu,
+__device__ inline R hop_triplet_fwd_u(const Fields<R>& f, const Geom& g, const int* c, int i, int mu,
                                       const Q<R>& U) {
   V3<R> r = qrot(U, ld3(f, shifted(g, c, mu, 1)));
   return -dot3(ld3(f, i), r);
@@ -79,16 +85,16 @@ __device__ inline R hop_triplet_fwd_u(const Fields<R>& f, const Geom& g, const i
 
 // su2link_staple (staples.c:134-193)
 template <typename R, int CC>
-__device__ inline Q<R> link_staple(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+__device__ inline Q<R> link_staple(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
                                    int mu) {
   Q<R> V = qscale(wilson_staple(f, g, c, i, mu), (R)(-0.5 * cp.beta));
   const int nh = NHIGGS;
   if (nh > 0) {
-    int64_t xp = shifted(g, c, mu, 1);
+    int xp = shifted(g, c, mu, 1);
     for (int h = 0; h < nh; h++) {
-      Q<R> nphi = ld4<R>(f.phi[h], xp);
-      if (HAS(C_U1)) nphi = qmul(nphi, u1phase(f.u1[mu][i]));
-      Q<R> t = qmul(nphi, qdag(ld4<R>(f.phi[h], i)));
+      Q<R> nphi = ld4<R>(php(f, h), xp);
+      if (HAS(C_U1)) nphi = qmul(nphi, u1phase(a1p(f, mu)[i]));
+      Q<R> t = qmul(nphi, qdag(ld4<R>(php(f, h), i)));
       V.a -= (R)0.5 * t.a;
       V.b -= (R)0.5 * t.b;
       V.c -= (R)0.5 * t.c;
@@ -100,10 +106,10 @@ __device__ inline Q<R> link_staple(const Fields<R>& f, const Geom& g, const Coup
 
 // su2ptrace (su2u1.c:108-116) at site x (index i, coords c)
 template <typename R>
-__device__ inline R ptrace(const Fields<R>& f, const Geom& g, const int* c, int64_t i, int mu, int nu) {
-  Q<R> s = qmul(qmul(ld4<R>(f.link[mu], i), ld4<R>(f.link[nu], shifted(g, c, mu, 1))),
-                qdag(ld4<R>(f.link[mu], shifted(g, c, nu, 1))));
-  return (R)2 * qdot0(s, qdag(ld4<R>(f.link[nu], i)));
+__device__ inline R ptrace(const Fields<R>& f, const Geom& g, const int* c, int i, int mu, int nu) {
+  Q<R> s = qmul(qmul(ld4<R>(lk(f, mu), i), ld4<R>(lk(f, nu), shifted(g, c, mu, 1))),
+                qdag(ld4<R>(lk(f, mu), shifted(g, c, nu, 1))));
+  return (R)2 * qdot0(s, qdag(ld4<R>(lk(f, nu), i)));
 }
 
 // ---------------------------------------------------------------------------
@@ -126,22 +132,22 @@ __device__ inline R hop_trace(const Coup& cp, const Q<R>& p1, const Q<R>& u, con
   return qdot0(qdag(p1), t);
 }
 template <typename R, int CC>
-__device__ inline R hop_doublet_fwd(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+__device__ inline R hop_doublet_fwd(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
                                     int mu, int h) {
-  R al = HAS(C_U1) ? f.u1[mu][i] : (R)0;
-  return -hop_trace<R, CC>(cp, ld4<R>(f.phi[h], i), ld4<R>(f.link[mu], i), ld4<R>(f.phi[h], shifted(g, c, mu, 1)), al);
+  R al = HAS(C_U1) ? a1p(f, mu)[i] : (R)0;
+  return -hop_trace<R, CC>(cp, ld4<R>(php(f, h), i), ld4<R>(lk(f, mu), i), ld4<R>(php(f, h), shifted(g, c, mu, 1)), al);
 }
 template <typename R, int CC>
-__device__ inline R hop_doublet_bwd(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+__device__ inline R hop_doublet_bwd(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
                                     int mu, int h) {
-  int64_t pm = shifted(g, c, mu, -1);
-  R al = HAS(C_U1) ? f.u1[mu][pm] : (R)0;
-  return -hop_trace<R, CC>(cp, ld4<R>(f.phi[h], pm), ld4<R>(f.link[mu], pm), ld4<R>(f.phi[h], i), al);
+  int pm = shifted(g, c, mu, -1);
+  R al = HAS(C_U1) ? a1p(f, mu)[pm] : (R)0;
+  return -hop_trace<R, CC>(cp, ld4<R>(php(f, h), pm), ld4<R>(lk(f, mu), pm), ld4<R>(php(f, h), i), al);
 }
 template <typename R, int CC>
-__device__ inline R covariant_doublet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+__device__ inline R covariant_doublet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
                                       int h) {
-  R tot = 0, mod = doubletsq(ld4<R>(f.phi[h], i));
+  R tot = 0, mod = doubletsq(ld4<R>(php(f, h), i));
 #pragma unroll
   for (int d = 0; d < 3; d++) tot += (R)2 * mod + hop_doublet_fwd<R, CC>(f, g, cp, c, i, d, h);
   return tot;
@@ -149,12 +155,12 @@ __device__ inline R covariant_doublet(const Fields<R>& f, const Geom& g, const C
 
 // potential_singlet (su2u1.c:708-723)
 template <typename R, int CC>
-__device__ inline R potential_singlet(const Fields<R>& f, const Coup& cp, int64_t i) {
+__device__ inline R potential_singlet(const Fields<R>& f, const Coup& cp, int i) {
   R S = f.sing[i];
   R pot = (R)cp.b1s * S + (R)0.5 * (R)cp.msqs * S * S + (R)(1.0 / 3.0) * (R)cp.b3s * S * S * S +
           (R)0.25 * (R)cp.b4s * S * S * S * S;
   if (NHIGGS == 1) {
-    R mod = doubletsq(ld4<R>(f.phi[0], i));
+    R mod = doubletsq(ld4<R>(php(f, 0), i));
     pot += (R)0.5 * (R)cp.a1s * S * mod + (R)0.5 * (R)cp.a2s * S * S * mod;
   }
   return pot;
@@ -162,15 +168,15 @@ __device__ inline R potential_singlet(const Fields<R>& f, const Coup& cp, int64_
 
 // higgspotential (su2u1.c:528-572)
 template <typename R, int CC>
-__device__ inline R higgspotential(const Fields<R>& f, const Coup& cp, int64_t i) {
+__device__ inline R higgspotential(const Fields<R>& f, const Coup& cp, int i) {
   R pot = 0, mod = 0;
   const int nh = NHIGGS;
   if (nh > 0) {
-    Q<R> h1 = ld4<R>(f.phi[0], i);
+    Q<R> h1 = ld4<R>(php(f, 0), i);
     mod = doubletsq(h1);
     pot += (R)cp.msq * mod + (R)cp.lam * mod * mod;
     if (nh == 2) {
-      Q<R> h2 = ld4<R>(f.phi[1], i);
+      Q<R> h2 = ld4<R>(php(f, 1), i);
       R f11 = mod, f22 = doubletsq(h2);
       R Re = (R)0.5 * (h1.a * h2.a + h1.b * h2.b + h1.c * h2.c + h1.d * h2.d);
       R Im = (R)0.5 * (h1.d * h2.a + h1.c * h2.b - h1.b * h2.c - h1.a * h2.d);
@@ -191,7 +197,7 @@ __device__ inline R higgspotential(const Fields<R>& f, const Coup& cp, int64_t i
 
 // localact_doublet (su2u1.c:495-510)
 template <typename R, int CC>
-__device__ inline R localact_doublet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+__device__ inline R localact_doublet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
                                      int h) {
   R tot = covariant_doublet<R, CC>(f, g, cp, c, i, h);
 #pragma unroll
@@ -202,17 +208,17 @@ __device__ inline R localact_doublet(const Fields<R>& f, const Geom& g, const Co
 
 // staple_doublet (staples.c:243-302)
 template <typename R, int CC>
-__device__ inline Q<R> staple_doublet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+__device__ inline Q<R> staple_doublet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
                                       int h) {
   Q<R> res{(R)0, (R)0, (R)0, (R)0};
 #pragma unroll
   for (int d = 0; d < 3; d++) {
-    int64_t xp = shifted(g, c, d, 1), xm = shifted(g, c, d, -1);
-    Q<R> w = qmul(ld4<R>(f.link[d], i), ld4<R>(f.phi[h], xp));
-    if (HAS(C_U1)) w = qmul(w, u1phase(f.u1[d][i]));
+    int xp = shifted(g, c, d, 1), xm = shifted(g, c, d, -1);
+    Q<R> w = qmul(ld4<R>(lk(f, d), i), ld4<R>(php(f, h), xp));
+    if (HAS(C_U1)) w = qmul(w, u1phase(a1p(f, d)[i]));
     res.a -= w.a; res.b -= w.b; res.c -= w.c; res.d -= w.d;
-    w = qmul(qdag(ld4<R>(f.link[d], xm)), ld4<R>(f.phi[h], xm));
-    if (HAS(C_U1)) w = qmul(w, qdag(u1phase(f.u1[d][xm])));
+    w = qmul(qdag(ld4<R>(lk(f, d), xm)), ld4<R>(php(f, h), xm));
+    if (HAS(C_U1)) w = qmul(w, qdag(u1phase(a1p(f, d)[xm])));
     res.a -= w.a; res.b -= w.b; res.c -= w.c; res.d -= w.d;
   }
   return res;
@@ -222,18 +228,18 @@ __device__ inline Q<R> staple_doublet(const Fields<R>& f, const Geom& g, const C
 // triplet
 // ---------------------------------------------------------------------------
 template <typename R>
-__device__ inline R hop_triplet_fwd(const Fields<R>& f, const Geom& g, const int* c, int64_t i, int mu) {
-  return hop_triplet_fwd_u(f, g, c, i, mu, ld4<R>(f.link[mu], i));
+__device__ inline R hop_triplet_fwd(const Fields<R>& f, const Geom& g, const int* c, int i, int mu) {
+  return hop_triplet_fwd_u(f, g, c, i, mu, ld4<R>(lk(f, mu), i));
 }
 // hopping_triplet_backward (su2u1.c:623-637)
 template <typename R>
-__device__ inline R hop_triplet_bwd(const Fields<R>& f, const Geom& g, const int* c, int64_t i, int mu) {
-  int64_t pm = shifted(g, c, mu, -1);
-  V3<R> r = qrot(ld4<R>(f.link[mu], pm), ld3(f, i));
+__device__ inline R hop_triplet_bwd(const Fields<R>& f, const Geom& g, const int* c, int i, int mu) {
+  int pm = shifted(g, c, mu, -1);
+  V3<R> r = qrot(ld4<R>(lk(f, mu), pm), ld3(f, i));
   return -dot3(ld3(f, pm), r);
 }
 template <typename R>
-__device__ inline R covariant_triplet(const Fields<R>& f, const Geom& g, const int* c, int64_t i) {
+__device__ inline R covariant_triplet(const Fields<R>& f, const Geom& g, const int* c, int i) {
   R tot = 0, mod = tripletsq(ld3(f, i));
 #pragma unroll
   for (int d = 0; d < 3; d++) tot += (R)2 * mod + hop_triplet_fwd(f, g, c, i, d);
@@ -241,27 +247,27 @@ __device__ inline R covariant_triplet(const Fields<R>& f, const Geom& g, const i
 }
 // localact_triplet (su2u1.c:657-679)
 template <typename R, int CC>
-__device__ inline R localact_triplet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i) {
+__device__ inline R localact_triplet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i) {
   R tot = covariant_triplet(f, g, c, i);
 #pragma unroll
   for (int d = 0; d < 3; d++) tot += hop_triplet_bwd(f, g, c, i, d);
   R mod = tripletsq(ld3(f, i));
   tot += (R)cp.msqT * mod + (R)cp.b4 * mod * mod;
-  if (NHIGGS > 0) tot += (R)cp.a2 * doubletsq(ld4<R>(f.phi[0], i)) * mod;
+  if (NHIGGS > 0) tot += (R)cp.a2 * doubletsq(ld4<R>(php(f, 0), i)) * mod;
   return tot;
 }
 
 // localact_su2link (su2u1.c:166-198)
 template <typename R, int CC>
-__device__ inline R localact_su2link(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+__device__ inline R localact_su2link(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
                                      int mu) {
   R tot = 0;
 #pragma unroll
   for (int nu = 0; nu < 3; nu++) {
     if (nu == mu) continue;
     tot += ((R)1 - (R)0.5 * ptrace(f, g, c, i, mu, nu));
-    int cm[3] = {c[0], c[1], c[2]};
-    cm[nu] = cm[nu] == 0 ? g.L[nu] - 1 : cm[nu] - 1;
+    int cm[3];
+    shift_coords(g, c, nu, -1, cm);
     tot += ((R)1 - (R)0.5 * ptrace(f, g, cm, shifted(g, c, nu, -1), mu, nu));
   }
   tot *= (R)cp.beta;
@@ -274,12 +280,12 @@ __device__ inline R localact_su2link(const Fields<R>& f, const Geom& g, const Co
 // U(1)
 // ---------------------------------------------------------------------------
 template <typename R>
-__device__ inline R u1ptrace(const Fields<R>& f, const Geom& g, const int* c, int64_t i, int d1, int d2) {
-  return f.u1[d1][i] + f.u1[d2][shifted(g, c, d1, 1)] - f.u1[d1][shifted(g, c, d2, 1)] - f.u1[d2][i];
+__device__ inline R u1ptrace(const Fields<R>& f, const Geom& g, const int* c, int i, int d1, int d2) {
+  return a1p(f, d1)[i] + a1p(f, d2)[shifted(g, c, d1, 1)] - a1p(f, d1)[shifted(g, c, d2, 1)] - a1p(f, d2)[i];
 }
 // local_u1wilson (su2u1.c:316-328)
 template <typename R>
-__device__ inline R local_u1wilson(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i) {
+__device__ inline R local_u1wilson(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i) {
   R res = 0;
 #pragma unroll
   for (int d1 = 0; d1 < 3; d1++)
@@ -289,15 +295,15 @@ __device__ inline R local_u1wilson(const Fields<R>& f, const Geom& g, const Coup
 }
 // localact_u1link (su2u1.c:336-354)
 template <typename R, int CC>
-__device__ inline R localact_u1link(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+__device__ inline R localact_u1link(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
                                     int mu) {
   R tot = 0;
 #pragma unroll
   for (int nu = 0; nu < 3; nu++) {
     if (nu == mu) continue;
     tot += ((R)1 - mcos((R)cp.r_u1 * u1ptrace(f, g, c, i, mu, nu)));
-    int cm[3] = {c[0], c[1], c[2]};
-    cm[nu] = cm[nu] == 0 ? g.L[nu] - 1 : cm[nu] - 1;
+    int cm[3];
+    shift_coords(g, c, nu, -1, cm);
     tot += ((R)1 - mcos((R)cp.r_u1 * u1ptrace(f, g, cm, shifted(g, c, nu, -1), mu, nu)));
   }
   tot *= (R)cp.betau1;
@@ -343,12 +349,12 @@ __device__ inline R polysolve3(R a, R b, R c, R d, int* fallback) {
 // drawn in the reference's order (4 per trial, 3 per sphere trial, 1 for the
 // triplet accept/reject).
 template <typename R, int CC>
-__device__ inline int heatbath(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i, int mu,
+__device__ inline int heatbath(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i, int mu,
                                SiteRng<R>& rng, int* kpcap, int* err) {
   Q<R> old{};
   R oldact = 0;
   if (HAS(C_T)) {
-    old = ld4<R>(f.link[mu], i);
+    old = ld4<R>(lk(f, mu), i);
     oldact = hop_triplet_fwd_u(f, g, c, i, mu, old);
   }
   Q<R> V = link_staple<R, CC>(f, g, cp, c, i, mu);
@@ -357,11 +363,10 @@ __device__ inline int heatbath(const Fields<R>& f, const Geom& g, const Coup& cp
   a *= (R)2;
   R a0, r1, r2, r3, d;
   int loop = 1;
-  const R twopi = (R)(2 * 3.14159265358979323846);
   do {
     r1 = -mlog((R)1 - rng.uni()) / a;
     r2 = -mlog((R)1 - rng.uni()) / a;
-    r3 = mcos(twopi * rng.uni());
+    r3 = mcos2pi(rng.uni());
     r3 *= r3;
     d = r1 * r3 + r2;
     r3 = (R)1 - rng.uni();
@@ -393,15 +398,24 @@ __device__ inline int heatbath(const Fields<R>& f, const Geom& g, const Coup& cp
   }
   d = msqrt(d);
   Q<R> nl{a0, r1 * (rad / d), r2 * (rad / d), r3 * (rad / d)};
-  Q<R> U = qmul(nl, qdag(V));
-  st4<R>(f.link[mu], i, U);
+  Q<R> U = unitize(qmul(nl, qdag(V)));
+  st4<R>(lk(f, mu), i, U);
   if (HAS(C_T)) {
     R diff = oldact - hop_triplet_fwd_u(f, g, c, i, mu, U);
     if (rng.uni() < mexp(diff)) return 1;
-    st4<R>(f.link[mu], i, old);
+    st4<R>(lk(f, mu), i, old);
     return 0;
   }
   return 1;
+}
+
+// FP32 form: every link written is re-normalised to unit length, so rounding
+// never accumulates in the SU(2) constraint (the FP64 path writes the
+// reference's arithmetic unchanged)
+template <typename R>
+__device__ inline Q<R> unitize(const Q<R>& q) {
+  if (sizeof(R) == 8) return q;
+  return qscale(q, (R)rsqrtf((float)qsq(q)));
 }
 
 // Metropolis decision (metropolis.c:15-167)
@@ -414,9 +428,9 @@ __device__ inline int metro_accept(R diff, SiteRng<R>& rng) {
 
 // metro_su2link (metropolis.c:15-41) with random_su2link (init.c:43-58)
 template <typename R, int CC>
-__device__ inline int metro_link(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i, int mu,
+__device__ inline int metro_link(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i, int mu,
                                  SiteRng<R>& rng) {
-  Q<R> old = ld4<R>(f.link[mu], i);
+  Q<R> old = ld4<R>(lk(f, mu), i);
   R a0 = localact_su2link<R, CC>(f, g, cp, c, i, mu);
   Q<R> u;
   u.a = (R)10 * (rng.uni() - (R)0.5);
@@ -425,50 +439,50 @@ __device__ inline int metro_link(const Fields<R>& f, const Geom& g, const Coup& 
   u.d = (R)1 * (rng.uni() - (R)0.5);
   R n = msqrt(u.a * u.a + u.b * u.b + u.c * u.c + u.d * u.d);
   u = Q<R>{u.a / n, u.b / n, u.c / n, u.d / n};
-  st4<R>(f.link[mu], i, qmul(old, u));
+  st4<R>(lk(f, mu), i, unitize(qmul(old, u)));
   R a1 = localact_su2link<R, CC>(f, g, cp, c, i, mu);
   if (metro_accept(a1 - a0, rng)) return 1;
-  st4<R>(f.link[mu], i, old);
+  st4<R>(lk(f, mu), i, old);
   return 0;
 }
 
 // metro_u1link (metropolis.c:48-70)
 template <typename R, int CC>
-__device__ inline int metro_u1(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i, int mu,
+__device__ inline int metro_u1(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i, int mu,
                                SiteRng<R>& rng) {
-  R old = f.u1[mu][i];
+  R old = a1p(f, mu)[i];
   R a0 = localact_u1link<R, CC>(f, g, cp, c, i, mu);
-  f.u1[mu][i] = old + (R)0.95 * (rng.uni() - (R)0.5);
+  a1p(f, mu)[i] = old + (R)0.95 * (rng.uni() - (R)0.5);
   R a1 = localact_u1link<R, CC>(f, g, cp, c, i, mu);
   if (metro_accept(a1 - a0, rng)) return 1;
-  f.u1[mu][i] = old;
+  a1p(f, mu)[i] = old;
   return 0;
 }
 
 // metro_doublet (metropolis.c:77-106)
 template <typename R, int CC>
-__device__ inline int metro_doublet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+__device__ inline int metro_doublet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
                                     int h, SiteRng<R>& rng) {
-  Q<R> old = ld4<R>(f.phi[h], i);
+  Q<R> old = ld4<R>(php(f, h), i);
   R a0 = localact_doublet<R, CC>(f, g, cp, c, i, h);
   Q<R> nw = old;
   nw.a += (R)1 * (rng.uni() - (R)0.5);
   nw.b += (R)1 * (rng.uni() - (R)0.5);
   nw.c += (R)1 * (rng.uni() - (R)0.5);
   nw.d += (R)1 * (rng.uni() - (R)0.5);
-  st4<R>(f.phi[h], i, nw);
+  st4<R>(php(f, h), i, nw);
   R a1 = localact_doublet<R, CC>(f, g, cp, c, i, h);
   if (metro_accept(a1 - a0, rng)) return 1;
-  st4<R>(f.phi[h], i, old);
+  st4<R>(php(f, h), i, old);
   return 0;
 }
 
 // overrelax_doublet (overrelax.c:54-128)
 template <typename R, int CC>
-__device__ inline int overrelax_doublet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+__device__ inline int overrelax_doublet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
                                         SiteRng<R>& rng, int* fallback) {
   Q<R> s = staple_doublet<R, CC>(f, g, cp, c, i, 0);
-  Q<R> p = ld4<R>(f.phi[0], i);
+  Q<R> p = ld4<R>(php(f, 0), i);
   R F = msqrt(s.a * s.a + s.b * s.b + s.c * s.c + s.d * s.d);
   R X = (p.a * s.a + p.b * s.b + p.c * s.c + p.d * s.d) / F;
   R y0 = p.a - X * s.a / F, y1 = p.b - X * s.b / F, y2 = p.c - X * s.c / F, y3 = p.d - X * s.d / F;
@@ -486,7 +500,7 @@ __device__ inline int overrelax_doublet(const Fields<R>& f, const Geom& g, const
   R dVn = F + (R)2 * B * newX + (R)4 * C * (newX * newX * newX + Ysq * newX);
   if (mabs(dV / dVn) >= rng.uni()) {
     R k = (newX + X);
-    st4<R>(f.phi[0], i, Q<R>{-p.a + k * s.a / F, -p.b + k * s.b / F, -p.c + k * s.c / F, -p.d + k * s.d / F});
+    st4<R>(php(f, 0), i, Q<R>{-p.a + k * s.a / F, -p.b + k * s.b / F, -p.c + k * s.c / F, -p.d + k * s.d / F});
     return 1;
   }
   return 0;
@@ -494,20 +508,20 @@ __device__ inline int overrelax_doublet(const Fields<R>& f, const Geom& g, const
 
 // overrelax_higgs2 (overrelax.c:295-417)
 template <typename R, int CC>
-__device__ inline int overrelax_higgs2(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+__device__ inline int overrelax_higgs2(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
                                        int h, SiteRng<R>& rng, int* fallback) {
   Q<R> s = staple_doublet<R, CC>(f, g, cp, c, i, h);
-  Q<R> fv = ld4<R>(f.phi[h], i);
+  Q<R> fv = ld4<R>(php(f, h), i);
   Q<R> H;
   R l67re, l67im, lore, loim, lam12, msq;
   int sign;
   if (h == 0) {
-    H = ld4<R>(f.phi[1], i);
+    H = ld4<R>(php(f, 1), i);
     sign = -1;
     lam12 = cp.lam; msq = cp.msq;
     l67re = cp.lam7re; l67im = cp.lam7im; lore = cp.lam6re; loim = -cp.lam6im;
   } else {
-    H = ld4<R>(f.phi[0], i);
+    H = ld4<R>(php(f, 0), i);
     sign = 1;
     lam12 = cp.lam2; msq = cp.msq2;
     l67re = cp.lam6re; l67im = -cp.lam6im; lore = cp.lam7re; loim = cp.lam7im;
@@ -544,7 +558,7 @@ __device__ inline int overrelax_higgs2(const Fields<R>& f, const Geom& g, const 
   R dV = (R)4 * b4 * X * X * X + (R)3 * b3 * X * X + (R)2 * b2 * X + b1;
   R dVn = (R)4 * b4 * Xn * Xn * Xn + (R)3 * b3 * Xn * Xn + (R)2 * b2 * Xn + b1;
   if (mabs(dV / dVn) >= rng.uni()) {
-    st4<R>(f.phi[h], i, Q<R>{fr[0] + sv[0] * (Xn - X), fr[1] + sv[1] * (Xn - X), fr[2] + sv[2] * (Xn - X),
+    st4<R>(php(f, h), i, Q<R>{fr[0] + sv[0] * (Xn - X), fr[1] + sv[1] * (Xn - X), fr[2] + sv[2] * (Xn - X),
                              fr[3] + sv[3] * (Xn - X)});
     return 1;
   }
@@ -554,15 +568,15 @@ __device__ inline int overrelax_higgs2(const Fields<R>& f, const Geom& g, const 
 // overrelax_triplet (overrelax.c:137-236); no portal term in B (the
 // reference's "#ifdef HIGGS" there is never defined)
 template <typename R, int CC>
-__device__ inline int overrelax_triplet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+__device__ inline int overrelax_triplet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
                                         SiteRng<R>& rng, int* fallback) {
   V3<R> s{(R)0, (R)0, (R)0};
 #pragma unroll
   for (int d = 0; d < 3; d++) {
-    int64_t xp = shifted(g, c, d, 1), xm = shifted(g, c, d, -1);
-    V3<R> r = qrot(ld4<R>(f.link[d], i), ld3(f, xp));
+    int xp = shifted(g, c, d, 1), xm = shifted(g, c, d, -1);
+    V3<R> r = qrot(ld4<R>(lk(f, d), i), ld3(f, xp));
     s.x -= r.x; s.y -= r.y; s.z -= r.z;
-    r = qrot(qdag(ld4<R>(f.link[d], xm)), ld3(f, xm));
+    r = qrot(qdag(ld4<R>(lk(f, d), xm)), ld3(f, xm));
     s.x -= r.x; s.y -= r.y; s.z -= r.z;
   }
   V3<R> t = ld3(f, i);
@@ -586,7 +600,7 @@ __device__ inline int overrelax_triplet(const Fields<R>& f, const Geom& g, const
 
 // metro_triplet (metropolis.c:113-143)
 template <typename R, int CC>
-__device__ inline int metro_triplet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+__device__ inline int metro_triplet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
                                     SiteRng<R>& rng) {
   V3<R> old = ld3(f, i);
   R a0 = localact_triplet<R, CC>(f, g, cp, c, i);
@@ -603,7 +617,7 @@ __device__ inline int metro_triplet(const Fields<R>& f, const Geom& g, const Cou
 
 // localact_singlet (su2u1.c:688-705)
 template <typename R, int CC>
-__device__ inline R localact_singlet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i) {
+__device__ inline R localact_singlet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i) {
   R S = f.sing[i], res = (R)3 * S * S;
 #pragma unroll
   for (int d = 0; d < 3; d++) res -= S * (f.sing[shifted(g, c, d, 1)] + f.sing[shifted(g, c, d, -1)]);
@@ -613,7 +627,7 @@ __device__ inline R localact_singlet(const Fields<R>& f, const Geom& g, const Co
 
 // overrelax_singlet (overrelax.c:243-285)
 template <typename R, int CC>
-__device__ inline int overrelax_singlet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+__device__ inline int overrelax_singlet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
                                         SiteRng<R>& rng, int* fallback) {
   R S = f.sing[i];
   R c1 = (R)cp.b1s;
@@ -623,7 +637,7 @@ __device__ inline int overrelax_singlet(const Fields<R>& f, const Geom& g, const
   R c3 = (R)(1.0 / 3.0) * (R)cp.b3s;
   R c4 = (R)0.25 * (R)cp.b4s;
   if (NHIGGS == 1) {
-    R phisq = doubletsq(ld4<R>(f.phi[0], i));
+    R phisq = doubletsq(ld4<R>(php(f, 0), i));
     c1 += (R)0.5 * (R)cp.a1s * phisq;
     c2 += (R)0.5 * (R)cp.a2s * phisq;
   }
@@ -642,7 +656,7 @@ __device__ inline int overrelax_singlet(const Fields<R>& f, const Geom& g, const
 
 // metro_singlet (metropolis.c:148-167)
 template <typename R, int CC>
-__device__ inline int metro_singlet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i,
+__device__ inline int metro_singlet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
                                     SiteRng<R>& rng) {
   R old = f.sing[i];
   R a0 = localact_singlet<R, CC>(f, g, cp, c, i);
@@ -655,12 +669,12 @@ __device__ inline int metro_singlet(const Fields<R>& f, const Geom& g, const Cou
 
 // order-parameter contribution of one site (calc_orderparam, multicanonical.c:709-751)
 template <typename R>
-__device__ inline double orderparam_site(const Fields<R>& f, int op, int64_t i) {
+__device__ inline double orderparam_site(const Fields<R>& f, int op, int i) {
   switch (op) {
     case 2: return (double)tripletsq(ld3(f, i));
-    case 3: return (double)doubletsq(ld4<R>(f.phi[0], i)) - (double)tripletsq(ld3(f, i));
-    case 1: return (double)doubletsq(ld4<R>(f.phi[0], i));
-    case 4: return (double)doubletsq(ld4<R>(f.phi[1], i));
+    case 3: return (double)doubletsq(ld4<R>(php(f, 0), i)) - (double)tripletsq(ld3(f, i));
+    case 1: return (double)doubletsq(ld4<R>(php(f, 0), i));
+    case 4: return (double)doubletsq(ld4<R>(php(f, 1), i));
   }
   return 0.0;
 }
@@ -676,7 +690,7 @@ struct PassArgs {
   int sub;      // direction for links, doublet index for doublets
   int alg;      // algorithm (links) or forced Metropolis flag (scalars)
   uint32_t pass;
-  int64_t t_lo, t_hi;       // site range inside the parity
+  int t_lo, t_hi;       // site range inside the parity
   void* backup;             // multicanonical backup of the updated field (or null)
   int op;                   // order parameter to reduce (0: none)
   double* partials;         // per-block order-parameter sums (or null)
@@ -685,14 +699,14 @@ struct PassArgs {
 };
 
 template <typename R, int CC>
-__global__ void __launch_bounds__(BLOCK) k_link(Fields<R> f, PassArgs a) {
+__global__ void __launch_bounds__(BLOCK, MinBlocks<R>::value) k_link(Fields<R> f, PassArgs a) {
   const Coup& cp = a.cp;
-  int64_t t = a.t_lo + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int t = a.t_lo + (int)blockIdx.x * blockDim.x + threadIdx.x;
   int acc = 0, cap = 0, err = 0;
   if (t < a.t_hi) {
     int c[3];
     site_coords(a.g, a.parity, t, c);
-    int64_t i = a.parity * a.g.half + t;
+    int i = a.parity * a.g.half + t;
     SiteRng<R> rng(a.rk, *a.rk.sweep, (uint32_t)i, a.pass);
     if (a.alg == ALG_HEATBATH) acc = heatbath<R, CC>(f, a.g, cp, c, i, a.sub, rng, &cap, &err);
     else acc = metro_link<R, CC>(f, a.g, cp, c, i, a.sub, rng);
@@ -703,14 +717,14 @@ __global__ void __launch_bounds__(BLOCK) k_link(Fields<R> f, PassArgs a) {
 }
 
 template <typename R, int CC>
-__global__ void __launch_bounds__(BLOCK) k_u1(Fields<R> f, PassArgs a) {
+__global__ void __launch_bounds__(BLOCK, MinBlocks<R>::value) k_u1(Fields<R> f, PassArgs a) {
   const Coup& cp = a.cp;
-  int64_t t = a.t_lo + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int t = a.t_lo + (int)blockIdx.x * blockDim.x + threadIdx.x;
   int acc = 0;
   if (t < a.t_hi) {
     int c[3];
     site_coords(a.g, a.parity, t, c);
-    int64_t i = a.parity * a.g.half + t;
+    int i = a.parity * a.g.half + t;
     SiteRng<R> rng(a.rk, *a.rk.sweep, (uint32_t)i, a.pass);
     acc = metro_u1<R, CC>(f, a.g, cp, c, i, a.sub, rng);
   }
@@ -721,20 +735,20 @@ __global__ void __launch_bounds__(BLOCK) k_u1(Fields<R> f, PassArgs a) {
 // the singlet; optional multicanonical backup of the old values and block
 // sums of the order parameter over the new ones
 template <typename R, int CC, int FIELD>
-__global__ void __launch_bounds__(BLOCK) k_scalar(Fields<R> f, PassArgs a) {
+__global__ void __launch_bounds__(BLOCK, MinBlocks<R>::value) k_scalar(Fields<R> f, PassArgs a) {
   const Coup& cp = a.cp;
-  int64_t t = a.t_lo + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int t = a.t_lo + (int)blockIdx.x * blockDim.x + threadIdx.x;
   int acc = 0, fb = 0;
   double opv = 0.0;
   bool orr = false;
   if (t < a.t_hi) {
     int c[3];
     site_coords(a.g, a.parity, t, c);
-    int64_t i = a.parity * a.g.half + t;
+    int i = a.parity * a.g.half + t;
     SiteRng<R> rng(a.rk, *a.rk.sweep, (uint32_t)i, a.pass);
     if (FIELD == 0) {
       const int h = a.sub;
-      if (a.backup) ((V4<R>*)a.backup)[i] = f.phi[h][i];
+      if (a.backup) ((V4<R>*)a.backup)[i] = php(f, h)[i];
       orr = cp.alg_d == ALG_OR && !a.alg;
       if (orr) acc = NHIGGS == 2 ? overrelax_higgs2<R, CC>(f, a.g, cp, c, i, h, rng, &fb)
                                  : overrelax_doublet<R, CC>(f, a.g, cp, c, i, rng, &fb);
@@ -769,7 +783,7 @@ __global__ void __launch_bounds__(BLOCK) k_scalar(Fields<R> f, PassArgs a) {
 // order parameter of a whole parity (calc_orderparam)
 template <typename R>
 __global__ void __launch_bounds__(BLOCK) k_orderparam(Fields<R> f, Geom g, int parity, int op, double* partials) {
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int t = (int)blockIdx.x * blockDim.x + threadIdx.x;
   double v = 0.0;
   if (t < g.half) v = orderparam_site<R>(f, op, parity * g.half + t);
   double s = block_sum(v);
@@ -778,12 +792,12 @@ __global__ void __launch_bounds__(BLOCK) k_orderparam(Fields<R> f, Geom g, int p
 
 // restore a block of the parity from the backup if the last check rejected
 template <typename R, int FIELD>
-__global__ void k_muca_restore(Fields<R> f, const MucaDev* m, const void* backup, int h, int64_t lo, int64_t hi) {
+__global__ void k_muca_restore(Fields<R> f, const MucaDev* m, const void* backup, int h, int lo, int hi) {
   if (m->last_accept) return;
-  int64_t i = lo + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int i = lo + (int)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= hi) return;
   if (FIELD == 0) {
-    f.phi[h][i] = ((const V4<R>*)backup)[i];
+    php(f, h)[i] = ((const V4<R>*)backup)[i];
   } else {
     const R* b = (const R*)backup;
     f.trip[0][i] = b[3 * i]; f.trip[1][i] = b[3 * i + 1]; f.trip[2][i] = b[3 * i + 2];
@@ -1028,8 +1042,8 @@ __device__ inline CM<R> proj_mat(const V3<R>& a) {
   return P;
 }
 template <typename R>
-__device__ inline CM<R> project_u1(const Fields<R>& f, const Geom& g, const int* c, int64_t i, int d) {
-  Q<R> u = ld4<R>(f.link[d], i);
+__device__ inline CM<R> project_u1(const Fields<R>& f, const Geom& g, const int* c, int i, int d) {
+  Q<R> u = ld4<R>(lk(f, d), i);
   CM<R> U;
   U.re[0] = u.a; U.im[0] = u.d;
   U.re[1] = u.c; U.im[1] = u.b;
@@ -1039,11 +1053,11 @@ __device__ inline CM<R> project_u1(const Fields<R>& f, const Geom& g, const int*
 }
 // alpha_proj (magfield.c:189-216)
 template <typename R>
-__device__ inline R alpha_proj(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int64_t i, int d1,
+__device__ inline R alpha_proj(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i, int d1,
                                int d2) {
-  int c1[3] = {c[0], c[1], c[2]}, c2[3] = {c[0], c[1], c[2]};
-  c1[d1] = c1[d1] + 1 == g.L[d1] ? 0 : c1[d1] + 1;
-  c2[d2] = c2[d2] + 1 == g.L[d2] ? 0 : c2[d2] + 1;
+  int c1[3], c2[3];
+  shift_coords(g, c, d1, 1, c1);
+  shift_coords(g, c, d2, 1, c2);
   CM<R> u1 = project_u1(f, g, c, i, d1);
   CM<R> u2 = project_u1(f, g, c1, shifted(g, c, d1, 1), d2);
   CM<R> u3 = project_u1(f, g, c2, shifted(g, c, d2, 1), d1);
@@ -1056,10 +1070,10 @@ __device__ inline R alpha_proj(const Fields<R>& f, const Geom& g, const Coup& cp
 // alpha(x; 0,1), alpha(x; 0,2), alpha(x; 1,2) for every site
 template <typename R>
 __global__ void __launch_bounds__(BLOCK) k_alpha(Fields<R> f, Geom g, Coup cp, double* alpha) {
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int t = (int)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= g.V) return;
   int parity = t >= g.half;
-  int64_t tp = t - parity * g.half;
+  int tp = t - parity * g.half;
   int c[3];
   site_coords(g, parity, tp, c);
   alpha[t] = (double)alpha_proj(f, g, cp, c, t, 0, 1);
@@ -1067,17 +1081,36 @@ __global__ void __launch_bounds__(BLOCK) k_alpha(Fields<R> f, Geom g, Coup cp, d
   alpha[2 * g.V + t] = (double)alpha_proj(f, g, cp, c, t, 1, 2);
 }
 
-// per-site terms of measure() summed over the block into partials[block][NSUMS]
+// which of the NSUMS volume sums a content produces
+template <int CC>
+__device__ inline bool sum_active(int k, int rt) {
+  const bool h1 = SU2_HAS(CC, rt, C_H1), h2 = SU2_HAS(CC, rt, C_H2), t = SU2_HAS(CC, rt, C_T),
+             s = SU2_HAS(CC, rt, C_S), u = SU2_HAS(CC, rt, C_U1);
+  const int nh = h2 ? 2 : (h1 ? 1 : 0);
+  switch (k) {
+    case 0: case 1: return true;
+    case 2: return u;
+    case 3: case 4: case 5: return nh > 0;
+    case 6: case 7: case 8: case 9: case 10: return nh > 1;
+    case 11: case 12: case 13: case 15: case 16: return t;
+    case 14: return t && nh > 0;
+    case 17: case 18: case 19: case 20: case 21: return s;
+    case 22: case 23: return s && nh == 1;
+  }
+  return false;
+}
+
+// per-site terms of measure() summed over the block into partials[k][block]
 template <typename R, int CC>
 __global__ void __launch_bounds__(BLOCK) k_measure(Fields<R> f, Geom g, Coup cp, const double* alpha,
                                                    double* partials) {
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int t = (int)blockIdx.x * blockDim.x + threadIdx.x;
   double m[NSUMS];
 #pragma unroll
   for (int k = 0; k < NSUMS; k++) m[k] = 0.0;
   if (t < g.V) {
     int parity = t >= g.half;
-    int64_t i = t;
+    int i = t;
     int c[3];
     site_coords(g, parity, t - parity * g.half, c);
     // local_su2wilson (su2u1.c:143-157)
@@ -1096,7 +1129,7 @@ __global__ void __launch_bounds__(BLOCK) k_measure(Fields<R> f, Geom g, Coup cp,
     act += (double)higgspotential<R, CC>(f, cp, i);
     const int nh = NHIGGS;
     for (int h = 0; h < nh; h++) {
-      R mod = doubletsq(ld4<R>(f.phi[h], i));
+      R mod = doubletsq(ld4<R>(php(f, h), i));
       R cov = covariant_doublet<R, CC>(f, g, cp, c, i, h);
       act += (double)cov;
       m[3 + 3 * h] = (double)cov;
@@ -1108,7 +1141,7 @@ __global__ void __launch_bounds__(BLOCK) k_measure(Fields<R> f, Geom g, Coup cp,
       act += (double)covt;
       V3<R> tr = ld3(f, i);
       R tm = tripletsq(tr);
-      if (nh > 0) m[14] = (double)(doubletsq(ld4<R>(f.phi[0], i)) * tm);
+      if (nh > 0) m[14] = (double)(doubletsq(ld4<R>(php(f, 0), i)) * tm);
       m[12] = (double)tm;
       m[13] = (double)(tm * tm);
       R hs = 0;
@@ -1116,10 +1149,10 @@ __global__ void __launch_bounds__(BLOCK) k_measure(Fields<R> f, Geom g, Coup cp,
       for (int d = 0; d < 3; d++) hs += hop_triplet_fwd(f, g, c, i, d);
       m[11] = (double)hs;
       // magcharge_cube (magfield.c:262-280) from the alpha planes
-      const int64_t V = g.V;
+      const int V = g.V;
       double q = 0.0;
       {
-        int64_t n0 = shifted(g, c, 0, 1), n1 = shifted(g, c, 1, 1), n2 = shifted(g, c, 2, 1);
+        int n0 = shifted(g, c, 0, 1), n1 = shifted(g, c, 1, 1), n2 = shifted(g, c, 2, 1);
         double B1 = alpha[2 * V + i], B2 = alpha[2 * V + n0];
         q += B2 - B1;
         B1 = -alpha[V + i];
@@ -1133,7 +1166,7 @@ __global__ void __launch_bounds__(BLOCK) k_measure(Fields<R> f, Geom g, Coup cp,
       m[16] = fabs(q);
     }
     if (nh == 2) {
-      Q<R> h1 = ld4<R>(f.phi[0], i), h2 = ld4<R>(f.phi[1], i);
+      Q<R> h1 = ld4<R>(php(f, 0), i), h2 = ld4<R>(php(f, 1), i);
       m[9] = (double)((R)0.5 * (h1.a * h2.a + h1.b * h2.b + h1.c * h2.c + h1.d * h2.d));
       m[10] = (double)((R)0.5 * (h1.d * h2.a + h1.c * h2.b - h1.b * h2.c - h1.a * h2.d));
     }
@@ -1154,7 +1187,7 @@ __global__ void __launch_bounds__(BLOCK) k_measure(Fields<R> f, Geom g, Coup cp,
       m[20] = (double)(S * S * S);
       m[21] = (double)(S * S * S * S);
       if (nh == 1) {
-        R mod = doubletsq(ld4<R>(f.phi[0], i));
+        R mod = doubletsq(ld4<R>(php(f, 0), i));
         m[22] = (double)(mod * S);
         m[23] = (double)(mod * S * S);
       }
@@ -1165,6 +1198,7 @@ __global__ void __launch_bounds__(BLOCK) k_measure(Fields<R> f, Geom g, Coup cp,
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < NSUMS; k++) {
+    if (!sum_active<CC>(k, cp.content)) continue;
     double v = m[k];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -1173,30 +1207,28 @@ __global__ void __launch_bounds__(BLOCK) k_measure(Fields<R> f, Geom g, Coup cp,
   __syncthreads();
   if (threadIdx.x < NSUMS) {
     double v = 0.0;
+    if (sum_active<CC>(threadIdx.x, cp.content))
 #pragma unroll
-    for (int ww = 0; ww < BLOCK / 32; ww++) v += sm[ww][threadIdx.x];
-    partials[(int64_t)blockIdx.x * NSUMS + threadIdx.x] = v;
+      for (int ww = 0; ww < BLOCK / 32; ww++) v += sm[ww][threadIdx.x];
+    partials[threadIdx.x * gridDim.x + blockIdx.x] = v;
   }
 }
 
 #ifdef SU2_WITH_GLOBAL
-// fixed-order sum of partials[np][NSUMS] -> out[NSUMS]; one block of 256
+// fixed-order sum of partials[NSUMS][np] -> out[NSUMS]; one block per sum
 __global__ void k_reduce_partials(const double* partials, int np, double* out) {
   __shared__ double red[256];
-  for (int k = 0; k < NSUMS; k++) {
-    double v = 0.0;
-    for (int b = threadIdx.x; b < np; b += blockDim.x) v += partials[(int64_t)b * NSUMS + k];
-    red[threadIdx.x] = v;
-    __syncthreads();
-    for (int s = blockDim.x >> 1; s > 0; s >>= 1) {
-      if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) out[k] = red[0];
+  const double* row = partials + (size_t)blockIdx.x * np;
+  double v = 0.0;
+  for (int b = threadIdx.x; b < np; b += blockDim.x) v += row[b];
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int s = blockDim.x >> 1; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
     __syncthreads();
   }
+  if (threadIdx.x == 0) out[blockIdx.x] = red[0];
 }
-
 #endif  // SU2_WITH_GLOBAL
 
 // ---------------------------------------------------------------------------
@@ -1205,17 +1237,17 @@ __global__ void k_reduce_partials(const double* partials, int np, double* out) {
 template <typename R, int CC>
 __global__ void __launch_bounds__(BLOCK) k_flow(Fields<R> in, Fields<R> out, Geom g, Coup cp, R dt,
                                                 unsigned long long* first_zero) {
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int t = (int)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= g.V) return;
   int parity = t >= g.half;
-  int64_t i = t;
+  int i = t;
   int c[3];
   site_coords(g, parity, t - parity * g.half, c);
 #pragma unroll
   for (int mu = 0; mu < 3; mu++) {
     // grad_force_link (gradflow.c:190-258)
     Q<R> s = qscale(wilson_staple(in, g, c, i, mu), (R)(-cp.beta / 8.0));
-    Q<R> U = ld4<R>(in.link[mu], i);
+    Q<R> U = ld4<R>(lk(in, mu), i);
     if (HAS(C_T)) {
       V3<R> a1 = ld3(in, i), a2 = ld3(in, shifted(g, c, mu, 1));
       Q<R> r = qmul(qmul(Q<R>{(R)0, a2.x, a2.y, a2.z}, qdag(U)), Q<R>{(R)0, a1.x, a1.y, a1.z});
@@ -1236,29 +1268,29 @@ __global__ void __launch_bounds__(BLOCK) k_flow(Fields<R> in, Fields<R> out, Geo
     // flow_gauge (gradflow.c:361-401)
     if (mod <= (R)0) {
       atomicMin(first_zero, (unsigned long long)(i * 3 + mu));
-      st4<R>(out.link[mu], i, U);
+      st4<R>(lk(out, mu), i, U);
       continue;
     }
     mod = msqrt(mod);
     R sm = msin(mod);
     Q<R> u{mcos(mod), sm * z[0] / mod, sm * z[1] / mod, sm * z[2] / mod};
-    st4<R>(out.link[mu], i, qmul(u, U));
+    st4<R>(lk(out, mu), i, qmul(u, U));
   }
   if (HAS(C_T)) {
     // grad_force_triplet (gradflow.c:267-330) and flow_triplet (405-414)
     R res[3] = {0, 0, 0};
 #pragma unroll
     for (int d = 0; d < 3; d++) {
-      V3<R> r = qrot(ld4<R>(in.link[d], i), ld3(in, shifted(g, c, d, 1)));
+      V3<R> r = qrot(ld4<R>(lk(in, d), i), ld3(in, shifted(g, c, d, 1)));
       res[0] -= r.x; res[1] -= r.y; res[2] -= r.z;
-      int64_t xm = shifted(g, c, d, -1);
-      r = qrot(qdag(ld4<R>(in.link[d], xm)), ld3(in, xm));
+      int xm = shifted(g, c, d, -1);
+      r = qrot(qdag(ld4<R>(lk(in, d), xm)), ld3(in, xm));
       res[0] -= r.x; res[1] -= r.y; res[2] -= r.z;
     }
     V3<R> tr = ld3(in, i);
     R tv[3] = {tr.x, tr.y, tr.z};
     R ts = tripletsq(tr);
-    R hm = NHIGGS > 0 ? doubletsq(ld4<R>(in.phi[0], i)) : (R)0;
+    R hm = NHIGGS > 0 ? doubletsq(ld4<R>(php(in, 0), i)) : (R)0;
 #pragma unroll
     for (int a = 0; a < 3; a++) {
       res[a] += ((R)6 + (R)cp.msqT + (R)2 * (R)cp.b4 * ts) * tv[a];
@@ -1273,11 +1305,11 @@ __global__ void __launch_bounds__(BLOCK) k_flow(Fields<R> in, Fields<R> out, Geo
 template <typename R>
 __global__ void k_flow_fixup(Fields<R> in, Fields<R> out, Geom g, const unsigned long long* first_zero) {
   unsigned long long fz = *first_zero;
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int t = (int)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= g.V * 3 || (unsigned long long)t < fz) return;
-  int64_t i = t / 3;
+  int i = t / 3;
   int mu = (int)(t - i * 3);
-  out.link[mu][i] = in.link[mu][i];
+  lk(out, mu)[i] = lk(in, mu)[i];
 }
 
 // ---------------------------------------------------------------------------
@@ -1285,27 +1317,27 @@ __global__ void k_flow_fixup(Fields<R> in, Fields<R> out, Geom g, const unsigned
 // ---------------------------------------------------------------------------
 // host AoS FP64 (lattice-file order) <-> device SoA
 template <typename R>
-__global__ void k_import(Fields<R> f, int64_t V, int kind, int h, const double* src) {
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void k_import(Fields<R> f, int V, int kind, int h, const double* src) {
+  int t = (int)blockIdx.x * blockDim.x + threadIdx.x;
   switch (kind) {
     case 0:  // links [V][3][4]
       if (t < V * 3) {
-        int64_t i = t / 3;
+        int i = t / 3;
         int d = (int)(t - i * 3);
         const double* s = src + t * 4;
-        st4<R>(f.link[d], i, Q<R>{(R)s[0], (R)s[1], (R)s[2], (R)s[3]});
+        st4<R>(lk(f, d), i, Q<R>{(R)s[0], (R)s[1], (R)s[2], (R)s[3]});
       }
       break;
     case 1:  // u1 [V][3]
       if (t < V * 3) {
-        int64_t i = t / 3;
-        f.u1[t - i * 3][i] = (R)src[t];
+        int i = t / 3;
+        a1p(f, t - i * 3)[i] = (R)src[t];
       }
       break;
     case 2:  // doublet [V][4]
       if (t < V) {
         const double* s = src + t * 4;
-        st4<R>(f.phi[h], t, Q<R>{(R)s[0], (R)s[1], (R)s[2], (R)s[3]});
+        st4<R>(php(f, h), t, Q<R>{(R)s[0], (R)s[1], (R)s[2], (R)s[3]});
       }
       break;
     case 3:  // triplet [V][3]
@@ -1317,27 +1349,27 @@ __global__ void k_import(Fields<R> f, int64_t V, int kind, int h, const double* 
   }
 }
 template <typename R>
-__global__ void k_export(Fields<R> f, int64_t V, int kind, int h, double* dst) {
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void k_export(Fields<R> f, int V, int kind, int h, double* dst) {
+  int t = (int)blockIdx.x * blockDim.x + threadIdx.x;
   switch (kind) {
     case 0:
       if (t < V * 3) {
-        int64_t i = t / 3;
+        int i = t / 3;
         int d = (int)(t - i * 3);
-        Q<R> q = ld4<R>(f.link[d], i);
+        Q<R> q = ld4<R>(lk(f, d), i);
         double* s = dst + t * 4;
         s[0] = q.a; s[1] = q.b; s[2] = q.c; s[3] = q.d;
       }
       break;
     case 1:
       if (t < V * 3) {
-        int64_t i = t / 3;
-        dst[t] = f.u1[t - i * 3][i];
+        int i = t / 3;
+        dst[t] = a1p(f, t - i * 3)[i];
       }
       break;
     case 2:
       if (t < V) {
-        Q<R> q = ld4<R>(f.phi[h], t);
+        Q<R> q = ld4<R>(php(f, h), t);
         double* s = dst + t * 4;
         s[0] = q.a; s[1] = q.b; s[2] = q.c; s[3] = q.d;
       }
@@ -1356,15 +1388,15 @@ __global__ void k_export(Fields<R> f, int64_t V, int kind, int h, double* dst) {
 
 // renormalise every link to unit norm (FP32 form, every `interval` sweeps)
 template <typename R>
-__global__ void k_reunitarize(Fields<R> f, int64_t V, const uint32_t* sweep, int interval) {
+__global__ void k_reunitarize(Fields<R> f, int V, const uint32_t* sweep, int interval) {
   if (interval <= 0 || (*sweep % (uint32_t)interval) != (uint32_t)(interval - 1)) return;
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int t = (int)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= V * 3) return;
-  int64_t i = t / 3;
+  int i = t / 3;
   int d = (int)(t - i * 3);
-  Q<R> q = ld4<R>(f.link[d], i);
+  Q<R> q = ld4<R>(lk(f, d), i);
   R n = (R)1 / msqrt(qsq(q));
-  st4<R>(f.link[d], i, qscale(q, n));
+  st4<R>(lk(f, d), i, qscale(q, n));
 }
 
 #undef HAS

@@ -134,6 +134,7 @@ static int valid_params(const su2gpu_params* p) {
   if (p->dim != 3) { set_err("only dim 3 is supported on the GPU (got %d)", p->dim); return 0; }
   for (int d = 0; d < 3; d++)
     if (p->L[d] < 2 || (p->L[d] & 1)) { set_err("L%d = %d: side lengths must be even and >= 2", d + 1, p->L[d]); return 0; }
+  if ((double)p->L[0] * p->L[1] * p->L[2] * 3.0 >= 2147483647.0) { set_err("lattice too large (3 V must fit in 31 bits)"); return 0; }
   if (p->precision != 64 && p->precision != 32) { set_err("precision must be 64 or 32"); return 0; }
   int c = p->content;
   if ((c & SU2GPU_HIGGS1) && (c & SU2GPU_HIGGS2)) { set_err("HIGGS1 and HIGGS2 are exclusive"); return 0; }
@@ -563,12 +564,8 @@ static int enqueue_sweep(su2gpu_ctx* c, int64_t* tot) {
           if ((rc = scalar_pass(c, base, 2, 0, par, force, pass++, tot))) return rc;
       }
   }
-  if (c->prec == 32 && p.reunitarize_interval > 0) {
-    mark(c, 5);
-    c->pops->reunitarize(c->F(), c->g.V, c->d_sweep, p.reunitarize_interval, c->st);
-    c->launches++;
-    CKL();
-  }
+  // FP32: links are re-normalised where they are written (heatbath and
+  // Metropolis kernels), which subsumes a periodic re-unitarisation pass
   mark(c, -1);
   return SU2GPU_OK;
 }
