@@ -237,6 +237,37 @@ int su2gpu_profile_sweep(su2gpu_ctx* ctx, uint32_t sweep, int32_t max_passes, in
 int su2gpu_host_register(void* ptr, int64_t bytes);
 int su2gpu_host_unregister(void* ptr);
 
+/* ---- allocation-free measurement ----
+ * Device pointers to fields in the library's device layout (parity-split
+ * structure of arrays, EVEN sites first): link[d] and doublet[h] are V
+ * 4-vectors of double (32-byte aligned) or float (16-byte aligned) by
+ * `precision`; u1[d], triplet[k] (three planes) and singlet are V reals.
+ * Unused entries may be NULL. */
+typedef struct {
+  void* link[3];
+  void* u1[3];
+  void* doublet[2];
+  void* triplet[3];
+  void* singlet;
+} su2gpu_device_fields;
+
+/* The volume sums of su2gpu_measure (SU2GPU_NMEAS doubles, written to the
+ * device buffer `device_sums`) for a caller that cannot allocate device
+ * memory -- e.g. a framework whose allocator owns all device memory, or a
+ * service loop that must not risk the device-wide synchronisation of a
+ * cudaMalloc.  No counterpart in the reference: it exists for such callers.
+ * The call allocates nothing: its scratch (per-block partial sums) is a
+ * file-scope device array of 3 MiB that every GPU loading the library holds
+ * until exit, which limits it to lattices of at most 2,097,152 sites (128^3);
+ * larger ones return SU2GPU_ERR_CAPACITY.  All calls share that array, so
+ * calls that overlap on the GPU race; serialise them.  The first call on a
+ * device looks up the array's address on that device -- make it before any
+ * stream capture.  Asynchronous on `cuda_stream` (a cudaStream_t, NULL = the
+ * default stream); errors are reported by the return code and
+ * su2gpu_last_error(). */
+int su2gpu_measure_noalloc(const su2gpu_params* p, const su2gpu_device_fields* fields, double* device_sums,
+                           void* cuda_stream);
+
 /* Last CUDA / kernel error as text. */
 const char* su2gpu_last_error(void);
 

@@ -155,6 +155,18 @@ class Weight(ctypes.Structure):
     ]
 
 
+class DeviceFields(ctypes.Structure):
+    """su2gpu_device_fields: device pointers in the library's field layout."""
+
+    _fields_ = [
+        ("link", ctypes.c_void_p * 3),
+        ("u1", ctypes.c_void_p * 3),
+        ("doublet", ctypes.c_void_p * 2),
+        ("triplet", ctypes.c_void_p * 3),
+        ("singlet", ctypes.c_void_p),
+    ]
+
+
 def make_params(content="fund", L=(8, 8, 8), precision=64, **kw):
     """Parameters with the reference config's defaults (su2higgs config:1-156)
     overridden by keyword arguments; `content` is a name or a bit mask."""

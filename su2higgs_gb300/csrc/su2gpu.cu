@@ -28,6 +28,10 @@ static void set_err(const char* fmt, ...) {
   vsnprintf(g_err, sizeof(g_err), fmt, ap);
   va_end(ap);
 }
+// C++ linkage, not part of the ABI: lets other units of the library set the
+// text returned by su2gpu_last_error
+__attribute__((visibility("hidden"))) void su2gpu_record_error(const char* msg) { set_err("%s", msg); }
+
 #define CK(call)                                                                     \
   do {                                                                               \
     cudaError_t e_ = (call);                                                         \
