@@ -182,6 +182,13 @@ int su2gpu_update_lattice(su2gpu_ctx* ctx, uint32_t sweep);
  * CUDA graph of one sweep. */
 int su2gpu_run_sweeps(su2gpu_ctx* ctx, uint32_t first_sweep, int32_t nsweeps, int32_t use_graph);
 int su2gpu_get_counters(su2gpu_ctx* ctx, int64_t* counters /* SU2GPU_NCOUNTERS */);
+/* One half-sweep, the body of one checkerboard_sweep_*() call (update.c:35-259)
+ * without multicanonical checks, for tests and diagnostics.  kind: 0 SU(2)
+ * links (algorithm_su2link), 1 U(1) links, 2 doublet, 3 doublet forced
+ * Metropolis, 4 triplet, 5 triplet forced Metropolis, 6 singlet, 7 singlet
+ * forced Metropolis; sub = direction or doublet index; pass and sweep select
+ * the random stream. */
+int su2gpu_run_halfsweep(su2gpu_ctx* ctx, int32_t kind, int32_t parity, int32_t sub, uint32_t pass, uint32_t sweep);
 int su2gpu_reset_counters(su2gpu_ctx* ctx);
 
 /* measure() volume sums (SU2GPU_NMEAS doubles, FP64 accumulation). */

@@ -384,20 +384,34 @@ __device__ inline int heatbath(const Fields<R>& f, const Geom& g, const Coup& cp
   }
   if (rad < (R)0) return 0;
   rad = msqrt(rad);
-  d = 2;
-  int it = 0;
-  while (d > (R)1 || d == (R)0) {
-    r1 = (R)2 * rng.uni() - (R)1;
-    r2 = (R)2 * rng.uni() - (R)1;
-    r3 = (R)2 * rng.uni() - (R)1;
-    d = r1 * r1 + r2 * r2 + r3 * r3;
-    if (++it > 4096) {  // probability (1 - pi/6)^4096: never; guards a NaN state
-      *err = 1;
-      return 0;
+  Q<R> nl;
+  if constexpr (sizeof(R) == 8) {
+    // uniform direction on S^2 by rejection from the cube (heatbath.c:82-93)
+    d = 2;
+    int it = 0;
+    while (d > (R)1 || d == (R)0) {
+      r1 = (R)2 * rng.uni() - (R)1;
+      r2 = (R)2 * rng.uni() - (R)1;
+      r3 = (R)2 * rng.uni() - (R)1;
+      d = r1 * r1 + r2 * r2 + r3 * r3;
+      if (++it > 4096) {  // probability (1 - pi/6)^4096: never; guards a NaN state
+        *err = 1;
+        return 0;
+      }
     }
+    d = msqrt(d);
+    nl = Q<R>{a0, r1 * (rad / d), r2 * (rad / d), r3 * (rad / d)};
+  } else {
+    // FP32 form: the same uniform direction drawn directly (Archimedes:
+    // cos(theta) uniform on [-1,1], azimuth uniform), no rejection loop to
+    // diverge a warp
+    float z = 2.0f * rng.uni() - 1.0f;
+    float ph = rng.uni();
+    float sn, cs;
+    sincospif(2.0f * ph, &sn, &cs);
+    float s = sqrtf(fmaxf(0.0f, 1.0f - z * z)) * rad;
+    nl = Q<R>{a0, s * cs, s * sn, z * rad};
   }
-  d = msqrt(d);
-  Q<R> nl{a0, r1 * (rad / d), r2 * (rad / d), r3 * (rad / d)};
   Q<R> U = unitize(qmul(nl, qdag(V)));
   st4<R>(lk(f, mu), i, U);
   if (HAS(C_T)) {

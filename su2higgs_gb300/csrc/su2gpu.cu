@@ -711,6 +711,52 @@ int su2gpu_host_unregister(void* p) {
   return SU2GPU_OK;
 }
 
+int su2gpu_run_halfsweep(su2gpu_ctx* c, int32_t kind, int32_t parity, int32_t sub, uint32_t pass, uint32_t sweep) {
+  if (!c || kind < 0 || kind > 7 || (parity != 0 && parity != 1)) return SU2GPU_ERR_INVALID;
+  int field = kind < 2 ? -1 : (kind - 2) / 2;  // 0 doublet, 1 triplet, 2 singlet
+  if ((kind == 1 && !c->has_u1) || (field == 0 && sub >= c->nh) || (field == 1 && !c->has_t) ||
+      (field == 2 && !c->has_s) || (kind <= 1 && (sub < 0 || sub > 2))) {
+    set_err("half-sweep kind %d / index %d not present in this content", kind, sub);
+    return SU2GPU_ERR_INVALID;
+  }
+  const int64_t N = c->g.half;
+  k_set_u32<<<1, 1, 0, c->st>>>(c->d_sweep, sweep);
+  CKL();
+  PassArgs a;
+  memset(&a, 0, sizeof(a));
+  a.g = c->g;
+  a.cp = c->cp;
+  a.rk = RngKey{(uint32_t)c->seed, (uint32_t)(c->seed >> 32), c->chain, c->d_sweep};
+  a.ctr = c->d_ctr;
+  a.err = c->d_err;
+  a.parity = parity;
+  a.sub = sub;
+  a.pass = pass;
+  a.t_lo = 0;
+  a.t_hi = (int)N;
+  if (kind == 0) {
+    a.alg = c->p.algorithm_su2link;
+    c->ops->link(c->F(), a, nblk(N, BLOCK), c->st);
+    c->host_tot[SU2GPU_C_TOTAL_SU2LINK] += N;
+  } else if (kind == 1) {
+    c->ops->u1(c->F(), a, nblk(N, BLOCK), c->st);
+    c->host_tot[SU2GPU_C_TOTAL_U1LINK] += N;
+  } else {
+    int metro = (kind & 1);
+    int alg = field == 0 ? c->p.algorithm_su2doublet : (field == 1 ? c->p.algorithm_su2triplet : c->p.algorithm_singlet);
+    bool orr = alg == SU2GPU_OVERRELAX && !metro;
+    int idx = field == 0 ? (orr ? SU2GPU_C_TOTAL_OR_DOUBLET : SU2GPU_C_TOTAL_DOUBLET) + sub
+                         : (field == 1 ? (orr ? SU2GPU_C_TOTAL_OR_TRIPLET : SU2GPU_C_TOTAL_TRIPLET)
+                                       : (orr ? SU2GPU_C_TOTAL_OR_SINGLET : SU2GPU_C_TOTAL_SINGLET));
+    c->host_tot[idx] += N;
+    a.alg = metro;
+    c->ops->scalar(field, c->F(), a, nblk(N, BLOCK), c->st);
+  }
+  CKL();
+  CK(cudaStreamSynchronize(c->st));
+  return check_device_error(c);
+}
+
 int su2gpu_get_counters(su2gpu_ctx* c, int64_t* out) {
   if (!c || !out) return SU2GPU_ERR_INVALID;
   unsigned long long d[SU2GPU_NCOUNTERS];

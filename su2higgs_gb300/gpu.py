@@ -66,6 +66,7 @@ def lib():
         L.su2gpu_profile_sweep.argtypes = [vp, u32, i32, vp, vp, ctypes.POINTER(i32)]
         L.su2gpu_host_register.argtypes = [vp, i64]
         L.su2gpu_host_unregister.argtypes = [vp]
+        L.su2gpu_run_halfsweep.argtypes = [vp, i32, i32, i32, u32, u32]
         _lib = L
     return _lib
 
@@ -142,6 +143,11 @@ class Lattice:
 
     def run_sweeps(self, first_sweep, n, graph=True):
         check(lib().su2gpu_run_sweeps(self._h, first_sweep, n, 1 if graph else 0))
+
+    def run_halfsweep(self, kind, parity, sub, pass_, sweep):
+        """One half-sweep (kind 0 links, 1 U(1), 2/3 doublet OR|Metropolis,
+        4/5 triplet, 6/7 singlet; see su2gpu_run_halfsweep)."""
+        check(lib().su2gpu_run_halfsweep(self._h, kind, parity, sub, pass_, sweep))
 
     def counters(self):
         c = np.zeros(abi.NCOUNTERS, np.int64)
