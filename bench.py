@@ -232,6 +232,7 @@ def run_gpu(args):
     f = hot_fields(p, seed)
     lat = gpu.Lattice(p, seed=seed, chain=rank)
     lat.upload(**f)
+    variants, _ = lat.autotune()
     stream = torch.cuda.Stream(device=dev)
     lat.set_stream(stream.cuda_stream)
     K, W = args.steps, args.warmup
@@ -332,6 +333,7 @@ def run_gpu(args):
         p64 = abi.make_params(content, L=L, precision=64)
         lat64 = gpu.Lattice(p64, seed=seed)
         lat64.upload(**f)
+        lat64.autotune()
         lat64.set_stream(stream.cuda_stream)
         n64 = max(3, min(K // 4, 25))
         with torch.cuda.stream(stream):
@@ -371,9 +373,11 @@ def run_gpu(args):
                        "couplings": {"betasu2": p.betasu2, "msq": p.msq_phi, "lambda": p.lambda_phi},
                        "reunitarize_interval": p.reunitarize_interval if prec == 32 else None,
                        "l2": "flushed between steps (256 MiB write outside the step events)",
-                       "parallelism": f"replicas x{world}", "graph": True},
+                       "parallelism": f"replicas x{world}", "graph": True,
+                       "launch_variants": [int(v) for v in variants]},
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "fp64_plain": fp64,
-            "gpu_launches": int(K * (launches_sweep + 2)),
+            # per step: the sweep's kernels, the sweep-counter set/increment, measure + reduction
+            "gpu_launches": int(K * (launches_sweep + 4)),
             "clocks": clk, "wall_s_timed_region": t_wall,
             "step_ms_p50": float(np.percentile(step_ms, 50)), "step_ms_p99": float(np.percentile(step_ms, 99)),
         }

@@ -240,6 +240,14 @@ int su2gpu_launches_per_sweep(su2gpu_ctx* ctx, int32_t* n);
  * 2 doublet, 3 triplet, 4 singlet, 5 reunitarisation; ms[k] its duration. */
 int su2gpu_profile_sweep(su2gpu_ctx* ctx, uint32_t sweep, int32_t max_passes, int32_t* kinds, float* ms,
                          int32_t* npasses);
+/* Launch-shape autotuner: times every launch-shape variant (block size x
+ * register budget) of each update kernel kind -- 0 SU(2) links, 1 U(1),
+ * 2 doublet, 3 triplet, 4 singlet -- on a scratch copy of the fields (the
+ * chain is not advanced) and keeps the fastest.  choices[5] / best_ms[5]
+ * (may be NULL) receive the picks and their mean launch times. */
+int su2gpu_autotune(su2gpu_ctx* ctx, int32_t* choices, float* best_ms);
+/* Set the launch-shape variants explicitly (choices[5], each in [0, 4)). */
+int su2gpu_set_variants(su2gpu_ctx* ctx, const int32_t* choices);
 /* Page-lock host memory for the host-buffer entry points. */
 int su2gpu_host_register(void* ptr, int64_t bytes);
 int su2gpu_host_unregister(void* ptr);

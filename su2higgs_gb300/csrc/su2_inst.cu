@@ -10,17 +10,54 @@ namespace su2 {
 using R = SU2_R;
 constexpr int CCI = SU2_CC;
 
-static void l_link(const void* f, const PassArgs& a, unsigned nb, cudaStream_t st) {
-  k_link<R, CCI><<<nb, BLOCK, 0, st>>>(*(const Fields<R>*)f, a);
+template <int V>
+static unsigned l_link_v(const void* f, const PassArgs& a, cudaStream_t st) {
+  constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB;
+  unsigned nb = (unsigned)((a.t_hi - a.t_lo + BS - 1) / BS);
+  if (nb) k_link<R, CCI, BS, MB><<<nb, BS, 0, st>>>(*(const Fields<R>*)f, a);
+  return nb;
 }
-static void l_u1(const void* f, const PassArgs& a, unsigned nb, cudaStream_t st) {
-  k_u1<R, CCI><<<nb, BLOCK, 0, st>>>(*(const Fields<R>*)f, a);
+template <int V>
+static unsigned l_u1_v(const void* f, const PassArgs& a, cudaStream_t st) {
+  constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB;
+  unsigned nb = (unsigned)((a.t_hi - a.t_lo + BS - 1) / BS);
+  if (nb) k_u1<R, CCI, BS, MB><<<nb, BS, 0, st>>>(*(const Fields<R>*)f, a);
+  return nb;
 }
-static void l_scalar(int field, const void* f, const PassArgs& a, unsigned nb, cudaStream_t st) {
+template <int V>
+static unsigned l_scalar_v(int field, const void* f, const PassArgs& a, cudaStream_t st) {
+  constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB;
+  unsigned nb = (unsigned)((a.t_hi - a.t_lo + BS - 1) / BS);
+  if (!nb) return 0;
   const Fields<R>& F = *(const Fields<R>*)f;
-  if (field == 0) k_scalar<R, CCI, 0><<<nb, BLOCK, 0, st>>>(F, a);
-  else if (field == 1) k_scalar<R, CCI, 1><<<nb, BLOCK, 0, st>>>(F, a);
-  else k_scalar<R, CCI, 2><<<nb, BLOCK, 0, st>>>(F, a);
+  if (field == 0) k_scalar<R, CCI, 0, BS, MB><<<nb, BS, 0, st>>>(F, a);
+  else if (field == 1) k_scalar<R, CCI, 1, BS, MB><<<nb, BS, 0, st>>>(F, a);
+  else k_scalar<R, CCI, 2, BS, MB><<<nb, BS, 0, st>>>(F, a);
+  return nb;
+}
+static unsigned l_link(int v, const void* f, const PassArgs& a, cudaStream_t st) {
+  switch (v) {
+    case 1: return l_link_v<1>(f, a, st);
+    case 2: return l_link_v<2>(f, a, st);
+    case 3: return l_link_v<3>(f, a, st);
+    default: return l_link_v<0>(f, a, st);
+  }
+}
+static unsigned l_u1(int v, const void* f, const PassArgs& a, cudaStream_t st) {
+  switch (v) {
+    case 1: return l_u1_v<1>(f, a, st);
+    case 2: return l_u1_v<2>(f, a, st);
+    case 3: return l_u1_v<3>(f, a, st);
+    default: return l_u1_v<0>(f, a, st);
+  }
+}
+static unsigned l_scalar(int v, int field, const void* f, const PassArgs& a, cudaStream_t st) {
+  switch (v) {
+    case 1: return l_scalar_v<1>(field, f, a, st);
+    case 2: return l_scalar_v<2>(field, f, a, st);
+    case 3: return l_scalar_v<3>(field, f, a, st);
+    default: return l_scalar_v<0>(field, f, a, st);
+  }
 }
 static void l_measure(const void* f, const Geom& g, const Coup& cp, const double* alpha, double* partials,
                       unsigned nb, cudaStream_t st) {

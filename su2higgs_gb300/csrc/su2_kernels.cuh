@@ -24,6 +24,17 @@ template <typename R>
 struct MinBlocks {
   static constexpr int value = sizeof(R) == 4 ? 8 : 4;
 };
+
+// launch shapes of the update kernels the autotuner chooses from:
+// (threads per block, resident blocks per SM asked of the compiler, which
+// sets the register budget: 65536 / (threads * blocks))
+constexpr int NVARIANTS = 4;
+template <typename R, int V>
+struct Variant;
+template <typename R> struct Variant<R, 0> { static constexpr int BS = 128, MINB = sizeof(R) == 4 ? 8 : 4; };
+template <typename R> struct Variant<R, 1> { static constexpr int BS = 128, MINB = sizeof(R) == 4 ? 5 : 3; };
+template <typename R> struct Variant<R, 2> { static constexpr int BS = 256, MINB = sizeof(R) == 4 ? 4 : 2; };
+template <typename R> struct Variant<R, 3> { static constexpr int BS = 64, MINB = sizeof(R) == 4 ? 12 : 6; };
 constexpr int NSUMS = 24;
 
 // ---------------------------------------------------------------------------
@@ -712,8 +723,8 @@ struct PassArgs {
   int* err;                 // device error flag
 };
 
-template <typename R, int CC>
-__global__ void __launch_bounds__(BLOCK, MinBlocks<R>::value) k_link(Fields<R> f, PassArgs a) {
+template <typename R, int CC, int BS, int MINB>
+__global__ void __launch_bounds__(BS, MINB) k_link(Fields<R> f, PassArgs a) {
   const Coup& cp = a.cp;
   int t = a.t_lo + (int)blockIdx.x * blockDim.x + threadIdx.x;
   int acc = 0, cap = 0, err = 0;
@@ -730,8 +741,8 @@ __global__ void __launch_bounds__(BLOCK, MinBlocks<R>::value) k_link(Fields<R> f
   if (err) atomicOr(a.err, 1);
 }
 
-template <typename R, int CC>
-__global__ void __launch_bounds__(BLOCK, MinBlocks<R>::value) k_u1(Fields<R> f, PassArgs a) {
+template <typename R, int CC, int BS, int MINB>
+__global__ void __launch_bounds__(BS, MINB) k_u1(Fields<R> f, PassArgs a) {
   const Coup& cp = a.cp;
   int t = a.t_lo + (int)blockIdx.x * blockDim.x + threadIdx.x;
   int acc = 0;
@@ -748,8 +759,8 @@ __global__ void __launch_bounds__(BLOCK, MinBlocks<R>::value) k_u1(Fields<R> f, 
 // one parity (or a contiguous block of it) of one doublet / the triplet /
 // the singlet; optional multicanonical backup of the old values and block
 // sums of the order parameter over the new ones
-template <typename R, int CC, int FIELD>
-__global__ void __launch_bounds__(BLOCK, MinBlocks<R>::value) k_scalar(Fields<R> f, PassArgs a) {
+template <typename R, int CC, int FIELD, int BS, int MINB>
+__global__ void __launch_bounds__(BS, MINB) k_scalar(Fields<R> f, PassArgs a) {
   const Coup& cp = a.cp;
   int t = a.t_lo + (int)blockIdx.x * blockDim.x + threadIdx.x;
   int acc = 0, fb = 0;

@@ -10,12 +10,15 @@ namespace su2 {
 
 struct PassArgs;
 
+// The update launchers take a launch-shape variant (0..NVARIANTS-1, see
+// Variant in su2_kernels.cuh) and the site range in the PassArgs; they return
+// the number of blocks launched (the length of any per-block partial sums).
 struct Ops {
   int prec;     // 64 or 32
   int content;  // C_GENERIC or a content mask
-  void (*link)(const void* f, const PassArgs& a, unsigned nblocks, cudaStream_t st);
-  void (*u1)(const void* f, const PassArgs& a, unsigned nblocks, cudaStream_t st);
-  void (*scalar)(int field, const void* f, const PassArgs& a, unsigned nblocks, cudaStream_t st);
+  unsigned (*link)(int variant, const void* f, const PassArgs& a, cudaStream_t st);
+  unsigned (*u1)(int variant, const void* f, const PassArgs& a, cudaStream_t st);
+  unsigned (*scalar)(int variant, int field, const void* f, const PassArgs& a, cudaStream_t st);
   void (*measure)(const void* f, const Geom& g, const Coup& cp, const double* alpha, double* partials,
                   unsigned nblocks, cudaStream_t st);
   void (*flow)(const void* fin, const void* fout, const Geom& g, const Coup& cp, double dt,

@@ -115,6 +115,7 @@ struct su2gpu_ctx {
   uint32_t* d_sweep = nullptr;
   unsigned long long* d_fz = nullptr;
   int64_t host_tot[SU2GPU_NCOUNTERS] = {0};
+  int var[5] = {0, 0, 0, 0, 0};  // launch-shape variant per kernel kind (link, U(1), doublet, triplet, singlet)
   uint64_t seed = 0;
   uint32_t chain = 0;
   // multicanonical
@@ -432,7 +433,7 @@ static int scalar_pass(su2gpu_ctx* c, const PassArgs& base, int field, int h, in
   if (!do_muca) {
     a.t_lo = 0;
     a.t_hi = N;
-    c->ops->scalar(field, c->F(), a, nblk(N, BLOCK), c->st);
+    c->ops->scalar(c->var[2 + field], field, c->F(), a, c->st);
     c->launches++;
     CKL();
     return SU2GPU_OK;
@@ -455,8 +456,7 @@ static int scalar_pass(su2gpu_ctx* c, const PassArgs& base, int field, int h, in
     a.t_lo = k * interval;
     a.t_hi = (k + 1) * interval;
     a.partials = fused ? partials : nullptr;
-    unsigned nb = nblk(a.t_hi - a.t_lo, BLOCK);
-    c->ops->scalar(field, c->F(), a, nb, c->st);
+    unsigned nb = c->ops->scalar(c->var[2 + field], field, c->F(), a, c->st);
     CKL();
     unsigned np = nb;
     if (!fused) {
@@ -477,7 +477,7 @@ static int scalar_pass(su2gpu_ctx* c, const PassArgs& base, int field, int h, in
       a.t_lo = lo;
       a.t_hi = hi;
       a.partials = nullptr;
-      c->ops->scalar(field, c->F(), a, nblk(hi - lo, BLOCK), c->st);
+      c->ops->scalar(c->var[2 + field], field, c->F(), a, c->st);
       c->launches++;
       CKL();
     } else {
@@ -517,7 +517,7 @@ static int enqueue_sweep(su2gpu_ctx* c, int64_t* tot) {
         PassArgs a = base;
         a.parity = par; a.sub = mu; a.alg = p.algorithm_su2link; a.pass = pass++; a.t_lo = 0; a.t_hi = N;
         mark(c, 0);
-        c->ops->link(c->F(), a, nblk(N, BLOCK), c->st);
+        c->ops->link(c->var[0], c->F(), a, c->st);
         c->launches++;
         CKL();
         tot[SU2GPU_C_TOTAL_SU2LINK] += N;
@@ -528,7 +528,7 @@ static int enqueue_sweep(su2gpu_ctx* c, int64_t* tot) {
           PassArgs a = base;
           a.parity = par; a.sub = mu; a.pass = pass++; a.t_lo = 0; a.t_hi = N;
           mark(c, 1);
-          c->ops->u1(c->F(), a, nblk(N, BLOCK), c->st);
+          c->ops->u1(c->var[1], c->F(), a, c->st);
           c->launches++;
           CKL();
           tot[SU2GPU_C_TOTAL_U1LINK] += N;
@@ -736,10 +736,10 @@ int su2gpu_run_halfsweep(su2gpu_ctx* c, int32_t kind, int32_t parity, int32_t su
   a.t_hi = (int)N;
   if (kind == 0) {
     a.alg = c->p.algorithm_su2link;
-    c->ops->link(c->F(), a, nblk(N, BLOCK), c->st);
+    c->ops->link(c->var[0], c->F(), a, c->st);
     c->host_tot[SU2GPU_C_TOTAL_SU2LINK] += N;
   } else if (kind == 1) {
-    c->ops->u1(c->F(), a, nblk(N, BLOCK), c->st);
+    c->ops->u1(c->var[1], c->F(), a, c->st);
     c->host_tot[SU2GPU_C_TOTAL_U1LINK] += N;
   } else {
     int metro = (kind & 1);
@@ -750,11 +750,103 @@ int su2gpu_run_halfsweep(su2gpu_ctx* c, int32_t kind, int32_t parity, int32_t su
                                        : (orr ? SU2GPU_C_TOTAL_OR_SINGLET : SU2GPU_C_TOTAL_SINGLET));
     c->host_tot[idx] += N;
     a.alg = metro;
-    c->ops->scalar(field, c->F(), a, nblk(N, BLOCK), c->st);
+    c->ops->scalar(c->var[2 + field], field, c->F(), a, c->st);
   }
   CKL();
   CK(cudaStreamSynchronize(c->st));
   return check_device_error(c);
+}
+
+// Launch-shape autotuner: times every variant of every update kernel kind of
+// this content on a scratch copy of the fields (the chain itself is not
+// advanced, its counters are untouched) and keeps the fastest.
+int su2gpu_autotune(su2gpu_ctx* c, int32_t* choices, float* best_ms) {
+  if (!c) return SU2GPU_ERR_INVALID;
+  DevBuf tmp, ctr;
+  int rc = tmp.ensure(c->fields.n);
+  if (rc) return rc;
+  if ((rc = ctr.ensure(4096))) { tmp.release(); return rc; }
+  CK(cudaMemcpyAsync(tmp.p, c->fields.p, c->fields.n, cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaMemsetAsync(ctr.p, 0, 4096, c->st));
+  Fields<double> f64;
+  Fields<float> f32;
+  if (c->prec == 64) carve(f64, (char*)tmp.p, &c->p, c->g.V);
+  else carve(f32, (char*)tmp.p, &c->p, c->g.V);
+  const void* F = c->prec == 64 ? (const void*)&f64 : (const void*)&f32;
+  k_set_u32<<<1, 1, 0, c->st>>>((uint32_t*)((char*)ctr.p + 1024), 0x7fffffffu);
+  PassArgs a;
+  memset(&a, 0, sizeof(a));
+  a.g = c->g;
+  a.cp = c->cp;
+  a.rk = RngKey{(uint32_t)c->seed ^ 0x5eedu, (uint32_t)(c->seed >> 32), c->chain, (uint32_t*)((char*)ctr.p + 1024)};
+  a.ctr = (unsigned long long*)ctr.p;
+  a.err = (int*)((char*)ctr.p + 512);
+  a.t_lo = 0;
+  a.t_hi = (int)c->g.half;
+  bool present[5] = {true, (bool)c->has_u1, c->nh > 0, (bool)c->has_t, (bool)c->has_s};
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int reps = 4;
+  for (int kind = 0; kind < 5; kind++) {
+    if (!present[kind]) continue;
+    float best = 1e30f;
+    int bestv = 0;
+    for (int v = 0; v < NVARIANTS; v++) {
+      float ms = 0.f;
+      for (int r = -1; r < reps; r++) {  // r = -1: warm-up
+        a.parity = r & 1;
+        a.sub = (r + 3) % 3;
+        a.pass = 60000 + r;
+        a.alg = kind == 0 ? c->p.algorithm_su2link : 0;
+        if (kind == 2) a.sub = 0;
+        cudaEventRecord(e0, c->st);
+        if (kind == 0) c->ops->link(v, F, a, c->st);
+        else if (kind == 1) c->ops->u1(v, F, a, c->st);
+        else c->ops->scalar(v, kind - 2, F, a, c->st);
+        cudaEventRecord(e1, c->st);
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) {
+          set_err("autotune: %s", cudaGetErrorString(e));
+          return SU2GPU_ERR_CUDA;
+        }
+        float t = 0.f;
+        cudaEventElapsedTime(&t, e0, e1);
+        if (r >= 0) ms += t;
+      }
+      if (ms < best) {
+        best = ms;
+        bestv = v;
+      }
+    }
+    c->var[kind] = bestv;
+    if (best_ms) best_ms[kind] = best / reps;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CK(cudaStreamSynchronize(c->st));
+  tmp.release();
+  ctr.release();
+  if (choices)
+    for (int k = 0; k < 5; k++) choices[k] = c->var[k];
+  if (c->gexec) {
+    cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+  }
+  return SU2GPU_OK;
+}
+
+int su2gpu_set_variants(su2gpu_ctx* c, const int32_t* choices) {
+  if (!c || !choices) return SU2GPU_ERR_INVALID;
+  for (int k = 0; k < 5; k++) {
+    if (choices[k] < 0 || choices[k] >= NVARIANTS) return SU2GPU_ERR_INVALID;
+    c->var[k] = choices[k];
+  }
+  if (c->gexec) {
+    cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+  }
+  return SU2GPU_OK;
 }
 
 int su2gpu_get_counters(su2gpu_ctx* c, int64_t* out) {

@@ -67,6 +67,8 @@ def lib():
         L.su2gpu_host_register.argtypes = [vp, i64]
         L.su2gpu_host_unregister.argtypes = [vp]
         L.su2gpu_run_halfsweep.argtypes = [vp, i32, i32, i32, u32, u32]
+        L.su2gpu_autotune.argtypes = [vp, vp, vp]
+        L.su2gpu_set_variants.argtypes = [vp, vp]
         _lib = L
     return _lib
 
@@ -143,6 +145,18 @@ class Lattice:
 
     def run_sweeps(self, first_sweep, n, graph=True):
         check(lib().su2gpu_run_sweeps(self._h, first_sweep, n, 1 if graph else 0))
+
+    def autotune(self):
+        """Pick the fastest launch shape per update kernel kind; returns
+        (choices, mean launch ms) for link, U(1), doublet, triplet, singlet."""
+        ch = np.zeros(5, np.int32)
+        ms = np.zeros(5, np.float32)
+        check(lib().su2gpu_autotune(self._h, _p(ch), _p(ms)))
+        return ch, ms
+
+    def set_variants(self, choices):
+        ch = np.ascontiguousarray(choices, dtype=np.int32)
+        check(lib().su2gpu_set_variants(self._h, _p(ch)))
 
     def run_halfsweep(self, kind, parity, sub, pass_, sweep):
         """One half-sweep (kind 0 links, 1 U(1), 2/3 doublet OR|Metropolis,
