@@ -19,6 +19,10 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", ARCH, "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "-Wno-deprecated-gpu-targets", "--expt-relaxed-constexpr"]
 
+# FP32 units: approximate division and square root, denormals flushed (the
+# FP32 form is validated statistically; the FP64 units keep IEEE arithmetic)
+FP32_FLAGS = ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"]
+
 UNITS = [
     # name, source, defines
     ("inst_f64_generic", "su2_inst.cu", ["SU2_R=double", "SU2_CC=-1", "SU2_OPS=ops_f64_generic",
@@ -70,7 +74,8 @@ def build(verbose=False, force=False, jobs=None):
         obj = os.path.join(BUILD, name + ".o")
         if not force and not _stale(obj, deps):
             return obj
-        cmd = [exe] + NVCC_FLAGS + ["-D" + d for d in defs] + ["-c", os.path.join(CSRC, src), "-o", obj]
+        extra = FP32_FLAGS if "SU2_R=float" in defs else []
+        cmd = [exe] + NVCC_FLAGS + extra + ["-D" + d for d in defs] + ["-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

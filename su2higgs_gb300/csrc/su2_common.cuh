@@ -316,7 +316,7 @@ __device__ inline void st3(const Fields<R>& f, int i, const V3<R>& v) {
   f.trip[2][i] = v.z;
 }
 
-// couplings (reference params, su2.h:76-181)
+// couplings (reference params, su2.h:76-181), kept in double on the host
 struct Coup {
   double beta, msq, lam;
   double msqT, a2, b4;
@@ -326,6 +326,34 @@ struct Coup {
   int content;
   int alg_link, alg_u1, alg_d, alg_t, alg_s;
 };
+
+// the couplings in the kernels' working precision, converted once on the
+// host (a double-to-float conversion per use would run on the FP64 pipe)
+template <typename R>
+struct CoupT {
+  R beta, msq, lam;
+  R msqT, a2, b4;
+  R betau1, r_u1;
+  R b1s, msqs, b3s, b4s, a1s, a2s;
+  R msq2, m12re, m12im, lam2, lam3, lam4, lam5re, lam5im, lam6re, lam6im, lam7re, lam7im;
+  int content;
+  int alg_link, alg_u1, alg_d, alg_t, alg_s;
+};
+
+template <typename R>
+__host__ __device__ inline CoupT<R> coup_as(const Coup& c) {
+  CoupT<R> r;
+  r.beta = (R)c.beta; r.msq = (R)c.msq; r.lam = (R)c.lam;
+  r.msqT = (R)c.msqT; r.a2 = (R)c.a2; r.b4 = (R)c.b4;
+  r.betau1 = (R)c.betau1; r.r_u1 = (R)c.r_u1;
+  r.b1s = (R)c.b1s; r.msqs = (R)c.msqs; r.b3s = (R)c.b3s; r.b4s = (R)c.b4s; r.a1s = (R)c.a1s; r.a2s = (R)c.a2s;
+  r.msq2 = (R)c.msq2; r.m12re = (R)c.m12re; r.m12im = (R)c.m12im;
+  r.lam2 = (R)c.lam2; r.lam3 = (R)c.lam3; r.lam4 = (R)c.lam4; r.lam5re = (R)c.lam5re; r.lam5im = (R)c.lam5im;
+  r.lam6re = (R)c.lam6re; r.lam6im = (R)c.lam6im; r.lam7re = (R)c.lam7re; r.lam7im = (R)c.lam7im;
+  r.content = c.content;
+  r.alg_link = c.alg_link; r.alg_u1 = c.alg_u1; r.alg_d = c.alg_d; r.alg_t = c.alg_t; r.alg_s = c.alg_s;
+  return r;
+}
 
 // device multicanonical state (weight struct, su2.h:235-274)
 struct MucaDev {

@@ -61,11 +61,11 @@ static unsigned l_scalar(int v, int field, const void* f, const PassArgs& a, cud
 }
 static void l_measure(const void* f, const Geom& g, const Coup& cp, const double* alpha, double* partials,
                       unsigned nb, cudaStream_t st) {
-  k_measure<R, CCI><<<nb, BLOCK, 0, st>>>(*(const Fields<R>*)f, g, cp, alpha, partials);
+  k_measure<R, CCI><<<nb, BLOCK, 0, st>>>(*(const Fields<R>*)f, g, coup_as<R>(cp), alpha, partials);
 }
 static void l_flow(const void* fin, const void* fout, const Geom& g, const Coup& cp, double dt,
                    unsigned long long* fz, unsigned nb, cudaStream_t st) {
-  k_flow<R, CCI><<<nb, BLOCK, 0, st>>>(*(const Fields<R>*)fin, *(const Fields<R>*)fout, g, cp, (R)dt, fz);
+  k_flow<R, CCI><<<nb, BLOCK, 0, st>>>(*(const Fields<R>*)fin, *(const Fields<R>*)fout, g, coup_as<R>(cp), (R)dt, fz);
 }
 
 const Ops SU2_OPS = {sizeof(R) == 8 ? 64 : 32, CCI, l_link, l_u1, l_scalar, l_measure, l_flow};
@@ -84,7 +84,7 @@ static void p_restore(int field, const void* f, const MucaDev* m, const void* ba
   else k_muca_restore<R, 1><<<nb, 256, 0, st>>>(*(const Fields<R>*)f, m, backup, h, lo, hi);
 }
 static void p_alpha(const void* f, const Geom& g, const Coup& cp, double* alpha, cudaStream_t st) {
-  k_alpha<R><<<nblk(g.V, BLOCK), BLOCK, 0, st>>>(*(const Fields<R>*)f, g, cp, alpha);
+  k_alpha<R><<<nblk(g.V, BLOCK), BLOCK, 0, st>>>(*(const Fields<R>*)f, g, coup_as<R>(cp), alpha);
 }
 static void p_import(const void* f, int64_t V, int kind, int h, const double* src, cudaStream_t st) {
   k_import<R><<<nblk(V * 3, 256), 256, 0, st>>>(*(const Fields<R>*)f, V, kind, h, src);

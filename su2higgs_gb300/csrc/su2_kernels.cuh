@@ -96,9 +96,9 @@ __device__ inline R hop_triplet_fwd_u(const Fields<R>& f, const Geom& g, const i
 
 // su2link_staple (staples.c:134-193)
 template <typename R, int CC>
-__device__ inline Q<R> link_staple(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
+__device__ inline Q<R> link_staple(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
                                    int mu) {
-  Q<R> V = qscale(wilson_staple(f, g, c, i, mu), (R)(-0.5 * cp.beta));
+  Q<R> V = qscale(wilson_staple(f, g, c, i, mu), (R)-0.5 * cp.beta);
   const int nh = NHIGGS;
   if (nh > 0) {
     int xp = shifted(g, c, mu, 1);
@@ -137,26 +137,26 @@ __device__ inline R tripletsq(const V3<R>& a) {
 
 // hopping_trace(_su2u1) (su2u1.c:388-418): Re Tr Phi1^+ U Phi2 e^{-i a s3}
 template <typename R, int CC>
-__device__ inline R hop_trace(const Coup& cp, const Q<R>& p1, const Q<R>& u, const Q<R>& p2, R alpha) {
+__device__ inline R hop_trace(const CoupT<R>& cp, const Q<R>& p1, const Q<R>& u, const Q<R>& p2, R alpha) {
   Q<R> t = qmul(u, p2);
   if (HAS(C_U1)) t = qmul(t, u1phase(alpha));
   return qdot0(qdag(p1), t);
 }
 template <typename R, int CC>
-__device__ inline R hop_doublet_fwd(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
+__device__ inline R hop_doublet_fwd(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
                                     int mu, int h) {
   R al = HAS(C_U1) ? a1p(f, mu)[i] : (R)0;
   return -hop_trace<R, CC>(cp, ld4<R>(php(f, h), i), ld4<R>(lk(f, mu), i), ld4<R>(php(f, h), shifted(g, c, mu, 1)), al);
 }
 template <typename R, int CC>
-__device__ inline R hop_doublet_bwd(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
+__device__ inline R hop_doublet_bwd(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
                                     int mu, int h) {
   int pm = shifted(g, c, mu, -1);
   R al = HAS(C_U1) ? a1p(f, mu)[pm] : (R)0;
   return -hop_trace<R, CC>(cp, ld4<R>(php(f, h), pm), ld4<R>(lk(f, mu), pm), ld4<R>(php(f, h), i), al);
 }
 template <typename R, int CC>
-__device__ inline R covariant_doublet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
+__device__ inline R covariant_doublet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
                                       int h) {
   R tot = 0, mod = doubletsq(ld4<R>(php(f, h), i));
 #pragma unroll
@@ -166,7 +166,7 @@ __device__ inline R covariant_doublet(const Fields<R>& f, const Geom& g, const C
 
 // potential_singlet (su2u1.c:708-723)
 template <typename R, int CC>
-__device__ inline R potential_singlet(const Fields<R>& f, const Coup& cp, int i) {
+__device__ inline R potential_singlet(const Fields<R>& f, const CoupT<R>& cp, int i) {
   R S = f.sing[i];
   R pot = (R)cp.b1s * S + (R)0.5 * (R)cp.msqs * S * S + (R)(1.0 / 3.0) * (R)cp.b3s * S * S * S +
           (R)0.25 * (R)cp.b4s * S * S * S * S;
@@ -179,7 +179,7 @@ __device__ inline R potential_singlet(const Fields<R>& f, const Coup& cp, int i)
 
 // higgspotential (su2u1.c:528-572)
 template <typename R, int CC>
-__device__ inline R higgspotential(const Fields<R>& f, const Coup& cp, int i) {
+__device__ inline R higgspotential(const Fields<R>& f, const CoupT<R>& cp, int i) {
   R pot = 0, mod = 0;
   const int nh = NHIGGS;
   if (nh > 0) {
@@ -208,7 +208,7 @@ __device__ inline R higgspotential(const Fields<R>& f, const Coup& cp, int i) {
 
 // localact_doublet (su2u1.c:495-510)
 template <typename R, int CC>
-__device__ inline R localact_doublet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
+__device__ inline R localact_doublet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
                                      int h) {
   R tot = covariant_doublet<R, CC>(f, g, cp, c, i, h);
 #pragma unroll
@@ -219,7 +219,7 @@ __device__ inline R localact_doublet(const Fields<R>& f, const Geom& g, const Co
 
 // staple_doublet (staples.c:243-302)
 template <typename R, int CC>
-__device__ inline Q<R> staple_doublet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
+__device__ inline Q<R> staple_doublet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
                                       int h) {
   Q<R> res{(R)0, (R)0, (R)0, (R)0};
 #pragma unroll
@@ -258,7 +258,7 @@ __device__ inline R covariant_triplet(const Fields<R>& f, const Geom& g, const i
 }
 // localact_triplet (su2u1.c:657-679)
 template <typename R, int CC>
-__device__ inline R localact_triplet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i) {
+__device__ inline R localact_triplet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i) {
   R tot = covariant_triplet(f, g, c, i);
 #pragma unroll
   for (int d = 0; d < 3; d++) tot += hop_triplet_bwd(f, g, c, i, d);
@@ -270,7 +270,7 @@ __device__ inline R localact_triplet(const Fields<R>& f, const Geom& g, const Co
 
 // localact_su2link (su2u1.c:166-198)
 template <typename R, int CC>
-__device__ inline R localact_su2link(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
+__device__ inline R localact_su2link(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
                                      int mu) {
   R tot = 0;
 #pragma unroll
@@ -296,7 +296,7 @@ __device__ inline R u1ptrace(const Fields<R>& f, const Geom& g, const int* c, in
 }
 // local_u1wilson (su2u1.c:316-328)
 template <typename R>
-__device__ inline R local_u1wilson(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i) {
+__device__ inline R local_u1wilson(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i) {
   R res = 0;
 #pragma unroll
   for (int d1 = 0; d1 < 3; d1++)
@@ -306,7 +306,7 @@ __device__ inline R local_u1wilson(const Fields<R>& f, const Geom& g, const Coup
 }
 // localact_u1link (su2u1.c:336-354)
 template <typename R, int CC>
-__device__ inline R localact_u1link(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
+__device__ inline R localact_u1link(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
                                     int mu) {
   R tot = 0;
 #pragma unroll
@@ -360,7 +360,7 @@ __device__ inline R polysolve3(R a, R b, R c, R d, int* fallback) {
 // drawn in the reference's order (4 per trial, 3 per sphere trial, 1 for the
 // triplet accept/reject).
 template <typename R, int CC>
-__device__ inline int heatbath(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i, int mu,
+__device__ inline int heatbath(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i, int mu,
                                SiteRng<R>& rng, int* kpcap, int* err) {
   Q<R> old{};
   R oldact = 0;
@@ -453,7 +453,7 @@ __device__ inline int metro_accept(R diff, SiteRng<R>& rng) {
 
 // metro_su2link (metropolis.c:15-41) with random_su2link (init.c:43-58)
 template <typename R, int CC>
-__device__ inline int metro_link(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i, int mu,
+__device__ inline int metro_link(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i, int mu,
                                  SiteRng<R>& rng) {
   Q<R> old = ld4<R>(lk(f, mu), i);
   R a0 = localact_su2link<R, CC>(f, g, cp, c, i, mu);
@@ -473,7 +473,7 @@ __device__ inline int metro_link(const Fields<R>& f, const Geom& g, const Coup& 
 
 // metro_u1link (metropolis.c:48-70)
 template <typename R, int CC>
-__device__ inline int metro_u1(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i, int mu,
+__device__ inline int metro_u1(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i, int mu,
                                SiteRng<R>& rng) {
   R old = a1p(f, mu)[i];
   R a0 = localact_u1link<R, CC>(f, g, cp, c, i, mu);
@@ -486,7 +486,7 @@ __device__ inline int metro_u1(const Fields<R>& f, const Geom& g, const Coup& cp
 
 // metro_doublet (metropolis.c:77-106)
 template <typename R, int CC>
-__device__ inline int metro_doublet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
+__device__ inline int metro_doublet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
                                     int h, SiteRng<R>& rng) {
   Q<R> old = ld4<R>(php(f, h), i);
   R a0 = localact_doublet<R, CC>(f, g, cp, c, i, h);
@@ -504,7 +504,7 @@ __device__ inline int metro_doublet(const Fields<R>& f, const Geom& g, const Cou
 
 // overrelax_doublet (overrelax.c:54-128)
 template <typename R, int CC>
-__device__ inline int overrelax_doublet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
+__device__ inline int overrelax_doublet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
                                         SiteRng<R>& rng, int* fallback) {
   Q<R> s = staple_doublet<R, CC>(f, g, cp, c, i, 0);
   Q<R> p = ld4<R>(php(f, 0), i);
@@ -533,7 +533,7 @@ __device__ inline int overrelax_doublet(const Fields<R>& f, const Geom& g, const
 
 // overrelax_higgs2 (overrelax.c:295-417)
 template <typename R, int CC>
-__device__ inline int overrelax_higgs2(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
+__device__ inline int overrelax_higgs2(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
                                        int h, SiteRng<R>& rng, int* fallback) {
   Q<R> s = staple_doublet<R, CC>(f, g, cp, c, i, h);
   Q<R> fv = ld4<R>(php(f, h), i);
@@ -593,7 +593,7 @@ __device__ inline int overrelax_higgs2(const Fields<R>& f, const Geom& g, const 
 // overrelax_triplet (overrelax.c:137-236); no portal term in B (the
 // reference's "#ifdef HIGGS" there is never defined)
 template <typename R, int CC>
-__device__ inline int overrelax_triplet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
+__device__ inline int overrelax_triplet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
                                         SiteRng<R>& rng, int* fallback) {
   V3<R> s{(R)0, (R)0, (R)0};
 #pragma unroll
@@ -625,7 +625,7 @@ __device__ inline int overrelax_triplet(const Fields<R>& f, const Geom& g, const
 
 // metro_triplet (metropolis.c:113-143)
 template <typename R, int CC>
-__device__ inline int metro_triplet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
+__device__ inline int metro_triplet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
                                     SiteRng<R>& rng) {
   V3<R> old = ld3(f, i);
   R a0 = localact_triplet<R, CC>(f, g, cp, c, i);
@@ -642,7 +642,7 @@ __device__ inline int metro_triplet(const Fields<R>& f, const Geom& g, const Cou
 
 // localact_singlet (su2u1.c:688-705)
 template <typename R, int CC>
-__device__ inline R localact_singlet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i) {
+__device__ inline R localact_singlet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i) {
   R S = f.sing[i], res = (R)3 * S * S;
 #pragma unroll
   for (int d = 0; d < 3; d++) res -= S * (f.sing[shifted(g, c, d, 1)] + f.sing[shifted(g, c, d, -1)]);
@@ -652,7 +652,7 @@ __device__ inline R localact_singlet(const Fields<R>& f, const Geom& g, const Co
 
 // overrelax_singlet (overrelax.c:243-285)
 template <typename R, int CC>
-__device__ inline int overrelax_singlet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
+__device__ inline int overrelax_singlet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
                                         SiteRng<R>& rng, int* fallback) {
   R S = f.sing[i];
   R c1 = (R)cp.b1s;
@@ -681,7 +681,7 @@ __device__ inline int overrelax_singlet(const Fields<R>& f, const Geom& g, const
 
 // metro_singlet (metropolis.c:148-167)
 template <typename R, int CC>
-__device__ inline int metro_singlet(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i,
+__device__ inline int metro_singlet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
                                     SiteRng<R>& rng) {
   R old = f.sing[i];
   R a0 = localact_singlet<R, CC>(f, g, cp, c, i);
@@ -709,7 +709,8 @@ __device__ inline double orderparam_site(const Fields<R>& f, int op, int i) {
 // ---------------------------------------------------------------------------
 struct PassArgs {
   Geom g;
-  Coup cp;
+  CoupT<double> cpd;  // couplings for FP64 kernels
+  CoupT<float> cpf;   // the same for FP32 kernels
   RngKey rk;
   int parity;
   int sub;      // direction for links, doublet index for doublets
@@ -723,9 +724,16 @@ struct PassArgs {
   int* err;                 // device error flag
 };
 
+template <typename R>
+__device__ inline const CoupT<R>& coup(const PassArgs& a);
+template <>
+__device__ inline const CoupT<double>& coup<double>(const PassArgs& a) { return a.cpd; }
+template <>
+__device__ inline const CoupT<float>& coup<float>(const PassArgs& a) { return a.cpf; }
+
 template <typename R, int CC, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_link(Fields<R> f, PassArgs a) {
-  const Coup& cp = a.cp;
+  const CoupT<R>& cp = coup<R>(a);
   int t = a.t_lo + (int)blockIdx.x * blockDim.x + threadIdx.x;
   int acc = 0, cap = 0, err = 0;
   if (t < a.t_hi) {
@@ -743,7 +751,7 @@ __global__ void __launch_bounds__(BS, MINB) k_link(Fields<R> f, PassArgs a) {
 
 template <typename R, int CC, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_u1(Fields<R> f, PassArgs a) {
-  const Coup& cp = a.cp;
+  const CoupT<R>& cp = coup<R>(a);
   int t = a.t_lo + (int)blockIdx.x * blockDim.x + threadIdx.x;
   int acc = 0;
   if (t < a.t_hi) {
@@ -761,7 +769,7 @@ __global__ void __launch_bounds__(BS, MINB) k_u1(Fields<R> f, PassArgs a) {
 // sums of the order parameter over the new ones
 template <typename R, int CC, int FIELD, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_scalar(Fields<R> f, PassArgs a) {
-  const Coup& cp = a.cp;
+  const CoupT<R>& cp = coup<R>(a);
   int t = a.t_lo + (int)blockIdx.x * blockDim.x + threadIdx.x;
   int acc = 0, fb = 0;
   double opv = 0.0;
@@ -1078,7 +1086,7 @@ __device__ inline CM<R> project_u1(const Fields<R>& f, const Geom& g, const int*
 }
 // alpha_proj (magfield.c:189-216)
 template <typename R>
-__device__ inline R alpha_proj(const Fields<R>& f, const Geom& g, const Coup& cp, const int* c, int i, int d1,
+__device__ inline R alpha_proj(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i, int d1,
                                int d2) {
   int c1[3], c2[3];
   shift_coords(g, c, d1, 1, c1);
@@ -1094,7 +1102,7 @@ __device__ inline R alpha_proj(const Fields<R>& f, const Geom& g, const Coup& cp
 
 // alpha(x; 0,1), alpha(x; 0,2), alpha(x; 1,2) for every site
 template <typename R>
-__global__ void __launch_bounds__(BLOCK) k_alpha(Fields<R> f, Geom g, Coup cp, double* alpha) {
+__global__ void __launch_bounds__(BLOCK) k_alpha(Fields<R> f, Geom g, CoupT<R> cp, double* alpha) {
   int t = (int)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= g.V) return;
   int parity = t >= g.half;
@@ -1127,7 +1135,7 @@ __device__ inline bool sum_active(int k, int rt) {
 
 // per-site terms of measure() summed over the block into partials[k][block]
 template <typename R, int CC>
-__global__ void __launch_bounds__(BLOCK) k_measure(Fields<R> f, Geom g, Coup cp, const double* alpha,
+__global__ void __launch_bounds__(BLOCK) k_measure(Fields<R> f, Geom g, CoupT<R> cp, const double* alpha,
                                                    double* partials) {
   int t = (int)blockIdx.x * blockDim.x + threadIdx.x;
   double m[NSUMS];
@@ -1260,7 +1268,7 @@ __global__ void k_reduce_partials(const double* partials, int np, double* out) {
 // gradient flow (gradflow.c:190-414): forces from `in`, Euler step into `out`
 // ---------------------------------------------------------------------------
 template <typename R, int CC>
-__global__ void __launch_bounds__(BLOCK) k_flow(Fields<R> in, Fields<R> out, Geom g, Coup cp, R dt,
+__global__ void __launch_bounds__(BLOCK) k_flow(Fields<R> in, Fields<R> out, Geom g, CoupT<R> cp, R dt,
                                                 unsigned long long* first_zero) {
   int t = (int)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= g.V) return;
@@ -1271,7 +1279,7 @@ __global__ void __launch_bounds__(BLOCK) k_flow(Fields<R> in, Fields<R> out, Geo
 #pragma unroll
   for (int mu = 0; mu < 3; mu++) {
     // grad_force_link (gradflow.c:190-258)
-    Q<R> s = qscale(wilson_staple(in, g, c, i, mu), (R)(-cp.beta / 8.0));
+    Q<R> s = qscale(wilson_staple(in, g, c, i, mu), -cp.beta / (R)8);
     Q<R> U = ld4<R>(lk(in, mu), i);
     if (HAS(C_T)) {
       V3<R> a1 = ld3(in, i), a2 = ld3(in, shifted(g, c, mu, 1));
@@ -1286,7 +1294,7 @@ __global__ void __launch_bounds__(BLOCK) k_flow(Fields<R> in, Fields<R> out, Geo
     R z[3], mod = 0;
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-      fz[a] *= (R)(4.0 / cp.beta);
+      fz[a] *= (R)4 / cp.beta;
       z[a] = dt * fz[a];
       mod += z[a] * z[a];
     }

@@ -41,7 +41,7 @@ static __device__ __align__(256) double g_noalloc_partials[NSUMS * NOALLOC_MAX_B
 // of the magnetic charge computed where they are needed instead of being read
 // from a scratch plane of 3 V doubles.
 template <typename R>
-__global__ void __launch_bounds__(BLOCK) k_measure_noalloc(Fields<R> f, Geom g, Coup cp, double* partials) {
+__global__ void __launch_bounds__(BLOCK) k_measure_noalloc(Fields<R> f, Geom g, CoupT<R> cp, double* partials) {
   constexpr int CC = C_GENERIC;
   const bool has_u1 = SU2_HAS(CC, cp.content, C_U1), has_t = SU2_HAS(CC, cp.content, C_T),
              has_s = SU2_HAS(CC, cp.content, C_S);
@@ -255,7 +255,7 @@ extern "C" int su2gpu_measure_noalloc(const su2gpu_params* p, const su2gpu_devic
     f.phi[0] = (D4*)df->doublet[0];
     f.phi[1] = (D4*)df->doublet[1];
     f.sing = (double*)df->singlet;
-    k_measure_noalloc<double><<<nb, BLOCK, 0, st>>>(f, g, cp, scratch);
+    k_measure_noalloc<double><<<nb, BLOCK, 0, st>>>(f, g, coup_as<double>(cp), scratch);
   } else {
     Fields<float> f;
     memset(&f, 0, sizeof(f));
@@ -267,7 +267,7 @@ extern "C" int su2gpu_measure_noalloc(const su2gpu_params* p, const su2gpu_devic
     f.phi[0] = (F4*)df->doublet[0];
     f.phi[1] = (F4*)df->doublet[1];
     f.sing = (float*)df->singlet;
-    k_measure_noalloc<float><<<nb, BLOCK, 0, st>>>(f, g, cp, scratch);
+    k_measure_noalloc<float><<<nb, BLOCK, 0, st>>>(f, g, coup_as<float>(cp), scratch);
   }
   if ((e = cudaGetLastError()) != cudaSuccess) return noalloc_fail(SU2GPU_ERR_CUDA, cudaGetErrorString(e));
   launch_reduce_partials(scratch, (int)nb, device_sums, st);

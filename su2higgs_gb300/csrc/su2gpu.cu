@@ -505,7 +505,8 @@ static int enqueue_sweep(su2gpu_ctx* c, int64_t* tot) {
   PassArgs base;
   memset(&base, 0, sizeof(base));
   base.g = c->g;
-  base.cp = c->cp;
+  base.cpd = coup_as<double>(c->cp);
+  base.cpf = coup_as<float>(c->cp);
   base.rk = RngKey{(uint32_t)c->seed, (uint32_t)(c->seed >> 32), c->chain, c->d_sweep};
   base.ctr = c->d_ctr;
   base.err = c->d_err;
@@ -725,7 +726,8 @@ int su2gpu_run_halfsweep(su2gpu_ctx* c, int32_t kind, int32_t parity, int32_t su
   PassArgs a;
   memset(&a, 0, sizeof(a));
   a.g = c->g;
-  a.cp = c->cp;
+  a.cpd = coup_as<double>(c->cp);
+  a.cpf = coup_as<float>(c->cp);
   a.rk = RngKey{(uint32_t)c->seed, (uint32_t)(c->seed >> 32), c->chain, c->d_sweep};
   a.ctr = c->d_ctr;
   a.err = c->d_err;
@@ -777,7 +779,8 @@ int su2gpu_autotune(su2gpu_ctx* c, int32_t* choices, float* best_ms) {
   PassArgs a;
   memset(&a, 0, sizeof(a));
   a.g = c->g;
-  a.cp = c->cp;
+  a.cpd = coup_as<double>(c->cp);
+  a.cpf = coup_as<float>(c->cp);
   a.rk = RngKey{(uint32_t)c->seed ^ 0x5eedu, (uint32_t)(c->seed >> 32), c->chain, (uint32_t*)((char*)ctr.p + 1024)};
   a.ctr = (unsigned long long*)ctr.p;
   a.err = (int*)((char*)ctr.p + 512);
