@@ -74,7 +74,9 @@ def build(verbose=False, force=False, jobs=None):
         obj = os.path.join(BUILD, name + ".o")
         if not force and not _stale(obj, deps):
             return obj
-        extra = FP32_FLAGS if "SU2_R=float" in defs else []
+        # the allocation-free unit instantiates FP32 kernels too: same FP32 flags
+        # (they change single-precision arithmetic only)
+        extra = FP32_FLAGS if ("SU2_R=float" in defs or name == "su2_noalloc") else []
         cmd = [exe] + NVCC_FLAGS + extra + ["-D" + d for d in defs] + ["-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)
