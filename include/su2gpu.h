@@ -252,6 +252,61 @@ int su2gpu_set_variants(su2gpu_ctx* ctx, const int32_t* choices);
 int su2gpu_host_register(void* ptr, int64_t bytes);
 int su2gpu_host_unregister(void* ptr);
 
+/* ---- pools of independent chains (batched and served forms) ----
+ * A pool holds many independent Markov chains of one field content,
+ * precision and update recipe (algorithms and update counts), each with its
+ * own lattice size, couplings, seed, chain id and sweep counter, in one
+ * device arena.  Each half-sweep of the update_lattice() sequence
+ * (update.c:270-430) is one launch over every chain of the pool, and a sweep
+ * of the whole pool is replayed as one CUDA graph until the membership
+ * changes.  A chain of a pool follows exactly the trajectory a single-lattice
+ * context with the same parameters, seed and chain id follows (same random
+ * numbers, same fields bit for bit).  Multicanonical weighting is not
+ * available in pools.  The reference runs one chain per process: these have
+ * no counterpart there. */
+typedef struct su2gpu_pool su2gpu_pool;
+/* Device bytes one chain of these parameters takes in a pool's arena. */
+int64_t su2gpu_pool_chain_bytes(const su2gpu_params* p);
+/* A pool for chains of `recipe`'s content / precision / algorithms / update
+ * counts, with an arena of `arena_bytes` device bytes and at most
+ * `max_chains` chains. */
+int su2gpu_pool_create(const su2gpu_params* recipe, int64_t arena_bytes, int32_t max_chains, su2gpu_pool** out);
+int su2gpu_pool_destroy(su2gpu_pool* pool);
+/* Admit a chain (cold start, sweep counter 0).  SU2GPU_ERR_CAPACITY when the
+ * arena or the slot table is full; SU2GPU_ERR_INVALID when the recipe
+ * differs from the pool's.  *slot receives the chain's slot. */
+int su2gpu_pool_add(su2gpu_pool* pool, const su2gpu_params* p, uint64_t seed, uint32_t chain, int32_t* slot);
+/* Retire a chain: its arena bytes and slot become free. */
+int su2gpu_pool_remove(su2gpu_pool* pool, int32_t slot);
+/* Chains, arena bytes in use, free, and the largest free extent. */
+int su2gpu_pool_info(su2gpu_pool* pool, int32_t* nactive, int64_t* used_bytes, int64_t* free_bytes,
+                     int64_t* largest_free);
+/* Active slots in increasing order (up to `max`); *n = their number. */
+int su2gpu_pool_active(su2gpu_pool* pool, int32_t* slots, int32_t max, int32_t* n);
+/* Host fields of one chain, in the reference's site order and layout (as
+ * su2gpu_upload_fields / su2gpu_download_fields). */
+int su2gpu_pool_upload(su2gpu_pool* pool, int32_t slot, const double* link, const double* u1, const double* doublet0,
+                       const double* doublet1, const double* triplet, const double* singlet);
+int su2gpu_pool_download(su2gpu_pool* pool, int32_t slot, double* link, double* u1, double* doublet0,
+                         double* doublet1, double* triplet, double* singlet);
+/* Set one chain's sweep counter (the random stream's sweep index). */
+int su2gpu_pool_set_sweep(su2gpu_pool* pool, int32_t slot, uint32_t sweep);
+/* `nsweeps` sweeps of every active chain; each chain's sweep counter
+ * advances by one per sweep.  use_graph != 0 replays one captured sweep. */
+int su2gpu_pool_run(su2gpu_pool* pool, int32_t nsweeps, int32_t use_graph);
+/* measure() sums of every active chain, in slot order:
+ * sums[k * SU2GPU_NMEAS + m] for the k-th active chain. */
+int su2gpu_pool_measure(su2gpu_pool* pool, double* sums, int32_t max_chains, int32_t* nchains);
+/* One chain's counters (SU2GPU_NCOUNTERS, as su2gpu_get_counters). */
+int su2gpu_pool_counters(su2gpu_pool* pool, int32_t slot, int64_t* out);
+/* Launch-shape autotuner over the pool's current chains (as su2gpu_autotune;
+ * runs on a scratch copy, the chains do not advance). */
+int su2gpu_pool_autotune(su2gpu_pool* pool, int32_t* choices, float* best_ms);
+int su2gpu_pool_set_variants(su2gpu_pool* pool, const int32_t* choices);
+/* Gradient flow of one chain (as su2gpu_grad_flow; the chain is unchanged). */
+int su2gpu_pool_grad_flow(su2gpu_pool* pool, int32_t slot, double t_max, double dt, int32_t meas_interval,
+                          double* rows, int32_t maxrows, int32_t* nrows);
+
 /* ---- allocation-free measurement ----
  * Device pointers to fields in the library's device layout (parity-split
  * structure of arrays, EVEN sites first): link[d] and doublet[h] are V

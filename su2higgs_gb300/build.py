@@ -37,6 +37,7 @@ UNITS = [
     ("inst_f32_su2u1s", "su2_inst.cu", ["SU2_R=float", "SU2_CC=25", "SU2_OPS=ops_f32_su2u1s"]),
     ("su2gpu", "su2gpu.cu", []),
     ("su2_noalloc", "su2_noalloc.cu", []),
+    ("su2_pool", "su2_pool.cu", []),
 ]
 EXTRA_SOURCES = []  # (name, source) of further host units, appended by later modules
 

@@ -35,6 +35,8 @@ template <typename R> struct Variant<R, 0> { static constexpr int BS = 128, MINB
 template <typename R> struct Variant<R, 1> { static constexpr int BS = 128, MINB = sizeof(R) == 4 ? 5 : 3; };
 template <typename R> struct Variant<R, 2> { static constexpr int BS = 256, MINB = sizeof(R) == 4 ? 4 : 2; };
 template <typename R> struct Variant<R, 3> { static constexpr int BS = 64, MINB = sizeof(R) == 4 ? 12 : 6; };
+// threads per block of each variant, for host code that builds tile tables
+constexpr int kVariantBS[NVARIANTS] = {128, 128, 256, 64};
 constexpr int NSUMS = 24;
 
 // ---------------------------------------------------------------------------

@@ -9,6 +9,7 @@
 namespace su2 {
 
 struct PassArgs;
+struct PoolArgs;
 
 // The update launchers take a launch-shape variant (0..NVARIANTS-1, see
 // Variant in su2_kernels.cuh) and the site range in the PassArgs; they return
@@ -23,6 +24,12 @@ struct Ops {
                   unsigned nblocks, cudaStream_t st);
   void (*flow)(const void* fin, const void* fout, const Geom& g, const Coup& cp, double dt,
                unsigned long long* first_zero, unsigned nblocks, cudaStream_t st);
+  // pools of chains (su2_pool.cuh): nblocks = length of the tile table, which
+  // must have been built for the variant's block size
+  void (*pool_link)(int variant, const PoolArgs& a, unsigned nblocks, cudaStream_t st);
+  void (*pool_u1)(int variant, const PoolArgs& a, unsigned nblocks, cudaStream_t st);
+  void (*pool_scalar)(int variant, int field, const PoolArgs& a, unsigned nblocks, cudaStream_t st);
+  void (*pool_measure)(const PoolArgs& a, double* partials, unsigned nblocks, cudaStream_t st);
 };
 
 struct PrecOps {
@@ -48,5 +55,8 @@ void launch_muca_decide(MucaDev* w, const double* partials, int np, double vol, 
                         uint32_t pass, uint32_t check, unsigned long long* ctr, cudaStream_t st);
 void launch_muca_set_param(MucaDev* w, const double* partials, int np, double vol, int parity, cudaStream_t st);
 void launch_reduce_partials(const double* partials, int np, double* out, cudaStream_t st);
+void launch_pool_reduce(const double* partials, int nblocks, const int* first, int nchains, double* out,
+                        cudaStream_t st);
+void launch_pool_next_sweep(uint32_t* const* sweeps, int n, cudaStream_t st);
 
 }  // namespace su2

@@ -1,0 +1,628 @@
+// su2_pool.cu -- pools of independent chains (the batched and served forms):
+// chains of one field content, precision and update recipe with their own
+// lattice sizes, couplings, seeds and sweep counters, resident in one device
+// arena.  Every half-sweep of update_lattice() (update.c:270-430) is a single
+// launch over all chains; a sweep of the whole pool is replayed as one CUDA
+// graph until the membership changes.  Admission is by device footprint: a
+// chain is accepted when its fields fit in the arena.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdarg>
+#include <cstring>
+#include <vector>
+
+#include "su2_host.h"
+#include "su2_pool.cuh"
+
+using namespace su2;
+
+namespace {
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  su2gpu_record_error(buf);
+  return code;
+}
+
+#define PCK(call)                                                                               \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess) return fail(SU2GPU_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+struct Buf {
+  void* p = nullptr;
+  size_t n = 0;
+  int ensure(size_t bytes) {
+    if (bytes <= n) return 0;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) return fail(SU2GPU_ERR_NOMEM, "cudaMalloc(%zu) failed", bytes);
+    n = bytes;
+    return 0;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+__global__ void k_cold_links4f(F4* p, int64_t n) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) p[k] = F4{1.f, 0.f, 0.f, 0.f};
+}
+__global__ void k_cold_links4d(D4* p, int64_t n) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) p[k] = D4{1.0, 0.0, 0.0, 0.0};
+}
+
+struct Slot {
+  bool active = false;
+  su2gpu_params p;
+  Geom g;
+  Coup cp;
+  size_t off = 0, bytes = 0;
+  uint64_t seed = 0;
+  uint32_t chain = 0;
+  int64_t tot[SU2GPU_NCOUNTERS] = {0};
+};
+
+}  // namespace
+
+struct su2gpu_pool {
+  su2gpu_params recipe;
+  int prec, content;
+  const Ops* ops;
+  const PrecOps* pops;
+  cudaStream_t st = nullptr;
+  Buf arena;
+  std::vector<std::pair<size_t, size_t>> free_list;  // (offset, length), sorted by offset
+  std::vector<Slot> slots;
+  int max_slots;
+  Buf slotmem;   // per slot: sweep counter word + 24 counters
+  Buf descs;     // ChainDesc<R>[max_slots]
+  Buf tiles[NVARIANTS], mtiles, mfirst, sweepptrs, partials, sums, stage, err;
+  int ntiles[NVARIANTS] = {0, 0, 0, 0}, nmtiles = 0;
+  std::vector<int> active;  // active slots in slot order
+  bool dirty = true;
+  cudaGraphExec_t gexec = nullptr;
+  int var[5] = {0, 0, 0, 0, 0};
+  int64_t sweep_passes[SU2GPU_NCOUNTERS] = {0};  // half-sweeps of each kind in one sweep (graph replay)
+  size_t rsize() const { return prec == 64 ? 8 : 4; }
+};
+
+namespace {
+
+int arena_alloc(su2gpu_pool* P, size_t bytes, size_t* off) {
+  for (size_t k = 0; k < P->free_list.size(); k++) {
+    auto& fr = P->free_list[k];
+    if (fr.second >= bytes) {
+      *off = fr.first;
+      fr.first += bytes;
+      fr.second -= bytes;
+      if (!fr.second) P->free_list.erase(P->free_list.begin() + k);
+      return 0;
+    }
+  }
+  return -1;
+}
+
+void arena_free(su2gpu_pool* P, size_t off, size_t bytes) {
+  P->free_list.push_back({off, bytes});
+  std::sort(P->free_list.begin(), P->free_list.end());
+  std::vector<std::pair<size_t, size_t>> merged;
+  for (auto& fr : P->free_list) {
+    if (!merged.empty() && merged.back().first + merged.back().second == fr.first) merged.back().second += fr.second;
+    else merged.push_back(fr);
+  }
+  P->free_list.swap(merged);
+}
+
+template <typename R>
+ChainDesc<R> make_desc(su2gpu_pool* P, int s, char* arena_base, char* slot_base) {
+  const Slot& sl = P->slots[s];
+  ChainDesc<R> d;
+  memset(&d, 0, sizeof(d));
+  carve(d.f, arena_base + sl.off, &sl.p, sl.g.V);
+  d.g = sl.g;
+  d.cp = coup_as<R>(sl.cp);
+  d.k0 = (uint32_t)sl.seed;
+  d.k1 = (uint32_t)(sl.seed >> 32);
+  d.chain = sl.chain;
+  d.sweep = (uint32_t*)(slot_base + (size_t)s * 256);
+  d.ctr = (unsigned long long*)(slot_base + (size_t)s * 256 + 32);
+  return d;
+}
+
+// descriptors and tile tables for the current membership
+int rebuild(su2gpu_pool* P, void* arena_base = nullptr, void* slot_base = nullptr, void* descs = nullptr) {
+  char* ab = (char*)(arena_base ? arena_base : P->arena.p);
+  char* sb = (char*)(slot_base ? slot_base : P->slotmem.p);
+  void* dd = descs ? descs : P->descs.p;
+  P->active.clear();
+  for (int s = 0; s < (int)P->slots.size(); s++)
+    if (P->slots[s].active) P->active.push_back(s);
+  size_t dsz = P->prec == 64 ? sizeof(ChainDesc<double>) : sizeof(ChainDesc<float>);
+  std::vector<unsigned char> hd(dsz * P->max_slots, 0);
+  for (int s : P->active) {
+    if (P->prec == 64) {
+      ChainDesc<double> d = make_desc<double>(P, s, ab, sb);
+      memcpy(hd.data() + dsz * s, &d, dsz);
+    } else {
+      ChainDesc<float> d = make_desc<float>(P, s, ab, sb);
+      memcpy(hd.data() + dsz * s, &d, dsz);
+    }
+  }
+  PCK(cudaMemcpyAsync(dd, hd.data(), hd.size(), cudaMemcpyHostToDevice, P->st));
+  if (!descs) {
+    for (int v = 0; v < NVARIANTS; v++) {
+      std::vector<int2> t;
+      int bs = kVariantBS[v];
+      for (int s : P->active)
+        for (int t0 = 0; t0 < P->slots[s].g.half; t0 += bs) t.push_back(int2{s, t0});
+      P->ntiles[v] = (int)t.size();
+      if (int rc = P->tiles[v].ensure(std::max<size_t>(t.size(), 1) * sizeof(int2))) return rc;
+      if (!t.empty()) PCK(cudaMemcpyAsync(P->tiles[v].p, t.data(), t.size() * sizeof(int2), cudaMemcpyHostToDevice, P->st));
+    }
+    std::vector<int2> mt;
+    std::vector<int> first;
+    std::vector<uint32_t*> sp;
+    for (int s : P->active) {
+      first.push_back((int)mt.size());
+      for (int t0 = 0; t0 < P->slots[s].g.V; t0 += BLOCK) mt.push_back(int2{s, t0});
+      sp.push_back((uint32_t*)(sb + (size_t)s * 256));
+    }
+    first.push_back((int)mt.size());
+    P->nmtiles = (int)mt.size();
+    int rc;
+    if ((rc = P->mtiles.ensure(std::max<size_t>(mt.size(), 1) * sizeof(int2))) ||
+        (rc = P->mfirst.ensure(first.size() * sizeof(int))) ||
+        (rc = P->sweepptrs.ensure(std::max<size_t>(sp.size(), 1) * sizeof(void*))) ||
+        (rc = P->partials.ensure(std::max<size_t>(mt.size(), 1) * NSUMS * 8)) ||
+        (rc = P->sums.ensure(std::max<size_t>(P->active.size(), 1) * NSUMS * 8)))
+      return rc;
+    if (!mt.empty()) PCK(cudaMemcpyAsync(P->mtiles.p, mt.data(), mt.size() * sizeof(int2), cudaMemcpyHostToDevice, P->st));
+    PCK(cudaMemcpyAsync(P->mfirst.p, first.data(), first.size() * sizeof(int), cudaMemcpyHostToDevice, P->st));
+    if (!sp.empty()) PCK(cudaMemcpyAsync(P->sweepptrs.p, sp.data(), sp.size() * sizeof(void*), cudaMemcpyHostToDevice, P->st));
+    if (P->gexec) {
+      cudaGraphExecDestroy(P->gexec);
+      P->gexec = nullptr;
+    }
+    P->dirty = false;
+  }
+  PCK(cudaStreamSynchronize(P->st));
+  return SU2GPU_OK;
+}
+
+// one sweep of every active chain (update.c:270-430 order); `tot` receives the
+// per-chain half-site totals of one sweep
+int enqueue_pool_sweep(su2gpu_pool* P, const void* descs, const int2* const* tiles, unsigned long long* unused,
+                       int64_t* tot) {
+  (void)unused;
+  const su2gpu_params& p = P->recipe;
+  PoolArgs a;
+  memset(&a, 0, sizeof(a));
+  a.descs = descs;
+  a.err = (int*)P->err.p;
+  uint32_t pass = 0;
+  const int nh = nhiggs_of(p.content);
+  auto vt = [&](int kind) { return P->var[kind]; };
+  for (int k = 0; k < p.update_links; k++) {
+    for (int mu = 0; mu < 3; mu++)
+      for (int par = 0; par <= 1; par++) {
+        a.parity = par; a.sub = mu; a.alg = p.algorithm_su2link; a.pass = pass++;
+        a.tiles = tiles[vt(0)];
+        P->ops->pool_link(vt(0), a, P->ntiles[vt(0)], P->st);
+        tot[SU2GPU_C_TOTAL_SU2LINK] += 1;
+      }
+    if (p.content & SU2GPU_U1)
+      for (int mu = 0; mu < 3; mu++)
+        for (int par = 0; par <= 1; par++) {
+          a.parity = par; a.sub = mu; a.alg = 0; a.pass = pass++;
+          a.tiles = tiles[vt(1)];
+          P->ops->pool_u1(vt(1), a, P->ntiles[vt(1)], P->st);
+          tot[SU2GPU_C_TOTAL_U1LINK] += 1;
+        }
+  }
+  int nsweeps = p.scalar_sweeps + 1;
+  for (int s = 0; s < nsweeps; s++) {
+    struct F { int field, count, alg; };
+    F fields[3] = {{0, nh > 0 ? p.update_su2doublet : 0, p.algorithm_su2doublet},
+                   {1, (p.content & SU2GPU_TRIPLET) ? p.update_su2triplet : 0, p.algorithm_su2triplet},
+                   {2, (p.content & SU2GPU_SINGLET) ? p.update_singlet : 0, p.algorithm_singlet}};
+    for (const F& fd : fields)
+      for (int k = 0; k < fd.count; k++) {
+        int force = 0;
+        if (s >= nsweeps - 1) {
+          if (fd.alg == SU2GPU_OVERRELAX) force = 1;
+          else continue;
+        }
+        int nrep = fd.field == 0 ? nh : 1;
+        for (int h = 0; h < nrep; h++)
+          for (int par = 0; par <= 1; par++) {
+            a.parity = par; a.sub = h; a.alg = force; a.pass = pass++;
+            int kind = 2 + fd.field;
+            a.tiles = tiles[vt(kind)];
+            P->ops->pool_scalar(vt(kind), fd.field, a, P->ntiles[vt(kind)], P->st);
+            bool orr = fd.alg == SU2GPU_OVERRELAX && !force;
+            int idx = fd.field == 0 ? (orr ? SU2GPU_C_TOTAL_OR_DOUBLET : SU2GPU_C_TOTAL_DOUBLET) + h
+                                    : (fd.field == 1 ? (orr ? SU2GPU_C_TOTAL_OR_TRIPLET : SU2GPU_C_TOTAL_TRIPLET)
+                                                     : (orr ? SU2GPU_C_TOTAL_OR_SINGLET : SU2GPU_C_TOTAL_SINGLET));
+            tot[idx] += 1;
+          }
+      }
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(SU2GPU_ERR_CUDA, "pool sweep launch: %s", cudaGetErrorString(e));
+  return SU2GPU_OK;
+}
+
+bool same_recipe(const su2gpu_params* a, const su2gpu_params* b) {
+  return a->content == b->content && a->precision == b->precision && a->algorithm_su2link == b->algorithm_su2link &&
+         a->algorithm_u1link == b->algorithm_u1link && a->algorithm_su2doublet == b->algorithm_su2doublet &&
+         a->algorithm_su2triplet == b->algorithm_su2triplet && a->algorithm_singlet == b->algorithm_singlet &&
+         a->update_links == b->update_links && a->scalar_sweeps == b->scalar_sweeps &&
+         a->update_su2doublet == b->update_su2doublet && a->update_su2triplet == b->update_su2triplet &&
+         a->update_singlet == b->update_singlet;
+}
+
+}  // namespace
+
+extern "C" {
+
+int64_t su2gpu_pool_chain_bytes(const su2gpu_params* p) {
+  if (!p || p->dim != 3) return -1;
+  for (int d = 0; d < 3; d++)
+    if (p->L[d] < 2 || (p->L[d] & 1)) return -1;
+  return (int64_t)field_bytes(p, (int64_t)p->L[0] * p->L[1] * p->L[2]);
+}
+
+int su2gpu_pool_create(const su2gpu_params* recipe, int64_t arena_bytes, int32_t max_chains, su2gpu_pool** out) {
+  if (!recipe || !out || arena_bytes <= 0 || max_chains <= 0) return fail(SU2GPU_ERR_INVALID, "bad pool arguments");
+  if (recipe->precision != 64 && recipe->precision != 32) return fail(SU2GPU_ERR_INVALID, "precision must be 64 or 32");
+  if ((recipe->content & SU2GPU_HIGGS1) && (recipe->content & SU2GPU_HIGGS2))
+    return fail(SU2GPU_ERR_INVALID, "HIGGS1 and HIGGS2 are exclusive");
+  if (recipe->algorithm_su2link != SU2GPU_HEATBATH && recipe->algorithm_su2link != SU2GPU_METROPOLIS)
+    return fail(SU2GPU_ERR_INVALID, "algorithm_su2link must be heatbath or metropolis");
+  su2gpu_pool* P = new su2gpu_pool();
+  P->recipe = *recipe;
+  P->prec = recipe->precision;
+  P->content = recipe->content & 0x1f;
+  P->ops = pick_ops(P->prec, P->content);
+  P->pops = P->prec == 64 ? &precops_f64 : &precops_f32;
+  P->max_slots = max_chains;
+  P->slots.resize(max_chains);
+  int rc;
+  if (cudaStreamCreateWithFlags(&P->st, cudaStreamNonBlocking) != cudaSuccess) {
+    delete P;
+    return fail(SU2GPU_ERR_CUDA, "cudaStreamCreate failed");
+  }
+  size_t dsz = P->prec == 64 ? sizeof(ChainDesc<double>) : sizeof(ChainDesc<float>);
+  if ((rc = P->arena.ensure((size_t)arena_bytes)) || (rc = P->slotmem.ensure((size_t)max_chains * 256)) ||
+      (rc = P->descs.ensure(dsz * max_chains)) || (rc = P->err.ensure(256))) {
+    su2gpu_pool_destroy(P);
+    return rc;
+  }
+  P->free_list.push_back({0, (size_t)arena_bytes});
+  cudaMemsetAsync(P->slotmem.p, 0, P->slotmem.n, P->st);
+  cudaMemsetAsync(P->err.p, 0, P->err.n, P->st);
+  if (cudaStreamSynchronize(P->st) != cudaSuccess) {
+    su2gpu_pool_destroy(P);
+    return fail(SU2GPU_ERR_CUDA, "pool initialisation failed");
+  }
+  *out = P;
+  return SU2GPU_OK;
+}
+
+int su2gpu_pool_destroy(su2gpu_pool* P) {
+  if (!P) return SU2GPU_OK;
+  if (P->st) cudaStreamSynchronize(P->st);
+  if (P->gexec) cudaGraphExecDestroy(P->gexec);
+  P->arena.release(); P->slotmem.release(); P->descs.release(); P->mtiles.release(); P->mfirst.release();
+  P->sweepptrs.release(); P->partials.release(); P->sums.release(); P->stage.release(); P->err.release();
+  for (int v = 0; v < NVARIANTS; v++) P->tiles[v].release();
+  if (P->st) cudaStreamDestroy(P->st);
+  delete P;
+  return SU2GPU_OK;
+}
+
+int su2gpu_pool_add(su2gpu_pool* P, const su2gpu_params* p, uint64_t seed, uint32_t chain, int32_t* slot_out) {
+  if (!P || !p || !slot_out) return fail(SU2GPU_ERR_INVALID, "null argument");
+  if (!same_recipe(&P->recipe, p)) return fail(SU2GPU_ERR_INVALID, "chain recipe (content, precision, algorithms, update counts) differs from the pool's");
+  if (p->dim != 3) return fail(SU2GPU_ERR_INVALID, "only dim 3 is supported");
+  for (int d = 0; d < 3; d++)
+    if (p->L[d] < 2 || (p->L[d] & 1)) return fail(SU2GPU_ERR_INVALID, "side lengths must be even and >= 2");
+  int64_t V = (int64_t)p->L[0] * p->L[1] * p->L[2];
+  if (V * 3 >= 2147483647LL) return fail(SU2GPU_ERR_INVALID, "lattice too large");
+  int s = -1;
+  for (int k = 0; k < P->max_slots; k++)
+    if (!P->slots[k].active) { s = k; break; }
+  if (s < 0) return fail(SU2GPU_ERR_CAPACITY, "pool has no free chain slot (%d)", P->max_slots);
+  size_t bytes = field_bytes(p, V), off = 0;
+  if (arena_alloc(P, bytes, &off)) return fail(SU2GPU_ERR_CAPACITY, "chain of %zu bytes does not fit in the arena", bytes);
+  Slot& sl = P->slots[s];
+  sl = Slot();
+  sl.active = true;
+  sl.p = *p;
+  for (int d = 0; d < 3; d++) sl.g.L[d] = p->L[d];
+  sl.g.hL0 = p->L[0] / 2;
+  sl.g.V = (int)V;
+  sl.g.half = (int)(V / 2);
+  sl.cp = make_coup(p);
+  sl.off = off;
+  sl.bytes = bytes;
+  sl.seed = seed;
+  sl.chain = chain;
+  char* base = (char*)P->arena.p + off;
+  PCK(cudaMemsetAsync(base, 0, bytes, P->st));
+  PCK(cudaMemsetAsync((char*)P->slotmem.p + (size_t)s * 256, 0, 256, P->st));
+  // cold links (setsu2, init.c:18-28): the three link arrays lead the chain's block
+  size_t lbytes = align256((size_t)V * 4 * P->rsize());
+  for (int d = 0; d < 3; d++) {
+    if (P->prec == 64) k_cold_links4d<<<(unsigned)((V + 255) / 256), 256, 0, P->st>>>((D4*)(base + d * lbytes), V);
+    else k_cold_links4f<<<(unsigned)((V + 255) / 256), 256, 0, P->st>>>((F4*)(base + d * lbytes), V);
+  }
+  PCK(cudaGetLastError());
+  PCK(cudaStreamSynchronize(P->st));
+  P->dirty = true;
+  *slot_out = s;
+  return SU2GPU_OK;
+}
+
+int su2gpu_pool_remove(su2gpu_pool* P, int32_t s) {
+  if (!P || s < 0 || s >= P->max_slots || !P->slots[s].active) return fail(SU2GPU_ERR_INVALID, "no such chain slot");
+  PCK(cudaStreamSynchronize(P->st));
+  arena_free(P, P->slots[s].off, P->slots[s].bytes);
+  P->slots[s].active = false;
+  P->dirty = true;
+  return SU2GPU_OK;
+}
+
+int su2gpu_pool_info(su2gpu_pool* P, int32_t* nactive, int64_t* used_bytes, int64_t* free_bytes, int64_t* largest_free) {
+  if (!P) return SU2GPU_ERR_INVALID;
+  int n = 0;
+  int64_t used = 0;
+  for (auto& sl : P->slots)
+    if (sl.active) { n++; used += sl.bytes; }
+  int64_t fr = 0, big = 0;
+  for (auto& f : P->free_list) { fr += f.second; big = std::max<int64_t>(big, f.second); }
+  if (nactive) *nactive = n;
+  if (used_bytes) *used_bytes = used;
+  if (free_bytes) *free_bytes = fr;
+  if (largest_free) *largest_free = big;
+  return SU2GPU_OK;
+}
+
+static int slot_transfer(su2gpu_pool* P, int32_t s, int upload, double* link, double* u1, double* d0, double* d1,
+                         double* trip, double* sing) {
+  if (!P || s < 0 || s >= P->max_slots || !P->slots[s].active) return fail(SU2GPU_ERR_INVALID, "no such chain slot");
+  const Slot& sl = P->slots[s];
+  int64_t V = sl.g.V;
+  int rc = P->stage.ensure((size_t)V * 12 * 8);
+  if (rc) return rc;
+  Fields<double> f64;
+  Fields<float> f32;
+  char* base = (char*)P->arena.p + sl.off;
+  if (P->prec == 64) carve(f64, base, &sl.p, V);
+  else carve(f32, base, &sl.p, V);
+  const void* F = P->prec == 64 ? (const void*)&f64 : (const void*)&f32;
+  int nh = nhiggs_of(P->content);
+  struct Item { double* h; int kind, hid; size_t n; bool present; };
+  Item items[] = {{link, 0, 0, (size_t)V * 12, true},
+                  {u1, 1, 0, (size_t)V * 3, (bool)(P->content & SU2GPU_U1)},
+                  {d0, 2, 0, (size_t)V * 4, nh > 0},
+                  {d1, 2, 1, (size_t)V * 4, nh > 1},
+                  {trip, 3, 0, (size_t)V * 3, (bool)(P->content & SU2GPU_TRIPLET)},
+                  {sing, 4, 0, (size_t)V, (bool)(P->content & SU2GPU_SINGLET)}};
+  double* st = (double*)P->stage.p;
+  for (const Item& it : items) {
+    if (!it.present || !it.h) continue;
+    if (upload) {
+      PCK(cudaMemcpyAsync(st, it.h, it.n * 8, cudaMemcpyHostToDevice, P->st));
+      P->pops->import(F, V, it.kind, it.hid, st, P->st);
+    } else {
+      P->pops->exportf(F, V, it.kind, it.hid, st, P->st);
+      PCK(cudaMemcpyAsync(it.h, st, it.n * 8, cudaMemcpyDeviceToHost, P->st));
+    }
+    PCK(cudaStreamSynchronize(P->st));
+  }
+  return SU2GPU_OK;
+}
+
+int su2gpu_pool_upload(su2gpu_pool* P, int32_t s, const double* link, const double* u1, const double* d0,
+                       const double* d1, const double* trip, const double* sing) {
+  return slot_transfer(P, s, 1, (double*)link, (double*)u1, (double*)d0, (double*)d1, (double*)trip, (double*)sing);
+}
+
+int su2gpu_pool_download(su2gpu_pool* P, int32_t s, double* link, double* u1, double* d0, double* d1, double* trip,
+                         double* sing) {
+  return slot_transfer(P, s, 0, link, u1, d0, d1, trip, sing);
+}
+
+int su2gpu_pool_set_sweep(su2gpu_pool* P, int32_t s, uint32_t sweep) {
+  if (!P || s < 0 || s >= P->max_slots || !P->slots[s].active) return fail(SU2GPU_ERR_INVALID, "no such chain slot");
+  PCK(cudaMemcpyAsync((char*)P->slotmem.p + (size_t)s * 256, &sweep, 4, cudaMemcpyHostToDevice, P->st));
+  PCK(cudaStreamSynchronize(P->st));
+  return SU2GPU_OK;
+}
+
+int su2gpu_pool_run(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
+  if (!P || nsweeps < 0) return SU2GPU_ERR_INVALID;
+  int rc;
+  if (P->dirty && (rc = rebuild(P))) return rc;
+  if (P->active.empty() || !nsweeps) return SU2GPU_OK;
+  const int2* tiles[NVARIANTS];
+  for (int v = 0; v < NVARIANTS; v++) tiles[v] = (const int2*)P->tiles[v].p;
+  int64_t tot[SU2GPU_NCOUNTERS] = {0};
+  if (use_graph) {
+    if (!P->gexec) {
+      cudaGraph_t graph;
+      PCK(cudaStreamBeginCapture(P->st, cudaStreamCaptureModeThreadLocal));
+      rc = enqueue_pool_sweep(P, P->descs.p, tiles, nullptr, tot);
+      launch_pool_next_sweep((uint32_t* const*)P->sweepptrs.p, (int)P->active.size(), P->st);
+      cudaError_t e = cudaStreamEndCapture(P->st, &graph);
+      if (rc) return rc;
+      if (e != cudaSuccess) return fail(SU2GPU_ERR_CUDA, "pool graph capture: %s", cudaGetErrorString(e));
+      e = cudaGraphInstantiate(&P->gexec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (e != cudaSuccess) return fail(SU2GPU_ERR_CUDA, "pool graph instantiate: %s", cudaGetErrorString(e));
+      memcpy(P->sweep_passes, tot, sizeof(tot));
+    }
+    for (int k = 0; k < nsweeps; k++) PCK(cudaGraphLaunch(P->gexec, P->st));
+    memcpy(tot, P->sweep_passes, sizeof(tot));
+  } else {
+    for (int k = 0; k < nsweeps; k++) {
+      int64_t t1[SU2GPU_NCOUNTERS] = {0};
+      if ((rc = enqueue_pool_sweep(P, P->descs.p, tiles, nullptr, t1))) return rc;
+      launch_pool_next_sweep((uint32_t* const*)P->sweepptrs.p, (int)P->active.size(), P->st);
+      if (k == 0) memcpy(tot, t1, sizeof(t1));
+    }
+  }
+  for (int s : P->active)
+    for (int k = 0; k < SU2GPU_NCOUNTERS; k++) P->slots[s].tot[k] += tot[k] * (int64_t)P->slots[s].g.half * nsweeps;
+  PCK(cudaStreamSynchronize(P->st));
+  int herr = 0;
+  PCK(cudaMemcpy(&herr, P->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (herr) return fail(SU2GPU_ERR_KERNEL, "a pool kernel reported an invalid state (NaN fields?)");
+  return SU2GPU_OK;
+}
+
+int su2gpu_pool_active(su2gpu_pool* P, int32_t* slots, int32_t max, int32_t* n) {
+  if (!P || !n) return SU2GPU_ERR_INVALID;
+  int k = 0;
+  for (int s = 0; s < P->max_slots; s++)
+    if (P->slots[s].active) {
+      if (slots && k < max) slots[k] = s;
+      k++;
+    }
+  *n = k;
+  return SU2GPU_OK;
+}
+
+// measure() sums of every active chain, in slot order: sums[k*NMEAS + m]
+int su2gpu_pool_measure(su2gpu_pool* P, double* sums, int32_t max_chains, int32_t* nchains) {
+  if (!P || !sums || !nchains) return SU2GPU_ERR_INVALID;
+  int rc;
+  if (P->dirty && (rc = rebuild(P))) return rc;
+  int n = (int)P->active.size();
+  *nchains = n;
+  if (!n) return SU2GPU_OK;
+  if (n > max_chains) return fail(SU2GPU_ERR_INVALID, "output holds %d chains, pool has %d", max_chains, n);
+  PoolArgs a;
+  memset(&a, 0, sizeof(a));
+  a.descs = P->descs.p;
+  a.tiles = (const int2*)P->mtiles.p;
+  a.err = (int*)P->err.p;
+  P->ops->pool_measure(a, (double*)P->partials.p, P->nmtiles, P->st);
+  launch_pool_reduce((const double*)P->partials.p, P->nmtiles, (const int*)P->mfirst.p, n, (double*)P->sums.p, P->st);
+  PCK(cudaGetLastError());
+  PCK(cudaMemcpyAsync(sums, P->sums.p, (size_t)n * NSUMS * 8, cudaMemcpyDeviceToHost, P->st));
+  PCK(cudaStreamSynchronize(P->st));
+  return SU2GPU_OK;
+}
+
+int su2gpu_pool_counters(su2gpu_pool* P, int32_t s, int64_t* out) {
+  if (!P || !out || s < 0 || s >= P->max_slots || !P->slots[s].active) return fail(SU2GPU_ERR_INVALID, "no such chain slot");
+  unsigned long long d[SU2GPU_NCOUNTERS];
+  PCK(cudaMemcpyAsync(d, (char*)P->slotmem.p + (size_t)s * 256 + 32, sizeof(d), cudaMemcpyDeviceToHost, P->st));
+  PCK(cudaStreamSynchronize(P->st));
+  for (int k = 0; k < SU2GPU_NCOUNTERS; k++) out[k] = (int64_t)d[k] + P->slots[s].tot[k];
+  return SU2GPU_OK;
+}
+
+// launch shapes for the pool's kernels, timed on a scratch copy of the arena
+int su2gpu_pool_autotune(su2gpu_pool* P, int32_t* choices, float* best_ms) {
+  if (!P) return SU2GPU_ERR_INVALID;
+  int rc;
+  if (P->dirty && (rc = rebuild(P))) return rc;
+  if (P->active.empty()) return SU2GPU_OK;
+  size_t used = 0;
+  for (int s : P->active) used = std::max(used, P->slots[s].off + P->slots[s].bytes);
+  Buf arena2, slot2, desc2;
+  if ((rc = arena2.ensure(used)) || (rc = slot2.ensure(P->slotmem.n)) || (rc = desc2.ensure(P->descs.n))) return rc;
+  PCK(cudaMemcpyAsync(arena2.p, P->arena.p, used, cudaMemcpyDeviceToDevice, P->st));
+  PCK(cudaMemcpyAsync(slot2.p, P->slotmem.p, P->slotmem.n, cudaMemcpyDeviceToDevice, P->st));
+  if ((rc = rebuild(P, arena2.p, slot2.p, desc2.p))) return rc;
+  const int nh = nhiggs_of(P->content);
+  bool present[5] = {true, (bool)(P->content & SU2GPU_U1), nh > 0, (bool)(P->content & SU2GPU_TRIPLET),
+                     (bool)(P->content & SU2GPU_SINGLET)};
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  PoolArgs a;
+  memset(&a, 0, sizeof(a));
+  a.descs = desc2.p;
+  a.err = (int*)P->err.p;
+  const int reps = 3;
+  for (int kind = 0; kind < 5; kind++) {
+    if (!present[kind]) continue;
+    float best = 1e30f;
+    int bestv = 0;
+    for (int v = 0; v < NVARIANTS; v++) {
+      float ms = 0.f;
+      for (int r = -1; r < reps; r++) {
+        a.parity = r & 1;
+        a.sub = kind <= 1 ? (r + 3) % 3 : 0;
+        a.alg = kind == 0 ? P->recipe.algorithm_su2link : 0;
+        a.pass = 60000 + r;
+        a.tiles = (const int2*)P->tiles[v].p;
+        cudaEventRecord(e0, P->st);
+        if (kind == 0) P->ops->pool_link(v, a, P->ntiles[v], P->st);
+        else if (kind == 1) P->ops->pool_u1(v, a, P->ntiles[v], P->st);
+        else P->ops->pool_scalar(v, kind - 2, a, P->ntiles[v], P->st);
+        cudaEventRecord(e1, P->st);
+        PCK(cudaEventSynchronize(e1));
+        float t = 0.f;
+        cudaEventElapsedTime(&t, e0, e1);
+        if (r >= 0) ms += t;
+      }
+      if (ms < best) { best = ms; bestv = v; }
+    }
+    P->var[kind] = bestv;
+    if (best_ms) best_ms[kind] = best / reps;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  PCK(cudaStreamSynchronize(P->st));
+  arena2.release(); slot2.release(); desc2.release();
+  if (P->gexec) { cudaGraphExecDestroy(P->gexec); P->gexec = nullptr; }
+  if (choices)
+    for (int k = 0; k < 5; k++) choices[k] = P->var[k];
+  return SU2GPU_OK;
+}
+
+int su2gpu_pool_set_variants(su2gpu_pool* P, const int32_t* choices) {
+  if (!P || !choices) return SU2GPU_ERR_INVALID;
+  for (int k = 0; k < 5; k++) {
+    if (choices[k] < 0 || choices[k] >= NVARIANTS) return SU2GPU_ERR_INVALID;
+    P->var[k] = choices[k];
+  }
+  if (P->gexec) { cudaGraphExecDestroy(P->gexec); P->gexec = nullptr; }
+  return SU2GPU_OK;
+}
+
+}  // extern "C"
+
+// gradient flow of one chain (gradflow.c:46-173): a context over the chain's
+// fields in the arena runs the single-lattice flow on its own copies
+extern "C" int su2gpu_pool_grad_flow(su2gpu_pool* P, int32_t s, double t_max, double dt, int32_t meas_interval,
+                                     double* rows, int32_t maxrows, int32_t* nrows) {
+  if (!P || !rows || !nrows || meas_interval <= 0 || dt <= 0 || s < 0 || s >= P->max_slots || !P->slots[s].active)
+    return fail(SU2GPU_ERR_INVALID, "bad flow arguments");
+  PCK(cudaStreamSynchronize(P->st));
+  su2gpu_ctx* c = nullptr;
+  int rc = su2gpu_attach(&P->slots[s].p, (char*)P->arena.p + P->slots[s].off, &c);
+  if (rc) return rc;
+  rc = su2gpu_grad_flow(c, t_max, dt, meas_interval, rows, maxrows, nrows);
+  su2gpu_destroy(c);
+  return rc;
+}

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "../../include/su2gpu.h"
+#include "su2_host.h"
 #include "su2_kernels.cuh"
 #include "su2_ops.h"
 
@@ -30,7 +31,7 @@ static void set_err(const char* fmt, ...) {
 }
 // C++ linkage, not part of the ABI: lets other units of the library set the
 // text returned by su2gpu_last_error
-__attribute__((visibility("hidden"))) void su2gpu_record_error(const char* msg) { set_err("%s", msg); }
+void su2gpu_record_error(const char* msg) { set_err("%s", msg); }
 
 #define CK(call)                                                                     \
   do {                                                                               \
@@ -108,6 +109,7 @@ struct su2gpu_ctx {
   std::vector<cudaEvent_t>* prof = nullptr;  // per-pass events while profiling
   std::vector<int>* prof_kind = nullptr;
   DevBuf fields, stage, ctrbuf, partials, sums, alpha, backup, muca, flow, rows;
+  bool borrowed = false;  // fields belong to another allocation (su2gpu_attach)
   Fields<double> f64{};
   Fields<float> f32{};
   unsigned long long* d_ctr = nullptr;  // [24] counters (accepted + muca)
@@ -132,8 +134,6 @@ struct su2gpu_ctx {
   size_t v4size() const { return prec == 64 ? 32 : 16; }
 };
 
-static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
-
 static int valid_params(const su2gpu_params* p) {
   if (!p) return 0;
   if (p->dim != 3) { set_err("only dim 3 is supported on the GPU (got %d)", p->dim); return 0; }
@@ -153,32 +153,7 @@ static int valid_params(const su2gpu_params* p) {
   return 1;
 }
 
-static size_t field_bytes(const su2gpu_params* p, int64_t V) {
-  size_t r = p->precision == 64 ? 8 : 4, v4 = 4 * r;
-  int nh = (p->content & SU2GPU_HIGGS2) ? 2 : ((p->content & SU2GPU_HIGGS1) ? 1 : 0);
-  size_t b = 3 * align256(V * v4);
-  if (p->content & SU2GPU_U1) b += 3 * align256(V * r);
-  b += nh * align256(V * v4);
-  if (p->content & SU2GPU_TRIPLET) b += 3 * align256(V * r);
-  if (p->content & SU2GPU_SINGLET) b += align256(V * r);
-  return b;
-}
-
-template <typename R>
-static void carve(Fields<R>& f, char* base, const su2gpu_params* p, int64_t V) {
-  size_t r = sizeof(R), v4 = 4 * r, off = 0;
-  int nh = (p->content & SU2GPU_HIGGS2) ? 2 : ((p->content & SU2GPU_HIGGS1) ? 1 : 0);
-  memset(&f, 0, sizeof(f));
-  for (int d = 0; d < 3; d++) { f.link[d] = (V4<R>*)(base + off); off += align256(V * v4); }
-  if (p->content & SU2GPU_U1)
-    for (int d = 0; d < 3; d++) { f.u1[d] = (R*)(base + off); off += align256(V * r); }
-  for (int h = 0; h < nh; h++) { f.phi[h] = (V4<R>*)(base + off); off += align256(V * v4); }
-  if (p->content & SU2GPU_TRIPLET)
-    for (int k = 0; k < 3; k++) { f.trip[k] = (R*)(base + off); off += align256(V * r); }
-  if (p->content & SU2GPU_SINGLET) { f.sing = (R*)(base + off); off += align256(V * r); }
-}
-
-static Coup make_coup(const su2gpu_params* p) {
+Coup su2::make_coup(const su2gpu_params* p) {
   Coup c;
   c.beta = p->betasu2; c.msq = p->msq_phi; c.lam = p->lambda_phi;
   c.msqT = p->msq_triplet; c.a2 = p->a2; c.b4 = p->b4;
@@ -193,7 +168,7 @@ static Coup make_coup(const su2gpu_params* p) {
   return c;
 }
 
-static const Ops* pick_ops(int prec, int content) {
+const Ops* su2::pick_ops(int prec, int content) {
   int c = content & 0x1f;
   if (prec == 64) {
     if (c == C_H1) return &ops_f64_fund;
@@ -239,7 +214,7 @@ int64_t su2gpu_footprint_bytes(const su2gpu_params* p) {
   return (int64_t)b;
 }
 
-int su2gpu_create(const su2gpu_params* p, su2gpu_ctx** out) {
+static int create_ctx(const su2gpu_params* p, void* borrowed, su2gpu_ctx** out) {
   if (!out) return SU2GPU_ERR_INVALID;
   *out = nullptr;
   if (!valid_params(p)) return SU2GPU_ERR_INVALID;
@@ -265,7 +240,12 @@ int su2gpu_create(const su2gpu_params* p, su2gpu_ctx** out) {
   }
   c->st = c->own_st;
   int64_t V = c->g.V;
-  if ((rc = c->fields.ensure(field_bytes(p, V))) ||
+  if (borrowed) {
+    c->fields.p = borrowed;
+    c->fields.n = field_bytes(p, V);
+    c->borrowed = true;
+  }
+  if ((!borrowed && (rc = c->fields.ensure(field_bytes(p, V)))) ||
       (rc = c->ctrbuf.ensure(4096)) ||
       (rc = c->partials.ensure((size_t)(nblk(V, BLOCK) + 2) * NSUMS * 8)) ||
       (rc = c->sums.ensure(NSUMS * 8))) {
@@ -278,14 +258,14 @@ int su2gpu_create(const su2gpu_params* p, su2gpu_ctx** out) {
   c->d_err = (int*)((char*)c->ctrbuf.p + 512);
   c->d_sweep = (uint32_t*)((char*)c->ctrbuf.p + 1024);
   c->d_fz = (unsigned long long*)((char*)c->ctrbuf.p + 1536);
-  if (cudaMemsetAsync(c->fields.p, 0, c->fields.n, c->st) != cudaSuccess ||
+  if ((!borrowed && cudaMemsetAsync(c->fields.p, 0, c->fields.n, c->st) != cudaSuccess) ||
       cudaMemsetAsync(c->ctrbuf.p, 0, c->ctrbuf.n, c->st) != cudaSuccess) {
     set_err("cudaMemset failed");
     su2gpu_destroy(c);
     return SU2GPU_ERR_CUDA;
   }
   // cold links: unit quaternions (setsu2, init.c:18-28)
-  {
+  if (!borrowed) {
     std::vector<double> one((size_t)V * 12, 0.0);
     for (int64_t k = 0; k < V * 3; k++) one[(size_t)k * 4] = 1.0;
     if ((rc = c->stage.ensure((size_t)V * 12 * 8))) { su2gpu_destroy(c); return rc; }
@@ -301,15 +281,23 @@ int su2gpu_create(const su2gpu_params* p, su2gpu_ctx** out) {
       return SU2GPU_ERR_CUDA;
     }
   }
+  if (borrowed && cudaStreamSynchronize(c->st) != cudaSuccess) {
+    set_err("context set-up failed: %s", cudaGetErrorString(cudaGetLastError()));
+    su2gpu_destroy(c);
+    return SU2GPU_ERR_CUDA;
+  }
   *out = c;
   return SU2GPU_OK;
 }
+
+int su2gpu_create(const su2gpu_params* p, su2gpu_ctx** out) { return create_ctx(p, nullptr, out); }
 
 int su2gpu_destroy(su2gpu_ctx* c) {
   if (!c) return SU2GPU_OK;
   if (c->st) cudaStreamSynchronize(c->st);
   if (c->own_st) cudaStreamSynchronize(c->own_st);
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  if (c->borrowed) c->fields.p = nullptr;
   c->fields.release(); c->stage.release(); c->ctrbuf.release(); c->partials.release(); c->sums.release();
   c->alpha.release(); c->backup.release(); c->muca.release(); c->flow.release(); c->rows.release();
   if (c->own_st) cudaStreamDestroy(c->own_st);
@@ -1120,3 +1108,8 @@ int su2gpu_update_lattice_host(su2gpu_ctx* c, uint32_t sweep, double* link, doub
 }
 
 }  // extern "C"
+
+int su2gpu_attach(const su2gpu_params* p, void* fields, su2gpu_ctx** out) {
+  if (!fields) return SU2GPU_ERR_INVALID;
+  return create_ctx(p, fields, out);
+}

@@ -69,6 +69,25 @@ def lib():
         L.su2gpu_run_halfsweep.argtypes = [vp, i32, i32, i32, u32, u32]
         L.su2gpu_autotune.argtypes = [vp, vp, vp]
         L.su2gpu_set_variants.argtypes = [vp, vp]
+        P = ctypes.POINTER(abi.Params)
+        L.su2gpu_pool_chain_bytes.restype = i64
+        L.su2gpu_pool_chain_bytes.argtypes = [P]
+        L.su2gpu_pool_create.argtypes = [P, i64, i32, ctypes.POINTER(vp)]
+        L.su2gpu_pool_destroy.argtypes = [vp]
+        L.su2gpu_pool_add.argtypes = [vp, P, u64, u32, ctypes.POINTER(i32)]
+        L.su2gpu_pool_remove.argtypes = [vp, i32]
+        L.su2gpu_pool_info.argtypes = [vp, ctypes.POINTER(i32)] + [ctypes.POINTER(i64)] * 3
+        L.su2gpu_pool_active.argtypes = [vp, vp, i32, ctypes.POINTER(i32)]
+        L.su2gpu_pool_upload.argtypes = [vp, i32] + [vp] * 6
+        L.su2gpu_pool_download.argtypes = [vp, i32] + [vp] * 6
+        L.su2gpu_pool_set_sweep.argtypes = [vp, i32, u32]
+        L.su2gpu_pool_run.argtypes = [vp, i32, i32]
+        L.su2gpu_pool_measure.argtypes = [vp, vp, i32, ctypes.POINTER(i32)]
+        L.su2gpu_pool_counters.argtypes = [vp, i32, vp]
+        L.su2gpu_pool_autotune.argtypes = [vp, vp, vp]
+        L.su2gpu_pool_set_variants.argtypes = [vp, vp]
+        L.su2gpu_pool_grad_flow.argtypes = [vp, i32, ctypes.c_double, ctypes.c_double, i32, vp, i32,
+                                            ctypes.POINTER(i32)]
         _lib = L
     return _lib
 
@@ -258,3 +277,122 @@ def device_info():
     fr = ctypes.c_int64()
     check(lib().su2gpu_device_info(ctypes.byref(sm), ctypes.byref(ma), ctypes.byref(mi), ctypes.byref(fr)))
     return dict(sm_count=sm.value, cc=(ma.value, mi.value), free_bytes=fr.value)
+
+
+def _shapes(p):
+    V, nh = p.sites(), p.nhiggs()
+    return {
+        "link": (V, 3, 4),
+        "u1": (V, 3) if p.content & abi.U1 else None,
+        "d0": (V, 4) if nh > 0 else None,
+        "d1": (V, 4) if nh > 1 else None,
+        "trip": (V, 3) if p.content & abi.TRIPLET else None,
+        "sing": (V,) if p.content & abi.SINGLET else None,
+    }
+
+
+class CapacityError(SU2GPUError):
+    """The pool's arena or slot table cannot take the chain."""
+
+
+class Pool:
+    """Many independent chains of one content / precision / update recipe in
+    one device arena (a su2gpu pool); every half-sweep is one launch over all
+    chains.  A chain follows the trajectory of a `Lattice` with the same
+    parameters, seed and chain id."""
+
+    def __init__(self, recipe, arena_bytes, max_chains=1024):
+        self.recipe = recipe
+        self._h = ctypes.c_void_p()
+        self._params = {}
+        check(lib().su2gpu_pool_create(ctypes.byref(recipe), int(arena_bytes), int(max_chains),
+                                       ctypes.byref(self._h)))
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().su2gpu_pool_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def chain_bytes(params):
+        return int(lib().su2gpu_pool_chain_bytes(ctypes.byref(params)))
+
+    def add(self, params, seed=0, chain=0):
+        """Admit a chain; returns its slot.  Raises CapacityError when the
+        arena or the slot table is full."""
+        s = ctypes.c_int32()
+        rc = lib().su2gpu_pool_add(self._h, ctypes.byref(params), seed, chain, ctypes.byref(s))
+        if rc == abi.ERR_CAPACITY:
+            raise CapacityError(lib().su2gpu_last_error().decode())
+        check(rc)
+        self._params[s.value] = params
+        return s.value
+
+    def remove(self, slot):
+        check(lib().su2gpu_pool_remove(self._h, slot))
+        self._params.pop(slot, None)
+
+    def info(self):
+        n, u, f, b = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        check(lib().su2gpu_pool_info(self._h, ctypes.byref(n), ctypes.byref(u), ctypes.byref(f), ctypes.byref(b)))
+        return {"chains": n.value, "used_bytes": u.value, "free_bytes": f.value, "largest_free": b.value}
+
+    def active(self):
+        n = ctypes.c_int32()
+        check(lib().su2gpu_pool_active(self._h, None, 0, ctypes.byref(n)))
+        out = np.zeros(max(n.value, 1), dtype=np.int32)
+        check(lib().su2gpu_pool_active(self._h, _p(out), n.value, ctypes.byref(n)))
+        return out[:n.value]
+
+    def upload(self, slot, **fields):
+        arrs = [None if fields.get(n) is None else np.ascontiguousarray(fields[n], dtype=np.float64)
+                for n in FIELD_NAMES]
+        check(lib().su2gpu_pool_upload(self._h, slot, *[_p(a) for a in arrs]))
+
+    def download(self, slot):
+        out = {n: (None if shp is None else np.zeros(shp)) for n, shp in _shapes(self._params[slot]).items()}
+        check(lib().su2gpu_pool_download(self._h, slot, *[_p(out[n]) for n in FIELD_NAMES]))
+        return out
+
+    def set_sweep(self, slot, sweep):
+        check(lib().su2gpu_pool_set_sweep(self._h, slot, sweep))
+
+    def run(self, nsweeps, graph=True):
+        check(lib().su2gpu_pool_run(self._h, nsweeps, 1 if graph else 0))
+
+    def measure(self):
+        """{slot: measure() sums} of every active chain."""
+        slots = self.active()
+        out = np.zeros((max(len(slots), 1), abi.NMEAS))
+        n = ctypes.c_int32()
+        check(lib().su2gpu_pool_measure(self._h, _p(out), out.shape[0], ctypes.byref(n)))
+        return {int(s): out[k].copy() for k, s in enumerate(slots)}
+
+    def counters(self, slot):
+        out = np.zeros(abi.NCOUNTERS, dtype=np.int64)
+        check(lib().su2gpu_pool_counters(self._h, slot, _p(out)))
+        return out
+
+    def autotune(self):
+        ch = np.zeros(5, dtype=np.int32)
+        ms = np.zeros(5, dtype=np.float32)
+        check(lib().su2gpu_pool_autotune(self._h, _p(ch), _p(ms)))
+        return ch, ms
+
+    def set_variants(self, choices):
+        ch = np.ascontiguousarray(choices, dtype=np.int32)
+        check(lib().su2gpu_pool_set_variants(self._h, _p(ch)))
+
+    def grad_flow(self, slot, t_max, dt, meas_interval=1):
+        maxrows = int(np.ceil(t_max / dt)) // meas_interval + 3
+        rows = np.zeros((maxrows, 1 + abi.NMEAS))
+        n = ctypes.c_int32()
+        check(lib().su2gpu_pool_grad_flow(self._h, slot, t_max, dt, meas_interval, _p(rows), maxrows,
+                                          ctypes.byref(n)))
+        return rows[:n.value]
