@@ -3,22 +3,29 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference] [--workload NAME]
 
-A step is one full sweep of the update recipe of the workload (link heatbath
-for every direction and parity, 4 overrelaxation + 1 Metropolis passes of the
-Higgs doublet) followed by one measurement of all volume sums, on a device-
-resident lattice.  The default workload is the FP32 precision form at scale:
-SU(2) + fundamental Higgs on 128^3, beta = 8, m^2 = -0.1, lambda = 0.002,
-seeded hot start, links re-normalised every 10 sweeps, FP64 sums.
+Default workload, batched384_adj_f32 -- the FP32 batched form: 384 independent
+SU(2) + adjoint Higgs chains (side L uniform over {8,12,16,24,32,48}, beta
+uniform in [6,12], m^2_adj scanning [-0.3,0.1], lambda_adj 0.005; 11.0 M sites
+in all) resident in one device pool.  A step is 10 sweeps of every chain (each
+sweep one CUDA-graph replay: 6 link heatbath + 10 triplet half-sweeps, every
+half-sweep one launch over all chains) followed by the measurement of every
+chain; the default 100 steps are the workload's 1000 sweeps per chain.
+Single-lattice workloads (fund128_f32 ...): a step is one sweep of SU(2) +
+fundamental Higgs plus its measurement.
 
-value      site-updates/s = V * K / (sum of per-step CUDA-event times); an L2
-           flush (a 256 MiB write) runs between steps, outside the events
-e2e        the same metric through the host-buffer C ABI call
-           su2gpu_update_lattice_host (FP64 AoS host arrays, page-locked):
-           upload + sweep + download + measure per step, wall clock
-roofline   the kernel kind with the largest share of a profiled pass of the
-           same steps (CUDA events around every pass on the launching stream)
-cpu_baseline  the oracle's C restatement of the sweep, one thread, one sweep
-           of the same lattice on the host cores
+value      site-updates/s = sites * sweeps / (sum of per-step CUDA-event
+           times on the launching stream); the fields (660 MB for the
+           ensemble, 128 MB+ for 128^3) exceed the 126 MB L2 and a 256 MiB
+           write flushes L2 between steps, outside the events
+e2e        the same metric through the host-buffer C ABI (FP64 AoS host
+           arrays, page-locked): upload of every chain + sweeps + measure +
+           download per step, wall clock
+fp64_plain the plain FP64 single-lattice sweep on the same lattices run one
+           after another (the metric's comparison)
+roofline   the kernel kind with the largest share of profiled sweeps (CUDA
+           events around every pass on the launching stream)
+cpu_baseline  the oracle's C restatement of the sweep, one thread, on a
+           bounded sample of the same lattices
 
 --impl reference runs that CPU restatement on all host cores instead (one
 independent lattice per core; the reference itself is serial C).
@@ -50,14 +57,22 @@ WORKLOADS = {
     "fund160_f32": ("fund", (160, 160, 160), 32),
 }
 
+BATCHED = {
+    # name: (chains, sweeps per step)
+    "batched384_adj_f32": (384, 10),
+    "batched96_adj_f32": (96, 10),
+}
+
 # Compulsory device traffic per lattice site, in reals, for one launch of each
-# pass kind of the fundamental content (each array element a launch must touch
-# counted once): link heatbath reads the two other directions everywhere (8),
-# the updated direction everywhere and writes half of it (4 + 2), the doublet
-# everywhere (4) -> 18; a doublet pass reads the doublet everywhere (4), all
-# links (12) and writes half the doublet (2) -> 18; the measurement reads every
-# field once (16).
-REALS_PER_SITE = {0: 18, 2: 18}
+# pass kind (each array element a launch must touch counted once).
+# Fundamental content: link heatbath reads the two other directions everywhere
+# (8), the updated direction everywhere and writes half of it (4 + 2), the
+# doublet everywhere (4) -> 18; a doublet pass reads the doublet everywhere
+# (4), all links (12) and writes half the doublet (2) -> 18.  Adjoint content:
+# link heatbath 8 + 4 + 2 + the triplet everywhere (3) -> 17; a triplet pass
+# reads all links (12) and the triplet everywhere (3) and writes half of it
+# (1.5) -> 16.5.
+REALS_PER_SITE = {"fund": {0: 18, 2: 18}, "adj": {0: 17, 3: 16.5}}
 REALS_MEASURE = 16
 KIND_NAMES = {0: "link_heatbath", 1: "u1_metropolis", 2: "doublet_update", 3: "triplet_update",
               4: "singlet_update", 5: "reunitarize"}
@@ -167,10 +182,72 @@ def _cpu_worker(args):
     return cpu_sample_sweeps(content, L, seed, nsweeps)
 
 
+def _cpu_chain_worker(args):
+    """One sweep + measure of one ensemble chain with the oracle (FP64)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from native import Fields, Oracle
+    from su2higgs_gb300 import abi, workloads
+    L, beta, msq, b4, seed, chain = args
+    p = abi.make_params("adj", L=(L, L, L), precision=64, betasu2=beta, msq_triplet=msq, b4=b4)
+    f = workloads.hot_fields(p, seed)
+    o = Oracle(p)
+    o.put(Fields(p, link=f["link"], trip=f["trip"]))
+    o.set_rng(seed, 0, chain)
+    t0 = time.perf_counter()
+    o.update()
+    o.measure()
+    return p.sites(), time.perf_counter() - t0, os.getpid()
+
+
+def run_reference_batched(args):
+    """The oracle's FP64 restatement of the reference's serial sweep on all
+    host cores: each step sweeps 4 x cores chains of the ensemble (cycling
+    through it), one process per core, largest first so that the cores stay
+    balanced as they would over a long run; a step lasts as long as the
+    busiest core's sweeps (set-up excluded, as on the GPU)."""
+    from su2higgs_gb300 import workloads
+    import multiprocessing as mp
+    nchains, S = BATCHED[args.workload]
+    specs = workloads.batched_ensemble(nchains)
+    cores = os.cpu_count() or 1
+    jobs = [(int(p.L[0]), float(p.betasu2), float(p.msq_triplet), float(p.b4), seed, chain) for p, seed, chain in specs]
+    ctx = mp.get_context("spawn")
+    done, wall, nxt = 0, 0.0, 0
+    per_step = 4 * cores
+    with ctx.Pool(cores) as pool:
+        for s in range(args.warmup + args.steps):
+            batch = sorted((jobs[(nxt + k) % len(jobs)] for k in range(per_step)), key=lambda j: -j[0])
+            nxt += per_step
+            res = pool.map(_cpu_chain_worker, batch, chunksize=1)
+            if s < args.warmup:
+                continue
+            per_pid = {}
+            for n, t, pid in res:
+                per_pid[pid] = per_pid.get(pid, 0.0) + t
+            done += sum(r[0] for r in res)
+            wall += max(per_pid.values())
+    value = done / wall
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "site-updates/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / max(args.steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "content": "SU(2) + adjoint Higgs", "chains": nchains,
+                   "sample": f"{per_step} chains of the ensemble per step, one sweep + measure each"},
+        "cpu_baseline": {"value": value, "unit": "site-updates/s", "cores": cores, "kind": "port",
+                         "sample": f"{per_step} ensemble chains per step (one process per core, cycling through the "
+                                   f"{nchains} chains), 1 sweep + measure each; oracle C restatement of the "
+                                   "reference's serial sweep"},
+        "e2e": {"value": value, "unit": "site-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     rank, world, _ = env_rank()
     if rank != 0:
         return
+    if args.workload in BATCHED:
+        return run_reference_batched(args)
     content, L, prec = WORKLOADS[args.workload]
     import multiprocessing as mp
     cores = os.cpu_count() or 1
@@ -290,7 +367,7 @@ def run_gpu(args):
     nlaunch = int(np.sum(kinds == top))
     avg_ms = shares[top] / nlaunch
     rsize = 4 if prec == 32 else 8
-    alg_bytes = REALS_PER_SITE.get(top, 18) * rsize * V
+    alg_bytes = REALS_PER_SITE[content].get(top, 18) * rsize * V
     achieved = alg_bytes / (avg_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
     traffic = None
@@ -387,13 +464,245 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def roofline_of(kinds, ms, content, prec, sites, workload):
+    """The kernel kind with the largest time share, its algorithmic bytes per
+    launch (REALS_PER_SITE x sites) over its mean launch time."""
+    shares = {}
+    for kd in np.unique(kinds):
+        shares[int(kd)] = float(ms[kinds == kd].sum())
+    top = max(shares, key=shares.get)
+    nlaunch = int(np.sum(kinds == top))
+    avg_ms = shares[top] / nlaunch
+    rsize = 4 if prec == 32 else 8
+    alg_bytes = REALS_PER_SITE[content].get(top, 18) * rsize * sites
+    achieved = alg_bytes / (avg_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = None
+    tr_path = os.path.join(ROOT, "profiles", f"traffic_{workload}.json")
+    if os.path.exists(tr_path):
+        with open(tr_path) as fh:
+            traffic = json.load(fh).get(KIND_NAMES[top])
+    tot = sum(shares.values())
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic, "kernel": KIND_NAMES[top], "peak_source": peak_kind,
+            "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_ms, "launches_profiled": nlaunch,
+            "time_share": shares[top] / tot, "shares": {KIND_NAMES[k]: v / tot for k, v in shares.items()}}
+
+
+def cpu_sample_chains(specs, budget_s=15.0):
+    """The oracle's C restatement, one thread: one sweep + measure of chains
+    of the ensemble, smallest side first, until about budget_s seconds."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from native import Fields, Oracle
+    from su2higgs_gb300 import abi, workloads
+    order = sorted(range(len(specs)), key=lambda k: specs[k][0].L[0])
+    # one chain of every side, then more of the same mix while time is left
+    by_side = {}
+    for k in order:
+        by_side.setdefault(specs[k][0].L[0], []).append(k)
+    picks = []
+    for rnd in range(max(len(v) for v in by_side.values())):
+        for side in sorted(by_side):
+            if rnd < len(by_side[side]):
+                picks.append(by_side[side][rnd])
+    sites, t, used = 0, 0.0, []
+    for k in picks:
+        p, seed, chain = specs[k]
+        p64 = abi.make_params("adj", L=tuple(p.L[:3]), precision=64, betasu2=p.betasu2,
+                              msq_triplet=p.msq_triplet, b4=p.b4)
+        f = workloads.hot_fields(p64, seed)
+        o = Oracle(p64)
+        o.put(Fields(p64, link=f["link"], trip=f["trip"]))
+        o.set_rng(seed, 0, chain)
+        t0 = time.perf_counter()
+        o.update()
+        o.measure()
+        t += time.perf_counter() - t0
+        sites += p64.sites()
+        used.append(p.L[0])
+        if t > budget_s:
+            break
+    return sites, t, used
+
+
+def run_gpu_batched(args):
+    import torch
+    from su2higgs_gb300 import abi, gpu, workloads
+
+    rank, world, local = env_rank()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    nchains, S = BATCHED[args.workload]
+    specs = workloads.batched_ensemble(nchains, seed=20261203 + 1000003 * rank)
+    sites = sum(p.sites() for p, _, _ in specs)
+    arena = sum(gpu.Pool.chain_bytes(p) for p, _, _ in specs)
+    pool = gpu.Pool(specs[0][0], arena_bytes=arena, max_chains=nchains)
+    host = []
+    for p, seed, chain in specs:
+        slot = pool.add(p, seed=seed, chain=chain)
+        f = workloads.hot_fields(p, seed)
+        pool.upload(slot, **f)
+        host.append((slot, f))
+    variants, _ = pool.autotune()
+    stream = torch.cuda.Stream(device=dev)
+    pool.set_stream(stream.cuda_stream)
+    K, W = args.steps, args.warmup
+    sums = torch.zeros((2, nchains, abi.NMEAS), dtype=torch.float64, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    launches_sweep = pool.launches_per_sweep()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    with torch.cuda.stream(stream):
+        for w in range(W):
+            pool.enqueue(S, graph=True)
+            pool.enqueue_measure(sums[0].data_ptr(), nchains)
+            flush.zero_()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        clocks = ClockSampler(local)
+        clocks.start()
+        t_wall0 = time.perf_counter()
+        for k in range(K):
+            starts[k].record(stream)
+            pool.enqueue(S, graph=True)
+            pool.enqueue_measure(sums[1].data_ptr(), nchains)
+            ends[k].record(stream)
+            flush.zero_()
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall0
+        clk = clocks.stop()
+    if dist:
+        dist.barrier()
+    pool.run(0)  # surfaces any error recorded by the kernels
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    dev_ms = float(np.sum(step_ms))
+    t = torch.tensor([dev_ms], dtype=torch.float64, device=dev)
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev_ms = float(t.item())
+    value = world * sites * S * K / (dev_ms * 1e-3)
+    m_last = sums[1].cpu().numpy()
+    assert np.all(np.isfinite(m_last)), "non-finite measurement"
+
+    pool.set_stream(None)
+    kinds_all, ms_all = [], []
+    for k in range(3):
+        kd, ms = pool.profile_sweep()
+        kinds_all.append(kd)
+        ms_all.append(ms)
+    roofline = roofline_of(np.concatenate(kinds_all), np.concatenate(ms_all), "adj", 32, sites, args.workload)
+
+    # end to end through the pool's host-buffer C ABI: every chain's FP64
+    # fields uploaded from page-locked memory, S sweeps, measurement,
+    # every chain downloaded, per step
+    e2e = None
+    if rank == 0:
+        arrays = [a for _, f in host for a in f.values()]
+        for a in arrays:
+            gpu.host_register(a)
+        h2d = sum(a.nbytes for a in arrays)
+        n_e2e = max(3, min(K, 10))
+        e2e_pool = gpu.Pool(specs[0][0], arena_bytes=arena, max_chains=nchains)
+        e2e_pool.set_variants(variants)
+        slots = [e2e_pool.add(p, seed=seed, chain=chain) for p, seed, chain in specs]
+
+        def e2e_step():
+            for slot, (_, f) in zip(slots, host):
+                e2e_pool.upload(slot, **f)
+            e2e_pool.run(S, graph=True)
+            e2e_pool.measure()
+            for slot, (_, f) in zip(slots, host):
+                e2e_pool.download(slot, out=f)  # in place, into the same page-locked arrays
+        e2e_step()
+        t0 = time.perf_counter()
+        for k in range(n_e2e):
+            e2e_step()
+        te = time.perf_counter() - t0
+        for a in arrays:
+            gpu.host_unregister(a)
+        e2e = {"value": sites * S * n_e2e / te, "unit": "site-updates/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": h2d + nchains * abi.NMEAS * 8, "steps": n_e2e, "sweeps_per_step": S}
+        e2e_pool.close()
+
+    # the plain FP64 sweep on the same lattices, one single-lattice context
+    # after another (every 4th chain of the ensemble)
+    fp64 = None
+    if rank == 0 and not args.no_fp64:
+        tot_sites, tot_ms = 0, 0.0
+        n64 = 3
+        with torch.cuda.stream(stream):
+            for p, seed, chain in specs[::4]:
+                p64 = abi.make_params("adj", L=tuple(p.L[:3]), precision=64, betasu2=p.betasu2,
+                                      msq_triplet=p.msq_triplet, b4=p.b4)
+                lat = gpu.Lattice(p64, seed=seed, chain=chain)
+                lat.upload(**workloads.hot_fields(p64, seed))
+                lat.set_stream(stream.cuda_stream)
+                lat.enqueue_sweeps(0, 2, graph=True)
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                lat.enqueue_sweeps(2, n64, graph=True)
+                lat.enqueue_measure(sums[0].data_ptr())
+                b.record(stream)
+                torch.cuda.synchronize()
+                tot_ms += a.elapsed_time(b)
+                tot_sites += p64.sites() * n64
+                lat.close()
+        v64 = tot_sites / (tot_ms * 1e-3)
+        fp64 = {"value": v64, "unit": "site-updates/s", "chains": len(specs[::4]), "sweeps_each": n64,
+                "fp32_batched_over_fp64_plain": value / world / v64,
+                "what": "every 4th chain of the ensemble as an FP64 single-lattice context (graph replay), "
+                        "one after another"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        n, tcpu, used = cpu_sample_chains(specs)
+        cpu = {"value": n / tcpu, "unit": "site-updates/s", "cores": 1, "kind": "port",
+               "sample": f"1 sweep + measure of {len(used)} chains of the ensemble (sides {sorted(set(used))}), "
+                         f"oracle C restatement in FP64, 1 thread ({tcpu:.1f} s)"}
+
+    if rank == 0:
+        Ls = [p.L[0] for p, _, _ in specs]
+        line = {
+            "metric": METRIC, "value": value, "unit": "site-updates/s", "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": dev_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "content": "SU(2) + adjoint Higgs", "chains": nchains,
+                       "sites_total": sites, "sweeps_per_step": S, "sweeps_per_chain": S * (K + W),
+                       "sides": {str(L): Ls.count(L) for L in sorted(set(Ls))},
+                       "betasu2": list(workloads.ENSEMBLE_BETA), "msq_adj": list(workloads.ENSEMBLE_MSQ_ADJ),
+                       "lambda_adj": workloads.ENSEMBLE_LAMBDA_ADJ,
+                       "precision": "FP32 fields, FP64 reductions",
+                       "recipe": "1 link heatbath (3 directions x 2 parities) + 4 triplet overrelax + "
+                                 "1 triplet Metropolis (x 2 parities) per sweep; measure every chain each step",
+                       "l2": "fields 660 MB > L2; 256 MiB write between steps outside the step events",
+                       "parallelism": f"replicas x{world}", "graph": True,
+                       "launch_variants": [int(v) for v in variants]},
+            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "fp64_plain": fp64,
+            # per step: S graph replays of the sweep's kernels + measure + per-chain reduction
+            "gpu_launches": int(K * (S * launches_sweep + 2)),
+            "clocks": clk, "wall_s_timed_region": t_wall,
+            "step_ms_p50": float(np.percentile(step_ms, 50)), "step_ms_p99": float(np.percentile(step_ms, 99)),
+        }
+        print(json.dumps(line), flush=True)
+    pool.close()
+    if dist:
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--workload", default="fund128_f32", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="batched384_adj_f32", choices=sorted(WORKLOADS) + sorted(BATCHED))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison")
     args = ap.parse_args()
@@ -401,6 +710,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload in BATCHED:
+        run_gpu_batched(args)
     else:
         run_gpu(args)
 

@@ -259,9 +259,12 @@ int su2gpu_host_unregister(void* ptr);
  * device arena.  Each half-sweep of the update_lattice() sequence
  * (update.c:270-430) is one launch over every chain of the pool, and a sweep
  * of the whole pool is replayed as one CUDA graph until the membership
- * changes.  A chain of a pool follows exactly the trajectory a single-lattice
+ * changes.  A chain of a pool follows the trajectory a single-lattice
  * context with the same parameters, seed and chain id follows (same random
- * numbers, same fields bit for bit).  Multicanonical weighting is not
+ * numbers, same accept/reject decisions, fields equal to rounding: the two
+ * kernels may form fused multiply-adds differently), and a chain's results
+ * do not depend on the other chains of its pool (bit for bit).
+ * Multicanonical weighting is not
  * available in pools.  The reference runs one chain per process: these have
  * no counterpart there. */
 typedef struct su2gpu_pool su2gpu_pool;
@@ -297,6 +300,19 @@ int su2gpu_pool_run(su2gpu_pool* pool, int32_t nsweeps, int32_t use_graph);
 /* measure() sums of every active chain, in slot order:
  * sums[k * SU2GPU_NMEAS + m] for the k-th active chain. */
 int su2gpu_pool_measure(su2gpu_pool* pool, double* sums, int32_t max_chains, int32_t* nchains);
+/* Asynchronous forms on the pool's execution stream: enqueue `nsweeps`
+ * sweeps, or the measurement into the DEVICE buffer `device_sums`
+ * (max_chains * SU2GPU_NMEAS doubles).  Errors recorded by the kernels
+ * surface at the next su2gpu_pool_run. */
+int su2gpu_pool_enqueue(su2gpu_pool* pool, int32_t nsweeps, int32_t use_graph);
+int su2gpu_pool_enqueue_measure(su2gpu_pool* pool, double* device_sums, int32_t max_chains, int32_t* nchains);
+/* Execution stream (a cudaStream_t; NULL = the pool's own stream). */
+int su2gpu_pool_set_stream(su2gpu_pool* pool, void* cuda_stream);
+/* Kernel launches of one pool sweep (passes + the sweep-counter increment). */
+int su2gpu_pool_launches_per_sweep(su2gpu_pool* pool, int32_t* n);
+/* One sweep of every chain with CUDA events around every pass (the chains
+ * advance): kinds / ms as su2gpu_profile_sweep. */
+int su2gpu_pool_profile_sweep(su2gpu_pool* pool, int32_t max_passes, int32_t* kinds, float* ms, int32_t* npasses);
 /* One chain's counters (SU2GPU_NCOUNTERS, as su2gpu_get_counters). */
 int su2gpu_pool_counters(su2gpu_pool* pool, int32_t slot, int64_t* out);
 /* Launch-shape autotuner over the pool's current chains (as su2gpu_autotune;

@@ -83,7 +83,10 @@ struct su2gpu_pool {
   int prec, content;
   const Ops* ops;
   const PrecOps* pops;
-  cudaStream_t st = nullptr;
+  cudaStream_t st = nullptr;      // execution stream (the caller's, or own_st)
+  cudaStream_t own_st = nullptr;  // the pool's own stream; graphs are captured on it
+  std::vector<cudaEvent_t>* prof = nullptr;  // per-pass events while profiling
+  std::vector<int>* prof_kind = nullptr;
   Buf arena;
   std::vector<std::pair<size_t, size_t>> free_list;  // (offset, length), sorted by offset
   std::vector<Slot> slots;
@@ -97,6 +100,12 @@ struct su2gpu_pool {
   cudaGraphExec_t gexec = nullptr;
   int var[5] = {0, 0, 0, 0, 0};
   int64_t sweep_passes[SU2GPU_NCOUNTERS] = {0};  // half-sweeps of each kind in one sweep (graph replay)
+  // host images of the descriptor and tile tables; members, so that they
+  // outlive every asynchronous copy from them
+  std::vector<unsigned char> h_desc;
+  std::vector<int2> h_tiles[NVARIANTS], h_mtiles;
+  std::vector<int> h_first;
+  std::vector<uint32_t*> h_sweeps;
   size_t rsize() const { return prec == 64 ? 8 : 4; }
 };
 
@@ -152,7 +161,9 @@ int rebuild(su2gpu_pool* P, void* arena_base = nullptr, void* slot_base = nullpt
   for (int s = 0; s < (int)P->slots.size(); s++)
     if (P->slots[s].active) P->active.push_back(s);
   size_t dsz = P->prec == 64 ? sizeof(ChainDesc<double>) : sizeof(ChainDesc<float>);
-  std::vector<unsigned char> hd(dsz * P->max_slots, 0);
+  PCK(cudaStreamSynchronize(P->st));  // no copy from the host images is in flight
+  std::vector<unsigned char>& hd = P->h_desc;
+  hd.assign(dsz * P->max_slots, 0);
   for (int s : P->active) {
     if (P->prec == 64) {
       ChainDesc<double> d = make_desc<double>(P, s, ab, sb);
@@ -165,7 +176,8 @@ int rebuild(su2gpu_pool* P, void* arena_base = nullptr, void* slot_base = nullpt
   PCK(cudaMemcpyAsync(dd, hd.data(), hd.size(), cudaMemcpyHostToDevice, P->st));
   if (!descs) {
     for (int v = 0; v < NVARIANTS; v++) {
-      std::vector<int2> t;
+      std::vector<int2>& t = P->h_tiles[v];
+      t.clear();
       int bs = kVariantBS[v];
       for (int s : P->active)
         for (int t0 = 0; t0 < P->slots[s].g.half; t0 += bs) t.push_back(int2{s, t0});
@@ -173,9 +185,12 @@ int rebuild(su2gpu_pool* P, void* arena_base = nullptr, void* slot_base = nullpt
       if (int rc = P->tiles[v].ensure(std::max<size_t>(t.size(), 1) * sizeof(int2))) return rc;
       if (!t.empty()) PCK(cudaMemcpyAsync(P->tiles[v].p, t.data(), t.size() * sizeof(int2), cudaMemcpyHostToDevice, P->st));
     }
-    std::vector<int2> mt;
-    std::vector<int> first;
-    std::vector<uint32_t*> sp;
+    std::vector<int2>& mt = P->h_mtiles;
+    std::vector<int>& first = P->h_first;
+    std::vector<uint32_t*>& sp = P->h_sweeps;
+    mt.clear();
+    first.clear();
+    sp.clear();
     for (int s : P->active) {
       first.push_back((int)mt.size());
       for (int t0 = 0; t0 < P->slots[s].g.V; t0 += BLOCK) mt.push_back(int2{s, t0});
@@ -203,6 +218,15 @@ int rebuild(su2gpu_pool* P, void* arena_base = nullptr, void* slot_base = nullpt
   return SU2GPU_OK;
 }
 
+void mark(su2gpu_pool* P, int kind) {
+  if (!P->prof) return;
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  cudaEventRecord(e, P->st);
+  P->prof->push_back(e);
+  P->prof_kind->push_back(kind);
+}
+
 // one sweep of every active chain (update.c:270-430 order); `tot` receives the
 // per-chain half-site totals of one sweep
 int enqueue_pool_sweep(su2gpu_pool* P, const void* descs, const int2* const* tiles, unsigned long long* unused,
@@ -212,6 +236,7 @@ int enqueue_pool_sweep(su2gpu_pool* P, const void* descs, const int2* const* til
   PoolArgs a;
   memset(&a, 0, sizeof(a));
   a.descs = descs;
+  a.nslots = P->max_slots;
   a.err = (int*)P->err.p;
   uint32_t pass = 0;
   const int nh = nhiggs_of(p.content);
@@ -221,6 +246,7 @@ int enqueue_pool_sweep(su2gpu_pool* P, const void* descs, const int2* const* til
       for (int par = 0; par <= 1; par++) {
         a.parity = par; a.sub = mu; a.alg = p.algorithm_su2link; a.pass = pass++;
         a.tiles = tiles[vt(0)];
+        mark(P, 0);
         P->ops->pool_link(vt(0), a, P->ntiles[vt(0)], P->st);
         tot[SU2GPU_C_TOTAL_SU2LINK] += 1;
       }
@@ -229,6 +255,7 @@ int enqueue_pool_sweep(su2gpu_pool* P, const void* descs, const int2* const* til
         for (int par = 0; par <= 1; par++) {
           a.parity = par; a.sub = mu; a.alg = 0; a.pass = pass++;
           a.tiles = tiles[vt(1)];
+          mark(P, 1);
           P->ops->pool_u1(vt(1), a, P->ntiles[vt(1)], P->st);
           tot[SU2GPU_C_TOTAL_U1LINK] += 1;
         }
@@ -252,6 +279,7 @@ int enqueue_pool_sweep(su2gpu_pool* P, const void* descs, const int2* const* til
             a.parity = par; a.sub = h; a.alg = force; a.pass = pass++;
             int kind = 2 + fd.field;
             a.tiles = tiles[vt(kind)];
+            mark(P, kind);
             P->ops->pool_scalar(vt(kind), fd.field, a, P->ntiles[vt(kind)], P->st);
             bool orr = fd.alg == SU2GPU_OVERRELAX && !force;
             int idx = fd.field == 0 ? (orr ? SU2GPU_C_TOTAL_OR_DOUBLET : SU2GPU_C_TOTAL_DOUBLET) + h
@@ -261,6 +289,7 @@ int enqueue_pool_sweep(su2gpu_pool* P, const void* descs, const int2* const* til
           }
       }
   }
+  mark(P, -1);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(SU2GPU_ERR_CUDA, "pool sweep launch: %s", cudaGetErrorString(e));
   return SU2GPU_OK;
@@ -302,10 +331,11 @@ int su2gpu_pool_create(const su2gpu_params* recipe, int64_t arena_bytes, int32_t
   P->max_slots = max_chains;
   P->slots.resize(max_chains);
   int rc;
-  if (cudaStreamCreateWithFlags(&P->st, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&P->own_st, cudaStreamNonBlocking) != cudaSuccess) {
     delete P;
     return fail(SU2GPU_ERR_CUDA, "cudaStreamCreate failed");
   }
+  P->st = P->own_st;
   size_t dsz = P->prec == 64 ? sizeof(ChainDesc<double>) : sizeof(ChainDesc<float>);
   if ((rc = P->arena.ensure((size_t)arena_bytes)) || (rc = P->slotmem.ensure((size_t)max_chains * 256)) ||
       (rc = P->descs.ensure(dsz * max_chains)) || (rc = P->err.ensure(256))) {
@@ -326,11 +356,12 @@ int su2gpu_pool_create(const su2gpu_params* recipe, int64_t arena_bytes, int32_t
 int su2gpu_pool_destroy(su2gpu_pool* P) {
   if (!P) return SU2GPU_OK;
   if (P->st) cudaStreamSynchronize(P->st);
+  if (P->own_st) cudaStreamSynchronize(P->own_st);
   if (P->gexec) cudaGraphExecDestroy(P->gexec);
   P->arena.release(); P->slotmem.release(); P->descs.release(); P->mtiles.release(); P->mfirst.release();
   P->sweepptrs.release(); P->partials.release(); P->sums.release(); P->stage.release(); P->err.release();
   for (int v = 0; v < NVARIANTS; v++) P->tiles[v].release();
-  if (P->st) cudaStreamDestroy(P->st);
+  if (P->own_st) cudaStreamDestroy(P->own_st);
   delete P;
   return SU2GPU_OK;
 }
@@ -455,8 +486,8 @@ int su2gpu_pool_set_sweep(su2gpu_pool* P, int32_t s, uint32_t sweep) {
   return SU2GPU_OK;
 }
 
-int su2gpu_pool_run(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
-  if (!P || nsweeps < 0) return SU2GPU_ERR_INVALID;
+static int pool_enqueue(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
+  if (!P || nsweeps < 0) return fail(SU2GPU_ERR_INVALID, "bad pool run arguments");
   int rc;
   if (P->dirty && (rc = rebuild(P))) return rc;
   if (P->active.empty() || !nsweeps) return SU2GPU_OK;
@@ -466,10 +497,14 @@ int su2gpu_pool_run(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
   if (use_graph) {
     if (!P->gexec) {
       cudaGraph_t graph;
+      cudaStream_t exec = P->st;
+      PCK(cudaStreamSynchronize(exec));
+      P->st = P->own_st;
       PCK(cudaStreamBeginCapture(P->st, cudaStreamCaptureModeThreadLocal));
       rc = enqueue_pool_sweep(P, P->descs.p, tiles, nullptr, tot);
       launch_pool_next_sweep((uint32_t* const*)P->sweepptrs.p, (int)P->active.size(), P->st);
       cudaError_t e = cudaStreamEndCapture(P->st, &graph);
+      P->st = exec;
       if (rc) return rc;
       if (e != cudaSuccess) return fail(SU2GPU_ERR_CUDA, "pool graph capture: %s", cudaGetErrorString(e));
       e = cudaGraphInstantiate(&P->gexec, graph, 0);
@@ -489,11 +524,87 @@ int su2gpu_pool_run(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
   }
   for (int s : P->active)
     for (int k = 0; k < SU2GPU_NCOUNTERS; k++) P->slots[s].tot[k] += tot[k] * (int64_t)P->slots[s].g.half * nsweeps;
+  return SU2GPU_OK;
+}
+
+static int pool_check(su2gpu_pool* P) {
   PCK(cudaStreamSynchronize(P->st));
   int herr = 0;
-  PCK(cudaMemcpy(&herr, P->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+  PCK(cudaMemcpyAsync(&herr, P->err.p, sizeof(int), cudaMemcpyDeviceToHost, P->st));
+  PCK(cudaStreamSynchronize(P->st));
   if (herr) return fail(SU2GPU_ERR_KERNEL, "a pool kernel reported an invalid state (NaN fields?)");
   return SU2GPU_OK;
+}
+
+int su2gpu_pool_run(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
+  int rc = pool_enqueue(P, nsweeps, use_graph);
+  if (rc) return rc;
+  return pool_check(P);
+}
+
+int su2gpu_pool_enqueue(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
+  return pool_enqueue(P, nsweeps, use_graph);
+}
+
+int su2gpu_pool_set_stream(su2gpu_pool* P, void* stream) {
+  if (!P) return SU2GPU_ERR_INVALID;
+  PCK(cudaStreamSynchronize(P->st));
+  P->st = stream ? (cudaStream_t)stream : P->own_st;
+  return SU2GPU_OK;
+}
+
+int su2gpu_pool_launches_per_sweep(su2gpu_pool* P, int32_t* n) {
+  if (!P || !n) return SU2GPU_ERR_INVALID;
+  // the recipe's passes per sweep, in the order of enqueue_pool_sweep
+  const su2gpu_params& p = P->recipe;
+  const int nh = nhiggs_of(p.content);
+  int passes = p.update_links * 6 * (1 + ((p.content & SU2GPU_U1) ? 1 : 0));
+  int nsw = p.scalar_sweeps + 1;
+  auto count = [&](int upd, int alg, int rep) {
+    int c = 0;
+    for (int s = 0; s < nsw; s++)
+      for (int k = 0; k < upd; k++) {
+        if (s >= nsw - 1 && alg != SU2GPU_OVERRELAX) continue;
+        c += 2 * rep;
+      }
+    return c;
+  };
+  if (nh) passes += count(p.update_su2doublet, p.algorithm_su2doublet, nh);
+  if (p.content & SU2GPU_TRIPLET) passes += count(p.update_su2triplet, p.algorithm_su2triplet, 1);
+  if (p.content & SU2GPU_SINGLET) passes += count(p.update_singlet, p.algorithm_singlet, 1);
+  *n = passes + 1;  // + the sweep-counter increment
+  return SU2GPU_OK;
+}
+
+// one sweep of every chain with CUDA events around every pass (the chains advance)
+int su2gpu_pool_profile_sweep(su2gpu_pool* P, int32_t maxp, int32_t* kinds, float* ms, int32_t* npasses) {
+  if (!P || !kinds || !ms || !npasses) return SU2GPU_ERR_INVALID;
+  int rc;
+  if (P->dirty && (rc = rebuild(P))) return rc;
+  *npasses = 0;
+  if (P->active.empty()) return SU2GPU_OK;
+  const int2* tiles[NVARIANTS];
+  for (int v = 0; v < NVARIANTS; v++) tiles[v] = (const int2*)P->tiles[v].p;
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> kd;
+  int64_t tot[SU2GPU_NCOUNTERS] = {0};
+  P->prof = &ev;
+  P->prof_kind = &kd;
+  rc = enqueue_pool_sweep(P, P->descs.p, tiles, nullptr, tot);
+  P->prof = nullptr;
+  P->prof_kind = nullptr;
+  if (!rc) launch_pool_next_sweep((uint32_t* const*)P->sweepptrs.p, (int)P->active.size(), P->st);
+  for (int s : P->active)
+    for (int k = 0; k < SU2GPU_NCOUNTERS; k++) P->slots[s].tot[k] += tot[k] * (int64_t)P->slots[s].g.half;
+  if (!rc) rc = pool_check(P);
+  int n = 0;
+  for (size_t k = 0; !rc && k + 1 < ev.size() && n < maxp; k++, n++) {
+    kinds[n] = kd[k];
+    cudaEventElapsedTime(&ms[n], ev[k], ev[k + 1]);
+  }
+  for (cudaEvent_t e : ev) cudaEventDestroy(e);
+  *npasses = n;
+  return rc;
 }
 
 int su2gpu_pool_active(su2gpu_pool* P, int32_t* slots, int32_t max, int32_t* n) {
@@ -509,8 +620,7 @@ int su2gpu_pool_active(su2gpu_pool* P, int32_t* slots, int32_t max, int32_t* n) 
 }
 
 // measure() sums of every active chain, in slot order: sums[k*NMEAS + m]
-int su2gpu_pool_measure(su2gpu_pool* P, double* sums, int32_t max_chains, int32_t* nchains) {
-  if (!P || !sums || !nchains) return SU2GPU_ERR_INVALID;
+static int pool_enqueue_measure(su2gpu_pool* P, double* dev_out, int32_t max_chains, int32_t* nchains) {
   int rc;
   if (P->dirty && (rc = rebuild(P))) return rc;
   int n = (int)P->active.size();
@@ -520,14 +630,27 @@ int su2gpu_pool_measure(su2gpu_pool* P, double* sums, int32_t max_chains, int32_
   PoolArgs a;
   memset(&a, 0, sizeof(a));
   a.descs = P->descs.p;
+  a.nslots = P->max_slots;
   a.tiles = (const int2*)P->mtiles.p;
   a.err = (int*)P->err.p;
   P->ops->pool_measure(a, (double*)P->partials.p, P->nmtiles, P->st);
-  launch_pool_reduce((const double*)P->partials.p, P->nmtiles, (const int*)P->mfirst.p, n, (double*)P->sums.p, P->st);
+  launch_pool_reduce((const double*)P->partials.p, P->nmtiles, (const int*)P->mfirst.p, n, dev_out, P->st);
   PCK(cudaGetLastError());
-  PCK(cudaMemcpyAsync(sums, P->sums.p, (size_t)n * NSUMS * 8, cudaMemcpyDeviceToHost, P->st));
+  return SU2GPU_OK;
+}
+
+int su2gpu_pool_measure(su2gpu_pool* P, double* sums, int32_t max_chains, int32_t* nchains) {
+  if (!P || !sums || !nchains) return SU2GPU_ERR_INVALID;
+  int rc = pool_enqueue_measure(P, (double*)P->sums.p, max_chains, nchains);
+  if (rc || !*nchains) return rc;
+  PCK(cudaMemcpyAsync(sums, P->sums.p, (size_t)*nchains * NSUMS * 8, cudaMemcpyDeviceToHost, P->st));
   PCK(cudaStreamSynchronize(P->st));
   return SU2GPU_OK;
+}
+
+int su2gpu_pool_enqueue_measure(su2gpu_pool* P, double* device_sums, int32_t max_chains, int32_t* nchains) {
+  if (!P || !device_sums || !nchains) return SU2GPU_ERR_INVALID;
+  return pool_enqueue_measure(P, device_sums, max_chains, nchains);
 }
 
 int su2gpu_pool_counters(su2gpu_pool* P, int32_t s, int64_t* out) {
@@ -561,6 +684,7 @@ int su2gpu_pool_autotune(su2gpu_pool* P, int32_t* choices, float* best_ms) {
   PoolArgs a;
   memset(&a, 0, sizeof(a));
   a.descs = desc2.p;
+  a.nslots = P->max_slots;
   a.err = (int*)P->err.p;
   const int reps = 3;
   for (int kind = 0; kind < 5; kind++) {

@@ -22,12 +22,21 @@ struct __align__(16) ChainDesc {
 };
 
 struct PoolArgs {
-  const void* descs;  // ChainDesc<R>[slots]
+  const void* descs;  // ChainDesc<R>[nslots]
   const int2* tiles;  // (slot, first site of the tile inside the parity / lattice)
+  int nslots;
   int parity, sub, alg;
   uint32_t pass;
   int* err;
 };
+
+// a tile whose slot lies outside the descriptor table (a corrupted table)
+// is reported through the error flag and skipped by the whole block
+__device__ inline bool bad_tile(const PoolArgs& a, int2 tile) {
+  if ((unsigned)tile.x < (unsigned)a.nslots && tile.y >= 0) return false;
+  if (threadIdx.x == 0) atomicOr(a.err, 2);
+  return true;
+}
 
 template <typename R>
 __device__ inline const ChainDesc<R>& stage_desc(const PoolArgs& a, int slot) {
@@ -44,6 +53,7 @@ __device__ inline const ChainDesc<R>& stage_desc(const PoolArgs& a, int slot) {
 template <typename R, int CC, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_pool_link(PoolArgs a) {
   int2 tile = a.tiles[blockIdx.x];
+  if (bad_tile(a, tile)) return;
   const ChainDesc<R>& d = stage_desc<R>(a, tile.x);
   const CoupT<R>& cp = d.cp;
   int t = tile.y + threadIdx.x;
@@ -64,6 +74,7 @@ __global__ void __launch_bounds__(BS, MINB) k_pool_link(PoolArgs a) {
 template <typename R, int CC, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_pool_u1(PoolArgs a) {
   int2 tile = a.tiles[blockIdx.x];
+  if (bad_tile(a, tile)) return;
   const ChainDesc<R>& d = stage_desc<R>(a, tile.x);
   int t = tile.y + threadIdx.x;
   int acc = 0;
@@ -80,6 +91,7 @@ __global__ void __launch_bounds__(BS, MINB) k_pool_u1(PoolArgs a) {
 template <typename R, int CC, int FIELD, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_pool_scalar(PoolArgs a) {
   int2 tile = a.tiles[blockIdx.x];
+  if (bad_tile(a, tile)) return;
   const ChainDesc<R>& d = stage_desc<R>(a, tile.x);
   const CoupT<R>& cp = d.cp;
   int t = tile.y + threadIdx.x;
@@ -123,6 +135,7 @@ __global__ void k_pool_next_sweep(uint32_t* const* sweeps, int n) {
 template <typename R, int CC>
 __global__ void __launch_bounds__(BLOCK) k_pool_measure(PoolArgs a, const double* alpha_unused, double* partials) {
   int2 tile = a.tiles[blockIdx.x];
+  if (bad_tile(a, tile)) return;
   const ChainDesc<R>& d = stage_desc<R>(a, tile.x);
   const CoupT<R>& cp = d.cp;
   const Fields<R>& f = d.f;

@@ -86,6 +86,11 @@ def lib():
         L.su2gpu_pool_counters.argtypes = [vp, i32, vp]
         L.su2gpu_pool_autotune.argtypes = [vp, vp, vp]
         L.su2gpu_pool_set_variants.argtypes = [vp, vp]
+        L.su2gpu_pool_enqueue.argtypes = [vp, i32, i32]
+        L.su2gpu_pool_enqueue_measure.argtypes = [vp, vp, i32, ctypes.POINTER(i32)]
+        L.su2gpu_pool_set_stream.argtypes = [vp, vp]
+        L.su2gpu_pool_launches_per_sweep.argtypes = [vp, ctypes.POINTER(i32)]
+        L.su2gpu_pool_profile_sweep.argtypes = [vp, i32, vp, vp, ctypes.POINTER(i32)]
         L.su2gpu_pool_grad_flow.argtypes = [vp, i32, ctypes.c_double, ctypes.c_double, i32, vp, i32,
                                             ctypes.POINTER(i32)]
         _lib = L
@@ -355,9 +360,17 @@ class Pool:
                 for n in FIELD_NAMES]
         check(lib().su2gpu_pool_upload(self._h, slot, *[_p(a) for a in arrs]))
 
-    def download(self, slot):
-        out = {n: (None if shp is None else np.zeros(shp)) for n, shp in _shapes(self._params[slot]).items()}
-        check(lib().su2gpu_pool_download(self._h, slot, *[_p(out[n]) for n in FIELD_NAMES]))
+    def download(self, slot, out=None):
+        """The chain's FP64 host fields; `out` (a dict of C-contiguous float64
+        arrays of the right shapes) receives them in place when given."""
+        shapes = _shapes(self._params[slot])
+        if out is None:
+            out = {n: (None if shp is None else np.zeros(shp)) for n, shp in shapes.items()}
+        for n, shp in shapes.items():
+            a = out.get(n)
+            if a is not None and (a.shape != shp or a.dtype != np.float64 or not a.flags.c_contiguous):
+                raise ValueError(f"{n}: need a C-contiguous float64 array of shape {shp}")
+        check(lib().su2gpu_pool_download(self._h, slot, *[_p(out.get(n)) for n in FIELD_NAMES]))
         return out
 
     def set_sweep(self, slot, sweep):
@@ -373,6 +386,31 @@ class Pool:
         n = ctypes.c_int32()
         check(lib().su2gpu_pool_measure(self._h, _p(out), out.shape[0], ctypes.byref(n)))
         return {int(s): out[k].copy() for k, s in enumerate(slots)}
+
+    def enqueue(self, nsweeps, graph=True):
+        check(lib().su2gpu_pool_enqueue(self._h, nsweeps, 1 if graph else 0))
+
+    def enqueue_measure(self, device_ptr, max_chains):
+        """Measurement of every active chain into a device buffer of
+        max_chains * NMEAS doubles (asynchronous); returns the chain count."""
+        n = ctypes.c_int32()
+        check(lib().su2gpu_pool_enqueue_measure(self._h, ctypes.c_void_p(device_ptr), max_chains, ctypes.byref(n)))
+        return n.value
+
+    def set_stream(self, stream_ptr):
+        check(lib().su2gpu_pool_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)))
+
+    def launches_per_sweep(self):
+        n = ctypes.c_int32()
+        check(lib().su2gpu_pool_launches_per_sweep(self._h, ctypes.byref(n)))
+        return n.value
+
+    def profile_sweep(self, max_passes=512):
+        kinds = np.zeros(max_passes, dtype=np.int32)
+        ms = np.zeros(max_passes, dtype=np.float32)
+        n = ctypes.c_int32()
+        check(lib().su2gpu_pool_profile_sweep(self._h, max_passes, _p(kinds), _p(ms), ctypes.byref(n)))
+        return kinds[:n.value], ms[:n.value]
 
     def counters(self, slot):
         out = np.zeros(abi.NCOUNTERS, dtype=np.int64)

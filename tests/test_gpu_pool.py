@@ -1,10 +1,15 @@
 """Pools of independent chains (the batched form) through the C ABI.
 
 * A chain of a pool follows the trajectory of a single-lattice context with
-  the same parameters, seed and chain id: fields and counters bit for bit,
-  measure() sums to 1e-12 relative (the per-chain reduction order differs).
+  the same parameters, seed and chain id: the same random numbers and
+  accept/reject decisions (counters equal), fields equal to rounding -- the
+  per-site arithmetic is the same source compiled into two kernels, whose
+  fused multiply-adds the compiler may form differently (1e-11 absolute after
+  three FP64 sweeps, as the oracle parity tests; 1e-4 for FP32 fields) --
+  and measure() sums to 1e-12 relative (FP64) or 1e-6 (FP32).
 * Membership does not change a chain's trajectory: a chain alone and the
-  same chain among others, admitted and retired around it, agree bit for bit.
+  same chain among others, admitted and retired around it, agree bit for bit
+  (one kernel, random numbers keyed by chain and site).
 * FP64 pool chains against the oracle (1e-9 after two sweeps, as the
   single-lattice parity tests).
 * Admission by arena footprint; autotuning does not advance the chains;
@@ -30,7 +35,15 @@ def gpu():
 def fields_equal(a, b):
     for n in a:
         if a[n] is not None:
-            assert np.array_equal(a[n], b[n]), n
+            d = np.abs(a[n] - b[n])
+            assert np.array_equal(a[n], b[n]), (n, float(d.max()), int(np.count_nonzero(d)), d.size)
+
+
+def fields_close(a, b, atol):
+    for n in a:
+        if a[n] is not None:
+            d = np.abs(a[n] - b[n])
+            assert d.max() < atol, (n, float(d.max()), int(np.count_nonzero(d)), d.size)
 
 
 def chain_specs(content, precision):
@@ -71,11 +84,12 @@ def test_pool_chains_equal_single_lattices(gpu, content, precision, graph):
     pool.run(2, graph=graph)
     pool.run(1, graph=graph)
     sums = pool.measure()
+    atol, rtol = (1e-11, 1e-12) if precision == 64 else (1e-4, 1e-6)
     for s, (p, seed, chain), f in zip(slots, specs, inputs):
         want_f, want_c, want_m = single_run(gpu, p, f, seed, chain, 3)
-        fields_equal(pool.download(s), want_f)
+        fields_close(pool.download(s), want_f, atol)
         assert np.array_equal(pool.counters(s), want_c)
-        ok, k, a, b = measure_close(sums[s], want_m, 1e-12)
+        ok, k, a, b = measure_close(sums[s], want_m, rtol)
         assert ok, (s, k, a, b)
 
 
@@ -172,7 +186,8 @@ def test_pool_autotune_does_not_advance(gpu):
     for s, (p, seed, chain) in zip(slots, specs):
         lat = gpu.Lattice(p, seed=seed, chain=chain)
         lat.run_sweeps(0, 3, graph=False)
-        fields_equal(pool.download(s), lat.download())
+        fields_close(pool.download(s), lat.download(), 1e-4)
+        assert np.array_equal(pool.counters(s), lat.counters())
 
 
 def test_pool_grad_flow_equals_lattice(gpu):
@@ -188,3 +203,46 @@ def test_pool_grad_flow_equals_lattice(gpu):
     assert rp.shape == rl.shape
     assert np.array_equal(rp, rl)
     fields_equal(pool.download(s), f)
+
+
+def test_pool_ensemble_async_api(gpu):
+    """A 64-chain slice of the batched ensemble (sides 8..48) through the
+    asynchronous entry points: enqueue on a caller stream, measurement into a
+    device buffer, profiled sweeps; chains still equal single lattices."""
+    import torch
+    from su2higgs_gb300 import workloads
+    specs = workloads.batched_ensemble(64, seed=77)
+    arena = sum(gpu.Pool.chain_bytes(p) for p, _, _ in specs)
+    pool = gpu.Pool(specs[0][0], arena_bytes=arena, max_chains=64)
+    slots = []
+    for p, seed, chain in specs:
+        s = pool.add(p, seed=seed, chain=chain)
+        pool.upload(s, **workloads.hot_fields(p, seed))
+        slots.append(s)
+    assert pool.info()["free_bytes"] == 0
+    assert pool.launches_per_sweep() == 6 + 10 + 1
+    stream = torch.cuda.Stream()
+    sums = torch.zeros((64, abi.NMEAS), dtype=torch.float64, device="cuda")
+    pool.set_stream(stream.cuda_stream)
+    with torch.cuda.stream(stream):
+        pool.enqueue(2, graph=True)
+        assert pool.enqueue_measure(sums.data_ptr(), 64) == 64
+    stream.synchronize()
+    pool.set_stream(None)
+    pool.run(0)
+    kinds, ms = pool.profile_sweep()
+    assert sorted(set(kinds.tolist())) == [0, 3] and len(kinds) == 16 and np.all(ms > 0)
+    host_sums = pool.measure()
+    dev = sums.cpu().numpy()
+    for k in range(0, 64, 8):
+        p, seed, chain = specs[k]
+        lat = gpu.Lattice(p, seed=seed, chain=chain)
+        lat.upload(**workloads.hot_fields(p, seed))
+        lat.run_sweeps(0, 2, graph=True)
+        ok, i, a, b = measure_close(dev[k], lat.measure(), 1e-6)
+        assert ok, (k, i, a, b)
+        lat.run_sweeps(2, 1, graph=False)
+        fields_close(pool.download(slots[k]), lat.download(), 1e-4)
+        assert np.array_equal(pool.counters(slots[k]), lat.counters())
+        ok, i, a, b = measure_close(host_sums[slots[k]], lat.measure(), 1e-6)
+        assert ok, (k, i, a, b)
