@@ -187,11 +187,12 @@ def _cpu_chain_worker(args):
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from native import Fields, Oracle
     from su2higgs_gb300 import abi, workloads
-    L, beta, msq, b4, seed, chain = args
-    p = abi.make_params("adj", L=(L, L, L), precision=64, betasu2=beta, msq_triplet=msq, b4=b4)
+    content, L, beta, msq, seed, chain = args
+    kw = dict(msq_triplet=msq, b4=0.005) if content == "adj" else dict(msq_phi=msq)
+    p = abi.make_params(content, L=(L, L, L), precision=64, betasu2=beta, **kw)
     f = workloads.hot_fields(p, seed)
     o = Oracle(p)
-    o.put(Fields(p, link=f["link"], trip=f["trip"]))
+    o.put(Fields(p, **f))
     o.set_rng(seed, 0, chain)
     t0 = time.perf_counter()
     o.update()
@@ -205,18 +206,26 @@ def run_reference_batched(args):
     through it), one process per core, largest first so that the cores stay
     balanced as they would over a long run; a step lasts as long as the
     busiest core's sweeps (set-up excluded, as on the GPU)."""
-    from su2higgs_gb300 import workloads
+    from su2higgs_gb300 import serve, workloads
     import multiprocessing as mp
-    nchains, S = BATCHED[args.workload]
-    specs = workloads.batched_ensemble(nchains)
+    if args.workload == "served":
+        # requests with L <= 32 only, so that a step stays well under a
+        # second: the CPU sweep's cost per site does not depend on L
+        stream = serve.make_stream(args.serve_rate, args.serve_window, seed=20261203)
+        jobs = [(r.content, r.L, r.betasu2, r.msq, r.seed, r.rid) for r in stream if r.L <= 32]
+        nchains, what = len(jobs), "requests (L <= 32) of the served stream"
+    else:
+        nchains, S = BATCHED[args.workload]
+        specs = workloads.batched_ensemble(nchains)
+        jobs = [("adj", int(p.L[0]), float(p.betasu2), float(p.msq_triplet), seed, chain) for p, seed, chain in specs]
+        what = "chains of the batched ensemble"
     cores = os.cpu_count() or 1
-    jobs = [(int(p.L[0]), float(p.betasu2), float(p.msq_triplet), float(p.b4), seed, chain) for p, seed, chain in specs]
     ctx = mp.get_context("spawn")
     done, wall, nxt = 0, 0.0, 0
     per_step = 4 * cores
     with ctx.Pool(cores) as pool:
         for s in range(args.warmup + args.steps):
-            batch = sorted((jobs[(nxt + k) % len(jobs)] for k in range(per_step)), key=lambda j: -j[0])
+            batch = sorted((jobs[(nxt + k) % len(jobs)] for k in range(per_step)), key=lambda j: -j[1])
             nxt += per_step
             res = pool.map(_cpu_chain_worker, batch, chunksize=1)
             if s < args.warmup:
@@ -231,11 +240,11 @@ def run_reference_batched(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "site-updates/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / max(args.steps, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": args.workload, "content": "SU(2) + adjoint Higgs", "chains": nchains,
-                   "sample": f"{per_step} chains of the ensemble per step, one sweep + measure each"},
+        "config": {"workload": args.workload, "chains": nchains,
+                   "sample": f"{per_step} {what} per step, one sweep + measure each"},
         "cpu_baseline": {"value": value, "unit": "site-updates/s", "cores": cores, "kind": "port",
-                         "sample": f"{per_step} ensemble chains per step (one process per core, cycling through the "
-                                   f"{nchains} chains), 1 sweep + measure each; oracle C restatement of the "
+                         "sample": f"{per_step} {what} per step (one process per core, cycling through "
+                                   f"{nchains} of them), 1 sweep + measure each; oracle C restatement of the "
                                    "reference's serial sweep"},
         "e2e": {"value": value, "unit": "site-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -246,7 +255,7 @@ def run_reference(args):
     rank, world, _ = env_rank()
     if rank != 0:
         return
-    if args.workload in BATCHED:
+    if args.workload in BATCHED or args.workload == "served":
         return run_reference_batched(args)
     content, L, prec = WORKLOADS[args.workload]
     import multiprocessing as mp
@@ -696,15 +705,95 @@ def run_gpu_batched(args):
         dist.destroy_process_group()
 
 
+def run_gpu_served(args):
+    """The served stream: Poisson arrivals of single-chain requests (side L
+    in {16,32,64,96,128}, content fundamental / adjoint / SU(2)xU(1)+singlet,
+    500-5000 sweeps, 30% with a gradient flow t = 0..4, dt = 0.01) played in
+    real time through the continuous-batching server; arrivals stop after
+    --serve-window seconds and the run ends --serve-drain seconds later."""
+    from su2higgs_gb300 import abi, gpu, serve
+
+    rank, world, local = env_rank()
+    gpu.lib()
+    rate, window, drain = args.serve_rate, args.serve_window, args.serve_drain
+    stream = serve.make_stream(rate, window, seed=20261203 + rank)
+    arena = int(args.serve_arena_gb * (1 << 30))
+    srv = serve.Server(gpu.Pool, gpu.Pool.chain_bytes, arena_bytes=arena, max_chains=1024,
+                       quantum=args.serve_quantum)
+    clocks = ClockSampler(local)
+    clocks.start()
+    t0 = time.perf_counter()
+    res = srv.serve(stream, deadline=window + drain)
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    srv.close()
+    done = list(res.values())
+    lat = np.array([r.latency for r in done]) if done else np.array([np.nan])
+    offered = sum(r.sweeps * r.L ** 3 for r in stream) / window
+    value = world * srv.site_updates / wall
+
+    # the plain FP64 sweep run serially: one single-lattice FP64 context per
+    # sampled request, a few sweeps each
+    fp64 = None
+    if rank == 0 and not args.no_fp64:
+        tot_sites, tot_s = 0, 0.0
+        sample = stream[:: max(1, len(stream) // 15)][:15]
+        for r in sample:
+            p64 = r.params(64)
+            lat64 = gpu.Lattice(p64, seed=r.seed, chain=r.rid)
+            n = 5
+            lat64.run_sweeps(0, 1, graph=True)
+            t1 = time.perf_counter()
+            lat64.run_sweeps(1, n, graph=True)
+            tot_s += time.perf_counter() - t1
+            tot_sites += p64.sites() * n
+            lat64.close()
+        v64 = tot_sites / tot_s
+        fp64 = {"value": v64, "unit": "site-updates/s", "requests_sampled": len(sample),
+                "served_over_fp64_plain": value / world / v64,
+                "what": "sampled requests as FP64 single-lattice contexts, 5 sweeps each, one after another"}
+    d2h = sum(r.sums.nbytes + r.counters.nbytes + (0 if r.flow_rows is None else r.flow_rows.nbytes) for r in done)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "site-updates/s", "n_gpus": world, "steps": len(done),
+            "warmup": 0, "ms_per_step": 1e3 * wall / max(len(done), 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "served", "arrival_rate_per_s": rate, "arrival_window_s": window,
+                       "drain_s": drain, "requests": len(stream), "sides": list(serve.SIDES),
+                       "contents": list(serve.CONTENTS), "sweeps": list(serve.SWEEPS),
+                       "flow_fraction": serve.FLOW_FRACTION, "flow": serve.FLOW,
+                       "arena_per_content_gb": args.serve_arena_gb, "quantum_sweeps": args.serve_quantum,
+                       "precision": "FP32 fields, FP64 reductions", "start": "cold",
+                       "parallelism": f"replicas x{world}"},
+            "serving": {"completed": len(done), "unfinished": srv.unfinished,
+                        "p50_latency_s": float(np.percentile(lat, 50)),
+                        "p99_latency_s": float(np.percentile(lat, 99)),
+                        "mean_queue_s": float(np.mean([r.admitted - r.arrival for r in done])) if done else None,
+                        "offered_site_updates_per_s": offered, "achieved_over_offered": value / world / offered,
+                        "completed_site_updates": int(sum(r.sweeps * r.sites for r in done))},
+            "e2e": {"value": value, "unit": "site-updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": d2h / max(len(done), 1),
+                    "what": "wall clock of the whole served run: requests in, results (sums, counters, flow rows) "
+                            "back to the host; chains start cold on the device"},
+            "fp64_plain": fp64, "clocks": clk, "wall_s": wall,
+        }
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--workload", default="batched384_adj_f32", choices=sorted(WORKLOADS) + sorted(BATCHED))
+    ap.add_argument("--workload", default="batched384_adj_f32", choices=sorted(WORKLOADS) + sorted(BATCHED) + ["served"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison")
+    ap.add_argument("--serve-rate", type=float, default=20.0, help="served: arrivals per second")
+    ap.add_argument("--serve-window", type=float, default=30.0, help="served: seconds of arrivals")
+    ap.add_argument("--serve-drain", type=float, default=30.0, help="served: seconds after the last arrival")
+    ap.add_argument("--serve-arena-gb", type=float, default=24.0, help="served: device arena per content (GB)")
+    ap.add_argument("--serve-quantum", type=int, default=50, help="served: sweeps per scheduling round")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -712,6 +801,8 @@ def main():
         run_reference(args)
     elif args.workload in BATCHED:
         run_gpu_batched(args)
+    elif args.workload == "served":
+        run_gpu_served(args)
     else:
         run_gpu(args)
 

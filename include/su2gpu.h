@@ -319,6 +319,11 @@ int su2gpu_pool_counters(su2gpu_pool* pool, int32_t slot, int64_t* out);
  * runs on a scratch copy, the chains do not advance). */
 int su2gpu_pool_autotune(su2gpu_pool* pool, int32_t* choices, float* best_ms);
 int su2gpu_pool_set_variants(su2gpu_pool* pool, const int32_t* choices);
+/* Copy one chain out of the pool into a new single-lattice context (same
+ * parameters, seed and chain id; release it with su2gpu_destroy).  The chain
+ * stays in the pool; the copy can go on (e.g. a gradient flow) while the pool
+ * runs on. */
+int su2gpu_pool_extract(su2gpu_pool* pool, int32_t slot, su2gpu_ctx** out);
 /* Gradient flow of one chain (as su2gpu_grad_flow; the chain is unchanged). */
 int su2gpu_pool_grad_flow(su2gpu_pool* pool, int32_t slot, double t_max, double dt, int32_t meas_interval,
                           double* rows, int32_t maxrows, int32_t* nrows);

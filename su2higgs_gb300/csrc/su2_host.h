@@ -58,3 +58,8 @@ SU2_HIDDEN void su2gpu_record_error(const char* msg);
 // su2gpu_destroy leaves the fields alone.  Used for per-chain operations of a
 // pool (gradient flow).
 SU2_HIDDEN int su2gpu_attach(const su2gpu_params* p, void* fields, su2gpu_ctx** out);
+
+// A context with its own copy of the fields at `fields` (device memory laid out
+// by carve() for p), seeded with (seed, chain); no cold start.
+SU2_HIDDEN int su2gpu_create_copy(const su2gpu_params* p, const void* fields, uint64_t seed, uint32_t chain,
+                                  su2gpu_ctx** out);

@@ -736,6 +736,15 @@ int su2gpu_pool_set_variants(su2gpu_pool* P, const int32_t* choices) {
 
 }  // extern "C"
 
+// a chain copied out of the pool into a single-lattice context of its own
+// (same parameters, seed and chain id; the chain stays in the pool)
+extern "C" int su2gpu_pool_extract(su2gpu_pool* P, int32_t s, su2gpu_ctx** out) {
+  if (!P || !out || s < 0 || s >= P->max_slots || !P->slots[s].active) return fail(SU2GPU_ERR_INVALID, "no such chain slot");
+  PCK(cudaStreamSynchronize(P->st));
+  const Slot& sl = P->slots[s];
+  return su2gpu_create_copy(&sl.p, (const char*)P->arena.p + sl.off, sl.seed, sl.chain, out);
+}
+
 // gradient flow of one chain (gradflow.c:46-173): a context over the chain's
 // fields in the arena runs the single-lattice flow on its own copies
 extern "C" int su2gpu_pool_grad_flow(su2gpu_pool* P, int32_t s, double t_max, double dt, int32_t meas_interval,

@@ -214,7 +214,7 @@ int64_t su2gpu_footprint_bytes(const su2gpu_params* p) {
   return (int64_t)b;
 }
 
-static int create_ctx(const su2gpu_params* p, void* borrowed, su2gpu_ctx** out) {
+static int create_ctx(const su2gpu_params* p, void* borrowed, const void* copy_from, su2gpu_ctx** out) {
   if (!out) return SU2GPU_ERR_INVALID;
   *out = nullptr;
   if (!valid_params(p)) return SU2GPU_ERR_INVALID;
@@ -258,14 +258,15 @@ static int create_ctx(const su2gpu_params* p, void* borrowed, su2gpu_ctx** out) 
   c->d_err = (int*)((char*)c->ctrbuf.p + 512);
   c->d_sweep = (uint32_t*)((char*)c->ctrbuf.p + 1024);
   c->d_fz = (unsigned long long*)((char*)c->ctrbuf.p + 1536);
-  if ((!borrowed && cudaMemsetAsync(c->fields.p, 0, c->fields.n, c->st) != cudaSuccess) ||
+  if ((!borrowed && !copy_from && cudaMemsetAsync(c->fields.p, 0, c->fields.n, c->st) != cudaSuccess) ||
+      (copy_from && cudaMemcpyAsync(c->fields.p, copy_from, c->fields.n, cudaMemcpyDeviceToDevice, c->st) != cudaSuccess) ||
       cudaMemsetAsync(c->ctrbuf.p, 0, c->ctrbuf.n, c->st) != cudaSuccess) {
     set_err("cudaMemset failed");
     su2gpu_destroy(c);
     return SU2GPU_ERR_CUDA;
   }
   // cold links: unit quaternions (setsu2, init.c:18-28)
-  if (!borrowed) {
+  if (!borrowed && !copy_from) {
     std::vector<double> one((size_t)V * 12, 0.0);
     for (int64_t k = 0; k < V * 3; k++) one[(size_t)k * 4] = 1.0;
     if ((rc = c->stage.ensure((size_t)V * 12 * 8))) { su2gpu_destroy(c); return rc; }
@@ -281,7 +282,7 @@ static int create_ctx(const su2gpu_params* p, void* borrowed, su2gpu_ctx** out) 
       return SU2GPU_ERR_CUDA;
     }
   }
-  if (borrowed && cudaStreamSynchronize(c->st) != cudaSuccess) {
+  if ((borrowed || copy_from) && cudaStreamSynchronize(c->st) != cudaSuccess) {
     set_err("context set-up failed: %s", cudaGetErrorString(cudaGetLastError()));
     su2gpu_destroy(c);
     return SU2GPU_ERR_CUDA;
@@ -290,7 +291,7 @@ static int create_ctx(const su2gpu_params* p, void* borrowed, su2gpu_ctx** out) 
   return SU2GPU_OK;
 }
 
-int su2gpu_create(const su2gpu_params* p, su2gpu_ctx** out) { return create_ctx(p, nullptr, out); }
+int su2gpu_create(const su2gpu_params* p, su2gpu_ctx** out) { return create_ctx(p, nullptr, nullptr, out); }
 
 int su2gpu_destroy(su2gpu_ctx* c) {
   if (!c) return SU2GPU_OK;
@@ -1111,5 +1112,13 @@ int su2gpu_update_lattice_host(su2gpu_ctx* c, uint32_t sweep, double* link, doub
 
 int su2gpu_attach(const su2gpu_params* p, void* fields, su2gpu_ctx** out) {
   if (!fields) return SU2GPU_ERR_INVALID;
-  return create_ctx(p, fields, out);
+  return create_ctx(p, fields, nullptr, out);
+}
+
+int su2gpu_create_copy(const su2gpu_params* p, const void* fields, uint64_t seed, uint32_t chain,
+                       su2gpu_ctx** out) {
+  if (!fields) return SU2GPU_ERR_INVALID;
+  int rc = create_ctx(p, nullptr, fields, out);
+  if (rc) return rc;
+  return su2gpu_set_seed(*out, seed, chain);
 }

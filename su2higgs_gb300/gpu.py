@@ -86,6 +86,7 @@ def lib():
         L.su2gpu_pool_counters.argtypes = [vp, i32, vp]
         L.su2gpu_pool_autotune.argtypes = [vp, vp, vp]
         L.su2gpu_pool_set_variants.argtypes = [vp, vp]
+        L.su2gpu_pool_extract.argtypes = [vp, i32, ctypes.POINTER(vp)]
         L.su2gpu_pool_enqueue.argtypes = [vp, i32, i32]
         L.su2gpu_pool_enqueue_measure.argtypes = [vp, vp, i32, ctypes.POINTER(i32)]
         L.su2gpu_pool_set_stream.argtypes = [vp, vp]
@@ -113,9 +114,12 @@ FIELD_NAMES = ("link", "u1", "d0", "d1", "trip", "sing")
 class Lattice:
     """One device-resident chain (a su2gpu context)."""
 
-    def __init__(self, params, seed=0, chain=0):
+    def __init__(self, params, seed=0, chain=0, _handle=None):
         self.params = params
         self.V = params.sites()
+        if _handle is not None:  # a context made by another entry point (Pool.extract)
+            self._h = _handle
+            return
         self._h = ctypes.c_void_p()
         check(lib().su2gpu_create(ctypes.byref(params), ctypes.byref(self._h)))
         check(lib().su2gpu_set_seed(self._h, seed, chain))
@@ -426,6 +430,13 @@ class Pool:
     def set_variants(self, choices):
         ch = np.ascontiguousarray(choices, dtype=np.int32)
         check(lib().su2gpu_pool_set_variants(self._h, _p(ch)))
+
+    def extract(self, slot):
+        """The chain copied into a `Lattice` of its own (same parameters,
+        seed and chain id); the chain stays in the pool."""
+        h = ctypes.c_void_p()
+        check(lib().su2gpu_pool_extract(self._h, slot, ctypes.byref(h)))
+        return Lattice(self._params[slot], _handle=h)
 
     def grad_flow(self, slot, t_max, dt, meas_interval=1):
         maxrows = int(np.ceil(t_max / dt)) // meas_interval + 3

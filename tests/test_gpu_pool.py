@@ -6,7 +6,8 @@
   per-site arithmetic is the same source compiled into two kernels, whose
   fused multiply-adds the compiler may form differently (1e-11 absolute after
   three FP64 sweeps, as the oracle parity tests; 1e-4 for FP32 fields) --
-  and measure() sums to 1e-12 relative (FP64) or 1e-6 (FP32).
+  and measure() sums to 1e-9 relative (FP64, as the oracle parity tests
+  after three sweeps) or 1e-6 (FP32).
 * Membership does not change a chain's trajectory: a chain alone and the
   same chain among others, admitted and retired around it, agree bit for bit
   (one kernel, random numbers keyed by chain and site).
@@ -84,7 +85,7 @@ def test_pool_chains_equal_single_lattices(gpu, content, precision, graph):
     pool.run(2, graph=graph)
     pool.run(1, graph=graph)
     sums = pool.measure()
-    atol, rtol = (1e-11, 1e-12) if precision == 64 else (1e-4, 1e-6)
+    atol, rtol = (1e-11, 1e-9) if precision == 64 else (1e-4, 1e-6)
     for s, (p, seed, chain), f in zip(slots, specs, inputs):
         want_f, want_c, want_m = single_run(gpu, p, f, seed, chain, 3)
         fields_close(pool.download(s), want_f, atol)
