@@ -318,7 +318,11 @@ def run_gpu(args):
     f = hot_fields(p, seed)
     lat = gpu.Lattice(p, seed=seed, chain=rank)
     lat.upload(**f)
-    variants, _ = lat.autotune()
+    if args.variants:
+        variants = np.array([int(x) for x in args.variants.split(",")], dtype=np.int32)
+        lat.set_variants(variants)
+    else:
+        variants, _ = lat.autotune()
     stream = torch.cuda.Stream(device=dev)
     lat.set_stream(stream.cuda_stream)
     K, W = args.steps, args.warmup
@@ -393,7 +397,7 @@ def run_gpu(args):
 
     # end to end through the host-buffer C ABI call (FP64 AoS host arrays)
     e2e = None
-    if rank == 0:
+    if rank == 0 and not args.no_e2e:
         host = {k: np.ascontiguousarray(v) for k, v in f.items()}
         for a in host.values():
             gpu.host_register(a)
@@ -557,7 +561,11 @@ def run_gpu_batched(args):
         f = workloads.hot_fields(p, seed)
         pool.upload(slot, **f)
         host.append((slot, f))
-    variants, _ = pool.autotune()
+    if args.variants:
+        variants = np.array([int(x) for x in args.variants.split(",")], dtype=np.int32)
+        pool.set_variants(variants)
+    else:
+        variants, _ = pool.autotune()
     stream = torch.cuda.Stream(device=dev)
     pool.set_stream(stream.cuda_stream)
     K, W = args.steps, args.warmup
@@ -612,7 +620,7 @@ def run_gpu_batched(args):
     # fields uploaded from page-locked memory, S sweeps, measurement,
     # every chain downloaded, per step
     e2e = None
-    if rank == 0:
+    if rank == 0 and not args.no_e2e:
         arrays = [a for _, f in host for a in f.values()]
         for a in arrays:
             gpu.host_register(a)
@@ -789,6 +797,9 @@ def main():
     ap.add_argument("--workload", default="batched384_adj_f32", choices=sorted(WORKLOADS) + sorted(BATCHED) + ["served"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end host-buffer measurement")
+    ap.add_argument("--variants", default=None,
+                    help="launch-shape variants of the 5 update kernel kinds, e.g. 0,0,0,0,0 (default: autotune)")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="served: arrivals per second")
     ap.add_argument("--serve-window", type=float, default=30.0, help="served: seconds of arrivals")
     ap.add_argument("--serve-drain", type=float, default=30.0, help="served: seconds after the last arrival")

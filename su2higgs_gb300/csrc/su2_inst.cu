@@ -110,7 +110,7 @@ static void lp_scalar(int v, int field, const PoolArgs& a, unsigned nb, cudaStre
   }
 }
 static void lp_measure(const PoolArgs& a, double* partials, unsigned nb, cudaStream_t st) {
-  if (nb) k_pool_measure<R, CCI><<<nb, BLOCK, 0, st>>>(a, nullptr, partials);
+  if (nb) k_pool_measure<R, CCI><<<nb, BLOCK, 0, st>>>(a, partials);
 }
 
 const Ops SU2_OPS = {sizeof(R) == 8 ? 64 : 32, CCI, l_link, l_u1, l_scalar, l_measure, l_flow,

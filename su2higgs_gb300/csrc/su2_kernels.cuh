@@ -1136,104 +1136,126 @@ __device__ inline bool sum_active(int k, int rt) {
 }
 
 // per-site terms of measure() summed over the block into partials[k][block]
-template <typename R, int CC>
-__global__ void __launch_bounds__(BLOCK) k_measure(Fields<R> f, Geom g, CoupT<R> cp, const double* alpha,
-                                                   double* partials) {
-  int t = (int)blockIdx.x * blockDim.x + threadIdx.x;
-  double m[NSUMS];
-#pragma unroll
-  for (int k = 0; k < NSUMS; k++) m[k] = 0.0;
-  if (t < g.V) {
-    int parity = t >= g.half;
-    int i = t;
-    int c[3];
-    site_coords(g, parity, t - parity * g.half, c);
-    // local_su2wilson (su2u1.c:143-157)
-    R wl = 0;
-    wl += ((R)1 - (R)0.5 * ptrace(f, g, c, i, 0, 1));
-    wl += ((R)1 - (R)0.5 * ptrace(f, g, c, i, 0, 2));
-    wl += ((R)1 - (R)0.5 * ptrace(f, g, c, i, 1, 2));
-    wl = (R)cp.beta * wl;
-    double act = (double)wl;
-    m[1] = (double)wl;
-    if (HAS(C_U1)) {
-      R u1w = local_u1wilson(f, g, cp, c, i);
-      act += (double)u1w;
-      m[2] = (double)u1w;
-    }
-    act += (double)higgspotential<R, CC>(f, cp, i);
-    const int nh = NHIGGS;
-    for (int h = 0; h < nh; h++) {
-      R mod = doubletsq(ld4<R>(php(f, h), i));
-      R cov = covariant_doublet<R, CC>(f, g, cp, c, i, h);
-      act += (double)cov;
-      m[3 + 3 * h] = (double)cov;
-      m[4 + 3 * h] = (double)mod;
-      m[5 + 3 * h] = (double)(mod * mod);
-    }
-    if (HAS(C_T)) {
-      R covt = covariant_triplet(f, g, c, i);
-      act += (double)covt;
-      V3<R> tr = ld3(f, i);
-      R tm = tripletsq(tr);
-      if (nh > 0) m[14] = (double)(doubletsq(ld4<R>(php(f, 0), i)) * tm);
-      m[12] = (double)tm;
-      m[13] = (double)(tm * tm);
-      R hs = 0;
-#pragma unroll
-      for (int d = 0; d < 3; d++) hs += hop_triplet_fwd(f, g, c, i, d);
-      m[11] = (double)hs;
-      // magcharge_cube (magfield.c:262-280) from the alpha planes
-      const int V = g.V;
-      double q = 0.0;
-      {
-        int n0 = shifted(g, c, 0, 1), n1 = shifted(g, c, 1, 1), n2 = shifted(g, c, 2, 1);
-        double B1 = alpha[2 * V + i], B2 = alpha[2 * V + n0];
-        q += B2 - B1;
-        B1 = -alpha[V + i];
-        B2 = -alpha[V + n1];
-        q += B2 - B1;
-        B1 = alpha[i];
-        B2 = alpha[n2];
-        q += B2 - B1;
-      }
-      m[15] = q;
-      m[16] = fabs(q);
-    }
-    if (nh == 2) {
-      Q<R> h1 = ld4<R>(php(f, 0), i), h2 = ld4<R>(php(f, 1), i);
-      m[9] = (double)((R)0.5 * (h1.a * h2.a + h1.b * h2.b + h1.c * h2.c + h1.d * h2.d));
-      m[10] = (double)((R)0.5 * (h1.d * h2.a + h1.c * h2.b - h1.b * h2.c - h1.a * h2.d));
-    }
-    if (HAS(C_S)) {
-      R S = f.sing[i];
-      R kin = (R)3 * S * S;
-      R scov = 0;
-#pragma unroll
-      for (int d = 0; d < 3; d++) {
-        R Sn = f.sing[shifted(g, c, d, 1)];
-        kin -= S * Sn;
-        scov += S * S - S * Sn;
-      }
-      act += (double)kin;
-      m[17] = (double)scov;
-      m[18] = (double)S;
-      m[19] = (double)(S * S);
-      m[20] = (double)(S * S * S);
-      m[21] = (double)(S * S * S * S);
-      if (nh == 1) {
-        R mod = doubletsq(ld4<R>(php(f, 0), i));
-        m[22] = (double)(mod * S);
-        m[23] = (double)(mod * S * S);
-      }
-    }
-    m[0] = act;
+// Sources of the projected U(1) field strengths alpha_proj (magfield.c:189-216)
+// of the magnetic charge: planes filled by k_alpha (plane 0 = (0,1), 1 = (0,2),
+// 2 = (1,2)), or the projections computed where they are needed.
+struct AlphaPlanes {
+  const double* a;
+  int V;
+  template <typename R>
+  __device__ double operator()(const Fields<R>&, const Geom&, const CoupT<R>&, const int*, int n, int plane) const {
+    return a[plane * V + n];
   }
+};
+struct AlphaOnTheFly {
+  template <typename R>
+  __device__ double operator()(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* cn, int n,
+                               int plane) const {
+    const int d1 = plane == 2 ? 1 : 0, d2 = plane == 0 ? 1 : 2;
+    return (double)alpha_proj(f, g, cp, cn, n, d1, d2);
+  }
+};
+
+// measure() (measure.c:110-233): the terms of site t (storage index) added to
+// m[NSUMS]; per-site quantities in R, sums in FP64
+template <typename R, int CC, typename AF>
+__device__ inline void measure_site(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, int t, const AF& alpha,
+                                    double* m) {
+  int parity = t >= g.half;
+  int i = t;
+  int c[3];
+  site_coords(g, parity, t - parity * g.half, c);
+  // local_su2wilson (su2u1.c:143-157)
+  R wl = 0;
+  wl += ((R)1 - (R)0.5 * ptrace(f, g, c, i, 0, 1));
+  wl += ((R)1 - (R)0.5 * ptrace(f, g, c, i, 0, 2));
+  wl += ((R)1 - (R)0.5 * ptrace(f, g, c, i, 1, 2));
+  wl = (R)cp.beta * wl;
+  double act = (double)wl;
+  m[1] += (double)wl;
+  if (SU2_HAS(CC, cp.content, C_U1)) {
+    R u1w = local_u1wilson(f, g, cp, c, i);
+    act += (double)u1w;
+    m[2] += (double)u1w;
+  }
+  act += (double)higgspotential<R, CC>(f, cp, i);
+  const int nh = SU2_HAS(CC, cp.content, C_H2) ? 2 : (SU2_HAS(CC, cp.content, C_H1) ? 1 : 0);
+  for (int h = 0; h < nh; h++) {
+    R mod = doubletsq(ld4<R>(php(f, h), i));
+    R cov = covariant_doublet<R, CC>(f, g, cp, c, i, h);
+    act += (double)cov;
+    m[3 + 3 * h] += (double)cov;
+    m[4 + 3 * h] += (double)mod;
+    m[5 + 3 * h] += (double)(mod * mod);
+  }
+  if (SU2_HAS(CC, cp.content, C_T)) {
+    R covt = covariant_triplet(f, g, c, i);
+    act += (double)covt;
+    V3<R> tr = ld3(f, i);
+    R tm = tripletsq(tr);
+    if (nh > 0) m[14] += (double)(doubletsq(ld4<R>(php(f, 0), i)) * tm);
+    m[12] += (double)tm;
+    m[13] += (double)(tm * tm);
+    R hs = 0;
+#pragma unroll
+    for (int d = 0; d < 3; d++) hs += hop_triplet_fwd(f, g, c, i, d);
+    m[11] += (double)hs;
+    // magcharge_cube (magfield.c:262-280)
+    int c0[3], c1[3], c2[3];
+    shift_coords(g, c, 0, 1, c0);
+    shift_coords(g, c, 1, 1, c1);
+    shift_coords(g, c, 2, 1, c2);
+    int n0 = shifted(g, c, 0, 1), n1 = shifted(g, c, 1, 1), n2 = shifted(g, c, 2, 1);
+    double q = 0.0;
+    double B1 = alpha(f, g, cp, c, i, 2), B2 = alpha(f, g, cp, c0, n0, 2);
+    q += B2 - B1;
+    B1 = -alpha(f, g, cp, c, i, 1);
+    B2 = -alpha(f, g, cp, c1, n1, 1);
+    q += B2 - B1;
+    B1 = alpha(f, g, cp, c, i, 0);
+    B2 = alpha(f, g, cp, c2, n2, 0);
+    q += B2 - B1;
+    m[15] += q;
+    m[16] += fabs(q);
+  }
+  if (nh == 2) {
+    Q<R> h1 = ld4<R>(php(f, 0), i), h2 = ld4<R>(php(f, 1), i);
+    m[9] += (double)((R)0.5 * (h1.a * h2.a + h1.b * h2.b + h1.c * h2.c + h1.d * h2.d));
+    m[10] += (double)((R)0.5 * (h1.d * h2.a + h1.c * h2.b - h1.b * h2.c - h1.a * h2.d));
+  }
+  if (SU2_HAS(CC, cp.content, C_S)) {
+    R S = f.sing[i];
+    R kin = (R)3 * S * S;
+    R scov = 0;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      R Sn = f.sing[shifted(g, c, d, 1)];
+      kin -= S * Sn;
+      scov += S * S - S * Sn;
+    }
+    act += (double)kin;
+    m[17] += (double)scov;
+    m[18] += (double)S;
+    m[19] += (double)(S * S);
+    m[20] += (double)(S * S * S);
+    m[21] += (double)(S * S * S * S);
+    if (nh == 1) {
+      R mod = doubletsq(ld4<R>(php(f, 0), i));
+      m[22] += (double)(mod * S);
+      m[23] += (double)(mod * S * S);
+    }
+  }
+  m[0] += act;
+}
+
+// sums of m[] over the block (blockDim.x == BLOCK) to partials[k * nblocks + block]
+template <int CC>
+__device__ inline void block_sums_out(const double* m, int content, double* partials, int nblocks, int block) {
   __shared__ double sm[BLOCK / 32][NSUMS];
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < NSUMS; k++) {
-    if (!sum_active<CC>(k, cp.content)) continue;
+    if (!sum_active<CC>(k, content)) continue;
     double v = m[k];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -1242,11 +1264,31 @@ __global__ void __launch_bounds__(BLOCK) k_measure(Fields<R> f, Geom g, CoupT<R>
   __syncthreads();
   if (threadIdx.x < NSUMS) {
     double v = 0.0;
-    if (sum_active<CC>(threadIdx.x, cp.content))
+    if (sum_active<CC>(threadIdx.x, content))
 #pragma unroll
       for (int ww = 0; ww < BLOCK / 32; ww++) v += sm[ww][threadIdx.x];
-    partials[threadIdx.x * gridDim.x + blockIdx.x] = v;
+    partials[threadIdx.x * nblocks + block] = v;
   }
+}
+
+// sites of one measurement block: MEAS_SPT per thread, BLOCK apart
+constexpr int MEAS_SPT = 8;
+constexpr int MEAS_TILE = BLOCK * MEAS_SPT;
+
+// measure() over the whole lattice; alpha = the k_alpha planes (triplet
+// content) or null.  gridDim.x = ceil(V / MEAS_TILE).
+template <typename R, int CC>
+__global__ void __launch_bounds__(BLOCK) k_measure(Fields<R> f, Geom g, CoupT<R> cp, const double* alpha,
+                                                   double* partials) {
+  double m[NSUMS];
+#pragma unroll
+  for (int k = 0; k < NSUMS; k++) m[k] = 0.0;
+  const AlphaPlanes ap{alpha, g.V};
+  for (int j = 0; j < MEAS_SPT; j++) {
+    int t = ((int)blockIdx.x * MEAS_SPT + j) * BLOCK + threadIdx.x;
+    if (t < g.V) measure_site<R, CC>(f, g, cp, t, ap, m);
+  }
+  block_sums_out<CC>(m, cp.content, partials, gridDim.x, blockIdx.x);
 }
 
 #ifdef SU2_WITH_GLOBAL

@@ -37,121 +37,18 @@ constexpr int NOALLOC_MAX_SITES = NOALLOC_MAX_BLOCKS * BLOCK;  // 2,097,152
 
 static __device__ __align__(256) double g_noalloc_partials[NSUMS * NOALLOC_MAX_BLOCKS];
 
-// The same per-site terms as k_measure, with the projected-U(1) field strengths
-// of the magnetic charge computed where they are needed instead of being read
-// from a scratch plane of 3 V doubles.
+// The per-site terms of measure(), one site per thread, with the projected-U(1)
+// field strengths of the magnetic charge computed where they are needed instead
+// of being read from a scratch plane of 3 V doubles.
 template <typename R>
 __global__ void __launch_bounds__(BLOCK) k_measure_noalloc(Fields<R> f, Geom g, CoupT<R> cp, double* partials) {
   constexpr int CC = C_GENERIC;
-  const bool has_u1 = SU2_HAS(CC, cp.content, C_U1), has_t = SU2_HAS(CC, cp.content, C_T),
-             has_s = SU2_HAS(CC, cp.content, C_S);
-  const int nh = SU2_HAS(CC, cp.content, C_H2) ? 2 : (SU2_HAS(CC, cp.content, C_H1) ? 1 : 0);
   int t = (int)blockIdx.x * blockDim.x + threadIdx.x;
   double m[NSUMS];
 #pragma unroll
   for (int k = 0; k < NSUMS; k++) m[k] = 0.0;
-  if (t < g.V) {
-    int parity = t >= g.half;
-    int i = t;
-    int c[3];
-    site_coords(g, parity, t - parity * g.half, c);
-    R wl = 0;
-    wl += ((R)1 - (R)0.5 * ptrace(f, g, c, i, 0, 1));
-    wl += ((R)1 - (R)0.5 * ptrace(f, g, c, i, 0, 2));
-    wl += ((R)1 - (R)0.5 * ptrace(f, g, c, i, 1, 2));
-    wl = (R)cp.beta * wl;
-    double act = (double)wl;
-    m[1] = (double)wl;
-    if (has_u1) {
-      R u1w = local_u1wilson(f, g, cp, c, i);
-      act += (double)u1w;
-      m[2] = (double)u1w;
-    }
-    act += (double)higgspotential<R, CC>(f, cp, i);
-    for (int h = 0; h < nh; h++) {
-      R mod = doubletsq(ld4<R>(php(f, h), i));
-      R cov = covariant_doublet<R, CC>(f, g, cp, c, i, h);
-      act += (double)cov;
-      m[3 + 3 * h] = (double)cov;
-      m[4 + 3 * h] = (double)mod;
-      m[5 + 3 * h] = (double)(mod * mod);
-    }
-    if (has_t) {
-      R covt = covariant_triplet(f, g, c, i);
-      act += (double)covt;
-      V3<R> tr = ld3(f, i);
-      R tm = tripletsq(tr);
-      if (nh > 0) m[14] = (double)(doubletsq(ld4<R>(php(f, 0), i)) * tm);
-      m[12] = (double)tm;
-      m[13] = (double)(tm * tm);
-      R hs = 0;
-#pragma unroll
-      for (int d = 0; d < 3; d++) hs += hop_triplet_fwd(f, g, c, i, d);
-      m[11] = (double)hs;
-      int c0[3], c1[3], c2[3];
-      shift_coords(g, c, 0, 1, c0);
-      shift_coords(g, c, 1, 1, c1);
-      shift_coords(g, c, 2, 1, c2);
-      int n0 = shifted(g, c, 0, 1), n1 = shifted(g, c, 1, 1), n2 = shifted(g, c, 2, 1);
-      double q = 0.0;
-      double B1 = (double)alpha_proj(f, g, cp, c, i, 1, 2), B2 = (double)alpha_proj(f, g, cp, c0, n0, 1, 2);
-      q += B2 - B1;
-      B1 = -(double)alpha_proj(f, g, cp, c, i, 0, 2);
-      B2 = -(double)alpha_proj(f, g, cp, c1, n1, 0, 2);
-      q += B2 - B1;
-      B1 = (double)alpha_proj(f, g, cp, c, i, 0, 1);
-      B2 = (double)alpha_proj(f, g, cp, c2, n2, 0, 1);
-      q += B2 - B1;
-      m[15] = q;
-      m[16] = fabs(q);
-    }
-    if (nh == 2) {
-      Q<R> h1 = ld4<R>(php(f, 0), i), h2 = ld4<R>(php(f, 1), i);
-      m[9] = (double)((R)0.5 * (h1.a * h2.a + h1.b * h2.b + h1.c * h2.c + h1.d * h2.d));
-      m[10] = (double)((R)0.5 * (h1.d * h2.a + h1.c * h2.b - h1.b * h2.c - h1.a * h2.d));
-    }
-    if (has_s) {
-      R S = f.sing[i];
-      R kin = (R)3 * S * S;
-      R scov = 0;
-#pragma unroll
-      for (int d = 0; d < 3; d++) {
-        R Sn = f.sing[shifted(g, c, d, 1)];
-        kin -= S * Sn;
-        scov += S * S - S * Sn;
-      }
-      act += (double)kin;
-      m[17] = (double)scov;
-      m[18] = (double)S;
-      m[19] = (double)(S * S);
-      m[20] = (double)(S * S * S);
-      m[21] = (double)(S * S * S * S);
-      if (nh == 1) {
-        R mod = doubletsq(ld4<R>(php(f, 0), i));
-        m[22] = (double)(mod * S);
-        m[23] = (double)(mod * S * S);
-      }
-    }
-    m[0] = act;
-  }
-  __shared__ double sm[BLOCK / 32][NSUMS];
-  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-  for (int k = 0; k < NSUMS; k++) {
-    if (!sum_active<CC>(k, cp.content)) continue;
-    double v = m[k];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (lane == 0) sm[w][k] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x < NSUMS) {
-    double v = 0.0;
-    if (sum_active<CC>(threadIdx.x, cp.content))
-#pragma unroll
-      for (int ww = 0; ww < BLOCK / 32; ww++) v += sm[ww][threadIdx.x];
-    partials[threadIdx.x * gridDim.x + blockIdx.x] = v;
-  }
+  if (t < g.V) measure_site<R, CC>(f, g, cp, t, AlphaOnTheFly{}, m);
+  block_sums_out<CC>(m, cp.content, partials, gridDim.x, blockIdx.x);
 }
 
 // device address of g_noalloc_partials, looked up once per device

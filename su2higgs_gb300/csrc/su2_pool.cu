@@ -193,7 +193,7 @@ int rebuild(su2gpu_pool* P, void* arena_base = nullptr, void* slot_base = nullpt
     sp.clear();
     for (int s : P->active) {
       first.push_back((int)mt.size());
-      for (int t0 = 0; t0 < P->slots[s].g.V; t0 += BLOCK) mt.push_back(int2{s, t0});
+      for (int t0 = 0; t0 < P->slots[s].g.V; t0 += MEAS_TILE) mt.push_back(int2{s, t0});
       sp.push_back((uint32_t*)(sb + (size_t)s * 256));
     }
     first.push_back((int)mt.size());

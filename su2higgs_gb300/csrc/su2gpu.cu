@@ -869,7 +869,7 @@ static int enqueue_measure(su2gpu_ctx* c, const void* F, const Coup& cp, double*
     c->pops->alpha(F, c->g, cp, (double*)c->alpha.p, c->st);
     CKL();
   }
-  unsigned nb = nblk(V, BLOCK);
+  unsigned nb = nblk(V, MEAS_TILE);
   c->ops->measure(F, c->g, cp, (const double*)c->alpha.p, (double*)c->partials.p, nb, c->st);
   CKL();
   launch_reduce_partials((const double*)c->partials.p, (int)nb, out, c->st);
