@@ -66,13 +66,18 @@ BATCHED = {
 # Compulsory device traffic per lattice site, in reals, for one launch of each
 # pass kind (each array element a launch must touch counted once).
 # Fundamental content: link heatbath reads the two other directions everywhere
-# (8), the updated direction everywhere and writes half of it (4 + 2), the
-# doublet everywhere (4) -> 18; a doublet pass reads the doublet everywhere
-# (4), all links (12) and writes half the doublet (2) -> 18.  Adjoint content:
-# link heatbath 8 + 4 + 2 + the triplet everywhere (3) -> 17; a triplet pass
-# reads all links (12) and the triplet everywhere (3) and writes half of it
-# (1.5) -> 16.5.
-REALS_PER_SITE = {"fund": {0: 18, 2: 18}, "adj": {0: 17, 3: 16.5}}
+# (8), the updated direction at the other parity (2; the heatbath draw does not
+# depend on the old link), writes half of it (2) and reads the doublet
+# everywhere (4) -> 16; a doublet pass reads the doublet everywhere (4), all
+# links (12) and writes half the doublet (2) -> 18.  Adjoint content: the link
+# update reads the updated direction everywhere (its Metropolis correction
+# needs the old link): 8 + 4 + 2 + the triplet everywhere (3) -> 17; a triplet
+# pass reads all links (12) and the triplet everywhere (3) and writes half of
+# it (1.5) -> 16.5.
+REALS_PER_SITE = {"fund": {0: 16, 2: 18}, "adj": {0: 17, 3: 16.5}}
+# Compulsory reals per site-update of a whole sweep (6 link half-passes, 10
+# scalar half-passes, one measurement reading every field once)
+REALS_PER_SITE_UPDATE = {"fund": 6 * 16 + 10 * 18 + 16, "adj": 6 * 17 + 10 * 16.5 + 15}
 REALS_MEASURE = 16
 KIND_NAMES = {0: "link_heatbath", 1: "u1_metropolis", 2: "doublet_update", 3: "triplet_update",
               4: "singlet_update", 5: "reunitarize"}
@@ -466,6 +471,7 @@ def run_gpu(args):
                        "parallelism": f"replicas x{world}", "graph": True,
                        "launch_variants": [int(v) for v in variants]},
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "fp64_plain": fp64,
+            "sweep_roofline": sweep_roofline(value / world, content, prec),
             # per step: the sweep's kernels, the sweep-counter set/increment, measure + reduction
             "gpu_launches": int(K * (launches_sweep + 4)),
             "clocks": clk, "wall_s_timed_region": t_wall,
@@ -475,6 +481,17 @@ def run_gpu(args):
     lat.close()
     if dist:
         dist.destroy_process_group()
+
+
+def sweep_roofline(site_updates_per_s, content, prec):
+    """The whole sweep against HBM: site-updates/s x compulsory bytes per
+    site-update over the measured copy bandwidth (one GPU)."""
+    rsize = 4 if prec == 32 else 8
+    b = REALS_PER_SITE_UPDATE[content] * rsize
+    peak, kind = measured_peaks()
+    achieved = site_updates_per_s * b / 1e9
+    return {"bytes_per_site_update": b, "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": kind}
 
 
 def roofline_of(kinds, ms, content, prec, sites, workload):
@@ -702,6 +719,7 @@ def run_gpu_batched(args):
                        "parallelism": f"replicas x{world}", "graph": True,
                        "launch_variants": [int(v) for v in variants]},
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "fp64_plain": fp64,
+            "sweep_roofline": sweep_roofline(value / world, "adj", 32),
             # per step: S graph replays of the sweep's kernels + measure + per-chain reduction
             "gpu_launches": int(K * (S * launches_sweep + 2)),
             "clocks": clk, "wall_s_timed_region": t_wall,

@@ -1,6 +1,11 @@
 /* su2_main.c -- bin/su2, the drop-in for the reference's program (main.c):
  *
- *   bin/su2 [--content NAME] [--precision 64|32] [--seed N] <config>
+ *   bin/su2 [--content NAME] [--precision 64|32] [--seed N] [--files-only] <config>
+ *
+ * --files-only runs the host side of a run of 0 iterations without touching
+ * the GPU: read the config, the lattice file and (multicanonical runs) the
+ * weight file, and write labels, lattice and weight back as the reference
+ * does; a check of file compatibility that needs no device.
  *
  * Same config keys, same outputs (labels, measure, measure_flow, lattice,
  * weight) and the same iteration structure as main.c:10-421: thermalise with
@@ -33,15 +38,50 @@ static double wall(void) {
     }                                                                          \
   } while (0)
 
+/* the file side of a run of 0 iterations (main.c:200-290, 395-401) */
+static int files_roundtrip(host_params* hp, host_muca* hm) {
+  int64_t V = 1;
+  for (int d = 0; d < hp->p.dim; d++) V *= hp->p.L[d];
+  double* arrays[6] = {0};
+  for (int k = 0; k < 6; k++) {
+    int64_t n = field_count(hp, k);
+    if (n) arrays[k] = (double*)calloc((size_t)(V * n), sizeof(double));
+  }
+  long citer = 0;
+  double total_time = 0.0, comms_time = 0.0;
+  if (access(hp->latticefile, R_OK) == 0) {
+    load_lattice(hp->latticefile, hp, &citer, &total_time, &comms_time, arrays);
+  } else {
+    for (int64_t k = 0; k < V * hp->p.dim; k++) arrays[0][4 * k] = 1.0;
+    for (int h = 0; h < hp->nhiggs; h++)
+      for (int64_t i = 0; i < V; i++) arrays[2 + h][4 * i] = hp->phi0;
+    if (hp->triplet)
+      for (int64_t i = 0; i < V; i++) arrays[4][3 * i] = hp->sigma0;
+    if (hp->singlet)
+      for (int64_t i = 0; i < V; i++) arrays[5][i] = hp->singlet0;
+    hp->reset = 1;
+  }
+  print_labels(hp);
+  if (hp->multicanonical) {
+    su2gpu_weight w;
+    load_weight(&w, hm); /* writes the weight back, as load_weight() does */
+  }
+  save_lattice(hp->latticefile, hp, hp->reset ? 1 : citer + 1, 0.0, 0.0, arrays);
+  for (int k = 0; k < 6; k++) free(arrays[k]);
+  return 0;
+}
+
 int main(int argc, char** argv) {
   const char* content = NULL;
   const char* precision = NULL;
   const char* seed_arg = NULL;
+  int files_only = 0;
   int a = 1;
   while (a < argc && !strncmp(argv[a], "--", 2)) {
     if (!strcmp(argv[a], "--content") && a + 1 < argc) content = argv[++a];
     else if (!strcmp(argv[a], "--precision") && a + 1 < argc) precision = argv[++a];
     else if (!strcmp(argv[a], "--seed") && a + 1 < argc) seed_arg = argv[++a];
+    else if (!strcmp(argv[a], "--files-only")) files_only = 1;
     else break;
     a++;
   }
@@ -68,6 +108,8 @@ int main(int argc, char** argv) {
 
   host_muca hm;
   read_weight_parameters(cfg, &hp, &hm);
+
+  if (files_only) return files_roundtrip(&hp, &hm);
 
   double t0 = wall();
   su2gpu_ctx* ctx = NULL;

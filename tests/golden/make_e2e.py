@@ -1,0 +1,124 @@
+"""Golden files of the reference program itself (bin/su2 drop-in checks).
+
+Runs the reference's own serial binaries (built from its sources by
+`make -C oracle/ref`, outputs in oracle/_ref/su2_<content>) in scratch
+directories and stores, per case, in e2e_<case>.npz:
+
+  config        the config file (the reference's sample config, main keys set)
+  lattice_in    a seeded hot lattice in the reference's binary format
+                (checkpoint.c:84-122), iteration counter 0
+  labels        the labels file the reference writes (measure.c:15-64)
+  measure       its measure file after `iterations 1`: the row of the loaded
+                configuration, taken before the first update (main.c:306-310)
+  measure_flow  its measure_flow block of the same configuration
+                (gradflow.c:66-160), flow before the first update
+  lattice_out0  the lattice file it writes after `iterations 0` (fields as
+                loaded, header iteration 1; the two time doubles are not
+                compared)
+  weight        (muca case) the weight file the reference wrote during a
+                multicanonical run (multicanonical.c:82-111)
+
+Run here, where the reference sources are: python tests/golden/make_e2e.py
+"""
+import os
+import re
+import shutil
+import struct
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from su2higgs_gb300 import abi, workloads  # noqa: E402
+
+REF_CONFIG = "/root/reference/config"
+REF_BIN = os.path.join(ROOT, "oracle", "_ref")
+L = (6, 4, 8)
+
+CASES = {
+    # case: (binary content, config overrides)
+    "fund": ("fund", {}),
+    "adj": ("adj", {}),
+    "su2u1s": ("su2u1s", {}),
+    "fund_muca": ("fund", {"multicanonical": 1, "muca_mode": 1, "bins": 20, "min": 0.0, "max": 0.6,
+                           "iterations": 30, "interval": 10, "do_flow": 0}),
+}
+
+
+def set_key(text, key, value):
+    pat = re.compile(r"^%s\s+\S+.*$" % re.escape(key), re.M)
+    if pat.search(text):
+        return pat.sub(lambda m: f"{key} {value}", text, count=1)
+    return text + f"\n{key} {value}\n"
+
+
+def make_config(over):
+    text = open(REF_CONFIG).read()
+    base = dict(L1=L[0], L2=L[1], L3=L[2], reset=0, iterations=1, n_thermalize=0, interval=1, checkpoint=1000,
+                run_checks=0, multicanonical=0, do_flow=1, flow_interval=1, flow_t_max=0.1, flow_dt=0.02,
+                flow_meas_interval=2, do_z_meas=0, setup_wall=0, scalar_sweeps=4, do_correlators=0,
+                measure_local=0)
+    base.update(over)
+    for k, v in base.items():
+        text = set_key(text, k, v)
+    return text
+
+
+def lattice_bytes(content, seed, it=0):
+    p = abi.make_params(content, L=L)
+    f = workloads.hot_fields(p, seed, phi_sigma=0.5, trip_sigma=0.4, sing_sigma=0.4)
+    out = struct.pack("ii", 1, 3) + struct.pack("iii", *L) + struct.pack("ldd", it, 0.0, 0.0)
+    for n in ("link", "u1", "d0", "d1", "trip", "sing"):
+        if n in f:
+            out += np.ascontiguousarray(f[n], dtype=np.float64).tobytes()
+    return out
+
+
+def run_ref(content, config, lattice, extra=None):
+    d = tempfile.mkdtemp()
+    try:
+        open(os.path.join(d, "config"), "w").write(config)
+        open(os.path.join(d, "lattice"), "wb").write(lattice)
+        if extra:
+            for name, data in extra.items():
+                open(os.path.join(d, name), "wb").write(data)
+        r = subprocess.run([os.path.join(REF_BIN, "su2_" + content), "config"], cwd=d, capture_output=True,
+                           text=True, timeout=600)
+        if r.returncode != 0:
+            raise RuntimeError(r.stdout[-2000:] + r.stderr[-2000:])
+        out = {}
+        for name in ("labels", "measure", "measure_flow", "lattice", "weight"):
+            path = os.path.join(d, name)
+            if os.path.exists(path):
+                out[name] = open(path, "rb").read()
+        return out
+    finally:
+        shutil.rmtree(d)
+
+
+def main():
+    for case, (content, over) in CASES.items():
+        config = make_config(over)
+        lat = lattice_bytes(content, 1000 + len(case))
+        got = run_ref(content, config, lat)
+        rec = {"config": np.frombuffer(config.encode(), dtype=np.uint8), "content": np.array(content),
+               "lattice_in": np.frombuffer(lat, dtype=np.uint8),
+               "labels": np.frombuffer(got["labels"], dtype=np.uint8),
+               "measure": np.frombuffer(got["measure"], dtype=np.uint8)}
+        if "measure_flow" in got:
+            rec["measure_flow"] = np.frombuffer(got["measure_flow"], dtype=np.uint8)
+        if "weight" in got:
+            rec["weight"] = np.frombuffer(got["weight"], dtype=np.uint8)
+        got0 = run_ref(content, set_key(config, "iterations", 0), lat)
+        rec["lattice_out0"] = np.frombuffer(got0["lattice"], dtype=np.uint8)
+        np.savez_compressed(os.path.join(HERE, f"e2e_{case}.npz"), **rec)
+        print(case, {k: len(v) for k, v in got.items()})
+
+
+if __name__ == "__main__":
+    main()

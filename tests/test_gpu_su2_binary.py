@@ -1,0 +1,67 @@
+"""bin/su2, the drop-in for the reference's program, against the reference's
+own outputs (tests/golden/e2e_<case>.npz): from the same config and lattice
+file, with reset 0, the first measure row and the first measure_flow block are
+taken on the loaded configuration before any update (main.c:306-318), so
+they are deterministic.  Checked: the labels file byte for byte, the same
+number of columns and lines, every printed value within the stated tolerance
+of the reference's (FP64 path: 1e-6 relative -- six printed digits, so equal
+up to the rounding of the last printed digit; FP32 form: 1e-4 relative,
+1e-5 absolute), and the lattice file the run leaves behind is a valid
+checkpoint of the right size that bin/su2 reads back."""
+import numpy as np
+import pytest
+
+import e2e_util as E
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def binary():
+    return E.ensure_binary()
+
+
+def rows(text):
+    return [line.split() for line in text.decode().splitlines() if line.strip()]
+
+
+def close(a, b, rtol, atol):
+    x, y = float(a), float(b)
+    return abs(x - y) <= atol + rtol * max(abs(x), abs(y))
+
+
+def compare_rows(got, want, rtol, atol):
+    assert len(got) == len(want), (got, want)
+    for rg, rw in zip(got, want):
+        if rg[0].startswith("="):
+            assert rg == rw
+            continue
+        assert len(rg) == len(rw), (rg, rw)
+        for a, b in zip(rg, rw):
+            assert close(a, b, rtol, atol), (a, b, rg, rw)
+
+
+@pytest.mark.parametrize("precision,rtol,atol", [(64, 1e-6, 1e-12), (32, 1e-4, 1e-5)])
+@pytest.mark.parametrize("case", ["fund", "adj", "su2u1s"])
+def test_first_measurement_and_flow_match_reference(binary, case, precision, rtol, atol, tmp_path):
+    d = str(tmp_path)
+    g = E.stage(case, d)
+    E.run(d, g["bin_content"], "--precision", str(precision), "--seed", "7")
+    assert E.read(d, "labels") == g["labels"]
+    got = rows(E.read(d, "measure"))
+    want = rows(g["measure"])
+    assert len(got) == len(want) == 1
+    compare_rows(got, want, rtol, atol)
+    if precision == 64:
+        # FP64: the printed row is the reference's except in a last-digit
+        # rounding case
+        same = sum(a == b for a, b in zip(got[0], want[0]))
+        assert same >= len(want[0]) - 1, (got, want)
+    compare_rows(rows(E.read(d, "measure_flow")), rows(g["measure_flow"]), rtol, atol)
+    out = E.read(d, "lattice")
+    assert len(out) == len(g["lattice_in"])
+    assert out[:20] == g["lattice_in"][:20]
+    # the checkpoint it wrote is read back (a run of 0 iterations keeps it)
+    E.run(d, g["bin_content"], "--files-only")
+    again = E.read(d, "lattice")
+    assert again[44:] == out[44:]
