@@ -87,6 +87,26 @@ def env_rank():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def replica_seed(base, rank):
+    """Seed of a rank's replica: independent chains per rank (weak scaling)."""
+    return base + 1000003 * rank
+
+
+def max_over_ranks(ms, dist, device):
+    """The slowest rank's time (every rank gets it); ms itself without ranks."""
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate(units_per_rank, world, ms):
+    """Whole-job throughput: the units every rank processed over the slowest
+    rank's time."""
+    return world * units_per_rank / (ms * 1e-3)
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -319,7 +339,7 @@ def run_gpu(args):
     content, L, prec = WORKLOADS[args.workload]
     p = abi.make_params(content, L=L, precision=prec)
     V = p.sites()
-    seed = 20261203 + rank
+    seed = replica_seed(20261203, rank)
     f = hot_fields(p, seed)
     lat = gpu.Lattice(p, seed=seed, chain=rank)
     lat.upload(**f)
@@ -360,12 +380,8 @@ def run_gpu(args):
     if dist:
         dist.barrier()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    dev_ms = float(np.sum(step_ms))
-    t = torch.tensor([dev_ms], dtype=torch.float64, device=dev)
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    dev_ms = float(t.item())
-    value = world * V * K / (dev_ms * 1e-3)
+    dev_ms = max_over_ranks(float(np.sum(step_ms)), dist, dev)
+    value = aggregate(V * K, world, dev_ms)
     m_last = sums[W + K - 1].cpu().numpy()
     assert np.all(np.isfinite(m_last)), "non-finite measurement"
 
@@ -568,7 +584,7 @@ def run_gpu_batched(args):
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     nchains, S = BATCHED[args.workload]
-    specs = workloads.batched_ensemble(nchains, seed=20261203 + 1000003 * rank)
+    specs = workloads.batched_ensemble(nchains, seed=replica_seed(20261203, rank))
     sites = sum(p.sites() for p, _, _ in specs)
     arena = sum(gpu.Pool.chain_bytes(p) for p, _, _ in specs)
     pool = gpu.Pool(specs[0][0], arena_bytes=arena, max_chains=nchains)
@@ -616,12 +632,8 @@ def run_gpu_batched(args):
         dist.barrier()
     pool.run(0)  # surfaces any error recorded by the kernels
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
-    dev_ms = float(np.sum(step_ms))
-    t = torch.tensor([dev_ms], dtype=torch.float64, device=dev)
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    dev_ms = float(t.item())
-    value = world * sites * S * K / (dev_ms * 1e-3)
+    dev_ms = max_over_ranks(float(np.sum(step_ms)), dist, dev)
+    value = aggregate(sites * S * K, world, dev_ms)
     m_last = sums[1].cpu().numpy()
     assert np.all(np.isfinite(m_last)), "non-finite measurement"
 
@@ -742,7 +754,7 @@ def run_gpu_served(args):
     rank, world, local = env_rank()
     gpu.lib()
     rate, window, drain = args.serve_rate, args.serve_window, args.serve_drain
-    stream = serve.make_stream(rate, window, seed=20261203 + rank)
+    stream = serve.make_stream(rate, window, seed=replica_seed(20261203, rank))
     arena = int(args.serve_arena_gb * (1 << 30))
     srv = serve.Server(gpu.Pool, gpu.Pool.chain_bytes, arena_bytes=arena, max_chains=1024,
                        quantum=args.serve_quantum)
