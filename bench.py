@@ -659,13 +659,13 @@ def run_gpu_batched(args):
         e2e_pool.set_variants(variants)
         slots = [e2e_pool.add(p, seed=seed, chain=chain) for p, seed, chain in specs]
 
+        fields = [f for _, f in host]
+
         def e2e_step():
-            for slot, (_, f) in zip(slots, host):
-                e2e_pool.upload(slot, **f)
+            e2e_pool.upload_many(slots, fields)
             e2e_pool.run(S, graph=True)
             e2e_pool.measure()
-            for slot, (_, f) in zip(slots, host):
-                e2e_pool.download(slot, out=f)  # in place, into the same page-locked arrays
+            e2e_pool.download_many(slots, fields)  # in place, into the same page-locked arrays
         e2e_step()
         t0 = time.perf_counter()
         for k in range(n_e2e):

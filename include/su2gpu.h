@@ -165,7 +165,9 @@ int64_t su2gpu_footprint_bytes(const su2gpu_params* p);
 int su2gpu_layout_tables(su2gpu_ctx* ctx, int64_t* next, int64_t* prev, int64_t* coords, int32_t* parity);
 
 /* Field transfer (FP64 AoS host arrays in layout order; NULL for absent
- * fields).  link: V*dim*4, u1: V*dim, doublet: V*4, triplet: V*3, singlet: V. */
+ * fields).  link: V*dim*4, u1: V*dim, doublet: V*4, triplet: V*3, singlet: V.
+ * Page-locked arrays (su2gpu_host_register) are converted by the device in
+ * place, without a staging copy. */
 int su2gpu_upload_fields(su2gpu_ctx* ctx, const double* link, const double* u1, const double* doublet0,
                          const double* doublet1, const double* triplet, const double* singlet);
 int su2gpu_download_fields(su2gpu_ctx* ctx, double* link, double* u1, double* doublet0,
@@ -292,6 +294,12 @@ int su2gpu_pool_upload(su2gpu_pool* pool, int32_t slot, const double* link, cons
                        const double* doublet1, const double* triplet, const double* singlet);
 int su2gpu_pool_download(su2gpu_pool* pool, int32_t slot, double* link, double* u1, double* doublet0,
                          double* doublet1, double* triplet, double* singlet);
+/* The same for n chains in one call, waiting once: fields[k][j] is field k
+ * (0 link, 1 u1, 2 doublet0, 3 doublet1, 4 triplet, 5 singlet) of slots[j];
+ * fields[k] == NULL skips field k.  Page-locked host arrays (see
+ * su2gpu_host_register) are read / written in place by the device. */
+int su2gpu_pool_upload_many(su2gpu_pool* pool, int32_t n, const int32_t* slots, const double* const* const* fields);
+int su2gpu_pool_download_many(su2gpu_pool* pool, int32_t n, const int32_t* slots, double* const* const* fields);
 /* Set one chain's sweep counter (the random stream's sweep index). */
 int su2gpu_pool_set_sweep(su2gpu_pool* pool, int32_t slot, uint32_t sweep);
 /* `nsweeps` sweeps of every active chain; each chain's sweep counter

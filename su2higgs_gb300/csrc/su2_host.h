@@ -7,6 +7,8 @@
 #include <cstdint>
 #include <cstring>
 
+#include <cuda_runtime.h>
+
 #include "../../include/su2gpu.h"
 #include "su2_ops.h"
 
@@ -43,6 +45,25 @@ inline void carve(Fields<R>& f, char* base, const su2gpu_params* p, int64_t V) {
   if (p->content & SU2GPU_TRIPLET)
     for (int k = 0; k < 3; k++) { f.trip[k] = (R*)(base + off); off += align256(V * r); }
   if (p->content & SU2GPU_SINGLET) { f.sing = (R*)(base + off); off += align256(V * r); }
+}
+
+// Device address through which kernels can read or write the host buffer
+// [p, p + bytes) directly: page-locked memory registered with (or allocated
+// by) CUDA, which on a unified-address system is mapped into the device's
+// address space.  Null for pageable memory or a buffer only partly
+// registered; the caller then stages through device memory.
+inline void* host_device_view(const void* p, size_t bytes) {
+  if (!p || !bytes) return nullptr;
+  cudaPointerAttributes a0, a1;
+  const char* last = (const char*)p + bytes - 1;
+  if (cudaPointerGetAttributes(&a0, p) != cudaSuccess || cudaPointerGetAttributes(&a1, last) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer || !a1.devicePointer)
+    return nullptr;
+  if ((const char*)a1.devicePointer - (const char*)a0.devicePointer != (ptrdiff_t)(bytes - 1)) return nullptr;
+  return a0.devicePointer;
 }
 
 SU2_HIDDEN Coup make_coup(const su2gpu_params* p);

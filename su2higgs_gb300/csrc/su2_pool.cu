@@ -65,6 +65,10 @@ __global__ void k_cold_links4d(D4* p, int64_t n) {
   if (k < n) p[k] = D4{1.0, 0.0, 0.0, 0.0};
 }
 
+// doubles per site of one chain's host arrays (links 12, U(1) 3, two doublets
+// 8, triplet 3, singlet 1)
+constexpr int STAGE_REALS = 27;
+
 struct Slot {
   bool active = false;
   su2gpu_params p;
@@ -94,6 +98,8 @@ struct su2gpu_pool {
   Buf slotmem;   // per slot: sweep counter word + 24 counters
   Buf descs;     // ChainDesc<R>[max_slots]
   Buf tiles[NVARIANTS], mtiles, mfirst, sweepptrs, partials, sums, stage, err;
+  int64_t stage_sites = 0;          // sites each staging half holds (STAGE_REALS doubles per site)
+  cudaEvent_t stage_ev[2] = {nullptr, nullptr};
   int ntiles[NVARIANTS] = {0, 0, 0, 0}, nmtiles = 0;
   std::vector<int> active;  // active slots in slot order
   bool dirty = true;
@@ -336,6 +342,11 @@ int su2gpu_pool_create(const su2gpu_params* recipe, int64_t arena_bytes, int32_t
     return fail(SU2GPU_ERR_CUDA, "cudaStreamCreate failed");
   }
   P->st = P->own_st;
+  if (cudaEventCreateWithFlags(&P->stage_ev[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&P->stage_ev[1], cudaEventDisableTiming) != cudaSuccess) {
+    su2gpu_pool_destroy(P);
+    return fail(SU2GPU_ERR_CUDA, "cudaEventCreate failed");
+  }
   size_t dsz = P->prec == 64 ? sizeof(ChainDesc<double>) : sizeof(ChainDesc<float>);
   if ((rc = P->arena.ensure((size_t)arena_bytes)) || (rc = P->slotmem.ensure((size_t)max_chains * 256)) ||
       (rc = P->descs.ensure(dsz * max_chains)) || (rc = P->err.ensure(256))) {
@@ -361,6 +372,8 @@ int su2gpu_pool_destroy(su2gpu_pool* P) {
   P->arena.release(); P->slotmem.release(); P->descs.release(); P->mtiles.release(); P->mfirst.release();
   P->sweepptrs.release(); P->partials.release(); P->sums.release(); P->stage.release(); P->err.release();
   for (int v = 0; v < NVARIANTS; v++) P->tiles[v].release();
+  for (int k = 0; k < 2; k++)
+    if (P->stage_ev[k]) cudaEventDestroy(P->stage_ev[k]);
   if (P->own_st) cudaStreamDestroy(P->own_st);
   delete P;
   return SU2GPU_OK;
@@ -433,13 +446,16 @@ int su2gpu_pool_info(su2gpu_pool* P, int32_t* nactive, int64_t* used_bytes, int6
   return SU2GPU_OK;
 }
 
-static int slot_transfer(su2gpu_pool* P, int32_t s, int upload, double* link, double* u1, double* d0, double* d1,
-                         double* trip, double* sing) {
+// one chain's fields to / from FP64 AoS host arrays.  Uploads from
+// page-locked arrays are read by the conversion kernel in place; other
+// uploads and every download go through staging memory: the chain's arrays
+// at their own offsets in one of two staging halves (`half`), so that one
+// chain's copies overlap the next chain's conversion.  The caller waits on
+// P->stage_ev[half] before reusing a half.
+static int slot_transfer(su2gpu_pool* P, int32_t s, int upload, double* const* h, int half) {
   if (!P || s < 0 || s >= P->max_slots || !P->slots[s].active) return fail(SU2GPU_ERR_INVALID, "no such chain slot");
   const Slot& sl = P->slots[s];
   int64_t V = sl.g.V;
-  int rc = P->stage.ensure((size_t)V * 12 * 8);
-  if (rc) return rc;
   Fields<double> f64;
   Fields<float> f32;
   char* base = (char*)P->arena.p + sl.off;
@@ -447,36 +463,83 @@ static int slot_transfer(su2gpu_pool* P, int32_t s, int upload, double* link, do
   else carve(f32, base, &sl.p, V);
   const void* F = P->prec == 64 ? (const void*)&f64 : (const void*)&f32;
   int nh = nhiggs_of(P->content);
-  struct Item { double* h; int kind, hid; size_t n; bool present; };
-  Item items[] = {{link, 0, 0, (size_t)V * 12, true},
-                  {u1, 1, 0, (size_t)V * 3, (bool)(P->content & SU2GPU_U1)},
-                  {d0, 2, 0, (size_t)V * 4, nh > 0},
-                  {d1, 2, 1, (size_t)V * 4, nh > 1},
-                  {trip, 3, 0, (size_t)V * 3, (bool)(P->content & SU2GPU_TRIPLET)},
-                  {sing, 4, 0, (size_t)V, (bool)(P->content & SU2GPU_SINGLET)}};
-  double* st = (double*)P->stage.p;
-  for (const Item& it : items) {
-    if (!it.present || !it.h) continue;
-    if (upload) {
-      PCK(cudaMemcpyAsync(st, it.h, it.n * 8, cudaMemcpyHostToDevice, P->st));
-      P->pops->import(F, V, it.kind, it.hid, st, P->st);
-    } else {
-      P->pops->exportf(F, V, it.kind, it.hid, st, P->st);
-      PCK(cudaMemcpyAsync(it.h, st, it.n * 8, cudaMemcpyDeviceToHost, P->st));
-    }
+  struct Item { int kind, hid; size_t n; bool present; };
+  const Item items[6] = {{0, 0, (size_t)V * 12, true},
+                         {1, 0, (size_t)V * 3, (bool)(P->content & SU2GPU_U1)},
+                         {2, 0, (size_t)V * 4, nh > 0},
+                         {2, 1, (size_t)V * 4, nh > 1},
+                         {3, 0, (size_t)V * 3, (bool)(P->content & SU2GPU_TRIPLET)},
+                         {4, 0, (size_t)V, (bool)(P->content & SU2GPU_SINGLET)}};
+  if ((size_t)V > (size_t)P->stage_sites) {
+    // staging for a chain this large: both halves grow (waits for all copies)
     PCK(cudaStreamSynchronize(P->st));
+    P->stage_sites = V;
+    int rc = P->stage.ensure(2 * (size_t)V * STAGE_REALS * 8);
+    if (rc) return rc;
   }
+  double* st = (double*)((char*)P->stage.p + (size_t)half * (size_t)P->stage_sites * STAGE_REALS * 8);
+  size_t off = 0;
+  for (int k = 0; k < 6; k++) {
+    const Item& it = items[k];
+    if (!it.present || !h[k]) continue;
+    if (upload) {
+      double* direct = (double*)host_device_view(h[k], it.n * 8);
+      if (direct) {
+        P->pops->import(F, V, it.kind, it.hid, direct, P->st);
+        continue;
+      }
+      PCK(cudaMemcpyAsync(st + off, h[k], it.n * 8, cudaMemcpyHostToDevice, P->st));
+      P->pops->import(F, V, it.kind, it.hid, st + off, P->st);
+    } else {
+      P->pops->exportf(F, V, it.kind, it.hid, st + off, P->st);
+      PCK(cudaMemcpyAsync(h[k], st + off, it.n * 8, cudaMemcpyDeviceToHost, P->st));
+    }
+    off += it.n;
+  }
+  PCK(cudaEventRecord(P->stage_ev[half], P->st));
+  PCK(cudaGetLastError());
   return SU2GPU_OK;
 }
 
 int su2gpu_pool_upload(su2gpu_pool* P, int32_t s, const double* link, const double* u1, const double* d0,
                        const double* d1, const double* trip, const double* sing) {
-  return slot_transfer(P, s, 1, (double*)link, (double*)u1, (double*)d0, (double*)d1, (double*)trip, (double*)sing);
+  double* h[6] = {(double*)link, (double*)u1, (double*)d0, (double*)d1, (double*)trip, (double*)sing};
+  int rc = slot_transfer(P, s, 1, h, 0);
+  if (rc) return rc;
+  PCK(cudaStreamSynchronize(P->st));
+  return SU2GPU_OK;
 }
 
 int su2gpu_pool_download(su2gpu_pool* P, int32_t s, double* link, double* u1, double* d0, double* d1, double* trip,
                          double* sing) {
-  return slot_transfer(P, s, 0, link, u1, d0, d1, trip, sing);
+  double* h[6] = {link, u1, d0, d1, trip, sing};
+  int rc = slot_transfer(P, s, 0, h, 0);
+  if (rc) return rc;
+  PCK(cudaStreamSynchronize(P->st));
+  return SU2GPU_OK;
+}
+
+// many chains in one call: fields[k][j] is field k (link, u1, doublet0,
+// doublet1, triplet, singlet) of slots[j]; a null fields[k] skips field k
+static int many_transfer(su2gpu_pool* P, int32_t n, const int32_t* slots, int upload, double* const* const* fields) {
+  if (!P || n < 0 || (n && !slots) || !fields) return fail(SU2GPU_ERR_INVALID, "bad arguments");
+  for (int32_t j = 0; j < n; j++) {
+    double* h[6];
+    for (int k = 0; k < 6; k++) h[k] = fields[k] ? fields[k][j] : nullptr;
+    PCK(cudaEventSynchronize(P->stage_ev[j & 1]));  // the half's previous copies are done
+    int rc = slot_transfer(P, slots[j], upload, h, j & 1);
+    if (rc) return rc;
+  }
+  PCK(cudaStreamSynchronize(P->st));
+  return SU2GPU_OK;
+}
+
+int su2gpu_pool_upload_many(su2gpu_pool* P, int32_t n, const int32_t* slots, const double* const* const* fields) {
+  return many_transfer(P, n, slots, 1, (double* const* const*)fields);
+}
+
+int su2gpu_pool_download_many(su2gpu_pool* P, int32_t n, const int32_t* slots, double* const* const* fields) {
+  return many_transfer(P, n, slots, 0, fields);
 }
 
 int su2gpu_pool_set_sweep(su2gpu_pool* P, int32_t s, uint32_t sweep) {

@@ -346,9 +346,20 @@ static int transfer(su2gpu_ctx* c, int upload, double* link, double* u1, double*
       {trip, 3, 0, (size_t)V * 3, (bool)c->has_t},
       {sing, 4, 0, (size_t)V, (bool)c->has_s},
   };
+  // uploads from page-locked host arrays are read by the conversion kernel in
+  // place (as fast as a copy, one pass); everything else goes through the
+  // staging buffer, one array at a time: downloads are converted on the
+  // device and copied by the copy engine, which writes host memory far faster
+  // than kernel stores do
   for (const Item& it : items) {
     if (!it.present || !it.h) continue;
     if (upload) {
+      double* direct = (double*)host_device_view(it.h, it.n * 8);
+      if (direct) {
+        c->pops->import(c->F(), V, it.kind, it.h_id, direct, c->st);
+        CKL();
+        continue;
+      }
       CK(cudaMemcpyAsync(st, it.h, it.n * 8, cudaMemcpyHostToDevice, c->st));
       c->pops->import(c->F(), V, it.kind, it.h_id, st, c->st);
       CKL();
@@ -357,8 +368,9 @@ static int transfer(su2gpu_ctx* c, int upload, double* link, double* u1, double*
       CKL();
       CK(cudaMemcpyAsync(it.h, st, it.n * 8, cudaMemcpyDeviceToHost, c->st));
     }
-    CK(cudaStreamSynchronize(c->st));
+    CK(cudaStreamSynchronize(c->st));  // the staging buffer is reused by the next array
   }
+  CK(cudaStreamSynchronize(c->st));
   return SU2GPU_OK;
 }
 

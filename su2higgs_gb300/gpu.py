@@ -87,6 +87,8 @@ def lib():
         L.su2gpu_pool_autotune.argtypes = [vp, vp, vp]
         L.su2gpu_pool_set_variants.argtypes = [vp, vp]
         L.su2gpu_pool_extract.argtypes = [vp, i32, ctypes.POINTER(vp)]
+        L.su2gpu_pool_upload_many.argtypes = [vp, i32, vp, vp]
+        L.su2gpu_pool_download_many.argtypes = [vp, i32, vp, vp]
         L.su2gpu_pool_enqueue.argtypes = [vp, i32, i32]
         L.su2gpu_pool_enqueue_measure.argtypes = [vp, vp, i32, ctypes.POINTER(i32)]
         L.su2gpu_pool_set_stream.argtypes = [vp, vp]
@@ -376,6 +378,39 @@ class Pool:
                 raise ValueError(f"{n}: need a C-contiguous float64 array of shape {shp}")
         check(lib().su2gpu_pool_download(self._h, slot, *[_p(out.get(n)) for n in FIELD_NAMES]))
         return out
+
+    def _many(self, fn, slots, fields):
+        n = len(slots)
+        keep = []
+        tables = (ctypes.c_void_p * 6)()
+        for k, name in enumerate(FIELD_NAMES):
+            arrs = [f.get(name) for f in fields]
+            if all(a is None for a in arrs):
+                continue
+            t = (ctypes.c_void_p * n)(*[None if a is None else a.ctypes.data for a in arrs])
+            keep.append(t)
+            tables[k] = ctypes.cast(t, ctypes.c_void_p)
+        sl = np.ascontiguousarray(slots, dtype=np.int32)
+        check(fn(self._h, n, _p(sl), ctypes.cast(tables, ctypes.c_void_p)))
+
+    def upload_many(self, slots, fields):
+        """Upload the chains `slots` in one call; fields[j] is a dict of
+        C-contiguous float64 arrays (as `upload`) for slots[j]."""
+        for f in fields:
+            for a in f.values():
+                if a is not None and (a.dtype != np.float64 or not a.flags.c_contiguous):
+                    raise ValueError("upload_many needs C-contiguous float64 arrays")
+        self._many(lib().su2gpu_pool_upload_many, slots, fields)
+
+    def download_many(self, slots, fields):
+        """Download the chains `slots` in one call into the arrays of
+        fields[j] (dicts as `download(out=...)` takes)."""
+        for s, f in zip(slots, fields):
+            shapes = _shapes(self._params[s])
+            for n, a in f.items():
+                if a is not None and (a.shape != shapes[n] or a.dtype != np.float64 or not a.flags.c_contiguous):
+                    raise ValueError(f"{n}: need a C-contiguous float64 array of shape {shapes[n]}")
+        self._many(lib().su2gpu_pool_download_many, slots, fields)
 
     def set_sweep(self, slot, sweep):
         check(lib().su2gpu_pool_set_sweep(self._h, slot, sweep))
