@@ -48,13 +48,22 @@ __host__ __device__ inline void site_coords(const Geom& g, int parity, int t, in
 
 __host__ __device__ inline int wrap(int v, int L) { return v >= L ? v - L : (v < 0 ? v + L : v); }
 
-// index of the site at c + s1*e_d1 + s2*e_d2 (periodic, |s| <= 1); written
+// lexicographic step from c to c + s*e_d (s in {-1, 0, 1}), periodic
+__host__ __device__ inline int lex_step(const Geom& g, const int* c, int d, int s) {
+  const int st = d == 0 ? 1 : (d == 1 ? g.L[0] : g.L[0] * g.L[1]);
+  const int cd = d == 0 ? c[0] : (d == 1 ? c[1] : c[2]);
+  const int lm = (d == 0 ? g.L[0] : (d == 1 ? g.L[1] : g.L[2])) - 1;
+  return s > 0 ? (cd == lm ? -lm * st : st) : (s < 0 ? (cd == 0 ? lm * st : -st) : 0);
+}
+
+// index of the site at c + s1*e_d1 + s2*e_d2 (periodic, |s| <= 1): the
+// lexicographic index of c (shared by every neighbour of the site) plus the
+// steps, and the parity, which every unit step flips (even sides); written
 // with selects so that runtime directions never index an array
 __host__ __device__ inline int shifted(const Geom& g, const int* c, int d1, int s1, int d2 = 0, int s2 = 0) {
-  int x = wrap(c[0] + (d1 == 0 ? s1 : 0) + (d2 == 0 ? s2 : 0), g.L[0]);
-  int y = wrap(c[1] + (d1 == 1 ? s1 : 0) + (d2 == 1 ? s2 : 0), g.L[1]);
-  int z = wrap(c[2] + (d1 == 2 ? s1 : 0) + (d2 == 2 ? s2 : 0), g.L[2]);
-  return site_index(g, x, y, z);
+  int n = c[0] + g.L[0] * (c[1] + g.L[1] * c[2]) + lex_step(g, c, d1, s1) + lex_step(g, c, d2, s2);
+  int par = (c[0] + c[1] + c[2] + s1 + s2) & 1;
+  return par * g.half + (n >> 1);
 }
 // coordinates of c + s*e_d
 __host__ __device__ inline void shift_coords(const Geom& g, const int* c, int d, int s, int* o) {
