@@ -28,7 +28,34 @@ struct Geom {
   int hL0;   // L0 / 2
   int V;     // sites (< 2^31)
   int half;  // sites per parity
+  // division by hL0 and by L1 as a multiply and shift (div30)
+  unsigned m_hl0, m_l1;
+  int s_hl0, s_l1;
 };
+
+// floor(n / d) for 0 <= n < 2^30 as (n * m) >> s with l = ceil(log2 d),
+// s = 30 + l, m = floor(2^s / d) + 1 < 2^31: then 2^s <= m d <= 2^s + 2^l,
+// which makes the quotient exact (Granlund & Montgomery, PLDI 1994, thm 4.2)
+inline void div30_magic(unsigned d, unsigned* m, int* s) {
+  int l = 0;
+  while ((1ull << l) < d) l++;
+  *s = 30 + l;
+  *m = (unsigned)((1ull << *s) / d + 1);
+}
+__host__ __device__ inline unsigned div30(unsigned n, unsigned m, int s) {
+  return (unsigned)(((unsigned long long)n * m) >> s);
+}
+
+inline Geom make_geom(int L0, int L1, int L2) {
+  Geom g;
+  g.L[0] = L0; g.L[1] = L1; g.L[2] = L2;
+  g.hL0 = L0 / 2;
+  g.V = L0 * L1 * L2;
+  g.half = g.V / 2;
+  div30_magic((unsigned)g.hL0, &g.m_hl0, &g.s_hl0);
+  div30_magic((unsigned)L1, &g.m_l1, &g.s_l1);
+  return g;
+}
 
 __host__ __device__ inline int site_index(const Geom& g, int x, int y, int z) {
   int n = x + g.L[0] * (y + g.L[1] * z);
@@ -37,9 +64,9 @@ __host__ __device__ inline int site_index(const Geom& g, int x, int y, int z) {
 
 // coordinates of the t-th site of a parity
 __host__ __device__ inline void site_coords(const Geom& g, int parity, int t, int* c) {
-  unsigned r = (unsigned)t / (unsigned)g.hL0;
+  unsigned r = div30((unsigned)t, g.m_hl0, g.s_hl0);
   int k = t - (int)r * g.hL0;
-  unsigned z = r / (unsigned)g.L[1];
+  unsigned z = div30(r, g.m_l1, g.s_l1);
   int y = (int)(r - z * (unsigned)g.L[1]);
   c[0] = 2 * k + ((parity + y + (int)z) & 1);
   c[1] = y;

@@ -15,14 +15,22 @@ template <int V>
 static unsigned l_link_v(const void* f, const PassArgs& a, cudaStream_t st) {
   constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB;
   unsigned nb = (unsigned)((a.t_hi - a.t_lo + BS - 1) / BS);
-  if (nb) k_link<R, CCI, BS, MB><<<nb, BS, 0, st>>>(*(const Fields<R>*)f, a);
+  if (!nb) return 0;
+  const Fields<R>& F = *(const Fields<R>*)f;
+  if (a.sub == 0) k_link<R, CCI, 0, BS, MB><<<nb, BS, 0, st>>>(F, a);
+  else if (a.sub == 1) k_link<R, CCI, 1, BS, MB><<<nb, BS, 0, st>>>(F, a);
+  else k_link<R, CCI, 2, BS, MB><<<nb, BS, 0, st>>>(F, a);
   return nb;
 }
 template <int V>
 static unsigned l_u1_v(const void* f, const PassArgs& a, cudaStream_t st) {
   constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB;
   unsigned nb = (unsigned)((a.t_hi - a.t_lo + BS - 1) / BS);
-  if (nb) k_u1<R, CCI, BS, MB><<<nb, BS, 0, st>>>(*(const Fields<R>*)f, a);
+  if (!nb) return 0;
+  const Fields<R>& F = *(const Fields<R>*)f;
+  if (a.sub == 0) k_u1<R, CCI, 0, BS, MB><<<nb, BS, 0, st>>>(F, a);
+  else if (a.sub == 1) k_u1<R, CCI, 1, BS, MB><<<nb, BS, 0, st>>>(F, a);
+  else k_u1<R, CCI, 2, BS, MB><<<nb, BS, 0, st>>>(F, a);
   return nb;
 }
 template <int V>
@@ -71,11 +79,19 @@ static void l_flow(const void* fin, const void* fout, const Geom& g, const Coup&
 
 template <int V>
 static void lp_link_v(const PoolArgs& a, unsigned nb, cudaStream_t st) {
-  if (nb) k_pool_link<R, CCI, Variant<R, V>::BS, Variant<R, V>::MINB><<<nb, Variant<R, V>::BS, 0, st>>>(a);
+  constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB;
+  if (!nb) return;
+  if (a.sub == 0) k_pool_link<R, CCI, 0, BS, MB><<<nb, BS, 0, st>>>(a);
+  else if (a.sub == 1) k_pool_link<R, CCI, 1, BS, MB><<<nb, BS, 0, st>>>(a);
+  else k_pool_link<R, CCI, 2, BS, MB><<<nb, BS, 0, st>>>(a);
 }
 template <int V>
 static void lp_u1_v(const PoolArgs& a, unsigned nb, cudaStream_t st) {
-  if (nb) k_pool_u1<R, CCI, Variant<R, V>::BS, Variant<R, V>::MINB><<<nb, Variant<R, V>::BS, 0, st>>>(a);
+  constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB;
+  if (!nb) return;
+  if (a.sub == 0) k_pool_u1<R, CCI, 0, BS, MB><<<nb, BS, 0, st>>>(a);
+  else if (a.sub == 1) k_pool_u1<R, CCI, 1, BS, MB><<<nb, BS, 0, st>>>(a);
+  else k_pool_u1<R, CCI, 2, BS, MB><<<nb, BS, 0, st>>>(a);
 }
 template <int V>
 static void lp_scalar_v(int field, const PoolArgs& a, unsigned nb, cudaStream_t st) {

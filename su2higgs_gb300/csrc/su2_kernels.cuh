@@ -733,7 +733,9 @@ __device__ inline const CoupT<double>& coup<double>(const PassArgs& a) { return 
 template <>
 __device__ inline const CoupT<float>& coup<float>(const PassArgs& a) { return a.cpf; }
 
-template <typename R, int CC, int BS, int MINB>
+// MU: the link direction of the pass, a template parameter so that every
+// neighbour offset and field pointer of the staple is fixed at compile time
+template <typename R, int CC, int MU, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_link(Fields<R> f, PassArgs a) {
   const CoupT<R>& cp = coup<R>(a);
   int t = a.t_lo + (int)blockIdx.x * blockDim.x + threadIdx.x;
@@ -743,15 +745,15 @@ __global__ void __launch_bounds__(BS, MINB) k_link(Fields<R> f, PassArgs a) {
     site_coords(a.g, a.parity, t, c);
     int i = a.parity * a.g.half + t;
     SiteRng<R> rng(a.rk, *a.rk.sweep, (uint32_t)i, a.pass);
-    if (a.alg == ALG_HEATBATH) acc = heatbath<R, CC>(f, a.g, cp, c, i, a.sub, rng, &cap, &err);
-    else acc = metro_link<R, CC>(f, a.g, cp, c, i, a.sub, rng);
+    if (a.alg == ALG_HEATBATH) acc = heatbath<R, CC>(f, a.g, cp, c, i, MU, rng, &cap, &err);
+    else acc = metro_link<R, CC>(f, a.g, cp, c, i, MU, rng);
   }
   warp_count(a.ctr + 1, acc);
   warp_count(a.ctr + 22, cap);
   if (err) atomicOr(a.err, 1);
 }
 
-template <typename R, int CC, int BS, int MINB>
+template <typename R, int CC, int MU, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_u1(Fields<R> f, PassArgs a) {
   const CoupT<R>& cp = coup<R>(a);
   int t = a.t_lo + (int)blockIdx.x * blockDim.x + threadIdx.x;
@@ -761,7 +763,7 @@ __global__ void __launch_bounds__(BS, MINB) k_u1(Fields<R> f, PassArgs a) {
     site_coords(a.g, a.parity, t, c);
     int i = a.parity * a.g.half + t;
     SiteRng<R> rng(a.rk, *a.rk.sweep, (uint32_t)i, a.pass);
-    acc = metro_u1<R, CC>(f, a.g, cp, c, i, a.sub, rng);
+    acc = metro_u1<R, CC>(f, a.g, cp, c, i, MU, rng);
   }
   warp_count(a.ctr + 3, acc);
 }

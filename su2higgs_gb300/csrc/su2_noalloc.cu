@@ -123,11 +123,7 @@ extern "C" int su2gpu_measure_noalloc(const su2gpu_params* p, const su2gpu_devic
   double* scratch = noalloc_scratch(dev, &e);
   if (!scratch) return noalloc_fail(SU2GPU_ERR_CUDA, cudaGetErrorString(e));
 
-  Geom g;
-  for (int d = 0; d < 3; d++) g.L[d] = p->L[d];
-  g.hL0 = p->L[0] / 2;
-  g.V = p->L[0] * p->L[1] * p->L[2];
-  g.half = g.V / 2;
+  Geom g = make_geom(p->L[0], p->L[1], p->L[2]);
   Coup cp;
   memset(&cp, 0, sizeof(cp));
   cp.beta = p->betasu2; cp.msq = p->msq_phi; cp.lam = p->lambda_phi;

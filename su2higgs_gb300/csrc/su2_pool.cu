@@ -397,10 +397,7 @@ int su2gpu_pool_add(su2gpu_pool* P, const su2gpu_params* p, uint64_t seed, uint3
   sl = Slot();
   sl.active = true;
   sl.p = *p;
-  for (int d = 0; d < 3; d++) sl.g.L[d] = p->L[d];
-  sl.g.hL0 = p->L[0] / 2;
-  sl.g.V = (int)V;
-  sl.g.half = (int)(V / 2);
+  sl.g = make_geom(p->L[0], p->L[1], p->L[2]);
   sl.cp = make_coup(p);
   sl.off = off;
   sl.bytes = bytes;

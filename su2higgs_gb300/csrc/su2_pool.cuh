@@ -50,7 +50,7 @@ __device__ inline const ChainDesc<R>& stage_desc(const PoolArgs& a, int slot) {
   return *(const ChainDesc<R>*)buf;
 }
 
-template <typename R, int CC, int BS, int MINB>
+template <typename R, int CC, int MU, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_pool_link(PoolArgs a) {
   int2 tile = a.tiles[blockIdx.x];
   if (bad_tile(a, tile)) return;
@@ -63,15 +63,15 @@ __global__ void __launch_bounds__(BS, MINB) k_pool_link(PoolArgs a) {
     site_coords(d.g, a.parity, t, c);
     int i = a.parity * d.g.half + t;
     SiteRng<R> rng(RngKey{d.k0, d.k1, d.chain, d.sweep}, *d.sweep, (uint32_t)i, a.pass);
-    if (a.alg == ALG_HEATBATH) acc = heatbath<R, CC>(d.f, d.g, cp, c, i, a.sub, rng, &cap, &err);
-    else acc = metro_link<R, CC>(d.f, d.g, cp, c, i, a.sub, rng);
+    if (a.alg == ALG_HEATBATH) acc = heatbath<R, CC>(d.f, d.g, cp, c, i, MU, rng, &cap, &err);
+    else acc = metro_link<R, CC>(d.f, d.g, cp, c, i, MU, rng);
   }
   warp_count(d.ctr + 1, acc);
   warp_count(d.ctr + 22, cap);
   if (err) atomicOr(a.err, 1);
 }
 
-template <typename R, int CC, int BS, int MINB>
+template <typename R, int CC, int MU, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_pool_u1(PoolArgs a) {
   int2 tile = a.tiles[blockIdx.x];
   if (bad_tile(a, tile)) return;
@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(BS, MINB) k_pool_u1(PoolArgs a) {
     site_coords(d.g, a.parity, t, c);
     int i = a.parity * d.g.half + t;
     SiteRng<R> rng(RngKey{d.k0, d.k1, d.chain, d.sweep}, *d.sweep, (uint32_t)i, a.pass);
-    acc = metro_u1<R, CC>(d.f, d.g, d.cp, c, i, a.sub, rng);
+    acc = metro_u1<R, CC>(d.f, d.g, d.cp, c, i, MU, rng);
   }
   warp_count(d.ctr + 3, acc);
 }

@@ -225,10 +225,7 @@ static int create_ctx(const su2gpu_params* p, void* borrowed, const void* copy_f
   c->has_t = !!(p->content & SU2GPU_TRIPLET);
   c->has_s = !!(p->content & SU2GPU_SINGLET);
   c->has_u1 = !!(p->content & SU2GPU_U1);
-  for (int d = 0; d < 3; d++) c->g.L[d] = p->L[d];
-  c->g.hL0 = p->L[0] / 2;
-  c->g.V = (int64_t)p->L[0] * p->L[1] * p->L[2];
-  c->g.half = c->g.V / 2;
+  c->g = make_geom(p->L[0], p->L[1], p->L[2]);
   c->cp = make_coup(p);
   c->ops = pick_ops(c->prec, p->content);
   c->pops = c->prec == 64 ? &precops_f64 : &precops_f32;

@@ -1,13 +1,15 @@
 """Pools of independent chains (the batched form) through the C ABI.
 
-* A chain of a pool follows the trajectory of a single-lattice context with
-  the same parameters, seed and chain id: the same random numbers and
+* FP64: a chain of a pool follows the trajectory of a single-lattice context
+  with the same parameters, seed and chain id: the same random numbers and
   accept/reject decisions (counters equal), fields equal to rounding -- the
   per-site arithmetic is the same source compiled into two kernels, whose
-  fused multiply-adds the compiler may form differently (1e-11 absolute after
-  three FP64 sweeps, as the oracle parity tests; 1e-4 for FP32 fields) --
-  and measure() sums to 1e-9 relative (FP64, as the oracle parity tests
-  after three sweeps) or 1e-6 (FP32).
+  fused multiply-adds the compiler may form differently -- 1e-9 absolute
+  after three sweeps and measure() sums to 1e-9 relative, as the oracle parity
+  tests.  In FP32 such a rounding difference can flip an accept/reject
+  decision and the two trajectories part; FP32 pool chains are checked
+  statistically instead (observables of pool chains against FP64
+  single-lattice chains within 3 sigma).
 * Membership does not change a chain's trajectory: a chain alone and the
   same chain among others, admitted and retired around it, agree bit for bit
   (one kernel, random numbers keyed by chain and site).
@@ -69,8 +71,8 @@ def as_dict(f):
     return {n: getattr(f, n) for n in ("link", "u1", "d0", "d1", "trip", "sing")}
 
 
-@pytest.mark.parametrize("content,precision", [("fund", 32), ("adj", 32), ("su2u1s", 64), ("higgs2", 64),
-                                               ("fundadj", 32), ("adj", 64)])
+@pytest.mark.parametrize("content,precision", [("fund", 64), ("su2u1s", 64), ("higgs2", 64), ("fundadj", 64),
+                                               ("adj", 64)])
 @pytest.mark.parametrize("graph", [True, False])
 def test_pool_chains_equal_single_lattices(gpu, content, precision, graph):
     specs = chain_specs(content, precision)
@@ -85,7 +87,7 @@ def test_pool_chains_equal_single_lattices(gpu, content, precision, graph):
     pool.run(2, graph=graph)
     pool.run(1, graph=graph)
     sums = pool.measure()
-    atol, rtol = (1e-11, 1e-9) if precision == 64 else (1e-4, 1e-6)
+    atol, rtol = 1e-9, 1e-9
     for s, (p, seed, chain), f in zip(slots, specs, inputs):
         want_f, want_c, want_m = single_run(gpu, p, f, seed, chain, 3)
         fields_close(pool.download(s), want_f, atol)
@@ -172,7 +174,7 @@ def test_pool_admission_by_footprint(gpu):
 
 
 def test_pool_autotune_does_not_advance(gpu):
-    specs = chain_specs("su2u1s", 32)
+    specs = chain_specs("su2u1s", 64)
     pool = gpu.Pool(specs[0][0], arena_bytes=64 << 20, max_chains=8)
     slots = [pool.add(p, seed=seed, chain=chain) for p, seed, chain in specs]
     pool.run(1)
@@ -187,7 +189,7 @@ def test_pool_autotune_does_not_advance(gpu):
     for s, (p, seed, chain) in zip(slots, specs):
         lat = gpu.Lattice(p, seed=seed, chain=chain)
         lat.run_sweeps(0, 3, graph=False)
-        fields_close(pool.download(s), lat.download(), 1e-4)
+        fields_close(pool.download(s), lat.download(), 1e-9)
         assert np.array_equal(pool.counters(s), lat.counters())
 
 
@@ -212,7 +214,7 @@ def test_pool_ensemble_async_api(gpu):
     device buffer, profiled sweeps; chains still equal single lattices."""
     import torch
     from su2higgs_gb300 import workloads
-    specs = workloads.batched_ensemble(64, seed=77)
+    specs = workloads.batched_ensemble(64, seed=77, precision=64)
     arena = sum(gpu.Pool.chain_bytes(p) for p, _, _ in specs)
     pool = gpu.Pool(specs[0][0], arena_bytes=arena, max_chains=64)
     slots = []
@@ -240,10 +242,51 @@ def test_pool_ensemble_async_api(gpu):
         lat = gpu.Lattice(p, seed=seed, chain=chain)
         lat.upload(**workloads.hot_fields(p, seed))
         lat.run_sweeps(0, 2, graph=True)
-        ok, i, a, b = measure_close(dev[k], lat.measure(), 1e-6)
+        ok, i, a, b = measure_close(dev[k], lat.measure(), 1e-9)
         assert ok, (k, i, a, b)
         lat.run_sweeps(2, 1, graph=False)
-        fields_close(pool.download(slots[k]), lat.download(), 1e-4)
+        fields_close(pool.download(slots[k]), lat.download(), 1e-9)
         assert np.array_equal(pool.counters(slots[k]), lat.counters())
-        ok, i, a, b = measure_close(host_sums[slots[k]], lat.measure(), 1e-6)
+        ok, i, a, b = measure_close(host_sums[slots[k]], lat.measure(), 1e-9)
         assert ok, (k, i, a, b)
+
+
+def test_pool_fp32_samples_the_fp64_distribution(gpu):
+    """FP32 pool chains (fundamental Higgs, 8^3, beta 8, m^2 -0.1, lambda 0.002)
+    against FP64 single-lattice chains: plaquette, phi^2 and the hopping term
+    agree within 3 sigma of binned jackknife errors."""
+    from stats import compare_means
+    p32 = abi.make_params("fund", L=(8, 8, 8), precision=32)
+    p64 = abi.make_params("fund", L=(8, 8, 8), precision=64)
+    nchains, ntherm, nmeas = 4, 200, 3000
+    pool = gpu.Pool(p32, arena_bytes=8 << 20, max_chains=nchains)
+    slots = []
+    for k in range(nchains):
+        s = pool.add(p32, seed=500 + k, chain=k)
+        f = as_dict(hot_fields(p32, seed=600 + k, phi_mean=1.0))
+        pool.upload(s, **{n: v for n, v in f.items() if v is not None})
+        slots.append(s)
+    pool.run(ntherm)
+    V = p32.sites()
+    obs32 = {s: [] for s in slots}
+    for _ in range(nmeas):
+        pool.run(1)
+        for s, m in pool.measure().items():
+            obs32[s].append((m[abi.M_WILSON] / (V * p32.betasu2), m[abi.M_PHI2] / V, m[abi.M_COV_PHI] / (3 * V)))
+    obs64 = []
+    for k in range(nchains):
+        lat = gpu.Lattice(p64, seed=700 + k, chain=k)
+        f = as_dict(hot_fields(p64, seed=600 + k, phi_mean=1.0))
+        lat.upload(**{n: v for n, v in f.items() if v is not None})
+        lat.run_sweeps(0, ntherm, graph=True)
+        rows = []
+        for sw in range(nmeas):
+            lat.update_lattice(ntherm + sw)
+            m = lat.measure()
+            rows.append((m[abi.M_WILSON] / (V * p64.betasu2), m[abi.M_PHI2] / V, m[abi.M_COV_PHI] / (3 * V)))
+        obs64.append(np.array(rows))
+    a = np.concatenate([np.array(obs32[s]) for s in slots])
+    b = np.concatenate(obs64)
+    for k, name in enumerate(("plaquette", "phi2", "hopping")):
+        z, ma, mb = compare_means(a[:, k], b[:, k])
+        assert z < 3.0, (name, z, ma, mb)
