@@ -305,9 +305,14 @@ struct V3 {
 // vec(u (0,b) u^dagger): the adjoint rotation of a triplet by a link
 template <typename R>
 __device__ inline V3<R> qrot(const Q<R>& u, const V3<R>& b) {
-  Q<R> vb{(R)0, b.x, b.y, b.z};
-  Q<R> o = qmul(qmul(u, vb), qdag(u));
-  return V3<R>{o.b, o.c, o.d};
+  // vector part of (u (0, b)) u^dagger, written out: the zero real part of
+  // (0, b) and the real part of the result are never formed
+  const R pa = -(u.b * b.x + u.c * b.y + u.d * b.z);
+  const R px = u.a * b.x - (u.c * b.z - u.d * b.y);
+  const R py = u.a * b.y - (u.d * b.x - u.b * b.z);
+  const R pz = u.a * b.z - (u.b * b.y - u.c * b.x);
+  return V3<R>{u.a * px - pa * u.b + (py * u.d - pz * u.c), u.a * py - pa * u.c + (pz * u.b - px * u.d),
+               u.a * pz - pa * u.d + (px * u.c - py * u.b)};
 }
 template <typename R>
 __device__ inline R dot3(const V3<R>& a, const V3<R>& b) {

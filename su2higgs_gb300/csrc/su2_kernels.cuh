@@ -511,8 +511,15 @@ __device__ inline int overrelax_doublet(const Fields<R>& f, const Geom& g, const
   Q<R> s = staple_doublet<R, CC>(f, g, cp, c, i, 0);
   Q<R> p = ld4<R>(php(f, 0), i);
   R F = msqrt(s.a * s.a + s.b * s.b + s.c * s.c + s.d * s.d);
-  R X = (p.a * s.a + p.b * s.b + p.c * s.c + p.d * s.d) / F;
-  R y0 = p.a - X * s.a / F, y1 = p.b - X * s.b / F, y2 = p.c - X * s.c / F, y3 = p.d - X * s.d / F;
+  // FP32: one reciprocal instead of nine divisions (the FP64 path divides as
+  // the reference does)
+  const bool f32 = sizeof(R) == 4;
+  const R iF = f32 ? (R)1 / F : (R)0;
+  R X = f32 ? (p.a * s.a + p.b * s.b + p.c * s.c + p.d * s.d) * iF : (p.a * s.a + p.b * s.b + p.c * s.c + p.d * s.d) / F;
+  R y0 = f32 ? p.a - X * s.a * iF : p.a - X * s.a / F;
+  R y1 = f32 ? p.b - X * s.b * iF : p.b - X * s.b / F;
+  R y2 = f32 ? p.c - X * s.c * iF : p.c - X * s.c / F;
+  R y3 = f32 ? p.d - X * s.d * iF : p.d - X * s.d / F;
   R Ysq = y0 * y0 + y1 * y1 + y2 * y2 + y3 * y3;
   R B = (R)0.5 * (R)cp.msq + (R)3;
   if (HAS(C_T)) B += (R)0.5 * (R)cp.a2 * tripletsq(ld3(f, i));
@@ -527,7 +534,8 @@ __device__ inline int overrelax_doublet(const Fields<R>& f, const Geom& g, const
   R dVn = F + (R)2 * B * newX + (R)4 * C * (newX * newX * newX + Ysq * newX);
   if (mabs(dV / dVn) >= rng.uni()) {
     R k = (newX + X);
-    st4<R>(php(f, 0), i, Q<R>{-p.a + k * s.a / F, -p.b + k * s.b / F, -p.c + k * s.c / F, -p.d + k * s.d / F});
+    st4<R>(php(f, 0), i, f32 ? Q<R>{-p.a + k * s.a * iF, -p.b + k * s.b * iF, -p.c + k * s.c * iF, -p.d + k * s.d * iF}
+                             : Q<R>{-p.a + k * s.a / F, -p.b + k * s.b / F, -p.c + k * s.c / F, -p.d + k * s.d / F});
     return 1;
   }
   return 0;
@@ -608,8 +616,14 @@ __device__ inline int overrelax_triplet(const Fields<R>& f, const Geom& g, const
   }
   V3<R> t = ld3(f, i);
   R F = msqrt(s.x * s.x + s.y * s.y + s.z * s.z);
-  R X = (t.x * s.x + t.y * s.y + t.z * s.z) / F;
-  R y0 = t.x - X * s.x / F, y1 = t.y - X * s.y / F, y2 = t.z - X * s.z / F;
+  // FP32: one reciprocal instead of seven divisions (the FP64 path divides as
+  // the reference does)
+  const bool f32 = sizeof(R) == 4;
+  const R iF = f32 ? (R)1 / F : (R)0;
+  R X = f32 ? (t.x * s.x + t.y * s.y + t.z * s.z) * iF : (t.x * s.x + t.y * s.y + t.z * s.z) / F;
+  R y0 = f32 ? t.x - X * s.x * iF : t.x - X * s.x / F;
+  R y1 = f32 ? t.y - X * s.y * iF : t.y - X * s.y / F;
+  R y2 = f32 ? t.z - X * s.z * iF : t.z - X * s.z / F;
   R Ysq = y0 * y0 + y1 * y1 + y2 * y2;
   R B = (R)0.5 * (R)cp.msqT + (R)3;
   R C = (R)0.25 * (R)cp.b4;
@@ -619,7 +633,8 @@ __device__ inline int overrelax_triplet(const Fields<R>& f, const Geom& g, const
   R dVn = F + (R)2 * B * newX + (R)4 * C * (newX * newX * newX + Ysq * newX);
   if (mabs(dV / dVn) >= rng.uni()) {
     R k = newX + X;
-    st3(f, i, V3<R>{-t.x + k * s.x / F, -t.y + k * s.y / F, -t.z + k * s.z / F});
+    st3(f, i, f32 ? V3<R>{-t.x + k * s.x * iF, -t.y + k * s.y * iF, -t.z + k * s.z * iF}
+                  : V3<R>{-t.x + k * s.x / F, -t.y + k * s.y / F, -t.z + k * s.z / F});
     return 1;
   }
   return 0;

@@ -81,3 +81,23 @@ def kp_a0_cdf(alpha):
         a = np.asarray(a, dtype=np.float64)
         return 1.0 - np.interp(1.0 - a, y, cum)
     return cdf
+
+
+def chains_mean(chains):
+    """Mean over independent chains and its error: the chains' binned
+    jackknife errors (each aware of its own autocorrelation) combined."""
+    ms, es = [], []
+    for x in chains:
+        m, e, _ = jackknife_mean(x)
+        ms.append(m)
+        es.append(e)
+    n = len(ms)
+    return float(np.mean(ms)), float(np.sqrt(np.sum(np.square(es))) / n)
+
+
+def compare_chain_means(a_chains, b_chains):
+    """|mean(a) - mean(b)| in units of the combined error, for two sets of
+    independent chains."""
+    ma, ea = chains_mean(a_chains)
+    mb, eb = chains_mean(b_chains)
+    return abs(ma - mb) / np.sqrt(ea ** 2 + eb ** 2 + 1e-300), (ma, ea), (mb, eb)
