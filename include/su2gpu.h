@@ -210,6 +210,16 @@ int su2gpu_muca_init_last_max(su2gpu_ctx* ctx);
  * Returns the number of rows in *nrows (at most maxrows). */
 int su2gpu_grad_flow(su2gpu_ctx* ctx, double t_max, double dt, int32_t meas_interval,
                      double* rows, int32_t maxrows, int32_t* nrows);
+/* measure_local (measure.c:368-487): per site, in storage order, Tr Sigma^2
+ * and the magnetic charge in units of 2 pi sqrt(beta) (magcharge_cube,
+ * magfield.c:262-280): out[2 i], out[2 i + 1] for site i, V x 2 doubles.
+ * Triplet content only (the reference writes no values without it). */
+int su2gpu_measure_local(su2gpu_ctx* ctx, double* out);
+/* su2gpu_grad_flow that also returns measure_local of the flowed fields at
+ * every measurement (gradflow.c:81-86, 124-129, 151-156): local holds
+ * max_local blocks of V x 2 doubles, filled in measurement order. */
+int su2gpu_grad_flow_local(su2gpu_ctx* ctx, double t_max, double dt, int32_t meas_interval, double* rows,
+                           int32_t maxrows, int32_t* nrows, double* local, int32_t max_local);
 
 /* Drop-in form of update_lattice() with host buffers: upload the host
  * fields, run one sweep, download them again (the reference mutates its host

@@ -1275,6 +1275,15 @@ int orc_update_lattice(orc_ctx* c) {
 /* ------------------------------------------------------------------ */
 /* measure() sums (measure.c:71-243)                                   */
 /* ------------------------------------------------------------------ */
+/* measure_local (measure.c:368-487): per site in storage order, Tr Sigma^2
+ * and magcharge_cube / (2 pi sqrt(beta)) */
+void orc_measure_local(const orc_ctx* c, double* out) {
+  for (long i = 0; i < c->V; i++) {
+    out[2 * i] = c->has_trip ? tripletsq(TRP(c, i)) : 0.0;
+    out[2 * i + 1] = c->has_trip ? orc_magcharge_cube(c, i) / (2.0 * M_PI * sqrt(c->p.betasu2)) : 0.0;
+  }
+}
+
 void orc_measure(const orc_ctx* c, double* m) {
   for (int k = 0; k < SU2GPU_NMEAS; k++) m[k] = 0.0;
   for (long i = 0; i < c->V; i++) {

@@ -29,6 +29,7 @@ int orc_update_lattice(orc_ctx* c);
 void orc_counters(const orc_ctx* c, int64_t* out);
 void orc_reset_counters(orc_ctx* c);
 void orc_measure(const orc_ctx* c, double* sums);
+void orc_measure_local(const orc_ctx* c, double* out);
 
 /* per-site kernels */
 void orc_wilson_staple(const orc_ctx* c, long i, int dir, double* V);

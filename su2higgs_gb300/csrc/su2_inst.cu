@@ -160,7 +160,12 @@ static void p_reunit(const void* f, int64_t V, const uint32_t* sweep, int interv
 static void p_fixup(const void* fin, const void* fout, const Geom& g, const unsigned long long* fz, cudaStream_t st) {
   k_flow_fixup<R><<<nblk(g.V * 3, 256), 256, 0, st>>>(*(const Fields<R>*)fin, *(const Fields<R>*)fout, g, fz);
 }
-const PrecOps SU2_WITH_PREC = {p_orderparam, p_restore, p_alpha, p_import, p_export, p_reunit, p_fixup};
+static void p_measure_local(const void* f, const Geom& g, const Coup& cp, double denom, double* out,
+                            cudaStream_t st) {
+  k_measure_local<R><<<nblk(g.V, BLOCK), BLOCK, 0, st>>>(*(const Fields<R>*)f, g, coup_as<R>(cp), denom, out);
+}
+const PrecOps SU2_WITH_PREC = {p_orderparam, p_restore, p_alpha, p_import, p_export, p_reunit, p_fixup,
+                               p_measure_local};
 #endif
 
 #ifdef SU2_WITH_GLOBAL

@@ -1173,6 +1173,42 @@ struct AlphaOnTheFly {
   }
 };
 
+// magcharge_cube (magfield.c:262-280): the divergence of the magnetic field
+// of the projected U(1) over the cube at site i (coordinates c)
+template <typename R, typename AF>
+__device__ inline double magcharge_site(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
+                                        const AF& alpha) {
+  int c0[3], c1[3], c2[3];
+  shift_coords(g, c, 0, 1, c0);
+  shift_coords(g, c, 1, 1, c1);
+  shift_coords(g, c, 2, 1, c2);
+  int n0 = shifted(g, c, 0, 1), n1 = shifted(g, c, 1, 1), n2 = shifted(g, c, 2, 1);
+  double q = 0.0;
+  double B1 = alpha(f, g, cp, c, i, 2), B2 = alpha(f, g, cp, c0, n0, 2);
+  q += B2 - B1;
+  B1 = -alpha(f, g, cp, c, i, 1);
+  B2 = -alpha(f, g, cp, c1, n1, 1);
+  q += B2 - B1;
+  B1 = alpha(f, g, cp, c, i, 0);
+  B2 = alpha(f, g, cp, c2, n2, 0);
+  q += B2 - B1;
+  return q;
+}
+
+// measure_local (measure.c:368-487): per site (storage order) Tr Sigma^2 and
+// the magnetic charge in units of 2 pi sqrt(beta) -- an integer up to rounding
+template <typename R>
+__global__ void __launch_bounds__(BLOCK) k_measure_local(Fields<R> f, Geom g, CoupT<R> cp, double denom,
+                                                         double* out) {
+  int t = (int)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.V) return;
+  int parity = t >= g.half;
+  int c[3];
+  site_coords(g, parity, t - parity * g.half, c);
+  out[2 * (size_t)t] = (double)tripletsq(ld3(f, t));
+  out[2 * (size_t)t + 1] = magcharge_site(f, g, cp, c, t, AlphaOnTheFly{}) / denom;
+}
+
 // measure() (measure.c:110-233): the terms of site t (storage index) added to
 // m[NSUMS]; per-site quantities in R, sums in FP64
 template <typename R, int CC, typename AF>
@@ -1217,21 +1253,7 @@ __device__ inline void measure_site(const Fields<R>& f, const Geom& g, const Cou
 #pragma unroll
     for (int d = 0; d < 3; d++) hs += hop_triplet_fwd(f, g, c, i, d);
     m[11] += (double)hs;
-    // magcharge_cube (magfield.c:262-280)
-    int c0[3], c1[3], c2[3];
-    shift_coords(g, c, 0, 1, c0);
-    shift_coords(g, c, 1, 1, c1);
-    shift_coords(g, c, 2, 1, c2);
-    int n0 = shifted(g, c, 0, 1), n1 = shifted(g, c, 1, 1), n2 = shifted(g, c, 2, 1);
-    double q = 0.0;
-    double B1 = alpha(f, g, cp, c, i, 2), B2 = alpha(f, g, cp, c0, n0, 2);
-    q += B2 - B1;
-    B1 = -alpha(f, g, cp, c, i, 1);
-    B2 = -alpha(f, g, cp, c1, n1, 1);
-    q += B2 - B1;
-    B1 = alpha(f, g, cp, c, i, 0);
-    B2 = alpha(f, g, cp, c2, n2, 0);
-    q += B2 - B1;
+    double q = magcharge_site(f, g, cp, c, i, alpha);
     m[15] += q;
     m[16] += fabs(q);
   }

@@ -43,6 +43,8 @@ struct PrecOps {
   void (*reunitarize)(const void* f, int64_t V, const uint32_t* sweep, int interval, cudaStream_t st);
   void (*flow_fixup)(const void* fin, const void* fout, const Geom& g, const unsigned long long* fz,
                      cudaStream_t st);
+  // per-site Tr Sigma^2 and magnetic charge / denom, out[2 V] (storage order)
+  void (*measure_local)(const void* f, const Geom& g, const Coup& cp, double denom, double* out, cudaStream_t st);
 };
 
 // instantiations (su2_inst.cu)

@@ -108,7 +108,7 @@ struct su2gpu_ctx {
   int launches = 0;               // kernel launches enqueued by the last sweep
   std::vector<cudaEvent_t>* prof = nullptr;  // per-pass events while profiling
   std::vector<int>* prof_kind = nullptr;
-  DevBuf fields, stage, ctrbuf, partials, sums, alpha, backup, muca, flow, rows;
+  DevBuf fields, stage, ctrbuf, partials, sums, alpha, backup, muca, flow, rows, local;
   bool borrowed = false;  // fields belong to another allocation (su2gpu_attach)
   Fields<double> f64{};
   Fields<float> f32{};
@@ -298,6 +298,7 @@ int su2gpu_destroy(su2gpu_ctx* c) {
   if (c->borrowed) c->fields.p = nullptr;
   c->fields.release(); c->stage.release(); c->ctrbuf.release(); c->partials.release(); c->sums.release();
   c->alpha.release(); c->backup.release(); c->muca.release(); c->flow.release(); c->rows.release();
+  c->local.release();
   if (c->own_st) cudaStreamDestroy(c->own_st);
   delete c;
   return SU2GPU_OK;
@@ -1031,7 +1032,7 @@ static double triplet_tree_mass(const su2gpu_params* p) {
 
 template <typename R>
 static int flow_impl(su2gpu_ctx* c, Fields<R>& main, double t_max, double dt, int32_t mi, double* rows,
-                     int32_t maxrows, int32_t* nrows) {
+                     int32_t maxrows, int32_t* nrows, double* local, int32_t max_local) {
   int64_t V = c->g.V;
   size_t lb = align256((size_t)V * sizeof(V4<R>)), tb = align256((size_t)V * sizeof(R));
   size_t per = 3 * lb + (c->has_t ? 3 * tb : 0);
@@ -1060,10 +1061,22 @@ static int flow_impl(su2gpu_ctx* c, Fields<R>& main, double t_max, double dt, in
   std::vector<double> times;
   int nr = 0;
   double t = 0.0;
+  // measure_local of the flowed fields at every measurement (gradflow.c:81-86),
+  // copied to the caller's host buffer, V x 2 doubles per measurement
+  int nl = 0;
+  const double denom = 2.0 * M_PI * sqrt(c->p.betasu2);
+  if (local && max_local > 0 && (rc = c->local.ensure((size_t)V * 2 * 8))) return rc;
   auto meas = [&](double tt) -> int {
     if (nr >= maxrows) return SU2GPU_OK;
     int r = enqueue_measure(c, &A, cp, drows + (size_t)nr * NSUMS);
     if (r) return r;
+    if (local && nl < max_local) {
+      c->pops->measure_local(&A, c->g, cp, denom, (double*)c->local.p, c->st);
+      CKL();
+      CK(cudaMemcpyAsync(local + (size_t)nl * V * 2, c->local.p, (size_t)V * 2 * 8, cudaMemcpyDeviceToHost, c->st));
+      CK(cudaStreamSynchronize(c->st));
+      nl++;
+    }
     times.push_back(tt);
     nr++;
     return SU2GPU_OK;
@@ -1101,9 +1114,35 @@ extern "C" {
 
 int su2gpu_grad_flow(su2gpu_ctx* c, double t_max, double dt, int32_t meas_interval, double* rows, int32_t maxrows,
                      int32_t* nrows) {
+  return su2gpu_grad_flow_local(c, t_max, dt, meas_interval, rows, maxrows, nrows, nullptr, 0);
+}
+
+int su2gpu_grad_flow_local(su2gpu_ctx* c, double t_max, double dt, int32_t meas_interval, double* rows,
+                           int32_t maxrows, int32_t* nrows, double* local, int32_t max_local) {
   if (!c || !rows || !nrows || meas_interval <= 0 || dt <= 0) return SU2GPU_ERR_INVALID;
-  if (c->prec == 64) return flow_impl<double>(c, c->f64, t_max, dt, meas_interval, rows, maxrows, nrows);
-  return flow_impl<float>(c, c->f32, t_max, dt, meas_interval, rows, maxrows, nrows);
+  if (local && !c->has_t) {
+    set_err("local measurements need the triplet");
+    return SU2GPU_ERR_INVALID;
+  }
+  if (c->prec == 64)
+    return flow_impl<double>(c, c->f64, t_max, dt, meas_interval, rows, maxrows, nrows, local, max_local);
+  return flow_impl<float>(c, c->f32, t_max, dt, meas_interval, rows, maxrows, nrows, local, max_local);
+}
+
+int su2gpu_measure_local(su2gpu_ctx* c, double* out) {
+  if (!c || !out) return SU2GPU_ERR_INVALID;
+  if (!c->has_t) {
+    set_err("local measurements need the triplet");
+    return SU2GPU_ERR_INVALID;
+  }
+  int64_t V = c->g.V;
+  int rc = c->local.ensure((size_t)V * 2 * 8);
+  if (rc) return rc;
+  c->pops->measure_local(c->F(), c->g, c->cp, 2.0 * M_PI * sqrt(c->p.betasu2), (double*)c->local.p, c->st);
+  CKL();
+  CK(cudaMemcpyAsync(out, c->local.p, (size_t)V * 2 * 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return SU2GPU_OK;
 }
 
 // ---------------------------------------------------------------------------

@@ -55,6 +55,9 @@ def lib():
         L.su2gpu_calc_orderparam.argtypes = [vp, i32, dp]
         L.su2gpu_muca_init_last_max.argtypes = [vp]
         L.su2gpu_grad_flow.argtypes = [vp, ctypes.c_double, ctypes.c_double, i32, vp, i32, ctypes.POINTER(i32)]
+        L.su2gpu_grad_flow_local.argtypes = [vp, ctypes.c_double, ctypes.c_double, i32, vp, i32, ctypes.POINTER(i32),
+                                             vp, i32]
+        L.su2gpu_measure_local.argtypes = [vp, vp]
         L.su2gpu_update_lattice_host.argtypes = [vp, u32] + [vp] * 6
         L.su2gpu_stream_uniform.restype = ctypes.c_double
         L.su2gpu_stream_uniform.argtypes = [u64, u32, u32, u32, u32, u32]
@@ -239,6 +242,25 @@ class Lattice:
         n = ctypes.c_int32(0)
         check(lib().su2gpu_grad_flow(self._h, t_max, dt, meas_interval, _p(rows), maxrows, ctypes.byref(n)))
         return rows[: n.value].copy()
+
+    def measure_local(self):
+        """measure_local (measure.c:368): per site in storage order,
+        (Tr Sigma^2, magnetic charge in units of 2 pi sqrt(beta))."""
+        out = np.zeros((self.V, 2))
+        check(lib().su2gpu_measure_local(self._h, _p(out)))
+        return out
+
+    def grad_flow_local(self, t_max, dt, meas_interval, maxrows=None):
+        """grad_flow plus measure_local of the flowed fields at every
+        measurement: (rows, array of shape (rows, V, 2))."""
+        if maxrows is None:
+            maxrows = int(t_max / dt) // meas_interval + 4
+        rows = np.zeros((maxrows, 1 + abi.NMEAS))
+        local = np.zeros((maxrows, self.V, 2))
+        n = ctypes.c_int32(0)
+        check(lib().su2gpu_grad_flow_local(self._h, t_max, dt, meas_interval, _p(rows), maxrows, ctypes.byref(n),
+                                           _p(local), maxrows))
+        return rows[: n.value].copy(), local[: n.value].copy()
 
     def set_stream(self, stream_ptr):
         """Run on a caller's CUDA stream (an int cudaStream_t, e.g.

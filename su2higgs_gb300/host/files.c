@@ -146,6 +146,46 @@ void print_labels(const host_params* hp) {
   fclose(f);
 }
 
+/* print_labels_local (measure.c:347-362) */
+void print_labels_local(const host_params* hp, const char* fname) {
+  FILE* f = fopen(fname, "w+");
+  if (!f) return;
+  int k = 1;
+  for (int dir = 0; dir < hp->p.dim; dir++) {
+    fprintf(f, "%d x%d\n", k, dir);
+    k++;
+  }
+  if (hp->triplet) {
+    fprintf(f, "%d Sigma^2\n", k); k++;
+    fprintf(f, "%d magnetic charge (integer)\n", k); k++;
+  }
+  fclose(f);
+}
+
+/* measure_local's binary file (measure.c:368-487, serial layout): per site i
+ * of the storage order (EVEN sites first) its coordinates as ints, the
+ * triplet's two doubles, and a newline byte */
+int write_measure_local(const char* fname, const host_params* hp, const double* vals) {
+  FILE* f = fopen(fname, "wb");
+  if (!f) return -1;
+  const int* L = hp->p.L;
+  long V = (long)L[0] * L[1] * L[2], half = V / 2;
+  for (long i = 0; i < V; i++) {
+    /* the closed form of the EVEN-first order: t-th site of its parity */
+    int parity = i >= half;
+    long t = i - parity * half;
+    long r = t / (L[0] / 2);
+    int k = (int)(t - r * (L[0] / 2));
+    int z = (int)(r / L[1]), y = (int)(r - (long)z * L[1]);
+    int c[3] = {2 * k + ((parity + y + z) & 1), y, z};
+    fwrite(c, sizeof(int), 3, f);
+    if (hp->triplet && vals) fwrite(vals + 2 * i, sizeof(double), 2, f);
+    fwrite("\n", 1, 1, f);
+  }
+  fclose(f);
+  return 0;
+}
+
 /* one measure() row from the volume sums (measure.c:182-307) */
 void write_measure_row(FILE* f, const host_params* hp, const double* m, const su2gpu_weight* w, int have_muca) {
   double weight = 0.0, muca_param = 0.0;

@@ -62,6 +62,7 @@ static int files_roundtrip(host_params* hp, host_muca* hm) {
     hp->reset = 1;
   }
   print_labels(hp);
+  if (hp->do_local_meas) print_labels_local(hp, "labels_local");
   if (hp->multicanonical) {
     su2gpu_weight w;
     load_weight(&w, hm); /* writes the weight back, as load_weight() does */
@@ -148,7 +149,7 @@ int main(int argc, char** argv) {
   GPU(su2gpu_upload_fields(ctx, arrays[0], arrays[1], arrays[2], arrays[3], arrays[4], arrays[5]));
 
   print_labels(&hp);
-  if (hp.do_local_meas) printf("WARNING: measure_local is not available in this build; ignored\n");
+  if (hp.do_local_meas) print_labels_local(&hp, "labels_local");
 
   FILE* results = fopen(hp.resultsfile, "a");
   su2gpu_weight w;
@@ -212,7 +213,21 @@ int main(int argc, char** argv) {
       int maxrows = (int)(hp.flow_t_max / hp.flow_dt) / (hp.flow_meas_interval > 0 ? hp.flow_meas_interval : 1) + 4;
       double* rows = (double*)malloc(sizeof(double) * maxrows * nmeas);
       int32_t nr = 0;
-      GPU(su2gpu_grad_flow(ctx, hp.flow_t_max, hp.flow_dt, hp.flow_meas_interval, rows, maxrows, &nr));
+      double* local = NULL;
+      if (hp.do_local_meas && hp.triplet) {
+        local = (double*)malloc(sizeof(double) * (size_t)maxrows * (size_t)V * 2);
+        GPU(su2gpu_grad_flow_local(ctx, hp.flow_t_max, hp.flow_dt, hp.flow_meas_interval, rows, maxrows, &nr, local,
+                                   maxrows));
+      } else {
+        GPU(su2gpu_grad_flow(ctx, hp.flow_t_max, hp.flow_dt, hp.flow_meas_interval, rows, maxrows, &nr));
+      }
+      /* measure_local files of the flow (gradflow.c:81-86, 124-129, 151-156) */
+      for (int r = 0; hp.do_local_meas && r < nr; r++) {
+        char fname[200];
+        snprintf(fname, sizeof(fname), "measure_local_%d_%d", flow_id, r + 1);
+        write_measure_local(fname, &hp, local ? local + (size_t)r * V * 2 : NULL);
+      }
+      free(local);
       if (hp.multicanonical) GPU(su2gpu_muca_get(ctx, &w));
       FILE* ff = fopen("measure_flow", "a");
       fprintf(ff, "\n =========== Flow id: %d ===========\n", flow_id);

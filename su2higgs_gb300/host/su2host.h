@@ -59,6 +59,10 @@ int save_lattice(const char* fname, const host_params* hp, long iter, double tot
 int load_lattice(const char* fname, const host_params* hp, long* iter, double* total_time, double* comms_time,
                  double** arrays);
 void print_labels(const host_params* hp);
+void print_labels_local(const host_params* hp, const char* fname);
+/* one measure_local file: per site in storage order its coordinates and, with
+ * the triplet, (Tr Sigma^2, magnetic charge) from vals[2 V] */
+int write_measure_local(const char* fname, const host_params* hp, const double* vals);
 void write_measure_row(FILE* f, const host_params* hp, const double* sums, const su2gpu_weight* w, int have_muca);
 int load_weight(su2gpu_weight* w, host_muca* hm);
 void save_weight(const su2gpu_weight* w);

@@ -12,6 +12,10 @@ directories and stores, per case, in e2e_<case>.npz:
                 configuration, taken before the first update (main.c:306-310)
   measure_flow  its measure_flow block of the same configuration
                 (gradflow.c:66-160), flow before the first update
+  labels_local, measure_local_1_<k>
+                (fund, adj: measure_local 1) the local-measurement labels and
+                the binary per-site files written at every flow measurement
+                (measure.c:347-487)
   lattice_out0  the lattice file it writes after `iterations 0` (fields as
                 loaded, header iteration 1; the two time doubles are not
                 compared)
@@ -42,8 +46,8 @@ L = (6, 4, 8)
 
 CASES = {
     # case: (binary content, config overrides)
-    "fund": ("fund", {}),
-    "adj": ("adj", {}),
+    "fund": ("fund", {"measure_local": 1}),
+    "adj": ("adj", {"measure_local": 1}),
     "su2u1s": ("su2u1s", {}),
     "fund_muca": ("fund", {"multicanonical": 1, "muca_mode": 1, "bins": 20, "min": 0.0, "max": 0.6,
                            "iterations": 30, "interval": 10, "do_flow": 0}),
@@ -92,10 +96,10 @@ def run_ref(content, config, lattice, extra=None):
         if r.returncode != 0:
             raise RuntimeError(r.stdout[-2000:] + r.stderr[-2000:])
         out = {}
-        for name in ("labels", "measure", "measure_flow", "lattice", "weight"):
-            path = os.path.join(d, name)
-            if os.path.exists(path):
-                out[name] = open(path, "rb").read()
+        for name in sorted(os.listdir(d)):
+            if name in ("labels", "measure", "measure_flow", "lattice", "weight", "labels_local") or \
+                    name.startswith("measure_local_"):
+                out[name] = open(os.path.join(d, name), "rb").read()
         return out
     finally:
         shutil.rmtree(d)
@@ -114,6 +118,9 @@ def main():
             rec["measure_flow"] = np.frombuffer(got["measure_flow"], dtype=np.uint8)
         if "weight" in got:
             rec["weight"] = np.frombuffer(got["weight"], dtype=np.uint8)
+        for name, data in got.items():
+            if name == "labels_local" or name.startswith("measure_local_"):
+                rec[name] = np.frombuffer(data, dtype=np.uint8)
         got0 = run_ref(content, set_key(config, "iterations", 0), lat)
         rec["lattice_out0"] = np.frombuffer(got0["lattice"], dtype=np.uint8)
         np.savez_compressed(os.path.join(HERE, f"e2e_{case}.npz"), **rec)

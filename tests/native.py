@@ -67,6 +67,11 @@ def oracle_lib():
         lib.orc_flow_step.argtypes = [ctypes.c_void_p, ctypes.c_double]
         lib.orc_grad_flow.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                       ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+        # the handle is a 64-bit pointer: never let ctypes pass it as a C int
+        for name in ("orc_put_fields", "orc_get_fields"):
+            getattr(lib, name).argtypes = [ctypes.c_void_p] * 7
+        for name in ("orc_counters", "orc_measure", "orc_measure_local"):
+            getattr(lib, name).argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         _oracle = lib
     return _oracle
 
@@ -175,6 +180,11 @@ class Oracle:
         m = np.zeros(abi.NMEAS)
         self.lib.orc_measure(self.h, _P(m))
         return m
+
+    def measure_local(self):
+        out = np.zeros((self.p.sites(), 2))
+        self.lib.orc_measure_local(self.h, _P(out))
+        return out
 
     def muca_set(self, w):
         self.lib.orc_muca_set(self.h, ctypes.byref(w.struct))

@@ -6,8 +6,9 @@ they are deterministic.  Checked: the labels file byte for byte, the same
 number of columns and lines, every printed value within the stated tolerance
 of the reference's (FP64 path: 1e-6 relative -- six printed digits, so equal
 up to the rounding of the last printed digit; FP32 form: 1e-4 relative,
-1e-5 absolute), and the lattice file the run leaves behind is a valid
-checkpoint of the right size that bin/su2 reads back."""
+1e-5 absolute), the measure_local files of the flow (coordinates exact, the
+values within the same tolerances), and the lattice file the run leaves
+behind is a valid checkpoint of the right size that bin/su2 reads back."""
 import numpy as np
 import pytest
 
@@ -58,6 +59,20 @@ def test_first_measurement_and_flow_match_reference(binary, case, precision, rto
         same = sum(a == b for a, b in zip(got[0], want[0]))
         assert same >= len(want[0]) - 1, (got, want)
     compare_rows(rows(E.read(d, "measure_flow")), rows(g["measure_flow"]), rtol, atol)
+    # measure_local files of the flow (binary: 3 ints of coordinates, with the
+    # triplet Tr Sigma^2 and the charge as doubles, a newline byte per site)
+    local = sorted(k for k in g if k.startswith("measure_local_"))
+    if local:
+        assert E.read(d, "labels_local") == g["labels_local"]
+        has_t = g["content"] in ("adj", "fundadj")
+        dt = np.dtype([("c", "<i4", 3)] + ([("v", "<f8", 2)] if has_t else []) + [("nl", "u1")])
+        for name in local:
+            a = np.frombuffer(E.read(d, name), dtype=dt)
+            b = np.frombuffer(g[name], dtype=dt)
+            assert len(a) == len(b) and np.array_equal(a["c"], b["c"]) and np.all(a["nl"] == 10), name
+            if has_t:
+                assert np.allclose(a["v"][:, 0], b["v"][:, 0], rtol=rtol, atol=atol), name
+                assert np.max(np.abs(a["v"][:, 1] - b["v"][:, 1])) < (1e-9 if precision == 64 else 1e-3), name
     out = E.read(d, "lattice")
     assert len(out) == len(g["lattice_in"])
     assert out[:20] == g["lattice_in"][:20]
