@@ -215,6 +215,13 @@ int su2gpu_grad_flow(su2gpu_ctx* ctx, double t_max, double dt, int32_t meas_inte
  * magfield.c:262-280): out[2 i], out[2 i + 1] for site i, V x 2 doubles.
  * Triplet content only (the reference writes no values without it). */
 int su2gpu_measure_local(su2gpu_ctx* ctx, double* out);
+/* measure_along_z (z_coord.c:206-300): profiles along the "z direction", the
+ * longest direction with ties going to the last one (init_z_coord,
+ * z_coord.c:18-24), returned in *z_dir.  sums[4 z + q] for 0 <= z < L[z_dir]
+ * is the sum over the plane z of q = 0 phi^2 (first doublet), 1 Tr Sigma^2,
+ * 2 S, 3 S^2; columns of fields the content lacks are 0.  The reference's
+ * rows are these sums divided by the plane's area V / L[z_dir]. */
+int su2gpu_measure_z(su2gpu_ctx* ctx, int32_t* z_dir, double* sums);
 /* su2gpu_grad_flow that also returns measure_local of the flowed fields at
  * every measurement (gradflow.c:81-86, 124-129, 151-156): local holds
  * max_local blocks of V x 2 doubles, filled in measurement order. */

@@ -1284,6 +1284,30 @@ void orc_measure_local(const orc_ctx* c, double* out) {
   }
 }
 
+/* init_z_coord + measure_along_z (z_coord.c:18-24, 206-300): the longest
+ * direction (ties to the last), then per plane z the sums over its sites, in
+ * storage order, of phi^2 (first doublet), Tr Sigma^2, S, S^2 */
+void orc_measure_z(const orc_ctx* c, int* zdir_out, double* sums) {
+  int zd = c->D - 1;
+  for (int d = c->D - 1; d >= 0; d--)
+    if (c->p.L[d] > c->p.L[zd]) zd = d;
+  int Lz = c->p.L[zd];
+  for (long k = 0; k < 4L * Lz; k++) sums[k] = 0.0;
+  for (int z = 0; z < Lz; z++)
+    for (long i = 0; i < c->V; i++) {
+      if (c->coords[i * c->D + zd] != z) continue;
+      double* m = sums + 4 * z;
+      if (c->nh > 0) m[0] += doubletsq(PHI(c, 0, i));
+      if (c->has_trip) m[1] += tripletsq(TRP(c, i));
+      if (c->has_sing) {
+        double sv = c->sing[i];
+        m[2] += sv;
+        m[3] += sv * sv;
+      }
+    }
+  *zdir_out = zd;
+}
+
 void orc_measure(const orc_ctx* c, double* m) {
   for (int k = 0; k < SU2GPU_NMEAS; k++) m[k] = 0.0;
   for (long i = 0; i < c->V; i++) {

@@ -30,6 +30,7 @@ void orc_counters(const orc_ctx* c, int64_t* out);
 void orc_reset_counters(orc_ctx* c);
 void orc_measure(const orc_ctx* c, double* sums);
 void orc_measure_local(const orc_ctx* c, double* out);
+void orc_measure_z(const orc_ctx* c, int* zdir, double* sums);
 
 /* per-site kernels */
 void orc_wilson_staple(const orc_ctx* c, long i, int dir, double* V);

@@ -164,8 +164,11 @@ static void p_measure_local(const void* f, const Geom& g, const Coup& cp, double
                             cudaStream_t st) {
   k_measure_local<R><<<nblk(g.V, BLOCK), BLOCK, 0, st>>>(*(const Fields<R>*)f, g, coup_as<R>(cp), denom, out);
 }
+static void p_measure_z(const void* f, const Geom& g, int content, int zdir, double* out, cudaStream_t st) {
+  k_measure_z<R><<<g.L[zdir], ZBLOCK, 0, st>>>(*(const Fields<R>*)f, g, content, zdir, out);
+}
 const PrecOps SU2_WITH_PREC = {p_orderparam, p_restore, p_alpha, p_import, p_export, p_reunit, p_fixup,
-                               p_measure_local};
+                               p_measure_local, p_measure_z};
 #endif
 
 #ifdef SU2_WITH_GLOBAL

@@ -1209,6 +1209,49 @@ __global__ void __launch_bounds__(BLOCK) k_measure_local(Fields<R> f, Geom g, Co
   out[2 * (size_t)t + 1] = magcharge_site(f, g, cp, c, t, AlphaOnTheFly{}) / denom;
 }
 
+// measure_along_z (z_coord.c:206-300): sums over the plane z of phi^2 (first
+// doublet), Tr Sigma^2, S and S^2; one block per plane, the plane's sites
+// enumerated by the two other coordinates (lower direction fastest) and summed
+// in a fixed order.  out[z][4], columns of absent fields zero.
+constexpr int ZBLOCK = 256;
+template <typename R>
+__global__ void __launch_bounds__(ZBLOCK) k_measure_z(Fields<R> f, Geom g, int content, int zdir, double* out) {
+  const int z = blockIdx.x;
+  const int dlo = zdir == 0 ? 1 : 0, dhi = zdir == 2 ? 1 : 2;
+  const int La = g.L[dlo], area = g.V / g.L[zdir];
+  const bool h = content & (C_H1 | C_H2), tr = content & C_T, sg = content & C_S;
+  double m[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int k = threadIdx.x; k < area; k += ZBLOCK) {
+    int c[3];
+    c[zdir] = z;
+    c[dlo] = k % La;
+    c[dhi] = k / La;
+    int i = site_index(g, c[0], c[1], c[2]);
+    if (h) m[0] += (double)doubletsq(ld4<R>(f.phi[0], i));
+    if (tr) m[1] += (double)tripletsq(ld3(f, i));
+    if (sg) {
+      R s = f.sing[i];
+      m[2] += (double)s;
+      m[3] += (double)(s * s);
+    }
+  }
+  __shared__ double sm[ZBLOCK / 32][4];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    double v = m[q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sm[w][q] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    double v = 0.0;
+    for (int ww = 0; ww < ZBLOCK / 32; ww++) v += sm[ww][threadIdx.x];
+    out[4 * (size_t)z + threadIdx.x] = v;
+  }
+}
+
 // measure() (measure.c:110-233): the terms of site t (storage index) added to
 // m[NSUMS]; per-site quantities in R, sums in FP64
 template <typename R, int CC, typename AF>

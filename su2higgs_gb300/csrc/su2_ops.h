@@ -45,6 +45,8 @@ struct PrecOps {
                      cudaStream_t st);
   // per-site Tr Sigma^2 and magnetic charge / denom, out[2 V] (storage order)
   void (*measure_local)(const void* f, const Geom& g, const Coup& cp, double denom, double* out, cudaStream_t st);
+  // plane sums along direction zdir: out[L[zdir]][4] (phi^2, Tr Sigma^2, S, S^2)
+  void (*measure_z)(const void* f, const Geom& g, int content, int zdir, double* out, cudaStream_t st);
 };
 
 // instantiations (su2_inst.cu)

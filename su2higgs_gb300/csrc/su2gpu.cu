@@ -1129,6 +1129,23 @@ int su2gpu_grad_flow_local(su2gpu_ctx* c, double t_max, double dt, int32_t meas_
   return flow_impl<float>(c, c->f32, t_max, dt, meas_interval, rows, maxrows, nrows, local, max_local);
 }
 
+int su2gpu_measure_z(su2gpu_ctx* c, int32_t* z_dir, double* sums) {
+  if (!c || !sums) return SU2GPU_ERR_INVALID;
+  // init_z_coord (z_coord.c:18-24): the longest direction, ties to the last
+  int zd = 2;
+  for (int d = 2; d >= 0; d--)
+    if (c->g.L[d] > c->g.L[zd]) zd = d;
+  const int Lz = c->g.L[zd];
+  int rc = c->local.ensure((size_t)c->g.V * 2 * 8 > (size_t)Lz * 4 * 8 ? (size_t)c->g.V * 2 * 8 : (size_t)Lz * 4 * 8);
+  if (rc) return rc;
+  c->pops->measure_z(c->F(), c->g, c->cp.content, zd, (double*)c->local.p, c->st);
+  CKL();
+  CK(cudaMemcpyAsync(sums, c->local.p, (size_t)Lz * 4 * 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (z_dir) *z_dir = zd;
+  return SU2GPU_OK;
+}
+
 int su2gpu_measure_local(su2gpu_ctx* c, double* out) {
   if (!c || !out) return SU2GPU_ERR_INVALID;
   if (!c->has_t) {

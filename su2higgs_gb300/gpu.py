@@ -58,6 +58,7 @@ def lib():
         L.su2gpu_grad_flow_local.argtypes = [vp, ctypes.c_double, ctypes.c_double, i32, vp, i32, ctypes.POINTER(i32),
                                              vp, i32]
         L.su2gpu_measure_local.argtypes = [vp, vp]
+        L.su2gpu_measure_z.argtypes = [vp, ctypes.POINTER(i32), vp]
         L.su2gpu_update_lattice_host.argtypes = [vp, u32] + [vp] * 6
         L.su2gpu_stream_uniform.restype = ctypes.c_double
         L.su2gpu_stream_uniform.argtypes = [u64, u32, u32, u32, u32, u32]
@@ -249,6 +250,14 @@ class Lattice:
         out = np.zeros((self.V, 2))
         check(lib().su2gpu_measure_local(self._h, _p(out)))
         return out
+
+    def measure_z(self):
+        """measure_along_z (z_coord.c:206): (z direction, plane sums of
+        phi^2, Tr Sigma^2, S, S^2 for every z)."""
+        zd = ctypes.c_int32()
+        out = np.zeros((max(self.params.L[:3]), 4))
+        check(lib().su2gpu_measure_z(self._h, ctypes.byref(zd), _p(out)))
+        return zd.value, out[: self.params.L[zd.value]].copy()
 
     def grad_flow_local(self, t_max, dt, meas_interval, maxrows=None):
         """grad_flow plus measure_local of the flowed fields at every

@@ -100,17 +100,26 @@ static int opt_int(const char* fname, const char* label, int dflt) {
  * -DSINGLET, -DU1, -DGRADFLOW; default Makefile:12 = NHIGGS=1 SINGLET U1).
  * Here the optional keys nhiggs/triplet/singlet/u1/gradflow select it; the
  * environment variable SU2_CONTENT (a name: pure, fund, adj, su2u1s, fundadj,
- * higgs2, optionally +gradflow) is applied before them. */
+ * higgs2, optionally +gradflow and +measure_z) is applied before them. */
 static void read_content(const char* fname, host_params* hp) {
-  hp->nhiggs = 1; hp->triplet = 0; hp->singlet = 1; hp->u1 = 1; hp->gradflow = 0;
+  hp->nhiggs = 1; hp->triplet = 0; hp->singlet = 1; hp->u1 = 1; hp->gradflow = 0; hp->measure_z = 0;
   const char* env = getenv("SU2_CONTENT");
   if (env && *env) {
     char name[64];
     snprintf(name, sizeof(name), "%s", env);
+    /* modifiers after the name: +gradflow (-DGRADFLOW), +measure_z (-DMEASURE_Z) */
     char* plus = strchr(name, '+');
     if (plus) {
-      if (!strcasecmp(plus + 1, "gradflow")) hp->gradflow = 1;
       *plus = 0;
+      char* tok = plus + 1;
+      while (tok && *tok) {
+        char* next = strchr(tok, '+');
+        if (next) *next++ = 0;
+        if (!strcasecmp(tok, "gradflow")) hp->gradflow = 1;
+        else if (!strcasecmp(tok, "measure_z")) hp->measure_z = 1;
+        else { printf("!!! Unknown SU2_CONTENT modifier %s\n", tok); die(2); }
+        tok = next;
+      }
     }
     if (!strcasecmp(name, "pure")) { hp->nhiggs = 0; hp->triplet = 0; hp->singlet = 0; hp->u1 = 0; }
     else if (!strcasecmp(name, "fund")) { hp->nhiggs = 1; hp->triplet = 0; hp->singlet = 0; hp->u1 = 0; }
@@ -125,6 +134,7 @@ static void read_content(const char* fname, host_params* hp) {
   hp->singlet = opt_int(fname, "singlet", hp->singlet);
   hp->u1 = opt_int(fname, "u1", hp->u1);
   hp->gradflow = opt_int(fname, "gradflow", hp->gradflow);
+  hp->measure_z = opt_int(fname, "measure_z", hp->measure_z);
 }
 
 void read_parameters(const char* fname, host_params* hp) {
@@ -190,6 +200,7 @@ void read_parameters(const char* fname, host_params* hp) {
   hp->reset = cfg_get_int(f, "reset");
   hp->multicanonical = cfg_get_int(f, "multicanonical");
   hp->do_local_meas = cfg_get_int(f, "measure_local");
+  if (hp->measure_z) hp->meas_interval_z = cfg_get_long(f, "interval_z");
   p->update_links = cfg_get_int(f, "update_links");
   p->update_su2doublet = cfg_get_int(f, "update_doublet");
   p->scalar_sweeps = cfg_get_int(f, "scalar_sweeps");
@@ -242,6 +253,10 @@ void read_parameters(const char* fname, host_params* hp) {
     hp->flow_meas_interval = cfg_get_int(f, "flow_meas_interval");
     hp->flow_dt = cfg_get_double(f, "flow_dt");
     hp->flow_t_max = cfg_get_double(f, "flow_t_max");
+  }
+  if (hp->measure_z) {
+    hp->do_z_meas = cfg_get_int(f, "do_z_meas");
+    hp->setup_wall = cfg_get_int(f, "setup_wall");
   }
   fclose(f);
 

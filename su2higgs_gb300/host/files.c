@@ -186,6 +186,96 @@ int write_measure_local(const char* fname, const host_params* hp, const double* 
   return 0;
 }
 
+/* init_z_coord (z_coord.c:18-24): the longest direction, ties to the last */
+int z_direction(const host_params* hp) {
+  int zd = hp->p.dim - 1;
+  for (int d = hp->p.dim - 1; d >= 0; d--)
+    if (hp->p.L[d] > hp->p.L[zd]) zd = d;
+  return zd;
+}
+
+/* print_z_labels (z_coord.c:78-106) */
+void print_z_labels(const host_params* hp) {
+  FILE* f = fopen("labels_z", "w+");
+  if (!f) return;
+  int k = 1;
+  fprintf(f, "%d z\n", k); k++;
+  if (hp->nhiggs > 0) { fprintf(f, "%d phi^2\n", k); k++; }
+  if (hp->triplet) { fprintf(f, "%d Sigma^2\n", k); k++; }
+  if (hp->singlet) {
+    fprintf(f, "%d S\n", k); k++;
+    fprintf(f, "%d S^2\n", k); k++;
+  }
+  fclose(f);
+}
+
+/* the rows measure_along_z (z_coord.c:274-292) appends: z, then the plane
+ * averages of the quantities the content has */
+void write_measure_z(const host_params* hp, int zdir, const double* sums) {
+  FILE* f = fopen("measure_z", "a");
+  if (!f) return;
+  long Lz = hp->p.L[zdir];
+  double area = (double)(volume(hp) / Lz);
+  for (long z = 0; z < Lz; z++) {
+    fprintf(f, "%ld ", z);
+    const double* m = sums + 4 * z;
+    if (hp->nhiggs > 0) fprintf(f, "%g ", m[0] / area);
+    if (hp->triplet) fprintf(f, "%g ", m[1] / area);
+    if (hp->singlet) fprintf(f, "%g %g ", m[2] / area, m[3] / area);
+    fprintf(f, "\n");
+  }
+  fclose(f);
+}
+
+/* uniform deviates in [0, 1) for prepare_wall: splitmix64 (Steele, Lea &
+ * Flood, OOPSLA 2014), the top 53 bits */
+static double wall_uniform(uint64_t* s) {
+  uint64_t z = (*s += 0x9e3779b97f4a7c15ull);
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  z ^= z >> 31;
+  return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+void prepare_wall(const host_params* hp, double* const* arrays, uint64_t seed) {
+  const int* L = hp->p.L;
+  int zd = z_direction(hp);
+  long V = volume(hp), half = V / 2;
+  uint64_t st = seed ^ 0x5eed3a11ull;
+  for (long i = 0; i < V; i++) {
+    int parity = i >= half;
+    long t = i - parity * half;
+    long r = t / (L[0] / 2);
+    int k = (int)(t - r * (L[0] / 2));
+    int z = (int)(r / L[1]), y = (int)(r - (long)z * L[1]);
+    int c[3] = {2 * k + ((parity + y + z) & 1), y, z};
+    int small = c[zd] < 0.5 * L[zd];
+    for (int db = 0; db < hp->nhiggs; db++) {
+      double* phi = arrays[2 + db] + 4 * i;
+      double a = small ? 0.01 : 0.05;
+      phi[0] = (small ? 0.2 : 1.2) + a * wall_uniform(&st);
+      for (int q = 1; q < 4; q++) phi[q] = a * wall_uniform(&st);
+    }
+    if (hp->triplet) {
+      double* s3 = arrays[4] + 3 * i;
+      double a = small ? 0.05 : 0.01;
+      s3[0] = (small ? 1.5 : 0.2) + a * wall_uniform(&st);
+      s3[1] = a * wall_uniform(&st);
+      s3[2] = a * wall_uniform(&st);
+    }
+    if (hp->singlet) arrays[5][i] = (small ? 0.8 : 0.1) + 0.01 * wall_uniform(&st);
+    for (int dir = 0; dir < hp->p.dim; dir++) {
+      double u = 1.0 - (small ? 0.03 : 0.4) * wall_uniform(&st);
+      double* U = arrays[0] + 4 * (i * hp->p.dim + dir);
+      U[0] = u;
+      U[1] = sqrt(1.0 - u * u);
+      U[2] = 0.0;
+      U[3] = 0.0;
+    }
+  }
+  printf("Wall profile initialized.\n");
+}
+
 /* one measure() row from the volume sums (measure.c:182-307) */
 void write_measure_row(FILE* f, const host_params* hp, const double* m, const su2gpu_weight* w, int have_muca) {
   double weight = 0.0, muca_param = 0.0;

@@ -61,6 +61,7 @@ static int files_roundtrip(host_params* hp, host_muca* hm) {
       for (int64_t i = 0; i < V; i++) arrays[5][i] = hp->singlet0;
     hp->reset = 1;
   }
+  if (hp->measure_z && hp->do_z_meas) print_z_labels(hp);
   print_labels(hp);
   if (hp->do_local_meas) print_labels_local(hp, "labels_local");
   if (hp->multicanonical) {
@@ -146,8 +147,14 @@ int main(int argc, char** argv) {
       for (int64_t i = 0; i < V; i++) arrays[5][i] = hp.singlet0;
     hp.reset = 1;
   }
+  /* main.c:189-199: a phase-interface start overrides the field initialisation */
+  if (hp.measure_z && hp.reset && hp.setup_wall) prepare_wall(&hp, arrays, seed);
   GPU(su2gpu_upload_fields(ctx, arrays[0], arrays[1], arrays[2], arrays[3], arrays[4], arrays[5]));
 
+  if (hp.measure_z && hp.do_z_meas) {
+    print_z_labels(&hp);
+    printf("Measuring profiles along direction %d every %ld iterations\n", z_direction(&hp) + 1, hp.meas_interval_z);
+  }
   print_labels(&hp);
   if (hp.do_local_meas) print_labels_local(&hp, "labels_local");
 
@@ -209,6 +216,14 @@ int main(int argc, char** argv) {
       if (hp.multicanonical) GPU(su2gpu_muca_get(ctx, &w));
       write_measure_row(results, &hp, m, &w, hp.multicanonical);
     }
+    const int zmeas = hp.measure_z && hp.do_z_meas && hp.meas_interval_z > 0;
+    if (zmeas && iter % hp.meas_interval_z == 0) {
+      double* zs = (double*)malloc(sizeof(double) * 4 * (size_t)hp.p.L[z_direction(&hp)]);
+      int32_t zd = 0;
+      GPU(su2gpu_measure_z(ctx, &zd, zs));
+      write_measure_z(&hp, zd, zs);
+      free(zs);
+    }
     if (hp.gradflow && hp.do_flow && hp.flow_interval > 0 && iter % hp.flow_interval == 0) {
       int maxrows = (int)(hp.flow_t_max / hp.flow_dt) / (hp.flow_meas_interval > 0 ? hp.flow_meas_interval : 1) + 4;
       double* rows = (double*)malloc(sizeof(double) * maxrows * nmeas);
@@ -257,6 +272,7 @@ int main(int argc, char** argv) {
     long n = 1;
     while (iter + n <= hp.iterations && (hp.interval <= 0 || (iter + n) % hp.interval != 0) &&
            !(hp.gradflow && hp.do_flow && hp.flow_interval > 0 && (iter + n) % hp.flow_interval == 0) &&
+           !(zmeas && (iter + n) % hp.meas_interval_z == 0) &&
            (hp.checkpoint <= 0 || (iter + n - 1) % hp.checkpoint != 0) && n < 1000000)
       n++;
     GPU(su2gpu_run_sweeps(ctx, sweep, (int32_t)n, hp.use_graph));

@@ -24,6 +24,9 @@ typedef struct {
   /* gradient flow */
   int do_flow, flow_interval, flow_meas_interval;
   double flow_dt, flow_t_max;
+  /* profiles along z (the reference's -DMEASURE_Z build, z_coord.c) */
+  int measure_z, do_z_meas, setup_wall;
+  long meas_interval_z;
   /* additions of this implementation (optional keys) */
   uint64_t seed;
   int have_seed;
@@ -60,6 +63,14 @@ int load_lattice(const char* fname, const host_params* hp, long* iter, double* t
                  double** arrays);
 void print_labels(const host_params* hp);
 void print_labels_local(const host_params* hp, const char* fname);
+void print_z_labels(const host_params* hp);
+/* one measure_along_z block appended to measure_z from the plane sums
+ * sums[4 z + q] (q: phi^2, Tr Sigma^2, S, S^2) along direction zdir */
+void write_measure_z(const host_params* hp, int zdir, const double* sums);
+/* prepare_wall (z_coord.c:304-375): two phases split at the middle of the z
+ * direction, in the FP64 host arrays; seed drives the host's own stream */
+void prepare_wall(const host_params* hp, double* const* arrays, uint64_t seed);
+int z_direction(const host_params* hp);
 /* one measure_local file: per site in storage order its coordinates and, with
  * the triplet, (Tr Sigma^2, magnetic charge) from vals[2 V] */
 int write_measure_local(const char* fname, const host_params* hp, const double* vals);

@@ -9,7 +9,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 BIN = os.path.join(ROOT, "bin", "su2")
-CASES = ("fund", "adj", "su2u1s", "fund_muca")
+CASES = ("fund", "adj", "su2u1s", "fund_muca", "su2u1s_z", "fundadj_z")
 
 
 def ensure_binary():
@@ -23,12 +23,10 @@ def ensure_binary():
 
 
 def load_case(case):
-    """The golden run; "bin_content" is the field content to give bin/su2:
-    the reference binaries were built with -DGRADFLOW."""
+    """The golden run; "bin_content" is the field content to give bin/su2
+    (the -D flags the reference binary was built with)."""
     d = np.load(os.path.join(GOLDEN, f"e2e_{case}.npz"))
-    g = {k: (str(d[k]) if k == "content" else bytes(d[k])) for k in d.files}
-    g["bin_content"] = g["content"] + "+gradflow"
-    return g
+    return {k: (str(d[k]) if k in ("content", "bin_content") else bytes(d[k])) for k in d.files}
 
 
 def stage(case, tmpdir):

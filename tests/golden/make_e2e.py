@@ -21,6 +21,11 @@ directories and stores, per case, in e2e_<case>.npz:
                 compared)
   weight        (muca case) the weight file the reference wrote during a
                 multicanonical run (multicanonical.c:82-111)
+  labels_z, measure_z
+                (the _z cases, -DMEASURE_Z builds) the profile labels and the
+                first measure_along_z block, of the loaded configuration
+                (z_coord.c:78-300)
+  bin_content   the --content argument that makes bin/su2 the same program
 
 Run here, where the reference sources are: python tests/golden/make_e2e.py
 """
@@ -45,12 +50,18 @@ REF_BIN = os.path.join(ROOT, "oracle", "_ref")
 L = (6, 4, 8)
 
 CASES = {
-    # case: (binary content, config overrides)
-    "fund": ("fund", {"measure_local": 1}),
-    "adj": ("adj", {"measure_local": 1}),
-    "su2u1s": ("su2u1s", {}),
-    "fund_muca": ("fund", {"multicanonical": 1, "muca_mode": 1, "bins": 20, "min": 0.0, "max": 0.6,
-                           "iterations": 30, "interval": 10, "do_flow": 0}),
+    # case: (reference binary, field content, bin/su2 content, config overrides)
+    "fund": ("fund", "fund", "fund+gradflow", {"measure_local": 1}),
+    "adj": ("adj", "adj", "adj+gradflow", {"measure_local": 1}),
+    "su2u1s": ("su2u1s", "su2u1s", "su2u1s+gradflow", {}),
+    "fund_muca": ("fund", "fund", "fund+gradflow", {"multicanonical": 1, "muca_mode": 1, "bins": 20, "min": 0.0,
+                                                     "max": 0.6, "iterations": 30, "interval": 10, "do_flow": 0}),
+    # profiles along z (-DMEASURE_Z builds): the first measure_z block is of
+    # the loaded configuration, before any update (main.c:308-311)
+    "su2u1s_z": ("su2u1sz", "su2u1s", "su2u1s+measure_z", {"do_flow": 0, "do_z_meas": 1, "interval_z": 1,
+                                                          "setup_wall": 0}),
+    "fundadj_z": ("fundadjz", "fundadj", "fundadj+measure_z", {"do_flow": 0, "do_z_meas": 1, "interval_z": 1,
+                                                               "setup_wall": 0}),
 }
 
 
@@ -97,8 +108,8 @@ def run_ref(content, config, lattice, extra=None):
             raise RuntimeError(r.stdout[-2000:] + r.stderr[-2000:])
         out = {}
         for name in sorted(os.listdir(d)):
-            if name in ("labels", "measure", "measure_flow", "lattice", "weight", "labels_local") or \
-                    name.startswith("measure_local_"):
+            if name in ("labels", "measure", "measure_flow", "lattice", "weight", "labels_local", "labels_z",
+                        "measure_z") or name.startswith("measure_local_"):
                 out[name] = open(os.path.join(d, name), "rb").read()
         return out
     finally:
@@ -106,11 +117,12 @@ def run_ref(content, config, lattice, extra=None):
 
 
 def main():
-    for case, (content, over) in CASES.items():
+    for case, (binary, content, bin_content, over) in CASES.items():
         config = make_config(over)
         lat = lattice_bytes(content, 1000 + len(case))
-        got = run_ref(content, config, lat)
+        got = run_ref(binary, config, lat)
         rec = {"config": np.frombuffer(config.encode(), dtype=np.uint8), "content": np.array(content),
+               "bin_content": np.array(bin_content),
                "lattice_in": np.frombuffer(lat, dtype=np.uint8),
                "labels": np.frombuffer(got["labels"], dtype=np.uint8),
                "measure": np.frombuffer(got["measure"], dtype=np.uint8)}
@@ -119,9 +131,9 @@ def main():
         if "weight" in got:
             rec["weight"] = np.frombuffer(got["weight"], dtype=np.uint8)
         for name, data in got.items():
-            if name == "labels_local" or name.startswith("measure_local_"):
+            if name in ("labels_local", "labels_z", "measure_z") or name.startswith("measure_local_"):
                 rec[name] = np.frombuffer(data, dtype=np.uint8)
-        got0 = run_ref(content, set_key(config, "iterations", 0), lat)
+        got0 = run_ref(binary, set_key(config, "iterations", 0), lat)
         rec["lattice_out0"] = np.frombuffer(got0["lattice"], dtype=np.uint8)
         np.savez_compressed(os.path.join(HERE, f"e2e_{case}.npz"), **rec)
         print(case, {k: len(v) for k, v in got.items()})

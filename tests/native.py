@@ -72,6 +72,7 @@ def oracle_lib():
             getattr(lib, name).argtypes = [ctypes.c_void_p] * 7
         for name in ("orc_counters", "orc_measure", "orc_measure_local"):
             getattr(lib, name).argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        lib.orc_measure_z.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]
         _oracle = lib
     return _oracle
 
@@ -185,6 +186,12 @@ class Oracle:
         out = np.zeros((self.p.sites(), 2))
         self.lib.orc_measure_local(self.h, _P(out))
         return out
+
+    def measure_z(self):
+        zd = ctypes.c_int()
+        out = np.zeros((max(self.p.L[:3]), 4))
+        self.lib.orc_measure_z(self.h, ctypes.byref(zd), _P(out))
+        return zd.value, out[: self.p.L[zd.value]]
 
     def muca_set(self, w):
         self.lib.orc_muca_set(self.h, ctypes.byref(w.struct))

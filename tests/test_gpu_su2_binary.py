@@ -80,3 +80,18 @@ def test_first_measurement_and_flow_match_reference(binary, case, precision, rto
     E.run(d, g["bin_content"], "--files-only")
     again = E.read(d, "lattice")
     assert again[44:] == out[44:]
+
+
+@pytest.mark.parametrize("precision,rtol,atol", [(64, 1e-6, 1e-12), (32, 1e-4, 1e-5)])
+@pytest.mark.parametrize("case", ["su2u1s_z", "fundadj_z"])
+def test_first_z_profile_matches_reference(binary, case, precision, rtol, atol, tmp_path):
+    """Profiles along z (the reference's -DMEASURE_Z build): labels_z byte for
+    byte, and the first measure_z block -- plane averages of the loaded
+    configuration, taken before the first update -- value by value."""
+    d = str(tmp_path)
+    g = E.stage(case, d)
+    E.run(d, g["bin_content"], "--precision", str(precision), "--seed", "7")
+    assert E.read(d, "labels") == g["labels"]
+    assert E.read(d, "labels_z") == g["labels_z"]
+    compare_rows(rows(E.read(d, "measure")), rows(g["measure"]), rtol, atol)
+    compare_rows(rows(E.read(d, "measure_z")), rows(g["measure_z"]), rtol, atol)
