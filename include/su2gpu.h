@@ -267,6 +267,20 @@ int su2gpu_profile_sweep(su2gpu_ctx* ctx, uint32_t sweep, int32_t max_passes, in
 int su2gpu_autotune(su2gpu_ctx* ctx, int32_t* choices, float* best_ms);
 /* Set the launch-shape variants explicitly (choices[5], each in [0, 4)). */
 int su2gpu_set_variants(su2gpu_ctx* ctx, const int32_t* choices);
+/* The reference's random_sweeps mode (update.c:278-300, 338-344, used by the
+ * heatbath trajectories, hb_trajectory.c:16-21): every sweep updates the
+ * links in a random order of (direction, parity) and each scalar sweep starts
+ * with a random parity.  The order of sweep s is su2gpu_sweep_order(seed,
+ * chain, s, ...); sweeps in this mode are not replayed as a graph. */
+int su2gpu_set_random_sweeps(su2gpu_ctx* ctx, int32_t on);
+/* The order used in random_sweeps mode (a pure host computation): for each
+ * of update_links repetitions six (direction, parity) pairs, link_dirs[6 k +
+ * j] / link_pars[6 k + j], drawn as the reference does (two independent
+ * Fisher-Yates shuffles, update.c:461-468); scalar_first[s] (0 EVEN, 1 ODD)
+ * for s <= scalar_sweeps.  The random numbers are the order stream: Philox
+ * counter (0xfffffffe, draw >> 1, sweep, chain). */
+int su2gpu_sweep_order(uint64_t seed, uint32_t chain, uint32_t sweep, int32_t update_links, int32_t scalar_sweeps,
+                       int32_t* link_dirs, int32_t* link_pars, int32_t* scalar_first);
 /* Page-lock host memory for the host-buffer entry points. */
 int su2gpu_host_register(void* ptr, int64_t bytes);
 int su2gpu_host_unregister(void* ptr);

@@ -41,6 +41,7 @@ struct orc_ctx {
   uint64_t seed;
   uint32_t sweep, chain;
   int pass;
+  int random_sweeps;
   /* multicanonical */
   int muca_on;
   su2gpu_weight w;
@@ -1227,19 +1228,78 @@ static int sweep_scalar(orc_ctx* c, int par, int metro, int field, int h) {
   return accept;
 }
 
-/* update_lattice (update.c:270-430), non-random order */
+/* The order stream of the random_sweeps mode: 64-bit draws, draw k is half
+ * k & 1 of the Philox block (site 0xfffffffe, block k >> 1, sweep, chain). */
+typedef struct {
+  uint32_t key[2], sweep, chain, draw;
+} orc_order_stream;
+
+static uint64_t order_next(orc_order_stream* s) {
+  uint32_t ctr[4] = {0xfffffffeu, (s->draw >> 1) & 0xffffu, s->sweep, s->chain}, out[4];
+  orc_philox4x32_10(ctr, s->key, out);
+  uint64_t v = (s->draw & 1) ? (((uint64_t)out[2] << 32) | out[3]) : (((uint64_t)out[0] << 32) | out[1]);
+  s->draw++;
+  return v;
+}
+
+/* shuffle (update.c:461-468): Fisher-Yates from the top, j = iran() % (i+1) */
+static void shuffle_ints(orc_order_stream* s, int* a, int n) {
+  for (int i = n - 1; i > 0; i--) {
+    int j = (int)(order_next(s) % (uint64_t)(i + 1));
+    int t = a[i]; a[i] = a[j]; a[j] = t;
+  }
+}
+
+/* The pass order of update_lattice in random_sweeps mode (update.c:278-300,
+ * 338-344): per link repetition the parity array [E,O,E,O,..] and the
+ * direction array [0,0,1,1,..] shuffled independently, then per scalar sweep
+ * the parity updated first (EVEN when dran() < 0.5). */
+void orc_sweep_order(uint64_t seed, uint32_t chain, uint32_t sweep, int D, int update_links, int scalar_sweeps,
+                     int* dirs, int* pars, int* first) {
+  orc_order_stream s = {{(uint32_t)seed, (uint32_t)(seed >> 32)}, sweep, chain, 0};
+  for (int k = 0; k < update_links; k++) {
+    int* pa = pars + 2 * D * k;
+    int* da = dirs + 2 * D * k;
+    for (int j = 0; j < 2 * D; j++) { pa[j] = j % 2 ? ODD : EVEN; da[j] = j / 2; }
+    shuffle_ints(&s, pa, 2 * D);
+    shuffle_ints(&s, da, 2 * D);
+  }
+  for (int t = 0; t <= scalar_sweeps; t++) {
+    double u = (double)(order_next(&s) >> 11) * (1.0 / 9007199254740992.0);
+    first[t] = u < 0.5 ? EVEN : ODD;
+  }
+}
+
+void orc_set_random_sweeps(orc_ctx* c, int on) { c->random_sweeps = on ? 1 : 0; }
+
+/* update_lattice (update.c:270-430): the fixed order, or the random one */
 int orc_update_lattice(orc_ctx* c) {
   const su2gpu_params* p = &c->p;
+  int nl = p->update_links > 0 ? p->update_links : 0;
+  int* dirs = (int*)malloc(sizeof(int) * (2 * c->D * nl + 1));
+  int* pars = (int*)malloc(sizeof(int) * (2 * c->D * nl + 1));
+  int* first = (int*)malloc(sizeof(int) * (p->scalar_sweeps + 1));
+  if (c->random_sweeps) {
+    orc_sweep_order(c->seed, c->chain, c->sweep, c->D, nl, p->scalar_sweeps, dirs, pars, first);
+  } else {
+    for (int k = 0; k < nl; k++)
+      for (int j = 0; j < 2 * c->D; j++) {
+        pars[2 * c->D * k + j] = j % 2 ? ODD : EVEN;
+        dirs[2 * c->D * k + j] = j / 2;
+      }
+    for (int t = 0; t <= p->scalar_sweeps; t++) first[t] = EVEN;
+  }
   c->pass = 0;
-  for (int k = 0; k < p->update_links; k++) {
-    for (int mu = 0; mu < c->D; mu++)
-      for (int par = 0; par <= 1; par++) { sweep_links(c, par, mu, p->algorithm_su2link); c->pass++; }
+  for (int k = 0; k < nl; k++) {
+    const int* pa = pars + 2 * c->D * k;
+    const int* da = dirs + 2 * c->D * k;
+    for (int j = 0; j < 2 * c->D; j++) { sweep_links(c, pa[j], da[j], p->algorithm_su2link); c->pass++; }
     if (c->has_u1)
-      for (int mu = 0; mu < c->D; mu++)
-        for (int par = 0; par <= 1; par++) { sweep_u1(c, par, mu); c->pass++; }
+      for (int j = 0; j < 2 * c->D; j++) { sweep_u1(c, pa[j], da[j]); c->pass++; }
   }
   int nsweeps = p->scalar_sweeps + 1;
   for (int s = 0; s < nsweeps; s++) {
+    const int pr[2] = {first[s], first[s] == EVEN ? ODD : EVEN};
     if (c->nh > 0)
       for (int k = 0; k < p->update_su2doublet; k++) {
         int force = 0;
@@ -1248,7 +1308,7 @@ int orc_update_lattice(orc_ctx* c) {
           else continue;
         }
         for (int h = 0; h < c->nh; h++)
-          for (int par = 0; par <= 1; par++) { sweep_scalar(c, par, force, 0, h); c->pass++; }
+          for (int j = 0; j <= 1; j++) { sweep_scalar(c, pr[j], force, 0, h); c->pass++; }
       }
     if (c->has_trip)
       for (int k = 0; k < p->update_su2triplet; k++) {
@@ -1257,7 +1317,7 @@ int orc_update_lattice(orc_ctx* c) {
           if (p->algorithm_su2triplet == SU2GPU_OVERRELAX) force = 1;
           else continue;
         }
-        for (int par = 0; par <= 1; par++) { sweep_scalar(c, par, force, 1, 0); c->pass++; }
+        for (int j = 0; j <= 1; j++) { sweep_scalar(c, pr[j], force, 1, 0); c->pass++; }
       }
     if (c->has_sing)
       for (int k = 0; k < p->update_singlet; k++) {
@@ -1266,9 +1326,12 @@ int orc_update_lattice(orc_ctx* c) {
           if (p->algorithm_singlet == SU2GPU_OVERRELAX) force = 1;
           else continue;
         }
-        for (int par = 0; par <= 1; par++) { sweep_scalar(c, par, force, 2, 0); c->pass++; }
+        for (int j = 0; j <= 1; j++) { sweep_scalar(c, pr[j], force, 2, 0); c->pass++; }
       }
   }
+  free(dirs);
+  free(pars);
+  free(first);
   return c->pass;
 }
 

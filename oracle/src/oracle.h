@@ -26,6 +26,9 @@ void orc_get_fields(const orc_ctx* c, double* link, double* u1, double* d0, doub
                     double* sing);
 void orc_set_rng(orc_ctx* c, uint64_t seed, uint32_t sweep, uint32_t chain);
 int orc_update_lattice(orc_ctx* c);
+void orc_set_random_sweeps(orc_ctx* c, int on);
+void orc_sweep_order(uint64_t seed, uint32_t chain, uint32_t sweep, int D, int update_links, int scalar_sweeps,
+                     int* dirs, int* pars, int* first);
 void orc_counters(const orc_ctx* c, int64_t* out);
 void orc_reset_counters(orc_ctx* c);
 void orc_measure(const orc_ctx* c, double* sums);

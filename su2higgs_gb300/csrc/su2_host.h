@@ -66,6 +66,49 @@ inline void* host_device_view(const void* p, size_t bytes) {
   return a0.devicePointer;
 }
 
+// Sweep order of the reference's random_sweeps mode (update.c:278-300,
+// 338-344): per update_links repetition two independent Fisher-Yates
+// shuffles (shuffle, update.c:461-468) of the parity array [E,O,E,O,E,O] and
+// of the direction array [0,0,1,1,2,2] -- so a (direction, parity) pair may
+// repeat and another be skipped, as there -- then per scalar sweep the parity
+// updated first, EVEN when the uniform is below 0.5.  The random numbers come
+// from the order stream: Philox with counter (ORDER_SITE, block, sweep, chain),
+// 64-bit draw k = half k&1 of block k>>1; iran() is the draw itself, dran()
+// its top 53 bits.
+constexpr uint32_t ORDER_SITE = 0xfffffffeu;
+inline void sweep_order(uint64_t seed, uint32_t chain, uint32_t sweep, int update_links, int scalar_sweeps,
+                        int32_t* link_dirs, int32_t* link_pars, int32_t* scalar_first) {
+  uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  uint32_t draw = 0;
+  auto next64 = [&]() -> uint64_t {
+    uint32_t b = draw >> 1, h = draw & 1;
+    draw++;
+    uint32_t c0 = ORDER_SITE, c1 = b & 0xffffu, c2 = sweep, c3 = chain;
+    philox4x32_10(c0, c1, c2, c3, k0, k1);
+    return h ? (((uint64_t)c2 << 32) | c3) : (((uint64_t)c0 << 32) | c1);
+  };
+  for (int k = 0; k < update_links; k++) {
+    int32_t* par = link_pars + 6 * k;
+    int32_t* dir = link_dirs + 6 * k;
+    for (int j = 0; j < 6; j++) {
+      par[j] = j & 1;
+      dir[j] = j >> 1;
+    }
+    for (int i = 5; i > 0; i--) {
+      int j = (int)(next64() % (uint64_t)(i + 1));
+      int t = par[i]; par[i] = par[j]; par[j] = t;
+    }
+    for (int i = 5; i > 0; i--) {
+      int j = (int)(next64() % (uint64_t)(i + 1));
+      int t = dir[i]; dir[i] = dir[j]; dir[j] = t;
+    }
+  }
+  for (int s = 0; s <= scalar_sweeps; s++) {
+    double u = (double)(next64() >> 11) * (1.0 / 9007199254740992.0);
+    scalar_first[s] = u < 0.5 ? 0 : 1;
+  }
+}
+
 SU2_HIDDEN Coup make_coup(const su2gpu_params* p);
 SU2_HIDDEN const Ops* pick_ops(int prec, int content);
 

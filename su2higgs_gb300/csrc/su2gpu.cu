@@ -118,6 +118,7 @@ struct su2gpu_ctx {
   unsigned long long* d_fz = nullptr;
   int64_t host_tot[SU2GPU_NCOUNTERS] = {0};
   int var[5] = {0, 0, 0, 0, 0};  // launch-shape variant per kernel kind (link, U(1), doublet, triplet, singlet)
+  int random_sweeps = 0;         // the reference's random_sweeps mode: the order changes every sweep
   uint64_t seed = 0;
   uint32_t chain = 0;
   // multicanonical
@@ -497,8 +498,20 @@ static int scalar_pass(su2gpu_ctx* c, const PassArgs& base, int field, int h, in
   return SU2GPU_OK;
 }
 
-static int enqueue_sweep(su2gpu_ctx* c, int64_t* tot) {
+static int enqueue_sweep(su2gpu_ctx* c, int64_t* tot, uint32_t host_sweep) {
   const su2gpu_params& p = c->p;
+  // pass order: the fixed one, or in random_sweeps mode the one drawn for
+  // this sweep (sweep_order)
+  std::vector<int32_t> ldir(6 * (size_t)p.update_links), lpar(6 * (size_t)p.update_links),
+      sfirst((size_t)p.scalar_sweeps + 1);
+  if (c->random_sweeps) {
+    sweep_order(c->seed, c->chain, host_sweep, p.update_links, p.scalar_sweeps, ldir.data(), lpar.data(),
+                sfirst.data());
+  } else {
+    for (int k = 0; k < p.update_links; k++)
+      for (int j = 0; j < 6; j++) { ldir[6 * k + j] = j >> 1; lpar[6 * k + j] = j & 1; }
+    for (int s = 0; s <= p.scalar_sweeps; s++) sfirst[s] = 0;
+  }
   c->launches = 0;
   const int64_t N = c->g.half;
   PassArgs base;
@@ -512,30 +525,30 @@ static int enqueue_sweep(su2gpu_ctx* c, int64_t* tot) {
   uint32_t pass = 0;
   int rc;
   for (int k = 0; k < p.update_links; k++) {
-    for (int mu = 0; mu < 3; mu++)
-      for (int par = 0; par <= 1; par++) {
+    for (int j = 0; j < 6; j++) {
+      PassArgs a = base;
+      a.parity = lpar[6 * k + j]; a.sub = ldir[6 * k + j]; a.alg = p.algorithm_su2link; a.pass = pass++;
+      a.t_lo = 0; a.t_hi = N;
+      mark(c, 0);
+      c->ops->link(c->var[0], c->F(), a, c->st);
+      c->launches++;
+      CKL();
+      tot[SU2GPU_C_TOTAL_SU2LINK] += N;
+    }
+    if (c->has_u1)
+      for (int j = 0; j < 6; j++) {
         PassArgs a = base;
-        a.parity = par; a.sub = mu; a.alg = p.algorithm_su2link; a.pass = pass++; a.t_lo = 0; a.t_hi = N;
-        mark(c, 0);
-        c->ops->link(c->var[0], c->F(), a, c->st);
+        a.parity = lpar[6 * k + j]; a.sub = ldir[6 * k + j]; a.pass = pass++; a.t_lo = 0; a.t_hi = N;
+        mark(c, 1);
+        c->ops->u1(c->var[1], c->F(), a, c->st);
         c->launches++;
         CKL();
-        tot[SU2GPU_C_TOTAL_SU2LINK] += N;
+        tot[SU2GPU_C_TOTAL_U1LINK] += N;
       }
-    if (c->has_u1)
-      for (int mu = 0; mu < 3; mu++)
-        for (int par = 0; par <= 1; par++) {
-          PassArgs a = base;
-          a.parity = par; a.sub = mu; a.pass = pass++; a.t_lo = 0; a.t_hi = N;
-          mark(c, 1);
-          c->ops->u1(c->var[1], c->F(), a, c->st);
-          c->launches++;
-          CKL();
-          tot[SU2GPU_C_TOTAL_U1LINK] += N;
-        }
   }
   int nsweeps = p.scalar_sweeps + 1;
   for (int s = 0; s < nsweeps; s++) {
+    const int p0 = sfirst[s], pr[2] = {p0, 1 - p0};
     if (c->nh > 0)
       for (int k = 0; k < p.update_su2doublet; k++) {
         int force = 0;
@@ -544,8 +557,8 @@ static int enqueue_sweep(su2gpu_ctx* c, int64_t* tot) {
           else continue;
         }
         for (int h = 0; h < c->nh; h++)
-          for (int par = 0; par <= 1; par++)
-            if ((rc = scalar_pass(c, base, 0, h, par, force, pass++, tot))) return rc;
+          for (int j = 0; j <= 1; j++)
+            if ((rc = scalar_pass(c, base, 0, h, pr[j], force, pass++, tot))) return rc;
       }
     if (c->has_t)
       for (int k = 0; k < p.update_su2triplet; k++) {
@@ -554,8 +567,8 @@ static int enqueue_sweep(su2gpu_ctx* c, int64_t* tot) {
           if (p.algorithm_su2triplet == SU2GPU_OVERRELAX) force = 1;
           else continue;
         }
-        for (int par = 0; par <= 1; par++)
-          if ((rc = scalar_pass(c, base, 1, 0, par, force, pass++, tot))) return rc;
+        for (int j = 0; j <= 1; j++)
+          if ((rc = scalar_pass(c, base, 1, 0, pr[j], force, pass++, tot))) return rc;
       }
     if (c->has_s)
       for (int k = 0; k < p.update_singlet; k++) {
@@ -564,8 +577,8 @@ static int enqueue_sweep(su2gpu_ctx* c, int64_t* tot) {
           if (p.algorithm_singlet == SU2GPU_OVERRELAX) force = 1;
           else continue;
         }
-        for (int par = 0; par <= 1; par++)
-          if ((rc = scalar_pass(c, base, 2, 0, par, force, pass++, tot))) return rc;
+        for (int j = 0; j <= 1; j++)
+          if ((rc = scalar_pass(c, base, 2, 0, pr[j], force, pass++, tot))) return rc;
       }
   }
   // FP32: links are re-normalised where they are written (heatbath and
@@ -589,7 +602,7 @@ int su2gpu_update_lattice(su2gpu_ctx* c, uint32_t sweep) {
   if (!c) return SU2GPU_ERR_INVALID;
   k_set_u32<<<1, 1, 0, c->st>>>(c->d_sweep, sweep);
   CKL();
-  int rc = enqueue_sweep(c, c->host_tot);
+  int rc = enqueue_sweep(c, c->host_tot, sweep);
   if (rc) return rc;
   CK(cudaStreamSynchronize(c->st));
   return SU2GPU_OK;
@@ -598,7 +611,7 @@ int su2gpu_update_lattice(su2gpu_ctx* c, uint32_t sweep) {
 static int enqueue_sweeps(su2gpu_ctx* c, uint32_t first_sweep, int32_t nsweeps, int32_t use_graph) {
   k_set_u32<<<1, 1, 0, c->st>>>(c->d_sweep, first_sweep);
   CKL();
-  if (use_graph) {
+  if (use_graph && !c->random_sweeps) {  // a random order differs every sweep: no replay
     if (!c->gexec) {
       int64_t tot[SU2GPU_NCOUNTERS] = {0};
       cudaGraph_t graph;
@@ -606,7 +619,7 @@ static int enqueue_sweeps(su2gpu_ctx* c, uint32_t first_sweep, int32_t nsweeps, 
       CK(cudaStreamSynchronize(exec));
       c->st = c->own_st;
       CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
-      int rc = enqueue_sweep(c, tot);
+      int rc = enqueue_sweep(c, tot, first_sweep);
       k_inc_u32<<<1, 1, 0, c->st>>>(c->d_sweep);
       cudaError_t e = cudaStreamEndCapture(c->st, &graph);
       c->st = exec;
@@ -624,7 +637,7 @@ static int enqueue_sweeps(su2gpu_ctx* c, uint32_t first_sweep, int32_t nsweeps, 
     }
   } else {
     for (int s = 0; s < nsweeps; s++) {
-      int rc = enqueue_sweep(c, c->host_tot);
+      int rc = enqueue_sweep(c, c->host_tot, first_sweep + (uint32_t)s);
       if (rc) return rc;
       k_inc_u32<<<1, 1, 0, c->st>>>(c->d_sweep);
       CKL();
@@ -646,6 +659,21 @@ int su2gpu_enqueue_sweeps(su2gpu_ctx* c, uint32_t first_sweep, int32_t nsweeps, 
   return enqueue_sweeps(c, first_sweep, nsweeps, use_graph);
 }
 
+int su2gpu_set_random_sweeps(su2gpu_ctx* c, int32_t on) {
+  if (!c) return SU2GPU_ERR_INVALID;
+  c->random_sweeps = on ? 1 : 0;
+  if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
+  return SU2GPU_OK;
+}
+
+int su2gpu_sweep_order(uint64_t seed, uint32_t chain, uint32_t sweep, int32_t update_links, int32_t scalar_sweeps,
+                       int32_t* link_dirs, int32_t* link_pars, int32_t* scalar_first) {
+  if (update_links < 0 || scalar_sweeps < 0 || (update_links && (!link_dirs || !link_pars)) || !scalar_first)
+    return SU2GPU_ERR_INVALID;
+  sweep_order(seed, chain, sweep, update_links, scalar_sweeps, link_dirs, link_pars, scalar_first);
+  return SU2GPU_OK;
+}
+
 int su2gpu_set_stream(su2gpu_ctx* c, void* stream) {
   if (!c) return SU2GPU_ERR_INVALID;
   CK(cudaStreamSynchronize(c->st));
@@ -663,7 +691,7 @@ int su2gpu_launches_per_sweep(su2gpu_ctx* c, int32_t* n) {
   CK(cudaStreamSynchronize(exec));
   c->st = c->own_st;
   CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
-  int rc = enqueue_sweep(c, tot);
+  int rc = enqueue_sweep(c, tot, 0);
   cudaError_t e = cudaStreamEndCapture(c->st, &graph);
   c->st = exec;
   if (rc) return rc;
@@ -684,7 +712,7 @@ int su2gpu_profile_sweep(su2gpu_ctx* c, uint32_t sweep, int32_t maxp, int32_t* k
   k_set_u32<<<1, 1, 0, c->st>>>(c->d_sweep, sweep);
   c->prof = &ev;
   c->prof_kind = &kd;
-  int rc = enqueue_sweep(c, c->host_tot);
+  int rc = enqueue_sweep(c, c->host_tot, sweep);
   c->prof = nullptr;
   c->prof_kind = nullptr;
   if (rc) return rc;

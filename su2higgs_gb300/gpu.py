@@ -64,6 +64,8 @@ def lib():
         L.su2gpu_stream_uniform.argtypes = [u64, u32, u32, u32, u32, u32]
         L.su2gpu_device_info.argtypes = [ctypes.POINTER(ctypes.c_int)] * 3 + [ctypes.POINTER(i64)]
         L.su2gpu_set_stream.argtypes = [vp, vp]
+        L.su2gpu_set_random_sweeps.argtypes = [vp, i32]
+        L.su2gpu_sweep_order.argtypes = [u64, u32, u32, i32, i32, vp, vp, vp]
         L.su2gpu_enqueue_sweeps.argtypes = [vp, u32, i32, i32]
         L.su2gpu_enqueue_measure.argtypes = [vp, vp]
         L.su2gpu_launches_per_sweep.argtypes = [vp, ctypes.POINTER(i32)]
@@ -176,6 +178,11 @@ class Lattice:
 
     def update_lattice(self, sweep):
         check(lib().su2gpu_update_lattice(self._h, sweep))
+
+    def set_random_sweeps(self, on=True):
+        """The reference's random_sweeps mode: the pass order of every sweep
+        drawn from the order stream (sweep_order)."""
+        check(lib().su2gpu_set_random_sweeps(self._h, 1 if on else 0))
 
     def run_sweeps(self, first_sweep, n, graph=True):
         check(lib().su2gpu_run_sweeps(self._h, first_sweep, n, 1 if graph else 0))
@@ -303,6 +310,17 @@ class Lattice:
 def stream_uniform(seed, site, pass_, draw, sweep, chain=0):
     """The uniform the kernels draw (host evaluation of the Philox stream)."""
     return lib().su2gpu_stream_uniform(seed, site, pass_, draw, sweep, chain)
+
+
+def sweep_order(seed, chain, sweep, update_links=1, scalar_sweeps=4):
+    """Pass order of `sweep` in random_sweeps mode: (link_dirs, link_pars)
+    as (update_links, 6) arrays and the parity each scalar sweep starts
+    with (scalar_sweeps + 1 entries, 0 EVEN)."""
+    d = np.zeros((max(update_links, 1), 6), np.int32)
+    q = np.zeros((max(update_links, 1), 6), np.int32)
+    f = np.zeros(scalar_sweeps + 1, np.int32)
+    check(lib().su2gpu_sweep_order(seed, chain, sweep, update_links, scalar_sweeps, _p(d), _p(q), _p(f)))
+    return d[:update_links], q[:update_links], f
 
 
 def host_register(arr):

@@ -73,6 +73,9 @@ def oracle_lib():
         for name in ("orc_counters", "orc_measure", "orc_measure_local"):
             getattr(lib, name).argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         lib.orc_measure_z.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]
+        lib.orc_set_random_sweeps.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        lib.orc_sweep_order.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         _oracle = lib
     return _oracle
 
@@ -168,6 +171,9 @@ class Oracle:
 
     def set_rng(self, seed, sweep, chain=0):
         self.lib.orc_set_rng(self.h, seed, sweep, chain)
+
+    def set_random_sweeps(self, on=True):
+        self.lib.orc_set_random_sweeps(self.h, 1 if on else 0)
 
     def update(self):
         return self.lib.orc_update_lattice(self.h)
@@ -507,3 +513,13 @@ def rel_err(a, b, floor=1e-300):
     b = np.asarray(b, dtype=np.float64)
     den = np.maximum(np.maximum(np.abs(a), np.abs(b)), floor)
     return float(np.max(np.abs(a - b) / den)) if a.size else 0.0
+
+
+def oracle_sweep_order(seed, chain, sweep, update_links=1, scalar_sweeps=4, D=3):
+    """The oracle's pass order of `sweep` in random_sweeps mode."""
+    lib = oracle_lib()
+    d = np.zeros((max(update_links, 1), 2 * D), np.int32)
+    q = np.zeros((max(update_links, 1), 2 * D), np.int32)
+    f = np.zeros(scalar_sweeps + 1, np.int32)
+    lib.orc_sweep_order(seed, chain, sweep, D, update_links, scalar_sweeps, _P(d), _P(q), _P(f))
+    return d[:update_links], q[:update_links], f
