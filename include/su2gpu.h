@@ -267,6 +267,14 @@ int su2gpu_profile_sweep(su2gpu_ctx* ctx, uint32_t sweep, int32_t max_passes, in
 int su2gpu_autotune(su2gpu_ctx* ctx, int32_t* choices, float* best_ms);
 /* Set the launch-shape variants explicitly (choices[5], each in [0, 4)). */
 int su2gpu_set_variants(su2gpu_ctx* ctx, const int32_t* choices);
+/* A second context with the same parameters and a device copy of ctx's
+ * fields (alloc_fields + copy_fields of the heatbath trajectories,
+ * hb_trajectory.c:26-29), seeded (seed, chain); no weight, fixed sweep
+ * order. */
+int su2gpu_clone(su2gpu_ctx* ctx, uint64_t seed, uint32_t chain, su2gpu_ctx** out);
+/* Device-to-device copy of src's fields into dst (copy_fields,
+ * hb_trajectory.c:61); both have the same lattice, content and precision. */
+int su2gpu_copy_fields(su2gpu_ctx* dst, su2gpu_ctx* src);
 /* The reference's random_sweeps mode (update.c:278-300, 338-344, used by the
  * heatbath trajectories, hb_trajectory.c:16-21): every sweep updates the
  * links in a random order of (direction, parity) and each scalar sweep starts

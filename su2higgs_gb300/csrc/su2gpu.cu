@@ -666,6 +666,26 @@ int su2gpu_set_random_sweeps(su2gpu_ctx* c, int32_t on) {
   return SU2GPU_OK;
 }
 
+int su2gpu_clone(su2gpu_ctx* src, uint64_t seed, uint32_t chain, su2gpu_ctx** out) {
+  if (!src || !out) return SU2GPU_ERR_INVALID;
+  CK(cudaStreamSynchronize(src->st));
+  return su2gpu_create_copy(&src->p, src->fields.p, seed, chain, out);
+}
+
+int su2gpu_copy_fields(su2gpu_ctx* dst, su2gpu_ctx* src) {
+  if (!dst || !src) return SU2GPU_ERR_INVALID;
+  if (dst == src) return SU2GPU_OK;
+  if (dst->prec != src->prec || dst->p.content != src->p.content || dst->fields.n != src->fields.n ||
+      dst->p.L[0] != src->p.L[0] || dst->p.L[1] != src->p.L[1] || dst->p.L[2] != src->p.L[2]) {
+    set_err("su2gpu_copy_fields: the contexts differ in lattice, content or precision");
+    return SU2GPU_ERR_INVALID;
+  }
+  CK(cudaStreamSynchronize(src->st));
+  CK(cudaMemcpyAsync(dst->fields.p, src->fields.p, dst->fields.n, cudaMemcpyDeviceToDevice, dst->st));
+  CK(cudaStreamSynchronize(dst->st));
+  return SU2GPU_OK;
+}
+
 int su2gpu_sweep_order(uint64_t seed, uint32_t chain, uint32_t sweep, int32_t update_links, int32_t scalar_sweeps,
                        int32_t* link_dirs, int32_t* link_pars, int32_t* scalar_first) {
   if (update_links < 0 || scalar_sweeps < 0 || (update_links && (!link_dirs || !link_pars)) || !scalar_first)

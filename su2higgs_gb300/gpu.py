@@ -65,6 +65,8 @@ def lib():
         L.su2gpu_device_info.argtypes = [ctypes.POINTER(ctypes.c_int)] * 3 + [ctypes.POINTER(i64)]
         L.su2gpu_set_stream.argtypes = [vp, vp]
         L.su2gpu_set_random_sweeps.argtypes = [vp, i32]
+        L.su2gpu_clone.argtypes = [vp, u64, u32, ctypes.POINTER(vp)]
+        L.su2gpu_copy_fields.argtypes = [vp, vp]
         L.su2gpu_sweep_order.argtypes = [u64, u32, u32, i32, i32, vp, vp, vp]
         L.su2gpu_enqueue_sweeps.argtypes = [vp, u32, i32, i32]
         L.su2gpu_enqueue_measure.argtypes = [vp, vp]
@@ -178,6 +180,17 @@ class Lattice:
 
     def update_lattice(self, sweep):
         check(lib().su2gpu_update_lattice(self._h, sweep))
+
+    def clone(self, seed, chain=0):
+        """A new chain with a device copy of this one's fields."""
+        h = ctypes.c_void_p()
+        check(lib().su2gpu_clone(self._h, seed, chain, ctypes.byref(h)))
+        return Lattice(self.params, _handle=h)
+
+    def copy_fields_from(self, other):
+        """Device copy of `other`'s fields into this chain (same lattice,
+        content and precision)."""
+        check(lib().su2gpu_copy_fields(self._h, other._h))
 
     def set_random_sweeps(self, on=True):
         """The reference's random_sweeps mode: the pass order of every sweep

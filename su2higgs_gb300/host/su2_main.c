@@ -10,7 +10,9 @@
  * Same config keys, same outputs (labels, measure, measure_flow, lattice,
  * weight) and the same iteration structure as main.c:10-421: thermalise with
  * the weight read-only after a reset, then per iteration measure (every
- * `interval`), flow (every `flow_interval`), update, checkpoint.  All field
+ * `interval`), flow (every `flow_interval`), heatbath trajectories (every
+ * `mode_interval` of realtime_config, -DHB_TRAJECTORY builds: content
+ * modifier +hb_trajectory), update, checkpoint.  All field
  * updates, measurements and flows run on the GPU through libsu2gpu; runs of
  * iterations without host work in between are replayed as one CUDA graph.
  */
@@ -170,6 +172,22 @@ int main(int argc, char** argv) {
     GPU(su2gpu_muca_get(ctx, &w));
     if (w.mode == SU2GPU_MUCA_READONLY) printf("Read-only run, will not modify weight. \n");
   }
+  /* main.c:223-240 */
+  host_traj traj;
+  memset(&traj, 0, sizeof(traj));
+  const int dotraj = hp.hb_trajectory && hp.do_trajectory;
+  if (dotraj) {
+    printf("\nReal time simulation: reading file \"realtime_config\"\n");
+    read_realtime_config("realtime_config", &traj);
+    print_realtime_params(&hp, &traj);
+    if (!hp.multicanonical) {
+      printf("\nError: Need multicanonical for heatbath trajectories!! Exiting...\n");
+      die(-44);
+    }
+    FILE* tf = fopen("trajectory", "a");
+    fprintf(tf, "===== Realtime trajectories: min=%g, max=%g, n_traj=%d ===== \n", traj.min, traj.max, traj.n_traj);
+    fclose(tf);
+  }
   if (hp.gradflow && hp.do_flow) {
     printf("\n----- Gradient flow every %d iterations -----\n", hp.flow_interval);
     printf("dt %lf\tt_max %lf\t\tmeas_interval %d \n", hp.flow_dt, hp.flow_t_max, hp.flow_meas_interval);
@@ -208,6 +226,7 @@ int main(int argc, char** argv) {
   comms_time = 0.0;
   double tstart = wall();
   int flow_id = 1;
+  int traj_id = 1;
   int nmeas = 1 + SU2GPU_NMEAS;
   while (iter <= hp.iterations) {
     if (hp.interval > 0 && iter % hp.interval == 0) {
@@ -268,11 +287,17 @@ int main(int argc, char** argv) {
       free(rows);
       flow_id++;
     }
+    if (dotraj && iter % traj.mode_interval == 0) {
+      GPU(su2gpu_muca_get(ctx, &w));
+      GPU(make_realtime_trajectories(ctx, &hp, &w, &traj, traj_id, seed, NULL));
+      traj_id++;
+    }
     /* iterations up to the next host event run back to back */
     long n = 1;
     while (iter + n <= hp.iterations && (hp.interval <= 0 || (iter + n) % hp.interval != 0) &&
            !(hp.gradflow && hp.do_flow && hp.flow_interval > 0 && (iter + n) % hp.flow_interval == 0) &&
            !(zmeas && (iter + n) % hp.meas_interval_z == 0) &&
+           !(dotraj && (iter + n) % traj.mode_interval == 0) &&
            (hp.checkpoint <= 0 || (iter + n - 1) % hp.checkpoint != 0) && n < 1000000)
       n++;
     GPU(su2gpu_run_sweeps(ctx, sweep, (int32_t)n, hp.use_graph));

@@ -27,6 +27,8 @@ typedef struct {
   /* profiles along z (the reference's -DMEASURE_Z build, z_coord.c) */
   int measure_z, do_z_meas, setup_wall;
   long meas_interval_z;
+  /* heatbath real-time trajectories (the reference's -DHB_TRAJECTORY build) */
+  int hb_trajectory, do_trajectory;
   /* additions of this implementation (optional keys) */
   uint64_t seed;
   int have_seed;
@@ -39,6 +41,13 @@ typedef struct {
   int mode, checks_per_sweep, bins, orderparam;
   double min, max, delta;
 } host_muca;
+
+/* settings of the heatbath trajectories, read from "realtime_config"
+ * (trajectory struct, su2.h:566-575) */
+typedef struct {
+  int n_traj, interval, mode_interval;
+  double min, max;
+} host_traj;
 
 /* config.c */
 int cfg_open(const char* fname, FILE** f);
@@ -80,5 +89,15 @@ void save_weight(const su2gpu_weight* w);
 void linearize_weight(su2gpu_weight* w);
 double get_weight(const su2gpu_weight* w, double val);
 void print_acceptance(const host_params* hp, const int64_t* c);
+
+/* trajectory.c */
+void read_realtime_config(const char* fname, host_traj* t);
+void print_realtime_params(const host_params* hp, const host_traj* t);
+/* one set of trajectories from the configuration in `ctx` (the fields are
+ * not changed); `w` is the run's weight, used read-only for the order
+ * parameter; sweeps run on a second context seeded by (seed, chain
+ * 0x40000000 + id) */
+int make_realtime_trajectories(su2gpu_ctx* ctx, const host_params* hp, const su2gpu_weight* w,
+                               const host_traj* t, int id, uint64_t seed, int64_t* counters);
 
 #endif

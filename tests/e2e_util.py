@@ -9,7 +9,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 BIN = os.path.join(ROOT, "bin", "su2")
-CASES = ("fund", "adj", "su2u1s", "fund_muca", "su2u1s_z", "fundadj_z")
+CASES = ("fund", "adj", "su2u1s", "fund_muca", "su2u1s_z", "fundadj_z", "fund_traj")
 
 
 def ensure_binary():
@@ -38,6 +38,11 @@ def stage(case, tmpdir):
     if "weight" in g:
         with open(os.path.join(tmpdir, "weight"), "wb") as f:
             f.write(g["weight"])
+    # further inputs of the case (in_<file name>)
+    for k in g:
+        if k.startswith("in_"):
+            with open(os.path.join(tmpdir, k[3:]), "wb") as f:
+                f.write(g[k])
     return g
 
 

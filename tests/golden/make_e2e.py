@@ -25,6 +25,13 @@ directories and stores, per case, in e2e_<case>.npz:
                 (the _z cases, -DMEASURE_Z builds) the profile labels and the
                 first measure_along_z block, of the loaded configuration
                 (z_coord.c:78-300)
+  trajectory    (fund_traj, the -DHB_TRAJECTORY build) the trajectory file of
+                one set of heatbath trajectories started at iteration 1 from
+                the loaded configuration (hb_trajectory.c:10-94), in a band of
+                +-1e-4 around its order parameter so that every trajectory
+                ends after one sweep
+  in_<name>     further input files of the case (flat read-only weight,
+                realtime_config), written next to the config before the run
   bin_content   the --content argument that makes bin/su2 the same program
 
 Run here, where the reference sources are: python tests/golden/make_e2e.py
@@ -62,7 +69,45 @@ CASES = {
                                                           "setup_wall": 0}),
     "fundadj_z": ("fundadjz", "fundadj", "fundadj+measure_z", {"do_flow": 0, "do_z_meas": 1, "interval_z": 1,
                                                                "setup_wall": 0}),
+    # heatbath trajectories (-DHB_TRAJECTORY): a read-only flat weight, one
+    # set at iteration 1 (mode_interval 1)
+    "fund_traj": ("fundt", "fund", "fund+hb_trajectory", {"do_flow": 0, "multicanonical": 1, "muca_mode": 0,
+                                                          "bins": 20, "min": 0.0, "max": 1.2, "orderparam": "phisq",
+                                                          "do_trajectory": 1}),
 }
+
+TRAJ_BAND = 1e-4
+TRAJ_N = 3
+
+
+def flat_weight(bins=20, lo=0.0, hi=1.2):
+    """A flat weight file in the reference's format (save_weight,
+    multicanonical.c:82-99): bins delta last_max wrk_min wrk_max, then the
+    bins+1 bin starts with weight 0."""
+    lines = ["%d %.12f %d %f %f" % (bins, 0.3, 0, lo, hi)]
+    for i in range(bins + 1):
+        lines.append("%f %f" % (lo + i * (hi - lo) / bins, 0.0))
+    return ("\n".join(lines) + "\n").encode()
+
+
+def phisq(content, lat):
+    """calc_orderparam PHISQ (multicanonical.c:709-749) of a lattice file:
+    sum of |phi|^2 / 2 over the EVEN then the ODD sites, each divided by the
+    volume."""
+    V = L[0] * L[1] * L[2]
+    off = 44 + 8 * V * 3 * 4
+    phi = np.frombuffer(lat[off:off + 8 * V * 4], dtype=np.float64).reshape(V, 4)
+    sq = 0.5 * np.sum(phi * phi, axis=1)
+    return float(np.sum(sq[: V // 2]) / V + np.sum(sq[V // 2:]) / V)
+
+
+def extra_inputs(case, content, lat):
+    if case != "fund_traj":
+        return {}
+    v0 = phisq(content, lat)
+    rt = "n_traj %d\ninterval 1\nmode_interval 1\nmin %.10f\nmax %.10f\n" % (TRAJ_N, v0 - TRAJ_BAND,
+                                                                              v0 + TRAJ_BAND)
+    return {"weight": flat_weight(), "realtime_config": rt.encode()}
 
 
 def set_key(text, key, value):
@@ -109,18 +154,21 @@ def run_ref(content, config, lattice, extra=None):
         out = {}
         for name in sorted(os.listdir(d)):
             if name in ("labels", "measure", "measure_flow", "lattice", "weight", "labels_local", "labels_z",
-                        "measure_z") or name.startswith("measure_local_"):
+                        "measure_z", "trajectory") or name.startswith("measure_local_"):
                 out[name] = open(os.path.join(d, name), "rb").read()
         return out
     finally:
         shutil.rmtree(d)
 
 
-def main():
+def main(only=None):
     for case, (binary, content, bin_content, over) in CASES.items():
+        if only and case not in only:
+            continue
         config = make_config(over)
         lat = lattice_bytes(content, 1000 + len(case))
-        got = run_ref(binary, config, lat)
+        extra = extra_inputs(case, content, lat)
+        got = run_ref(binary, config, lat, extra)
         rec = {"config": np.frombuffer(config.encode(), dtype=np.uint8), "content": np.array(content),
                "bin_content": np.array(bin_content),
                "lattice_in": np.frombuffer(lat, dtype=np.uint8),
@@ -128,16 +176,18 @@ def main():
                "measure": np.frombuffer(got["measure"], dtype=np.uint8)}
         if "measure_flow" in got:
             rec["measure_flow"] = np.frombuffer(got["measure_flow"], dtype=np.uint8)
-        if "weight" in got:
+        if "weight" in got and "weight" not in extra:
             rec["weight"] = np.frombuffer(got["weight"], dtype=np.uint8)
+        for name, data in extra.items():
+            rec["in_" + name] = np.frombuffer(data, dtype=np.uint8)
         for name, data in got.items():
-            if name in ("labels_local", "labels_z", "measure_z") or name.startswith("measure_local_"):
+            if name in ("labels_local", "labels_z", "measure_z", "trajectory") or name.startswith("measure_local_"):
                 rec[name] = np.frombuffer(data, dtype=np.uint8)
-        got0 = run_ref(binary, set_key(config, "iterations", 0), lat)
+        got0 = run_ref(binary, set_key(config, "iterations", 0), lat, extra)
         rec["lattice_out0"] = np.frombuffer(got0["lattice"], dtype=np.uint8)
         np.savez_compressed(os.path.join(HERE, f"e2e_{case}.npz"), **rec)
         print(case, {k: len(v) for k, v in got.items()})
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -76,3 +76,33 @@ def test_random_order_run_sweeps_equals_stepwise(gpu):
     for s in range(9, 12):
         b.update_lattice(s)
     assert np.array_equal(a.download()["link"], b.download()["link"])
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_clone_and_copy_fields(gpu, precision):
+    """su2gpu_clone / su2gpu_copy_fields (the field copies of the heatbath
+    trajectories, hb_trajectory.c:26-29, 61): a clone starts from the same
+    fields, runs its own stream, and copy_fields restores it exactly."""
+    p = abi.make_params("fund", L=(8, 8, 8), precision=precision)
+    f = hot_fields(abi.make_params("fund", L=(8, 8, 8)), seed=4, phi_mean=0.5)
+    lat = gpu.Lattice(p, seed=1)
+    upload(lat, f)
+    before = lat.download()
+    c = lat.clone(seed=5, chain=0x40000001)
+    for k, v in c.download().items():
+        if v is not None:
+            assert np.array_equal(v, before[k]), k
+    c.set_random_sweeps(True)
+    c.run_sweeps(0, 3, graph=False)
+    assert not np.array_equal(c.download()["link"], before["link"])
+    c.copy_fields_from(lat)
+    for k, v in c.download().items():
+        if v is not None:
+            assert np.array_equal(v, before[k]), k
+    # the source is untouched
+    assert np.array_equal(lat.download()["d0"], before["d0"])
+    other = gpu.Lattice(abi.make_params("fund", L=(8, 8, 6), precision=precision), seed=1)
+    with pytest.raises(gpu.SU2GPUError):
+        other.copy_fields_from(lat)
+    c.close()
+    other.close()

@@ -95,3 +95,46 @@ def test_first_z_profile_matches_reference(binary, case, precision, rtol, atol, 
     assert E.read(d, "labels_z") == g["labels_z"]
     compare_rows(rows(E.read(d, "measure")), rows(g["measure"]), rtol, atol)
     compare_rows(rows(E.read(d, "measure_z")), rows(g["measure_z"]), rtol, atol)
+
+
+def _realtime_band(g):
+    kv = dict(line.split()[:2] for line in g["in_realtime_config"].decode().splitlines() if line.strip())
+    return float(kv["min"]), float(kv["max"]), int(kv["n_traj"])
+
+
+@pytest.mark.parametrize("precision,tol", [(64, 1e-7), (32, 1e-5)])
+def test_trajectories_match_reference(binary, precision, tol, tmp_path):
+    """Heatbath trajectories (the reference's -DHB_TRAJECTORY build,
+    hb_trajectory.c:10-94): the trajectory file has the reference's lines --
+    run header, set header with the start value, one header per trajectory,
+    "sweeps value" rows -- and each trajectory starts at the order parameter
+    of the loaded configuration (within `tol`) and ends, in the band of
+    +-1e-4 around it, after its first sweep with a value outside the band
+    (the value itself is random).  The main run is unchanged by the
+    trajectories: its first measure row is the reference's."""
+    d = str(tmp_path)
+    g = E.stage("fund_traj", d)
+    E.run(d, g["bin_content"], "--precision", str(precision), "--seed", "7")
+    lo, hi, n = _realtime_band(g)
+    got = E.read(d, "trajectory").decode().splitlines()
+    want = g["trajectory"].decode().splitlines()
+    assert len(got) == len(want)
+    starts = 0
+    for a, b in zip(got, want):
+        if not b.strip() or b.startswith("=") or b.startswith("--- Traj"):
+            assert a == b
+        elif b.startswith("----- Begin set"):
+            pa, pb = a.split(), b.split()
+            assert pa[:5] == pb[:5] and pa[6:] == pb[6:]
+            assert close(pa[5], pb[5], 1e-6 if precision == 64 else 1e-5, tol)
+        else:
+            (ia, va), (ib, vb) = a.split(), b.split()
+            assert ia == ib
+            if ib == "0":
+                starts += 1
+                assert close(va, vb, 0.0, tol)
+            else:
+                assert float(va) < lo or float(va) > hi
+                assert len(va.split(".")[1]) == 8
+    assert starts == n
+    compare_rows(rows(E.read(d, "measure")), rows(g["measure"]), 1e-6 if precision == 64 else 1e-4, 1e-5)

@@ -25,6 +25,8 @@ def test_labels_lattice_weight_roundtrip(binary, case, tmp_path):
     assert E.lattice_equal(E.read(str(tmp_path), "lattice"), g["lattice_out0"])
     if "weight" in g:
         assert E.read(str(tmp_path), "weight") == g["weight"]
+    if "in_weight" in g:  # a read-only weight is left as it was (save_weight, multicanonical.c:85-87)
+        assert E.read(str(tmp_path), "weight") == g["in_weight"]
 
 
 def test_cold_start_header(binary, tmp_path):
