@@ -125,8 +125,8 @@ def test_trajectories_match_reference(binary, precision, tol, tmp_path):
             assert a == b
         elif b.startswith("----- Begin set"):
             pa, pb = a.split(), b.split()
-            assert pa[:5] == pb[:5] and pa[6:] == pb[6:]
-            assert close(pa[5], pb[5], 1e-6 if precision == 64 else 1e-5, tol)
+            assert pa[:6] == pb[:6] and pa[7:] == pb[7:]
+            assert close(pa[6], pb[6], 1e-6 if precision == 64 else 1e-5, tol)
         else:
             (ia, va), (ib, vb) = a.split(), b.split()
             assert ia == ib
