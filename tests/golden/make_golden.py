@@ -139,6 +139,8 @@ MUCA_CASES = {
     "fund_phisq_cps5": ("fund", "phisq", 0, 5, 3),
     "adj_sigmasq_fast": ("adj", "Sigmasq", 1, 1, 12),
     "fundadj_p2ms2": ("fundadj", "phi2minusSigma2", 1, 2, 3),
+    # two doublets, the order parameter on the second one (PHI2SQ)
+    "higgs2_phi2sq_fast": ("higgs2", "phi2sq", 1, 2, 3),
 }
 
 
@@ -149,6 +151,8 @@ def gen_muca(name):
     # a weight around the starting order parameter, steep enough to reject often
     if op == "phisq":
         R0 = float(np.mean(0.5 * np.sum(f.d0 ** 2, axis=1)))
+    elif op == "phi2sq":
+        R0 = float(np.mean(0.5 * np.sum(f.d1 ** 2, axis=1)))
     elif op == "Sigmasq":
         R0 = float(np.mean(0.5 * np.sum(f.trip ** 2, axis=1)))
     else:
@@ -224,7 +228,11 @@ def gen_flow(name):
     np.savez_compressed(os.path.join(HERE, f"flow_{name}.npz"), **out)
 
 
-def main():
+def main(only=None):
+    if only:
+        for m in only:
+            gen_muca(m)
+        return
     if not ref_available("fund"):
         sys.exit("reference harness not built: make -C oracle/ref REF=<su2higgs checkout>")
     gen_layout()
@@ -241,4 +249,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])
