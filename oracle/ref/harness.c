@@ -442,3 +442,94 @@ int ref_grad_flow(double tmax, double dt, int flow_id, double* out, int maxrows,
   return rowcap_per;
 }
 #endif
+
+/* ---- correlators and blocking ---- */
+#ifdef CORRELATORS
+/* The values of one measure_correlators() row set (correlation.c:350-398)
+ * at full precision: per distance d < L[dir]/2 ten doubles -- the Higgs
+ * correlator, the Sigma^2 correlator, then photon_correl() for (transmom,
+ * mode) = (1,0), (2,0), (1,1), (2,1), each re and im (absent columns 0). */
+#ifdef TRIPLET
+/* defined in correlation.c:257 without a declaration in su2.h */
+complex photon_correl(lattice* l, fields const* f, params const* p, int d, int dir, int transmom, int mode);
+#endif
+static void corr_rows(lattice* l, fields const* f, int dir, double* out) {
+  int maxd = l->L[dir] / 2;
+  for (int d = 0; d < maxd; d++) {
+    double* r = out + 10 * d;
+    for (int k = 0; k < 10; k++) r[k] = 0.0;
+#if (NHIGGS > 0)
+    r[0] = higgs_correlator(l, f, d, dir, 0);
+#endif
+#ifdef TRIPLET
+    r[1] = triplet_correlator(l, f, d, dir);
+    const int tm[4] = {1, 2, 1, 2}, md[4] = {0, 0, 1, 1};
+    for (int k = 0; k < 4; k++) {
+      complex c = photon_correl(l, f, &P, d, dir, tm[k], md[k]);
+      r[2 + 2 * k] = c.re;
+      r[3 + 2 * k] = c.im;
+    }
+#endif
+  }
+}
+int ref_longest_dir(void) { return L.longest_dir; }
+int ref_correlators(int dir, double* out) {
+  corr_rows(&L, &F, dir, out);
+  return L.L[dir] / 2;
+}
+#ifdef BLOCKING
+/* main.c:106-157: blocked lattices in every direction but the longest, as
+ * many levels as asked for and possible */
+#define MAXBLOCK 8
+static lattice BL[MAXBLOCK];
+static fields BF[MAXBLOCK];
+static int block_dir_h[4];
+static int nblocked = 0;
+int ref_block_setup(int levels) {
+  if (nblocked) return nblocked;
+  L.blocklist.sends = 0; L.blocklist.recvs = 0;
+  realloc_comlist(&L.blocklist, RECV);
+  L.standby = 0;
+  L.blocking_level = 0;
+  for (int d = 0; d < L.dim; d++) block_dir_h[d] = d != L.longest_dir;
+  int mx = max_block_level(&L, block_dir_h);
+  if (levels > mx) levels = mx;
+  if (levels > MAXBLOCK) levels = MAXBLOCK;
+  for (int k = 0; k < levels; k++) {
+    lattice* base = k ? &BL[k - 1] : &L;
+    BL[k].blocklist.sends = 0; BL[k].blocklist.recvs = 0;
+    block_lattice(base, &BL[k], block_dir_h);
+    alloc_fields(&BL[k], &BF[k]);
+    BL[k].blocking_level = k + 1;
+  }
+  nblocked = levels;
+  return levels;
+}
+/* measure_blocked_correlators (correlation.c:404-432) for level k+1 from
+ * level k (the fields level 0): smear_fields, make_blocked_fields, then the
+ * correlator rows on the blocked lattice.  Also returns the blocked links
+ * and triplet in the blocked lattice's storage order with its coordinates
+ * and L; the value is the number of blocked sites. */
+long ref_blocked_level(int k, int dir, double* corr, double* link, double* trip, long* coords, int* Lb) {
+  if (k < 0 || k >= nblocked) return -1;
+  lattice* base = k ? &BL[k - 1] : &L;
+  fields* fb = k ? &BF[k - 1] : &F;
+  fields fs;
+  alloc_fields(base, &fs);
+  smear_fields(base, fb, &fs, block_dir_h);
+  make_blocked_fields(base, &BL[k], &fs, &BF[k]);
+  free_fields(base, &fs);
+  corr_rows(&BL[k], &BF[k], dir, corr);
+  long V = BL[k].sites;
+  int D = BL[k].dim;
+  memcpy(link, &BF[k].su2link[0][0][0], sizeof(double) * V * D * 4);
+#ifdef TRIPLET
+  if (trip) memcpy(trip, &BF[k].su2triplet[0][0], sizeof(double) * V * 3);
+#endif
+  for (long i = 0; i < V; i++)
+    for (int d = 0; d < D; d++) coords[i * D + d] = BL[k].coords[i][d];
+  for (int d = 0; d < D; d++) Lb[d] = BL[k].L[d];
+  return V;
+}
+#endif
+#endif

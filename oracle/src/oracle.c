@@ -1546,6 +1546,223 @@ int orc_grad_flow(orc_ctx* c, double t_max, double dt, int meas_interval, double
 }
 
 /* ------------------------------------------------------------------ */
+/* correlators and blocking (correlation.c, blocking.c, su2u1.c)       */
+/* ------------------------------------------------------------------ */
+
+/* su2plaquette + the three other plaquettes of clover_su2 (su2u1.c:119-136,
+ * 207-274): the clover of the (d1, d2) plane at site i */
+static void clover(const orc_ctx* c, long i, int d1, int d2, double* cl) {
+  double a[4], b[4], t[4], s[4], u[4];
+  /* U_1(x) U_2(x+1) U_1(x+2)^+ U_2(x)^+ */
+  qdag(LNK(c, NX(c, i, d2), d1), a);
+  qdag(LNK(c, i, d2), b);
+  qmul(a, b, t);
+  qmul(LNK(c, NX(c, i, d1), d2), t, s);
+  qmul(LNK(c, i, d1), s, cl);
+  /* U_2(x) U_1(x+2-1)^+ U_2(x-1)^+ U_1(x-1) */
+  long xm1 = PV(c, i, d1), x21 = PV(c, NX(c, i, d2), d1);
+  qdag(LNK(c, xm1, d2), a);
+  qmul(a, LNK(c, xm1, d1), t);
+  qdag(LNK(c, x21, d1), b);
+  qmul(b, t, s);
+  qmul(LNK(c, i, d2), s, u);
+  for (int k = 0; k < 4; k++) cl[k] += u[k];
+  /* U_1(x-1)^+ U_2(x-2-1)^+ U_1(x-1-2) U_2(x-2) */
+  long xm12 = PV(c, xm1, d2), xm2 = PV(c, i, d2);
+  qmul(LNK(c, xm12, d1), LNK(c, xm2, d2), t);
+  qdag(LNK(c, xm12, d2), a);
+  qmul(a, t, s);
+  qdag(LNK(c, xm1, d1), b);
+  qmul(b, s, u);
+  for (int k = 0; k < 4; k++) cl[k] += u[k];
+  /* U_2(x-2)^+ U_1(x-2) U_2(x+1-2) U_1(x)^+ */
+  long x12 = NX(c, xm2, d1);
+  qdag(LNK(c, i, d1), a);
+  qmul(LNK(c, x12, d2), a, t);
+  qmul(LNK(c, xm2, d1), t, s);
+  qdag(LNK(c, xm2, d2), b);
+  qmul(b, s, u);
+  for (int k = 0; k < 4; k++) cl[k] += u[k];
+}
+
+/* site phase 2 pi p.x of photon_correl's momentum (correlation.c:140-146,
+ * 226-231): only the components of mom that are non-zero */
+static double phase_px(const orc_ctx* c, long i, const int* mom) {
+  double px = 0.0;
+  for (int d = 0; d < c->D; d++)
+    if (mom[d] != 0) px += (double)(mom[d] * c->coords[i * c->D + d]) / (double)c->p.L[d];
+  return px;
+}
+
+/* the plane operators at x_dir = z, summed over the plane's sites in storage
+ * order (sites_at_coord, layout.c:798-816): h, s (plane_sum of doubletsq /
+ * tripletsq, correlation.c:16-33), and per (transmom, mode) one complex
+ * number: mode 0 projected_photon_operator (correlation.c:99-164), mode 1
+ * photon_projection_full (correlation.c:207-253) */
+static void plane_ops(const orc_ctx* c, int dir, long z, double* h, double* s, double op[4][2]) {
+  int d1 = dir == 0 ? 1 : 0, d2 = dir == 2 ? 1 : 2;
+  *h = 0.0; *s = 0.0;
+  for (int k = 0; k < 4; k++) op[k][0] = op[k][1] = 0.0;
+  for (int k = 0; c->has_trip && k < 4; k++) {
+    int tm = (k & 1) ? 2 : 1, mode = k >> 1;
+    /* photon_correl (correlation.c:270-274): the loop over dir0 stops after
+     * dir0 = 0, so the momentum is (tm, 0, 0) when dir != 0, else zero */
+    int mom[4] = {0, 0, 0, 0};
+    if (dir != 0) mom[0] = tm;
+    for (long i = 0; i < c->V; i++) {
+      if (c->coords[i * c->D + dir] != z) continue;
+      double px = phase_px(c, i, mom), val;
+      if (mode == 0) {
+        double cl[4];
+        clover(c, i, d1, d2, cl);
+        cl[0] = 0.0;
+        for (int q = 1; q < 4; q++) cl[q] /= 4.0;
+        const double* a = TRP(c, i);
+        val = a[0] * cl[1] + a[1] * cl[2] + a[2] * cl[3];
+      } else {
+        double alpha = 0.0;
+        for (int e1 = 0; e1 < c->D; e1++)
+          for (int e2 = e1 + 1; e2 < c->D; e2++)
+            if (e1 != dir && e2 != dir) alpha += orc_alpha_proj(c, i, e1, e2);
+        val = 2.0 * alpha;
+      }
+      op[k][0] += val * cos(2.0 * M_PI * px);
+      op[k][1] += val * sin(2.0 * M_PI * px);
+    }
+  }
+  for (long i = 0; i < c->V; i++) {
+    if (c->coords[i * c->D + dir] != z) continue;
+    if (c->nh > 0) *h += doubletsq(PHI(c, 0, i));
+    if (c->has_trip) *s += tripletsq(TRP(c, i));
+  }
+}
+
+/* measure_correlators (correlation.c:350-398) before formatting: per
+ * distance d < L[dir]/2 ten values -- higgs_correlator (correlation.c:39-58),
+ * triplet_correlator (65-83), photon_correl for (transmom, mode) = (1,0),
+ * (2,0), (1,1), (2,1) re/im (257-315); absent fields give 0 */
+int orc_correlators(const orc_ctx* c, int dir, double* out) {
+  long Lz = c->p.L[dir];
+  double* h = (double*)calloc(Lz, sizeof(double));
+  double* s = (double*)calloc(Lz, sizeof(double));
+  double (*op)[4][2] = calloc(Lz, sizeof(*op));
+  for (long z = 0; z < Lz; z++) plane_ops(c, dir, z, &h[z], &s[z], op[z]);
+  int maxd = (int)(Lz / 2);
+  for (int d = 0; d < maxd; d++) {
+    double* r = out + 10 * d;
+    double hc = 0.0, sc = 0.0, pre[4] = {0, 0, 0, 0}, pim[4] = {0, 0, 0, 0};
+    for (long z = 0; z < Lz; z++) {
+      long zd = (z + d) % Lz;
+      hc += h[z] * h[zd];
+      sc += s[z] * s[zd];
+      for (int k = 0; k < 4; k++) {
+        /* O1 . O2^* through cmult (stddefs.h:93-98) */
+        double ar = op[z][k][0], ai = op[z][k][1], br = op[zd][k][0], bi = -op[zd][k][1];
+        pre[k] += ar * br - ai * bi;
+        pim[k] += br * ai + ar * bi;
+      }
+    }
+    r[0] = c->nh > 0 ? 4.0 * hc / (double)c->V : 0.0;
+    r[1] = c->has_trip ? sc / (double)c->V : 0.0;
+    for (int k = 0; k < 4; k++) {
+      r[2 + 2 * k] = c->has_trip ? pre[k] / (double)c->V : 0.0;
+      r[3 + 2 * k] = c->has_trip ? pim[k] / (double)c->V : 0.0;
+    }
+  }
+  free(h); free(s); free(op);
+  return maxd;
+}
+
+/* su2staple_wilson_onedir with dagger = 1 (staples.c:197-232): the two
+ * staples of U_mu(x) in the (mu, nu) plane, each conjugated:
+ *   U_nu(x) U_mu(x+nu) U_nu(x+mu)^+  +  U_nu(x-nu)^+ U_mu(x-nu) U_nu(x+mu-nu) */
+static void staple_onedir_dag(const orc_ctx* c, long i, int mu, int nu, double* res) {
+  double a[4], t[4], s[4];
+  long xp = NX(c, i, mu), xn = NX(c, i, nu), xm = PV(c, i, nu), xpm = PV(c, xp, nu);
+  qdag(LNK(c, xp, nu), a);
+  qmul(LNK(c, xn, mu), a, t);
+  qmul(LNK(c, i, nu), t, res);
+  qmul(LNK(c, xm, mu), LNK(c, xpm, nu), t);
+  qdag(LNK(c, xm, nu), a);
+  qmul(a, t, s);
+  for (int k = 0; k < 4; k++) res[k] += s[k];
+}
+
+/* smear_link (su2u1.c:752-795): V_dir(x) V_dir(x+dir) normalised, with
+ * V_dir(y) = (U_dir(y) + sum over smeared j != dir of both staples) / paths */
+static void smear_link(const orc_ctx* c, const int* sdir, long i, int dir, double* res) {
+  double r[4], v2[4], st[4];
+  long xp = NX(c, i, dir);
+  memcpy(r, LNK(c, i, dir), sizeof(r));
+  memcpy(v2, LNK(c, xp, dir), sizeof(v2));
+  int paths = 1;
+  for (int j = 0; j < c->D; j++) {
+    if (j == dir || !sdir[j]) continue;
+    staple_onedir_dag(c, i, dir, j, st);
+    for (int k = 0; k < 4; k++) r[k] += st[k];
+    staple_onedir_dag(c, xp, dir, j, st);
+    for (int k = 0; k < 4; k++) v2[k] += st[k];
+    paths += 2;
+  }
+  for (int k = 0; k < 4; k++) { r[k] /= (double)paths; v2[k] /= (double)paths; }
+  qmul(r, v2, res);
+  double det = sqrt(qsq(res));
+  for (int k = 0; k < 4; k++) res[k] /= det;
+}
+
+/* smear_triplet (su2u1.c:805-852): (Sigma(x) + sum over smeared j of
+ * U_j(x) Sigma(x+j) U_j(x)^+ + U_j(x-j)^+ Sigma(x-j) U_j(x-j)) / sites */
+static void smear_triplet(const orc_ctx* c, const int* sdir, long i, double* res) {
+  double cov[3] = {0, 0, 0}, r[3], ud[4];
+  int sites = 1;
+  for (int d = 0; d < c->D; d++) {
+    if (!sdir[d]) continue;
+    qrot(LNK(c, i, d), TRP(c, NX(c, i, d)), r);
+    for (int k = 0; k < 3; k++) cov[k] += r[k];
+    long xm = PV(c, i, d);
+    qdag(LNK(c, xm, d), ud);
+    qrot(ud, TRP(c, xm), r);
+    for (int k = 0; k < 3; k++) cov[k] += r[k];
+    sites += 2;
+  }
+  for (int k = 0; k < 3; k++) res[k] = (TRP(c, i)[k] + cov[k]) / (double)sites;
+}
+
+/* smear_fields + make_blocked_fields (su2u1.c:857-905, blocking.c:296-374):
+ * the site of dst with coordinates y takes the smeared fields of the src
+ * site with x_d = 2 y_d in the blocked directions, x_d = y_d elsewhere; links
+ * in unblocked directions are copied, the triplet is smeared over the
+ * blocked directions.  dst has the blocked sides. */
+int orc_block(const orc_ctx* src, const int* block_dir, orc_ctx* dst) {
+  int D = src->D;
+  for (int d = 0; d < D; d++)
+    if (dst->p.L[d] != (block_dir[d] ? src->p.L[d] / 2 : src->p.L[d])) return -1;
+  long* lex = (long*)malloc(sizeof(long) * src->V);
+  for (long i = 0; i < src->V; i++) {
+    long n = 0, st = 1;
+    for (int d = 0; d < D; d++) { n += src->coords[i * D + d] * st; st *= src->p.L[d]; }
+    lex[n] = i;
+  }
+  for (long j = 0; j < dst->V; j++) {
+    long n = 0, st = 1;
+    for (int d = 0; d < D; d++) {
+      long x = dst->coords[j * D + d] * (block_dir[d] ? 2 : 1);
+      n += x * st;
+      st *= src->p.L[d];
+    }
+    long i = lex[n];
+    for (int d = 0; d < D; d++) {
+      if (block_dir[d]) smear_link(src, block_dir, i, d, LNK(dst, j, d));
+      else memcpy(LNK(dst, j, d), LNK(src, i, d), 4 * sizeof(double));
+      if (src->has_u1 && dst->has_u1 && !block_dir[d]) dst->u1[j * D + d] = src->u1[i * D + d];
+    }
+    if (src->has_trip && dst->has_trip) smear_triplet(src, block_dir, i, TRP(dst, j));
+  }
+  free(lex);
+  return 0;
+}
+
+/* ------------------------------------------------------------------ */
 /* random stream probes (tests)                                        */
 /* ------------------------------------------------------------------ */
 void orc_philox_raw(const uint32_t* ctr, const uint32_t* key, uint32_t* out) { orc_philox4x32_10(ctr, key, out); }

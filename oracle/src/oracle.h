@@ -34,6 +34,8 @@ void orc_reset_counters(orc_ctx* c);
 void orc_measure(const orc_ctx* c, double* sums);
 void orc_measure_local(const orc_ctx* c, double* out);
 void orc_measure_z(const orc_ctx* c, int* zdir, double* sums);
+int orc_correlators(const orc_ctx* c, int dir, double* out);
+int orc_block(const orc_ctx* src, const int* block_dir, orc_ctx* dst);
 
 /* per-site kernels */
 void orc_wilson_staple(const orc_ctx* c, long i, int dir, double* V);

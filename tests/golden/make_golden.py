@@ -10,6 +10,11 @@ Every fixture stores its inputs, so the tests never regenerate them:
                          update_lattice() (update.c:270) with the Philox stream
   muca_<case>.npz        the same with multicanonical global accept/reject
   flow_<case>.npz        grad_flow() (gradflow.c:46) measurement rows
+  correl_<case>.npz      measure_correlators() values (correlation.c:350-398) of
+                         a hot lattice along the longest direction, and for
+                         each blocking level (smear_fields + make_blocked_fields,
+                         su2u1.c:857, blocking.c:296) the blocked links, triplet,
+                         coordinates and correlator values
 
 Run:  python tests/golden/make_golden.py
 """
@@ -228,10 +233,42 @@ def gen_flow(name):
     np.savez_compressed(os.path.join(HERE, f"flow_{name}.npz"), **out)
 
 
+CORREL_CASES = {
+    # name: (content, reference variant, L, blocking levels asked for)
+    "adj_6x4x8": ("adj", "adjc", (6, 4, 8), 2),
+    "adj_8x8x12": ("adj", "adjc", (8, 8, 12), 2),
+    "adj_12x8x8": ("adj", "adjc", (12, 8, 8), 2),
+    "fundadj_8x6x10": ("fundadj", "fundadjc", (8, 6, 10), 0),
+    "fund_6x8x4": ("fund", "fundc", (6, 8, 4), 0),
+}
+
+
+def gen_correl(name):
+    content, variant, L, levels = CORREL_CASES[name]
+    p = abi.make_params(content, L=L)
+    f = hot_fields(p, seed=SEED + 21, trip_sigma=0.5, phi_mean=0.4)
+    r = Ref(p, variant=variant)
+    r.put(f)
+    ld = r.longest_dir()
+    out = dict(fields_dict(f, "in_"), **param_dict(p))
+    out["dir"] = np.array(ld)
+    out["corr0"] = r.correlators(ld)
+    n = r.block_setup(levels) if levels else 0
+    out["levels"] = np.array(n)
+    for k in range(n):
+        b = r.blocked_level(k, ld)
+        for key in ("corr", "link", "trip", "coords", "L"):
+            out[f"b{k + 1}_{key}"] = b[key]
+    np.savez_compressed(os.path.join(HERE, f"correl_{name}.npz"), **out)
+
+
 def main(only=None):
     if only:
         for m in only:
-            gen_muca(m)
+            if m in CORREL_CASES:
+                gen_correl(m)
+            else:
+                gen_muca(m)
         return
     if not ref_available("fund"):
         sys.exit("reference harness not built: make -C oracle/ref REF=<su2higgs checkout>")
@@ -244,6 +281,8 @@ def main(only=None):
         gen_muca(m)
     for fl in FLOW_CASES:
         gen_flow(fl)
+    for c in CORREL_CASES:
+        gen_correl(c)
     total = sum(os.path.getsize(os.path.join(HERE, x)) for x in os.listdir(HERE) if x.endswith(".npz"))
     print(f"golden fixtures written, {total / 1024:.0f} KiB")
 

@@ -74,6 +74,8 @@ def oracle_lib():
             getattr(lib, name).argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         lib.orc_measure_z.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]
         lib.orc_set_random_sweeps.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        lib.orc_correlators.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        lib.orc_block.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         lib.orc_sweep_order.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         _oracle = lib
@@ -174,6 +176,33 @@ class Oracle:
 
     def set_random_sweeps(self, on=True):
         self.lib.orc_set_random_sweeps(self.h, 1 if on else 0)
+
+    def longest_dir(self):
+        """make_misc_tables (layout.c:773-777): the longest direction, ties to
+        the last."""
+        ld = self.p.dim - 1
+        for d in range(self.p.dim - 1, -1, -1):
+            if self.p.L[d] > self.p.L[ld]:
+                ld = d
+        return ld
+
+    def correlators(self, dir):
+        out = np.zeros((self.p.L[dir] // 2 + 1, 10))
+        n = self.lib.orc_correlators(self.h, dir, _P(out))
+        return out[:n].copy()
+
+    def block(self, block_dir):
+        """A new oracle lattice: this one smeared and blocked in the
+        directions block_dir[d] != 0."""
+        bd = np.ascontiguousarray(block_dir, dtype=np.int32)
+        L = tuple(self.p.L[d] // 2 if bd[d] else self.p.L[d] for d in range(self.p.dim))
+        q = abi.make_params(self.p.content, L=L)
+        for name, _ in abi.Params._fields_:
+            if name not in ("L", "dim"):
+                setattr(q, name, getattr(self.p, name))
+        out = Oracle(q)
+        assert self.lib.orc_block(self.h, _P(bd), out.h) == 0
+        return out
 
     def update(self):
         return self.lib.orc_update_lattice(self.h)
@@ -300,7 +329,7 @@ def reference_config(p, workdir, muca=None, flow=None, iterations=10, interval=1
         scalar_sweeps=p.scalar_sweeps, update_singlet=p.update_singlet, update_doublet=p.update_su2doublet,
         update_triplet=p.update_su2triplet, update_links=p.update_links,
         multicanonical=0, measure_local=0, do_flow=0, flow_meas_interval=10, flow_dt=0.05, flow_interval=1000,
-        flow_t_max=10,
+        flow_t_max=10, do_correlators=0, correlator_interval=1000, blocks=0,
     )
     if muca is not None:
         kv.update(multicanonical=1, **muca)
@@ -320,8 +349,8 @@ class Ref:
 
     _libs = {}
 
-    def __init__(self, p, workdir=None, muca=None, flow=None):
-        variant = REF_VARIANT[p.content & ~abi.GRADFLOW]
+    def __init__(self, p, workdir=None, muca=None, flow=None, variant=None):
+        variant = variant or REF_VARIANT[p.content & ~abi.GRADFLOW]
         path = os.path.join(REF_DIR, f"libref_{variant}.so")
         # each instance needs fresh globals: load a private copy of the library
         self.workdir = workdir or tempfile.mkdtemp(prefix="su2ref_")
@@ -364,6 +393,11 @@ class Ref:
             lib.ref_flow_step.argtypes = [ctypes.c_double]
             lib.ref_grad_flow.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_void_p,
                                           ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+        if hasattr(lib, "ref_correlators"):
+            lib.ref_correlators.argtypes = [ctypes.c_int, ctypes.c_void_p]
+        if hasattr(lib, "ref_blocked_level"):
+            lib.ref_blocked_level.restype = ctypes.c_long
+            lib.ref_blocked_level.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 5
         self.lib = lib
         self.p = p
         cfg = reference_config(p, self.workdir, muca=muca, flow=flow)
@@ -374,6 +408,35 @@ class Ref:
         finally:
             os.chdir(cwd)
         self.V = lib.ref_sites()
+
+    def longest_dir(self):
+        return self.lib.ref_longest_dir()
+
+    def correlators(self, dir):
+        """measure_correlators() values (correlation.c:350-398), full precision:
+        rows d < L[dir]/2 of (Higgs, Sigma^2, photon (1,0), (2,0), (1,1), (2,1)
+        re/im)."""
+        out = np.zeros((self.p.L[dir] // 2 + 1, 10))
+        n = self.lib.ref_correlators(dir, _P(out))
+        return out[:n].copy()
+
+    def block_setup(self, levels):
+        return self.lib.ref_block_setup(levels)
+
+    def blocked_level(self, k, dir):
+        """Smear level k (0 = the lattice itself), move it onto blocked level
+        k+1 and measure its correlators (correlation.c:404-432); returns the
+        correlator rows, the blocked links / triplet in the blocked lattice's
+        storage order, its coordinates and sides."""
+        V, D = self.V, self.p.dim
+        corr = np.zeros((self.p.L[dir] // 2 + 1, 10))
+        link, trip = np.zeros(V * D * 4), np.zeros(V * 3)
+        coords, Lb = np.zeros(V * D, np.int64), np.zeros(4, np.int32)
+        n = self.lib.ref_blocked_level(k, dir, _P(corr), _P(link), _P(trip), _P(coords), _P(Lb))
+        assert n > 0
+        return dict(corr=corr[: self.p.L[dir] // 2].copy(), link=link[: n * D * 4].reshape(n, D, 4).copy(),
+                    trip=trip[: n * 3].reshape(n, 3).copy(), coords=coords[: n * D].reshape(n, D).copy(),
+                    L=Lb[:D].copy())
 
     def tables(self):
         V, D = self.V, self.p.dim

@@ -135,3 +135,37 @@ def test_flow(name):
     step = fields_of(d, p, "step_")
     for k, v in o.get().max_abs_diff(step).items():
         assert v < 1e-13, (k, v)
+
+
+@pytest.mark.parametrize("name", names("correl_"))
+def test_correlators(name):
+    """measure_correlators (correlation.c:350-398) along the longest
+    direction, and on every blocking level the smeared, blocked links and
+    triplet (su2u1.c:752-905, blocking.c:296-374) in the blocked lattice's
+    storage order and the correlators measured there; 1e-12 relative to the
+    largest value of a column (the values are sums of products of plane sums
+    in another order), fields 1e-13."""
+    d = load(name)
+    p = params_of(d)
+    o = Oracle(p)
+    o.put(fields_of(d, p, "in_"))
+    ld = int(d["dir"])
+    assert o.longest_dir() == ld
+    corr_close(o.correlators(ld), d["corr0"])
+    bd = [int(k != ld) for k in range(3)]
+    cur = o
+    for k in range(1, int(d["levels"]) + 1):
+        cur = cur.block(bd)
+        assert list(cur.p.L[:3]) == list(d[f"b{k}_L"])
+        _, _, co, _ = cur.tables()
+        assert np.array_equal(co, d[f"b{k}_coords"])
+        got = cur.get()
+        assert np.max(np.abs(got.link - d[f"b{k}_link"])) < 1e-13
+        assert np.max(np.abs(got.trip - d[f"b{k}_trip"])) < 1e-13
+        corr_close(cur.correlators(ld), d[f"b{k}_corr"])
+
+
+def corr_close(got, want, rtol=1e-12):
+    assert got.shape == want.shape
+    scale = np.max(np.abs(want), axis=0) + 1e-300
+    assert np.all(np.abs(got - want) <= rtol * scale), np.max(np.abs(got - want) / scale, axis=0)
