@@ -18,6 +18,8 @@
  *   init_last_max()            multicanonical.c:826 -> su2gpu_muca_init_last_max
  *   load_lattice()/setfields() field upload      -> su2gpu_upload_fields
  *   save_lattice() field download                -> su2gpu_download_fields
+ *   measure_correlators()      correlation.c:350 -> su2gpu_measure_correlators
+ *   measure_blocked_correlators() correlation.c:404 -> su2gpu_measure_blocked_correlators
  */
 #ifndef SU2GPU_H
 #define SU2GPU_H
@@ -222,6 +224,38 @@ int su2gpu_measure_local(su2gpu_ctx* ctx, double* out);
  * 2 S, 3 S^2; columns of fields the content lacks are 0.  The reference's
  * rows are these sums divided by the plane's area V / L[z_dir]. */
 int su2gpu_measure_z(su2gpu_ctx* ctx, int32_t* z_dir, double* sums);
+/* Columns of the correlators (measure_correlators, correlation.c:350-398),
+ * per distance d: the Higgs correlator H(d) = 4 sum_z h(z) h(z+d) / V with h
+ * the plane sum of |phi|^2 / 2 (first doublet; higgs_correlator, 39-58), the
+ * Sigma^2 correlator (triplet_correlator, 65-83) and photon_correl (257-315)
+ * re/im for (transmom, mode) = (1,0), (2,0), (1,1), (2,1); absent fields 0. */
+enum {
+  SU2GPU_CORR_HIGGS = 0, SU2GPU_CORR_SIGMA2 = 1,
+  SU2GPU_CORR_PHOT10_RE = 2, SU2GPU_CORR_PHOT10_IM = 3, SU2GPU_CORR_PHOT20_RE = 4, SU2GPU_CORR_PHOT20_IM = 5,
+  SU2GPU_CORR_PHOT11_RE = 6, SU2GPU_CORR_PHOT11_IM = 7, SU2GPU_CORR_PHOT21_RE = 8, SU2GPU_CORR_PHOT21_IM = 9,
+  SU2GPU_NCORR = 10
+};
+/* measure_correlators (correlation.c:350-398) along direction dir:
+ * out[d * SU2GPU_NCORR + col] for 0 <= d < L[dir] / 2.  The reference
+ * measures along the longest direction (make_misc_tables, layout.c:773-777,
+ * ties to the last). */
+int su2gpu_measure_correlators(su2gpu_ctx* ctx, int32_t dir, double* out);
+/* measure_blocked_correlators (correlation.c:404-432) for blocking levels
+ * 1..levels: each level smears the previous one in the directions with
+ * block_dir[d] != 0 (smear_link, smear_triplet, su2u1.c:752-852) and keeps
+ * its sites of even coordinate there (make_blocked_fields, blocking.c:296),
+ * halving those sides.  As many levels as max_block_level (blocking.c:17-38)
+ * allows are made, *levels_done of them; out holds their correlators one
+ * level after another, L_k[dir] / 2 rows of SU2GPU_NCORR each.  Contents
+ * with a doublet return SU2GPU_ERR_UNSUPPORTED: the reference has no doublet
+ * smearing and writes no blocked correlators for them. */
+int su2gpu_measure_blocked_correlators(su2gpu_ctx* ctx, int32_t dir, const int32_t* block_dir, int32_t levels,
+                                       double* out, int32_t* levels_done);
+/* The fields of blocking level `level` (0 = the lattice itself) in
+ * lexicographic order of that level (x fastest): sides in Lb[3], links
+ * link[n][3][4], triplet trip[n][3] (either may be NULL). */
+int su2gpu_blocked_fields(su2gpu_ctx* ctx, const int32_t* block_dir, int32_t level, int32_t* Lb, double* link,
+                          double* trip);
 /* su2gpu_grad_flow that also returns measure_local of the flowed fields at
  * every measurement (gradflow.c:81-86, 124-129, 151-156): local holds
  * max_local blocks of V x 2 doubles, filled in measurement order. */

@@ -66,6 +66,9 @@ M_HOP_SIGMA, M_SIGMA2, M_SIGMA4, M_PHI2SIGMA2 = 11, 12, 13, 14
 M_MAGCHARGE, M_MAGCHARGE_ABS = 15, 16
 M_S_COV, M_S1, M_S2, M_S3, M_S4, M_SPHI2, M_S2PHI2 = 17, 18, 19, 20, 21, 22, 23
 NMEAS = 24
+# correlator columns (SU2GPU_CORR_*): Higgs, Sigma^2, photon (1,0), (2,0),
+# (1,1), (2,1) re/im
+NCORR = 10
 
 
 class Params(ctypes.Structure):

@@ -38,6 +38,7 @@ UNITS = [
     ("su2gpu", "su2gpu.cu", []),
     ("su2_noalloc", "su2_noalloc.cu", []),
     ("su2_pool", "su2_pool.cu", []),
+    ("su2_correl", "su2_correl.cu", []),
 ]
 EXTRA_SOURCES = []  # (name, source) of further host units, appended by later modules
 

@@ -4,6 +4,8 @@
 // on the device, measurements, gradient flow and CUDA-graph replay.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstddef>
 #include <cstdarg>
@@ -13,6 +15,7 @@
 #include <vector>
 
 #include "../../include/su2gpu.h"
+#include "su2_correl.h"
 #include "su2_host.h"
 #include "su2_kernels.cuh"
 #include "su2_ops.h"
@@ -108,7 +111,7 @@ struct su2gpu_ctx {
   int launches = 0;               // kernel launches enqueued by the last sweep
   std::vector<cudaEvent_t>* prof = nullptr;  // per-pass events while profiling
   std::vector<int>* prof_kind = nullptr;
-  DevBuf fields, stage, ctrbuf, partials, sums, alpha, backup, muca, flow, rows, local;
+  DevBuf fields, stage, ctrbuf, partials, sums, alpha, backup, muca, flow, rows, local, correl;
   bool borrowed = false;  // fields belong to another allocation (su2gpu_attach)
   Fields<double> f64{};
   Fields<float> f32{};
@@ -299,7 +302,7 @@ int su2gpu_destroy(su2gpu_ctx* c) {
   if (c->borrowed) c->fields.p = nullptr;
   c->fields.release(); c->stage.release(); c->ctrbuf.release(); c->partials.release(); c->sums.release();
   c->alpha.release(); c->backup.release(); c->muca.release(); c->flow.release(); c->rows.release();
-  c->local.release();
+  c->local.release(); c->correl.release();
   if (c->own_st) cudaStreamDestroy(c->own_st);
   delete c;
   return SU2GPU_OK;
@@ -1191,6 +1194,144 @@ int su2gpu_measure_z(su2gpu_ctx* c, int32_t* z_dir, double* sums) {
   CK(cudaMemcpyAsync(sums, c->local.p, (size_t)Lz * 4 * 8, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
   if (z_dir) *z_dir = zd;
+  return SU2GPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// correlators and blocking (correlation.c, blocking.c, su2u1.c:752-905)
+// ---------------------------------------------------------------------------
+// max_block_level (blocking.c:17-38): how many times every blocked direction
+// can be halved without making a side odd or smaller than 2 first
+static int block_levels_possible(const int* L, const int* bd, int want) {
+  int len[3] = {L[0], L[1], L[2]}, count = 0;
+  while (count < want) {
+    for (int d = 0; d < 3; d++)
+      if (bd[d] && (len[d] % 2 != 0 || len[d] <= 2)) return count;
+    for (int d = 0; d < 3; d++)
+      if (bd[d]) len[d] /= 2;
+    count++;
+  }
+  return count;
+}
+
+// The plain lattice of the fields, blocked `levels` times in the directions
+// bd; with out, the correlators along dir of the lattice itself (levels = 0)
+// or of every blocked level, one after another (L_k[dir]/2 rows each); with
+// last, the plain lattice of the last level is left in c->correl for a copy
+// to the host.
+static int correl_run(su2gpu_ctx* c, int dir, const int* bd, int levels, double* out, PlainLat* last) {
+  const int has_phi = c->nh > 0, has_trip = c->has_t;
+  int dev = 0, sm = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev);
+  // sides of every level, then the sizes of the buffers
+  std::vector<std::array<int, 3>> Ls(1, std::array<int, 3>{c->g.L[0], c->g.L[1], c->g.L[2]});
+  for (int k = 1; k <= levels; k++) {
+    std::array<int, 3> n = Ls.back();
+    for (int d = 0; d < 3; d++)
+      if (bd[d]) n[d] /= 2;
+    Ls.push_back(n);
+  }
+  auto vol = [](const std::array<int, 3>& L) { return (int64_t)L[0] * L[1] * L[2]; };
+  const size_t n0 = plain_doubles(c->g.V, has_phi, has_trip);
+  const size_t n1 = levels > 0 ? plain_doubles(vol(Ls[1]), 0, has_trip) : 0;
+  size_t npart = 0, ntot = 0, nout = 0;
+  const int first = levels > 0 ? 1 : 0;
+  for (int k = first; k <= levels; k++) {
+    PlainLat q = make_plain(Ls[k].data(), nullptr, 0, 0);
+    const int Lz = Ls[k][dir];
+    npart = std::max(npart, (size_t)Lz * correl_chunks(q, dir, sm) * NCORR_PLANE);
+    ntot = std::max(ntot, (size_t)Lz * NCORR_PLANE);
+    nout += (size_t)(Lz / 2) * NCORR;
+  }
+  int rc = c->correl.ensure((n0 + 2 * n1 + npart + ntot + nout) * sizeof(double));
+  if (rc) return rc;
+  double* base = (double*)c->correl.p;
+  double *ping[2] = {base + n0, base + n0 + n1}, *part = base + n0 + 2 * n1, *tot = part + npart, *dout = tot + ntot;
+  PlainLat cur = make_plain(Ls[0].data(), base, has_phi, has_trip);
+  launch_to_plain(c->prec, c->F(), c->g, has_phi, has_trip, cur, c->st);
+  CKL();
+  const double sqb = sqrt(c->p.betasu2);
+  double* o = dout;
+  if (out && levels == 0) {
+    launch_correlators(cur, dir, has_phi, has_trip, sqb, correl_chunks(cur, dir, sm), part, tot, o, c->st);
+    CKL();
+    o += (size_t)(Ls[0][dir] / 2) * NCORR;
+  }
+  for (int k = 1; k <= levels; k++) {
+    PlainLat nxt = make_plain(Ls[k].data(), ping[(k - 1) & 1], 0, has_trip);
+    launch_block(cur, nxt, bd, has_trip, c->st);
+    CKL();
+    cur = nxt;
+    if (out) {
+      launch_correlators(cur, dir, 0, has_trip, sqb, correl_chunks(cur, dir, sm), part, tot, o, c->st);
+      CKL();
+      o += (size_t)(Ls[k][dir] / 2) * NCORR;
+    }
+  }
+  if (out) CK(cudaMemcpyAsync(out, dout, (size_t)(o - dout) * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (last) *last = cur;
+  return SU2GPU_OK;
+}
+
+static int check_block_dir(su2gpu_ctx* c, const int32_t* block_dir, int* bd) {
+  int any = 0;
+  for (int d = 0; d < 3; d++) {
+    bd[d] = block_dir[d] ? 1 : 0;
+    any |= bd[d];
+  }
+  if (!any) {
+    set_err("no blocked direction");
+    return SU2GPU_ERR_INVALID;
+  }
+  (void)c;
+  return SU2GPU_OK;
+}
+
+int su2gpu_measure_correlators(su2gpu_ctx* c, int32_t dir, double* out) {
+  if (!c || !out || dir < 0 || dir > 2) return SU2GPU_ERR_INVALID;
+  return correl_run(c, dir, nullptr, 0, out, nullptr);
+}
+
+int su2gpu_measure_blocked_correlators(su2gpu_ctx* c, int32_t dir, const int32_t* block_dir, int32_t levels,
+                                       double* out, int32_t* levels_done) {
+  if (!c || !out || !block_dir || dir < 0 || dir > 2 || levels < 0) return SU2GPU_ERR_INVALID;
+  if (c->nh > 0) {
+    // measure_blocked_correlators (correlation.c:414-418) has no doublet smearing
+    set_err("blocked correlators with a doublet: the reference's Higgs smearing is not implemented");
+    return SU2GPU_ERR_UNSUPPORTED;
+  }
+  int bd[3];
+  int rc = check_block_dir(c, block_dir, bd);
+  if (rc) return rc;
+  const int n = block_levels_possible(c->g.L, bd, levels);
+  if (levels_done) *levels_done = n;
+  if (n == 0) return SU2GPU_OK;
+  return correl_run(c, dir, bd, n, out, nullptr);
+}
+
+int su2gpu_blocked_fields(su2gpu_ctx* c, const int32_t* block_dir, int32_t level, int32_t* Lb, double* link,
+                          double* trip) {
+  if (!c || !block_dir || !Lb || level < 0) return SU2GPU_ERR_INVALID;
+  int bd[3];
+  int rc = check_block_dir(c, block_dir, bd);
+  if (rc) return rc;
+  if (block_levels_possible(c->g.L, bd, level) < level) {
+    set_err("the lattice cannot be blocked %d times", level);
+    return SU2GPU_ERR_INVALID;
+  }
+  PlainLat q;
+  if ((rc = correl_run(c, 0, bd, level, nullptr, &q))) return rc;
+  for (int d = 0; d < 3; d++) Lb[d] = q.L[d];
+  const size_t V = (size_t)q.V;
+  std::vector<double> h(V * 15);
+  CK(cudaMemcpy(h.data(), q.link, V * 12 * sizeof(double), cudaMemcpyDeviceToHost));
+  if (trip && q.trip) CK(cudaMemcpy(h.data() + V * 12, q.trip, V * 3 * sizeof(double), cudaMemcpyDeviceToHost));
+  for (size_t n = 0; n < V; n++) {
+    for (int k = 0; link && k < 12; k++) link[n * 12 + k] = h[(size_t)k * V + n];
+    for (int k = 0; trip && q.trip && k < 3; k++) trip[n * 3 + k] = h[(size_t)(12 + k) * V + n];
+  }
   return SU2GPU_OK;
 }
 

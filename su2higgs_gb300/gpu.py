@@ -66,6 +66,9 @@ def lib():
         L.su2gpu_set_stream.argtypes = [vp, vp]
         L.su2gpu_set_random_sweeps.argtypes = [vp, i32]
         L.su2gpu_clone.argtypes = [vp, u64, u32, ctypes.POINTER(vp)]
+        L.su2gpu_measure_correlators.argtypes = [vp, i32, vp]
+        L.su2gpu_measure_blocked_correlators.argtypes = [vp, i32, vp, i32, vp, ctypes.POINTER(i32)]
+        L.su2gpu_blocked_fields.argtypes = [vp, vp, i32, vp, vp, vp]
         L.su2gpu_copy_fields.argtypes = [vp, vp]
         L.su2gpu_sweep_order.argtypes = [u64, u32, u32, i32, i32, vp, vp, vp]
         L.su2gpu_enqueue_sweeps.argtypes = [vp, u32, i32, i32]
@@ -278,6 +281,58 @@ class Lattice:
         out = np.zeros((max(self.params.L[:3]), 4))
         check(lib().su2gpu_measure_z(self._h, ctypes.byref(zd), _p(out)))
         return zd.value, out[: self.params.L[zd.value]].copy()
+
+    def longest_dir(self):
+        """The direction the reference measures correlators along
+        (make_misc_tables, layout.c:773-777): the longest, ties to the last."""
+        L = self.params.L
+        ld = 2
+        for d in (2, 1, 0):
+            if L[d] > L[ld]:
+                ld = d
+        return ld
+
+    def measure_correlators(self, dir=None):
+        """measure_correlators (correlation.c:350-398): rows d < L[dir]/2 of
+        abi.NCORR values."""
+        dir = self.longest_dir() if dir is None else dir
+        out = np.zeros((self.params.L[dir] // 2, abi.NCORR))
+        check(lib().su2gpu_measure_correlators(self._h, dir, _p(out)))
+        return out
+
+    def _block_sides(self, block_dir, levels):
+        sides = [tuple(self.params.L[:3])]
+        for _ in range(levels):
+            sides.append(tuple(n // 2 if b else n for n, b in zip(sides[-1], block_dir)))
+        return sides
+
+    def measure_blocked_correlators(self, block_dir, levels, dir=None):
+        """Correlators of blocking levels 1..levels (as many as the sides
+        allow): a list with one (L_k[dir]/2, NCORR) array per level made."""
+        dir = self.longest_dir() if dir is None else dir
+        bd = np.ascontiguousarray(block_dir, dtype=np.int32)
+        sides = self._block_sides(bd, levels)
+        out = np.zeros((sum(s[dir] // 2 for s in sides[1:]) + 1, abi.NCORR))
+        done = ctypes.c_int32()
+        check(lib().su2gpu_measure_blocked_correlators(self._h, dir, _p(bd), levels, _p(out), ctypes.byref(done)))
+        res, r = [], 0
+        for s in sides[1: 1 + done.value]:
+            res.append(out[r: r + s[dir] // 2].copy())
+            r += s[dir] // 2
+        return res
+
+    def blocked_fields(self, block_dir, level):
+        """Fields of blocking level `level` in its lexicographic order:
+        (sides, links (n, 3, 4), triplet (n, 3) or None)."""
+        bd = np.ascontiguousarray(block_dir, dtype=np.int32)
+        s = self._block_sides(bd, level)[-1]
+        n = s[0] * s[1] * s[2]
+        Lb = np.zeros(3, np.int32)
+        link = np.zeros((n, 3, 4))
+        trip = np.zeros((n, 3)) if self.params.content & abi.TRIPLET else None
+        check(lib().su2gpu_blocked_fields(self._h, _p(bd), level, _p(Lb), _p(link), _p(trip)))
+        assert tuple(Lb) == s
+        return s, link, trip
 
     def grad_flow_local(self, t_max, dt, meas_interval, maxrows=None):
         """grad_flow plus measure_local of the flowed fields at every

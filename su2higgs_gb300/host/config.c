@@ -100,17 +100,18 @@ static int opt_int(const char* fname, const char* label, int dflt) {
  * -DSINGLET, -DU1, -DGRADFLOW; default Makefile:12 = NHIGGS=1 SINGLET U1).
  * Here the optional keys nhiggs/triplet/singlet/u1/gradflow select it; the
  * environment variable SU2_CONTENT (a name: pure, fund, adj, su2u1s, fundadj,
- * higgs2, optionally +gradflow, +measure_z and +hb_trajectory) is applied
- * before them. */
+ * higgs2, optionally +gradflow, +measure_z, +hb_trajectory, +correlators
+ * and +blocking) is applied before them. */
 static void read_content(const char* fname, host_params* hp) {
   hp->nhiggs = 1; hp->triplet = 0; hp->singlet = 1; hp->u1 = 1; hp->gradflow = 0; hp->measure_z = 0;
-  hp->hb_trajectory = 0;
+  hp->hb_trajectory = 0; hp->correlators = 0; hp->blocking = 0;
   const char* env = getenv("SU2_CONTENT");
   if (env && *env) {
     char name[64];
     snprintf(name, sizeof(name), "%s", env);
     /* modifiers after the name: +gradflow (-DGRADFLOW), +measure_z
-     * (-DMEASURE_Z), +hb_trajectory (-DHB_TRAJECTORY) */
+     * (-DMEASURE_Z), +hb_trajectory (-DHB_TRAJECTORY), +correlators
+     * (-DCORRELATORS), +blocking (-DBLOCKING) */
     char* plus = strchr(name, '+');
     if (plus) {
       *plus = 0;
@@ -121,6 +122,8 @@ static void read_content(const char* fname, host_params* hp) {
         if (!strcasecmp(tok, "gradflow")) hp->gradflow = 1;
         else if (!strcasecmp(tok, "measure_z")) hp->measure_z = 1;
         else if (!strcasecmp(tok, "hb_trajectory")) hp->hb_trajectory = 1;
+        else if (!strcasecmp(tok, "correlators")) hp->correlators = 1;
+        else if (!strcasecmp(tok, "blocking")) hp->blocking = 1;
         else { printf("!!! Unknown SU2_CONTENT modifier %s\n", tok); die(2); }
         tok = next;
       }
@@ -140,6 +143,8 @@ static void read_content(const char* fname, host_params* hp) {
   hp->gradflow = opt_int(fname, "gradflow", hp->gradflow);
   hp->measure_z = opt_int(fname, "measure_z", hp->measure_z);
   hp->hb_trajectory = opt_int(fname, "hb_trajectory", hp->hb_trajectory);
+  hp->correlators = opt_int(fname, "correlators", hp->correlators);
+  hp->blocking = opt_int(fname, "blocking", hp->blocking);
 }
 
 void read_parameters(const char* fname, host_params* hp) {
@@ -253,6 +258,12 @@ void read_parameters(const char* fname, host_params* hp) {
     p->lam7_im = cfg_get_double(f, "lam7_im");
   }
   hp->do_trajectory = hp->hb_trajectory ? cfg_get_int(f, "do_trajectory") : 0; /* parameters.c:319-321 */
+  /* parameters.c:310-317 */
+  if (hp->correlators) {
+    hp->do_correlators = cfg_get_int(f, "do_correlators");
+    hp->correlator_interval = cfg_get_int(f, "correlator_interval");
+  }
+  if (hp->blocking) hp->blocks = cfg_get_int(f, "blocks");
   if (hp->gradflow) {
     hp->do_flow = cfg_get_int(f, "do_flow");
     hp->flow_interval = cfg_get_int(f, "flow_interval");

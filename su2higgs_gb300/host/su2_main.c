@@ -12,7 +12,9 @@
  * the weight read-only after a reset, then per iteration measure (every
  * `interval`), flow (every `flow_interval`), heatbath trajectories (every
  * `mode_interval` of realtime_config, -DHB_TRAJECTORY builds: content
- * modifier +hb_trajectory), update, checkpoint.  All field
+ * modifier +hb_trajectory), correlators (every `correlator_interval`,
+ * -DCORRELATORS / -DBLOCKING: modifiers +correlators, +blocking), update,
+ * checkpoint.  All field
  * updates, measurements and flows run on the GPU through libsu2gpu; runs of
  * iterations without host work in between are replayed as one CUDA graph.
  */
@@ -112,6 +114,52 @@ int main(int argc, char** argv) {
 
   host_muca hm;
   read_weight_parameters(cfg, &hp, &hm);
+
+  /* main.c:98-157: correlators along the longest direction (ties to the
+   * last, make_misc_tables layout.c:773-777); blocking in all the others */
+  int corr_dir = hp.p.dim - 1;
+  for (int d = hp.p.dim - 1; d >= 0; d--)
+    if (hp.p.L[d] > hp.p.L[corr_dir]) corr_dir = d;
+  const int docorr = hp.correlators && hp.do_correlators && hp.correlator_interval > 0;
+  if (hp.correlators && hp.do_correlators) {
+    print_labels_correlators(&hp);
+    printf("\nMeasuring correlation functions along direction %d every %d iterations\n", corr_dir + 1,
+           hp.correlator_interval);
+  }
+  int32_t block_dir[3] = {0, 0, 0};
+  int block_levels = 0;
+  if (hp.blocking) {
+    block_levels = hp.blocks;
+    printf("\n--- Using blocking in directions: ");
+    for (int d = 0; d < hp.p.dim; d++)
+      if (d != corr_dir) {
+        block_dir[d] = 1;
+        printf("%d ", d);
+      }
+    printf(", up to %d levels ---\n", block_levels);
+    /* max_block_level (blocking.c:17-38) */
+    int len[3] = {hp.p.L[0], hp.p.L[1], hp.p.L[2]}, mx = 0, ok = 1;
+    while (ok && mx < 64) {
+      for (int d = 0; d < 3 && ok; d++)
+        if (block_dir[d] && (len[d] % 2 != 0 || len[d] <= 2)) ok = 0;
+      if (!ok) break;
+      for (int d = 0; d < 3; d++)
+        if (block_dir[d]) len[d] /= 2;
+      mx++;
+    }
+    if (mx < block_levels) {
+      printf("Warning: unable to block to %d levels; max is %d. Using %d levels instead.\n", block_levels, mx, mx);
+      block_levels = mx;
+    }
+    int bl[3] = {hp.p.L[0], hp.p.L[1], hp.p.L[2]};
+    for (int k = 0; k < block_levels; k++) {
+      for (int d = 0; d < 3; d++)
+        if (block_dir[d]) bl[d] /= 2;
+      printf("Initializing blocked lattice of volume: %d x %d x %d (MPI size = 1)\n", bl[0], bl[1], bl[2]);
+    }
+    printf("--- Blocking structs ready ---\n\n");
+    fflush(stdout);
+  }
 
   if (files_only) return files_roundtrip(&hp, &hm);
 
@@ -227,6 +275,7 @@ int main(int argc, char** argv) {
   double tstart = wall();
   int flow_id = 1;
   int traj_id = 1;
+  int correlator_id = 1;
   int nmeas = 1 + SU2GPU_NMEAS;
   while (iter <= hp.iterations) {
     if (hp.interval > 0 && iter % hp.interval == 0) {
@@ -292,12 +341,37 @@ int main(int argc, char** argv) {
       GPU(make_realtime_trajectories(ctx, &hp, &w, &traj, traj_id, seed, NULL));
       traj_id++;
     }
+    /* main.c:330-349 */
+    if (docorr && iter % hp.correlator_interval == 0) {
+      const int nr = hp.p.L[corr_dir] / 2;
+      double* crows = (double*)malloc(sizeof(double) * (size_t)(nr > 0 ? nr : 1) * SU2GPU_NCORR *
+                                      (size_t)(block_levels + 1));
+      GPU(su2gpu_measure_correlators(ctx, corr_dir, crows));
+      write_correlators("correl0", &hp, correlator_id, crows, nr);
+      if (block_levels > 0) {
+        if (hp.nhiggs > 0) {
+          /* measure_blocked_correlators (correlation.c:414-418) */
+          for (int k = 0; k < block_levels; k++) printf("Error in correlation.c: Higgs smearing not yet implemented!!!\n");
+        } else {
+          int32_t done = 0;
+          GPU(su2gpu_measure_blocked_correlators(ctx, corr_dir, block_dir, block_levels, crows, &done));
+          for (int k = 0; k < done; k++) {
+            char fname[100];
+            snprintf(fname, sizeof(fname), "correl%d", k + 1);
+            write_correlators(fname, &hp, correlator_id, crows + (size_t)k * nr * SU2GPU_NCORR, nr);
+          }
+        }
+      }
+      free(crows);
+      correlator_id++;
+    }
     /* iterations up to the next host event run back to back */
     long n = 1;
     while (iter + n <= hp.iterations && (hp.interval <= 0 || (iter + n) % hp.interval != 0) &&
            !(hp.gradflow && hp.do_flow && hp.flow_interval > 0 && (iter + n) % hp.flow_interval == 0) &&
            !(zmeas && (iter + n) % hp.meas_interval_z == 0) &&
            !(dotraj && (iter + n) % traj.mode_interval == 0) &&
+           !(docorr && (iter + n) % hp.correlator_interval == 0) &&
            (hp.checkpoint <= 0 || (iter + n - 1) % hp.checkpoint != 0) && n < 1000000)
       n++;
     GPU(su2gpu_run_sweeps(ctx, sweep, (int32_t)n, hp.use_graph));

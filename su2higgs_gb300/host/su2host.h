@@ -29,6 +29,8 @@ typedef struct {
   long meas_interval_z;
   /* heatbath real-time trajectories (the reference's -DHB_TRAJECTORY build) */
   int hb_trajectory, do_trajectory;
+  /* correlators and blocking (-DCORRELATORS, -DBLOCKING) */
+  int correlators, blocking, do_correlators, correlator_interval, blocks;
   /* additions of this implementation (optional keys) */
   uint64_t seed;
   int have_seed;
@@ -89,6 +91,14 @@ void save_weight(const su2gpu_weight* w);
 void linearize_weight(su2gpu_weight* w);
 double get_weight(const su2gpu_weight* w, double val);
 void print_acceptance(const host_params* hp, const int64_t* c);
+
+/* correl.c */
+/* print_labels_correlators (correlation.c:320-346): labels_correl */
+void print_labels_correlators(const host_params* hp);
+/* one measure_correlators block (correlation.c:350-398) appended to fname:
+ * the header with meas_id, then per distance d < nrows the values of
+ * rows[d * SU2GPU_NCORR + col] the content has */
+void write_correlators(const char* fname, const host_params* hp, int meas_id, const double* rows, int nrows);
 
 /* trajectory.c */
 void read_realtime_config(const char* fname, host_traj* t);

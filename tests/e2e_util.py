@@ -9,7 +9,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 BIN = os.path.join(ROOT, "bin", "su2")
-CASES = ("fund", "adj", "su2u1s", "fund_muca", "su2u1s_z", "fundadj_z", "fund_traj")
+CASES = ("fund", "adj", "su2u1s", "fund_muca", "su2u1s_z", "fundadj_z", "fund_traj", "adj_corr", "fundadj_corr")
 
 
 def ensure_binary():

@@ -30,6 +30,11 @@ directories and stores, per case, in e2e_<case>.npz:
                 the loaded configuration (hb_trajectory.c:10-94), in a band of
                 +-1e-4 around its order parameter so that every trajectory
                 ends after one sweep
+  labels_correl, correl0, correl1
+                (the _corr cases, -DCORRELATORS -DBLOCKING builds) the
+                correlator labels and the first correlator blocks of the
+                loaded configuration, of the lattice itself and of its
+                blocking levels (correlation.c:320-432)
   in_<name>     further input files of the case (flat read-only weight,
                 realtime_config), written next to the config before the run
   bin_content   the --content argument that makes bin/su2 the same program
@@ -74,6 +79,12 @@ CASES = {
     "fund_traj": ("fundt", "fund", "fund+hb_trajectory", {"do_flow": 0, "multicanonical": 1, "muca_mode": 0,
                                                           "bins": 20, "min": 0.0, "max": 1.2, "orderparam": "phisq",
                                                           "do_trajectory": 1}),
+    # correlators along the longest direction, blocked once (6x4x8 -> 3x2x8);
+    # with a doublet the reference writes no blocked correlators
+    "adj_corr": ("adjc", "adj", "adj+correlators+blocking", {"do_flow": 0, "do_correlators": 1,
+                                                             "correlator_interval": 1, "blocks": 2}),
+    "fundadj_corr": ("fundadjc", "fundadj", "fundadj+correlators+blocking",
+                     {"do_flow": 0, "do_correlators": 1, "correlator_interval": 1, "blocks": 2}),
 }
 
 TRAJ_BAND = 1e-4
@@ -154,7 +165,8 @@ def run_ref(content, config, lattice, extra=None):
         out = {}
         for name in sorted(os.listdir(d)):
             if name in ("labels", "measure", "measure_flow", "lattice", "weight", "labels_local", "labels_z",
-                        "measure_z", "trajectory") or name.startswith("measure_local_"):
+                        "measure_z", "trajectory", "labels_correl") or name.startswith("measure_local_") \
+                    or name.startswith("correl"):
                 out[name] = open(os.path.join(d, name), "rb").read()
         return out
     finally:
@@ -181,7 +193,8 @@ def main(only=None):
         for name, data in extra.items():
             rec["in_" + name] = np.frombuffer(data, dtype=np.uint8)
         for name, data in got.items():
-            if name in ("labels_local", "labels_z", "measure_z", "trajectory") or name.startswith("measure_local_"):
+            if name in ("labels_local", "labels_z", "measure_z", "trajectory", "labels_correl") or \
+                    name.startswith("measure_local_") or name.startswith("correl"):
                 rec[name] = np.frombuffer(data, dtype=np.uint8)
         got0 = run_ref(binary, set_key(config, "iterations", 0), lat, extra)
         rec["lattice_out0"] = np.frombuffer(got0["lattice"], dtype=np.uint8)

@@ -138,3 +138,26 @@ def test_trajectories_match_reference(binary, precision, tol, tmp_path):
                 assert len(va.split(".")[1]) == 8
     assert starts == n
     compare_rows(rows(E.read(d, "measure")), rows(g["measure"]), 1e-6 if precision == 64 else 1e-4, 1e-5)
+
+
+@pytest.mark.parametrize("precision,rtol,atol", [(64, 1e-6, 1e-12), (32, 1e-4, 1e-5)])
+@pytest.mark.parametrize("case", ["adj_corr", "fundadj_corr"])
+def test_first_correlators_match_reference(binary, case, precision, rtol, atol, tmp_path):
+    """Correlators (the reference's -DCORRELATORS -DBLOCKING build):
+    labels_correl byte for byte; the first correl0 block -- of the loaded
+    configuration, before the first update -- and, without a doublet, the
+    first correl1 block of the blocked lattice (6x4x8 -> 3x2x8) value by
+    value; with a doublet no blocked file, as the reference writes none."""
+    d = str(tmp_path)
+    g = E.stage(case, d)
+    E.run(d, g["bin_content"], "--precision", str(precision), "--seed", "7")
+    assert E.read(d, "labels_correl") == g["labels_correl"]
+    for name in ("correl0", "correl1"):
+        if name in g:
+            got, want = rows(E.read(d, name)), rows(g[name])
+            # photon columns whose value is 0 up to rounding (imaginary parts at
+            # distance 0) are compared against the column's scale
+            compare_rows(got, want, rtol, atol if precision == 64 else 1e-3)
+        else:
+            import os
+            assert not os.path.exists(os.path.join(d, name))

@@ -19,7 +19,7 @@ def test_labels_lattice_weight_roundtrip(binary, case, tmp_path):
     g = E.stage(case, str(tmp_path))
     E.run(str(tmp_path), g["bin_content"], "--files-only")
     assert E.read(str(tmp_path), "labels") == g["labels"]
-    for extra in ("labels_local", "labels_z"):
+    for extra in ("labels_local", "labels_z", "labels_correl"):
         if extra in g:
             assert E.read(str(tmp_path), extra) == g[extra]
     assert E.lattice_equal(E.read(str(tmp_path), "lattice"), g["lattice_out0"])
