@@ -145,7 +145,7 @@ MUCA_CASES = {
     "adj_sigmasq_fast": ("adj", "Sigmasq", 1, 1, 12),
     "fundadj_p2ms2": ("fundadj", "phi2minusSigma2", 1, 2, 3),
     # two doublets, the order parameter on the second one (PHI2SQ)
-    "higgs2_phi2sq_fast": ("higgs2", "phi2sq", 1, 2, 3),
+    "higgs2_phi2sq_fast": ("higgs2", "phi2sq", 1, 2, 2),
 }
 
 
