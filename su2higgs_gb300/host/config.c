@@ -284,6 +284,8 @@ void read_parameters(const char* fname, host_params* hp) {
   p->precision = opt_int(fname, "precision", 64);
   p->reunitarize_interval = opt_int(fname, "reunitarize_interval", 10);
   hp->use_graph = opt_int(fname, "gpu_graph", 1);
+  hp->file_ranks = 1;
+  hp->lattice_mpi_size = opt_int(fname, "lattice_mpi_size", 0);
   char v[LINELEN];
   if (cfg_optional_string(fname, "seed", v)) {
     hp->seed = strtoull(v, NULL, 10);

@@ -32,14 +32,108 @@ static int64_t volume(const host_params* hp) {
   return v;
 }
 
+/* The order in which an N-rank run of the reference writes the sites of a
+ * field (write_field, checkpoint.c:226-269): rank 0's sites, then rank 1's,
+ * ...; a rank's sites in its storage order -- lexicographic in its slice,
+ * then EVEN (by the global coordinate sum) before ODD, stably (sitemap,
+ * layout.c:233-402; set_parity 410-450; paritymap 826-851).  The slicing
+ * follows make_slices (layout.c:112-225): the rank count is factorised into
+ * primes up to 29 and, from the largest prime down, each factor divides the
+ * longest side it divides (the first such direction on ties); rank r sits at
+ * the node coordinates of r in the grid of slices, x fastest.
+ * order[k] = lexicographic index (x fastest) of the k-th site of the file.
+ * Returns 0, or -1 when the lattice cannot be sliced that way. */
+int mpi_file_order(int dim, const int* L, int nranks, int64_t* order) {
+  static const int prime[10] = {2, 3, 5, 7, 11, 13, 17, 19, 23, 29};
+  int nf[10] = {0}, rest = nranks;
+  int64_t vol = 1;
+  for (int d = 0; d < dim; d++) vol *= L[d];
+  if (nranks < 1 || vol % nranks != 0) return -1;
+  for (int n = 0; n < 10; n++)
+    while (rest % prime[n] == 0) { rest /= prime[n]; nf[n]++; }
+  if (rest != 1) return -1;
+  int64_t slice[8];
+  int nsl[8];
+  for (int d = 0; d < dim; d++) { slice[d] = L[d]; nsl[d] = 1; }
+  for (int n = 9; n >= 0; n--)
+    for (int f = 0; f < nf[n]; f++) {
+      int64_t largest = 1;
+      for (int d = 0; d < dim; d++)
+        if (slice[d] > largest && slice[d] % prime[n] == 0) largest = slice[d];
+      if (largest == 1) return -1; /* no side divisible by this prime */
+      for (int d = 0; d < dim; d++)
+        if (slice[d] == largest) { slice[d] /= prime[n]; nsl[d] *= prime[n]; break; }
+    }
+  int64_t per = 1;
+  for (int d = 0; d < dim; d++) per *= slice[d];
+  int64_t k = 0;
+  for (int r = 0; r < nranks; r++) {
+    int64_t node[8], rr = r;
+    for (int d = 0; d < dim; d++) { node[d] = rr % nsl[d]; rr /= nsl[d]; }
+    for (int par = 0; par <= 1; par++)
+      for (int64_t j = 0; j < per; j++) {
+        int64_t x[8], jj = j, sum = 0, n = 0, stride = 1;
+        for (int d = 0; d < dim; d++) {
+          x[d] = node[d] * slice[d] + jj % slice[d];
+          jj /= slice[d];
+          sum += x[d];
+        }
+        if ((int)(sum & 1) != par) continue;
+        for (int d = 0; d < dim; d++) { n += x[d] * stride; stride *= L[d]; }
+        order[k++] = n;
+      }
+  }
+  return k == vol ? 0 : -1;
+}
+
+/* storage index of the serial layout (layout.c:657-704: lexicographic, then
+ * EVEN-first, stably) of every lexicographic index */
+static void serial_index(const host_params* hp, int64_t* idx) {
+  int64_t V = volume(hp), neven = 0;
+  for (int pass = 0; pass < 2; pass++) {
+    int64_t k = pass ? neven : 0;
+    for (int64_t n = 0; n < V; n++) {
+      int64_t r = n, sum = 0;
+      for (int d = 0; d < hp->p.dim; d++) { sum += r % hp->p.L[d]; r /= hp->p.L[d]; }
+      if ((int)(sum & 1) != pass) continue;
+      idx[n] = k++;
+    }
+    if (!pass) neven = k;
+  }
+}
+
+/* file position -> storage index of this program's arrays, for a file
+ * written by `ranks` ranks */
+static int64_t* file_to_storage(const host_params* hp, int ranks) {
+  int64_t V = volume(hp);
+  int64_t* ord = (int64_t*)malloc(sizeof(int64_t) * (size_t)V);
+  int64_t* ser = (int64_t*)malloc(sizeof(int64_t) * (size_t)V);
+  if (mpi_file_order(hp->p.dim, hp->p.L, ranks, ord)) {
+    free(ord);
+    free(ser);
+    return NULL;
+  }
+  serial_index(hp, ser);
+  for (int64_t k = 0; k < V; k++) ord[k] = ser[ord[k]];
+  free(ser);
+  return ord;
+}
+
 int save_lattice(const char* fname, const host_params* hp, long iter, double total_time, double comms_time,
                  double* const* arrays) {
+  int size = hp->lattice_mpi_size > 0 ? hp->lattice_mpi_size : (hp->file_ranks > 0 ? hp->file_ranks : 1);
+  int64_t* map = NULL;
+  if (size > 1 && !(map = file_to_storage(hp, size))) {
+    printf("!!! Cannot lay the lattice out for %d MPI ranks; writing it for 1\n", size);
+    size = 1;
+  }
   FILE* f = fopen(fname, "wb");
   if (!f) {
     printf("!!! Unable to open %s for writing\n", fname);
+    free(map);
     return -1;
   }
-  int size = 1, dim = hp->p.dim;
+  int dim = hp->p.dim;
   fwrite(&size, sizeof(int), 1, f);
   fwrite(&dim, sizeof(int), 1, f);
   fwrite(hp->p.L, sizeof(int), dim, f);
@@ -49,14 +143,23 @@ int save_lattice(const char* fname, const host_params* hp, long iter, double tot
   int64_t V = volume(hp);
   for (int k = 0; k < 6; k++) {
     int64_t n = field_count(hp, k);
-    if (n) fwrite(arrays[k], sizeof(double), (size_t)(V * n), f);
+    if (!n) continue;
+    if (!map) {
+      fwrite(arrays[k], sizeof(double), (size_t)(V * n), f);
+      continue;
+    }
+    double* buf = (double*)malloc(sizeof(double) * (size_t)(V * n));
+    for (int64_t q = 0; q < V; q++) memcpy(buf + q * n, arrays[k] + map[q] * n, sizeof(double) * (size_t)n);
+    fwrite(buf, sizeof(double), (size_t)(V * n), f);
+    free(buf);
   }
   fclose(f);
+  free(map);
   printf("Wrote fields to %s.\n", fname);
   return 0;
 }
 
-int load_lattice(const char* fname, const host_params* hp, long* iter, double* total_time, double* comms_time,
+int load_lattice(const char* fname, host_params* hp, long* iter, double* total_time, double* comms_time,
                  double** arrays) {
   FILE* f = fopen(fname, "rb");
   if (!f) return -1;
@@ -70,9 +173,13 @@ int load_lattice(const char* fname, const host_params* hp, long* iter, double* t
     printf("Error reading latticefile!\n");
     die(500);
   }
-  int ok = (dim == hp->p.dim && size == 1);
+  /* load_lattice (checkpoint.c:131-214) demands the run's own MPI size; a
+   * file of any rank count is read here, in that count's layout */
+  int64_t* map = NULL;
+  int ok = (dim == hp->p.dim && size >= 1);
   for (int d = 0; ok && d < dim; d++)
     if (L[d] != hp->p.L[d]) ok = 0;
+  if (ok && size > 1 && !(map = file_to_storage(hp, size))) ok = 0;
   if (!ok) {
     printf("Dimensions in latticefile do not match! Got:\n");
     printf(" \tMPI size %d, dimension %d, volume ", size, dim);
@@ -83,6 +190,8 @@ int load_lattice(const char* fname, const host_params* hp, long* iter, double* t
     printf("\b\b \b\n");
     die(501);
   }
+  if (size > 1) printf("Lattice file written by %d MPI ranks: reading it in their layout.\n", size);
+  hp->file_ranks = size;
   rd = 0;
   rd += (int)fread(iter, sizeof(long), 1, f);
   rd += (int)fread(total_time, sizeof(double), 1, f);
@@ -92,12 +201,18 @@ int load_lattice(const char* fname, const host_params* hp, long* iter, double* t
     int64_t n = field_count(hp, k);
     if (!n) continue;
     size_t want = (size_t)(V * n);
-    if (fread(arrays[k], sizeof(double), want, f) != want) {
+    double* dst = map ? (double*)malloc(sizeof(double) * want) : arrays[k];
+    if (fread(dst, sizeof(double), want, f) != want) {
       printf("Error reading field!\n");
       die(505);
     }
+    if (map) {
+      for (int64_t q = 0; q < V; q++) memcpy(arrays[k] + map[q] * n, dst + q * n, sizeof(double) * (size_t)n);
+      free(dst);
+    }
   }
   fclose(f);
+  free(map);
   return 0;
 }
 

@@ -29,6 +29,10 @@ typedef struct {
   long meas_interval_z;
   /* heatbath real-time trajectories (the reference's -DHB_TRAJECTORY build) */
   int hb_trajectory, do_trajectory;
+  /* rank count of the lattice file layout: file_ranks as read (1 for a new
+   * lattice), lattice_mpi_size the optional key that sets the layout written
+   * (0 = as read) */
+  int file_ranks, lattice_mpi_size;
   /* correlators and blocking (-DCORRELATORS, -DBLOCKING) */
   int correlators, blocking, do_correlators, correlator_interval, blocks;
   /* additions of this implementation (optional keys) */
@@ -68,9 +72,13 @@ void die(int code);
 
 /* files.c */
 int64_t field_count(const host_params* hp, int which); /* doubles per field array */
+/* site order of the lattice file of an nranks-rank run of the reference:
+ * order[k] = lexicographic index of the k-th site; 0, or -1 if the reference
+ * could not lay the lattice out on that many ranks */
+int mpi_file_order(int dim, const int* L, int nranks, int64_t* order);
 int save_lattice(const char* fname, const host_params* hp, long iter, double total_time, double comms_time,
                  double* const* arrays);
-int load_lattice(const char* fname, const host_params* hp, long* iter, double* total_time, double* comms_time,
+int load_lattice(const char* fname, host_params* hp, long* iter, double* total_time, double* comms_time,
                  double** arrays);
 void print_labels(const host_params* hp);
 void print_labels_local(const host_params* hp, const char* fname);

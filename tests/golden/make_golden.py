@@ -10,6 +10,9 @@ Every fixture stores its inputs, so the tests never regenerate them:
                          update_lattice() (update.c:270) with the Philox stream
   muca_<case>.npz        the same with multicanonical global accept/reject
   flow_<case>.npz        grad_flow() (gradflow.c:46) measurement rows
+  mpi_layout.npz         the order in which N-rank runs write the sites of a
+                         lattice file (write_field, checkpoint.c:226-269), from
+                         the reference's MPI layout code (layout.c with -DMPI)
   correl_<case>.npz      measure_correlators() values (correlation.c:350-398) of
                          a hot lattice along the longest direction, and for
                          each blocking level (smear_fields + make_blocked_fields,
@@ -262,10 +265,38 @@ def gen_correl(name):
     np.savez_compressed(os.path.join(HERE, f"correl_{name}.npz"), **out)
 
 
+MPI_LAYOUTS = [((6, 4, 8), n) for n in (2, 3, 4, 6, 8, 12, 16)] + [((8, 8, 8), 4), ((10, 6, 12), 15),
+                                                                   ((16, 8, 12), 12)]
+
+
+def gen_mpi_layout():
+    import ctypes
+    lib = ctypes.CDLL(os.path.join(os.path.dirname(os.path.dirname(HERE)), "oracle", "_ref", "libref_mpilayout.so"))
+    lib.ref_mpi_rank_sites.restype = ctypes.c_long
+    out = {}
+    for L, n in MPI_LAYOUTS:
+        V = int(np.prod(L))
+        parts = []
+        for r in range(n):
+            co = np.zeros(V * 3, np.int64)
+            ns = np.zeros(3, np.int32)
+            k = lib.ref_mpi_rank_sites(3, (ctypes.c_int * 3)(*L), n, r, co.ctypes.data_as(ctypes.c_void_p),
+                                       ns.ctypes.data_as(ctypes.c_void_p))
+            parts.append(co[: k * 3].reshape(k, 3))
+        co = np.concatenate(parts)
+        name = "x".join(map(str, L)) + f"_{n}"
+        # lexicographic index of every file position
+        out["order_" + name] = co[:, 0] + L[0] * (co[:, 1] + L[1] * co[:, 2])
+        out["nslices_" + name] = ns
+    np.savez_compressed(os.path.join(HERE, "mpi_layout.npz"), **out)
+
+
 def main(only=None):
     if only:
         for m in only:
-            if m in CORREL_CASES:
+            if m == "mpi_layout":
+                gen_mpi_layout()
+            elif m in CORREL_CASES:
                 gen_correl(m)
             else:
                 gen_muca(m)
@@ -283,6 +314,7 @@ def main(only=None):
         gen_flow(fl)
     for c in CORREL_CASES:
         gen_correl(c)
+    gen_mpi_layout()
     total = sum(os.path.getsize(os.path.join(HERE, x)) for x in os.listdir(HERE) if x.endswith(".npz"))
     print(f"golden fixtures written, {total / 1024:.0f} KiB")
 
