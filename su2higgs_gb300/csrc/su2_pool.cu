@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -100,6 +101,12 @@ struct su2gpu_pool {
   Buf tiles[NVARIANTS], mtiles, mfirst, sweepptrs, partials, sums, stage, err;
   int64_t stage_sites = 0;          // sites each staging half holds (STAGE_REALS doubles per site)
   cudaEvent_t stage_ev[2] = {nullptr, nullptr};
+  // batch transfers (upload_many / download_many): a ring of staging memory
+  // that the copy engines fill or drain on copy_st while the conversion
+  // kernels run on st, each chain's region guarded by device-side events
+  Buf ring;
+  cudaStream_t copy_st = nullptr;
+  std::vector<cudaEvent_t> ring_ev;  // two per chain of a batch: copied, converted
   int ntiles[NVARIANTS] = {0, 0, 0, 0}, nmtiles = 0;
   std::vector<int> active;  // active slots in slot order
   bool dirty = true;
@@ -374,6 +381,10 @@ int su2gpu_pool_destroy(su2gpu_pool* P) {
   for (int v = 0; v < NVARIANTS; v++) P->tiles[v].release();
   for (int k = 0; k < 2; k++)
     if (P->stage_ev[k]) cudaEventDestroy(P->stage_ev[k]);
+  if (P->copy_st) cudaStreamSynchronize(P->copy_st);
+  P->ring.release();
+  for (cudaEvent_t e : P->ring_ev) cudaEventDestroy(e);
+  if (P->copy_st) cudaStreamDestroy(P->copy_st);
   if (P->own_st) cudaStreamDestroy(P->own_st);
   delete P;
   return SU2GPU_OK;
@@ -518,15 +529,144 @@ int su2gpu_pool_download(su2gpu_pool* P, int32_t s, double* link, double* u1, do
 
 // many chains in one call: fields[k][j] is field k (link, u1, doublet0,
 // doublet1, triplet, singlet) of slots[j]; a null fields[k] skips field k
+// Field arrays of one chain and their FP64 element counts, in transfer order
+struct ChainIo {
+  int kind[6], hid[6];
+  size_t n[6];
+  int count = 0;
+  size_t total = 0;
+};
+static ChainIo chain_io(const su2gpu_pool* P, int64_t V, double* const* h, double** hp) {
+  ChainIo c;
+  const int nh = nhiggs_of(P->content);
+  const struct { int kind, hid; size_t n; bool present; } items[6] = {
+      {0, 0, (size_t)V * 12, true},
+      {1, 0, (size_t)V * 3, (bool)(P->content & SU2GPU_U1)},
+      {2, 0, (size_t)V * 4, nh > 0},
+      {2, 1, (size_t)V * 4, nh > 1},
+      {3, 0, (size_t)V * 3, (bool)(P->content & SU2GPU_TRIPLET)},
+      {4, 0, (size_t)V, (bool)(P->content & SU2GPU_SINGLET)}};
+  for (int k = 0; k < 6; k++) {
+    if (!items[k].present || !h[k]) continue;
+    c.kind[c.count] = items[k].kind;
+    c.hid[c.count] = items[k].hid;
+    c.n[c.count] = items[k].n;
+    hp[c.count] = h[k];
+    c.total += items[k].n;
+    c.count++;
+  }
+  return c;
+}
+
+// staging ring of batch transfers: 2 GiB (or the batch, if smaller; at least
+// the largest chain), or SU2GPU_RING_BYTES bytes when that is set
+static size_t ring_bytes() {
+  const char* e = getenv("SU2GPU_RING_BYTES");
+  if (e && *e) return (size_t)strtoull(e, nullptr, 10);
+  return (size_t)1 << 31;
+}
+
+// upload_many / download_many.  The batch goes through a staging ring: chain
+// j's host arrays are copied by the copy engines on copy_st and converted by
+// the kernels on st, with device-side events between the two streams per
+// chain (copied -> convert for uploads, converted -> copy for downloads), so
+// copies, conversions and the copies of the other direction overlap and the
+// host never waits inside the batch.  A chain's ring region is reused only
+// after the earlier chain in it was consumed (another device-side wait).
 static int many_transfer(su2gpu_pool* P, int32_t n, const int32_t* slots, int upload, double* const* const* fields) {
   if (!P || n < 0 || (n && !slots) || !fields) return fail(SU2GPU_ERR_INVALID, "bad arguments");
+  if (!n) return SU2GPU_OK;
+  size_t total = 0, largest = 0;
   for (int32_t j = 0; j < n; j++) {
-    double* h[6];
-    for (int k = 0; k < 6; k++) h[k] = fields[k] ? fields[k][j] : nullptr;
-    PCK(cudaEventSynchronize(P->stage_ev[j & 1]));  // the half's previous copies are done
-    int rc = slot_transfer(P, slots[j], upload, h, j & 1);
-    if (rc) return rc;
+    const int32_t s = slots[j];
+    if (s < 0 || s >= P->max_slots || !P->slots[s].active) return fail(SU2GPU_ERR_INVALID, "no such chain slot");
+    const size_t b = (size_t)P->slots[s].g.V * STAGE_REALS * 8;
+    total += b;
+    largest = std::max(largest, b);
   }
+  const size_t ring = std::max(largest, std::min(total, ring_bytes()));
+  int rc;
+  if (!P->copy_st && cudaStreamCreateWithFlags(&P->copy_st, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(SU2GPU_ERR_CUDA, "cudaStreamCreate failed");
+  if (P->ring.n < ring) {
+    PCK(cudaStreamSynchronize(P->copy_st));
+    PCK(cudaStreamSynchronize(P->st));
+    if ((rc = P->ring.ensure(ring))) return rc;
+  }
+  while (P->ring_ev.size() < 2 * (size_t)n + 1) {
+    cudaEvent_t e;
+    PCK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    P->ring_ev.push_back(e);
+  }
+  // the fields may still be in use by earlier work on st
+  PCK(cudaEventRecord(P->ring_ev[2 * n], P->st));
+  PCK(cudaStreamWaitEvent(P->copy_st, P->ring_ev[2 * n], 0));
+  struct Placed { size_t lo, hi; cudaEvent_t consumed; };
+  std::vector<Placed> live;  // ring regions whose chain may still be in flight
+  size_t head = 0;
+  char* rb = (char*)P->ring.p;
+  for (int32_t j = 0; j < n; j++) {
+    const Slot& sl = P->slots[slots[j]];
+    const int64_t V = sl.g.V;
+    double* h[6];
+    double* hp[6];
+    for (int k = 0; k < 6; k++) h[k] = fields[k] ? fields[k][j] : nullptr;
+    const ChainIo io = chain_io(P, V, h, hp);
+    const size_t bytes = io.total * 8;
+    if (head + bytes > ring) head = 0;
+    const size_t lo = head, hi = head + bytes;
+    head = hi;
+    // wait (on the device) for every earlier chain that used this region
+    cudaStream_t producer = upload ? P->copy_st : P->st;
+    for (size_t q = 0; q < live.size();) {
+      if (live[q].lo < hi && lo < live[q].hi) {
+        PCK(cudaStreamWaitEvent(producer, live[q].consumed, 0));
+        live.erase(live.begin() + q);
+      } else {
+        q++;
+      }
+    }
+    Fields<double> f64;
+    Fields<float> f32;
+    char* base = (char*)P->arena.p + sl.off;
+    if (P->prec == 64) carve(f64, base, &sl.p, V);
+    else carve(f32, base, &sl.p, V);
+    const void* F = P->prec == 64 ? (const void*)&f64 : (const void*)&f32;
+    cudaEvent_t ready = P->ring_ev[2 * j], consumed = P->ring_ev[2 * j + 1];
+    double* st = (double*)(rb + lo);
+    if (upload) {
+      size_t off = 0;
+      for (int k = 0; k < io.count; k++) {
+        PCK(cudaMemcpyAsync(st + off, hp[k], io.n[k] * 8, cudaMemcpyHostToDevice, P->copy_st));
+        off += io.n[k];
+      }
+      PCK(cudaEventRecord(ready, P->copy_st));
+      PCK(cudaStreamWaitEvent(P->st, ready, 0));
+      off = 0;
+      for (int k = 0; k < io.count; k++) {
+        P->pops->import(F, V, io.kind[k], io.hid[k], st + off, P->st);
+        off += io.n[k];
+      }
+      PCK(cudaEventRecord(consumed, P->st));
+    } else {
+      size_t off = 0;
+      for (int k = 0; k < io.count; k++) {
+        P->pops->exportf(F, V, io.kind[k], io.hid[k], st + off, P->st);
+        off += io.n[k];
+      }
+      PCK(cudaEventRecord(ready, P->st));
+      PCK(cudaStreamWaitEvent(P->copy_st, ready, 0));
+      off = 0;
+      for (int k = 0; k < io.count; k++) {
+        PCK(cudaMemcpyAsync(hp[k], st + off, io.n[k] * 8, cudaMemcpyDeviceToHost, P->copy_st));
+        off += io.n[k];
+      }
+      PCK(cudaEventRecord(consumed, P->copy_st));
+    }
+    PCK(cudaGetLastError());
+    live.push_back({lo, hi, consumed});
+  }
+  PCK(cudaStreamSynchronize(P->copy_st));
   PCK(cudaStreamSynchronize(P->st));
   return SU2GPU_OK;
 }

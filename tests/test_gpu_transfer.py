@@ -98,3 +98,33 @@ def test_pool_many_equals_single(gpu):
     finally:
         for f in pinned:
             unpin(gpu, f)
+
+
+@pytest.mark.parametrize("ring", ["1", "40000000"])
+def test_pool_many_through_a_small_ring(gpu, ring, monkeypatch):
+    """upload_many / download_many with a staging ring smaller than the batch
+    (SU2GPU_RING_BYTES): every chain waits on the device for the chains that
+    used its ring region before; the fields arrive intact both ways."""
+    from su2higgs_gb300 import workloads
+    monkeypatch.setenv("SU2GPU_RING_BYTES", ring)
+    specs = workloads.batched_ensemble(24, seed=9)
+    arena = sum(gpu.Pool.chain_bytes(p) for p, _, _ in specs)
+    inputs = [workloads.hot_fields(p, seed) for p, seed, _ in specs]
+    pool = gpu.Pool(specs[0][0], arena_bytes=arena, max_chains=24)
+    slots = [pool.add(p, seed=seed, chain=chain) for p, seed, chain in specs]
+    pinned = [pinned_copy(gpu, f) for f in inputs]
+    try:
+        pool.upload_many(slots, pinned)
+        for s, f in zip(slots, inputs):
+            got = pool.download(s)
+            for n in f:
+                assert np.array_equal(got[n].astype(np.float32), f[n].astype(np.float32)), n
+        pool.run(1)
+        want = [pool.download(s) for s in slots]
+        pool.download_many(slots, pinned)
+        for w, g in zip(want, pinned):
+            for n in g:
+                assert np.array_equal(g[n], w[n]), n
+    finally:
+        for f in pinned:
+            unpin(gpu, f)
