@@ -369,10 +369,23 @@ int su2gpu_pool_download(su2gpu_pool* pool, int32_t slot, double* link, double* 
                          double* doublet1, double* triplet, double* singlet);
 /* The same for n chains in one call, waiting once: fields[k][j] is field k
  * (0 link, 1 u1, 2 doublet0, 3 doublet1, 4 triplet, 5 singlet) of slots[j];
- * fields[k] == NULL skips field k.  Page-locked host arrays (see
- * su2gpu_host_register) are read / written in place by the device. */
+ * fields[k] == NULL skips field k.  The arrays go through a device staging
+ * ring (2 GiB at most, or SU2GPU_RING_BYTES bytes) by the copy engines, the
+ * conversion kernels following each chain's copy; page-locked host arrays
+ * (see su2gpu_host_register) copy at the full link rate. */
 int su2gpu_pool_upload_many(su2gpu_pool* pool, int32_t n, const int32_t* slots, const double* const* const* fields);
 int su2gpu_pool_download_many(su2gpu_pool* pool, int32_t n, const int32_t* slots, double* const* const* fields);
+/* One batch through the pool: upload the host fields in[k][j] of every
+ * active chain (slots lists each active chain once), run nsweeps sweeps,
+ * measure (sums[j * SU2GPU_NMEAS + ...] for slots[j], or NULL), and download
+ * the fields into out[k][j] (may be the same arrays as in).  The chains are
+ * split into groups of about equal size whose uploads, sweeps and downloads
+ * are pipelined on three streams (copy engine in, update kernels, copy engine
+ * out), so the host transfers of a group run under the sweeps of the others.
+ * The results equal su2gpu_pool_upload_many + su2gpu_pool_run +
+ * su2gpu_pool_measure + su2gpu_pool_download_many bit for bit. */
+int su2gpu_pool_cycle(su2gpu_pool* pool, int32_t n, const int32_t* slots, const double* const* const* in,
+                      int32_t nsweeps, int32_t use_graph, double* sums, double* const* const* out);
 /* Set one chain's sweep counter (the random stream's sweep index). */
 int su2gpu_pool_set_sweep(su2gpu_pool* pool, int32_t slot, uint32_t sweep);
 /* `nsweeps` sweeps of every active chain; each chain's sweep counter

@@ -182,9 +182,9 @@ void launch_muca_set_param(MucaDev* w, const double* partials, int np, double vo
 void launch_reduce_partials(const double* partials, int np, double* out, cudaStream_t st) {
   k_reduce_partials<<<NSUMS, 256, 0, st>>>(partials, np, out);
 }
-void launch_pool_reduce(const double* partials, int nblocks, const int* first, int nchains, double* out,
+void launch_pool_reduce(const double* partials, int nblocks, const int* first, int base, int nchains, double* out,
                         cudaStream_t st) {
-  if (nchains) k_pool_reduce<<<nchains, 128, 0, st>>>(partials, nblocks, first, out);
+  if (nchains) k_pool_reduce<<<nchains, 128, 0, st>>>(partials, nblocks, first, base, out);
 }
 void launch_pool_next_sweep(uint32_t* const* sweeps, int n, cudaStream_t st) {
   if (n) k_pool_next_sweep<<<(n + 255) / 256, 256, 0, st>>>(sweeps, n);

@@ -59,7 +59,7 @@ void launch_muca_decide(MucaDev* w, const double* partials, int np, double vol, 
                         uint32_t pass, uint32_t check, unsigned long long* ctr, cudaStream_t st);
 void launch_muca_set_param(MucaDev* w, const double* partials, int np, double vol, int parity, cudaStream_t st);
 void launch_reduce_partials(const double* partials, int np, double* out, cudaStream_t st);
-void launch_pool_reduce(const double* partials, int nblocks, const int* first, int nchains, double* out,
+void launch_pool_reduce(const double* partials, int nblocks, const int* first, int base, int nchains, double* out,
                         cudaStream_t st);
 void launch_pool_next_sweep(uint32_t* const* sweeps, int n, cudaStream_t st);
 

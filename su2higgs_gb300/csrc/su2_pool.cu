@@ -118,6 +118,14 @@ struct su2gpu_pool {
   std::vector<unsigned char> h_desc;
   std::vector<int2> h_tiles[NVARIANTS], h_mtiles;
   std::vector<int> h_first;
+  std::vector<int> h_tfirst[NVARIANTS];  // first update tile of each active chain (+ the end)
+  // pipelined cycles (su2gpu_pool_cycle): a second ring for the downloads,
+  // the download copy stream, and one sweep graph per group of chains
+  Buf ring_down;
+  cudaStream_t down_st = nullptr;
+  std::vector<cudaEvent_t> cyc_ev;
+  struct GroupGraph { int a0, a1; cudaGraphExec_t exec; };
+  std::vector<GroupGraph> ggraphs;
   std::vector<uint32_t*> h_sweeps;
   size_t rsize() const { return prec == 64 ? 8 : 4; }
 };
@@ -191,9 +199,13 @@ int rebuild(su2gpu_pool* P, void* arena_base = nullptr, void* slot_base = nullpt
     for (int v = 0; v < NVARIANTS; v++) {
       std::vector<int2>& t = P->h_tiles[v];
       t.clear();
+      P->h_tfirst[v].clear();
       int bs = kVariantBS[v];
-      for (int s : P->active)
+      for (int s : P->active) {
+        P->h_tfirst[v].push_back((int)t.size());
         for (int t0 = 0; t0 < P->slots[s].g.half; t0 += bs) t.push_back(int2{s, t0});
+      }
+      P->h_tfirst[v].push_back((int)t.size());
       P->ntiles[v] = (int)t.size();
       if (int rc = P->tiles[v].ensure(std::max<size_t>(t.size(), 1) * sizeof(int2))) return rc;
       if (!t.empty()) PCK(cudaMemcpyAsync(P->tiles[v].p, t.data(), t.size() * sizeof(int2), cudaMemcpyHostToDevice, P->st));
@@ -225,6 +237,8 @@ int rebuild(su2gpu_pool* P, void* arena_base = nullptr, void* slot_base = nullpt
       cudaGraphExecDestroy(P->gexec);
       P->gexec = nullptr;
     }
+    for (auto& gg : P->ggraphs) cudaGraphExecDestroy(gg.exec);
+    P->ggraphs.clear();
     P->dirty = false;
   }
   PCK(cudaStreamSynchronize(P->st));
@@ -242,9 +256,9 @@ void mark(su2gpu_pool* P, int kind) {
 
 // one sweep of every active chain (update.c:270-430 order); `tot` receives the
 // per-chain half-site totals of one sweep
-int enqueue_pool_sweep(su2gpu_pool* P, const void* descs, const int2* const* tiles, unsigned long long* unused,
+int enqueue_pool_sweep(su2gpu_pool* P, const void* descs, const int2* const* tiles, const int* nt,
                        int64_t* tot) {
-  (void)unused;
+  if (!nt) nt = P->ntiles;
   const su2gpu_params& p = P->recipe;
   PoolArgs a;
   memset(&a, 0, sizeof(a));
@@ -260,7 +274,7 @@ int enqueue_pool_sweep(su2gpu_pool* P, const void* descs, const int2* const* til
         a.parity = par; a.sub = mu; a.alg = p.algorithm_su2link; a.pass = pass++;
         a.tiles = tiles[vt(0)];
         mark(P, 0);
-        P->ops->pool_link(vt(0), a, P->ntiles[vt(0)], P->st);
+        P->ops->pool_link(vt(0), a, nt[vt(0)], P->st);
         tot[SU2GPU_C_TOTAL_SU2LINK] += 1;
       }
     if (p.content & SU2GPU_U1)
@@ -269,7 +283,7 @@ int enqueue_pool_sweep(su2gpu_pool* P, const void* descs, const int2* const* til
           a.parity = par; a.sub = mu; a.alg = 0; a.pass = pass++;
           a.tiles = tiles[vt(1)];
           mark(P, 1);
-          P->ops->pool_u1(vt(1), a, P->ntiles[vt(1)], P->st);
+          P->ops->pool_u1(vt(1), a, nt[vt(1)], P->st);
           tot[SU2GPU_C_TOTAL_U1LINK] += 1;
         }
   }
@@ -293,7 +307,7 @@ int enqueue_pool_sweep(su2gpu_pool* P, const void* descs, const int2* const* til
             int kind = 2 + fd.field;
             a.tiles = tiles[vt(kind)];
             mark(P, kind);
-            P->ops->pool_scalar(vt(kind), fd.field, a, P->ntiles[vt(kind)], P->st);
+            P->ops->pool_scalar(vt(kind), fd.field, a, nt[vt(kind)], P->st);
             bool orr = fd.alg == SU2GPU_OVERRELAX && !force;
             int idx = fd.field == 0 ? (orr ? SU2GPU_C_TOTAL_OR_DOUBLET : SU2GPU_C_TOTAL_DOUBLET) + h
                                     : (fd.field == 1 ? (orr ? SU2GPU_C_TOTAL_OR_TRIPLET : SU2GPU_C_TOTAL_TRIPLET)
@@ -382,9 +396,14 @@ int su2gpu_pool_destroy(su2gpu_pool* P) {
   for (int k = 0; k < 2; k++)
     if (P->stage_ev[k]) cudaEventDestroy(P->stage_ev[k]);
   if (P->copy_st) cudaStreamSynchronize(P->copy_st);
+  if (P->down_st) cudaStreamSynchronize(P->down_st);
   P->ring.release();
+  P->ring_down.release();
   for (cudaEvent_t e : P->ring_ev) cudaEventDestroy(e);
+  for (cudaEvent_t e : P->cyc_ev) cudaEventDestroy(e);
+  for (auto& gg : P->ggraphs) cudaGraphExecDestroy(gg.exec);
   if (P->copy_st) cudaStreamDestroy(P->copy_st);
+  if (P->down_st) cudaStreamDestroy(P->down_st);
   if (P->own_st) cudaStreamDestroy(P->own_st);
   delete P;
   return SU2GPU_OK;
@@ -566,13 +585,140 @@ static size_t ring_bytes() {
   return (size_t)1 << 31;
 }
 
+// A staging ring of host transfers: chain regions are placed one after
+// another and wrap to the start; a region is reused only after every earlier
+// chain placed over it was consumed, which the producer of the new chain
+// waits for on the device.
+struct Ring {
+  char* base = nullptr;
+  size_t cap = 0, head = 0;
+  struct Placed { size_t lo, hi; cudaEvent_t consumed; };
+  std::vector<Placed> live;
+};
+static int ring_take(Ring& R, size_t bytes, cudaStream_t producer, size_t* lo) {
+  if (R.head + bytes > R.cap) R.head = 0;
+  *lo = R.head;
+  const size_t hi = R.head + bytes;
+  R.head = hi;
+  for (size_t q = 0; q < R.live.size();) {
+    if (R.live[q].lo < hi && *lo < R.live[q].hi) {
+      PCK(cudaStreamWaitEvent(producer, R.live[q].consumed, 0));
+      R.live.erase(R.live.begin() + q);
+    } else {
+      q++;
+    }
+  }
+  return SU2GPU_OK;
+}
+
+// one chain's host arrays into its fields: copies on `copy`, conversion
+// kernels on `comp` once the copies are done (events `ready`, `consumed`)
+static int chain_up(su2gpu_pool* P, Ring& R, int32_t s, double* const* h, cudaEvent_t ready, cudaEvent_t consumed,
+                    cudaStream_t copy, cudaStream_t comp) {
+  const Slot& sl = P->slots[s];
+  const int64_t V = sl.g.V;
+  double* hp[6];
+  const ChainIo io = chain_io(P, V, h, hp);
+  size_t lo;
+  int rc = ring_take(R, io.total * 8, copy, &lo);
+  if (rc) return rc;
+  double* st = (double*)(R.base + lo);
+  Fields<double> f64;
+  Fields<float> f32;
+  char* base = (char*)P->arena.p + sl.off;
+  if (P->prec == 64) carve(f64, base, &sl.p, V);
+  else carve(f32, base, &sl.p, V);
+  const void* F = P->prec == 64 ? (const void*)&f64 : (const void*)&f32;
+  size_t off = 0;
+  for (int k = 0; k < io.count; k++) {
+    PCK(cudaMemcpyAsync(st + off, hp[k], io.n[k] * 8, cudaMemcpyHostToDevice, copy));
+    off += io.n[k];
+  }
+  PCK(cudaEventRecord(ready, copy));
+  PCK(cudaStreamWaitEvent(comp, ready, 0));
+  off = 0;
+  for (int k = 0; k < io.count; k++) {
+    P->pops->import(F, V, io.kind[k], io.hid[k], st + off, comp);
+    off += io.n[k];
+  }
+  PCK(cudaEventRecord(consumed, comp));
+  PCK(cudaGetLastError());
+  R.live.push_back({lo, lo + io.total * 8, consumed});
+  return SU2GPU_OK;
+}
+
+// one chain's fields into its host arrays: conversion kernels on `comp`,
+// copies on `copy` once they are done
+static int chain_down(su2gpu_pool* P, Ring& R, int32_t s, double* const* h, cudaEvent_t ready, cudaEvent_t consumed,
+                      cudaStream_t comp, cudaStream_t copy) {
+  const Slot& sl = P->slots[s];
+  const int64_t V = sl.g.V;
+  double* hp[6];
+  const ChainIo io = chain_io(P, V, h, hp);
+  size_t lo;
+  int rc = ring_take(R, io.total * 8, comp, &lo);
+  if (rc) return rc;
+  double* st = (double*)(R.base + lo);
+  Fields<double> f64;
+  Fields<float> f32;
+  char* base = (char*)P->arena.p + sl.off;
+  if (P->prec == 64) carve(f64, base, &sl.p, V);
+  else carve(f32, base, &sl.p, V);
+  const void* F = P->prec == 64 ? (const void*)&f64 : (const void*)&f32;
+  size_t off = 0;
+  for (int k = 0; k < io.count; k++) {
+    P->pops->exportf(F, V, io.kind[k], io.hid[k], st + off, comp);
+    off += io.n[k];
+  }
+  PCK(cudaEventRecord(ready, comp));
+  PCK(cudaStreamWaitEvent(copy, ready, 0));
+  off = 0;
+  for (int k = 0; k < io.count; k++) {
+    PCK(cudaMemcpyAsync(hp[k], st + off, io.n[k] * 8, cudaMemcpyDeviceToHost, copy));
+    off += io.n[k];
+  }
+  PCK(cudaEventRecord(consumed, copy));
+  PCK(cudaGetLastError());
+  R.live.push_back({lo, lo + io.total * 8, consumed});
+  return SU2GPU_OK;
+}
+
+static int ensure_events(std::vector<cudaEvent_t>& v, size_t n) {
+  while (v.size() < n) {
+    cudaEvent_t e;
+    PCK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    v.push_back(e);
+  }
+  return SU2GPU_OK;
+}
+
+static int ensure_stream(cudaStream_t* st) {
+  if (!*st && cudaStreamCreateWithFlags(st, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(SU2GPU_ERR_CUDA, "cudaStreamCreate failed");
+  return SU2GPU_OK;
+}
+
+// a ring buffer for a batch of `total` staged bytes whose largest chain
+// needs `largest`
+static int ensure_ring(su2gpu_pool* P, Buf& buf, size_t total, size_t largest, Ring* R) {
+  const size_t want = std::max(largest, std::min(total, ring_bytes()));
+  if (buf.n < want) {
+    if (P->copy_st) PCK(cudaStreamSynchronize(P->copy_st));
+    if (P->down_st) PCK(cudaStreamSynchronize(P->down_st));
+    PCK(cudaStreamSynchronize(P->st));
+    int rc = buf.ensure(want);
+    if (rc) return rc;
+  }
+  R->base = (char*)buf.p;
+  R->cap = want;
+  return SU2GPU_OK;
+}
+
 // upload_many / download_many.  The batch goes through a staging ring: chain
 // j's host arrays are copied by the copy engines on copy_st and converted by
 // the kernels on st, with device-side events between the two streams per
 // chain (copied -> convert for uploads, converted -> copy for downloads), so
-// copies, conversions and the copies of the other direction overlap and the
-// host never waits inside the batch.  A chain's ring region is reused only
-// after the earlier chain in it was consumed (another device-side wait).
+// copies and conversions overlap and the host never waits inside the batch.
 static int many_transfer(su2gpu_pool* P, int32_t n, const int32_t* slots, int upload, double* const* const* fields) {
   if (!P || n < 0 || (n && !slots) || !fields) return fail(SU2GPU_ERR_INVALID, "bad arguments");
   if (!n) return SU2GPU_OK;
@@ -584,87 +730,20 @@ static int many_transfer(su2gpu_pool* P, int32_t n, const int32_t* slots, int up
     total += b;
     largest = std::max(largest, b);
   }
-  const size_t ring = std::max(largest, std::min(total, ring_bytes()));
   int rc;
-  if (!P->copy_st && cudaStreamCreateWithFlags(&P->copy_st, cudaStreamNonBlocking) != cudaSuccess)
-    return fail(SU2GPU_ERR_CUDA, "cudaStreamCreate failed");
-  if (P->ring.n < ring) {
-    PCK(cudaStreamSynchronize(P->copy_st));
-    PCK(cudaStreamSynchronize(P->st));
-    if ((rc = P->ring.ensure(ring))) return rc;
-  }
-  while (P->ring_ev.size() < 2 * (size_t)n + 1) {
-    cudaEvent_t e;
-    PCK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    P->ring_ev.push_back(e);
-  }
+  Ring R;
+  if ((rc = ensure_stream(&P->copy_st)) || (rc = ensure_ring(P, P->ring, total, largest, &R)) ||
+      (rc = ensure_events(P->ring_ev, 2 * (size_t)n + 1)))
+    return rc;
   // the fields may still be in use by earlier work on st
   PCK(cudaEventRecord(P->ring_ev[2 * n], P->st));
   PCK(cudaStreamWaitEvent(P->copy_st, P->ring_ev[2 * n], 0));
-  struct Placed { size_t lo, hi; cudaEvent_t consumed; };
-  std::vector<Placed> live;  // ring regions whose chain may still be in flight
-  size_t head = 0;
-  char* rb = (char*)P->ring.p;
   for (int32_t j = 0; j < n; j++) {
-    const Slot& sl = P->slots[slots[j]];
-    const int64_t V = sl.g.V;
     double* h[6];
-    double* hp[6];
     for (int k = 0; k < 6; k++) h[k] = fields[k] ? fields[k][j] : nullptr;
-    const ChainIo io = chain_io(P, V, h, hp);
-    const size_t bytes = io.total * 8;
-    if (head + bytes > ring) head = 0;
-    const size_t lo = head, hi = head + bytes;
-    head = hi;
-    // wait (on the device) for every earlier chain that used this region
-    cudaStream_t producer = upload ? P->copy_st : P->st;
-    for (size_t q = 0; q < live.size();) {
-      if (live[q].lo < hi && lo < live[q].hi) {
-        PCK(cudaStreamWaitEvent(producer, live[q].consumed, 0));
-        live.erase(live.begin() + q);
-      } else {
-        q++;
-      }
-    }
-    Fields<double> f64;
-    Fields<float> f32;
-    char* base = (char*)P->arena.p + sl.off;
-    if (P->prec == 64) carve(f64, base, &sl.p, V);
-    else carve(f32, base, &sl.p, V);
-    const void* F = P->prec == 64 ? (const void*)&f64 : (const void*)&f32;
-    cudaEvent_t ready = P->ring_ev[2 * j], consumed = P->ring_ev[2 * j + 1];
-    double* st = (double*)(rb + lo);
-    if (upload) {
-      size_t off = 0;
-      for (int k = 0; k < io.count; k++) {
-        PCK(cudaMemcpyAsync(st + off, hp[k], io.n[k] * 8, cudaMemcpyHostToDevice, P->copy_st));
-        off += io.n[k];
-      }
-      PCK(cudaEventRecord(ready, P->copy_st));
-      PCK(cudaStreamWaitEvent(P->st, ready, 0));
-      off = 0;
-      for (int k = 0; k < io.count; k++) {
-        P->pops->import(F, V, io.kind[k], io.hid[k], st + off, P->st);
-        off += io.n[k];
-      }
-      PCK(cudaEventRecord(consumed, P->st));
-    } else {
-      size_t off = 0;
-      for (int k = 0; k < io.count; k++) {
-        P->pops->exportf(F, V, io.kind[k], io.hid[k], st + off, P->st);
-        off += io.n[k];
-      }
-      PCK(cudaEventRecord(ready, P->st));
-      PCK(cudaStreamWaitEvent(P->copy_st, ready, 0));
-      off = 0;
-      for (int k = 0; k < io.count; k++) {
-        PCK(cudaMemcpyAsync(hp[k], st + off, io.n[k] * 8, cudaMemcpyDeviceToHost, P->copy_st));
-        off += io.n[k];
-      }
-      PCK(cudaEventRecord(consumed, P->copy_st));
-    }
-    PCK(cudaGetLastError());
-    live.push_back({lo, hi, consumed});
+    rc = upload ? chain_up(P, R, slots[j], h, P->ring_ev[2 * j], P->ring_ev[2 * j + 1], P->copy_st, P->st)
+                : chain_down(P, R, slots[j], h, P->ring_ev[2 * j], P->ring_ev[2 * j + 1], P->st, P->copy_st);
+    if (rc) return rc;
   }
   PCK(cudaStreamSynchronize(P->copy_st));
   PCK(cudaStreamSynchronize(P->st));
@@ -740,6 +819,173 @@ int su2gpu_pool_run(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
   int rc = pool_enqueue(P, nsweeps, use_graph);
   if (rc) return rc;
   return pool_check(P);
+}
+
+// ---------------------------------------------------------------------------
+// pipelined cycle: upload, sweeps, measurement and download of the whole pool
+// with the host transfers of some groups of chains under the sweeps of others
+// ---------------------------------------------------------------------------
+// one sweep of the active chains [a0, a1): their tile ranges of every variant
+// and their sweep counters
+static int enqueue_group_sweep(su2gpu_pool* P, int a0, int a1, int64_t* tot) {
+  const int2* tiles[NVARIANTS];
+  int nt[NVARIANTS];
+  for (int v = 0; v < NVARIANTS; v++) {
+    tiles[v] = (const int2*)P->tiles[v].p + P->h_tfirst[v][a0];
+    nt[v] = P->h_tfirst[v][a1] - P->h_tfirst[v][a0];
+  }
+  int rc = enqueue_pool_sweep(P, P->descs.p, tiles, nt, tot);
+  if (rc) return rc;
+  launch_pool_next_sweep((uint32_t* const*)P->sweepptrs.p + a0, a1 - a0, P->st);
+  PCK(cudaGetLastError());
+  return SU2GPU_OK;
+}
+
+// the sweep graph of the group [a0, a1), captured on the pool's own stream
+static int group_graph(su2gpu_pool* P, int a0, int a1, cudaGraphExec_t* out) {
+  for (auto& gg : P->ggraphs)
+    if (gg.a0 == a0 && gg.a1 == a1) {
+      *out = gg.exec;
+      return SU2GPU_OK;
+    }
+  cudaStream_t exec = P->st;
+  PCK(cudaStreamSynchronize(exec));
+  PCK(cudaStreamSynchronize(P->own_st));
+  P->st = P->own_st;
+  cudaGraph_t graph;
+  PCK(cudaStreamBeginCapture(P->st, cudaStreamCaptureModeThreadLocal));
+  int64_t tot[SU2GPU_NCOUNTERS] = {0};
+  int rc = enqueue_group_sweep(P, a0, a1, tot);
+  cudaError_t e = cudaStreamEndCapture(P->st, &graph);
+  P->st = exec;
+  if (rc) return rc;
+  if (e != cudaSuccess) return fail(SU2GPU_ERR_CUDA, "group graph capture: %s", cudaGetErrorString(e));
+  cudaGraphExec_t ge;
+  e = cudaGraphInstantiate(&ge, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return fail(SU2GPU_ERR_CUDA, "group graph instantiate: %s", cudaGetErrorString(e));
+  P->ggraphs.push_back({a0, a1, ge});
+  *out = ge;
+  return SU2GPU_OK;
+}
+
+// measure() sums of the active chains [a0, a1) into sums[a][NSUMS]
+static void enqueue_group_measure(su2gpu_pool* P, int a0, int a1, double* sums) {
+  const int b0 = P->h_first[a0], b1 = P->h_first[a1];
+  PoolArgs a;
+  memset(&a, 0, sizeof(a));
+  a.descs = P->descs.p;
+  a.nslots = P->max_slots;
+  a.tiles = (const int2*)P->mtiles.p + b0;
+  a.err = (int*)P->err.p;
+  double* part = (double*)P->partials.p + (size_t)b0 * NSUMS;
+  P->ops->pool_measure(a, part, b1 - b0, P->st);
+  launch_pool_reduce(part, b1 - b0, (const int*)P->mfirst.p + a0, b0, a1 - a0, sums + (size_t)a0 * NSUMS, P->st);
+}
+
+// groups of consecutive active chains with about equal numbers of sites
+static std::vector<int> cycle_groups(const su2gpu_pool* P) {
+  const int na = (int)P->active.size();
+  int64_t total = 0;
+  for (int s : P->active) total += P->slots[s].g.V;
+  const int64_t bytes = total * STAGE_REALS * 8;
+  int G = (int)std::min<int64_t>(8, std::max<int64_t>(1, bytes / (64ll << 20)));
+  G = std::min(G, na);
+  std::vector<int> b(1, 0);
+  int64_t acc = 0;
+  for (int a = 0; a < na; a++) {
+    acc += P->slots[P->active[a]].g.V;
+    if ((int)b.size() < G && acc * G >= total * (int64_t)b.size() && a + 1 < na) b.push_back(a + 1);
+  }
+  b.push_back(na);
+  return b;
+}
+
+int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const double* const* const* in, int32_t nsweeps,
+                      int32_t use_graph, double* sums, double* const* const* out) {
+  if (!P || n < 0 || (n && !slots) || !in || !out || nsweeps < 0) return fail(SU2GPU_ERR_INVALID, "bad arguments");
+  int rc;
+  if (P->dirty && (rc = rebuild(P))) return rc;
+  const int na = (int)P->active.size();
+  if (n != na) return fail(SU2GPU_ERR_INVALID, "a cycle lists every active chain once (%d listed, %d active)", n, na);
+  if (!na) return SU2GPU_OK;
+  // position in the caller's lists of every active chain
+  std::vector<int> pos(na, -1), act_of(P->max_slots, -1);
+  for (int a = 0; a < na; a++) act_of[P->active[a]] = a;
+  size_t total = 0, largest = 0;
+  for (int j = 0; j < n; j++) {
+    const int s = slots[j];
+    if (s < 0 || s >= P->max_slots || act_of[s] < 0 || pos[act_of[s]] >= 0)
+      return fail(SU2GPU_ERR_INVALID, "slot %d is not an active chain listed once", s);
+    pos[act_of[s]] = j;
+    const size_t b = (size_t)P->slots[s].g.V * STAGE_REALS * 8;
+    total += b;
+    largest = std::max(largest, b);
+  }
+  const std::vector<int> groups = cycle_groups(P);
+  const int G = (int)groups.size() - 1;
+  std::vector<cudaGraphExec_t> gex(G, nullptr);
+  if (use_graph && nsweeps > 0)
+    for (int g = 0; g < G; g++)
+      if ((rc = group_graph(P, groups[g], groups[g + 1], &gex[g]))) return rc;
+  Ring up, down;
+  if ((rc = ensure_stream(&P->copy_st)) || (rc = ensure_stream(&P->down_st)) ||
+      (rc = ensure_ring(P, P->ring, total, largest, &up)) || (rc = ensure_ring(P, P->ring_down, total, largest, &down)) ||
+      (rc = ensure_events(P->cyc_ev, 4 * (size_t)na + 1)))
+    return rc;
+  std::vector<cudaEvent_t>& ev = P->cyc_ev;
+  // the fields may still be in use by earlier work on st
+  PCK(cudaEventRecord(ev[4 * na], P->st));
+  PCK(cudaStreamWaitEvent(P->copy_st, ev[4 * na], 0));
+  PCK(cudaStreamWaitEvent(P->down_st, ev[4 * na], 0));
+  int64_t tot[SU2GPU_NCOUNTERS] = {0};
+  for (int g = 0; g < G; g++) {
+    const int a0 = groups[g], a1 = groups[g + 1];
+    for (int a = a0; a < a1; a++) {
+      double* h[6];
+      for (int k = 0; k < 6; k++) h[k] = in[k] ? (double*)in[k][pos[a]] : nullptr;
+      if ((rc = chain_up(P, up, P->active[a], h, ev[4 * a], ev[4 * a + 1], P->copy_st, P->st))) return rc;
+    }
+    for (int k = 0; k < nsweeps; k++) {
+      if (use_graph) {
+        PCK(cudaGraphLaunch(gex[g], P->st));
+      } else {
+        int64_t t1[SU2GPU_NCOUNTERS] = {0};
+        if ((rc = enqueue_group_sweep(P, a0, a1, t1))) return rc;
+      }
+    }
+    if (sums) enqueue_group_measure(P, a0, a1, (double*)P->sums.p);
+    for (int a = a0; a < a1; a++) {
+      double* h[6];
+      for (int k = 0; k < 6; k++) h[k] = out[k] ? out[k][pos[a]] : nullptr;
+      if ((rc = chain_down(P, down, P->active[a], h, ev[4 * a + 2], ev[4 * a + 3], P->st, P->down_st))) return rc;
+    }
+  }
+  // half-sweeps of each kind in one sweep of a chain
+  {
+    const int2* tl[NVARIANTS] = {nullptr, nullptr, nullptr, nullptr};
+    int zero[NVARIANTS] = {0, 0, 0, 0};
+    cudaStream_t keep = P->st;
+    // counting only: no launch happens with zero tiles
+    rc = enqueue_pool_sweep(P, P->descs.p, tl, zero, tot);
+    P->st = keep;
+    if (rc) return rc;
+  }
+  std::vector<double> hs;
+  if (sums) {
+    hs.resize((size_t)na * NSUMS);
+    PCK(cudaMemcpyAsync(hs.data(), P->sums.p, hs.size() * 8, cudaMemcpyDeviceToHost, P->st));
+  }
+  PCK(cudaStreamSynchronize(P->copy_st));
+  PCK(cudaStreamSynchronize(P->down_st));
+  if ((rc = pool_check(P))) return rc;
+  if (sums)
+    for (int a = 0; a < na; a++) memcpy(sums + (size_t)pos[a] * NSUMS, hs.data() + (size_t)a * NSUMS, NSUMS * 8);
+  for (int a = 0; a < na; a++) {
+    Slot& sl = P->slots[P->active[a]];
+    for (int k = 0; k < SU2GPU_NCOUNTERS; k++) sl.tot[k] += tot[k] * (int64_t)sl.g.half * nsweeps;
+  }
+  return SU2GPU_OK;
 }
 
 int su2gpu_pool_enqueue(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
@@ -834,7 +1080,7 @@ static int pool_enqueue_measure(su2gpu_pool* P, double* dev_out, int32_t max_cha
   a.tiles = (const int2*)P->mtiles.p;
   a.err = (int*)P->err.p;
   P->ops->pool_measure(a, (double*)P->partials.p, P->nmtiles, P->st);
-  launch_pool_reduce((const double*)P->partials.p, P->nmtiles, (const int*)P->mfirst.p, n, dev_out, P->st);
+  launch_pool_reduce((const double*)P->partials.p, P->nmtiles, (const int*)P->mfirst.p, 0, n, dev_out, P->st);
   PCK(cudaGetLastError());
   return SU2GPU_OK;
 }
@@ -919,6 +1165,8 @@ int su2gpu_pool_autotune(su2gpu_pool* P, int32_t* choices, float* best_ms) {
   PCK(cudaStreamSynchronize(P->st));
   arena2.release(); slot2.release(); desc2.release();
   if (P->gexec) { cudaGraphExecDestroy(P->gexec); P->gexec = nullptr; }
+  for (auto& gg : P->ggraphs) cudaGraphExecDestroy(gg.exec);
+  P->ggraphs.clear();
   if (choices)
     for (int k = 0; k < 5; k++) choices[k] = P->var[k];
   return SU2GPU_OK;
@@ -931,6 +1179,8 @@ int su2gpu_pool_set_variants(su2gpu_pool* P, const int32_t* choices) {
     P->var[k] = choices[k];
   }
   if (P->gexec) { cudaGraphExecDestroy(P->gexec); P->gexec = nullptr; }
+  for (auto& gg : P->ggraphs) cudaGraphExecDestroy(gg.exec);
+  P->ggraphs.clear();
   return SU2GPU_OK;
 }
 

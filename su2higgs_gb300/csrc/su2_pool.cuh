@@ -150,12 +150,13 @@ __global__ void __launch_bounds__(BLOCK) k_pool_measure(PoolArgs a, double* part
 }
 
 #ifdef SU2_WITH_GLOBAL
-// per-chain sums: chain k owns blocks [first[k], first[k+1]) of the measure
-// tiles; one block per chain, fixed summation order
-__global__ void k_pool_reduce(const double* partials, int nblocks, const int* first, double* out) {
+// per-chain sums: chain k owns blocks [first[k], first[k+1]) - base of the
+// measure tiles (base: the first block of a group of chains); one block per
+// chain, fixed summation order
+__global__ void k_pool_reduce(const double* partials, int nblocks, const int* first, int base, double* out) {
   __shared__ double red[128];
   int k = blockIdx.x;
-  int b0 = first[k], b1 = first[k + 1];
+  int b0 = first[k] - base, b1 = first[k + 1] - base;
   for (int s = 0; s < NSUMS; s++) {
     const double* row = partials + (size_t)s * nblocks;
     double v = 0.0;

@@ -100,6 +100,7 @@ def lib():
         L.su2gpu_pool_extract.argtypes = [vp, i32, ctypes.POINTER(vp)]
         L.su2gpu_pool_upload_many.argtypes = [vp, i32, vp, vp]
         L.su2gpu_pool_download_many.argtypes = [vp, i32, vp, vp]
+        L.su2gpu_pool_cycle.argtypes = [vp, i32, vp, vp, i32, i32, vp, vp]
         L.su2gpu_pool_enqueue.argtypes = [vp, i32, i32]
         L.su2gpu_pool_enqueue_measure.argtypes = [vp, vp, i32, ctypes.POINTER(i32)]
         L.su2gpu_pool_set_stream.argtypes = [vp, vp]
@@ -496,9 +497,8 @@ class Pool:
         check(lib().su2gpu_pool_download(self._h, slot, *[_p(out.get(n)) for n in FIELD_NAMES]))
         return out
 
-    def _many(self, fn, slots, fields):
-        n = len(slots)
-        keep = []
+    @staticmethod
+    def _tables(n, fields, keep):
         tables = (ctypes.c_void_p * 6)()
         for k, name in enumerate(FIELD_NAMES):
             arrs = [f.get(name) for f in fields]
@@ -507,8 +507,34 @@ class Pool:
             t = (ctypes.c_void_p * n)(*[None if a is None else a.ctypes.data for a in arrs])
             keep.append(t)
             tables[k] = ctypes.cast(t, ctypes.c_void_p)
+        keep.append(tables)
+        return ctypes.cast(tables, ctypes.c_void_p)
+
+    def _many(self, fn, slots, fields):
+        n = len(slots)
+        keep = []
+        tables = self._tables(n, fields, keep)
         sl = np.ascontiguousarray(slots, dtype=np.int32)
-        check(fn(self._h, n, _p(sl), ctypes.cast(tables, ctypes.c_void_p)))
+        check(fn(self._h, n, _p(sl), tables))
+
+    def cycle(self, slots, fields_in, nsweeps, fields_out=None, graph=True):
+        """One pipelined batch (su2gpu_pool_cycle): upload every active
+        chain's fields, `nsweeps` sweeps, measurement, download into
+        fields_out (default: in place into fields_in).  Returns the
+        measurement sums, one row per slot."""
+        fields_out = fields_in if fields_out is None else fields_out
+        for f in list(fields_in) + list(fields_out):
+            for a in f.values():
+                if a is not None and (a.dtype != np.float64 or not a.flags.c_contiguous):
+                    raise ValueError("cycle needs C-contiguous float64 arrays")
+        n = len(slots)
+        keep = []
+        tin = self._tables(n, fields_in, keep)
+        tout = self._tables(n, fields_out, keep)
+        sums = np.zeros((n, abi.NMEAS))
+        sl = np.ascontiguousarray(slots, dtype=np.int32)
+        check(lib().su2gpu_pool_cycle(self._h, n, _p(sl), tin, nsweeps, 1 if graph else 0, _p(sums), tout))
+        return sums
 
     def upload_many(self, slots, fields):
         """Upload the chains `slots` in one call; fields[j] is a dict of

@@ -128,3 +128,47 @@ def test_pool_many_through_a_small_ring(gpu, ring, monkeypatch):
     finally:
         for f in pinned:
             unpin(gpu, f)
+
+
+@pytest.mark.parametrize("ring,graph", [("", True), ("", False), ("30000000", True)])
+def test_pool_cycle_equals_separate_calls(gpu, ring, graph, monkeypatch):
+    """su2gpu_pool_cycle -- uploads, sweeps, measurement and downloads of
+    groups of chains pipelined on three streams -- gives the fields, sums and
+    counters of upload_many + run + measure + download_many bit for bit, also
+    with a staging ring smaller than the batch and without graphs; twice in a
+    row (the sweep counters advance)."""
+    from su2higgs_gb300 import workloads
+    if ring:
+        monkeypatch.setenv("SU2GPU_RING_BYTES", ring)
+    specs = workloads.batched_ensemble(40, seed=13)
+    arena = sum(gpu.Pool.chain_bytes(p) for p, _, _ in specs)
+    inputs = [workloads.hot_fields(p, seed) for p, seed, _ in specs]
+
+    def fresh():
+        pool = gpu.Pool(specs[0][0], arena_bytes=arena, max_chains=40)
+        return pool, [pool.add(p, seed=seed, chain=chain) for p, seed, chain in specs]
+
+    a, sa = fresh()
+    b, sb = fresh()
+    pinned = [pinned_copy(gpu, f) for f in inputs]
+    outs = [{n: np.zeros_like(v) for n, v in f.items()} for f in inputs]
+    try:
+        for rep in range(2):
+            a.upload_many(sa, inputs if rep == 0 else want_fields)
+            a.run(3, graph=graph)
+            want_sums = a.measure()
+            want_fields = [{n: np.zeros_like(v) for n, v in f.items()} for f in inputs]
+            a.download_many(sa, want_fields)
+            order = list(range(len(sb)))[::-1]  # the caller's order need not be slot order
+            src = pinned if rep == 0 else [outs[j] for j in range(len(sb))]
+            got_sums = b.cycle([sb[j] for j in order], [src[j] for j in order], 3,
+                               [outs[j] for j in order], graph=graph)
+            for k, j in enumerate(order):
+                assert np.array_equal(got_sums[k], want_sums[sa[j]]), (rep, j)
+                for n in inputs[j]:
+                    assert np.array_equal(outs[j][n], want_fields[j][n]), (rep, j, n)
+        for x, y in zip(sa, sb):
+            assert np.array_equal(a.counters(x), b.counters(y))
+    finally:
+        for f in pinned:
+            unpin(gpu, f)
