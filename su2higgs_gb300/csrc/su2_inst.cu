@@ -2,6 +2,8 @@
 // times with -DSU2_R=<double|float> -DSU2_CC=<content mask or -1>
 // -DSU2_OPS=<table name>; the generic units also carry the content-free
 // kernels (-DSU2_WITH_PREC=<table name>) and, for FP64, the non-template ones.
+#include <algorithm>
+
 #include "su2_kernels.cuh"
 #include "su2_pool.cuh"
 #include "su2_ops.h"
@@ -167,8 +169,14 @@ static void p_measure_local(const void* f, const Geom& g, const Coup& cp, double
 static void p_measure_z(const void* f, const Geom& g, int content, int zdir, double* out, cudaStream_t st) {
   k_measure_z<R><<<g.L[zdir], ZBLOCK, 0, st>>>(*(const Fields<R>*)f, g, content, zdir, out);
 }
+static void p_pool_convert(const void* descs, const ConvItem* items, int n, int vmax, double* staging, int to_device,
+                           cudaStream_t st) {
+  if (n <= 0 || vmax <= 0) return;
+  dim3 grid(std::min(nblk(vmax, 256), 128u), (unsigned)n);
+  k_pool_convert<R><<<grid, 256, 0, st>>>(descs, items, staging, to_device);
+}
 const PrecOps SU2_WITH_PREC = {p_orderparam, p_restore, p_alpha, p_import, p_export, p_reunit, p_fixup,
-                               p_measure_local, p_measure_z};
+                               p_measure_local, p_measure_z, p_pool_convert};
 #endif
 
 #ifdef SU2_WITH_GLOBAL

@@ -32,6 +32,15 @@ struct Ops {
   void (*pool_measure)(const PoolArgs& a, double* partials, unsigned nblocks, cudaStream_t st);
 };
 
+// one chain of a multi-chain field conversion: its pool slot, the fields it
+// carries (bit 1 links, 2 U(1), 4 doublet 0, 8 doublet 1, 16 triplet, 32
+// singlet) and the offset, in doubles, of its host-layout block in staging
+// memory (fields one after another in that order, each [V][components])
+struct ConvItem {
+  int slot, mask;
+  long long off;
+};
+
 struct PrecOps {
   void (*orderparam)(const void* f, const Geom& g, int parity, int op, double* partials, unsigned nblocks,
                      cudaStream_t st);
@@ -47,6 +56,10 @@ struct PrecOps {
   void (*measure_local)(const void* f, const Geom& g, const Coup& cp, double denom, double* out, cudaStream_t st);
   // plane sums along direction zdir: out[L[zdir]][4] (phi^2, Tr Sigma^2, S, S^2)
   void (*measure_z)(const void* f, const Geom& g, int content, int zdir, double* out, cudaStream_t st);
+  // the host-layout FP64 blocks of `n` pool chains in staging memory <-> their
+  // device fields (to_device 1: import, 0: export); vmax = the largest V
+  void (*pool_convert)(const void* descs, const ConvItem* items, int n, int vmax, double* staging, int to_device,
+                       cudaStream_t st);
 };
 
 // instantiations (su2_inst.cu)

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstdarg>
@@ -126,6 +127,9 @@ struct su2gpu_pool {
   std::vector<cudaEvent_t> cyc_ev;
   struct GroupGraph { int a0, a1; cudaGraphExec_t exec; };
   std::vector<GroupGraph> ggraphs;
+  ConvItem* h_items = nullptr;  // page-locked conversion items of a cycle (2 per chain)
+  size_t h_items_n = 0;
+  Buf d_items;
   std::vector<uint32_t*> h_sweeps;
   size_t rsize() const { return prec == 64 ? 8 : 4; }
 };
@@ -402,6 +406,8 @@ int su2gpu_pool_destroy(su2gpu_pool* P) {
   for (cudaEvent_t e : P->ring_ev) cudaEventDestroy(e);
   for (cudaEvent_t e : P->cyc_ev) cudaEventDestroy(e);
   for (auto& gg : P->ggraphs) cudaGraphExecDestroy(gg.exec);
+  if (P->h_items) cudaFreeHost(P->h_items);
+  P->d_items.release();
   if (P->copy_st) cudaStreamDestroy(P->copy_st);
   if (P->down_st) cudaStreamDestroy(P->down_st);
   if (P->own_st) cudaStreamDestroy(P->own_st);
@@ -928,24 +934,76 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
   if (use_graph && nsweeps > 0)
     for (int g = 0; g < G; g++)
       if ((rc = group_graph(P, groups[g], groups[g + 1], &gex[g]))) return rc;
+  // staging bytes of every group; a group's chains sit side by side in the
+  // rings (a ring holds the largest group at least), so a chain only ever
+  // overlaps chains of earlier groups, whose release events are recorded
+  std::vector<size_t> gbytes(G, 0);
+  for (int g = 0; g < G; g++)
+    for (int a = groups[g]; a < groups[g + 1]; a++) gbytes[g] += (size_t)P->slots[P->active[a]].g.V * STAGE_REALS * 8;
+  const size_t gmax = *std::max_element(gbytes.begin(), gbytes.end());
   Ring up, down;
   if ((rc = ensure_stream(&P->copy_st)) || (rc = ensure_stream(&P->down_st)) ||
-      (rc = ensure_ring(P, P->ring, total, largest, &up)) || (rc = ensure_ring(P, P->ring_down, total, largest, &down)) ||
-      (rc = ensure_events(P->cyc_ev, 4 * (size_t)na + 1)))
+      (rc = ensure_ring(P, P->ring, total, gmax, &up)) || (rc = ensure_ring(P, P->ring_down, total, gmax, &down)) ||
+      (rc = ensure_events(P->cyc_ev, 4 * (size_t)G + 1)) || (rc = P->d_items.ensure(2 * (size_t)na * sizeof(ConvItem))))
     return rc;
+  if (P->h_items_n < 2 * (size_t)na) {
+    if (P->h_items) cudaFreeHost(P->h_items);
+    P->h_items = nullptr;
+    P->h_items_n = 0;
+    PCK(cudaMallocHost((void**)&P->h_items, 2 * (size_t)na * sizeof(ConvItem)));
+    P->h_items_n = 2 * (size_t)na;
+  }
   std::vector<cudaEvent_t>& ev = P->cyc_ev;
+  ConvItem* dit = (ConvItem*)P->d_items.p;
   // the fields may still be in use by earlier work on st
-  PCK(cudaEventRecord(ev[4 * na], P->st));
-  PCK(cudaStreamWaitEvent(P->copy_st, ev[4 * na], 0));
-  PCK(cudaStreamWaitEvent(P->down_st, ev[4 * na], 0));
+  PCK(cudaEventRecord(ev[4 * G], P->st));
+  PCK(cudaStreamWaitEvent(P->copy_st, ev[4 * G], 0));
+  PCK(cudaStreamWaitEvent(P->down_st, ev[4 * G], 0));
   int64_t tot[SU2GPU_NCOUNTERS] = {0};
+  // one chain's host arrays and their staging layout
+  auto layout = [&](int a, const double* const* const* tab, double** hp, ConvItem* it, size_t* bytes) {
+    const Slot& sl = P->slots[P->active[a]];
+    const int64_t V = sl.g.V;
+    double* h[6];
+    for (int k = 0; k < 6; k++) h[k] = tab[k] ? (double*)tab[k][pos[a]] : nullptr;
+    const ChainIo io = chain_io(P, V, h, hp);
+    int mask = 0;
+    for (int k = 0; k < io.count; k++) {
+      const int kind = io.kind[k];
+      mask |= kind == 0 ? 1 : kind == 1 ? 2 : kind == 2 ? (4 << io.hid[k]) : kind == 3 ? 16 : 32;
+    }
+    it->slot = P->active[a];
+    it->mask = mask;
+    *bytes = io.total * 8;
+    return io;
+  };
   for (int g = 0; g < G; g++) {
     const int a0 = groups[g], a1 = groups[g + 1];
+    int vmax = 0;
+    for (int a = a0; a < a1; a++) vmax = std::max(vmax, (int)P->slots[P->active[a]].g.V);
+    if (up.head + gbytes[g] > up.cap) up.head = 0;
+    if (down.head + gbytes[g] > down.cap) down.head = 0;
+    // the group's host arrays -> staging (copy engine), then one conversion launch
     for (int a = a0; a < a1; a++) {
-      double* h[6];
-      for (int k = 0; k < 6; k++) h[k] = in[k] ? (double*)in[k][pos[a]] : nullptr;
-      if ((rc = chain_up(P, up, P->active[a], h, ev[4 * a], ev[4 * a + 1], P->copy_st, P->st))) return rc;
+      double* hp[6];
+      size_t bytes, lo;
+      ConvItem& it = P->h_items[a];
+      const ChainIo io = layout(a, in, hp, &it, &bytes);
+      if ((rc = ring_take(up, bytes, P->copy_st, &lo))) return rc;
+      it.off = (long long)(lo / 8);
+      size_t off = 0;
+      for (int k = 0; k < io.count; k++) {
+        PCK(cudaMemcpyAsync((double*)(up.base + lo) + off, hp[k], io.n[k] * 8, cudaMemcpyHostToDevice, P->copy_st));
+        off += io.n[k];
+      }
+      up.live.push_back({lo, lo + bytes, ev[4 * g + 1]});
     }
+    PCK(cudaEventRecord(ev[4 * g], P->copy_st));
+    PCK(cudaStreamWaitEvent(P->st, ev[4 * g], 0));
+    PCK(cudaMemcpyAsync(dit + a0, P->h_items + a0, (a1 - a0) * sizeof(ConvItem), cudaMemcpyHostToDevice, P->st));
+    P->pops->pool_convert(P->descs.p, dit + a0, a1 - a0, vmax, (double*)up.base, 1, P->st);
+    PCK(cudaEventRecord(ev[4 * g + 1], P->st));
+    // sweeps and measurement of the group
     for (int k = 0; k < nsweeps; k++) {
       if (use_graph) {
         PCK(cudaGraphLaunch(gex[g], P->st));
@@ -955,11 +1013,36 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
       }
     }
     if (sums) enqueue_group_measure(P, a0, a1, (double*)P->sums.p);
+    // one conversion launch into staging, then the copies to the host arrays
+    std::vector<std::pair<ChainIo, size_t>> outs;
+    std::vector<std::array<double*, 6>> outp;
     for (int a = a0; a < a1; a++) {
-      double* h[6];
-      for (int k = 0; k < 6; k++) h[k] = out[k] ? out[k][pos[a]] : nullptr;
-      if ((rc = chain_down(P, down, P->active[a], h, ev[4 * a + 2], ev[4 * a + 3], P->st, P->down_st))) return rc;
+      std::array<double*, 6> hp;
+      size_t bytes, lo;
+      ConvItem& it = P->h_items[na + a];
+      const ChainIo io = layout(a, out, hp.data(), &it, &bytes);
+      if ((rc = ring_take(down, bytes, P->st, &lo))) return rc;
+      it.off = (long long)(lo / 8);
+      outs.push_back({io, lo});
+      outp.push_back(hp);
+      down.live.push_back({lo, lo + bytes, ev[4 * g + 3]});
     }
+    PCK(cudaMemcpyAsync(dit + na + a0, P->h_items + na + a0, (a1 - a0) * sizeof(ConvItem), cudaMemcpyHostToDevice,
+                        P->st));
+    P->pops->pool_convert(P->descs.p, dit + na + a0, a1 - a0, vmax, (double*)down.base, 0, P->st);
+    PCK(cudaEventRecord(ev[4 * g + 2], P->st));
+    PCK(cudaStreamWaitEvent(P->down_st, ev[4 * g + 2], 0));
+    for (size_t q = 0; q < outs.size(); q++) {
+      const ChainIo& io = outs[q].first;
+      size_t off = 0;
+      for (int k = 0; k < io.count; k++) {
+        PCK(cudaMemcpyAsync(outp[q][k], (double*)(down.base + outs[q].second) + off, io.n[k] * 8,
+                            cudaMemcpyDeviceToHost, P->down_st));
+        off += io.n[k];
+      }
+    }
+    PCK(cudaEventRecord(ev[4 * g + 3], P->down_st));
+    PCK(cudaGetLastError());
   }
   // half-sweeps of each kind in one sweep of a chain
   {

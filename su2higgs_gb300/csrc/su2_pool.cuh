@@ -8,6 +8,7 @@
 #pragma once
 
 #include "su2_kernels.cuh"
+#include "su2_ops.h"
 
 namespace su2 {
 
@@ -147,6 +148,78 @@ __global__ void __launch_bounds__(BLOCK) k_pool_measure(PoolArgs a, double* part
     if (t < d.g.V) measure_site<R, CC>(d.f, d.g, d.cp, t, AlphaOnTheFly{}, m);
   }
   block_sums_out<CC>(m, d.cp.content, partials, gridDim.x, blockIdx.x);
+}
+
+// Field conversion of many chains in one launch: block row blockIdx.y is
+// chain item y, its blocks stride over the chain's sites; each site moves all
+// the chain's fields between the host layout (FP64, [V][components] per field
+// in staging memory) and the device fields, with the conversions of
+// k_import / k_export.
+template <typename R>
+__global__ void __launch_bounds__(256) k_pool_convert(const void* descs, const ConvItem* items, double* stg,
+                                                      int to_device) {
+  const ConvItem it = items[blockIdx.y];
+  const ChainDesc<R>& d = ((const ChainDesc<R>*)descs)[it.slot];
+  const Fields<R> f = d.f;
+  const long long V = d.g.V;
+  long long o = it.off;
+  const long long o_link = o;
+  if (it.mask & 1) o += 12 * V;
+  const long long o_u1 = o;
+  if (it.mask & 2) o += 3 * V;
+  const long long o_d0 = o;
+  if (it.mask & 4) o += 4 * V;
+  const long long o_d1 = o;
+  if (it.mask & 8) o += 4 * V;
+  const long long o_tr = o;
+  if (it.mask & 16) o += 3 * V;
+  const long long o_s = o;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < V; t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)t;
+    if (it.mask & 1)
+#pragma unroll
+      for (int dd = 0; dd < 3; dd++) {
+        double* s = stg + o_link + (t * 3 + dd) * 4;
+        if (to_device) {
+          st4<R>(f.link[dd], i, Q<R>{(R)s[0], (R)s[1], (R)s[2], (R)s[3]});
+        } else {
+          Q<R> q = ld4<R>(f.link[dd], i);
+          s[0] = q.a; s[1] = q.b; s[2] = q.c; s[3] = q.d;
+        }
+      }
+    if (it.mask & 2)
+#pragma unroll
+      for (int dd = 0; dd < 3; dd++) {
+        double* s = stg + o_u1 + t * 3 + dd;
+        if (to_device) f.u1[dd][i] = (R)*s;
+        else *s = f.u1[dd][i];
+      }
+#pragma unroll
+    for (int h = 0; h < 2; h++)
+      if (it.mask & (4 << h)) {
+        double* s = stg + (h ? o_d1 : o_d0) + t * 4;
+        if (to_device) {
+          st4<R>(f.phi[h], i, Q<R>{(R)s[0], (R)s[1], (R)s[2], (R)s[3]});
+        } else {
+          Q<R> q = ld4<R>(f.phi[h], i);
+          s[0] = q.a; s[1] = q.b; s[2] = q.c; s[3] = q.d;
+        }
+      }
+    if (it.mask & 16) {
+      double* s = stg + o_tr + t * 3;
+      if (to_device) {
+        st3(f, i, V3<R>{(R)s[0], (R)s[1], (R)s[2]});
+      } else {
+        V3<R> v = ld3(f, i);
+        s[0] = v.x; s[1] = v.y; s[2] = v.z;
+      }
+    }
+    if (it.mask & 32) {
+      double* s = stg + o_s + t;
+      if (to_device) f.sing[i] = (R)*s;
+      else *s = f.sing[i];
+    }
+  }
 }
 
 #ifdef SU2_WITH_GLOBAL
