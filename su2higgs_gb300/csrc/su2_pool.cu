@@ -896,6 +896,8 @@ static std::vector<int> cycle_groups(const su2gpu_pool* P) {
   for (int s : P->active) total += P->slots[s].g.V;
   const int64_t bytes = total * STAGE_REALS * 8;
   int G = (int)std::min<int64_t>(8, std::max<int64_t>(1, bytes / (64ll << 20)));
+  const char* e = getenv("SU2GPU_CYCLE_GROUPS");
+  if (e && *e) G = std::max(1, atoi(e));
   G = std::min(G, na);
   std::vector<int> b(1, 0);
   int64_t acc = 0;
