@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <array>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdarg>
@@ -57,6 +58,12 @@ struct Buf {
     n = 0;
   }
 };
+
+__global__ void k_stamp(unsigned long long* out) {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  *out = t;
+}
 
 __global__ void k_cold_links4f(F4* p, int64_t n) {
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -889,7 +896,9 @@ static void enqueue_group_measure(su2gpu_pool* P, int a0, int a1, double* sums) 
   launch_pool_reduce(part, b1 - b0, (const int*)P->mfirst.p + a0, b0, a1 - a0, sums + (size_t)a0 * NSUMS, P->st);
 }
 
-// groups of consecutive active chains with about equal numbers of sites
+// groups of consecutive active chains: the middle ones with about equal
+// numbers of sites, the first and the last a quarter of that (the first
+// group's upload and the last one's download are not hidden under sweeps)
 static std::vector<int> cycle_groups(const su2gpu_pool* P) {
   const int na = (int)P->active.size();
   int64_t total = 0;
@@ -899,11 +908,14 @@ static std::vector<int> cycle_groups(const su2gpu_pool* P) {
   const char* e = getenv("SU2GPU_CYCLE_GROUPS");
   if (e && *e) G = std::max(1, atoi(e));
   G = std::min(G, na);
+  std::vector<double> edge(G + 1, 0.0);  // cumulative weight at each group's end
+  for (int g = 0; g < G; g++) edge[g + 1] = edge[g] + ((G > 2 && (g == 0 || g == G - 1)) ? 0.25 : 1.0);
   std::vector<int> b(1, 0);
   int64_t acc = 0;
   for (int a = 0; a < na; a++) {
     acc += P->slots[P->active[a]].g.V;
-    if ((int)b.size() < G && acc * G >= total * (int64_t)b.size() && a + 1 < na) b.push_back(a + 1);
+    const int k = (int)b.size();
+    if (k < G && a + 1 < na && (double)acc >= (double)total * edge[k] / edge[G]) b.push_back(a + 1);
   }
   b.push_back(na);
   return b;
@@ -962,6 +974,16 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
   PCK(cudaStreamWaitEvent(P->copy_st, ev[4 * G], 0));
   PCK(cudaStreamWaitEvent(P->down_st, ev[4 * G], 0));
   int64_t tot[SU2GPU_NCOUNTERS] = {0};
+  const bool trace = getenv("SU2GPU_CYCLE_TRACE") != nullptr;
+  std::vector<const char*> tname;
+  unsigned long long* dstamp = nullptr;
+  if (trace) cudaMalloc(&dstamp, 256 * sizeof(unsigned long long));
+  auto tmark = [&](const char* nm, cudaStream_t st) {
+    if (!trace || tname.size() >= 256) return;
+    k_stamp<<<1, 1, 0, st>>>(dstamp + tname.size());
+    tname.push_back(nm);
+  };
+  tmark("start", P->st);
   // one chain's host arrays and their staging layout
   auto layout = [&](int a, const double* const* const* tab, double** hp, ConvItem* it, size_t* bytes) {
     const Slot& sl = P->slots[P->active[a]];
@@ -985,7 +1007,8 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
     for (int a = a0; a < a1; a++) vmax = std::max(vmax, (int)P->slots[P->active[a]].g.V);
     if (up.head + gbytes[g] > up.cap) up.head = 0;
     if (down.head + gbytes[g] > down.cap) down.head = 0;
-    // the group's host arrays -> staging (copy engine), then one conversion launch
+    // upload stream: the group's host arrays -> staging (copy engine), then
+    // one conversion launch into the fields
     for (int a = a0; a < a1; a++) {
       double* hp[6];
       size_t bytes, lo;
@@ -1000,12 +1023,13 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
       }
       up.live.push_back({lo, lo + bytes, ev[4 * g + 1]});
     }
-    PCK(cudaEventRecord(ev[4 * g], P->copy_st));
-    PCK(cudaStreamWaitEvent(P->st, ev[4 * g], 0));
-    PCK(cudaMemcpyAsync(dit + a0, P->h_items + a0, (a1 - a0) * sizeof(ConvItem), cudaMemcpyHostToDevice, P->st));
-    P->pops->pool_convert(P->descs.p, dit + a0, a1 - a0, vmax, (double*)up.base, 1, P->st);
-    PCK(cudaEventRecord(ev[4 * g + 1], P->st));
-    // sweeps and measurement of the group
+    tmark("h2d done", P->copy_st);
+    PCK(cudaMemcpyAsync(dit + a0, P->h_items + a0, (a1 - a0) * sizeof(ConvItem), cudaMemcpyHostToDevice, P->copy_st));
+    P->pops->pool_convert(P->descs.p, dit + a0, a1 - a0, vmax, (double*)up.base, 1, P->copy_st);
+    PCK(cudaEventRecord(ev[4 * g + 1], P->copy_st));
+    tmark("import done", P->copy_st);
+    // update stream: the group's sweeps and measurement
+    PCK(cudaStreamWaitEvent(P->st, ev[4 * g + 1], 0));
     for (int k = 0; k < nsweeps; k++) {
       if (use_graph) {
         PCK(cudaGraphLaunch(gex[g], P->st));
@@ -1014,8 +1038,13 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
         if ((rc = enqueue_group_sweep(P, a0, a1, t1))) return rc;
       }
     }
+    tmark("sweeps done", P->st);
     if (sums) enqueue_group_measure(P, a0, a1, (double*)P->sums.p);
-    // one conversion launch into staging, then the copies to the host arrays
+    PCK(cudaEventRecord(ev[4 * g + 2], P->st));
+    tmark("measure done", P->st);
+    // download stream: one conversion launch into staging, then the copies
+    // to the host arrays
+    PCK(cudaStreamWaitEvent(P->down_st, ev[4 * g + 2], 0));
     std::vector<std::pair<ChainIo, size_t>> outs;
     std::vector<std::array<double*, 6>> outp;
     for (int a = a0; a < a1; a++) {
@@ -1023,17 +1052,16 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
       size_t bytes, lo;
       ConvItem& it = P->h_items[na + a];
       const ChainIo io = layout(a, out, hp.data(), &it, &bytes);
-      if ((rc = ring_take(down, bytes, P->st, &lo))) return rc;
+      if ((rc = ring_take(down, bytes, P->down_st, &lo))) return rc;
       it.off = (long long)(lo / 8);
       outs.push_back({io, lo});
       outp.push_back(hp);
       down.live.push_back({lo, lo + bytes, ev[4 * g + 3]});
     }
     PCK(cudaMemcpyAsync(dit + na + a0, P->h_items + na + a0, (a1 - a0) * sizeof(ConvItem), cudaMemcpyHostToDevice,
-                        P->st));
-    P->pops->pool_convert(P->descs.p, dit + na + a0, a1 - a0, vmax, (double*)down.base, 0, P->st);
-    PCK(cudaEventRecord(ev[4 * g + 2], P->st));
-    PCK(cudaStreamWaitEvent(P->down_st, ev[4 * g + 2], 0));
+                        P->down_st));
+    P->pops->pool_convert(P->descs.p, dit + na + a0, a1 - a0, vmax, (double*)down.base, 0, P->down_st);
+    tmark("export done", P->down_st);
     for (size_t q = 0; q < outs.size(); q++) {
       const ChainIo& io = outs[q].first;
       size_t off = 0;
@@ -1044,6 +1072,7 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
       }
     }
     PCK(cudaEventRecord(ev[4 * g + 3], P->down_st));
+    tmark("d2h done", P->down_st);
     PCK(cudaGetLastError());
   }
   // half-sweeps of each kind in one sweep of a chain
@@ -1064,6 +1093,12 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
   PCK(cudaStreamSynchronize(P->copy_st));
   PCK(cudaStreamSynchronize(P->down_st));
   if ((rc = pool_check(P))) return rc;
+  if (trace) {
+    std::vector<unsigned long long> h(tname.size());
+    cudaMemcpy(h.data(), dstamp, h.size() * 8, cudaMemcpyDeviceToHost);
+    for (size_t k = 0; k < h.size(); k++) fprintf(stderr, "cycle trace %2zu %-14s %8.3f ms\n", k, tname[k], (h[k] - h[0]) * 1e-6);
+    cudaFree(dstamp);
+  }
   if (sums)
     for (int a = 0; a < na; a++) memcpy(sums + (size_t)pos[a] * NSUMS, hs.data() + (size_t)a * NSUMS, NSUMS * 8);
   for (int a = 0; a < na; a++) {
