@@ -369,7 +369,11 @@ int su2gpu_pool_create(const su2gpu_params* recipe, int64_t arena_bytes, int32_t
   P->max_slots = max_chains;
   P->slots.resize(max_chains);
   int rc;
-  if (cudaStreamCreateWithFlags(&P->own_st, cudaStreamNonBlocking) != cudaSuccess) {
+  // the update stream at the highest priority: the transfer streams' kernels
+  // (field conversions) fill in around the sweeps instead of displacing them
+  int least = 0, greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  if (cudaStreamCreateWithPriority(&P->own_st, cudaStreamNonBlocking, greatest) != cudaSuccess) {
     delete P;
     return fail(SU2GPU_ERR_CUDA, "cudaStreamCreate failed");
   }
@@ -705,8 +709,11 @@ static int ensure_events(std::vector<cudaEvent_t>& v, size_t n) {
   return SU2GPU_OK;
 }
 
+// a transfer stream, at the lowest priority
 static int ensure_stream(cudaStream_t* st) {
-  if (!*st && cudaStreamCreateWithFlags(st, cudaStreamNonBlocking) != cudaSuccess)
+  int least = 0, greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  if (!*st && cudaStreamCreateWithPriority(st, cudaStreamNonBlocking, least) != cudaSuccess)
     return fail(SU2GPU_ERR_CUDA, "cudaStreamCreate failed");
   return SU2GPU_OK;
 }
