@@ -647,7 +647,9 @@ def run_gpu_batched(args):
 
     # end to end through the pool's host-buffer C ABI: every chain's FP64
     # fields uploaded from page-locked memory, S sweeps, measurement,
-    # every chain downloaded, per step
+    # every chain downloaded, per step -- one su2gpu_pool_cycle call, which
+    # pipelines groups of chains so that their host transfers run under the
+    # sweeps of the others
     e2e = None
     if rank == 0 and not args.no_e2e:
         arrays = [a for _, f in host for a in f.values()]
@@ -662,10 +664,8 @@ def run_gpu_batched(args):
         fields = [f for _, f in host]
 
         def e2e_step():
-            e2e_pool.upload_many(slots, fields)
-            e2e_pool.run(S, graph=True)
-            e2e_pool.measure()
-            e2e_pool.download_many(slots, fields)  # in place, into the same page-locked arrays
+            # in place: the step's results land in the same page-locked arrays
+            e2e_pool.cycle(slots, fields, S)
         e2e_step()
         t0 = time.perf_counter()
         for k in range(n_e2e):

@@ -9,7 +9,6 @@
 
 #include <algorithm>
 #include <array>
-#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdarg>
@@ -58,12 +57,6 @@ struct Buf {
     n = 0;
   }
 };
-
-__global__ void k_stamp(unsigned long long* out) {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  *out = t;
-}
 
 __global__ void k_cold_links4f(F4* p, int64_t n) {
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -911,7 +904,7 @@ static std::vector<int> cycle_groups(const su2gpu_pool* P) {
   int64_t total = 0;
   for (int s : P->active) total += P->slots[s].g.V;
   const int64_t bytes = total * STAGE_REALS * 8;
-  int G = (int)std::min<int64_t>(8, std::max<int64_t>(1, bytes / (64ll << 20)));
+  int G = (int)std::min<int64_t>(16, std::max<int64_t>(1, bytes / (64ll << 20)));
   const char* e = getenv("SU2GPU_CYCLE_GROUPS");
   if (e && *e) G = std::max(1, atoi(e));
   G = std::min(G, na);
@@ -981,16 +974,6 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
   PCK(cudaStreamWaitEvent(P->copy_st, ev[4 * G], 0));
   PCK(cudaStreamWaitEvent(P->down_st, ev[4 * G], 0));
   int64_t tot[SU2GPU_NCOUNTERS] = {0};
-  const bool trace = getenv("SU2GPU_CYCLE_TRACE") != nullptr;
-  std::vector<const char*> tname;
-  unsigned long long* dstamp = nullptr;
-  if (trace) cudaMalloc(&dstamp, 256 * sizeof(unsigned long long));
-  auto tmark = [&](const char* nm, cudaStream_t st) {
-    if (!trace || tname.size() >= 256) return;
-    k_stamp<<<1, 1, 0, st>>>(dstamp + tname.size());
-    tname.push_back(nm);
-  };
-  tmark("start", P->st);
   // one chain's host arrays and their staging layout
   auto layout = [&](int a, const double* const* const* tab, double** hp, ConvItem* it, size_t* bytes) {
     const Slot& sl = P->slots[P->active[a]];
@@ -1030,11 +1013,9 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
       }
       up.live.push_back({lo, lo + bytes, ev[4 * g + 1]});
     }
-    tmark("h2d done", P->copy_st);
     PCK(cudaMemcpyAsync(dit + a0, P->h_items + a0, (a1 - a0) * sizeof(ConvItem), cudaMemcpyHostToDevice, P->copy_st));
     P->pops->pool_convert(P->descs.p, dit + a0, a1 - a0, vmax, (double*)up.base, 1, P->copy_st);
     PCK(cudaEventRecord(ev[4 * g + 1], P->copy_st));
-    tmark("import done", P->copy_st);
     // update stream: the group's sweeps and measurement
     PCK(cudaStreamWaitEvent(P->st, ev[4 * g + 1], 0));
     for (int k = 0; k < nsweeps; k++) {
@@ -1045,10 +1026,8 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
         if ((rc = enqueue_group_sweep(P, a0, a1, t1))) return rc;
       }
     }
-    tmark("sweeps done", P->st);
     if (sums) enqueue_group_measure(P, a0, a1, (double*)P->sums.p);
     PCK(cudaEventRecord(ev[4 * g + 2], P->st));
-    tmark("measure done", P->st);
     // download stream: one conversion launch into staging, then the copies
     // to the host arrays
     PCK(cudaStreamWaitEvent(P->down_st, ev[4 * g + 2], 0));
@@ -1068,7 +1047,6 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
     PCK(cudaMemcpyAsync(dit + na + a0, P->h_items + na + a0, (a1 - a0) * sizeof(ConvItem), cudaMemcpyHostToDevice,
                         P->down_st));
     P->pops->pool_convert(P->descs.p, dit + na + a0, a1 - a0, vmax, (double*)down.base, 0, P->down_st);
-    tmark("export done", P->down_st);
     for (size_t q = 0; q < outs.size(); q++) {
       const ChainIo& io = outs[q].first;
       size_t off = 0;
@@ -1079,7 +1057,6 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
       }
     }
     PCK(cudaEventRecord(ev[4 * g + 3], P->down_st));
-    tmark("d2h done", P->down_st);
     PCK(cudaGetLastError());
   }
   // half-sweeps of each kind in one sweep of a chain
@@ -1100,12 +1077,6 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
   PCK(cudaStreamSynchronize(P->copy_st));
   PCK(cudaStreamSynchronize(P->down_st));
   if ((rc = pool_check(P))) return rc;
-  if (trace) {
-    std::vector<unsigned long long> h(tname.size());
-    cudaMemcpy(h.data(), dstamp, h.size() * 8, cudaMemcpyDeviceToHost);
-    for (size_t k = 0; k < h.size(); k++) fprintf(stderr, "cycle trace %2zu %-14s %8.3f ms\n", k, tname[k], (h[k] - h[0]) * 1e-6);
-    cudaFree(dstamp);
-  }
   if (sums)
     for (int a = 0; a < na; a++) memcpy(sums + (size_t)pos[a] * NSUMS, hs.data() + (size_t)a * NSUMS, NSUMS * 8);
   for (int a = 0; a < na; a++) {
