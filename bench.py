@@ -19,7 +19,9 @@ value      site-updates/s = sites * sweeps / (sum of per-step CUDA-event
            write flushes L2 between steps, outside the events
 e2e        the same metric through the host-buffer C ABI (FP64 AoS host
            arrays, page-locked): upload of every chain + sweeps + measure +
-           download per step, wall clock
+           download per step, wall clock; the batched workloads make one
+           su2gpu_pool_cycle call per step (groups of chains pipelined over
+           the copy engines and the update kernels)
 fp64_plain the plain FP64 single-lattice sweep on the same lattices run one
            after another (the metric's comparison)
 roofline   the kernel kind with the largest share of profiled sweeps (CUDA
