@@ -438,6 +438,7 @@ class Pool:
                                        ctypes.byref(self._h)))
 
     def close(self):
+        self.__dict__.pop("_tcache", None)
         if getattr(self, "_h", None) and self._h.value:
             lib().su2gpu_pool_destroy(self._h)
             self._h = ctypes.c_void_p()
@@ -510,6 +511,23 @@ class Pool:
         keep.append(tables)
         return ctypes.cast(tables, ctypes.c_void_p)
 
+    def _cached_tables(self, key, n, fields):
+        """Pointer tables of `fields`, rebuilt only when the arrays are not
+        the very objects of the previous call (a batch cycled in place passes
+        the same arrays every step)."""
+        arrs = [f.get(name) for f in fields for name in FIELD_NAMES]
+        cache = self.__dict__.setdefault("_tcache", {})
+        hit = cache.get(key)
+        if hit is not None and len(hit[0]) == len(arrs) and all(x is y for x, y in zip(hit[0], arrs)):
+            return hit[1]
+        for a in arrs:
+            if a is not None and (a.dtype != np.float64 or not a.flags.c_contiguous):
+                raise ValueError("cycle needs C-contiguous float64 arrays")
+        keep = []
+        tables = self._tables(n, fields, keep)
+        cache[key] = (arrs, tables, keep)
+        return tables
+
     def _many(self, fn, slots, fields):
         n = len(slots)
         keep = []
@@ -523,14 +541,9 @@ class Pool:
         fields_out (default: in place into fields_in).  Returns the
         measurement sums, one row per slot."""
         fields_out = fields_in if fields_out is None else fields_out
-        for f in list(fields_in) + list(fields_out):
-            for a in f.values():
-                if a is not None and (a.dtype != np.float64 or not a.flags.c_contiguous):
-                    raise ValueError("cycle needs C-contiguous float64 arrays")
         n = len(slots)
-        keep = []
-        tin = self._tables(n, fields_in, keep)
-        tout = self._tables(n, fields_out, keep)
+        tin = self._cached_tables("in", n, fields_in)
+        tout = self._cached_tables("out", n, fields_out)
         sums = np.zeros((n, abi.NMEAS))
         sl = np.ascontiguousarray(slots, dtype=np.int32)
         check(lib().su2gpu_pool_cycle(self._h, n, _p(sl), tin, nsweeps, 1 if graph else 0, _p(sums), tout))
