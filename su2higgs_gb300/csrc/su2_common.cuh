@@ -314,27 +314,6 @@ __device__ inline V3<R> qrot(const Q<R>& u, const V3<R>& b) {
   return V3<R>{u.a * px - pa * u.b + (py * u.d - pz * u.c), u.a * py - pa * u.c + (pz * u.b - px * u.d),
                u.a * pz - pa * u.d + (px * u.c - py * u.b)};
 }
-// Two adjoint rotations at once, (u, b) in lane 0 and (v, c) in lane 1 of
-// Blackwell's paired FP32 instructions: the formula of qrot term by term,
-// one paired instruction per scalar operation of both rotations.
-__device__ inline void qrot_pair(const Q<float>& u, const V3<float>& b, const Q<float>& v, const V3<float>& c,
-                                 V3<float>& r, V3<float>& s) {
-  const float2 ua{u.a, v.a}, ub{u.b, v.b}, uc{u.c, v.c}, ud{u.d, v.d};
-  const float2 nub{-u.b, -v.b}, nuc{-u.c, -v.c}, nud{-u.d, -v.d};
-  const float2 bx{b.x, c.x}, by{b.y, c.y}, bz{b.z, c.z};
-  // -(real part) of u (0, b), and its vector part
-  const float2 na = __ffma2_rn(ud, bz, __ffma2_rn(uc, by, __fmul2_rn(ub, bx)));
-  const float2 px = __ffma2_rn(ud, by, __ffma2_rn(nuc, bz, __fmul2_rn(ua, bx)));
-  const float2 py = __ffma2_rn(ub, bz, __ffma2_rn(nud, bx, __fmul2_rn(ua, by)));
-  const float2 pz = __ffma2_rn(uc, bx, __ffma2_rn(nub, by, __fmul2_rn(ua, bz)));
-  // vector part of (u (0, b)) u^dagger
-  const float2 rx = __ffma2_rn(nuc, pz, __ffma2_rn(ud, py, __ffma2_rn(na, ub, __fmul2_rn(ua, px))));
-  const float2 ry = __ffma2_rn(nud, px, __ffma2_rn(ub, pz, __ffma2_rn(na, uc, __fmul2_rn(ua, py))));
-  const float2 rz = __ffma2_rn(nub, py, __ffma2_rn(uc, px, __ffma2_rn(na, ud, __fmul2_rn(ua, pz))));
-  r = V3<float>{rx.x, ry.x, rz.x};
-  s = V3<float>{rx.y, ry.y, rz.y};
-}
-
 template <typename R>
 __device__ inline R dot3(const V3<R>& a, const V3<R>& b) {
   return a.x * b.x + a.y * b.y + a.z * b.z;

@@ -609,18 +609,10 @@ __device__ inline int overrelax_triplet(const Fields<R>& f, const Geom& g, const
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     int xp = shifted(g, c, d, 1), xm = shifted(g, c, d, -1);
-    if constexpr (sizeof(R) == 4) {
-      // FP32: the forward and the backward rotation in the two lanes of the
-      // paired FP32 instructions
-      V3<float> r1, r2;
-      qrot_pair(ld4<R>(lk(f, d), i), ld3(f, xp), qdag(ld4<R>(lk(f, d), xm)), ld3(f, xm), r1, r2);
-      s.x -= r1.x + r2.x; s.y -= r1.y + r2.y; s.z -= r1.z + r2.z;
-    } else {
-      V3<R> r = qrot(ld4<R>(lk(f, d), i), ld3(f, xp));
-      s.x -= r.x; s.y -= r.y; s.z -= r.z;
-      r = qrot(qdag(ld4<R>(lk(f, d), xm)), ld3(f, xm));
-      s.x -= r.x; s.y -= r.y; s.z -= r.z;
-    }
+    V3<R> r = qrot(ld4<R>(lk(f, d), i), ld3(f, xp));
+    s.x -= r.x; s.y -= r.y; s.z -= r.z;
+    r = qrot(qdag(ld4<R>(lk(f, d), xm)), ld3(f, xm));
+    s.x -= r.x; s.y -= r.y; s.z -= r.z;
   }
   V3<R> t = ld3(f, i);
   R F = msqrt(s.x * s.x + s.y * s.y + s.z * s.z);
