@@ -252,6 +252,18 @@ __device__ inline Q<R> ld4(const V4<R>* p, int i) {
   V4<R> v = p[i];
   return Q<R>{v.x, v.y, v.z, v.w};
 }
+// A load through the read-only data path, for values no thread writes during
+// the launch (a pass's neighbours of the other parity, the fields it does not
+// update); FP32 4-vectors as one 16-byte load, FP64 through the plain path.
+template <typename R>
+__device__ inline Q<R> ldro4(const V4<R>* p, int i) {
+  if constexpr (sizeof(R) == 4) {
+    float4 v = __ldg((const float4*)p + i);
+    return Q<R>{v.x, v.y, v.z, v.w};
+  } else {
+    return ld4<R>(p, i);
+  }
+}
 template <typename R>
 __device__ inline void st4(V4<R>* p, int i, const Q<R>& q) {
   V4<R> v;
@@ -349,6 +361,11 @@ __device__ inline V4<R>* php(const Fields<R>& f, int h) {
 template <typename R>
 __device__ inline V3<R> ld3(const Fields<R>& f, int i) {
   return V3<R>{f.trip[0][i], f.trip[1][i], f.trip[2][i]};
+}
+// the triplet of a site no thread writes during the launch (see ldro4)
+template <typename R>
+__device__ inline V3<R> ldro3(const Fields<R>& f, int i) {
+  return V3<R>{__ldg(f.trip[0] + i), __ldg(f.trip[1] + i), __ldg(f.trip[2] + i)};
 }
 template <typename R>
 __device__ inline void st3(const Fields<R>& f, int i, const V3<R>& v) {

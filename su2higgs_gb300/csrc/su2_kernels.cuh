@@ -80,9 +80,9 @@ __device__ inline Q<R> wilson_staple(const Fields<R>& f, const Geom& g, const in
     int xn = shifted(g, c, nu, 1);
     int xpm = shifted(g, c, mu, 1, nu, -1);
     int xm = shifted(g, c, nu, -1);
-    Q<R> up = qmul(qmul(ld4<R>(lk(f, nu), xp), qdag(ld4<R>(lk(f, mu), xn))), qdag(ld4<R>(lk(f, nu), i)));
+    Q<R> up = qmul(qmul(ldro4<R>(lk(f, nu), xp), qdag(ldro4<R>(lk(f, mu), xn))), qdag(ldro4<R>(lk(f, nu), i)));
     tot = qadd(tot, up);
-    Q<R> lo = qmul(qmul(qdag(ld4<R>(lk(f, nu), xpm)), qdag(ld4<R>(lk(f, mu), xm))), ld4<R>(lk(f, nu), xm));
+    Q<R> lo = qmul(qmul(qdag(ldro4<R>(lk(f, nu), xpm)), qdag(ldro4<R>(lk(f, mu), xm))), ldro4<R>(lk(f, nu), xm));
     tot = qadd(tot, lo);
   }
   return tot;
@@ -92,7 +92,7 @@ __device__ inline Q<R> wilson_staple(const Fields<R>& f, const Geom& g, const in
 template <typename R>
 __device__ inline R hop_triplet_fwd_u(const Fields<R>& f, const Geom& g, const int* c, int i, int mu,
                                       const Q<R>& U) {
-  V3<R> r = qrot(U, ld3(f, shifted(g, c, mu, 1)));
+  V3<R> r = qrot(U, ldro3(f, shifted(g, c, mu, 1)));
   return -dot3(ld3(f, i), r);
 }
 
@@ -105,9 +105,9 @@ __device__ inline Q<R> link_staple(const Fields<R>& f, const Geom& g, const Coup
   if (nh > 0) {
     int xp = shifted(g, c, mu, 1);
     for (int h = 0; h < nh; h++) {
-      Q<R> nphi = ld4<R>(php(f, h), xp);
+      Q<R> nphi = ldro4<R>(php(f, h), xp);
       if (HAS(C_U1)) nphi = qmul(nphi, u1phase(a1p(f, mu)[i]));
-      Q<R> t = qmul(nphi, qdag(ld4<R>(php(f, h), i)));
+      Q<R> t = qmul(nphi, qdag(ldro4<R>(php(f, h), i)));
       V.a -= (R)0.5 * t.a;
       V.b -= (R)0.5 * t.b;
       V.c -= (R)0.5 * t.c;
@@ -227,10 +227,10 @@ __device__ inline Q<R> staple_doublet(const Fields<R>& f, const Geom& g, const C
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     int xp = shifted(g, c, d, 1), xm = shifted(g, c, d, -1);
-    Q<R> w = qmul(ld4<R>(lk(f, d), i), ld4<R>(php(f, h), xp));
+    Q<R> w = qmul(ldro4<R>(lk(f, d), i), ldro4<R>(php(f, h), xp));
     if (HAS(C_U1)) w = qmul(w, u1phase(a1p(f, d)[i]));
     res.a -= w.a; res.b -= w.b; res.c -= w.c; res.d -= w.d;
-    w = qmul(qdag(ld4<R>(lk(f, d), xm)), ld4<R>(php(f, h), xm));
+    w = qmul(qdag(ldro4<R>(lk(f, d), xm)), ldro4<R>(php(f, h), xm));
     if (HAS(C_U1)) w = qmul(w, qdag(u1phase(a1p(f, d)[xm])));
     res.a -= w.a; res.b -= w.b; res.c -= w.c; res.d -= w.d;
   }
@@ -609,9 +609,9 @@ __device__ inline int overrelax_triplet(const Fields<R>& f, const Geom& g, const
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     int xp = shifted(g, c, d, 1), xm = shifted(g, c, d, -1);
-    V3<R> r = qrot(ld4<R>(lk(f, d), i), ld3(f, xp));
+    V3<R> r = qrot(ldro4<R>(lk(f, d), i), ldro3(f, xp));
     s.x -= r.x; s.y -= r.y; s.z -= r.z;
-    r = qrot(qdag(ld4<R>(lk(f, d), xm)), ld3(f, xm));
+    r = qrot(qdag(ldro4<R>(lk(f, d), xm)), ldro3(f, xm));
     s.x -= r.x; s.y -= r.y; s.z -= r.z;
   }
   V3<R> t = ld3(f, i);
