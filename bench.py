@@ -57,6 +57,11 @@ WORKLOADS = {
     "fund64_f64": ("fund", (64, 64, 64), 64),
     "fund16_f64": ("fund", (16, 16, 16), 64),
     "fund160_f32": ("fund", (160, 160, 160), 32),
+    # multicanonical SU(2) x U(1) + singlet, 96^3, beta_G 8, beta_U1 24: a
+    # seeded piecewise-linear weight over phi^2 (256 bins on [0, 3]), one
+    # global accept/reject per Higgs sweep; a gradient flow t = 0..4, step
+    # 0.01, timed after the sweeps
+    "muca96_su2u1s_f32": ("su2u1s", (96, 96, 96), 32),
 }
 
 BATCHED = {
@@ -76,10 +81,22 @@ BATCHED = {
 # needs the old link): 8 + 4 + 2 + the triplet everywhere (3) -> 17; a triplet
 # pass reads all links (12) and the triplet everywhere (3) and writes half of
 # it (1.5) -> 16.5.
-REALS_PER_SITE = {"fund": {0: 16, 2: 18}, "adj": {0: 17, 3: 16.5}}
+# SU(2) x U(1) + singlet content: the SU(2) link heatbath reads the two other
+# directions (8), the updated one at the other parity (2), the doublet (4) and
+# the U(1) angle of the updated direction at the updated sites (0.5), and
+# writes half the direction (2) -> 16.5; a U(1) pass reads the angles of the
+# two other directions (2), the updated one everywhere and writes half (1.5),
+# the doublet (4) and the SU(2) link at the updated sites (2) -> 9.5; a
+# doublet pass reads all links (12), all angles (3), the doublet everywhere
+# (4), the singlet at the updated sites (0.5), writes half the doublet (2) and,
+# multicanonical, its backup (2) -> 23.5; a singlet pass reads the singlet
+# everywhere (1) and the doublet at the updated sites (2), writes half (0.5)
+# -> 3.5.
+REALS_PER_SITE = {"fund": {0: 16, 2: 18}, "adj": {0: 17, 3: 16.5}, "su2u1s": {0: 16.5, 1: 9.5, 2: 23.5, 4: 3.5}}
 # Compulsory reals per site-update of a whole sweep (6 link half-passes, 10
 # scalar half-passes, one measurement reading every field once)
-REALS_PER_SITE_UPDATE = {"fund": 6 * 16 + 10 * 18 + 16, "adj": 6 * 17 + 10 * 16.5 + 15}
+REALS_PER_SITE_UPDATE = {"fund": 6 * 16 + 10 * 18 + 16, "adj": 6 * 17 + 10 * 16.5 + 15,
+                         "su2u1s": 6 * 16.5 + 6 * 9.5 + 10 * 23.5 + 10 * 3.5 + 20}
 REALS_MEASURE = 16
 KIND_NAMES = {0: "link_heatbath", 1: "u1_metropolis", 2: "doublet_update", 3: "triplet_update",
               4: "singlet_update", 5: "reunitarize"}
@@ -338,13 +355,21 @@ def run_gpu(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
+    from su2higgs_gb300 import workloads
     content, L, prec = WORKLOADS[args.workload]
-    p = abi.make_params(content, L=L, precision=prec)
+    muca = args.workload.startswith("muca")
+    p = workloads.muca_params(prec) if muca else abi.make_params(content, L=L, precision=prec)
     V = p.sites()
     seed = replica_seed(20261203, rank)
-    f = hot_fields(p, seed)
+    f = workloads.hot_fields(p, seed, phi_sigma=0.5, sing_sigma=0.3) if muca else hot_fields(p, seed)
     lat = gpu.Lattice(p, seed=seed, chain=rank)
     lat.upload(**f)
+    weight = None
+    if muca:
+        weight = workloads.muca_weight(seed)
+        lat.muca_set(weight.struct)
+        lat.calc_orderparam(0)
+        lat.calc_orderparam(1)
     if args.variants:
         variants = np.array([int(x) for x in args.variants.split(",")], dtype=np.int32)
         lat.set_variants(variants)
@@ -440,12 +465,32 @@ def run_gpu(args):
                "d2h_bytes_per_step": h2d + abi.NMEAS * 8, "steps": n_e2e}
         lat2.close()
 
+    # multicanonical statistics of the timed sweeps, and the gradient flow
+    muca_info = flow = None
+    if muca:
+        cnt = lat.counters()
+        muca_info = {"bins": workloads.MUCA_BINS, "range": list(workloads.MUCA_RANGE), "orderparam": "phi^2",
+                     "checks_per_higgs_sweep": 1, "mode": "read-only weight",
+                     "checks": int(cnt[abi.C_TOTAL_MUCA]), "accepted": int(cnt[abi.C_ACC_MUCA]),
+                     "phi2_last": float(lat.calc_orderparam(0))}
+        if rank == 0:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rows = lat.grad_flow(4.0, 0.01, 10)
+            tf = time.perf_counter() - t0
+            flow = {"t_max": 4.0, "dt": 0.01, "steps": 400, "measurements": int(len(rows)), "ms": 1e3 * tf,
+                    "site_steps_per_s": V * 400 / tf}
+
     # the plain FP64 sweep on the same lattice (the metric's comparison)
     fp64 = None
     if rank == 0 and prec == 32 and not args.no_fp64:
-        p64 = abi.make_params(content, L=L, precision=64)
+        p64 = workloads.muca_params(64) if muca else abi.make_params(content, L=L, precision=64)
         lat64 = gpu.Lattice(p64, seed=seed)
         lat64.upload(**f)
+        if muca:
+            lat64.muca_set(weight.struct)
+            lat64.calc_orderparam(0)
+            lat64.calc_orderparam(1)
         lat64.autotune()
         lat64.set_stream(stream.cuda_stream)
         n64 = max(3, min(K // 4, 25))
@@ -482,14 +527,20 @@ def run_gpu(args):
             "dtype": "f32" if prec == 32 else "f64", "data": "synthetic",
             "config": {"workload": args.workload, "content": content, "lattice": list(L),
                        "precision": f"FP{prec} fields, FP64 reductions" if prec == 32 else "FP64",
-                       "recipe": "1 link heatbath + 4 doublet overrelax + 1 doublet Metropolis, measure each sweep",
-                       "couplings": {"betasu2": p.betasu2, "msq": p.msq_phi, "lambda": p.lambda_phi},
+                       "recipe": ("1 SU(2) link heatbath + 1 U(1) Metropolis + 4 doublet and singlet overrelax + "
+                                  "1 Metropolis, a global multicanonical check after each doublet half-sweep, "
+                                  "measure each sweep") if muca else
+                                 "1 link heatbath + 4 doublet overrelax + 1 doublet Metropolis, measure each sweep",
+                       "couplings": {"betasu2": p.betasu2, "betau1": p.betau1, "msq": p.msq_phi,
+                                     "lambda": p.lambda_phi} if muca else
+                                    {"betasu2": p.betasu2, "msq": p.msq_phi, "lambda": p.lambda_phi},
                        "reunitarize_interval": p.reunitarize_interval if prec == 32 else None,
                        "l2": "flushed between steps (256 MiB write outside the step events)",
                        "parallelism": f"replicas x{world}", "graph": True,
                        "launch_variants": [int(v) for v in variants]},
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "fp64_plain": fp64,
             "sweep_roofline": sweep_roofline(value / world, content, prec),
+            "multicanonical": muca_info, "gradient_flow": flow,
             # per step: the sweep's kernels, the sweep-counter set/increment, measure + reduction
             "gpu_launches": int(K * (launches_sweep + 4)),
             "clocks": clk, "wall_s_timed_region": t_wall,
