@@ -314,17 +314,22 @@ template <typename R>
 struct V3 {
   R x, y, z;
 };
-// vec(u (0,b) u^dagger): the adjoint rotation of a triplet by a link
+// vec(u (0,b) u^dagger): the adjoint rotation of a triplet by a link.
+// Written out with explicit fused multiply-adds: the zero real part of (0, b)
+// and the real part of the result are never formed, and the rounding of every
+// step is fixed by the source, so every kernel that rotates -- whatever it
+// computes around the rotation -- gets the same bits.
+__device__ inline float fmaR(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ inline double fmaR(double a, double b, double c) { return fma(a, b, c); }
 template <typename R>
 __device__ inline V3<R> qrot(const Q<R>& u, const V3<R>& b) {
-  // vector part of (u (0, b)) u^dagger, written out: the zero real part of
-  // (0, b) and the real part of the result are never formed
-  const R pa = -(u.b * b.x + u.c * b.y + u.d * b.z);
-  const R px = u.a * b.x - (u.c * b.z - u.d * b.y);
-  const R py = u.a * b.y - (u.d * b.x - u.b * b.z);
-  const R pz = u.a * b.z - (u.b * b.y - u.c * b.x);
-  return V3<R>{u.a * px - pa * u.b + (py * u.d - pz * u.c), u.a * py - pa * u.c + (pz * u.b - px * u.d),
-               u.a * pz - pa * u.d + (px * u.c - py * u.b)};
+  const R na = fmaR(u.d, b.z, fmaR(u.c, b.y, u.b * b.x));  // -(real part of u (0, b))
+  const R px = fmaR(u.a, b.x, -fmaR(u.c, b.z, -(u.d * b.y)));
+  const R py = fmaR(u.a, b.y, -fmaR(u.d, b.x, -(u.b * b.z)));
+  const R pz = fmaR(u.a, b.z, -fmaR(u.b, b.y, -(u.c * b.x)));
+  return V3<R>{fmaR(u.a, px, fmaR(na, u.b, fmaR(py, u.d, -(pz * u.c)))),
+               fmaR(u.a, py, fmaR(na, u.c, fmaR(pz, u.b, -(px * u.d)))),
+               fmaR(u.a, pz, fmaR(na, u.d, fmaR(px, u.c, -(py * u.b))))};
 }
 template <typename R>
 __device__ inline R dot3(const V3<R>& a, const V3<R>& b) {
