@@ -15,35 +15,35 @@ constexpr int CCI = SU2_CC;
 
 template <int V>
 static unsigned l_link_v(const void* f, const PassArgs& a, cudaStream_t st) {
-  constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB, SP = Variant<R, V>::SPT;
-  unsigned nb = (unsigned)((a.t_hi - a.t_lo + BS * SP - 1) / (BS * SP));
+  constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB;
+  unsigned nb = (unsigned)((a.t_hi - a.t_lo + BS - 1) / BS);
   if (!nb) return 0;
   const Fields<R>& F = *(const Fields<R>*)f;
-  if (a.sub == 0) k_link<R, CCI, 0, BS, MB, SP><<<nb, BS, 0, st>>>(F, a);
-  else if (a.sub == 1) k_link<R, CCI, 1, BS, MB, SP><<<nb, BS, 0, st>>>(F, a);
-  else k_link<R, CCI, 2, BS, MB, SP><<<nb, BS, 0, st>>>(F, a);
+  if (a.sub == 0) k_link<R, CCI, 0, BS, MB><<<nb, BS, 0, st>>>(F, a);
+  else if (a.sub == 1) k_link<R, CCI, 1, BS, MB><<<nb, BS, 0, st>>>(F, a);
+  else k_link<R, CCI, 2, BS, MB><<<nb, BS, 0, st>>>(F, a);
   return nb;
 }
 template <int V>
 static unsigned l_u1_v(const void* f, const PassArgs& a, cudaStream_t st) {
-  constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB, SP = Variant<R, V>::SPT;
-  unsigned nb = (unsigned)((a.t_hi - a.t_lo + BS * SP - 1) / (BS * SP));
+  constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB;
+  unsigned nb = (unsigned)((a.t_hi - a.t_lo + BS - 1) / BS);
   if (!nb) return 0;
   const Fields<R>& F = *(const Fields<R>*)f;
-  if (a.sub == 0) k_u1<R, CCI, 0, BS, MB, SP><<<nb, BS, 0, st>>>(F, a);
-  else if (a.sub == 1) k_u1<R, CCI, 1, BS, MB, SP><<<nb, BS, 0, st>>>(F, a);
-  else k_u1<R, CCI, 2, BS, MB, SP><<<nb, BS, 0, st>>>(F, a);
+  if (a.sub == 0) k_u1<R, CCI, 0, BS, MB><<<nb, BS, 0, st>>>(F, a);
+  else if (a.sub == 1) k_u1<R, CCI, 1, BS, MB><<<nb, BS, 0, st>>>(F, a);
+  else k_u1<R, CCI, 2, BS, MB><<<nb, BS, 0, st>>>(F, a);
   return nb;
 }
 template <int V>
 static unsigned l_scalar_v(int field, const void* f, const PassArgs& a, cudaStream_t st) {
-  constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB, SP = Variant<R, V>::SPT;
-  unsigned nb = (unsigned)((a.t_hi - a.t_lo + BS * SP - 1) / (BS * SP));
+  constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB;
+  unsigned nb = (unsigned)((a.t_hi - a.t_lo + BS - 1) / BS);
   if (!nb) return 0;
   const Fields<R>& F = *(const Fields<R>*)f;
-  if (field == 0) k_scalar<R, CCI, 0, BS, MB, SP><<<nb, BS, 0, st>>>(F, a);
-  else if (field == 1) k_scalar<R, CCI, 1, BS, MB, SP><<<nb, BS, 0, st>>>(F, a);
-  else k_scalar<R, CCI, 2, BS, MB, SP><<<nb, BS, 0, st>>>(F, a);
+  if (field == 0) k_scalar<R, CCI, 0, BS, MB><<<nb, BS, 0, st>>>(F, a);
+  else if (field == 1) k_scalar<R, CCI, 1, BS, MB><<<nb, BS, 0, st>>>(F, a);
+  else k_scalar<R, CCI, 2, BS, MB><<<nb, BS, 0, st>>>(F, a);
   return nb;
 }
 static unsigned l_link(int v, const void* f, const PassArgs& a, cudaStream_t st) {
@@ -51,7 +51,6 @@ static unsigned l_link(int v, const void* f, const PassArgs& a, cudaStream_t st)
     case 1: return l_link_v<1>(f, a, st);
     case 2: return l_link_v<2>(f, a, st);
     case 3: return l_link_v<3>(f, a, st);
-    case 4: return l_link_v<4>(f, a, st);
     default: return l_link_v<0>(f, a, st);
   }
 }
@@ -60,7 +59,6 @@ static unsigned l_u1(int v, const void* f, const PassArgs& a, cudaStream_t st) {
     case 1: return l_u1_v<1>(f, a, st);
     case 2: return l_u1_v<2>(f, a, st);
     case 3: return l_u1_v<3>(f, a, st);
-    case 4: return l_u1_v<4>(f, a, st);
     default: return l_u1_v<0>(f, a, st);
   }
 }
@@ -69,7 +67,6 @@ static unsigned l_scalar(int v, int field, const void* f, const PassArgs& a, cud
     case 1: return l_scalar_v<1>(field, f, a, st);
     case 2: return l_scalar_v<2>(field, f, a, st);
     case 3: return l_scalar_v<3>(field, f, a, st);
-    case 4: return l_scalar_v<4>(field, f, a, st);
     default: return l_scalar_v<0>(field, f, a, st);
   }
 }
@@ -84,34 +81,33 @@ static void l_flow(const void* fin, const void* fout, const Geom& g, const Coup&
 
 template <int V>
 static void lp_link_v(const PoolArgs& a, unsigned nb, cudaStream_t st) {
-  constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB, SP = Variant<R, V>::SPT;
+  constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB;
   if (!nb) return;
-  if (a.sub == 0) k_pool_link<R, CCI, 0, BS, MB, SP><<<nb, BS, 0, st>>>(a);
-  else if (a.sub == 1) k_pool_link<R, CCI, 1, BS, MB, SP><<<nb, BS, 0, st>>>(a);
-  else k_pool_link<R, CCI, 2, BS, MB, SP><<<nb, BS, 0, st>>>(a);
+  if (a.sub == 0) k_pool_link<R, CCI, 0, BS, MB><<<nb, BS, 0, st>>>(a);
+  else if (a.sub == 1) k_pool_link<R, CCI, 1, BS, MB><<<nb, BS, 0, st>>>(a);
+  else k_pool_link<R, CCI, 2, BS, MB><<<nb, BS, 0, st>>>(a);
 }
 template <int V>
 static void lp_u1_v(const PoolArgs& a, unsigned nb, cudaStream_t st) {
-  constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB, SP = Variant<R, V>::SPT;
+  constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB;
   if (!nb) return;
-  if (a.sub == 0) k_pool_u1<R, CCI, 0, BS, MB, SP><<<nb, BS, 0, st>>>(a);
-  else if (a.sub == 1) k_pool_u1<R, CCI, 1, BS, MB, SP><<<nb, BS, 0, st>>>(a);
-  else k_pool_u1<R, CCI, 2, BS, MB, SP><<<nb, BS, 0, st>>>(a);
+  if (a.sub == 0) k_pool_u1<R, CCI, 0, BS, MB><<<nb, BS, 0, st>>>(a);
+  else if (a.sub == 1) k_pool_u1<R, CCI, 1, BS, MB><<<nb, BS, 0, st>>>(a);
+  else k_pool_u1<R, CCI, 2, BS, MB><<<nb, BS, 0, st>>>(a);
 }
 template <int V>
 static void lp_scalar_v(int field, const PoolArgs& a, unsigned nb, cudaStream_t st) {
-  constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB, SP = Variant<R, V>::SPT;
+  constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB;
   if (!nb) return;
-  if (field == 0) k_pool_scalar<R, CCI, 0, BS, MB, SP><<<nb, BS, 0, st>>>(a);
-  else if (field == 1) k_pool_scalar<R, CCI, 1, BS, MB, SP><<<nb, BS, 0, st>>>(a);
-  else k_pool_scalar<R, CCI, 2, BS, MB, SP><<<nb, BS, 0, st>>>(a);
+  if (field == 0) k_pool_scalar<R, CCI, 0, BS, MB><<<nb, BS, 0, st>>>(a);
+  else if (field == 1) k_pool_scalar<R, CCI, 1, BS, MB><<<nb, BS, 0, st>>>(a);
+  else k_pool_scalar<R, CCI, 2, BS, MB><<<nb, BS, 0, st>>>(a);
 }
 static void lp_link(int v, const PoolArgs& a, unsigned nb, cudaStream_t st) {
   switch (v) {
     case 1: lp_link_v<1>(a, nb, st); break;
     case 2: lp_link_v<2>(a, nb, st); break;
     case 3: lp_link_v<3>(a, nb, st); break;
-    case 4: lp_link_v<4>(a, nb, st); break;
     default: lp_link_v<0>(a, nb, st);
   }
 }
@@ -120,7 +116,6 @@ static void lp_u1(int v, const PoolArgs& a, unsigned nb, cudaStream_t st) {
     case 1: lp_u1_v<1>(a, nb, st); break;
     case 2: lp_u1_v<2>(a, nb, st); break;
     case 3: lp_u1_v<3>(a, nb, st); break;
-    case 4: lp_u1_v<4>(a, nb, st); break;
     default: lp_u1_v<0>(a, nb, st);
   }
 }
@@ -129,7 +124,6 @@ static void lp_scalar(int v, int field, const PoolArgs& a, unsigned nb, cudaStre
     case 1: lp_scalar_v<1>(field, a, nb, st); break;
     case 2: lp_scalar_v<2>(field, a, nb, st); break;
     case 3: lp_scalar_v<3>(field, a, nb, st); break;
-    case 4: lp_scalar_v<4>(field, a, nb, st); break;
     default: lp_scalar_v<0>(field, a, nb, st);
   }
 }

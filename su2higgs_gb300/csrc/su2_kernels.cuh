@@ -28,19 +28,15 @@ struct MinBlocks {
 // launch shapes of the update kernels the autotuner chooses from:
 // (threads per block, resident blocks per SM asked of the compiler, which
 // sets the register budget: 65536 / (threads * blocks))
-// and sites per thread (SPT): with two, a thread holds the neighbour values of
-// both of its sites before it updates either, so their loads overlap
-constexpr int NVARIANTS = 5;
+constexpr int NVARIANTS = 4;
 template <typename R, int V>
 struct Variant;
-template <typename R> struct Variant<R, 0> { static constexpr int BS = 128, MINB = sizeof(R) == 4 ? 8 : 4, SPT = 1; };
-template <typename R> struct Variant<R, 1> { static constexpr int BS = 128, MINB = sizeof(R) == 4 ? 5 : 3, SPT = 1; };
-template <typename R> struct Variant<R, 2> { static constexpr int BS = 256, MINB = sizeof(R) == 4 ? 4 : 2, SPT = 1; };
-template <typename R> struct Variant<R, 3> { static constexpr int BS = 64, MINB = sizeof(R) == 4 ? 12 : 6, SPT = 1; };
-template <typename R> struct Variant<R, 4> { static constexpr int BS = 128, MINB = sizeof(R) == 4 ? 4 : 2, SPT = 2; };
-// sites per block (threads x sites per thread) of each variant, for host code
-// that builds tile tables and grids
-constexpr int kVariantBS[NVARIANTS] = {128, 128, 256, 64, 256};
+template <typename R> struct Variant<R, 0> { static constexpr int BS = 128, MINB = sizeof(R) == 4 ? 8 : 4; };
+template <typename R> struct Variant<R, 1> { static constexpr int BS = 128, MINB = sizeof(R) == 4 ? 5 : 3; };
+template <typename R> struct Variant<R, 2> { static constexpr int BS = 256, MINB = sizeof(R) == 4 ? 4 : 2; };
+template <typename R> struct Variant<R, 3> { static constexpr int BS = 64, MINB = sizeof(R) == 4 ? 12 : 6; };
+// threads per block of each variant, for host code that builds tile tables
+constexpr int kVariantBS[NVARIANTS] = {128, 128, 256, 64};
 constexpr int NSUMS = 24;
 
 // ---------------------------------------------------------------------------
@@ -605,32 +601,20 @@ __device__ inline int overrelax_higgs2(const Fields<R>& f, const Geom& g, const 
 }
 
 // overrelax_triplet (overrelax.c:137-236); no portal term in B (the
-// reference's "#ifdef HIGGS" there is never defined).  In two steps: the
-// gather of the values a site needs (links U_d(x), U_d(x-d), neighbour
-// triplets, its own), then the reflection; a thread with two sites gathers
-// both before it updates either.
-template <typename R>
-struct TripletOR {
-  Q<R> U[6];   // U_d(x), then U_d(x-d)
-  V3<R> S[6];  // Sigma(x+d), then Sigma(x-d)
-  V3<R> t;     // Sigma(x)
-};
-template <typename R>
-__device__ inline void gather_or_triplet(const Fields<R>& f, const Geom& g, const int* c, int i, TripletOR<R>& o) {
+// reference's "#ifdef HIGGS" there is never defined)
+template <typename R, int CC>
+__device__ inline int overrelax_triplet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
+                                        SiteRng<R>& rng, int* fallback) {
+  V3<R> s{(R)0, (R)0, (R)0};
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     int xp = shifted(g, c, d, 1), xm = shifted(g, c, d, -1);
-    o.U[d] = ldro4<R>(lk(f, d), i);
-    o.S[d] = ldro3(f, xp);
-    o.U[3 + d] = ldro4<R>(lk(f, d), xm);
-    o.S[3 + d] = ldro3(f, xm);
+    V3<R> r = qrot(ldro4<R>(lk(f, d), i), ldro3(f, xp));
+    s.x -= r.x; s.y -= r.y; s.z -= r.z;
+    r = qrot(qdag(ldro4<R>(lk(f, d), xm)), ldro3(f, xm));
+    s.x -= r.x; s.y -= r.y; s.z -= r.z;
   }
-  o.t = ld3(f, i);
-}
-// the reflection of Sigma(x) = t given the rotated neighbour sum s
-template <typename R, int CC>
-__device__ inline int reflect_triplet(const Fields<R>& f, const CoupT<R>& cp, int i, const V3<R> t, const V3<R> s,
-                                      SiteRng<R>& rng, int* fallback) {
+  V3<R> t = ld3(f, i);
   R F = msqrt(s.x * s.x + s.y * s.y + s.z * s.z);
   // FP32: one reciprocal instead of seven divisions (the FP64 path divides as
   // the reference does)
@@ -654,35 +638,6 @@ __device__ inline int reflect_triplet(const Fields<R>& f, const CoupT<R>& cp, in
     return 1;
   }
   return 0;
-}
-template <typename R, int CC>
-__device__ inline int apply_or_triplet(const Fields<R>& f, const CoupT<R>& cp, int i, const TripletOR<R>& o,
-                                       SiteRng<R>& rng, int* fallback) {
-  V3<R> s{(R)0, (R)0, (R)0};
-#pragma unroll
-  for (int d = 0; d < 3; d++) {
-    V3<R> r = qrot(o.U[d], o.S[d]);
-    s.x -= r.x; s.y -= r.y; s.z -= r.z;
-    r = qrot(qdag(o.U[3 + d]), o.S[3 + d]);
-    s.x -= r.x; s.y -= r.y; s.z -= r.z;
-  }
-  return reflect_triplet<R, CC>(f, cp, i, o.t, s, rng, fallback);
-}
-// one site per thread: the rotations summed as their values arrive (the same
-// arithmetic as gather + apply, fewer values held at once)
-template <typename R, int CC>
-__device__ inline int overrelax_triplet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
-                                        SiteRng<R>& rng, int* fallback) {
-  V3<R> s{(R)0, (R)0, (R)0};
-#pragma unroll
-  for (int d = 0; d < 3; d++) {
-    int xp = shifted(g, c, d, 1), xm = shifted(g, c, d, -1);
-    V3<R> r = qrot(ldro4<R>(lk(f, d), i), ldro3(f, xp));
-    s.x -= r.x; s.y -= r.y; s.z -= r.z;
-    r = qrot(qdag(ldro4<R>(lk(f, d), xm)), ldro3(f, xm));
-    s.x -= r.x; s.y -= r.y; s.z -= r.z;
-  }
-  return reflect_triplet<R, CC>(f, cp, i, ld3(f, i), s, rng, fallback);
 }
 
 // metro_triplet (metropolis.c:113-143)
@@ -795,43 +750,35 @@ __device__ inline const CoupT<float>& coup<float>(const PassArgs& a) { return a.
 
 // MU: the link direction of the pass, a template parameter so that every
 // neighbour offset and field pointer of the staple is fixed at compile time
-template <typename R, int CC, int MU, int BS, int MINB, int SPT>
+template <typename R, int CC, int MU, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_link(Fields<R> f, PassArgs a) {
   const CoupT<R>& cp = coup<R>(a);
+  int t = a.t_lo + (int)blockIdx.x * blockDim.x + threadIdx.x;
   int acc = 0, cap = 0, err = 0;
-#pragma unroll
-  for (int q = 0; q < SPT; q++) {
-    const int t = a.t_lo + ((int)blockIdx.x * SPT + q) * BS + threadIdx.x;
-    if (t < a.t_hi) {
-      int c[3];
-      site_coords(a.g, a.parity, t, c);
-      int i = a.parity * a.g.half + t;
-      SiteRng<R> rng(a.rk, *a.rk.sweep, (uint32_t)i, a.pass);
-      int cq = 0;
-      if (a.alg == ALG_HEATBATH) acc += heatbath<R, CC>(f, a.g, cp, c, i, MU, rng, &cq, &err);
-      else acc += metro_link<R, CC>(f, a.g, cp, c, i, MU, rng);
-      cap += cq;
-    }
+  if (t < a.t_hi) {
+    int c[3];
+    site_coords(a.g, a.parity, t, c);
+    int i = a.parity * a.g.half + t;
+    SiteRng<R> rng(a.rk, *a.rk.sweep, (uint32_t)i, a.pass);
+    if (a.alg == ALG_HEATBATH) acc = heatbath<R, CC>(f, a.g, cp, c, i, MU, rng, &cap, &err);
+    else acc = metro_link<R, CC>(f, a.g, cp, c, i, MU, rng);
   }
   warp_count(a.ctr + 1, acc);
   warp_count(a.ctr + 22, cap);
   if (err) atomicOr(a.err, 1);
 }
 
-template <typename R, int CC, int MU, int BS, int MINB, int SPT>
+template <typename R, int CC, int MU, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_u1(Fields<R> f, PassArgs a) {
   const CoupT<R>& cp = coup<R>(a);
+  int t = a.t_lo + (int)blockIdx.x * blockDim.x + threadIdx.x;
   int acc = 0;
-#pragma unroll
-  for (int q = 0; q < SPT; q++) {
-    const int t = a.t_lo + ((int)blockIdx.x * SPT + q) * BS + threadIdx.x;
-    if (t < a.t_hi) {
-      int c[3];
-      site_coords(a.g, a.parity, t, c);
-      int i = a.parity * a.g.half + t;
-      SiteRng<R> rng(a.rk, *a.rk.sweep, (uint32_t)i, a.pass);
-      acc += metro_u1<R, CC>(f, a.g, cp, c, i, MU, rng);
-    }
+  if (t < a.t_hi) {
+    int c[3];
+    site_coords(a.g, a.parity, t, c);
+    int i = a.parity * a.g.half + t;
+    SiteRng<R> rng(a.rk, *a.rk.sweep, (uint32_t)i, a.pass);
+    acc = metro_u1<R, CC>(f, a.g, cp, c, i, MU, rng);
   }
   warp_count(a.ctr + 3, acc);
 }
@@ -839,65 +786,39 @@ __global__ void __launch_bounds__(BS, MINB) k_u1(Fields<R> f, PassArgs a) {
 // one parity (or a contiguous block of it) of one doublet / the triplet /
 // the singlet; optional multicanonical backup of the old values and block
 // sums of the order parameter over the new ones
-template <typename R, int CC, int FIELD, int BS, int MINB, int SPT>
+template <typename R, int CC, int FIELD, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_scalar(Fields<R> f, PassArgs a) {
   const CoupT<R>& cp = coup<R>(a);
+  int t = a.t_lo + (int)blockIdx.x * blockDim.x + threadIdx.x;
   int acc = 0, fb = 0;
   double opv = 0.0;
-  if (FIELD == 1 && SPT > 1 && cp.alg_t == ALG_OR && !a.alg && !a.backup && !a.partials) {
-    // triplet overrelaxation, several sites per thread: every site's values
-    // first, then the reflections
-    TripletOR<R> o[SPT];
-#pragma unroll
-    for (int q = 0; q < SPT; q++) {
-      const int t = a.t_lo + ((int)blockIdx.x * SPT + q) * BS + threadIdx.x;
-      if (t < a.t_hi) {
-        int c[3];
-        site_coords(a.g, a.parity, t, c);
-        gather_or_triplet(f, a.g, c, a.parity * a.g.half + t, o[q]);
+  bool orr = false;
+  if (t < a.t_hi) {
+    int c[3];
+    site_coords(a.g, a.parity, t, c);
+    int i = a.parity * a.g.half + t;
+    SiteRng<R> rng(a.rk, *a.rk.sweep, (uint32_t)i, a.pass);
+    if (FIELD == 0) {
+      const int h = a.sub;
+      if (a.backup) ((V4<R>*)a.backup)[i] = php(f, h)[i];
+      orr = cp.alg_d == ALG_OR && !a.alg;
+      if (orr) acc = NHIGGS == 2 ? overrelax_higgs2<R, CC>(f, a.g, cp, c, i, h, rng, &fb)
+                                 : overrelax_doublet<R, CC>(f, a.g, cp, c, i, rng, &fb);
+      else acc = metro_doublet<R, CC>(f, a.g, cp, c, i, h, rng);
+    } else if (FIELD == 1) {
+      if (a.backup) {
+        R* b = (R*)a.backup;
+        b[3 * i] = f.trip[0][i]; b[3 * i + 1] = f.trip[1][i]; b[3 * i + 2] = f.trip[2][i];
       }
+      orr = cp.alg_t == ALG_OR && !a.alg;
+      if (orr) acc = overrelax_triplet<R, CC>(f, a.g, cp, c, i, rng, &fb);
+      else acc = metro_triplet<R, CC>(f, a.g, cp, c, i, rng);
+    } else {
+      orr = cp.alg_s == ALG_OR && !a.alg;
+      if (orr) acc = overrelax_singlet<R, CC>(f, a.g, cp, c, i, rng, &fb);
+      else acc = metro_singlet<R, CC>(f, a.g, cp, c, i, rng);
     }
-#pragma unroll
-    for (int q = 0; q < SPT; q++) {
-      const int t = a.t_lo + ((int)blockIdx.x * SPT + q) * BS + threadIdx.x;
-      if (t < a.t_hi) {
-        const int i = a.parity * a.g.half + t;
-        SiteRng<R> rng(a.rk, *a.rk.sweep, (uint32_t)i, a.pass);
-        int fq = 0;
-        acc += apply_or_triplet<R, CC>(f, cp, i, o[q], rng, &fq);
-        fb += fq;
-      }
-    }
-  } else {
-#pragma unroll
-    for (int q = 0; q < SPT; q++) {
-      const int t = a.t_lo + ((int)blockIdx.x * SPT + q) * BS + threadIdx.x;
-      if (t >= a.t_hi) continue;
-      int c[3];
-      site_coords(a.g, a.parity, t, c);
-      int i = a.parity * a.g.half + t;
-      SiteRng<R> rng(a.rk, *a.rk.sweep, (uint32_t)i, a.pass);
-      int fq = 0;
-      if (FIELD == 0) {
-        const int h = a.sub;
-        if (a.backup) ((V4<R>*)a.backup)[i] = php(f, h)[i];
-        if (cp.alg_d == ALG_OR && !a.alg) acc += NHIGGS == 2 ? overrelax_higgs2<R, CC>(f, a.g, cp, c, i, h, rng, &fq)
-                                                             : overrelax_doublet<R, CC>(f, a.g, cp, c, i, rng, &fq);
-        else acc += metro_doublet<R, CC>(f, a.g, cp, c, i, h, rng);
-      } else if (FIELD == 1) {
-        if (a.backup) {
-          R* b = (R*)a.backup;
-          b[3 * i] = f.trip[0][i]; b[3 * i + 1] = f.trip[1][i]; b[3 * i + 2] = f.trip[2][i];
-        }
-        if (cp.alg_t == ALG_OR && !a.alg) acc += overrelax_triplet<R, CC>(f, a.g, cp, c, i, rng, &fq);
-        else acc += metro_triplet<R, CC>(f, a.g, cp, c, i, rng);
-      } else {
-        if (cp.alg_s == ALG_OR && !a.alg) acc += overrelax_singlet<R, CC>(f, a.g, cp, c, i, rng, &fq);
-        else acc += metro_singlet<R, CC>(f, a.g, cp, c, i, rng);
-      }
-      fb += fq;
-      if (a.partials) opv += orderparam_site<R>(f, a.op, i);
-    }
+    if (a.partials) opv = orderparam_site<R>(f, a.op, i);
   }
   // counters: doublet OR/Metropolis (+h), triplet, singlet
   int base_or = FIELD == 0 ? 10 + a.sub : (FIELD == 1 ? 15 : 19);

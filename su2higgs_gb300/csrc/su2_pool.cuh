@@ -51,127 +51,69 @@ __device__ inline const ChainDesc<R>& stage_desc(const PoolArgs& a, int slot) {
   return *(const ChainDesc<R>*)buf;
 }
 
-template <typename R, int CC, int MU, int BS, int MINB, int SPT>
+template <typename R, int CC, int MU, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_pool_link(PoolArgs a) {
   int2 tile = a.tiles[blockIdx.x];
   if (bad_tile(a, tile)) return;
   const ChainDesc<R>& d = stage_desc<R>(a, tile.x);
   const CoupT<R>& cp = d.cp;
+  int t = tile.y + threadIdx.x;
   int acc = 0, cap = 0, err = 0;
-#pragma unroll
-  for (int q = 0; q < SPT; q++) {
-    const int t = tile.y + q * BS + threadIdx.x;
-    if (t < d.g.half) {
-      int c[3];
-      site_coords(d.g, a.parity, t, c);
-      int i = a.parity * d.g.half + t;
-      SiteRng<R> rng(RngKey{d.k0, d.k1, d.chain, d.sweep}, *d.sweep, (uint32_t)i, a.pass);
-      int cq = 0;
-      if (a.alg == ALG_HEATBATH) acc += heatbath<R, CC>(d.f, d.g, cp, c, i, MU, rng, &cq, &err);
-      else acc += metro_link<R, CC>(d.f, d.g, cp, c, i, MU, rng);
-      cap += cq;
-    }
+  if (t < d.g.half) {
+    int c[3];
+    site_coords(d.g, a.parity, t, c);
+    int i = a.parity * d.g.half + t;
+    SiteRng<R> rng(RngKey{d.k0, d.k1, d.chain, d.sweep}, *d.sweep, (uint32_t)i, a.pass);
+    if (a.alg == ALG_HEATBATH) acc = heatbath<R, CC>(d.f, d.g, cp, c, i, MU, rng, &cap, &err);
+    else acc = metro_link<R, CC>(d.f, d.g, cp, c, i, MU, rng);
   }
   warp_count(d.ctr + 1, acc);
   warp_count(d.ctr + 22, cap);
   if (err) atomicOr(a.err, 1);
 }
 
-template <typename R, int CC, int MU, int BS, int MINB, int SPT>
+template <typename R, int CC, int MU, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_pool_u1(PoolArgs a) {
   int2 tile = a.tiles[blockIdx.x];
   if (bad_tile(a, tile)) return;
   const ChainDesc<R>& d = stage_desc<R>(a, tile.x);
+  int t = tile.y + threadIdx.x;
   int acc = 0;
-#pragma unroll
-  for (int q = 0; q < SPT; q++) {
-    const int t = tile.y + q * BS + threadIdx.x;
-    if (t < d.g.half) {
-      int c[3];
-      site_coords(d.g, a.parity, t, c);
-      int i = a.parity * d.g.half + t;
-      SiteRng<R> rng(RngKey{d.k0, d.k1, d.chain, d.sweep}, *d.sweep, (uint32_t)i, a.pass);
-      acc += metro_u1<R, CC>(d.f, d.g, d.cp, c, i, MU, rng);
-    }
+  if (t < d.g.half) {
+    int c[3];
+    site_coords(d.g, a.parity, t, c);
+    int i = a.parity * d.g.half + t;
+    SiteRng<R> rng(RngKey{d.k0, d.k1, d.chain, d.sweep}, *d.sweep, (uint32_t)i, a.pass);
+    acc = metro_u1<R, CC>(d.f, d.g, d.cp, c, i, MU, rng);
   }
   warp_count(d.ctr + 3, acc);
 }
 
-template <typename R, int CC, int FIELD, int BS, int MINB, int SPT>
+template <typename R, int CC, int FIELD, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_pool_scalar(PoolArgs a) {
   int2 tile = a.tiles[blockIdx.x];
   if (bad_tile(a, tile)) return;
   const ChainDesc<R>& d = stage_desc<R>(a, tile.x);
   const CoupT<R>& cp = d.cp;
+  int t = tile.y + threadIdx.x;
   int acc = 0, fb = 0;
-  constexpr int CCx = CC;
-  if constexpr (SPT == 1) {
-    int t = tile.y + threadIdx.x;
-    if (t < d.g.half) {
-      int c[3];
-      site_coords(d.g, a.parity, t, c);
-      int i = a.parity * d.g.half + t;
-      SiteRng<R> rng(RngKey{d.k0, d.k1, d.chain, d.sweep}, *d.sweep, (uint32_t)i, a.pass);
-      if (FIELD == 0) {
-        const bool orr = cp.alg_d == ALG_OR && !a.alg;
-        if (orr) acc = SU2_HAS(CCx, cp.content, C_H2) ? overrelax_higgs2<R, CC>(d.f, d.g, cp, c, i, a.sub, rng, &fb)
-                                                      : overrelax_doublet<R, CC>(d.f, d.g, cp, c, i, rng, &fb);
-        else acc = metro_doublet<R, CC>(d.f, d.g, cp, c, i, a.sub, rng);
-      } else if (FIELD == 1) {
-        if (cp.alg_t == ALG_OR && !a.alg) acc = overrelax_triplet<R, CC>(d.f, d.g, cp, c, i, rng, &fb);
-        else acc = metro_triplet<R, CC>(d.f, d.g, cp, c, i, rng);
-      } else {
-        if (cp.alg_s == ALG_OR && !a.alg) acc = overrelax_singlet<R, CC>(d.f, d.g, cp, c, i, rng, &fb);
-        else acc = metro_singlet<R, CC>(d.f, d.g, cp, c, i, rng);
-      }
-    }
-  } else if (FIELD == 1 && cp.alg_t == ALG_OR && !a.alg) {
-    // triplet overrelaxation, several sites per thread: every site's values
-    // first, then the reflections
-    TripletOR<R> o[SPT];
-#pragma unroll
-    for (int q = 0; q < SPT; q++) {
-      const int t = tile.y + q * BS + threadIdx.x;
-      if (t < d.g.half) {
-        int c[3];
-        site_coords(d.g, a.parity, t, c);
-        gather_or_triplet(d.f, d.g, c, a.parity * d.g.half + t, o[q]);
-      }
-    }
-#pragma unroll
-    for (int q = 0; q < SPT; q++) {
-      const int t = tile.y + q * BS + threadIdx.x;
-      if (t < d.g.half) {
-        const int i = a.parity * d.g.half + t;
-        SiteRng<R> rng(RngKey{d.k0, d.k1, d.chain, d.sweep}, *d.sweep, (uint32_t)i, a.pass);
-        int fq = 0;
-        acc += apply_or_triplet<R, CC>(d.f, cp, i, o[q], rng, &fq);
-        fb += fq;
-      }
-    }
-  } else {
-#pragma unroll
-    for (int q = 0; q < SPT; q++) {
-      const int t = tile.y + q * BS + threadIdx.x;
-      if (t >= d.g.half) continue;
-      int c[3];
-      site_coords(d.g, a.parity, t, c);
-      int i = a.parity * d.g.half + t;
-      SiteRng<R> rng(RngKey{d.k0, d.k1, d.chain, d.sweep}, *d.sweep, (uint32_t)i, a.pass);
-      int fq = 0;
-      if (FIELD == 0) {
-        const bool orr = cp.alg_d == ALG_OR && !a.alg;
-        if (orr) acc += SU2_HAS(CCx, cp.content, C_H2) ? overrelax_higgs2<R, CC>(d.f, d.g, cp, c, i, a.sub, rng, &fq)
-                                                       : overrelax_doublet<R, CC>(d.f, d.g, cp, c, i, rng, &fq);
-        else acc += metro_doublet<R, CC>(d.f, d.g, cp, c, i, a.sub, rng);
-      } else if (FIELD == 1) {
-        if (cp.alg_t == ALG_OR && !a.alg) acc += overrelax_triplet<R, CC>(d.f, d.g, cp, c, i, rng, &fq);
-        else acc += metro_triplet<R, CC>(d.f, d.g, cp, c, i, rng);
-      } else {
-        if (cp.alg_s == ALG_OR && !a.alg) acc += overrelax_singlet<R, CC>(d.f, d.g, cp, c, i, rng, &fq);
-        else acc += metro_singlet<R, CC>(d.f, d.g, cp, c, i, rng);
-      }
-      fb += fq;
+  if (t < d.g.half) {
+    int c[3];
+    site_coords(d.g, a.parity, t, c);
+    int i = a.parity * d.g.half + t;
+    SiteRng<R> rng(RngKey{d.k0, d.k1, d.chain, d.sweep}, *d.sweep, (uint32_t)i, a.pass);
+    constexpr int CCx = CC;
+    if (FIELD == 0) {
+      const bool orr = cp.alg_d == ALG_OR && !a.alg;
+      if (orr) acc = SU2_HAS(CCx, cp.content, C_H2) ? overrelax_higgs2<R, CC>(d.f, d.g, cp, c, i, a.sub, rng, &fb)
+                                                    : overrelax_doublet<R, CC>(d.f, d.g, cp, c, i, rng, &fb);
+      else acc = metro_doublet<R, CC>(d.f, d.g, cp, c, i, a.sub, rng);
+    } else if (FIELD == 1) {
+      if (cp.alg_t == ALG_OR && !a.alg) acc = overrelax_triplet<R, CC>(d.f, d.g, cp, c, i, rng, &fb);
+      else acc = metro_triplet<R, CC>(d.f, d.g, cp, c, i, rng);
+    } else {
+      if (cp.alg_s == ALG_OR && !a.alg) acc = overrelax_singlet<R, CC>(d.f, d.g, cp, c, i, rng, &fb);
+      else acc = metro_singlet<R, CC>(d.f, d.g, cp, c, i, rng);
     }
   }
   int base_or = FIELD == 0 ? 10 + a.sub : (FIELD == 1 ? 15 : 19);
