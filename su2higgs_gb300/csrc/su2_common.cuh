@@ -274,13 +274,18 @@ __device__ inline void st4(V4<R>* p, int i, const Q<R>& q) {
   p[i] = v;
 }
 
+__device__ inline float fmaR(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ inline double fmaR(double a, double b, double c) { return fma(a, b, c); }
+// quaternion product x y (the SU(2) product in the reference's 4-real
+// parametrisation, su2rot su2u1.c:60-71) with explicit fused multiply-adds,
+// which fixes the rounding of every step in the source
 template <typename R>
 __device__ inline Q<R> qmul(const Q<R>& x, const Q<R>& y) {
   Q<R> r;
-  r.a = x.a * y.a - x.b * y.b - x.c * y.c - x.d * y.d;
-  r.b = x.a * y.b + y.a * x.b - (x.c * y.d - x.d * y.c);
-  r.c = x.a * y.c + y.a * x.c - (x.d * y.b - x.b * y.d);
-  r.d = x.a * y.d + y.a * x.d - (x.b * y.c - x.c * y.b);
+  r.a = fmaR(x.a, y.a, -fmaR(x.b, y.b, fmaR(x.c, y.c, x.d * y.d)));
+  r.b = fmaR(x.a, y.b, fmaR(y.a, x.b, -fmaR(x.c, y.d, -(x.d * y.c))));
+  r.c = fmaR(x.a, y.c, fmaR(y.a, x.c, -fmaR(x.d, y.b, -(x.b * y.d))));
+  r.d = fmaR(x.a, y.d, fmaR(y.a, x.d, -fmaR(x.b, y.c, -(x.c * y.b))));
   return r;
 }
 template <typename R>
@@ -319,8 +324,6 @@ struct V3 {
 // and the real part of the result are never formed, and the rounding of every
 // step is fixed by the source, so every kernel that rotates -- whatever it
 // computes around the rotation -- gets the same bits.
-__device__ inline float fmaR(float a, float b, float c) { return fmaf(a, b, c); }
-__device__ inline double fmaR(double a, double b, double c) { return fma(a, b, c); }
 template <typename R>
 __device__ inline V3<R> qrot(const Q<R>& u, const V3<R>& b) {
   const R na = fmaR(u.d, b.z, fmaR(u.c, b.y, u.b * b.x));  // -(real part of u (0, b))
