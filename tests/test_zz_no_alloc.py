@@ -22,6 +22,11 @@ from su2higgs_gb300 import abi
 pytestmark = pytest.mark.gpu
 
 RTOL = 1e-12
+# FP32 fields: the allocation-free kernel is the content-generic instantiation
+# of the per-site measurement, `measure` the content-specialised one; the
+# compiler may fuse their multiply-adds differently, so a site's FP32 value
+# can differ in its last bit (one site in ~2000 moves a sum by ~5e-11)
+RTOL32 = 2e-6
 
 
 @pytest.fixture(scope="module")
@@ -79,7 +84,7 @@ def test_noalloc_measure_matches_measure(env, content, precision):
     torch.cuda.synchronize()
     got = out.cpu().numpy()
     for k in range(2):
-        ok, idx, a, b = measure_close(got[k], want, RTOL)
+        ok, idx, a, b = measure_close(got[k], want, RTOL if precision == 64 else RTOL32)
         assert ok, (k, idx, a, b)
     assert np.array_equal(got[0], got[1])
     del keep
