@@ -302,12 +302,12 @@ __device__ inline Q<R> qscale(const Q<R>& x, R s) {
 }
 template <typename R>
 __device__ inline R qsq(const Q<R>& x) {
-  return fmaR(x.a, x.a, fmaR(x.b, x.b, fmaR(x.c, x.c, x.d * x.d)));
+  return x.a * x.a + x.b * x.b + x.c * x.c + x.d * x.d;
 }
 // scalar part of x*y
 template <typename R>
 __device__ inline R qdot0(const Q<R>& x, const Q<R>& y) {
-  return fmaR(x.a, y.a, -fmaR(x.b, y.b, fmaR(x.c, y.c, x.d * y.d)));
+  return x.a * y.a - x.b * y.b - x.c * y.c - x.d * y.d;
 }
 // e^{-i alpha sigma_3}
 template <typename R>
@@ -336,7 +336,7 @@ __device__ inline V3<R> qrot(const Q<R>& u, const V3<R>& b) {
 }
 template <typename R>
 __device__ inline R dot3(const V3<R>& a, const V3<R>& b) {
-  return fmaR(a.x, b.x, fmaR(a.y, b.y, a.z * b.z));
+  return a.x * b.x + a.y * b.y + a.z * b.z;
 }
 
 // ---------------------------------------------------------------------------
