@@ -400,6 +400,17 @@ void ref_muca_arrays(double* pos, double* Wv, double* slope, double* b, int* hit
   }
 }
 double ref_get_weight(double v) { return get_weight(&W, v); }
+/* the number of checks between weight updates: load_weight fixes it (100, or
+ * 5000 in SLOW mode); a test of the SLOW recursion shortens it */
+void ref_muca_set_update_interval(int n) { W.update_interval = n; }
+/* the SLOW mode's accumulators (update_weight_slow, multicanonical.c:561-666) */
+void ref_muca_slow_arrays(long* gsum, long* nsum, double* hgram) {
+  for (int k = 0; k < W.bins + 2; k++) {
+    gsum[k] = W.mode == SLOW ? W.gsum[k] : 0;
+    nsum[k] = W.mode == SLOW ? W.nsum[k] : 0;
+    hgram[k] = W.mode == SLOW ? W.hgram[k] : 0.0;
+  }
+}
 int ref_whichbin(double v) { return whichbin(&W, v); }
 
 /* ---- gradient flow ---- */

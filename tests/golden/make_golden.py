@@ -140,7 +140,7 @@ def gen_sweep(case, seed=SEED + 1, first_sweep=5):
 
 
 MUCA_CASES = {
-    # name: (content, orderparam, mode, checks_per_sweep, nsweeps)
+    # name: (content, orderparam, mode, checks_per_sweep, nsweeps[, checks between weight updates])
     "su2u1s_phisq_ro": ("su2u1s", "phisq", 0, 1, 3),
     "su2u1s_phisq_fast": ("su2u1s", "phisq", 1, 1, 12),
     "fund_phisq_cps3": ("fund", "phisq", 1, 3, 4),
@@ -149,11 +149,15 @@ MUCA_CASES = {
     "fundadj_p2ms2": ("fundadj", "phi2minusSigma2", 1, 2, 3),
     # two doublets, the order parameter on the second one (PHI2SQ)
     "higgs2_phi2sq_fast": ("higgs2", "phi2sq", 1, 2, 2),
+    # the SLOW recursion (update_weight_slow): 60 checks a sweep, the weight
+    # updated every 40 checks instead of the reference's 5000
+    "fund_phisq_slow": ("fund", "phisq", 2, 5, 3, 40),
 }
 
 
 def gen_muca(name):
-    content, op, mode, cps, nsweeps = MUCA_CASES[name]
+    content, op, mode, cps, nsweeps = MUCA_CASES[name][:5]
+    interval = MUCA_CASES[name][5] if len(MUCA_CASES[name]) > 5 else None
     p = abi.make_params(content, L=LSMALL)
     f = hot_fields(p, seed=SEED + 7, phi_mean=0.5)
     # a weight around the starting order parameter, steep enough to reject often
@@ -182,6 +186,8 @@ def gen_muca(name):
     r = Ref(p, workdir=wd, muca=muca)
     r.put(f)
     r.muca_init()
+    if interval:
+        r.muca_set_update_interval(interval)
     st0 = r.muca_state()
     out = dict(fields_dict(f, "in_"), **param_dict(p))
     for k, v in st0.items():

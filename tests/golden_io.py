@@ -48,6 +48,9 @@ def weight_of(d, prefix):
                   checks_per_sweep=int(d[prefix + "checks_per_sweep"]))
     for k in ("pos", "W", "slope", "b", "hits"):
         getattr(w, k)[:] = d[prefix + k]
+    for k in ("gsum", "nsum", "hgram"):  # the SLOW mode's accumulators
+        if prefix + k in d:
+            getattr(w, k)[:] = d[prefix + k]
     s = w.struct
     for k in ("min", "max", "wrk_min", "wrk_max", "delta"):
         setattr(s, k, float(d[prefix + k]))

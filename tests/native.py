@@ -497,10 +497,15 @@ class Ref:
         self.lib.ref_muca_arrays(_P(pos), _P(W), _P(slope), _P(b), _P(hits))
         pv = np.zeros(2)
         self.lib.ref_muca_values(_P(pv))
+        gsum, nsum, hgram = np.zeros(n, np.int64), np.zeros(n, np.int64), np.zeros(n)
+        self.lib.ref_muca_slow_arrays(_P(gsum), _P(nsum), _P(hgram))
         return dict(bins=bins, min=sc[1], max=sc[2], wrk_min=sc[3], wrk_max=sc[4], delta=sc[5],
                     last_max=int(sc[6]), muca_count=int(sc[7]), update_interval=int(sc[8]), mode=int(sc[9]),
                     checks_per_sweep=int(sc[10]), orderparam=int(sc[11]), pos=pos, W=W, slope=slope, b=b,
-                    hits=hits, param_value=pv)
+                    hits=hits, param_value=pv, gsum=gsum, nsum=nsum, hgram=hgram)
+
+    def muca_set_update_interval(self, n):
+        self.lib.ref_muca_set_update_interval(n)
 
     def grad_flow(self, t_max, dt, flow_id=1, maxrows=2048):
         per = 64

@@ -116,6 +116,9 @@ def test_multicanonical_matches_reference(gpu, name):
     assert w.struct.muca_count == w1.struct.muca_count
     assert abs(w.struct.delta - w1.struct.delta) < 1e-15
     assert np.allclose(list(w.struct.param_value), list(w1.struct.param_value), rtol=1e-9, atol=0)
+    if w.struct.mode == abi.MUCA_SLOW:  # update_weight_slow's accumulators
+        assert np.array_equal(w.gsum, w1.gsum) and np.array_equal(w.nsum, w1.nsum)
+        assert np.allclose(w.hgram, w1.hgram, rtol=1e-9, atol=0)
 
 
 @pytest.mark.parametrize("name", names("flow_"))

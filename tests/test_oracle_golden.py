@@ -117,6 +117,9 @@ def test_muca(name):
     assert w.struct.muca_count == w1.struct.muca_count
     assert abs(w.struct.delta - w1.struct.delta) < 1e-15
     assert rel_err(list(w.struct.param_value), list(w1.struct.param_value)) < 1e-9
+    if w.struct.mode == abi.MUCA_SLOW:  # update_weight_slow's accumulators
+        assert np.array_equal(w.gsum, w1.gsum) and np.array_equal(w.nsum, w1.nsum)
+        assert rel_err(w.hgram, w1.hgram, 1e-9) < 1e-9
 
 
 @pytest.mark.parametrize("name", names("flow_"))
