@@ -156,9 +156,11 @@ def test_observables_gpu64_gpu32_oracle(gpu):
             assert pv > 1e-3, (name, tag, pv)
 
 
-def test_multicanonical_orderparam_distribution(gpu):
+@pytest.mark.parametrize("precision", [64, 32])
+def test_multicanonical_orderparam_distribution(gpu, precision):
     """READONLY multicanonical run (global accept/reject after each doublet
-    half-sweep): the order-parameter distribution of the GPU and the oracle."""
+    half-sweep): the order-parameter distribution of the GPU (FP64 fields, and
+    FP32 fields with the FP64 weight and decisions) and of the oracle."""
     p = abi.make_params("fund", L=(6, 6, 6))
     f = hot_fields(p, seed=8, phi_mean=1.0)
     # warm up to equilibrium with the oracle, then centre a tilted weight there
@@ -185,7 +187,7 @@ def test_multicanonical_orderparam_distribution(gpu):
     s.param_value[0] = ph[:half].sum() / p.sites()
     s.param_value[1] = ph[half:].sum() / p.sites()
     nmeas = 3000
-    lat = gpu.Lattice(p, seed=55)
+    lat = gpu.Lattice(abi.make_params("fund", L=(6, 6, 6), precision=precision), seed=55)
     lat.upload(link=f0.link, d0=f0.d0)
     lat.muca_set(s)
     o = Oracle(p)
