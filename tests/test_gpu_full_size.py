@@ -1,0 +1,209 @@
+"""Checks at the full sizes of the named workloads: SU(2) + fundamental Higgs
+at 128^3 and 64^3, the 96^3 multicanonical SU(2) x U(1) + singlet lattice and
+the 384-chain batched adjoint ensemble.  Element-wise comparison with the
+oracle over many sweeps would take minutes on the CPU at these sizes, so the
+oracle is used for one sweep (or two flow steps) and the rest is checked
+through properties that do not depend on the size:
+
+* one FP64 sweep of the whole 128^3 lattice against the oracle: fields within
+  1e-11 absolute (the one-sweep tolerance of the small-lattice parity tests),
+  accept/reject counters exact, and the measurement of the result within
+  1e-12 relative;
+* FP32 at 128^3: a graph replay equals stepwise launches bit for bit, two
+  contexts with one seed give the same fields, a different seed different
+  ones, the links stay unit quaternions (1e-6) through the reunitarisation
+  every 10 sweeps, and the FP32 measurement of the FP32 fields is within
+  2e-5 relative of the FP64 measurement of the same fields;
+* the 96^3 multicanonical lattice: one FP64 sweep with its global
+  accept/reject against the oracle (fields 1e-11, counters exact), and in
+  FP32 the order parameter the library reports equals the phi^2 volume
+  average of the fields it returns (1e-6 relative);
+* gradient flow of the 96^3 lattice: two FP64 steps against the oracle's rows
+  (1e-11 relative, as the flow parity tests);
+* the 384-chain ensemble: after three sweeps of the whole pool, sampled chains
+  (every side) are bit-identical to the same chains run alone.
+"""
+import numpy as np
+import pytest
+
+from golden_io import measure_close
+from native import Fields, Oracle
+from su2higgs_gb300 import abi, workloads
+
+pytestmark = pytest.mark.gpu
+
+ATOL1 = 1e-11
+RTOL = 1e-12
+RTOL_FLOW = 1e-11
+RTOL_MEAS32 = 2e-5
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    from su2higgs_gb300 import gpu as g
+    g.lib()
+    return g
+
+
+def max_diff(got, want):
+    return {n: float(np.max(np.abs(got[n] - w))) for n, w in want.items() if w is not None}
+
+
+def phisq_average(d0):
+    return 0.5 * float(np.sum(d0.astype(np.float64) ** 2)) / d0.shape[0]
+
+
+def test_fund128_fp64_sweep_matches_oracle(gpu):
+    p = abi.make_params("fund", L=(128, 128, 128))
+    f = workloads.hot_fields(p, seed=128)
+    lat = gpu.Lattice(p, seed=5)
+    lat.upload(**f)
+    lat.update_lattice(3)
+    o = Oracle(p)
+    o.put(Fields(p, **f))
+    o.set_rng(5, 3)
+    o.update()
+    want = o.get()
+    got = lat.download()
+    for n, v in max_diff(got, {n: getattr(want, n) for n in f}).items():
+        assert v < ATOL1, (n, v)
+    assert np.array_equal(lat.counters()[:22], o.counters()[:22])
+    ok, k, a, b = measure_close(lat.measure(), o.measure(), RTOL)
+    assert ok, (k, a, b)
+
+
+def test_fund128_fp32_properties(gpu):
+    p = abi.make_params("fund", L=(128, 128, 128), precision=32)
+    assert p.reunitarize_interval == 10
+    f = workloads.hot_fields(p, seed=1280)
+    a = gpu.Lattice(p, seed=17)
+    a.upload(**f)
+    a.run_sweeps(0, 21, graph=True)
+    b = gpu.Lattice(p, seed=17)
+    b.upload(**f)
+    for s in range(21):
+        b.update_lattice(s)
+    fa, fb = a.download(), b.download()
+    for n in f:
+        assert np.array_equal(fa[n], fb[n]), n
+    assert np.array_equal(a.counters(), b.counters())
+    del b
+
+    n = np.linalg.norm(fa["link"].astype(np.float64), axis=2)
+    assert np.max(np.abs(n - 1.0)) < 1e-6
+
+    c = gpu.Lattice(p, seed=18)
+    c.upload(**f)
+    c.run_sweeps(0, 1, graph=True)
+    a1 = gpu.Lattice(p, seed=17)
+    a1.upload(**f)
+    a1.run_sweeps(0, 1, graph=True)
+    assert not np.array_equal(c.download()["d0"], a1.download()["d0"])
+    del c, a1
+
+    p64 = abi.make_params("fund", L=(128, 128, 128))
+    l64 = gpu.Lattice(p64)
+    l64.upload(**{k: v.astype(np.float64) for k, v in fa.items() if v is not None})
+    m32, m64 = a.measure(), l64.measure()
+    ok, k, x, y = measure_close(m32, m64, RTOL_MEAS32)
+    assert ok, (k, x, y)
+
+
+def test_fund64_fp32_graph_equals_stepwise(gpu):
+    p = abi.make_params("fund", L=(64, 64, 64), precision=32)
+    f = workloads.hot_fields(p, seed=640)
+    a, b = gpu.Lattice(p, seed=2), gpu.Lattice(p, seed=2)
+    a.upload(**f)
+    b.upload(**f)
+    a.run_sweeps(100, 12, graph=True)
+    for s in range(100, 112):
+        b.update_lattice(s)
+    fa, fb = a.download(), b.download()
+    for n in f:
+        assert np.array_equal(fa[n], fb[n]), n
+    assert np.array_equal(a.counters(), b.counters())
+
+
+def test_muca96_fp64_sweep_matches_oracle(gpu):
+    p = workloads.muca_params(64)
+    f = workloads.hot_fields(p, seed=96, phi_sigma=0.5, sing_sigma=0.3)
+    w = workloads.muca_weight(96)
+    lat = gpu.Lattice(p, seed=9)
+    lat.upload(**f)
+    lat.muca_set(w.struct)
+    lat.update_lattice(0)
+    w_o = workloads.muca_weight(96)
+    o = Oracle(p)
+    o.put(Fields(p, **f))
+    o.muca_set(w_o)
+    o.set_rng(9, 0)
+    o.update()
+    want = o.get()
+    for n, v in max_diff(lat.download(), {n: getattr(want, n) for n in f}).items():
+        assert v < ATOL1, (n, v)
+    assert np.array_equal(lat.counters()[:22], o.counters()[:22])
+    ok, k, a, b = measure_close(lat.measure(), o.measure(), RTOL)
+    assert ok, (k, a, b)
+
+
+def test_muca96_fp32_orderparam_is_the_field_average(gpu):
+    p = workloads.muca_params(32)
+    f = workloads.hot_fields(p, seed=960, phi_sigma=0.5, sing_sigma=0.3)
+    w = workloads.muca_weight(960)
+    lat = gpu.Lattice(p, seed=4)
+    lat.upload(**f)
+    lat.muca_set(w.struct)
+    lat.run_sweeps(0, 3, graph=True)
+    got = lat.download()
+    want = phisq_average(got["d0"])
+    assert abs(lat.calc_orderparam(1) - want) <= 1e-6 * want
+    ctr = lat.counters()
+    assert ctr[:22].sum() > 0
+
+
+def test_muca96_flow_matches_oracle(gpu):
+    p = workloads.muca_params(64)
+    f = workloads.hot_fields(p, seed=961, phi_sigma=0.5, sing_sigma=0.3)
+    lat = gpu.Lattice(p)
+    lat.upload(**f)
+    rows = lat.grad_flow(0.02, 0.01, 1)
+    o = Oracle(p)
+    o.put(Fields(p, **f))
+    want = o.grad_flow(0.02, 0.01, 1)
+    assert rows.shape == want.shape and rows.shape[0] >= 2
+    for rg, ro in zip(rows, want):
+        assert rg[0] == ro[0]
+        ok, k, a, b = measure_close(rg[1:], ro[1:], RTOL_FLOW)
+        assert ok, (rg[0], k, a, b)
+
+
+def test_batched384_sampled_chains_equal_alone(gpu):
+    specs = workloads.batched_ensemble(384)
+    recipe = specs[0][0]
+    need = sum(gpu.Pool.chain_bytes(p) for p, _, _ in specs)
+    pool = gpu.Pool(recipe, arena_bytes=need + (64 << 20), max_chains=384)
+    slots, inputs = [], {}
+    sample = {}
+    for k, (p, seed, chain) in enumerate(specs):
+        s = pool.add(p, seed=seed, chain=chain)
+        f = workloads.hot_fields(p, seed)
+        pool.upload(s, **f)
+        slots.append(s)
+        L = p.L[0]
+        if L not in sample:
+            sample[L] = k
+            inputs[k] = f
+    assert len(sample) == len(workloads.ENSEMBLE_SIDES)
+    pool.run(3, graph=True)
+    for L, k in sorted(sample.items()):
+        p, seed, chain = specs[k]
+        alone = gpu.Pool(recipe, arena_bytes=gpu.Pool.chain_bytes(p) + (16 << 20), max_chains=1)
+        s = alone.add(p, seed=seed, chain=chain)
+        alone.upload(s, **inputs[k])
+        alone.run(3, graph=True)
+        got, want = pool.download(slots[k]), alone.download(s)
+        for n in want:
+            if want[n] is not None:
+                assert np.array_equal(got[n], want[n]), (L, n)
+        assert np.array_equal(pool.counters(slots[k]), alone.counters(s)), L
+        alone.close()
