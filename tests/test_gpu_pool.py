@@ -181,7 +181,7 @@ def test_pool_autotune_does_not_advance(gpu):
     before = {s: pool.download(s) for s in slots}
     ctr = {s: pool.counters(s) for s in slots}
     choices, ms = pool.autotune()
-    assert all(0 <= c < 5 for c in choices)
+    assert all(0 <= c < 4 for c in choices)
     for s in slots:
         fields_equal(pool.download(s), before[s])
         assert np.array_equal(pool.counters(s), ctr[s])
