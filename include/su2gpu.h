@@ -299,7 +299,7 @@ int su2gpu_profile_sweep(su2gpu_ctx* ctx, uint32_t sweep, int32_t max_passes, in
  * chain is not advanced) and keeps the fastest.  choices[5] / best_ms[5]
  * (may be NULL) receive the picks and their mean launch times. */
 int su2gpu_autotune(su2gpu_ctx* ctx, int32_t* choices, float* best_ms);
-/* Set the launch-shape variants explicitly (choices[5], each in [0, 5)). */
+/* Set the launch-shape variants explicitly (choices[5], each in [0, 4)). */
 int su2gpu_set_variants(su2gpu_ctx* ctx, const int32_t* choices);
 /* A second context with the same parameters and a device copy of ctx's
  * fields (alloc_fields + copy_fields of the heatbath trajectories,

@@ -51,7 +51,6 @@ static unsigned l_link(int v, const void* f, const PassArgs& a, cudaStream_t st)
     case 1: return l_link_v<1>(f, a, st);
     case 2: return l_link_v<2>(f, a, st);
     case 3: return l_link_v<3>(f, a, st);
-    case 4: return l_link_v<4>(f, a, st);
     default: return l_link_v<0>(f, a, st);
   }
 }
@@ -60,7 +59,6 @@ static unsigned l_u1(int v, const void* f, const PassArgs& a, cudaStream_t st) {
     case 1: return l_u1_v<1>(f, a, st);
     case 2: return l_u1_v<2>(f, a, st);
     case 3: return l_u1_v<3>(f, a, st);
-    case 4: return l_u1_v<4>(f, a, st);
     default: return l_u1_v<0>(f, a, st);
   }
 }
@@ -69,7 +67,6 @@ static unsigned l_scalar(int v, int field, const void* f, const PassArgs& a, cud
     case 1: return l_scalar_v<1>(field, f, a, st);
     case 2: return l_scalar_v<2>(field, f, a, st);
     case 3: return l_scalar_v<3>(field, f, a, st);
-    case 4: return l_scalar_v<4>(field, f, a, st);
     default: return l_scalar_v<0>(field, f, a, st);
   }
 }
@@ -111,7 +108,6 @@ static void lp_link(int v, const PoolArgs& a, unsigned nb, cudaStream_t st) {
     case 1: lp_link_v<1>(a, nb, st); break;
     case 2: lp_link_v<2>(a, nb, st); break;
     case 3: lp_link_v<3>(a, nb, st); break;
-    case 4: lp_link_v<4>(a, nb, st); break;
     default: lp_link_v<0>(a, nb, st);
   }
 }
@@ -120,7 +116,6 @@ static void lp_u1(int v, const PoolArgs& a, unsigned nb, cudaStream_t st) {
     case 1: lp_u1_v<1>(a, nb, st); break;
     case 2: lp_u1_v<2>(a, nb, st); break;
     case 3: lp_u1_v<3>(a, nb, st); break;
-    case 4: lp_u1_v<4>(a, nb, st); break;
     default: lp_u1_v<0>(a, nb, st);
   }
 }
@@ -129,7 +124,6 @@ static void lp_scalar(int v, int field, const PoolArgs& a, unsigned nb, cudaStre
     case 1: lp_scalar_v<1>(field, a, nb, st); break;
     case 2: lp_scalar_v<2>(field, a, nb, st); break;
     case 3: lp_scalar_v<3>(field, a, nb, st); break;
-    case 4: lp_scalar_v<4>(field, a, nb, st); break;
     default: lp_scalar_v<0>(field, a, nb, st);
   }
 }

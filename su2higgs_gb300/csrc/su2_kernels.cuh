@@ -28,18 +28,15 @@ struct MinBlocks {
 // launch shapes of the update kernels the autotuner chooses from:
 // (threads per block, resident blocks per SM asked of the compiler, which
 // sets the register budget: 65536 / (threads * blocks))
-constexpr int NVARIANTS = 5;
+constexpr int NVARIANTS = 4;
 template <typename R, int V>
 struct Variant;
 template <typename R> struct Variant<R, 0> { static constexpr int BS = 128, MINB = sizeof(R) == 4 ? 8 : 4; };
 template <typename R> struct Variant<R, 1> { static constexpr int BS = 128, MINB = sizeof(R) == 4 ? 5 : 3; };
 template <typename R> struct Variant<R, 2> { static constexpr int BS = 256, MINB = sizeof(R) == 4 ? 4 : 2; };
 template <typename R> struct Variant<R, 3> { static constexpr int BS = 64, MINB = sizeof(R) == 4 ? 12 : 6; };
-// more resident warps for kernels that fit a smaller budget (FP32: 48
-// registers, 40 warps per SM)
-template <typename R> struct Variant<R, 4> { static constexpr int BS = 128, MINB = sizeof(R) == 4 ? 10 : 5; };
 // threads per block of each variant, for host code that builds tile tables
-constexpr int kVariantBS[NVARIANTS] = {128, 128, 256, 64, 128};
+constexpr int kVariantBS[NVARIANTS] = {128, 128, 256, 64};
 constexpr int NSUMS = 24;
 
 // ---------------------------------------------------------------------------

@@ -108,7 +108,7 @@ struct su2gpu_pool {
   Buf ring;
   cudaStream_t copy_st = nullptr;
   std::vector<cudaEvent_t> ring_ev;  // two per chain of a batch: copied, converted
-  int ntiles[NVARIANTS] = {}, nmtiles = 0;
+  int ntiles[NVARIANTS] = {0, 0, 0, 0}, nmtiles = 0;
   std::vector<int> active;  // active slots in slot order
   bool dirty = true;
   cudaGraphExec_t gexec = nullptr;
@@ -1061,8 +1061,8 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
   }
   // half-sweeps of each kind in one sweep of a chain
   {
-    const int2* tl[NVARIANTS] = {};
-    int zero[NVARIANTS] = {};
+    const int2* tl[NVARIANTS] = {nullptr, nullptr, nullptr, nullptr};
+    int zero[NVARIANTS] = {0, 0, 0, 0};
     cudaStream_t keep = P->st;
     // counting only: no launch happens with zero tiles
     rc = enqueue_pool_sweep(P, P->descs.p, tl, zero, tot);

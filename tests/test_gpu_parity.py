@@ -216,7 +216,7 @@ def test_launch_variants_bit_identical(gpu, content, precision):
     p = abi.make_params(content, L=(12, 8, 10), precision=precision)
     f = hot_fields(p, seed=21, phi_mean=0.5)
     ref = None
-    for v in range(5):
+    for v in range(4):
         lat = gpu.Lattice(p, seed=8)
         upload(lat, f)
         lat.set_variants([v] * 5)
