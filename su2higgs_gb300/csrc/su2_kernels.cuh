@@ -244,29 +244,11 @@ template <typename R>
 __device__ inline R hop_triplet_fwd(const Fields<R>& f, const Geom& g, const int* c, int i, int mu) {
   return hop_triplet_fwd_u(f, g, c, i, mu, ld4<R>(lk(f, mu), i));
 }
-// hopping_triplet_backward (su2u1.c:623-637)
-template <typename R>
-__device__ inline R hop_triplet_bwd(const Fields<R>& f, const Geom& g, const int* c, int i, int mu) {
-  int pm = shifted(g, c, mu, -1);
-  V3<R> r = qrot(ld4<R>(lk(f, mu), pm), ld3(f, i));
-  return -dot3(ld3(f, pm), r);
-}
 template <typename R>
 __device__ inline R covariant_triplet(const Fields<R>& f, const Geom& g, const int* c, int i) {
   R tot = 0, mod = tripletsq(ld3(f, i));
 #pragma unroll
   for (int d = 0; d < 3; d++) tot += (R)2 * mod + hop_triplet_fwd(f, g, c, i, d);
-  return tot;
-}
-// localact_triplet (su2u1.c:657-679)
-template <typename R, int CC>
-__device__ inline R localact_triplet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i) {
-  R tot = covariant_triplet(f, g, c, i);
-#pragma unroll
-  for (int d = 0; d < 3; d++) tot += hop_triplet_bwd(f, g, c, i, d);
-  R mod = tripletsq(ld3(f, i));
-  tot += (R)cp.msqT * mod + (R)cp.b4 * mod * mod;
-  if (NHIGGS > 0) tot += (R)cp.a2 * doubletsq(ld4<R>(php(f, 0), i)) * mod;
   return tot;
 }
 
@@ -602,9 +584,12 @@ __device__ inline int overrelax_higgs2(const Fields<R>& f, const Geom& g, const 
 
 // overrelax_triplet (overrelax.c:137-236); no portal term in B (the
 // reference's "#ifdef HIGGS" there is never defined)
-template <typename R, int CC>
-__device__ inline int overrelax_triplet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
-                                        SiteRng<R>& rng, int* fallback) {
+// The triplet's staple s = -sum_d [R(U_d(x)) t(x+d) + R(U_d(x-d))^T t(x-d)]:
+// with it the local action (localact_triplet, su2u1.c:657-679) is
+// t.s + B t^2 + C t^4 (+ the portal a2 phi^2 t^2 / 2), B = 3 + msqT / 2,
+// C = b4 / 4, the form overrelax.c:137-236 works with.
+template <typename R>
+__device__ inline V3<R> staple_triplet(const Fields<R>& f, const Geom& g, const int* c, int i) {
   V3<R> s{(R)0, (R)0, (R)0};
 #pragma unroll
   for (int d = 0; d < 3; d++) {
@@ -614,6 +599,13 @@ __device__ inline int overrelax_triplet(const Fields<R>& f, const Geom& g, const
     r = qrot(qdag(ldro4<R>(lk(f, d), xm)), ldro3(f, xm));
     s.x -= r.x; s.y -= r.y; s.z -= r.z;
   }
+  return s;
+}
+
+template <typename R, int CC>
+__device__ inline int overrelax_triplet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
+                                        SiteRng<R>& rng, int* fallback) {
+  V3<R> s = staple_triplet(f, g, c, i);
   V3<R> t = ld3(f, i);
   R F = msqrt(s.x * s.x + s.y * s.y + s.z * s.z);
   // FP32: one reciprocal instead of seven divisions (the FP64 path divides as
@@ -640,20 +632,30 @@ __device__ inline int overrelax_triplet(const Fields<R>& f, const Geom& g, const
   return 0;
 }
 
-// metro_triplet (metropolis.c:113-143)
+// metro_triplet (metropolis.c:113-143).  The reference evaluates
+// localact_triplet before and after the change; in their difference every
+// term but t.s and the powers of t^2 cancels, so it is formed directly from
+// the staple: dS = (t'-t).s + (t'^2-t^2) (B + C (t'^2+t^2)) (+ portal).  One
+// gather of the neighbours instead of two, the field written only on accept.
 template <typename R, int CC>
 __device__ inline int metro_triplet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
                                     SiteRng<R>& rng) {
+  V3<R> s = staple_triplet(f, g, c, i);
   V3<R> old = ld3(f, i);
-  R a0 = localact_triplet<R, CC>(f, g, cp, c, i);
   V3<R> nw = old;
   nw.x += (R)1 * (rng.uni() - (R)0.5);
   nw.y += (R)1 * (rng.uni() - (R)0.5);
   nw.z += (R)1 * (rng.uni() - (R)0.5);
-  st3(f, i, nw);
-  R a1 = localact_triplet<R, CC>(f, g, cp, c, i);
-  if (metro_accept(a1 - a0, rng)) return 1;
-  st3(f, i, old);
+  const R dx = nw.x - old.x, dy = nw.y - old.y, dz = nw.z - old.z;
+  const R dsq = dx * (nw.x + old.x) + dy * (nw.y + old.y) + dz * (nw.z + old.z);
+  const R ssq = (nw.x * nw.x + nw.y * nw.y + nw.z * nw.z) + (old.x * old.x + old.y * old.y + old.z * old.z);
+  R B = (R)0.5 * (R)cp.msqT + (R)3;
+  if (NHIGGS > 0) B += (R)0.5 * (R)cp.a2 * doubletsq(ld4<R>(php(f, 0), i));
+  const R dS = dx * s.x + dy * s.y + dz * s.z + dsq * (B + (R)0.25 * (R)cp.b4 * ssq);
+  if (metro_accept(dS, rng)) {
+    st3(f, i, nw);
+    return 1;
+  }
   return 0;
 }
 
