@@ -13,32 +13,15 @@ namespace su2 {
 using R = SU2_R;
 constexpr int CCI = SU2_CC;
 
-// update kernels: launched with programmatic stream serialisation (the
-// kernels call pdl_enter first)
-template <typename... P, typename... A>
-static void launch_upd(void (*k)(P...), unsigned nb, int bs, cudaStream_t st, A... args) {
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(nb);
-  cfg.blockDim = dim3(bs);
-  cfg.dynamicSmemBytes = 0;
-  cfg.stream = st;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, k, args...);
-}
-
 template <int V>
 static unsigned l_link_v(const void* f, const PassArgs& a, cudaStream_t st) {
   constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB;
   unsigned nb = (unsigned)((a.t_hi - a.t_lo + BS - 1) / BS);
   if (!nb) return 0;
   const Fields<R>& F = *(const Fields<R>*)f;
-  if (a.sub == 0) launch_upd(k_link<R, CCI, 0, BS, MB>, nb, BS, st, F, a);
-  else if (a.sub == 1) launch_upd(k_link<R, CCI, 1, BS, MB>, nb, BS, st, F, a);
-  else launch_upd(k_link<R, CCI, 2, BS, MB>, nb, BS, st, F, a);
+  if (a.sub == 0) k_link<R, CCI, 0, BS, MB><<<nb, BS, 0, st>>>(F, a);
+  else if (a.sub == 1) k_link<R, CCI, 1, BS, MB><<<nb, BS, 0, st>>>(F, a);
+  else k_link<R, CCI, 2, BS, MB><<<nb, BS, 0, st>>>(F, a);
   return nb;
 }
 template <int V>
@@ -47,9 +30,9 @@ static unsigned l_u1_v(const void* f, const PassArgs& a, cudaStream_t st) {
   unsigned nb = (unsigned)((a.t_hi - a.t_lo + BS - 1) / BS);
   if (!nb) return 0;
   const Fields<R>& F = *(const Fields<R>*)f;
-  if (a.sub == 0) launch_upd(k_u1<R, CCI, 0, BS, MB>, nb, BS, st, F, a);
-  else if (a.sub == 1) launch_upd(k_u1<R, CCI, 1, BS, MB>, nb, BS, st, F, a);
-  else launch_upd(k_u1<R, CCI, 2, BS, MB>, nb, BS, st, F, a);
+  if (a.sub == 0) k_u1<R, CCI, 0, BS, MB><<<nb, BS, 0, st>>>(F, a);
+  else if (a.sub == 1) k_u1<R, CCI, 1, BS, MB><<<nb, BS, 0, st>>>(F, a);
+  else k_u1<R, CCI, 2, BS, MB><<<nb, BS, 0, st>>>(F, a);
   return nb;
 }
 template <int V>
@@ -58,9 +41,9 @@ static unsigned l_scalar_v(int field, const void* f, const PassArgs& a, cudaStre
   unsigned nb = (unsigned)((a.t_hi - a.t_lo + BS - 1) / BS);
   if (!nb) return 0;
   const Fields<R>& F = *(const Fields<R>*)f;
-  if (field == 0) launch_upd(k_scalar<R, CCI, 0, BS, MB>, nb, BS, st, F, a);
-  else if (field == 1) launch_upd(k_scalar<R, CCI, 1, BS, MB>, nb, BS, st, F, a);
-  else launch_upd(k_scalar<R, CCI, 2, BS, MB>, nb, BS, st, F, a);
+  if (field == 0) k_scalar<R, CCI, 0, BS, MB><<<nb, BS, 0, st>>>(F, a);
+  else if (field == 1) k_scalar<R, CCI, 1, BS, MB><<<nb, BS, 0, st>>>(F, a);
+  else k_scalar<R, CCI, 2, BS, MB><<<nb, BS, 0, st>>>(F, a);
   return nb;
 }
 static unsigned l_link(int v, const void* f, const PassArgs& a, cudaStream_t st) {
@@ -100,25 +83,25 @@ template <int V>
 static void lp_link_v(const PoolArgs& a, unsigned nb, cudaStream_t st) {
   constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB;
   if (!nb) return;
-  if (a.sub == 0) launch_upd(k_pool_link<R, CCI, 0, BS, MB>, nb, BS, st, a);
-  else if (a.sub == 1) launch_upd(k_pool_link<R, CCI, 1, BS, MB>, nb, BS, st, a);
-  else launch_upd(k_pool_link<R, CCI, 2, BS, MB>, nb, BS, st, a);
+  if (a.sub == 0) k_pool_link<R, CCI, 0, BS, MB><<<nb, BS, 0, st>>>(a);
+  else if (a.sub == 1) k_pool_link<R, CCI, 1, BS, MB><<<nb, BS, 0, st>>>(a);
+  else k_pool_link<R, CCI, 2, BS, MB><<<nb, BS, 0, st>>>(a);
 }
 template <int V>
 static void lp_u1_v(const PoolArgs& a, unsigned nb, cudaStream_t st) {
   constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB;
   if (!nb) return;
-  if (a.sub == 0) launch_upd(k_pool_u1<R, CCI, 0, BS, MB>, nb, BS, st, a);
-  else if (a.sub == 1) launch_upd(k_pool_u1<R, CCI, 1, BS, MB>, nb, BS, st, a);
-  else launch_upd(k_pool_u1<R, CCI, 2, BS, MB>, nb, BS, st, a);
+  if (a.sub == 0) k_pool_u1<R, CCI, 0, BS, MB><<<nb, BS, 0, st>>>(a);
+  else if (a.sub == 1) k_pool_u1<R, CCI, 1, BS, MB><<<nb, BS, 0, st>>>(a);
+  else k_pool_u1<R, CCI, 2, BS, MB><<<nb, BS, 0, st>>>(a);
 }
 template <int V>
 static void lp_scalar_v(int field, const PoolArgs& a, unsigned nb, cudaStream_t st) {
   constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB;
   if (!nb) return;
-  if (field == 0) launch_upd(k_pool_scalar<R, CCI, 0, BS, MB>, nb, BS, st, a);
-  else if (field == 1) launch_upd(k_pool_scalar<R, CCI, 1, BS, MB>, nb, BS, st, a);
-  else launch_upd(k_pool_scalar<R, CCI, 2, BS, MB>, nb, BS, st, a);
+  if (field == 0) k_pool_scalar<R, CCI, 0, BS, MB><<<nb, BS, 0, st>>>(a);
+  else if (field == 1) k_pool_scalar<R, CCI, 1, BS, MB><<<nb, BS, 0, st>>>(a);
+  else k_pool_scalar<R, CCI, 2, BS, MB><<<nb, BS, 0, st>>>(a);
 }
 static void lp_link(int v, const PoolArgs& a, unsigned nb, cudaStream_t st) {
   switch (v) {

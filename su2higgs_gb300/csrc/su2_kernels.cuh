@@ -42,18 +42,6 @@ constexpr int NSUMS = 24;
 // ---------------------------------------------------------------------------
 // reductions
 // ---------------------------------------------------------------------------
-// Programmatic dependent launch.  The update kernels are launched with
-// programmatic stream serialisation: each lets the next kernel of its stream
-// launch as soon as all of its own blocks are running, and waits for the
-// kernel before it to complete (its writes visible) before touching any
-// field.  The next pass's blocks are thus resident and past their launch
-// while this pass drains.  Without the launch attribute both instructions
-// return at once.
-__device__ inline void pdl_enter() {
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-}
-
 __device__ inline void warp_count(unsigned long long* ctr, int v) {
   // every lane of the warp reaches this call (no early returns in kernels)
   int s = __reduce_add_sync(0xffffffffu, v);
@@ -766,7 +754,6 @@ __device__ inline const CoupT<float>& coup<float>(const PassArgs& a) { return a.
 // neighbour offset and field pointer of the staple is fixed at compile time
 template <typename R, int CC, int MU, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_link(Fields<R> f, PassArgs a) {
-  pdl_enter();
   const CoupT<R>& cp = coup<R>(a);
   int t = a.t_lo + (int)blockIdx.x * blockDim.x + threadIdx.x;
   int acc = 0, cap = 0, err = 0;
@@ -785,7 +772,6 @@ __global__ void __launch_bounds__(BS, MINB) k_link(Fields<R> f, PassArgs a) {
 
 template <typename R, int CC, int MU, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_u1(Fields<R> f, PassArgs a) {
-  pdl_enter();
   const CoupT<R>& cp = coup<R>(a);
   int t = a.t_lo + (int)blockIdx.x * blockDim.x + threadIdx.x;
   int acc = 0;
@@ -804,7 +790,6 @@ __global__ void __launch_bounds__(BS, MINB) k_u1(Fields<R> f, PassArgs a) {
 // sums of the order parameter over the new ones
 template <typename R, int CC, int FIELD, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_scalar(Fields<R> f, PassArgs a) {
-  pdl_enter();
   const CoupT<R>& cp = coup<R>(a);
   int t = a.t_lo + (int)blockIdx.x * blockDim.x + threadIdx.x;
   int acc = 0, fb = 0;

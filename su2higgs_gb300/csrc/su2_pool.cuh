@@ -53,7 +53,6 @@ __device__ inline const ChainDesc<R>& stage_desc(const PoolArgs& a, int slot) {
 
 template <typename R, int CC, int MU, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_pool_link(PoolArgs a) {
-  pdl_enter();
   int2 tile = a.tiles[blockIdx.x];
   if (bad_tile(a, tile)) return;
   const ChainDesc<R>& d = stage_desc<R>(a, tile.x);
@@ -75,7 +74,6 @@ __global__ void __launch_bounds__(BS, MINB) k_pool_link(PoolArgs a) {
 
 template <typename R, int CC, int MU, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_pool_u1(PoolArgs a) {
-  pdl_enter();
   int2 tile = a.tiles[blockIdx.x];
   if (bad_tile(a, tile)) return;
   const ChainDesc<R>& d = stage_desc<R>(a, tile.x);
@@ -93,7 +91,6 @@ __global__ void __launch_bounds__(BS, MINB) k_pool_u1(PoolArgs a) {
 
 template <typename R, int CC, int FIELD, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_pool_scalar(PoolArgs a) {
-  pdl_enter();
   int2 tile = a.tiles[blockIdx.x];
   if (bad_tile(a, tile)) return;
   const ChainDesc<R>& d = stage_desc<R>(a, tile.x);
