@@ -389,8 +389,23 @@ int su2gpu_pool_cycle(su2gpu_pool* pool, int32_t n, const int32_t* slots, const 
 /* Set one chain's sweep counter (the random stream's sweep index). */
 int su2gpu_pool_set_sweep(su2gpu_pool* pool, int32_t slot, uint32_t sweep);
 /* `nsweeps` sweeps of every active chain; each chain's sweep counter
- * advances by one per sweep.  use_graph != 0 replays one captured sweep. */
+ * advances by one per sweep.  In the persistent mode (the default) the
+ * sweeps are one launch of a persistent kernel that works through the list
+ * of (sweep, pass, tile) items of all chains, each tile waiting only for its
+ * own chain's previous pass; use_graph != 0 replays it from a graph
+ * captured for this number of sweeps.  Otherwise every pass is one launch
+ * over all chains and use_graph != 0 replays one captured sweep.  Both modes
+ * give the same fields bit for bit. */
 int su2gpu_pool_run(su2gpu_pool* pool, int32_t nsweeps, int32_t use_graph);
+/* Persistent mode on (default) or off (one launch per pass). */
+int su2gpu_pool_set_persistent(su2gpu_pool* pool, int32_t on);
+int su2gpu_pool_get_persistent(su2gpu_pool* pool, int32_t* on);
+/* Check of the persistent kernel's bounded dependency wait: runs it on a
+ * work list whose dependencies are never met (pass 0 left out), so every
+ * wait gives up after spin_limit polls; the chains' fields and sweep
+ * counters are untouched.  *flags receives the kernel's error flags (bit 4:
+ * a wait timed out), which are then cleared. */
+int su2gpu_pool_check_wait_timeout(su2gpu_pool* pool, int32_t spin_limit, int32_t* flags);
 /* measure() sums of every active chain, in slot order:
  * sums[k * SU2GPU_NMEAS + m] for the k-th active chain. */
 int su2gpu_pool_measure(su2gpu_pool* pool, double* sums, int32_t max_chains, int32_t* nchains);
@@ -402,7 +417,10 @@ int su2gpu_pool_enqueue(su2gpu_pool* pool, int32_t nsweeps, int32_t use_graph);
 int su2gpu_pool_enqueue_measure(su2gpu_pool* pool, double* device_sums, int32_t max_chains, int32_t* nchains);
 /* Execution stream (a cudaStream_t; NULL = the pool's own stream). */
 int su2gpu_pool_set_stream(su2gpu_pool* pool, void* cuda_stream);
-/* Kernel launches of one pool sweep (passes + the sweep-counter increment). */
+/* Kernel launches of one pool sweep in the one-launch-per-pass mode (passes
+ * + the sweep-counter increment); in the persistent mode, of one
+ * su2gpu_pool_run call whatever its number of sweeps (the persistent kernel
+ * + the sweep-counter increment). */
 int su2gpu_pool_launches_per_sweep(su2gpu_pool* pool, int32_t* n);
 /* One sweep of every chain with CUDA events around every pass (the chains
  * advance): kinds / ms as su2gpu_profile_sweep. */

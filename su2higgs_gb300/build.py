@@ -35,6 +35,14 @@ UNITS = [
     ("inst_f32_fund", "su2_inst.cu", ["SU2_R=float", "SU2_CC=1", "SU2_OPS=ops_f32_fund"]),
     ("inst_f32_adj", "su2_inst.cu", ["SU2_R=float", "SU2_CC=4", "SU2_OPS=ops_f32_adj"]),
     ("inst_f32_su2u1s", "su2_inst.cu", ["SU2_R=float", "SU2_CC=25", "SU2_OPS=ops_f32_su2u1s"]),
+    ("persist_f64_generic", "su2_persist.cu", ["SU2_R=double", "SU2_CC=-1", "SU2_PERSIST=persist_f64_generic"]),
+    ("persist_f64_fund", "su2_persist.cu", ["SU2_R=double", "SU2_CC=1", "SU2_PERSIST=persist_f64_fund"]),
+    ("persist_f64_adj", "su2_persist.cu", ["SU2_R=double", "SU2_CC=4", "SU2_PERSIST=persist_f64_adj"]),
+    ("persist_f64_su2u1s", "su2_persist.cu", ["SU2_R=double", "SU2_CC=25", "SU2_PERSIST=persist_f64_su2u1s"]),
+    ("persist_f32_generic", "su2_persist.cu", ["SU2_R=float", "SU2_CC=-1", "SU2_PERSIST=persist_f32_generic"]),
+    ("persist_f32_fund", "su2_persist.cu", ["SU2_R=float", "SU2_CC=1", "SU2_PERSIST=persist_f32_fund"]),
+    ("persist_f32_adj", "su2_persist.cu", ["SU2_R=float", "SU2_CC=4", "SU2_PERSIST=persist_f32_adj"]),
+    ("persist_f32_su2u1s", "su2_persist.cu", ["SU2_R=float", "SU2_CC=25", "SU2_PERSIST=persist_f32_su2u1s"]),
     ("su2gpu", "su2gpu.cu", []),
     ("su2_noalloc", "su2_noalloc.cu", []),
     ("su2_pool", "su2_pool.cu", []),

@@ -255,14 +255,21 @@ __device__ inline Q<R> ld4(const V4<R>* p, int i) {
 // A load through the read-only data path, for values no thread writes during
 // the launch (a pass's neighbours of the other parity, the fields it does not
 // update); FP32 4-vectors as one 16-byte load, FP64 through the plain path.
+// Units that define SU2_COHERENT_LOADS (the persistent sweep kernel, whose
+// later passes read what its earlier passes wrote) use the plain path, since
+// the read-only path is not coherent with writes made during the launch.
 template <typename R>
 __device__ inline Q<R> ldro4(const V4<R>* p, int i) {
+#ifdef SU2_COHERENT_LOADS
+  return ld4<R>(p, i);
+#else
   if constexpr (sizeof(R) == 4) {
     float4 v = __ldg((const float4*)p + i);
     return Q<R>{v.x, v.y, v.z, v.w};
   } else {
     return ld4<R>(p, i);
   }
+#endif
 }
 template <typename R>
 __device__ inline void st4(V4<R>* p, int i, const Q<R>& q) {
@@ -373,7 +380,11 @@ __device__ inline V3<R> ld3(const Fields<R>& f, int i) {
 // the triplet of a site no thread writes during the launch (see ldro4)
 template <typename R>
 __device__ inline V3<R> ldro3(const Fields<R>& f, int i) {
+#ifdef SU2_COHERENT_LOADS
+  return ld3(f, i);
+#else
   return V3<R>{__ldg(f.trip[0] + i), __ldg(f.trip[1] + i), __ldg(f.trip[2] + i)};
+#endif
 }
 template <typename R>
 __device__ inline void st3(const Fields<R>& f, int i, const V3<R>& v) {

@@ -194,8 +194,8 @@ void launch_pool_reduce(const double* partials, int nblocks, const int* first, i
                         cudaStream_t st) {
   if (nchains) k_pool_reduce<<<nchains, 128, 0, st>>>(partials, nblocks, first, base, out);
 }
-void launch_pool_next_sweep(uint32_t* const* sweeps, int n, cudaStream_t st) {
-  if (n) k_pool_next_sweep<<<(n + 255) / 256, 256, 0, st>>>(sweeps, n);
+void launch_pool_next_sweep(uint32_t* const* sweeps, int n, cudaStream_t st, uint32_t inc) {
+  if (n) k_pool_next_sweep<<<(n + 255) / 256, 256, 0, st>>>(sweeps, n, inc);
 }
 #endif
 

@@ -74,6 +74,17 @@ void launch_muca_set_param(MucaDev* w, const double* partials, int np, double vo
 void launch_reduce_partials(const double* partials, int np, double* out, cudaStream_t st);
 void launch_pool_reduce(const double* partials, int nblocks, const int* first, int base, int nchains, double* out,
                         cudaStream_t st);
-void launch_pool_next_sweep(uint32_t* const* sweeps, int n, cudaStream_t st);
+void launch_pool_next_sweep(uint32_t* const* sweeps, int n, cudaStream_t st, uint32_t inc = 1);
+
+// the persistent sweep kernel of one (precision, content) instantiation
+// (su2_persist.cu): `launch` runs the work list of `args` (a PersistArgs)
+// on `grid` blocks of `threads`; blocks_per_sm: its resident blocks per SM
+struct PersistOps {
+  int threads;
+  void (*launch)(const void* args, unsigned grid, cudaStream_t st);
+  int (*blocks_per_sm)();
+};
+extern const PersistOps persist_f64_generic, persist_f64_fund, persist_f64_adj, persist_f64_su2u1s;
+extern const PersistOps persist_f32_generic, persist_f32_fund, persist_f32_adj, persist_f32_su2u1s;
 
 }  // namespace su2

@@ -112,6 +112,15 @@ struct su2gpu_pool {
   std::vector<int> active;  // active slots in slot order
   bool dirty = true;
   cudaGraphExec_t gexec = nullptr;
+  // the persistent sweep (k_pool_persist): on by default; its work counter
+  // and per-slot finished-tile counts, its resident grid, and the graph of
+  // one launch of gexec_p_n sweeps
+  const PersistOps* pers = nullptr;
+  bool persistent = true;
+  Buf qstate;
+  unsigned persist_grid = 0;
+  cudaGraphExec_t gexec_p = nullptr;
+  int gexec_p_n = 0;
   int var[5] = {0, 0, 0, 0, 0};
   int64_t sweep_passes[SU2GPU_NCOUNTERS] = {0};  // half-sweeps of each kind in one sweep (graph replay)
   // host images of the descriptor and tile tables; members, so that they
@@ -125,7 +134,7 @@ struct su2gpu_pool {
   Buf ring_down;
   cudaStream_t down_st = nullptr;
   std::vector<cudaEvent_t> cyc_ev;
-  struct GroupGraph { int a0, a1; cudaGraphExec_t exec; };
+  struct GroupGraph { int a0, a1, n; cudaGraphExec_t exec; };  // n: sweeps per replay
   std::vector<GroupGraph> ggraphs;
   ConvItem* h_items = nullptr;  // page-locked conversion items of a cycle (2 per chain)
   size_t h_items_n = 0;
@@ -159,6 +168,17 @@ void arena_free(su2gpu_pool* P, size_t off, size_t bytes) {
     else merged.push_back(fr);
   }
   P->free_list.swap(merged);
+}
+
+// the captured graphs of the current membership, launch shapes and mode
+void drop_graphs(su2gpu_pool* P) {
+  if (P->gexec) cudaGraphExecDestroy(P->gexec);
+  P->gexec = nullptr;
+  if (P->gexec_p) cudaGraphExecDestroy(P->gexec_p);
+  P->gexec_p = nullptr;
+  P->gexec_p_n = 0;
+  for (auto& gg : P->ggraphs) cudaGraphExecDestroy(gg.exec);
+  P->ggraphs.clear();
 }
 
 template <typename R>
@@ -237,12 +257,7 @@ int rebuild(su2gpu_pool* P, void* arena_base = nullptr, void* slot_base = nullpt
     if (!mt.empty()) PCK(cudaMemcpyAsync(P->mtiles.p, mt.data(), mt.size() * sizeof(int2), cudaMemcpyHostToDevice, P->st));
     PCK(cudaMemcpyAsync(P->mfirst.p, first.data(), first.size() * sizeof(int), cudaMemcpyHostToDevice, P->st));
     if (!sp.empty()) PCK(cudaMemcpyAsync(P->sweepptrs.p, sp.data(), sp.size() * sizeof(void*), cudaMemcpyHostToDevice, P->st));
-    if (P->gexec) {
-      cudaGraphExecDestroy(P->gexec);
-      P->gexec = nullptr;
-    }
-    for (auto& gg : P->ggraphs) cudaGraphExecDestroy(gg.exec);
-    P->ggraphs.clear();
+    drop_graphs(P);
     P->dirty = false;
   }
   PCK(cudaStreamSynchronize(P->st));
@@ -258,36 +273,22 @@ void mark(su2gpu_pool* P, int kind) {
   P->prof_kind->push_back(kind);
 }
 
-// one sweep of every active chain (update.c:270-430 order); `tot` receives the
+// the passes of one sweep (update.c:270-430 order); `tot` receives the
 // per-chain half-site totals of one sweep
-int enqueue_pool_sweep(su2gpu_pool* P, const void* descs, const int2* const* tiles, const int* nt,
-                       int64_t* tot) {
-  if (!nt) nt = P->ntiles;
-  const su2gpu_params& p = P->recipe;
-  PoolArgs a;
-  memset(&a, 0, sizeof(a));
-  a.descs = descs;
-  a.nslots = P->max_slots;
-  a.err = (int*)P->err.p;
+void sweep_recipe(const su2gpu_params& p, std::vector<PassDesc>& out, int64_t* tot) {
+  out.clear();
   uint32_t pass = 0;
   const int nh = nhiggs_of(p.content);
-  auto vt = [&](int kind) { return P->var[kind]; };
   for (int k = 0; k < p.update_links; k++) {
     for (int mu = 0; mu < 3; mu++)
       for (int par = 0; par <= 1; par++) {
-        a.parity = par; a.sub = mu; a.alg = p.algorithm_su2link; a.pass = pass++;
-        a.tiles = tiles[vt(0)];
-        mark(P, 0);
-        P->ops->pool_link(vt(0), a, nt[vt(0)], P->st);
+        out.push_back(PassDesc{0, (uint8_t)par, (uint8_t)mu, (uint8_t)p.algorithm_su2link, pass++});
         tot[SU2GPU_C_TOTAL_SU2LINK] += 1;
       }
     if (p.content & SU2GPU_U1)
       for (int mu = 0; mu < 3; mu++)
         for (int par = 0; par <= 1; par++) {
-          a.parity = par; a.sub = mu; a.alg = 0; a.pass = pass++;
-          a.tiles = tiles[vt(1)];
-          mark(P, 1);
-          P->ops->pool_u1(vt(1), a, nt[vt(1)], P->st);
+          out.push_back(PassDesc{1, (uint8_t)par, (uint8_t)mu, 0, pass++});
           tot[SU2GPU_C_TOTAL_U1LINK] += 1;
         }
   }
@@ -307,11 +308,7 @@ int enqueue_pool_sweep(su2gpu_pool* P, const void* descs, const int2* const* til
         int nrep = fd.field == 0 ? nh : 1;
         for (int h = 0; h < nrep; h++)
           for (int par = 0; par <= 1; par++) {
-            a.parity = par; a.sub = h; a.alg = force; a.pass = pass++;
-            int kind = 2 + fd.field;
-            a.tiles = tiles[vt(kind)];
-            mark(P, kind);
-            P->ops->pool_scalar(vt(kind), fd.field, a, nt[vt(kind)], P->st);
+            out.push_back(PassDesc{(uint8_t)(2 + fd.field), (uint8_t)par, (uint8_t)h, (uint8_t)force, pass++});
             bool orr = fd.alg == SU2GPU_OVERRELAX && !force;
             int idx = fd.field == 0 ? (orr ? SU2GPU_C_TOTAL_OR_DOUBLET : SU2GPU_C_TOTAL_DOUBLET) + h
                                     : (fd.field == 1 ? (orr ? SU2GPU_C_TOTAL_OR_TRIPLET : SU2GPU_C_TOTAL_TRIPLET)
@@ -320,9 +317,69 @@ int enqueue_pool_sweep(su2gpu_pool* P, const void* descs, const int2* const* til
           }
       }
   }
+}
+
+// one sweep of every chain of the tile tables, one launch per pass
+int enqueue_pool_sweep(su2gpu_pool* P, const void* descs, const int2* const* tiles, const int* nt,
+                       int64_t* tot) {
+  if (!nt) nt = P->ntiles;
+  std::vector<PassDesc> passes;
+  sweep_recipe(P->recipe, passes, tot);
+  PoolArgs a;
+  memset(&a, 0, sizeof(a));
+  a.descs = descs;
+  a.nslots = P->max_slots;
+  a.err = (int*)P->err.p;
+  for (const PassDesc& q : passes) {
+    const int kind = q.kind, v = P->var[kind];
+    a.parity = q.parity; a.sub = q.sub; a.alg = q.alg; a.pass = q.pass;
+    a.tiles = tiles[v];
+    mark(P, kind);
+    if (kind == 0) P->ops->pool_link(v, a, nt[v], P->st);
+    else if (kind == 1) P->ops->pool_u1(v, a, nt[v], P->st);
+    else P->ops->pool_scalar(v, kind - 2, a, nt[v], P->st);
+  }
   mark(P, -1);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(SU2GPU_ERR_CUDA, "pool sweep launch: %s", cudaGetErrorString(e));
+  return SU2GPU_OK;
+}
+
+// `nsweeps` sweeps of the chains of a range of the 128-site tile table
+// (variant 0) in one launch of the persistent kernel, then their sweep
+// counters + nsweeps.  first_item / spin_limit: see PersistArgs.
+int enqueue_persist(su2gpu_pool* P, const int2* tiles, int nt, uint32_t* const* sweeps, int nchains, int nsweeps,
+                    int64_t* tot, unsigned first_item = 0, int spin_limit = 1 << 18) {
+  std::vector<PassDesc> passes;
+  sweep_recipe(P->recipe, passes, tot);
+  if ((int)passes.size() > PERSIST_MAX_PASSES)
+    return fail(SU2GPU_ERR_INVALID, "%d passes per sweep: the persistent sweep takes at most %d", (int)passes.size(),
+                PERSIST_MAX_PASSES);
+  const double items = (double)nt * (double)passes.size() * (double)nsweeps;
+  if (items >= 4.0e9) return fail(SU2GPU_ERR_INVALID, "%d sweeps of %d tiles: too many work items for one launch",
+                                  nsweeps, nt);
+  if (kVariantBS[0] != P->pers->threads) return fail(SU2GPU_ERR_INVALID, "persistent sweep: tile size mismatch");
+  if (!P->persist_grid) return fail(SU2GPU_ERR_CUDA, "persistent sweep: no resident blocks per SM");
+  PersistArgs A;
+  memset(&A, 0, sizeof(A));
+  A.descs = P->descs.p;
+  A.tiles = tiles;
+  A.ntiles = nt;
+  A.nslots = P->max_slots;
+  A.npasses = (int)passes.size();
+  A.nsweeps = nsweeps;
+  A.first_item = first_item;
+  A.spin_limit = spin_limit;
+  A.head = (unsigned*)P->qstate.p;
+  A.done = (unsigned*)P->qstate.p + 1;
+  A.err = (int*)P->err.p;
+  for (size_t k = 0; k < passes.size(); k++) A.passes[k] = passes[k];
+  PCK(cudaMemsetAsync(P->qstate.p, 0, ((size_t)P->max_slots + 1) * sizeof(unsigned), P->st));
+  unsigned grid = (unsigned)std::min<double>((double)P->persist_grid, items);
+  P->pers->launch(&A, grid, P->st);
+  PCK(cudaGetLastError());
+  if (nsweeps > 0 && first_item == 0) launch_pool_next_sweep(sweeps, nchains, P->st, (uint32_t)nsweeps);
+  PCK(cudaGetLastError());
   return SU2GPU_OK;
 }
 
@@ -359,6 +416,7 @@ int su2gpu_pool_create(const su2gpu_params* recipe, int64_t arena_bytes, int32_t
   P->content = recipe->content & 0x1f;
   P->ops = pick_ops(P->prec, P->content);
   P->pops = P->prec == 64 ? &precops_f64 : &precops_f32;
+  P->pers = pick_persist(P->prec, P->content);
   P->max_slots = max_chains;
   P->slots.resize(max_chains);
   int rc;
@@ -378,11 +436,17 @@ int su2gpu_pool_create(const su2gpu_params* recipe, int64_t arena_bytes, int32_t
   }
   size_t dsz = P->prec == 64 ? sizeof(ChainDesc<double>) : sizeof(ChainDesc<float>);
   if ((rc = P->arena.ensure((size_t)arena_bytes)) || (rc = P->slotmem.ensure((size_t)max_chains * 256)) ||
-      (rc = P->descs.ensure(dsz * max_chains)) || (rc = P->err.ensure(256))) {
+      (rc = P->descs.ensure(dsz * max_chains)) || (rc = P->err.ensure(256)) ||
+      (rc = P->qstate.ensure(((size_t)max_chains + 1) * sizeof(unsigned)))) {
     su2gpu_pool_destroy(P);
     return rc;
   }
   P->free_list.push_back({0, (size_t)arena_bytes});
+  {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    P->persist_grid = (unsigned)std::max(0, sms * P->pers->blocks_per_sm());
+  }
   cudaMemsetAsync(P->slotmem.p, 0, P->slotmem.n, P->st);
   cudaMemsetAsync(P->err.p, 0, P->err.n, P->st);
   if (cudaStreamSynchronize(P->st) != cudaSuccess) {
@@ -397,7 +461,8 @@ int su2gpu_pool_destroy(su2gpu_pool* P) {
   if (!P) return SU2GPU_OK;
   if (P->st) cudaStreamSynchronize(P->st);
   if (P->own_st) cudaStreamSynchronize(P->own_st);
-  if (P->gexec) cudaGraphExecDestroy(P->gexec);
+  drop_graphs(P);
+  P->qstate.release();
   P->arena.release(); P->slotmem.release(); P->descs.release(); P->mtiles.release(); P->mfirst.release();
   P->sweepptrs.release(); P->partials.release(); P->sums.release(); P->stage.release(); P->err.release();
   for (int v = 0; v < NVARIANTS; v++) P->tiles[v].release();
@@ -409,7 +474,6 @@ int su2gpu_pool_destroy(su2gpu_pool* P) {
   P->ring_down.release();
   for (cudaEvent_t e : P->ring_ev) cudaEventDestroy(e);
   for (cudaEvent_t e : P->cyc_ev) cudaEventDestroy(e);
-  for (auto& gg : P->ggraphs) cudaGraphExecDestroy(gg.exec);
   if (P->h_items) cudaFreeHost(P->h_items);
   P->d_items.release();
   if (P->copy_st) cudaStreamDestroy(P->copy_st);
@@ -785,8 +849,39 @@ static int pool_enqueue(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
   if (P->active.empty() || !nsweeps) return SU2GPU_OK;
   const int2* tiles[NVARIANTS];
   for (int v = 0; v < NVARIANTS; v++) tiles[v] = (const int2*)P->tiles[v].p;
+  uint32_t* const* sweeps = (uint32_t* const*)P->sweepptrs.p;
+  const int na = (int)P->active.size();
   int64_t tot[SU2GPU_NCOUNTERS] = {0};
-  if (use_graph) {
+  if (P->persistent) {
+    // one launch of the persistent kernel for all nsweeps sweeps (in a graph
+    // captured for this number of sweeps)
+    if (use_graph) {
+      if (!P->gexec_p || P->gexec_p_n != nsweeps) {
+        if (P->gexec_p) cudaGraphExecDestroy(P->gexec_p);
+        P->gexec_p = nullptr;
+        cudaGraph_t graph;
+        cudaStream_t exec = P->st;
+        PCK(cudaStreamSynchronize(exec));
+        P->st = P->own_st;
+        PCK(cudaStreamBeginCapture(P->st, cudaStreamCaptureModeThreadLocal));
+        rc = enqueue_persist(P, tiles[0], P->ntiles[0], sweeps, na, nsweeps, tot);
+        cudaError_t e = cudaStreamEndCapture(P->st, &graph);
+        P->st = exec;
+        if (rc) return rc;
+        if (e != cudaSuccess) return fail(SU2GPU_ERR_CUDA, "pool graph capture: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&P->gexec_p, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return fail(SU2GPU_ERR_CUDA, "pool graph instantiate: %s", cudaGetErrorString(e));
+        P->gexec_p_n = nsweeps;
+      } else {
+        std::vector<PassDesc> passes;
+        sweep_recipe(P->recipe, passes, tot);
+      }
+      PCK(cudaGraphLaunch(P->gexec_p, P->st));
+    } else if ((rc = enqueue_persist(P, tiles[0], P->ntiles[0], sweeps, na, nsweeps, tot))) {
+      return rc;
+    }
+  } else if (use_graph) {
     if (!P->gexec) {
       cudaGraph_t graph;
       cudaStream_t exec = P->st;
@@ -794,7 +889,7 @@ static int pool_enqueue(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
       P->st = P->own_st;
       PCK(cudaStreamBeginCapture(P->st, cudaStreamCaptureModeThreadLocal));
       rc = enqueue_pool_sweep(P, P->descs.p, tiles, nullptr, tot);
-      launch_pool_next_sweep((uint32_t* const*)P->sweepptrs.p, (int)P->active.size(), P->st);
+      launch_pool_next_sweep(sweeps, na, P->st);
       cudaError_t e = cudaStreamEndCapture(P->st, &graph);
       P->st = exec;
       if (rc) return rc;
@@ -810,7 +905,7 @@ static int pool_enqueue(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
     for (int k = 0; k < nsweeps; k++) {
       int64_t t1[SU2GPU_NCOUNTERS] = {0};
       if ((rc = enqueue_pool_sweep(P, P->descs.p, tiles, nullptr, t1))) return rc;
-      launch_pool_next_sweep((uint32_t* const*)P->sweepptrs.p, (int)P->active.size(), P->st);
+      launch_pool_next_sweep(sweeps, na, P->st);
       if (k == 0) memcpy(tot, t1, sizeof(t1));
     }
   }
@@ -824,7 +919,9 @@ static int pool_check(su2gpu_pool* P) {
   int herr = 0;
   PCK(cudaMemcpyAsync(&herr, P->err.p, sizeof(int), cudaMemcpyDeviceToHost, P->st));
   PCK(cudaStreamSynchronize(P->st));
-  if (herr) return fail(SU2GPU_ERR_KERNEL, "a pool kernel reported an invalid state (NaN fields?)");
+  if (herr)
+    return fail(SU2GPU_ERR_KERNEL, "a pool kernel reported an invalid state (flags %d: 1 NaN fields, 2 bad tile, "
+                "4 persistent sweep dependency wait timed out)", herr);
   return SU2GPU_OK;
 }
 
@@ -838,26 +935,35 @@ int su2gpu_pool_run(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
 // pipelined cycle: upload, sweeps, measurement and download of the whole pool
 // with the host transfers of some groups of chains under the sweeps of others
 // ---------------------------------------------------------------------------
-// one sweep of the active chains [a0, a1): their tile ranges of every variant
-// and their sweep counters
-static int enqueue_group_sweep(su2gpu_pool* P, int a0, int a1, int64_t* tot) {
+// `n` sweeps of the active chains [a0, a1): their tile ranges and sweep
+// counters (persistent: one launch; otherwise one launch per pass and sweep)
+static int enqueue_group_sweep(su2gpu_pool* P, int a0, int a1, int n, int64_t* tot) {
+  uint32_t* const* sweeps = (uint32_t* const*)P->sweepptrs.p + a0;
+  if (P->persistent) {
+    const int2* t0 = (const int2*)P->tiles[0].p + P->h_tfirst[0][a0];
+    return enqueue_persist(P, t0, P->h_tfirst[0][a1] - P->h_tfirst[0][a0], sweeps, a1 - a0, n, tot);
+  }
   const int2* tiles[NVARIANTS];
   int nt[NVARIANTS];
   for (int v = 0; v < NVARIANTS; v++) {
     tiles[v] = (const int2*)P->tiles[v].p + P->h_tfirst[v][a0];
     nt[v] = P->h_tfirst[v][a1] - P->h_tfirst[v][a0];
   }
-  int rc = enqueue_pool_sweep(P, P->descs.p, tiles, nt, tot);
-  if (rc) return rc;
-  launch_pool_next_sweep((uint32_t* const*)P->sweepptrs.p + a0, a1 - a0, P->st);
+  for (int k = 0; k < n; k++) {
+    int64_t t1[SU2GPU_NCOUNTERS] = {0};
+    int rc = enqueue_pool_sweep(P, P->descs.p, tiles, nt, k ? t1 : tot);
+    if (rc) return rc;
+    launch_pool_next_sweep(sweeps, a1 - a0, P->st);
+  }
   PCK(cudaGetLastError());
   return SU2GPU_OK;
 }
 
-// the sweep graph of the group [a0, a1), captured on the pool's own stream
-static int group_graph(su2gpu_pool* P, int a0, int a1, cudaGraphExec_t* out) {
+// the sweep graph of the group [a0, a1) (n sweeps per replay), captured on
+// the pool's own stream
+static int group_graph(su2gpu_pool* P, int a0, int a1, int n, cudaGraphExec_t* out) {
   for (auto& gg : P->ggraphs)
-    if (gg.a0 == a0 && gg.a1 == a1) {
+    if (gg.a0 == a0 && gg.a1 == a1 && gg.n == n) {
       *out = gg.exec;
       return SU2GPU_OK;
     }
@@ -868,7 +974,7 @@ static int group_graph(su2gpu_pool* P, int a0, int a1, cudaGraphExec_t* out) {
   cudaGraph_t graph;
   PCK(cudaStreamBeginCapture(P->st, cudaStreamCaptureModeThreadLocal));
   int64_t tot[SU2GPU_NCOUNTERS] = {0};
-  int rc = enqueue_group_sweep(P, a0, a1, tot);
+  int rc = enqueue_group_sweep(P, a0, a1, n, tot);
   cudaError_t e = cudaStreamEndCapture(P->st, &graph);
   P->st = exec;
   if (rc) return rc;
@@ -877,7 +983,7 @@ static int group_graph(su2gpu_pool* P, int a0, int a1, cudaGraphExec_t* out) {
   e = cudaGraphInstantiate(&ge, graph, 0);
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) return fail(SU2GPU_ERR_CUDA, "group graph instantiate: %s", cudaGetErrorString(e));
-  P->ggraphs.push_back({a0, a1, ge});
+  P->ggraphs.push_back({a0, a1, n, ge});
   *out = ge;
   return SU2GPU_OK;
 }
@@ -945,9 +1051,11 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
   const std::vector<int> groups = cycle_groups(P);
   const int G = (int)groups.size() - 1;
   std::vector<cudaGraphExec_t> gex(G, nullptr);
+  // sweeps per graph replay: all of them in one persistent launch, else one
+  const int per_replay = P->persistent ? nsweeps : 1;
   if (use_graph && nsweeps > 0)
     for (int g = 0; g < G; g++)
-      if ((rc = group_graph(P, groups[g], groups[g + 1], &gex[g]))) return rc;
+      if ((rc = group_graph(P, groups[g], groups[g + 1], per_replay, &gex[g]))) return rc;
   // staging bytes of every group; a group's chains sit side by side in the
   // rings (a ring holds the largest group at least), so a chain only ever
   // overlaps chains of earlier groups, whose release events are recorded
@@ -1018,12 +1126,12 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
     PCK(cudaEventRecord(ev[4 * g + 1], P->copy_st));
     // update stream: the group's sweeps and measurement
     PCK(cudaStreamWaitEvent(P->st, ev[4 * g + 1], 0));
-    for (int k = 0; k < nsweeps; k++) {
+    if (nsweeps > 0) {
       if (use_graph) {
-        PCK(cudaGraphLaunch(gex[g], P->st));
+        for (int k = 0; k < nsweeps; k += per_replay) PCK(cudaGraphLaunch(gex[g], P->st));
       } else {
         int64_t t1[SU2GPU_NCOUNTERS] = {0};
-        if ((rc = enqueue_group_sweep(P, a0, a1, t1))) return rc;
+        if ((rc = enqueue_group_sweep(P, a0, a1, nsweeps, t1))) return rc;
       }
     }
     if (sums) enqueue_group_measure(P, a0, a1, (double*)P->sums.p);
@@ -1061,13 +1169,8 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
   }
   // half-sweeps of each kind in one sweep of a chain
   {
-    const int2* tl[NVARIANTS] = {nullptr, nullptr, nullptr, nullptr};
-    int zero[NVARIANTS] = {0, 0, 0, 0};
-    cudaStream_t keep = P->st;
-    // counting only: no launch happens with zero tiles
-    rc = enqueue_pool_sweep(P, P->descs.p, tl, zero, tot);
-    P->st = keep;
-    if (rc) return rc;
+    std::vector<PassDesc> passes;
+    sweep_recipe(P->recipe, passes, tot);
   }
   std::vector<double> hs;
   if (sums) {
@@ -1090,6 +1193,44 @@ int su2gpu_pool_enqueue(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
   return pool_enqueue(P, nsweeps, use_graph);
 }
 
+int su2gpu_pool_set_persistent(su2gpu_pool* P, int32_t on) {
+  if (!P) return SU2GPU_ERR_INVALID;
+  PCK(cudaStreamSynchronize(P->st));
+  P->persistent = on != 0;
+  drop_graphs(P);
+  return SU2GPU_OK;
+}
+
+int su2gpu_pool_get_persistent(su2gpu_pool* P, int32_t* on) {
+  if (!P || !on) return SU2GPU_ERR_INVALID;
+  *on = P->persistent ? 1 : 0;
+  return SU2GPU_OK;
+}
+
+// the persistent kernel on a work list whose dependencies never finish: the
+// list starts at pass 1 of the chains' first sweep, and pass 0 is never run,
+// so every item's wait runs out after spin_limit polls.  Fields and sweep
+// counters stay as they were; *flags receives the kernel's error flags
+// (4 = a wait timed out), which are cleared afterwards.
+int su2gpu_pool_check_wait_timeout(su2gpu_pool* P, int32_t spin_limit, int32_t* flags) {
+  if (!P || !flags || spin_limit < 1) return fail(SU2GPU_ERR_INVALID, "bad wait-timeout check arguments");
+  int rc;
+  if (P->dirty && (rc = rebuild(P))) return rc;
+  if (P->active.empty()) return fail(SU2GPU_ERR_INVALID, "the pool has no chains");
+  PCK(cudaStreamSynchronize(P->st));
+  int64_t tot[SU2GPU_NCOUNTERS] = {0};
+  const int nt = P->ntiles[0];
+  if ((rc = enqueue_persist(P, (const int2*)P->tiles[0].p, nt, (uint32_t* const*)P->sweepptrs.p,
+                            (int)P->active.size(), 1, tot, (unsigned)nt, spin_limit)))
+    return rc;
+  PCK(cudaStreamSynchronize(P->st));
+  int herr = 0;
+  PCK(cudaMemcpy(&herr, P->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+  PCK(cudaMemset(P->err.p, 0, sizeof(int)));
+  *flags = herr;
+  return SU2GPU_OK;
+}
+
 int su2gpu_pool_set_stream(su2gpu_pool* P, void* stream) {
   if (!P) return SU2GPU_ERR_INVALID;
   PCK(cudaStreamSynchronize(P->st));
@@ -1099,6 +1240,10 @@ int su2gpu_pool_set_stream(su2gpu_pool* P, void* stream) {
 
 int su2gpu_pool_launches_per_sweep(su2gpu_pool* P, int32_t* n) {
   if (!P || !n) return SU2GPU_ERR_INVALID;
+  if (P->persistent) {
+    *n = 2;
+    return SU2GPU_OK;
+  }
   // the recipe's passes per sweep, in the order of enqueue_pool_sweep
   const su2gpu_params& p = P->recipe;
   const int nh = nhiggs_of(p.content);
@@ -1262,9 +1407,7 @@ int su2gpu_pool_autotune(su2gpu_pool* P, int32_t* choices, float* best_ms) {
   cudaEventDestroy(e1);
   PCK(cudaStreamSynchronize(P->st));
   arena2.release(); slot2.release(); desc2.release();
-  if (P->gexec) { cudaGraphExecDestroy(P->gexec); P->gexec = nullptr; }
-  for (auto& gg : P->ggraphs) cudaGraphExecDestroy(gg.exec);
-  P->ggraphs.clear();
+  drop_graphs(P);
   if (choices)
     for (int k = 0; k < 5; k++) choices[k] = P->var[k];
   return SU2GPU_OK;
@@ -1276,9 +1419,7 @@ int su2gpu_pool_set_variants(su2gpu_pool* P, const int32_t* choices) {
     if (choices[k] < 0 || choices[k] >= NVARIANTS) return SU2GPU_ERR_INVALID;
     P->var[k] = choices[k];
   }
-  if (P->gexec) { cudaGraphExecDestroy(P->gexec); P->gexec = nullptr; }
-  for (auto& gg : P->ggraphs) cudaGraphExecDestroy(gg.exec);
-  P->ggraphs.clear();
+  drop_graphs(P);
   return SU2GPU_OK;
 }
 

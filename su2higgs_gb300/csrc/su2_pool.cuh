@@ -40,9 +40,9 @@ __device__ inline bool bad_tile(const PoolArgs& a, int2 tile) {
 }
 
 template <typename R>
-__device__ inline const ChainDesc<R>& stage_desc(const PoolArgs& a, int slot) {
+__device__ inline const ChainDesc<R>& stage_desc_slot(const void* descs, int slot) {
   __shared__ __align__(16) unsigned char buf[sizeof(ChainDesc<R>)];
-  const uint4* src = (const uint4*)((const ChainDesc<R>*)a.descs + slot);
+  const uint4* src = (const uint4*)((const ChainDesc<R>*)descs + slot);
   uint4* dst = (uint4*)buf;
   constexpr int N = (int)(sizeof(ChainDesc<R>) / sizeof(uint4));
   static_assert(sizeof(ChainDesc<R>) % sizeof(uint4) == 0, "descriptor must be a multiple of 16 bytes");
@@ -50,26 +50,88 @@ __device__ inline const ChainDesc<R>& stage_desc(const PoolArgs& a, int slot) {
   __syncthreads();
   return *(const ChainDesc<R>*)buf;
 }
+template <typename R>
+__device__ inline const ChainDesc<R>& stage_desc(const PoolArgs& a, int slot) {
+  return stage_desc_slot<R>(a.descs, slot);
+}
 
+// The per-tile work of the update passes: the sites [t0, t0 + blockDim.x)
+// of one parity of the chain d, with the chain's random stream at sweep
+// `sweep` and pass `pass`.  Every thread of the block calls these (the
+// counters are reduced per warp).
+template <typename R, int CC, int MU>
+__device__ inline void tile_link(const ChainDesc<R>& d, int parity, int alg, uint32_t pass, uint32_t sweep, int t0,
+                                 int* errp) {
+  int t = t0 + threadIdx.x;
+  int acc = 0, cap = 0, err = 0;
+  if (t < d.g.half) {
+    int c[3];
+    site_coords(d.g, parity, t, c);
+    int i = parity * d.g.half + t;
+    SiteRng<R> rng(RngKey{d.k0, d.k1, d.chain, d.sweep}, sweep, (uint32_t)i, pass);
+    if (alg == ALG_HEATBATH) acc = heatbath<R, CC>(d.f, d.g, d.cp, c, i, MU, rng, &cap, &err);
+    else acc = metro_link<R, CC>(d.f, d.g, d.cp, c, i, MU, rng);
+  }
+  warp_count(d.ctr + 1, acc);
+  warp_count(d.ctr + 22, cap);
+  if (err) atomicOr(errp, 1);
+}
+
+template <typename R, int CC, int MU>
+__device__ inline void tile_u1(const ChainDesc<R>& d, int parity, uint32_t pass, uint32_t sweep, int t0) {
+  int t = t0 + threadIdx.x;
+  int acc = 0;
+  if (t < d.g.half) {
+    int c[3];
+    site_coords(d.g, parity, t, c);
+    int i = parity * d.g.half + t;
+    SiteRng<R> rng(RngKey{d.k0, d.k1, d.chain, d.sweep}, sweep, (uint32_t)i, pass);
+    acc = metro_u1<R, CC>(d.f, d.g, d.cp, c, i, MU, rng);
+  }
+  warp_count(d.ctr + 3, acc);
+}
+
+// FIELD 0 doublet `sub`, 1 triplet, 2 singlet; force: the pass's forced
+// Metropolis flag (the last scalar sweep of an overrelaxation field)
+template <typename R, int CC, int FIELD>
+__device__ inline void tile_scalar(const ChainDesc<R>& d, int parity, int sub, int force, uint32_t pass,
+                                   uint32_t sweep, int t0) {
+  const CoupT<R>& cp = d.cp;
+  int t = t0 + threadIdx.x;
+  int acc = 0, fb = 0;
+  if (t < d.g.half) {
+    int c[3];
+    site_coords(d.g, parity, t, c);
+    int i = parity * d.g.half + t;
+    SiteRng<R> rng(RngKey{d.k0, d.k1, d.chain, d.sweep}, sweep, (uint32_t)i, pass);
+    constexpr int CCx = CC;
+    if (FIELD == 0) {
+      const bool orr = cp.alg_d == ALG_OR && !force;
+      if (orr) acc = SU2_HAS(CCx, cp.content, C_H2) ? overrelax_higgs2<R, CC>(d.f, d.g, cp, c, i, sub, rng, &fb)
+                                                    : overrelax_doublet<R, CC>(d.f, d.g, cp, c, i, rng, &fb);
+      else acc = metro_doublet<R, CC>(d.f, d.g, cp, c, i, sub, rng);
+    } else if (FIELD == 1) {
+      if (cp.alg_t == ALG_OR && !force) acc = overrelax_triplet<R, CC>(d.f, d.g, cp, c, i, rng, &fb);
+      else acc = metro_triplet<R, CC>(d.f, d.g, cp, c, i, rng);
+    } else {
+      if (cp.alg_s == ALG_OR && !force) acc = overrelax_singlet<R, CC>(d.f, d.g, cp, c, i, rng, &fb);
+      else acc = metro_singlet<R, CC>(d.f, d.g, cp, c, i, rng);
+    }
+  }
+  int base_or = FIELD == 0 ? 10 + sub : (FIELD == 1 ? 15 : 19);
+  int base_mt = FIELD == 0 ? 6 + sub : (FIELD == 1 ? 13 : 17);
+  bool any_or = (FIELD == 0 ? cp.alg_d : (FIELD == 1 ? cp.alg_t : cp.alg_s)) == ALG_OR && !force;
+  warp_count(d.ctr + (any_or ? base_or : base_mt), acc);
+  warp_count(d.ctr + 23, fb);
+}
+
+// one launch per pass: block b works on tile b of the table
 template <typename R, int CC, int MU, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_pool_link(PoolArgs a) {
   int2 tile = a.tiles[blockIdx.x];
   if (bad_tile(a, tile)) return;
   const ChainDesc<R>& d = stage_desc<R>(a, tile.x);
-  const CoupT<R>& cp = d.cp;
-  int t = tile.y + threadIdx.x;
-  int acc = 0, cap = 0, err = 0;
-  if (t < d.g.half) {
-    int c[3];
-    site_coords(d.g, a.parity, t, c);
-    int i = a.parity * d.g.half + t;
-    SiteRng<R> rng(RngKey{d.k0, d.k1, d.chain, d.sweep}, *d.sweep, (uint32_t)i, a.pass);
-    if (a.alg == ALG_HEATBATH) acc = heatbath<R, CC>(d.f, d.g, cp, c, i, MU, rng, &cap, &err);
-    else acc = metro_link<R, CC>(d.f, d.g, cp, c, i, MU, rng);
-  }
-  warp_count(d.ctr + 1, acc);
-  warp_count(d.ctr + 22, cap);
-  if (err) atomicOr(a.err, 1);
+  tile_link<R, CC, MU>(d, a.parity, a.alg, a.pass, *d.sweep, tile.y, a.err);
 }
 
 template <typename R, int CC, int MU, int BS, int MINB>
@@ -77,16 +139,7 @@ __global__ void __launch_bounds__(BS, MINB) k_pool_u1(PoolArgs a) {
   int2 tile = a.tiles[blockIdx.x];
   if (bad_tile(a, tile)) return;
   const ChainDesc<R>& d = stage_desc<R>(a, tile.x);
-  int t = tile.y + threadIdx.x;
-  int acc = 0;
-  if (t < d.g.half) {
-    int c[3];
-    site_coords(d.g, a.parity, t, c);
-    int i = a.parity * d.g.half + t;
-    SiteRng<R> rng(RngKey{d.k0, d.k1, d.chain, d.sweep}, *d.sweep, (uint32_t)i, a.pass);
-    acc = metro_u1<R, CC>(d.f, d.g, d.cp, c, i, MU, rng);
-  }
-  warp_count(d.ctr + 3, acc);
+  tile_u1<R, CC, MU>(d, a.parity, a.pass, *d.sweep, tile.y);
 }
 
 template <typename R, int CC, int FIELD, int BS, int MINB>
@@ -94,40 +147,161 @@ __global__ void __launch_bounds__(BS, MINB) k_pool_scalar(PoolArgs a) {
   int2 tile = a.tiles[blockIdx.x];
   if (bad_tile(a, tile)) return;
   const ChainDesc<R>& d = stage_desc<R>(a, tile.x);
-  const CoupT<R>& cp = d.cp;
-  int t = tile.y + threadIdx.x;
-  int acc = 0, fb = 0;
-  if (t < d.g.half) {
-    int c[3];
-    site_coords(d.g, a.parity, t, c);
-    int i = a.parity * d.g.half + t;
-    SiteRng<R> rng(RngKey{d.k0, d.k1, d.chain, d.sweep}, *d.sweep, (uint32_t)i, a.pass);
-    constexpr int CCx = CC;
-    if (FIELD == 0) {
-      const bool orr = cp.alg_d == ALG_OR && !a.alg;
-      if (orr) acc = SU2_HAS(CCx, cp.content, C_H2) ? overrelax_higgs2<R, CC>(d.f, d.g, cp, c, i, a.sub, rng, &fb)
-                                                    : overrelax_doublet<R, CC>(d.f, d.g, cp, c, i, rng, &fb);
-      else acc = metro_doublet<R, CC>(d.f, d.g, cp, c, i, a.sub, rng);
-    } else if (FIELD == 1) {
-      if (cp.alg_t == ALG_OR && !a.alg) acc = overrelax_triplet<R, CC>(d.f, d.g, cp, c, i, rng, &fb);
-      else acc = metro_triplet<R, CC>(d.f, d.g, cp, c, i, rng);
-    } else {
-      if (cp.alg_s == ALG_OR && !a.alg) acc = overrelax_singlet<R, CC>(d.f, d.g, cp, c, i, rng, &fb);
-      else acc = metro_singlet<R, CC>(d.f, d.g, cp, c, i, rng);
-    }
-  }
-  int base_or = FIELD == 0 ? 10 + a.sub : (FIELD == 1 ? 15 : 19);
-  int base_mt = FIELD == 0 ? 6 + a.sub : (FIELD == 1 ? 13 : 17);
-  bool any_or = (FIELD == 0 ? cp.alg_d : (FIELD == 1 ? cp.alg_t : cp.alg_s)) == ALG_OR && !a.alg;
-  warp_count(d.ctr + (any_or ? base_or : base_mt), acc);
-  warp_count(d.ctr + 23, fb);
+  tile_scalar<R, CC, FIELD>(d, a.parity, a.sub, a.alg, a.pass, *d.sweep, tile.y);
 }
 
+// ---------------------------------------------------------------------------
+// The persistent sweep: one launch runs `nsweeps` sweeps of every chain of
+// the tile table.  Its work list is (sweep, pass, tile) in that order; each
+// block takes the next item from an atomic counter until the list is done.
+// A tile of pass g of chain c needs pass g-1 of chain c finished, which a
+// per-chain count of finished tiles says (chain c has passed g-1 when the
+// count reaches g x its tiles; a tile of pass g cannot finish before that,
+// so the count is exact).  Chains do not wait for each other, so the passes
+// of different chains overlap and no pass drains the GPU before the next.
+// An item depends only on items earlier in the list, which blocks already
+// running hold, so the launch needs no co-residency: the earliest unfinished
+// item always has its inputs.  The wait is bounded: after spin_limit polls
+// (or at once once another block has given up) the block records error bit
+// 4, skips the item's work (its fields stay as they were) and counts it as
+// finished, so the launch always ends, within about one wait.
+// Fields are read with coherent loads (SU2_COHERENT_LOADS): later passes read
+// what earlier passes of the same launch wrote.
+// ---------------------------------------------------------------------------
+constexpr int PERSIST_MAX_PASSES = 64;
+
+// one pass of the sweep recipe: kind 0 links, 1 U(1), 2 doublet, 3 triplet,
+// 4 singlet; sub: the direction (links, U(1)) or the doublet; alg: the link
+// algorithm of a link pass, the forced Metropolis flag of a scalar pass (as
+// PoolArgs.alg); pass: the pass number within the sweep
+struct PassDesc {
+  uint8_t kind, parity, sub, alg;
+  uint32_t pass;
+};
+
+struct PersistArgs {
+  const void* descs;   // ChainDesc<R>[nslots]
+  const int2* tiles;   // (slot, t0) of every tile of one parity of every chain, chain by chain
+  int ntiles, nslots;
+  int npasses, nsweeps;
+  unsigned first_item;  // the work list starts here (0 in a sweep)
+  int spin_limit;       // polls of a dependency before giving up
+  unsigned* head;       // the work counter, 0 at launch
+  unsigned* done;       // finished tiles per slot, 0 at launch
+  int* err;
+  PassDesc passes[PERSIST_MAX_PASSES];
+};
+
+#ifdef SU2_COHERENT_LOADS
+__device__ inline unsigned ld_acquire_gpu(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// each pass kind as a function of its own (not inlined into the work loop),
+// so that each gets the kernel's register budget to itself instead of one
+// allocation across every kind
+template <typename R, int CC, int MU>
+__device__ __noinline__ void persist_link(const ChainDesc<R>& d, PassDesc p, uint32_t sweep, int t0, int* errp) {
+  tile_link<R, CC, MU>(d, p.parity, p.alg, p.pass, sweep, t0, errp);
+}
+template <typename R, int CC, int MU>
+__device__ __noinline__ void persist_u1(const ChainDesc<R>& d, PassDesc p, uint32_t sweep, int t0) {
+  tile_u1<R, CC, MU>(d, p.parity, p.pass, sweep, t0);
+}
+template <typename R, int CC, int FIELD>
+__device__ __noinline__ void persist_scalar(const ChainDesc<R>& d, PassDesc p, uint32_t sweep, int t0) {
+  tile_scalar<R, CC, FIELD>(d, p.parity, p.sub, p.alg, p.pass, sweep, t0);
+}
+
+template <typename R, int CC>
+__device__ inline void persist_tile(const ChainDesc<R>& d, PassDesc p, uint32_t sweep, int t0, int* errp) {
+  switch (p.kind) {
+    case 0:
+      if (p.sub == 0) persist_link<R, CC, 0>(d, p, sweep, t0, errp);
+      else if (p.sub == 1) persist_link<R, CC, 1>(d, p, sweep, t0, errp);
+      else persist_link<R, CC, 2>(d, p, sweep, t0, errp);
+      break;
+    case 1:
+      if (SU2_HAS(CC, d.cp.content, C_U1)) {
+        if (p.sub == 0) persist_u1<R, CC, 0>(d, p, sweep, t0);
+        else if (p.sub == 1) persist_u1<R, CC, 1>(d, p, sweep, t0);
+        else persist_u1<R, CC, 2>(d, p, sweep, t0);
+      }
+      break;
+    case 2:
+      if (SU2_HAS(CC, d.cp.content, C_H1 | C_H2)) persist_scalar<R, CC, 0>(d, p, sweep, t0);
+      break;
+    case 3:
+      if (SU2_HAS(CC, d.cp.content, C_T)) persist_scalar<R, CC, 1>(d, p, sweep, t0);
+      break;
+    default:
+      if (SU2_HAS(CC, d.cp.content, C_S)) persist_scalar<R, CC, 2>(d, p, sweep, t0);
+  }
+}
+
+template <typename R, int CC, int BS, int MINB>
+__global__ void __launch_bounds__(BS, MINB) k_pool_persist(PersistArgs a) {
+  __shared__ unsigned s_item;
+  __shared__ int s_go;
+  const unsigned total = (unsigned)a.ntiles * (unsigned)(a.npasses * a.nsweeps);
+  unsigned next = 0;
+  if (threadIdx.x == 0) next = atomicAdd(a.head, 1u) + a.first_item;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_item = next;
+      // the item after this one, fetched while this one runs
+      if (next < total) next = atomicAdd(a.head, 1u) + a.first_item;
+    }
+    __syncthreads();
+    const unsigned q = s_item;
+    if (q >= total) break;
+    const unsigned g = q / (unsigned)a.ntiles;
+    const int2 tile = a.tiles[q - g * (unsigned)a.ntiles];
+    const unsigned s = g / (unsigned)a.npasses, k = g - s * (unsigned)a.npasses;
+    const bool bad = (unsigned)tile.x >= (unsigned)a.nslots || tile.y < 0;
+    if (bad) {
+      if (threadIdx.x == 0) atomicOr(a.err, 2);
+      __syncthreads();  // every thread has read s_item before it is reused
+      continue;         // a corrupted table: the item is dropped (dependants time out)
+    }
+    const ChainDesc<R>& d = stage_desc_slot<R>(a.descs, tile.x);
+    if (threadIdx.x == 0) {
+      const unsigned ntc = (unsigned)((d.g.half + BS - 1) / BS);
+      const unsigned need = g * ntc;
+      int go = 1;
+      if (need) {
+        int polls = 0;
+        while (ld_acquire_gpu(a.done + tile.x) < need) {
+          // give up after spin_limit polls, or at once when another block
+          // already gave up (the launch then ends within one wait)
+          if (++polls > a.spin_limit || (*(volatile int*)a.err & 4)) {
+            atomicOr(a.err, 4);
+            go = 0;
+            break;
+          }
+          __nanosleep(64);
+        }
+      }
+      s_go = go;
+    }
+    __syncthreads();
+    if (s_go) persist_tile<R, CC>(d, a.passes[k], *d.sweep + s, tile.y, a.err);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      atomicAdd(a.done + tile.x, 1u);
+    }
+  }
+}
+#endif  // SU2_COHERENT_LOADS
+
 #ifdef SU2_WITH_GLOBAL
-// every active chain's sweep counter + 1
-__global__ void k_pool_next_sweep(uint32_t* const* sweeps, int n) {
+// every active chain's sweep counter + inc
+__global__ void k_pool_next_sweep(uint32_t* const* sweeps, int n, uint32_t inc) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < n) *sweeps[k] += 1u;
+  if (k < n) *sweeps[k] += inc;
 }
 #endif
 

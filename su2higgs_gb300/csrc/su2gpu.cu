@@ -186,6 +186,21 @@ const Ops* su2::pick_ops(int prec, int content) {
   return &ops_f32_generic;
 }
 
+// the persistent sweep kernel of the same instantiation as pick_ops
+const PersistOps* su2::pick_persist(int prec, int content) {
+  int c = content & 0x1f;
+  if (prec == 64) {
+    if (c == C_H1) return &persist_f64_fund;
+    if (c == C_T) return &persist_f64_adj;
+    if (c == (C_H1 | C_S | C_U1)) return &persist_f64_su2u1s;
+    return &persist_f64_generic;
+  }
+  if (c == C_H1) return &persist_f32_fund;
+  if (c == C_T) return &persist_f32_adj;
+  if (c == (C_H1 | C_S | C_U1)) return &persist_f32_su2u1s;
+  return &persist_f32_generic;
+}
+
 extern "C" {
 
 int su2gpu_version(void) { return 10000; }

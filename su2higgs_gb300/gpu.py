@@ -102,6 +102,9 @@ def lib():
         L.su2gpu_pool_download_many.argtypes = [vp, i32, vp, vp]
         L.su2gpu_pool_cycle.argtypes = [vp, i32, vp, vp, i32, i32, vp, vp]
         L.su2gpu_pool_enqueue.argtypes = [vp, i32, i32]
+        L.su2gpu_pool_set_persistent.argtypes = [vp, i32]
+        L.su2gpu_pool_get_persistent.argtypes = [vp, ctypes.POINTER(i32)]
+        L.su2gpu_pool_check_wait_timeout.argtypes = [vp, i32, ctypes.POINTER(i32)]
         L.su2gpu_pool_enqueue_measure.argtypes = [vp, vp, i32, ctypes.POINTER(i32)]
         L.su2gpu_pool_set_stream.argtypes = [vp, vp]
         L.su2gpu_pool_launches_per_sweep.argtypes = [vp, ctypes.POINTER(i32)]
@@ -584,6 +587,25 @@ class Pool:
 
     def enqueue(self, nsweeps, graph=True):
         check(lib().su2gpu_pool_enqueue(self._h, nsweeps, 1 if graph else 0))
+
+    @property
+    def persistent(self):
+        """Sweeps as one launch of the persistent work-list kernel (default)
+        rather than one launch per pass."""
+        on = ctypes.c_int32()
+        check(lib().su2gpu_pool_get_persistent(self._h, ctypes.byref(on)))
+        return bool(on.value)
+
+    @persistent.setter
+    def persistent(self, on):
+        check(lib().su2gpu_pool_set_persistent(self._h, 1 if on else 0))
+
+    def check_wait_timeout(self, spin_limit=2000):
+        """Run the persistent kernel on a work list whose dependencies never
+        finish; returns the kernel's error flags (4: a wait gave up)."""
+        flags = ctypes.c_int32()
+        check(lib().su2gpu_pool_check_wait_timeout(self._h, spin_limit, ctypes.byref(flags)))
+        return flags.value
 
     def enqueue_measure(self, device_ptr, max_chains):
         """Measurement of every active chain into a device buffer of

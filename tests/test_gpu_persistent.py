@@ -1,0 +1,140 @@
+"""The persistent pool sweep (k_pool_persist): one launch works through the
+(sweep, pass, tile) list of every chain, each tile waiting only for its own
+chain's previous pass.
+
+* Same results as one launch per pass, bit for bit: fields and counters of
+  every chain, FP64 and FP32, graph and direct launches, several sweeps per
+  launch, chains of uneven sizes, a single chain (every pass then waits for
+  the previous one), and the pipelined cycle.  The per-site code is the same
+  source in both modes and the random numbers are keyed by chain, site, sweep
+  and pass, not by block or order of execution.
+* The bounded dependency wait: a work list whose dependencies never finish
+  makes every wait give up; the kernel ends, reports flag 4, and leaves the
+  fields and sweep counters untouched; the pool works normally afterwards.
+"""
+import numpy as np
+import pytest
+
+from native import hot_fields
+from su2higgs_gb300 import abi
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    from su2higgs_gb300 import gpu as g
+    g.lib()
+    return g
+
+
+def as_dict(f):
+    return {n: getattr(f, n) for n in ("link", "u1", "d0", "d1", "trip", "sing")}
+
+
+def specs_of(content, precision):
+    base = dict(precision=precision)
+    return [
+        (abi.make_params(content, L=(8, 8, 8), betasu2=6.0, **base), 11, 0),
+        (abi.make_params(content, L=(12, 6, 10), betasu2=9.5, msq_triplet=-0.2, msq_phi=-0.05, **base), 12, 1),
+        (abi.make_params(content, L=(4, 4, 4), betasu2=12.0, **base), 11, 2),
+        (abi.make_params(content, L=(16, 16, 16), **base), 13, 3),
+        (abi.make_params(content, L=(24, 20, 22), betasu2=7.0, **base), 14, 4),
+    ]
+
+
+def make_pool(gpu, specs, persistent, inputs):
+    pool = gpu.Pool(specs[0][0], arena_bytes=128 << 20, max_chains=8)
+    pool.persistent = persistent
+    slots = []
+    for (p, seed, chain), f in zip(specs, inputs):
+        s = pool.add(p, seed=seed, chain=chain)
+        pool.upload(s, **f)
+        slots.append(s)
+    return pool, slots
+
+
+def assert_same(pa, sa, pb, sb):
+    for x, y in zip(sa, sb):
+        fa, fb = pa.download(x), pb.download(y)
+        for n in fa:
+            if fa[n] is not None:
+                d = np.abs(fa[n] - fb[n])
+                assert np.array_equal(fa[n], fb[n]), (x, n, float(d.max()), int(np.count_nonzero(d)))
+        assert np.array_equal(pa.counters(x), pb.counters(y)), x
+
+
+@pytest.mark.parametrize("content,precision", [("fund", 64), ("adj", 64), ("su2u1s", 64), ("higgs2", 64),
+                                               ("fundadj", 64), ("fund", 32), ("adj", 32), ("su2u1s", 32)])
+@pytest.mark.parametrize("graph", [True, False])
+def test_persistent_equals_per_pass(gpu, content, precision, graph):
+    specs = specs_of(content, precision)
+    inputs = [as_dict(hot_fields(p, seed=200 + k, phi_mean=0.5)) for k, (p, _, _) in enumerate(specs)]
+    a, sa = make_pool(gpu, specs, True, inputs)
+    b, sb = make_pool(gpu, specs, False, inputs)
+    assert a.persistent and not b.persistent
+    for n in (1, 3, 2):
+        a.run(n, graph=graph)
+        b.run(n, graph=graph)
+    assert_same(a, sa, b, sb)
+    ma, mb = a.measure(), b.measure()
+    for x, y in zip(sa, sb):
+        assert np.array_equal(ma[x], mb[y])
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_persistent_single_chain(gpu, precision):
+    p = abi.make_params("adj", L=(32, 32, 32), precision=precision)
+    f = [as_dict(hot_fields(p, seed=5, phi_mean=0.5))]
+    a, sa = make_pool(gpu, [(p, 3, 0)], True, f)
+    b, sb = make_pool(gpu, [(p, 3, 0)], False, f)
+    a.run(4)
+    b.run(4)
+    assert_same(a, sa, b, sb)
+
+
+def test_persistent_cycle_equals_per_pass(gpu):
+    specs = specs_of("su2u1s", 32)
+    inputs = [as_dict(hot_fields(p, seed=300 + k, phi_mean=0.5)) for k, (p, _, _) in enumerate(specs)]
+    outs = []
+    for persistent in (True, False):
+        pool, slots = make_pool(gpu, specs, persistent, inputs)
+        fields = [{n: v.copy() for n, v in f.items() if v is not None} for f in inputs]
+        sums = pool.cycle(slots, fields, 3)
+        outs.append((fields, sums, [pool.counters(s) for s in slots]))
+    (fa, ma, ca), (fb, mb, cb) = outs
+    for x, y in zip(fa, fb):
+        for n in x:
+            assert np.array_equal(x[n], y[n]), n
+    assert np.array_equal(ma, mb)
+    for x, y in zip(ca, cb):
+        assert np.array_equal(x, y)
+
+
+def test_persistent_wait_gives_up(gpu):
+    specs = specs_of("adj", 32)[:3]
+    inputs = [as_dict(hot_fields(p, seed=400 + k, phi_mean=0.5)) for k, (p, _, _) in enumerate(specs)]
+    pool, slots = make_pool(gpu, specs, True, inputs)
+    ref, rslots = make_pool(gpu, specs, True, inputs)
+    before = [pool.download(s) for s in slots]
+    flags = pool.check_wait_timeout(spin_limit=500)
+    assert flags & 4, flags
+    for s, f in zip(slots, before):
+        got = pool.download(s)
+        for n in f:
+            if f[n] is not None:
+                assert np.array_equal(got[n], f[n]), n
+    # the flags were cleared and the sweep counters did not move: the pool
+    # goes on exactly as one that never ran the check
+    pool.run(2)
+    ref.run(2)
+    assert_same(pool, slots, ref, rslots)
+
+
+def test_persistent_launch_count(gpu):
+    specs = specs_of("adj", 32)[:2]
+    inputs = [as_dict(hot_fields(p, seed=1)) for p, _, _ in specs]
+    pool, _ = make_pool(gpu, specs, True, inputs)
+    assert pool.launches_per_sweep() == 2
+    pool.persistent = False
+    assert pool.launches_per_sweep() == 6 + 10 + 1
