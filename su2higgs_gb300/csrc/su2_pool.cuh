@@ -58,9 +58,13 @@ __device__ inline const ChainDesc<R>& stage_desc(const PoolArgs& a, int slot) {
 // The per-tile work of the update passes: the sites [t0, t0 + blockDim.x)
 // of one parity of the chain d, with the chain's random stream at sweep
 // `sweep` and pass `pass`.  Every thread of the block calls these (the
-// counters are reduced per warp).
-template <typename R, int CC, int MU>
-__device__ inline void tile_link(const ChainDesc<R>& d, int parity, int alg, uint32_t pass, uint32_t sweep, int t0,
+// counters are reduced per warp).  They are functions of their own, not
+// inlined, with one instance per launch shape (BS, MINB): the one-launch-
+// per-pass kernels and the persistent kernel then run the same compiled
+// arithmetic (the compiler cannot fuse multiply-adds differently in the
+// two contexts) and give the same fields bit for bit.
+template <typename R, int CC, int MU, int BS, int MINB>
+__device__ __noinline__ void tile_link(const ChainDesc<R>& d, int parity, int alg, uint32_t pass, uint32_t sweep, int t0,
                                  int* errp) {
   int t = t0 + threadIdx.x;
   int acc = 0, cap = 0, err = 0;
@@ -77,8 +81,8 @@ __device__ inline void tile_link(const ChainDesc<R>& d, int parity, int alg, uin
   if (err) atomicOr(errp, 1);
 }
 
-template <typename R, int CC, int MU>
-__device__ inline void tile_u1(const ChainDesc<R>& d, int parity, uint32_t pass, uint32_t sweep, int t0) {
+template <typename R, int CC, int MU, int BS, int MINB>
+__device__ __noinline__ void tile_u1(const ChainDesc<R>& d, int parity, uint32_t pass, uint32_t sweep, int t0) {
   int t = t0 + threadIdx.x;
   int acc = 0;
   if (t < d.g.half) {
@@ -93,8 +97,8 @@ __device__ inline void tile_u1(const ChainDesc<R>& d, int parity, uint32_t pass,
 
 // FIELD 0 doublet `sub`, 1 triplet, 2 singlet; force: the pass's forced
 // Metropolis flag (the last scalar sweep of an overrelaxation field)
-template <typename R, int CC, int FIELD>
-__device__ inline void tile_scalar(const ChainDesc<R>& d, int parity, int sub, int force, uint32_t pass,
+template <typename R, int CC, int FIELD, int BS, int MINB>
+__device__ __noinline__ void tile_scalar(const ChainDesc<R>& d, int parity, int sub, int force, uint32_t pass,
                                    uint32_t sweep, int t0) {
   const CoupT<R>& cp = d.cp;
   int t = t0 + threadIdx.x;
@@ -131,7 +135,7 @@ __global__ void __launch_bounds__(BS, MINB) k_pool_link(PoolArgs a) {
   int2 tile = a.tiles[blockIdx.x];
   if (bad_tile(a, tile)) return;
   const ChainDesc<R>& d = stage_desc<R>(a, tile.x);
-  tile_link<R, CC, MU>(d, a.parity, a.alg, a.pass, *d.sweep, tile.y, a.err);
+  tile_link<R, CC, MU, BS, MINB>(d, a.parity, a.alg, a.pass, *d.sweep, tile.y, a.err);
 }
 
 template <typename R, int CC, int MU, int BS, int MINB>
@@ -139,7 +143,7 @@ __global__ void __launch_bounds__(BS, MINB) k_pool_u1(PoolArgs a) {
   int2 tile = a.tiles[blockIdx.x];
   if (bad_tile(a, tile)) return;
   const ChainDesc<R>& d = stage_desc<R>(a, tile.x);
-  tile_u1<R, CC, MU>(d, a.parity, a.pass, *d.sweep, tile.y);
+  tile_u1<R, CC, MU, BS, MINB>(d, a.parity, a.pass, *d.sweep, tile.y);
 }
 
 template <typename R, int CC, int FIELD, int BS, int MINB>
@@ -147,7 +151,7 @@ __global__ void __launch_bounds__(BS, MINB) k_pool_scalar(PoolArgs a) {
   int2 tile = a.tiles[blockIdx.x];
   if (bad_tile(a, tile)) return;
   const ChainDesc<R>& d = stage_desc<R>(a, tile.x);
-  tile_scalar<R, CC, FIELD>(d, a.parity, a.sub, a.alg, a.pass, *d.sweep, tile.y);
+  tile_scalar<R, CC, FIELD, BS, MINB>(d, a.parity, a.sub, a.alg, a.pass, *d.sweep, tile.y);
 }
 
 // ---------------------------------------------------------------------------
@@ -199,45 +203,32 @@ __device__ inline unsigned ld_acquire_gpu(const unsigned* p) {
   return v;
 }
 
-// each pass kind as a function of its own (not inlined into the work loop),
-// so that each gets the kernel's register budget to itself instead of one
-// allocation across every kind
-template <typename R, int CC, int MU>
-__device__ __noinline__ void persist_link(const ChainDesc<R>& d, PassDesc p, uint32_t sweep, int t0, int* errp) {
-  tile_link<R, CC, MU>(d, p.parity, p.alg, p.pass, sweep, t0, errp);
-}
-template <typename R, int CC, int MU>
-__device__ __noinline__ void persist_u1(const ChainDesc<R>& d, PassDesc p, uint32_t sweep, int t0) {
-  tile_u1<R, CC, MU>(d, p.parity, p.pass, sweep, t0);
-}
-template <typename R, int CC, int FIELD>
-__device__ __noinline__ void persist_scalar(const ChainDesc<R>& d, PassDesc p, uint32_t sweep, int t0) {
-  tile_scalar<R, CC, FIELD>(d, p.parity, p.sub, p.alg, p.pass, sweep, t0);
-}
-
-template <typename R, int CC>
+// one tile of pass p (the tile functions are not inlined: each keeps the
+// kernel's register budget to itself)
+template <typename R, int CC, int BS, int MINB>
 __device__ inline void persist_tile(const ChainDesc<R>& d, PassDesc p, uint32_t sweep, int t0, int* errp) {
   switch (p.kind) {
     case 0:
-      if (p.sub == 0) persist_link<R, CC, 0>(d, p, sweep, t0, errp);
-      else if (p.sub == 1) persist_link<R, CC, 1>(d, p, sweep, t0, errp);
-      else persist_link<R, CC, 2>(d, p, sweep, t0, errp);
+      if (p.sub == 0) tile_link<R, CC, 0, BS, MINB>(d, p.parity, p.alg, p.pass, sweep, t0, errp);
+      else if (p.sub == 1) tile_link<R, CC, 1, BS, MINB>(d, p.parity, p.alg, p.pass, sweep, t0, errp);
+      else tile_link<R, CC, 2, BS, MINB>(d, p.parity, p.alg, p.pass, sweep, t0, errp);
       break;
     case 1:
       if (SU2_HAS(CC, d.cp.content, C_U1)) {
-        if (p.sub == 0) persist_u1<R, CC, 0>(d, p, sweep, t0);
-        else if (p.sub == 1) persist_u1<R, CC, 1>(d, p, sweep, t0);
-        else persist_u1<R, CC, 2>(d, p, sweep, t0);
+        if (p.sub == 0) tile_u1<R, CC, 0, BS, MINB>(d, p.parity, p.pass, sweep, t0);
+        else if (p.sub == 1) tile_u1<R, CC, 1, BS, MINB>(d, p.parity, p.pass, sweep, t0);
+        else tile_u1<R, CC, 2, BS, MINB>(d, p.parity, p.pass, sweep, t0);
       }
       break;
     case 2:
-      if (SU2_HAS(CC, d.cp.content, C_H1 | C_H2)) persist_scalar<R, CC, 0>(d, p, sweep, t0);
+      if (SU2_HAS(CC, d.cp.content, C_H1 | C_H2))
+        tile_scalar<R, CC, 0, BS, MINB>(d, p.parity, p.sub, p.alg, p.pass, sweep, t0);
       break;
     case 3:
-      if (SU2_HAS(CC, d.cp.content, C_T)) persist_scalar<R, CC, 1>(d, p, sweep, t0);
+      if (SU2_HAS(CC, d.cp.content, C_T)) tile_scalar<R, CC, 1, BS, MINB>(d, p.parity, 0, p.alg, p.pass, sweep, t0);
       break;
     default:
-      if (SU2_HAS(CC, d.cp.content, C_S)) persist_scalar<R, CC, 2>(d, p, sweep, t0);
+      if (SU2_HAS(CC, d.cp.content, C_S)) tile_scalar<R, CC, 2, BS, MINB>(d, p.parity, 0, p.alg, p.pass, sweep, t0);
   }
 }
 
@@ -287,7 +278,7 @@ __global__ void __launch_bounds__(BS, MINB) k_pool_persist(PersistArgs a) {
       s_go = go;
     }
     __syncthreads();
-    if (s_go) persist_tile<R, CC>(d, a.passes[k], *d.sweep + s, tile.y, a.err);
+    if (s_go) persist_tile<R, CC, BS, MINB>(d, a.passes[k], *d.sweep + s, tile.y, a.err);
     __syncthreads();
     if (threadIdx.x == 0) {
       __threadfence();
