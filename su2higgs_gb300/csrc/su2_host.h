@@ -111,7 +111,7 @@ inline void sweep_order(uint64_t seed, uint32_t chain, uint32_t sweep, int updat
 
 SU2_HIDDEN Coup make_coup(const su2gpu_params* p);
 SU2_HIDDEN const Ops* pick_ops(int prec, int content);
-SU2_HIDDEN const PersistOps* pick_persist(int prec, int content);
+SU2_HIDDEN const PoolOps* pick_persist(int prec, int content);
 
 }  // namespace su2
 

@@ -79,60 +79,11 @@ static void l_flow(const void* fin, const void* fout, const Geom& g, const Coup&
   k_flow<R, CCI><<<nb, BLOCK, 0, st>>>(*(const Fields<R>*)fin, *(const Fields<R>*)fout, g, coup_as<R>(cp), (R)dt, fz);
 }
 
-template <int V>
-static void lp_link_v(const PoolArgs& a, unsigned nb, cudaStream_t st) {
-  constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB;
-  if (!nb) return;
-  if (a.sub == 0) k_pool_link<R, CCI, 0, BS, MB><<<nb, BS, 0, st>>>(a);
-  else if (a.sub == 1) k_pool_link<R, CCI, 1, BS, MB><<<nb, BS, 0, st>>>(a);
-  else k_pool_link<R, CCI, 2, BS, MB><<<nb, BS, 0, st>>>(a);
-}
-template <int V>
-static void lp_u1_v(const PoolArgs& a, unsigned nb, cudaStream_t st) {
-  constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB;
-  if (!nb) return;
-  if (a.sub == 0) k_pool_u1<R, CCI, 0, BS, MB><<<nb, BS, 0, st>>>(a);
-  else if (a.sub == 1) k_pool_u1<R, CCI, 1, BS, MB><<<nb, BS, 0, st>>>(a);
-  else k_pool_u1<R, CCI, 2, BS, MB><<<nb, BS, 0, st>>>(a);
-}
-template <int V>
-static void lp_scalar_v(int field, const PoolArgs& a, unsigned nb, cudaStream_t st) {
-  constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB;
-  if (!nb) return;
-  if (field == 0) k_pool_scalar<R, CCI, 0, BS, MB><<<nb, BS, 0, st>>>(a);
-  else if (field == 1) k_pool_scalar<R, CCI, 1, BS, MB><<<nb, BS, 0, st>>>(a);
-  else k_pool_scalar<R, CCI, 2, BS, MB><<<nb, BS, 0, st>>>(a);
-}
-static void lp_link(int v, const PoolArgs& a, unsigned nb, cudaStream_t st) {
-  switch (v) {
-    case 1: lp_link_v<1>(a, nb, st); break;
-    case 2: lp_link_v<2>(a, nb, st); break;
-    case 3: lp_link_v<3>(a, nb, st); break;
-    default: lp_link_v<0>(a, nb, st);
-  }
-}
-static void lp_u1(int v, const PoolArgs& a, unsigned nb, cudaStream_t st) {
-  switch (v) {
-    case 1: lp_u1_v<1>(a, nb, st); break;
-    case 2: lp_u1_v<2>(a, nb, st); break;
-    case 3: lp_u1_v<3>(a, nb, st); break;
-    default: lp_u1_v<0>(a, nb, st);
-  }
-}
-static void lp_scalar(int v, int field, const PoolArgs& a, unsigned nb, cudaStream_t st) {
-  switch (v) {
-    case 1: lp_scalar_v<1>(field, a, nb, st); break;
-    case 2: lp_scalar_v<2>(field, a, nb, st); break;
-    case 3: lp_scalar_v<3>(field, a, nb, st); break;
-    default: lp_scalar_v<0>(field, a, nb, st);
-  }
-}
 static void lp_measure(const PoolArgs& a, double* partials, unsigned nb, cudaStream_t st) {
   if (nb) k_pool_measure<R, CCI><<<nb, BLOCK, 0, st>>>(a, partials);
 }
 
-const Ops SU2_OPS = {sizeof(R) == 8 ? 64 : 32, CCI, l_link, l_u1, l_scalar, l_measure, l_flow,
-                     lp_link, lp_u1, lp_scalar, lp_measure};
+const Ops SU2_OPS = {sizeof(R) == 8 ? 64 : 32, CCI, l_link, l_u1, l_scalar, l_measure, l_flow, lp_measure};
 
 #ifdef SU2_WITH_PREC
 static unsigned nblk(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }

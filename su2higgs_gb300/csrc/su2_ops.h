@@ -24,11 +24,8 @@ struct Ops {
                   unsigned nblocks, cudaStream_t st);
   void (*flow)(const void* fin, const void* fout, const Geom& g, const Coup& cp, double dt,
                unsigned long long* first_zero, unsigned nblocks, cudaStream_t st);
-  // pools of chains (su2_pool.cuh): nblocks = length of the tile table, which
-  // must have been built for the variant's block size
-  void (*pool_link)(int variant, const PoolArgs& a, unsigned nblocks, cudaStream_t st);
-  void (*pool_u1)(int variant, const PoolArgs& a, unsigned nblocks, cudaStream_t st);
-  void (*pool_scalar)(int variant, int field, const PoolArgs& a, unsigned nblocks, cudaStream_t st);
+  // measurement of pools of chains (su2_pool.cuh): nblocks = length of the
+  // measurement tile table
   void (*pool_measure)(const PoolArgs& a, double* partials, unsigned nblocks, cudaStream_t st);
 };
 
@@ -76,15 +73,20 @@ void launch_pool_reduce(const double* partials, int nblocks, const int* first, i
                         cudaStream_t st);
 void launch_pool_next_sweep(uint32_t* const* sweeps, int n, cudaStream_t st, uint32_t inc = 1);
 
-// the persistent sweep kernel of one (precision, content) instantiation
-// (su2_persist.cu): `launch` runs the work list of `args` (a PersistArgs)
-// on `grid` blocks of `threads`; blocks_per_sm: its resident blocks per SM
-struct PersistOps {
+// the update kernels of pools of one (precision, content) instantiation
+// (su2_persist.cu).  launch: the persistent sweep, the work list of `args`
+// (a PersistArgs) on `grid` blocks of `threads`; blocks_per_sm: its resident
+// blocks per SM.  pool_*: one pass over the tile table (nblocks tiles, built
+// for the variant's block size).
+struct PoolOps {
   int threads;
   void (*launch)(const void* args, unsigned grid, cudaStream_t st);
   int (*blocks_per_sm)();
+  void (*pool_link)(int variant, const PoolArgs& a, unsigned nblocks, cudaStream_t st);
+  void (*pool_u1)(int variant, const PoolArgs& a, unsigned nblocks, cudaStream_t st);
+  void (*pool_scalar)(int variant, int field, const PoolArgs& a, unsigned nblocks, cudaStream_t st);
 };
-extern const PersistOps persist_f64_generic, persist_f64_fund, persist_f64_adj, persist_f64_su2u1s;
-extern const PersistOps persist_f32_generic, persist_f32_fund, persist_f32_adj, persist_f32_su2u1s;
+extern const PoolOps persist_f64_generic, persist_f64_fund, persist_f64_adj, persist_f64_su2u1s;
+extern const PoolOps persist_f32_generic, persist_f32_fund, persist_f32_adj, persist_f32_su2u1s;
 
 }  // namespace su2

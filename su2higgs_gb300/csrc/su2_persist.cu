@@ -1,9 +1,10 @@
-// su2_persist.cu -- the persistent sweep kernel of pools (k_pool_persist in
-// su2_pool.cuh) for one (precision, content): compiled like su2_inst.cu with
-// -DSU2_R / -DSU2_CC / -DSU2_PERSIST=<table name>.  Its own unit because the
-// per-site routines must read fields with coherent loads here
-// (SU2_COHERENT_LOADS), while the one-launch-per-pass kernels keep the
-// read-only data path.
+// su2_persist.cu -- the update kernels of pools (su2_pool.cuh) for one
+// (precision, content): the one-launch-per-pass kernels of every launch
+// shape and the persistent sweep kernel.  Compiled like su2_inst.cu with
+// -DSU2_R / -DSU2_CC / -DSU2_PERSIST=<table name>.  Fields are read with
+// coherent loads here (SU2_COHERENT_LOADS), which the persistent kernel
+// needs; the per-pass kernels live in the same unit so that both modes call
+// the same compiled per-tile functions and give the same fields bit for bit.
 #define SU2_COHERENT_LOADS 1
 #include "su2_pool.cuh"
 
@@ -15,6 +16,54 @@ constexpr int CCI = SU2_CC;
 // blocks per SM asked of the compiler
 constexpr int PBS = Variant<R, 0>::BS, PMB = Variant<R, 0>::MINB;
 
+template <int V>
+static void lp_link_v(const PoolArgs& a, unsigned nb, cudaStream_t st) {
+  constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB;
+  if (!nb) return;
+  if (a.sub == 0) k_pool_link<R, CCI, 0, BS, MB><<<nb, BS, 0, st>>>(a);
+  else if (a.sub == 1) k_pool_link<R, CCI, 1, BS, MB><<<nb, BS, 0, st>>>(a);
+  else k_pool_link<R, CCI, 2, BS, MB><<<nb, BS, 0, st>>>(a);
+}
+template <int V>
+static void lp_u1_v(const PoolArgs& a, unsigned nb, cudaStream_t st) {
+  constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB;
+  if (!nb) return;
+  if (a.sub == 0) k_pool_u1<R, CCI, 0, BS, MB><<<nb, BS, 0, st>>>(a);
+  else if (a.sub == 1) k_pool_u1<R, CCI, 1, BS, MB><<<nb, BS, 0, st>>>(a);
+  else k_pool_u1<R, CCI, 2, BS, MB><<<nb, BS, 0, st>>>(a);
+}
+template <int V>
+static void lp_scalar_v(int field, const PoolArgs& a, unsigned nb, cudaStream_t st) {
+  constexpr int BS = Variant<R, V>::BS, MB = Variant<R, V>::MINB;
+  if (!nb) return;
+  if (field == 0) k_pool_scalar<R, CCI, 0, BS, MB><<<nb, BS, 0, st>>>(a);
+  else if (field == 1) k_pool_scalar<R, CCI, 1, BS, MB><<<nb, BS, 0, st>>>(a);
+  else k_pool_scalar<R, CCI, 2, BS, MB><<<nb, BS, 0, st>>>(a);
+}
+static void lp_link(int v, const PoolArgs& a, unsigned nb, cudaStream_t st) {
+  switch (v) {
+    case 1: lp_link_v<1>(a, nb, st); break;
+    case 2: lp_link_v<2>(a, nb, st); break;
+    case 3: lp_link_v<3>(a, nb, st); break;
+    default: lp_link_v<0>(a, nb, st);
+  }
+}
+static void lp_u1(int v, const PoolArgs& a, unsigned nb, cudaStream_t st) {
+  switch (v) {
+    case 1: lp_u1_v<1>(a, nb, st); break;
+    case 2: lp_u1_v<2>(a, nb, st); break;
+    case 3: lp_u1_v<3>(a, nb, st); break;
+    default: lp_u1_v<0>(a, nb, st);
+  }
+}
+static void lp_scalar(int v, int field, const PoolArgs& a, unsigned nb, cudaStream_t st) {
+  switch (v) {
+    case 1: lp_scalar_v<1>(field, a, nb, st); break;
+    case 2: lp_scalar_v<2>(field, a, nb, st); break;
+    case 3: lp_scalar_v<3>(field, a, nb, st); break;
+    default: lp_scalar_v<0>(field, a, nb, st);
+  }
+}
 static void persist_launch(const void* args, unsigned grid, cudaStream_t st) {
   if (grid) k_pool_persist<R, CCI, PBS, PMB><<<grid, PBS, 0, st>>>(*(const PersistArgs*)args);
 }
@@ -26,6 +75,6 @@ static int persist_blocks_per_sm() {
   return n;
 }
 
-const PersistOps SU2_PERSIST = {PBS, persist_launch, persist_blocks_per_sm};
+const PoolOps SU2_PERSIST = {PBS, persist_launch, persist_blocks_per_sm, lp_link, lp_u1, lp_scalar};
 
 }  // namespace su2

@@ -115,7 +115,7 @@ struct su2gpu_pool {
   // the persistent sweep (k_pool_persist): on by default; its work counter
   // and per-slot finished-tile counts, its resident grid, and the graph of
   // one launch of gexec_p_n sweeps
-  const PersistOps* pers = nullptr;
+  const PoolOps* pers = nullptr;
   bool persistent = true;
   Buf qstate;
   unsigned persist_grid = 0;
@@ -335,9 +335,9 @@ int enqueue_pool_sweep(su2gpu_pool* P, const void* descs, const int2* const* til
     a.parity = q.parity; a.sub = q.sub; a.alg = q.alg; a.pass = q.pass;
     a.tiles = tiles[v];
     mark(P, kind);
-    if (kind == 0) P->ops->pool_link(v, a, nt[v], P->st);
-    else if (kind == 1) P->ops->pool_u1(v, a, nt[v], P->st);
-    else P->ops->pool_scalar(v, kind - 2, a, nt[v], P->st);
+    if (kind == 0) P->pers->pool_link(v, a, nt[v], P->st);
+    else if (kind == 1) P->pers->pool_u1(v, a, nt[v], P->st);
+    else P->pers->pool_scalar(v, kind - 2, a, nt[v], P->st);
   }
   mark(P, -1);
   cudaError_t e = cudaGetLastError();
@@ -1389,9 +1389,9 @@ int su2gpu_pool_autotune(su2gpu_pool* P, int32_t* choices, float* best_ms) {
         a.pass = 60000 + r;
         a.tiles = (const int2*)P->tiles[v].p;
         cudaEventRecord(e0, P->st);
-        if (kind == 0) P->ops->pool_link(v, a, P->ntiles[v], P->st);
-        else if (kind == 1) P->ops->pool_u1(v, a, P->ntiles[v], P->st);
-        else P->ops->pool_scalar(v, kind - 2, a, P->ntiles[v], P->st);
+        if (kind == 0) P->pers->pool_link(v, a, P->ntiles[v], P->st);
+        else if (kind == 1) P->pers->pool_u1(v, a, P->ntiles[v], P->st);
+        else P->pers->pool_scalar(v, kind - 2, a, P->ntiles[v], P->st);
         cudaEventRecord(e1, P->st);
         PCK(cudaEventSynchronize(e1));
         float t = 0.f;

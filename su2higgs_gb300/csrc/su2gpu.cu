@@ -186,8 +186,8 @@ const Ops* su2::pick_ops(int prec, int content) {
   return &ops_f32_generic;
 }
 
-// the persistent sweep kernel of the same instantiation as pick_ops
-const PersistOps* su2::pick_persist(int prec, int content) {
+// the pool update kernels of the same instantiation as pick_ops
+const PoolOps* su2::pick_persist(int prec, int content) {
   int c = content & 0x1f;
   if (prec == 64) {
     if (c == C_H1) return &persist_f64_fund;
