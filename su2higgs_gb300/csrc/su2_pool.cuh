@@ -168,7 +168,8 @@ __global__ void __launch_bounds__(BS, MINB) k_pool_scalar(PoolArgs a) {
 // item always has its inputs.  The wait is bounded: after spin_limit polls
 // (or at once once another block has given up) the block records error bit
 // 4, skips the item's work (its fields stay as they were) and counts it as
-// finished, so the launch always ends, within about one wait.
+// finished; from then on every item is skipped, so the launch ends within
+// about one wait and no item runs on inputs of the wrong pass.
 // Fields are read with coherent loads (SU2_COHERENT_LOADS): later passes read
 // what earlier passes of the same launch wrote.
 // ---------------------------------------------------------------------------
@@ -275,6 +276,9 @@ __global__ void __launch_bounds__(BS, MINB) k_pool_persist(PersistArgs a) {
           __nanosleep(64);
         }
       }
+      // once any wait has given up, no item runs: the counts of skipped
+      // items would otherwise satisfy later dependencies out of order
+      if (*(volatile int*)a.err & 4) go = 0;
       s_go = go;
     }
     __syncthreads();
