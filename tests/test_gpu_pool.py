@@ -223,7 +223,12 @@ def test_pool_ensemble_async_api(gpu):
         pool.upload(s, **workloads.hot_fields(p, seed))
         slots.append(s)
     assert pool.info()["free_bytes"] == 0
+    # persistent mode (default): the work-list kernel + the sweep-counter
+    # increment per call; one launch per pass otherwise
+    assert pool.launches_per_sweep() == 2
+    pool.persistent = False
     assert pool.launches_per_sweep() == 6 + 10 + 1
+    pool.persistent = True
     stream = torch.cuda.Stream()
     sums = torch.zeros((64, abi.NMEAS), dtype=torch.float64, device="cuda")
     pool.set_stream(stream.cuda_stream)
