@@ -118,6 +118,12 @@ struct su2gpu_pool {
   const PoolOps* pers = nullptr;
   bool persistent = true;
   Buf qstate;
+  // its work items: segments of seg_tiles 128-site tiles of one chain, and
+  // the first segment of each active chain (+ the end)
+  int seg_tiles = 8;
+  Buf segs;
+  std::vector<int2> h_segs;
+  std::vector<int> h_sfirst;
   unsigned persist_grid = 0;
   cudaGraphExec_t gexec_p = nullptr;
   int gexec_p_n = 0;
@@ -234,6 +240,18 @@ int rebuild(su2gpu_pool* P, void* arena_base = nullptr, void* slot_base = nullpt
       if (int rc = P->tiles[v].ensure(std::max<size_t>(t.size(), 1) * sizeof(int2))) return rc;
       if (!t.empty()) PCK(cudaMemcpyAsync(P->tiles[v].p, t.data(), t.size() * sizeof(int2), cudaMemcpyHostToDevice, P->st));
     }
+    P->h_segs.clear();
+    P->h_sfirst.clear();
+    for (int s : P->active) {
+      P->h_sfirst.push_back((int)P->h_segs.size());
+      const int step = kVariantBS[0] * P->seg_tiles;
+      for (int t0 = 0; t0 < P->slots[s].g.half; t0 += step) P->h_segs.push_back(int2{s, t0});
+    }
+    P->h_sfirst.push_back((int)P->h_segs.size());
+    if (int rc = P->segs.ensure(std::max<size_t>(P->h_segs.size(), 1) * sizeof(int2))) return rc;
+    if (!P->h_segs.empty())
+      PCK(cudaMemcpyAsync(P->segs.p, P->h_segs.data(), P->h_segs.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                          P->st));
     std::vector<int2>& mt = P->h_mtiles;
     std::vector<int>& first = P->h_first;
     std::vector<uint32_t*>& sp = P->h_sweeps;
@@ -345,9 +363,9 @@ int enqueue_pool_sweep(su2gpu_pool* P, const void* descs, const int2* const* til
   return SU2GPU_OK;
 }
 
-// `nsweeps` sweeps of the chains of a range of the 128-site tile table
-// (variant 0) in one launch of the persistent kernel, then their sweep
-// counters + nsweeps.  first_item / spin_limit: see PersistArgs.
+// `nsweeps` sweeps of the chains of a range of the segment table in one
+// launch of the persistent kernel, then their sweep counters + nsweeps.
+// first_item / spin_limit: see PersistArgs.
 int enqueue_persist(su2gpu_pool* P, const int2* tiles, int nt, uint32_t* const* sweeps, int nchains, int nsweeps,
                     int64_t* tot, unsigned first_item = 0, int spin_limit = 1 << 18) {
   std::vector<PassDesc> passes;
@@ -365,6 +383,7 @@ int enqueue_persist(su2gpu_pool* P, const int2* tiles, int nt, uint32_t* const* 
   A.descs = P->descs.p;
   A.tiles = tiles;
   A.ntiles = nt;
+  A.seg = P->seg_tiles;
   A.nslots = P->max_slots;
   A.npasses = (int)passes.size();
   A.nsweeps = nsweeps;
@@ -417,6 +436,7 @@ int su2gpu_pool_create(const su2gpu_params* recipe, int64_t arena_bytes, int32_t
   P->ops = pick_ops(P->prec, P->content);
   P->pops = P->prec == 64 ? &precops_f64 : &precops_f32;
   P->pers = pick_persist(P->prec, P->content);
+  if (const char* e = getenv("SU2GPU_PERSIST_TILES")) P->seg_tiles = std::max(1, atoi(e));
   P->max_slots = max_chains;
   P->slots.resize(max_chains);
   int rc;
@@ -463,6 +483,7 @@ int su2gpu_pool_destroy(su2gpu_pool* P) {
   if (P->own_st) cudaStreamSynchronize(P->own_st);
   drop_graphs(P);
   P->qstate.release();
+  P->segs.release();
   P->arena.release(); P->slotmem.release(); P->descs.release(); P->mtiles.release(); P->mfirst.release();
   P->sweepptrs.release(); P->partials.release(); P->sums.release(); P->stage.release(); P->err.release();
   for (int v = 0; v < NVARIANTS; v++) P->tiles[v].release();
@@ -864,7 +885,7 @@ static int pool_enqueue(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
         PCK(cudaStreamSynchronize(exec));
         P->st = P->own_st;
         PCK(cudaStreamBeginCapture(P->st, cudaStreamCaptureModeThreadLocal));
-        rc = enqueue_persist(P, tiles[0], P->ntiles[0], sweeps, na, nsweeps, tot);
+        rc = enqueue_persist(P, (const int2*)P->segs.p, (int)P->h_segs.size(), sweeps, na, nsweeps, tot);
         cudaError_t e = cudaStreamEndCapture(P->st, &graph);
         P->st = exec;
         if (rc) return rc;
@@ -878,7 +899,8 @@ static int pool_enqueue(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
         sweep_recipe(P->recipe, passes, tot);
       }
       PCK(cudaGraphLaunch(P->gexec_p, P->st));
-    } else if ((rc = enqueue_persist(P, tiles[0], P->ntiles[0], sweeps, na, nsweeps, tot))) {
+    } else if ((rc = enqueue_persist(P, (const int2*)P->segs.p, (int)P->h_segs.size(), sweeps, na, nsweeps,
+                                     tot))) {
       return rc;
     }
   } else if (use_graph) {
@@ -940,8 +962,8 @@ int su2gpu_pool_run(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
 static int enqueue_group_sweep(su2gpu_pool* P, int a0, int a1, int n, int64_t* tot) {
   uint32_t* const* sweeps = (uint32_t* const*)P->sweepptrs.p + a0;
   if (P->persistent) {
-    const int2* t0 = (const int2*)P->tiles[0].p + P->h_tfirst[0][a0];
-    return enqueue_persist(P, t0, P->h_tfirst[0][a1] - P->h_tfirst[0][a0], sweeps, a1 - a0, n, tot);
+    const int2* sg = (const int2*)P->segs.p + P->h_sfirst[a0];
+    return enqueue_persist(P, sg, P->h_sfirst[a1] - P->h_sfirst[a0], sweeps, a1 - a0, n, tot);
   }
   const int2* tiles[NVARIANTS];
   int nt[NVARIANTS];
@@ -1219,8 +1241,8 @@ int su2gpu_pool_check_wait_timeout(su2gpu_pool* P, int32_t spin_limit, int32_t* 
   if (P->active.empty()) return fail(SU2GPU_ERR_INVALID, "the pool has no chains");
   PCK(cudaStreamSynchronize(P->st));
   int64_t tot[SU2GPU_NCOUNTERS] = {0};
-  const int nt = P->ntiles[0];
-  if ((rc = enqueue_persist(P, (const int2*)P->tiles[0].p, nt, (uint32_t* const*)P->sweepptrs.p,
+  const int nt = (int)P->h_segs.size();
+  if ((rc = enqueue_persist(P, (const int2*)P->segs.p, nt, (uint32_t* const*)P->sweepptrs.p,
                             (int)P->active.size(), 1, tot, (unsigned)nt, spin_limit)))
     return rc;
   PCK(cudaStreamSynchronize(P->st));

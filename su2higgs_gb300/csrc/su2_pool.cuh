@@ -156,11 +156,13 @@ __global__ void __launch_bounds__(BS, MINB) k_pool_scalar(PoolArgs a) {
 
 // ---------------------------------------------------------------------------
 // The persistent sweep: one launch runs `nsweeps` sweeps of every chain of
-// the tile table.  Its work list is (sweep, pass, tile) in that order; each
-// block takes the next item from an atomic counter until the list is done.
-// A tile of pass g of chain c needs pass g-1 of chain c finished, which a
-// per-chain count of finished tiles says (chain c has passed g-1 when the
-// count reaches g x its tiles; a tile of pass g cannot finish before that,
+// the segment table.  A segment is up to `seg` consecutive 128-site tiles of
+// one parity of one chain.  The work list is (sweep, pass, segment) in that
+// order; each block takes the next item from an atomic counter until the
+// list is done, and runs the segment's tiles one after the other.  A segment
+// of pass g of chain c needs pass g-1 of chain c finished, which a per-chain
+// count of finished segments says (chain c has passed g-1 when the count
+// reaches g x its segments; a segment of pass g cannot finish before that,
 // so the count is exact).  Chains do not wait for each other, so the passes
 // of different chains overlap and no pass drains the GPU before the next.
 // An item depends only on items earlier in the list, which blocks already
@@ -186,8 +188,9 @@ struct PassDesc {
 
 struct PersistArgs {
   const void* descs;   // ChainDesc<R>[nslots]
-  const int2* tiles;   // (slot, t0) of every tile of one parity of every chain, chain by chain
-  int ntiles, nslots;
+  const int2* tiles;   // (slot, t0) of every segment of one parity of every chain, chain by chain
+  int ntiles, nslots;  // ntiles: segments in the table
+  int seg;             // tiles per segment (the last segment of a chain may have fewer)
   int npasses, nsweeps;
   unsigned first_item;  // the work list starts here (0 in a sweep)
   int spin_limit;       // polls of a dependency before giving up
@@ -261,7 +264,7 @@ __global__ void __launch_bounds__(BS, MINB) k_pool_persist(PersistArgs a) {
     const ChainDesc<R>& d = stage_desc_slot<R>(a.descs, tile.x);
     if (threadIdx.x == 0) {
       const unsigned ntc = (unsigned)((d.g.half + BS - 1) / BS);
-      const unsigned need = g * ntc;
+      const unsigned need = g * ((ntc + (unsigned)a.seg - 1) / (unsigned)a.seg);
       int go = 1;
       if (need) {
         int polls = 0;
@@ -282,7 +285,12 @@ __global__ void __launch_bounds__(BS, MINB) k_pool_persist(PersistArgs a) {
       s_go = go;
     }
     __syncthreads();
-    if (s_go) persist_tile<R, CC, BS, MINB>(d, a.passes[k], *d.sweep + s, tile.y, a.err);
+    if (s_go) {
+      const PassDesc p = a.passes[k];
+      const uint32_t sweep = *d.sweep + s;
+      for (int j = 0, t0 = tile.y; j < a.seg && t0 < d.g.half; j++, t0 += BS)
+        persist_tile<R, CC, BS, MINB>(d, p, sweep, t0, a.err);
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
       __threadfence();
