@@ -389,15 +389,17 @@ int su2gpu_pool_cycle(su2gpu_pool* pool, int32_t n, const int32_t* slots, const 
 /* Set one chain's sweep counter (the random stream's sweep index). */
 int su2gpu_pool_set_sweep(su2gpu_pool* pool, int32_t slot, uint32_t sweep);
 /* `nsweeps` sweeps of every active chain; each chain's sweep counter
- * advances by one per sweep.  In the persistent mode (the default) the
- * sweeps are one launch of a persistent kernel that works through the list
- * of (sweep, pass, tile) items of all chains, each tile waiting only for its
- * own chain's previous pass; use_graph != 0 replays it from a graph
+ * advances by one per sweep.  In the persistent mode the sweeps are one
+ * launch of a persistent kernel that works through the list of (sweep,
+ * pass, segment of tiles) items of all chains, each item waiting only for
+ * its own chain's previous pass; use_graph != 0 replays it from a graph
  * captured for this number of sweeps.  Otherwise every pass is one launch
  * over all chains and use_graph != 0 replays one captured sweep.  Both modes
  * give the same fields bit for bit. */
 int su2gpu_pool_run(su2gpu_pool* pool, int32_t nsweeps, int32_t use_graph);
-/* Persistent mode on (default) or off (one launch per pass). */
+/* Persistent mode: 1 on, 0 off (one launch per pass), -1 automatic (the
+ * default: persistent from 8 chains on).  get: the mode in effect for the
+ * current chains (1 / 0). */
 int su2gpu_pool_set_persistent(su2gpu_pool* pool, int32_t on);
 int su2gpu_pool_get_persistent(su2gpu_pool* pool, int32_t* on);
 /* Check of the persistent kernel's bounded dependency wait: runs it on a

@@ -116,11 +116,12 @@ struct su2gpu_pool {
   // and per-slot finished-tile counts, its resident grid, and the graph of
   // one launch of gexec_p_n sweeps
   const PoolOps* pers = nullptr;
-  bool persistent = true;
+  int persist_mode = -1;    // 1 on, 0 off (one launch per pass), -1 automatic
+  bool persistent = false;  // the mode in effect for the current membership
   Buf qstate;
   // its work items: segments of seg_tiles 128-site tiles of one chain, and
   // the first segment of each active chain (+ the end)
-  int seg_tiles = 8;
+  int seg_tiles = 8, seg_env = 0;
   Buf segs;
   std::vector<int2> h_segs;
   std::vector<int> h_sfirst;
@@ -240,6 +241,16 @@ int rebuild(su2gpu_pool* P, void* arena_base = nullptr, void* slot_base = nullpt
       if (int rc = P->tiles[v].ensure(std::max<size_t>(t.size(), 1) * sizeof(int2))) return rc;
       if (!t.empty()) PCK(cudaMemcpyAsync(P->tiles[v].p, t.data(), t.size() * sizeof(int2), cudaMemcpyHostToDevice, P->st));
     }
+    // the persistent mode and its segment size: at least 4 work items per
+    // resident block in a pass, at most 8 tiles per item; automatic mode uses
+    // it from 8 chains on, where passes of different chains can overlap (the
+    // passes of a single chain follow one another in either mode, and the
+    // per-pass launches then have less overhead)
+    int64_t ntiles_all = 0;
+    for (int s : P->active) ntiles_all += (P->slots[s].g.half + kVariantBS[0] - 1) / kVariantBS[0];
+    P->seg_tiles = P->seg_env ? P->seg_env
+                              : (int)std::max<int64_t>(1, std::min<int64_t>(8, ntiles_all / (4 * (int64_t)std::max(1u, P->persist_grid))));
+    P->persistent = P->persist_mode == 1 || (P->persist_mode < 0 && P->active.size() >= 8);
     P->h_segs.clear();
     P->h_sfirst.clear();
     for (int s : P->active) {
@@ -436,7 +447,7 @@ int su2gpu_pool_create(const su2gpu_params* recipe, int64_t arena_bytes, int32_t
   P->ops = pick_ops(P->prec, P->content);
   P->pops = P->prec == 64 ? &precops_f64 : &precops_f32;
   P->pers = pick_persist(P->prec, P->content);
-  if (const char* e = getenv("SU2GPU_PERSIST_TILES")) P->seg_tiles = std::max(1, atoi(e));
+  if (const char* e = getenv("SU2GPU_PERSIST_TILES")) P->seg_env = std::max(1, atoi(e));
   P->max_slots = max_chains;
   P->slots.resize(max_chains);
   int rc;
@@ -957,11 +968,17 @@ int su2gpu_pool_run(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
 // pipelined cycle: upload, sweeps, measurement and download of the whole pool
 // with the host transfers of some groups of chains under the sweeps of others
 // ---------------------------------------------------------------------------
+// whether the sweeps of the group [a0, a1) run as one persistent launch: in
+// the persistent mode, for groups of 8 chains or more (or when forced)
+static bool group_persistent(const su2gpu_pool* P, int a0, int a1) {
+  return P->persistent && (P->persist_mode == 1 || a1 - a0 >= 8);
+}
+
 // `n` sweeps of the active chains [a0, a1): their tile ranges and sweep
 // counters (persistent: one launch; otherwise one launch per pass and sweep)
 static int enqueue_group_sweep(su2gpu_pool* P, int a0, int a1, int n, int64_t* tot) {
   uint32_t* const* sweeps = (uint32_t* const*)P->sweepptrs.p + a0;
-  if (P->persistent) {
+  if (group_persistent(P, a0, a1)) {
     const int2* sg = (const int2*)P->segs.p + P->h_sfirst[a0];
     return enqueue_persist(P, sg, P->h_sfirst[a1] - P->h_sfirst[a0], sweeps, a1 - a0, n, tot);
   }
@@ -1074,10 +1091,12 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
   const int G = (int)groups.size() - 1;
   std::vector<cudaGraphExec_t> gex(G, nullptr);
   // sweeps per graph replay: all of them in one persistent launch, else one
-  const int per_replay = P->persistent ? nsweeps : 1;
+  std::vector<int> per_replay(G, 1);
+  for (int g = 0; g < G; g++)
+    if (group_persistent(P, groups[g], groups[g + 1])) per_replay[g] = std::max(1, (int)nsweeps);
   if (use_graph && nsweeps > 0)
     for (int g = 0; g < G; g++)
-      if ((rc = group_graph(P, groups[g], groups[g + 1], per_replay, &gex[g]))) return rc;
+      if ((rc = group_graph(P, groups[g], groups[g + 1], per_replay[g], &gex[g]))) return rc;
   // staging bytes of every group; a group's chains sit side by side in the
   // rings (a ring holds the largest group at least), so a chain only ever
   // overlaps chains of earlier groups, whose release events are recorded
@@ -1150,7 +1169,7 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
     PCK(cudaStreamWaitEvent(P->st, ev[4 * g + 1], 0));
     if (nsweeps > 0) {
       if (use_graph) {
-        for (int k = 0; k < nsweeps; k += per_replay) PCK(cudaGraphLaunch(gex[g], P->st));
+        for (int k = 0; k < nsweeps; k += per_replay[g]) PCK(cudaGraphLaunch(gex[g], P->st));
       } else {
         int64_t t1[SU2GPU_NCOUNTERS] = {0};
         if ((rc = enqueue_group_sweep(P, a0, a1, nsweeps, t1))) return rc;
@@ -1218,13 +1237,16 @@ int su2gpu_pool_enqueue(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
 int su2gpu_pool_set_persistent(su2gpu_pool* P, int32_t on) {
   if (!P) return SU2GPU_ERR_INVALID;
   PCK(cudaStreamSynchronize(P->st));
-  P->persistent = on != 0;
+  P->persist_mode = on < 0 ? -1 : (on ? 1 : 0);
+  P->dirty = true;  // the mode in effect and the segments are set at the rebuild
   drop_graphs(P);
   return SU2GPU_OK;
 }
 
 int su2gpu_pool_get_persistent(su2gpu_pool* P, int32_t* on) {
   if (!P || !on) return SU2GPU_ERR_INVALID;
+  int rc;
+  if (P->dirty && (rc = rebuild(P))) return rc;
   *on = P->persistent ? 1 : 0;
   return SU2GPU_OK;
 }
@@ -1262,6 +1284,8 @@ int su2gpu_pool_set_stream(su2gpu_pool* P, void* stream) {
 
 int su2gpu_pool_launches_per_sweep(su2gpu_pool* P, int32_t* n) {
   if (!P || !n) return SU2GPU_ERR_INVALID;
+  int rc;
+  if (P->dirty && (rc = rebuild(P))) return rc;
   if (P->persistent) {
     *n = 2;
     return SU2GPU_OK;

@@ -590,15 +590,17 @@ class Pool:
 
     @property
     def persistent(self):
-        """Sweeps as one launch of the persistent work-list kernel (default)
-        rather than one launch per pass."""
+        """Whether the sweeps run as one launch of the persistent work-list
+        kernel rather than one launch per pass, for the current chains."""
         on = ctypes.c_int32()
         check(lib().su2gpu_pool_get_persistent(self._h, ctypes.byref(on)))
         return bool(on.value)
 
     @persistent.setter
     def persistent(self, on):
-        check(lib().su2gpu_pool_set_persistent(self._h, 1 if on else 0))
+        """True / False force the mode; None: automatic (the default,
+        persistent from 8 chains on)."""
+        check(lib().su2gpu_pool_set_persistent(self._h, -1 if on is None else (1 if on else 0)))
 
     def check_wait_timeout(self, spin_limit=2000):
         """Run the persistent kernel on a work list whose dependencies never

@@ -138,3 +138,21 @@ def test_persistent_launch_count(gpu):
     assert pool.launches_per_sweep() == 2
     pool.persistent = False
     assert pool.launches_per_sweep() == 6 + 10 + 1
+
+
+def test_persistent_automatic_mode(gpu):
+    """Automatic (default) mode: persistent from 8 chains on, one launch per
+    pass below; the results are the same either way."""
+    p = abi.make_params("adj", L=(8, 8, 8), precision=32)
+    pool = gpu.Pool(p, arena_bytes=64 << 20, max_chains=16)
+    slots = []
+    for k in range(8):
+        slots.append(pool.add(p, seed=k, chain=k))
+        pool.upload(slots[-1], **as_dict(hot_fields(p, seed=k)))
+        assert pool.persistent == (k >= 7)
+    pool.remove(slots.pop())
+    assert not pool.persistent
+    pool.persistent = True
+    assert pool.persistent
+    pool.persistent = None
+    assert not pool.persistent
