@@ -398,8 +398,9 @@ int su2gpu_pool_set_sweep(su2gpu_pool* pool, int32_t slot, uint32_t sweep);
  * give the same fields bit for bit. */
 int su2gpu_pool_run(su2gpu_pool* pool, int32_t nsweeps, int32_t use_graph);
 /* Persistent mode: 1 on, 0 off (one launch per pass), -1 automatic (the
- * default: persistent from 8 chains on).  get: the mode in effect for the
- * current chains (1 / 0). */
+ * default: persistent for 8 chains or more with at least 16 tiles of 128
+ * sites per resident block in a pass, where it is the faster mode).  get:
+ * the mode in effect for the current chains (1 / 0). */
 int su2gpu_pool_set_persistent(su2gpu_pool* pool, int32_t on);
 int su2gpu_pool_get_persistent(su2gpu_pool* pool, int32_t* on);
 /* Check of the persistent kernel's bounded dependency wait: runs it on a

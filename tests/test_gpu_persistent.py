@@ -141,18 +141,25 @@ def test_persistent_launch_count(gpu):
 
 
 def test_persistent_automatic_mode(gpu):
-    """Automatic (default) mode: persistent from 8 chains on, one launch per
-    pass below; the results are the same either way."""
+    """Automatic (default) mode: persistent for 8 chains or more with enough
+    tiles per pass (16 per resident block), one launch per pass otherwise."""
     p = abi.make_params("adj", L=(8, 8, 8), precision=32)
     pool = gpu.Pool(p, arena_bytes=64 << 20, max_chains=16)
     slots = []
     for k in range(8):
         slots.append(pool.add(p, seed=k, chain=k))
         pool.upload(slots[-1], **as_dict(hot_fields(p, seed=k)))
-        assert pool.persistent == (k >= 7)
-    pool.remove(slots.pop())
-    assert not pool.persistent
+    assert not pool.persistent  # 16 tiles per pass
     pool.persistent = True
     assert pool.persistent
     pool.persistent = None
     assert not pool.persistent
+    pool.close()
+    from su2higgs_gb300 import workloads
+    specs = workloads.batched_ensemble(384)
+    need = sum(gpu.Pool.chain_bytes(q) for q, _, _ in specs)
+    big = gpu.Pool(specs[0][0], arena_bytes=need, max_chains=384)
+    for q, seed, chain in specs:
+        big.add(q, seed=seed, chain=chain)
+    assert big.persistent  # the 384-chain ensemble: 43k tiles per pass
+    big.close()
