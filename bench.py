@@ -588,6 +588,31 @@ def roofline_of(kinds, ms, content, prec, sites, workload):
             "time_share": shares[top] / tot, "shares": {KIND_NAMES[k]: v / tot for k, v in shares.items()}}
 
 
+def persistent_roofline(kinds, launch_ms, S, content, prec, sites, workload, step_ms):
+    """The persistent sweep kernel (one launch of S sweeps): algorithmic
+    bytes of the S sweeps (every pass: REALS_PER_SITE of its kind x sites;
+    the passes of one sweep counted from a profiled per-pass sweep) over the
+    median launch time."""
+    rsize = 4 if prec == 32 else 8
+    kinds = np.asarray(kinds)
+    nsw = max(1, int(np.sum(kinds == 0)) // 6)  # profiled sweeps (6 link passes each)
+    per_sweep = sum(REALS_PER_SITE[content].get(int(k), 18) for k in kinds) / nsw * rsize * sites
+    alg_bytes = per_sweep * S
+    avg_ms = float(np.median(launch_ms))
+    achieved = alg_bytes / (avg_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = None
+    tr_path = os.path.join(ROOT, "profiles", f"traffic_{workload}.json")
+    if os.path.exists(tr_path):
+        with open(tr_path) as fh:
+            t = json.load(fh).get("pool_sweep_persistent_per_sweep")
+        traffic = None if t is None else t * S
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic, "kernel": "pool_sweep_persistent (k_pool_persist)", "peak_source": peak_kind,
+            "algorithmic_bytes_per_launch": alg_bytes, "sweeps_per_launch": S, "avg_launch_ms": avg_ms,
+            "launches_profiled": len(launch_ms), "time_share": min(1.0, avg_ms / step_ms)}
+
+
 def cpu_sample_chains(specs, budget_s=15.0):
     """The oracle's C restatement, one thread: one sweep + measure of chains
     of the ensemble, smallest side first, until about budget_s seconds."""
@@ -637,6 +662,8 @@ def run_gpu_batched(args):
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     nchains, S = BATCHED[args.workload]
+    if args.sweeps_per_step:
+        S = args.sweeps_per_step
     specs = workloads.batched_ensemble(nchains, seed=replica_seed(20261203, rank))
     sites = sum(p.sites() for p, _, _ in specs)
     arena = sum(gpu.Pool.chain_bytes(p) for p, _, _ in specs)
@@ -690,13 +717,36 @@ def run_gpu_batched(args):
     m_last = sums[1].cpu().numpy()
     assert np.all(np.isfinite(m_last)), "non-finite measurement"
 
+    persistent = pool.persistent
+    # the sweep kernels alone: S sweeps per launch (persistent mode: one
+    # launch of the work-list kernel), CUDA events on the pool's stream,
+    # inputs (660 MB) larger than L2 and the L2 flushed between launches
+    sweep_ms = []
+    with torch.cuda.stream(stream):
+        for k in range(6):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            pool.enqueue(S, graph=True)
+            b.record(stream)
+            flush.zero_()
+            sweep_ms.append((a, b))
+        torch.cuda.synchronize()
+    sweep_ms = [a.elapsed_time(b) for a, b in sweep_ms][1:]
     pool.set_stream(None)
+    pool.run(0)
     kinds_all, ms_all = [], []
     for k in range(3):
         kd, ms = pool.profile_sweep()
         kinds_all.append(kd)
         ms_all.append(ms)
-    roofline = roofline_of(np.concatenate(kinds_all), np.concatenate(ms_all), "adj", 32, sites, args.workload)
+    kinds_all, ms_all = np.concatenate(kinds_all), np.concatenate(ms_all)
+    per_pass = roofline_of(kinds_all, ms_all, "adj", 32, sites, args.workload)
+    if persistent:
+        roofline = persistent_roofline(kinds_all, sweep_ms, S, "adj", 32, sites, args.workload,
+                                       float(np.median(step_ms)))
+        roofline["per_pass_mode"] = per_pass
+    else:
+        roofline = per_pass
 
     # end to end through the pool's host-buffer C ABI: every chain's FP64
     # fields uploaded from page-locked memory, S sweeps, measurement,
@@ -791,11 +841,15 @@ def run_gpu_batched(args):
                                  "1 triplet Metropolis (x 2 parities) per sweep; measure every chain each step",
                        "l2": "fields 660 MB > L2; 256 MiB write between steps outside the step events",
                        "parallelism": f"replicas x{world}", "graph": True,
+                       "sweep_mode": "persistent work-list kernel, S sweeps per launch" if persistent
+                       else "one launch per pass",
                        "launch_variants": [int(v) for v in variants]},
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "fp64_plain": fp64,
             "sweep_roofline": sweep_roofline(value / world, "adj", 32),
-            # per step: S graph replays of the sweep's kernels + measure + per-chain reduction
-            "gpu_launches": int(K * (S * launches_sweep + 2)),
+            # per step: the sweeps (persistent: one work-list kernel + the
+            # sweep-counter increment; otherwise S graph replays of one
+            # launch per pass) + measure + per-chain reduction
+            "gpu_launches": int(K * ((launches_sweep if persistent else S * launches_sweep) + 2)),
             "clocks": clk, "wall_s_timed_region": t_wall,
             "step_ms_p50": float(np.percentile(step_ms, 50)), "step_ms_p99": float(np.percentile(step_ms, 99)),
         }
@@ -890,6 +944,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end host-buffer measurement")
+    ap.add_argument("--sweeps-per-step", type=int, default=None,
+                    help="batched: sweeps per step (default: the workload's 10; 1 for a profiler capture of one sweep)")
     ap.add_argument("--variants", default=None,
                     help="launch-shape variants of the 5 update kernel kinds, e.g. 0,0,0,0,0 (default: autotune)")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="served: arrivals per second")
