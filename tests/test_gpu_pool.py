@@ -223,12 +223,15 @@ def test_pool_ensemble_async_api(gpu):
         pool.upload(s, **workloads.hot_fields(p, seed))
         slots.append(s)
     assert pool.info()["free_bytes"] == 0
-    # persistent mode (default): the work-list kernel + the sweep-counter
-    # increment per call; one launch per pass otherwise
+    # persistent mode: the work-list kernel + the sweep-counter increment per
+    # call; one launch per pass otherwise (what the automatic mode picks for
+    # these 64 chains, 8k tiles per pass)
+    pool.persistent = True
     assert pool.launches_per_sweep() == 2
     pool.persistent = False
     assert pool.launches_per_sweep() == 6 + 10 + 1
-    pool.persistent = True
+    pool.persistent = None
+    assert pool.launches_per_sweep() == 6 + 10 + 1
     stream = torch.cuda.Stream()
     sums = torch.zeros((64, abi.NMEAS), dtype=torch.float64, device="cuda")
     pool.set_stream(stream.cuda_stream)
