@@ -973,10 +973,13 @@ int su2gpu_pool_run(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
 // pipelined cycle: upload, sweeps, measurement and download of the whole pool
 // with the host transfers of some groups of chains under the sweeps of others
 // ---------------------------------------------------------------------------
-// whether the sweeps of the group [a0, a1) run as one persistent launch: in
-// the persistent mode, for groups of 8 chains or more (or when forced)
+// whether the sweeps of the group [a0, a1) run as one persistent launch:
+// when forced, or in the automatic mode by the pool's rule applied to the
+// group alone (8 chains or more, 16 tiles or more per resident block)
 static bool group_persistent(const su2gpu_pool* P, int a0, int a1) {
-  return P->persistent && (P->persist_mode == 1 || a1 - a0 >= 8);
+  if (P->persist_mode != -1) return P->persist_mode == 1;
+  const int64_t tiles = P->h_tfirst[0][a1] - P->h_tfirst[0][a0];
+  return a1 - a0 >= 8 && tiles >= 16 * (int64_t)std::max(1u, P->persist_grid);
 }
 
 // `n` sweeps of the active chains [a0, a1): their tile ranges and sweep
