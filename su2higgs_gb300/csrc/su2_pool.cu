@@ -123,7 +123,7 @@ struct su2gpu_pool {
   // the first segment of each active chain (+ the end)
   int seg_tiles = 8, seg_env = 0;
   Buf segs;
-  std::vector<int2> h_segs;
+  std::vector<int4> h_segs;  // (slot, t0, the chain's segment count, 0)
   std::vector<int> h_sfirst;
   unsigned persist_grid = 0;
   cudaGraphExec_t gexec_p = nullptr;
@@ -261,12 +261,13 @@ int rebuild(su2gpu_pool* P, void* arena_base = nullptr, void* slot_base = nullpt
     for (int s : P->active) {
       P->h_sfirst.push_back((int)P->h_segs.size());
       const int step = kVariantBS[0] * P->seg_tiles;
-      for (int t0 = 0; t0 < P->slots[s].g.half; t0 += step) P->h_segs.push_back(int2{s, t0});
+      const int half = (int)P->slots[s].g.half, nseg = (half + step - 1) / step;
+      for (int t0 = 0; t0 < half; t0 += step) P->h_segs.push_back(int4{s, t0, nseg, 0});
     }
     P->h_sfirst.push_back((int)P->h_segs.size());
-    if (int rc = P->segs.ensure(std::max<size_t>(P->h_segs.size(), 1) * sizeof(int2))) return rc;
+    if (int rc = P->segs.ensure(std::max<size_t>(P->h_segs.size(), 1) * sizeof(int4))) return rc;
     if (!P->h_segs.empty())
-      PCK(cudaMemcpyAsync(P->segs.p, P->h_segs.data(), P->h_segs.size() * sizeof(int2), cudaMemcpyHostToDevice,
+      PCK(cudaMemcpyAsync(P->segs.p, P->h_segs.data(), P->h_segs.size() * sizeof(int4), cudaMemcpyHostToDevice,
                           P->st));
     std::vector<int2>& mt = P->h_mtiles;
     std::vector<int>& first = P->h_first;
@@ -382,7 +383,7 @@ int enqueue_pool_sweep(su2gpu_pool* P, const void* descs, const int2* const* til
 // `nsweeps` sweeps of the chains of a range of the segment table in one
 // launch of the persistent kernel, then their sweep counters + nsweeps.
 // first_item / spin_limit: see PersistArgs.
-int enqueue_persist(su2gpu_pool* P, const int2* tiles, int nt, uint32_t* const* sweeps, int nchains, int nsweeps,
+int enqueue_persist(su2gpu_pool* P, const int4* tiles, int nt, uint32_t* const* sweeps, int nchains, int nsweeps,
                     int64_t* tot, unsigned first_item = 0, int spin_limit = 1 << 18) {
   std::vector<PassDesc> passes;
   sweep_recipe(P->recipe, passes, tot);
@@ -901,7 +902,7 @@ static int pool_enqueue(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
         PCK(cudaStreamSynchronize(exec));
         P->st = P->own_st;
         PCK(cudaStreamBeginCapture(P->st, cudaStreamCaptureModeThreadLocal));
-        rc = enqueue_persist(P, (const int2*)P->segs.p, (int)P->h_segs.size(), sweeps, na, nsweeps, tot);
+        rc = enqueue_persist(P, (const int4*)P->segs.p, (int)P->h_segs.size(), sweeps, na, nsweeps, tot);
         cudaError_t e = cudaStreamEndCapture(P->st, &graph);
         P->st = exec;
         if (rc) return rc;
@@ -915,7 +916,7 @@ static int pool_enqueue(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
         sweep_recipe(P->recipe, passes, tot);
       }
       PCK(cudaGraphLaunch(P->gexec_p, P->st));
-    } else if ((rc = enqueue_persist(P, (const int2*)P->segs.p, (int)P->h_segs.size(), sweeps, na, nsweeps,
+    } else if ((rc = enqueue_persist(P, (const int4*)P->segs.p, (int)P->h_segs.size(), sweeps, na, nsweeps,
                                      tot))) {
       return rc;
     }
@@ -987,7 +988,7 @@ static bool group_persistent(const su2gpu_pool* P, int a0, int a1) {
 static int enqueue_group_sweep(su2gpu_pool* P, int a0, int a1, int n, int64_t* tot) {
   uint32_t* const* sweeps = (uint32_t* const*)P->sweepptrs.p + a0;
   if (group_persistent(P, a0, a1)) {
-    const int2* sg = (const int2*)P->segs.p + P->h_sfirst[a0];
+    const int4* sg = (const int4*)P->segs.p + P->h_sfirst[a0];
     return enqueue_persist(P, sg, P->h_sfirst[a1] - P->h_sfirst[a0], sweeps, a1 - a0, n, tot);
   }
   const int2* tiles[NVARIANTS];
@@ -1272,7 +1273,7 @@ int su2gpu_pool_check_wait_timeout(su2gpu_pool* P, int32_t spin_limit, int32_t* 
   PCK(cudaStreamSynchronize(P->st));
   int64_t tot[SU2GPU_NCOUNTERS] = {0};
   const int nt = (int)P->h_segs.size();
-  if ((rc = enqueue_persist(P, (const int2*)P->segs.p, nt, (uint32_t* const*)P->sweepptrs.p,
+  if ((rc = enqueue_persist(P, (const int4*)P->segs.p, nt, (uint32_t* const*)P->sweepptrs.p,
                             (int)P->active.size(), 1, tot, (unsigned)nt, spin_limit)))
     return rc;
   PCK(cudaStreamSynchronize(P->st));

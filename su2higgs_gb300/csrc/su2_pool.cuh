@@ -188,7 +188,8 @@ struct PassDesc {
 
 struct PersistArgs {
   const void* descs;   // ChainDesc<R>[nslots]
-  const int2* tiles;   // (slot, t0) of every segment of one parity of every chain, chain by chain
+  const int4* tiles;   // (slot, t0, the chain's segment count, 0) of every segment of one parity of
+                       // every chain, chain by chain
   int ntiles, nslots;  // ntiles: segments in the table
   int seg;             // tiles per segment (the last segment of a chain may have fewer)
   int npasses, nsweeps;
@@ -239,60 +240,74 @@ __device__ inline void persist_tile(const ChainDesc<R>& d, PassDesc p, uint32_t 
 template <typename R, int CC, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_pool_persist(PersistArgs a) {
   __shared__ unsigned s_item;
+  __shared__ int4 s_tile, s_next;
   __shared__ int s_go;
-  const unsigned total = (unsigned)a.ntiles * (unsigned)(a.npasses * a.nsweeps);
+  __shared__ __align__(16) unsigned char dbuf[sizeof(ChainDesc<R>)];
+  constexpr int NDESC = (int)(sizeof(ChainDesc<R>) / sizeof(uint4));
+  static_assert(sizeof(ChainDesc<R>) % sizeof(uint4) == 0, "descriptor must be a multiple of 16 bytes");
+  const unsigned nt = (unsigned)a.ntiles;
+  const unsigned total = nt * (unsigned)(a.npasses * a.nsweeps);
+  // thread 0 keeps the next item (and its table entry in s_next), fetched
+  // while the current item runs
   unsigned next = 0;
-  if (threadIdx.x == 0) next = atomicAdd(a.head, 1u) + a.first_item;
+  if (threadIdx.x == 0) {
+    next = atomicAdd(a.head, 1u) + a.first_item;
+    if (next < total) s_next = a.tiles[next % nt];
+  }
   for (;;) {
     if (threadIdx.x == 0) {
       s_item = next;
-      // the item after this one, fetched while this one runs
+      s_tile = s_next;
       if (next < total) next = atomicAdd(a.head, 1u) + a.first_item;
     }
     __syncthreads();
     const unsigned q = s_item;
     if (q >= total) break;
-    const unsigned g = q / (unsigned)a.ntiles;
-    const int2 tile = a.tiles[q - g * (unsigned)a.ntiles];
+    const int4 tile = s_tile;
+    const unsigned g = q / nt;
     const unsigned s = g / (unsigned)a.npasses, k = g - s * (unsigned)a.npasses;
     const bool bad = (unsigned)tile.x >= (unsigned)a.nslots || tile.y < 0;
-    if (bad) {
-      if (threadIdx.x == 0) atomicOr(a.err, 2);
-      __syncthreads();  // every thread has read s_item before it is reused
-      continue;         // a corrupted table: the item is dropped (dependants time out)
-    }
-    const ChainDesc<R>& d = stage_desc_slot<R>(a.descs, tile.x);
-    if (threadIdx.x == 0) {
-      const unsigned ntc = (unsigned)((d.g.half + BS - 1) / BS);
-      const unsigned need = g * ((ntc + (unsigned)a.seg - 1) / (unsigned)a.seg);
-      int go = 1;
-      if (need) {
-        int polls = 0;
-        while (ld_acquire_gpu(a.done + tile.x) < need) {
-          // give up after spin_limit polls, or at once when another block
-          // already gave up (the launch then ends within one wait)
-          if (++polls > a.spin_limit || (*(volatile int*)a.err & 4)) {
-            atomicOr(a.err, 4);
-            go = 0;
-            break;
+    if (!bad) {
+      // the chain's descriptor, copied by the block while thread 0 checks
+      // that the chain has finished pass g-1 (g x its segments done)
+      const uint4* src = (const uint4*)((const ChainDesc<R>*)a.descs + tile.x);
+      for (int i = threadIdx.x; i < NDESC; i += BS) ((uint4*)dbuf)[i] = src[i];
+      if (threadIdx.x == 0) {
+        const unsigned need = g * (unsigned)tile.z;
+        int go = 1;
+        if (need) {
+          int polls = 0;
+          while (ld_acquire_gpu(a.done + tile.x) < need) {
+            // give up after spin_limit polls, or at once when another block
+            // already gave up (the launch then ends within one wait)
+            if (++polls > a.spin_limit || (*(volatile int*)a.err & 4)) {
+              atomicOr(a.err, 4);
+              go = 0;
+              break;
+            }
+            __nanosleep(64);
           }
-          __nanosleep(64);
         }
+        // once any wait has given up, no item runs: the counts of skipped
+        // items would otherwise satisfy later dependencies out of order
+        if (*(volatile int*)a.err & 4) go = 0;
+        s_go = go;
       }
-      // once any wait has given up, no item runs: the counts of skipped
-      // items would otherwise satisfy later dependencies out of order
-      if (*(volatile int*)a.err & 4) go = 0;
-      s_go = go;
+    } else if (threadIdx.x == 0) {
+      atomicOr(a.err, 2);  // a corrupted table: the item is dropped (dependants time out)
+      s_go = 0;
     }
+    if (threadIdx.x == 0 && next < total) s_next = a.tiles[next % nt];
     __syncthreads();
     if (s_go) {
+      const ChainDesc<R>& d = *(const ChainDesc<R>*)dbuf;
       const PassDesc p = a.passes[k];
       const uint32_t sweep = *d.sweep + s;
       for (int j = 0, t0 = tile.y; j < a.seg && t0 < d.g.half; j++, t0 += BS)
         persist_tile<R, CC, BS, MINB>(d, p, sweep, t0, a.err);
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && !bad) {
       __threadfence();
       atomicAdd(a.done + tile.x, 1u);
     }
