@@ -6,10 +6,10 @@
 Default workload, batched384_adj_f32 -- the FP32 batched form: 384 independent
 SU(2) + adjoint Higgs chains (side L uniform over {8,12,16,24,32,48}, beta
 uniform in [6,12], m^2_adj scanning [-0.3,0.1], lambda_adj 0.005; 11.0 M sites
-in all) resident in one device pool.  A step is 10 sweeps of every chain (each
-sweep one CUDA-graph replay: 6 link heatbath + 10 triplet half-sweeps, every
-half-sweep one launch over all chains) followed by the measurement of every
-chain; the default 100 steps are the workload's 1000 sweeps per chain.
+in all) resident in one device pool.  A step is 10 sweeps of every chain (6
+link heatbath + 10 triplet half-sweeps each) as one graph-replayed launch of
+the persistent work-list kernel, followed by the measurement of every chain;
+the default 100 steps are the workload's 1000 sweeps per chain.
 Single-lattice workloads (fund128_f32 ...): a step is one sweep of SU(2) +
 fundamental Higgs plus its measurement.
 
@@ -24,8 +24,11 @@ e2e        the same metric through the host-buffer C ABI (FP64 AoS host
            the copy engines and the update kernels)
 fp64_plain the plain FP64 single-lattice sweep on the same lattices run one
            after another (the metric's comparison)
-roofline   the kernel kind with the largest share of profiled sweeps (CUDA
-           events around every pass on the launching stream)
+roofline   the dominant kernel: for a pool in the persistent mode the
+           work-list kernel (CUDA events on its stream around launches of
+           the step's sweeps), with the one-launch-per-pass profile beside
+           it; otherwise the kernel kind with the largest share of profiled
+           sweeps (CUDA events around every pass on the launching stream)
 cpu_baseline  the oracle's C restatement of the sweep, one thread, on a
            bounded sample of the same lattices
 
