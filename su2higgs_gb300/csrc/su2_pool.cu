@@ -204,6 +204,8 @@ ChainDesc<R> make_desc(su2gpu_pool* P, int s, char* arena_base, char* slot_base)
   return d;
 }
 
+void sweep_recipe(const su2gpu_params& p, std::vector<PassDesc>& out, int64_t* tot);
+
 // descriptors and tile tables for the current membership
 int rebuild(su2gpu_pool* P, void* arena_base = nullptr, void* slot_base = nullptr, void* descs = nullptr) {
   char* ab = (char*)(arena_base ? arena_base : P->arena.p);
@@ -255,7 +257,11 @@ int rebuild(su2gpu_pool* P, void* arena_base = nullptr, void* slot_base = nullpt
     const int64_t grid = std::max<int64_t>(1, P->persist_grid);
     const int seg_auto = (int)std::max<int64_t>(1, std::min<int64_t>(8, ntiles_all / (4 * grid)));
     P->seg_tiles = P->seg_env ? P->seg_env : seg_auto;
-    P->persistent = P->persist_mode == 1 || (P->persist_mode < 0 && P->active.size() >= 8 && seg_auto >= 4);
+    std::vector<PassDesc> rec;
+    int64_t counts[SU2GPU_NCOUNTERS] = {0};
+    sweep_recipe(P->recipe, rec, counts);
+    P->persistent = P->persist_mode == 1 || (P->persist_mode < 0 && P->active.size() >= 8 && seg_auto >= 4 &&
+                                             (int)rec.size() <= PERSIST_MAX_PASSES);
     P->h_segs.clear();
     P->h_sfirst.clear();
     for (int s : P->active) {
@@ -390,9 +396,6 @@ int enqueue_persist(su2gpu_pool* P, const int4* tiles, int nt, uint32_t* const* 
   if ((int)passes.size() > PERSIST_MAX_PASSES)
     return fail(SU2GPU_ERR_INVALID, "%d passes per sweep: the persistent sweep takes at most %d", (int)passes.size(),
                 PERSIST_MAX_PASSES);
-  const double items = (double)nt * (double)passes.size() * (double)nsweeps;
-  if (items >= 4.0e9) return fail(SU2GPU_ERR_INVALID, "%d sweeps of %d tiles: too many work items for one launch",
-                                  nsweeps, nt);
   if (kVariantBS[0] != P->pers->threads) return fail(SU2GPU_ERR_INVALID, "persistent sweep: tile size mismatch");
   if (!P->persist_grid) return fail(SU2GPU_ERR_CUDA, "persistent sweep: no resident blocks per SM");
   PersistArgs A;
@@ -403,19 +406,26 @@ int enqueue_persist(su2gpu_pool* P, const int4* tiles, int nt, uint32_t* const* 
   A.seg = P->seg_tiles;
   A.nslots = P->max_slots;
   A.npasses = (int)passes.size();
-  A.nsweeps = nsweeps;
   A.first_item = first_item;
   A.spin_limit = spin_limit;
   A.head = (unsigned*)P->qstate.p;
   A.done = (unsigned*)P->qstate.p + 1;
   A.err = (int*)P->err.p;
   for (size_t k = 0; k < passes.size(); k++) A.passes[k] = passes[k];
-  PCK(cudaMemsetAsync(P->qstate.p, 0, ((size_t)P->max_slots + 1) * sizeof(unsigned), P->st));
-  unsigned grid = (unsigned)std::min<double>((double)P->persist_grid, items);
-  P->pers->launch(&A, grid, P->st);
-  PCK(cudaGetLastError());
-  if (nsweeps > 0 && first_item == 0) launch_pool_next_sweep(sweeps, nchains, P->st, (uint32_t)nsweeps);
-  PCK(cudaGetLastError());
+  // the work counter is 32 bits: at most 2^31 items per launch, more sweeps
+  // in several launches (each after the previous one's counter increment)
+  const int64_t per_sweep = (int64_t)nt * (int64_t)passes.size();
+  const int chunk = (int)std::max<int64_t>(1, std::min<int64_t>(nsweeps, (1LL << 31) / std::max<int64_t>(1, per_sweep)));
+  for (int s0 = 0; s0 < std::max(nsweeps, 1); s0 += chunk) {
+    const int n = std::min(chunk, std::max(nsweeps - s0, 1));
+    A.nsweeps = nsweeps > 0 ? n : 0;
+    PCK(cudaMemsetAsync(P->qstate.p, 0, P->qstate.n, P->st));
+    const unsigned grid = (unsigned)std::min<int64_t>(P->persist_grid, per_sweep * std::max(n, 1));
+    P->pers->launch(&A, grid, P->st);
+    PCK(cudaGetLastError());
+    if (nsweeps > 0 && first_item == 0) launch_pool_next_sweep(sweeps, nchains, P->st, (uint32_t)n);
+    PCK(cudaGetLastError());
+  }
   return SU2GPU_OK;
 }
 
