@@ -490,8 +490,9 @@ int su2gpu_pool_create(const su2gpu_params* recipe, int64_t arena_bytes, int32_t
   }
   P->free_list.push_back({0, (size_t)arena_bytes});
   {
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     P->persist_grid = (unsigned)std::max(0, sms * P->pers->blocks_per_sm());
   }
   cudaMemsetAsync(P->slotmem.p, 0, P->slotmem.n, P->st);
