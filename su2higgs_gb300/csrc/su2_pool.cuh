@@ -1,9 +1,11 @@
-// su2_pool.cuh -- kernels of a pool of independent chains (the batched form):
-// one launch per half-sweep covers every chain of the pool.  Block b works on
-// the tile (slot, t0) of its block table; the chain's descriptor (field
-// pointers, geometry, couplings, random key, sweep counter, counters) is staged
-// in shared memory once per block and the per-site update is the same device
-// code as the single-chain kernels.  Chains may differ in lattice size and
+// su2_pool.cuh -- kernels of a pool of independent chains (the batched form).
+// Two ways to sweep: one launch per half-sweep covering every chain (block b
+// works on the tile (slot, t0) of its block table), or the persistent
+// work-list kernel k_pool_persist running whole sweeps of every chain in one
+// launch.  Either way a block stages its chain's descriptor (field pointers,
+// geometry, couplings, random key, sweep counter, counters) in shared memory
+// and runs the same per-tile functions, whose per-site update is the device
+// code of the single-chain kernels.  Chains may differ in lattice size and
 // couplings; they share field content, precision and update recipe.
 #pragma once
 
