@@ -846,6 +846,7 @@ def run_gpu_batched(args):
                        "parallelism": f"replicas x{world}", "graph": True,
                        "sweep_mode": "persistent work-list kernel, S sweeps per launch" if persistent
                        else "one launch per pass",
+                       "persist_tiles_per_item": pool.persist_tiles if persistent else None,
                        "launch_variants": [int(v) for v in variants]},
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "fp64_plain": fp64,
             "sweep_roofline": sweep_roofline(value / world, "adj", 32),

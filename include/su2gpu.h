@@ -403,6 +403,10 @@ int su2gpu_pool_run(su2gpu_pool* pool, int32_t nsweeps, int32_t use_graph);
  * the mode in effect for the current chains (1 / 0). */
 int su2gpu_pool_set_persistent(su2gpu_pool* pool, int32_t on);
 int su2gpu_pool_get_persistent(su2gpu_pool* pool, int32_t* on);
+/* Tiles of 128 sites per work item of the persistent sweep: chosen from the
+ * tiles per pass, or timed by su2gpu_pool_autotune (4, 6, 8, 12 or 16) when
+ * the pool sweeps persistently. */
+int su2gpu_pool_get_persist_tiles(su2gpu_pool* pool, int32_t* tiles);
 /* Check of the persistent kernel's bounded dependency wait: runs it on a
  * work list whose dependencies are never met (pass 0 left out), so every
  * wait gives up after spin_limit polls; the chains' fields and sweep
@@ -431,7 +435,9 @@ int su2gpu_pool_profile_sweep(su2gpu_pool* pool, int32_t max_passes, int32_t* ki
 /* One chain's counters (SU2GPU_NCOUNTERS, as su2gpu_get_counters). */
 int su2gpu_pool_counters(su2gpu_pool* pool, int32_t slot, int64_t* out);
 /* Launch-shape autotuner over the pool's current chains (as su2gpu_autotune;
- * runs on a scratch copy, the chains do not advance). */
+ * runs on a scratch copy, the chains do not advance).  In the persistent
+ * mode it also times the persistent sweep's work-item sizes and keeps the
+ * fastest (su2gpu_pool_get_persist_tiles). */
 int su2gpu_pool_autotune(su2gpu_pool* pool, int32_t* choices, float* best_ms);
 int su2gpu_pool_set_variants(su2gpu_pool* pool, const int32_t* choices);
 /* Copy one chain out of the pool into a new single-lattice context (same

@@ -121,7 +121,7 @@ struct su2gpu_pool {
   Buf qstate;
   // its work items: segments of seg_tiles 128-site tiles of one chain, and
   // the first segment of each active chain (+ the end)
-  int seg_tiles = 8, seg_env = 0;
+  int seg_tiles = 8, seg_env = 0, seg_tuned = 0;  // seg_tuned: the autotuner's pick (0: none)
   Buf segs;
   std::vector<int4> h_segs;  // (slot, t0, the chain's segment count, 0)
   std::vector<int> h_sfirst;
@@ -206,6 +206,14 @@ ChainDesc<R> make_desc(su2gpu_pool* P, int s, char* arena_base, char* slot_base)
 
 void sweep_recipe(const su2gpu_params& p, std::vector<PassDesc>& out, int64_t* tot);
 
+// the work-list segments of slot s: (slot, t0, the chain's segment count, 0)
+// for every `seg` tiles of 128 sites of one parity
+void append_segments(const su2gpu_pool* P, int s, int seg, std::vector<int4>& out) {
+  const int step = kVariantBS[0] * seg;
+  const int half = (int)P->slots[s].g.half, nseg = (half + step - 1) / step;
+  for (int t0 = 0; t0 < half; t0 += step) out.push_back(int4{s, t0, nseg, 0});
+}
+
 // descriptors and tile tables for the current membership
 int rebuild(su2gpu_pool* P, void* arena_base = nullptr, void* slot_base = nullptr, void* descs = nullptr) {
   char* ab = (char*)(arena_base ? arena_base : P->arena.p);
@@ -256,7 +264,7 @@ int rebuild(su2gpu_pool* P, void* arena_base = nullptr, void* slot_base = nullpt
     for (int s : P->active) ntiles_all += (P->slots[s].g.half + kVariantBS[0] - 1) / kVariantBS[0];
     const int64_t grid = std::max<int64_t>(1, P->persist_grid);
     const int seg_auto = (int)std::max<int64_t>(1, std::min<int64_t>(8, ntiles_all / (4 * grid)));
-    P->seg_tiles = P->seg_env ? P->seg_env : seg_auto;
+    P->seg_tiles = P->seg_env ? P->seg_env : (P->seg_tuned ? P->seg_tuned : seg_auto);
     std::vector<PassDesc> rec;
     int64_t counts[SU2GPU_NCOUNTERS] = {0};
     sweep_recipe(P->recipe, rec, counts);
@@ -266,9 +274,7 @@ int rebuild(su2gpu_pool* P, void* arena_base = nullptr, void* slot_base = nullpt
     P->h_sfirst.clear();
     for (int s : P->active) {
       P->h_sfirst.push_back((int)P->h_segs.size());
-      const int step = kVariantBS[0] * P->seg_tiles;
-      const int half = (int)P->slots[s].g.half, nseg = (half + step - 1) / step;
-      for (int t0 = 0; t0 < half; t0 += step) P->h_segs.push_back(int4{s, t0, nseg, 0});
+      append_segments(P, s, P->seg_tiles, P->h_segs);
     }
     P->h_sfirst.push_back((int)P->h_segs.size());
     if (int rc = P->segs.ensure(std::max<size_t>(P->h_segs.size(), 1) * sizeof(int4))) return rc;
@@ -390,7 +396,8 @@ int enqueue_pool_sweep(su2gpu_pool* P, const void* descs, const int2* const* til
 // launch of the persistent kernel, then their sweep counters + nsweeps.
 // first_item / spin_limit: see PersistArgs.
 int enqueue_persist(su2gpu_pool* P, const int4* tiles, int nt, uint32_t* const* sweeps, int nchains, int nsweeps,
-                    int64_t* tot, unsigned first_item = 0, int spin_limit = 1 << 18) {
+                    int64_t* tot, unsigned first_item = 0, int spin_limit = 1 << 18, const void* descs = nullptr,
+                    int seg = 0) {
   std::vector<PassDesc> passes;
   sweep_recipe(P->recipe, passes, tot);
   if ((int)passes.size() > PERSIST_MAX_PASSES)
@@ -400,10 +407,10 @@ int enqueue_persist(su2gpu_pool* P, const int4* tiles, int nt, uint32_t* const* 
   if (!P->persist_grid) return fail(SU2GPU_ERR_CUDA, "persistent sweep: no resident blocks per SM");
   PersistArgs A;
   memset(&A, 0, sizeof(A));
-  A.descs = P->descs.p;
+  A.descs = descs ? descs : P->descs.p;
   A.tiles = tiles;
   A.ntiles = nt;
-  A.seg = P->seg_tiles;
+  A.seg = seg ? seg : P->seg_tiles;
   A.nslots = P->max_slots;
   A.npasses = (int)passes.size();
   A.first_item = first_item;
@@ -423,7 +430,7 @@ int enqueue_persist(su2gpu_pool* P, const int4* tiles, int nt, uint32_t* const* 
     const unsigned grid = (unsigned)std::min<int64_t>(P->persist_grid, per_sweep * std::max(n, 1));
     P->pers->launch(&A, grid, P->st);
     PCK(cudaGetLastError());
-    if (nsweeps > 0 && first_item == 0) launch_pool_next_sweep(sweeps, nchains, P->st, (uint32_t)n);
+    if (nsweeps > 0 && first_item == 0 && sweeps) launch_pool_next_sweep(sweeps, nchains, P->st, (uint32_t)n);
     PCK(cudaGetLastError());
   }
   return SU2GPU_OK;
@@ -1263,6 +1270,14 @@ int su2gpu_pool_set_persistent(su2gpu_pool* P, int32_t on) {
   return SU2GPU_OK;
 }
 
+int su2gpu_pool_get_persist_tiles(su2gpu_pool* P, int32_t* tiles) {
+  if (!P || !tiles) return SU2GPU_ERR_INVALID;
+  int rc;
+  if (P->dirty && (rc = rebuild(P))) return rc;
+  *tiles = P->seg_tiles;
+  return SU2GPU_OK;
+}
+
 int su2gpu_pool_get_persistent(su2gpu_pool* P, int32_t* on) {
   if (!P || !on) return SU2GPU_ERR_INVALID;
   int rc;
@@ -1469,8 +1484,48 @@ int su2gpu_pool_autotune(su2gpu_pool* P, int32_t* choices, float* best_ms) {
     P->var[kind] = bestv;
     if (best_ms) best_ms[kind] = best / reps;
   }
+  // the persistent sweep's work-item size (tiles per segment), when the pool
+  // sweeps persistently: one sweep of every chain per candidate, timed on
+  // the scratch copy, the fastest kept (unless SU2GPU_PERSIST_TILES fixes it)
+  if (P->persistent && !P->seg_env) {
+    int64_t ntiles_all = 0;
+    for (int s : P->active) ntiles_all += (P->slots[s].g.half + kVariantBS[0] - 1) / kVariantBS[0];
+    const int cand[5] = {4, 6, 8, 12, 16};
+    float best = 1e30f;
+    int bestseg = P->seg_tiles;
+    Buf segbuf;
+    std::vector<int4> tab;
+    for (int seg : cand) {
+      if (ntiles_all / seg < (int64_t)P->persist_grid) continue;  // at least one item per resident block and pass
+      tab.clear();
+      for (int s : P->active) append_segments(P, s, seg, tab);
+      if ((rc = segbuf.ensure(tab.size() * sizeof(int4)))) break;
+      PCK(cudaMemcpyAsync(segbuf.p, tab.data(), tab.size() * sizeof(int4), cudaMemcpyHostToDevice, P->st));
+      float ms = 0.f;
+      for (int r = -1; r < reps; r++) {
+        int64_t t1[SU2GPU_NCOUNTERS] = {0};
+        cudaEventRecord(e0, P->st);
+        rc = enqueue_persist(P, (const int4*)segbuf.p, (int)tab.size(), nullptr, (int)P->active.size(), 1, t1, 0,
+                             1 << 18, desc2.p, seg);
+        cudaEventRecord(e1, P->st);
+        if (rc) break;
+        PCK(cudaEventSynchronize(e1));
+        float t = 0.f;
+        cudaEventElapsedTime(&t, e0, e1);
+        if (r >= 0) ms += t;
+      }
+      if (rc) break;
+      if (ms < best) { best = ms; bestseg = seg; }
+    }
+    segbuf.release();
+    if (!rc) {
+      P->seg_tuned = bestseg;
+      P->dirty = true;  // the segment table is rebuilt with the pick
+    }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (rc) return rc;
   PCK(cudaStreamSynchronize(P->st));
   arena2.release(); slot2.release(); desc2.release();
   drop_graphs(P);

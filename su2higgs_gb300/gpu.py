@@ -103,6 +103,7 @@ def lib():
         L.su2gpu_pool_cycle.argtypes = [vp, i32, vp, vp, i32, i32, vp, vp]
         L.su2gpu_pool_enqueue.argtypes = [vp, i32, i32]
         L.su2gpu_pool_set_persistent.argtypes = [vp, i32]
+        L.su2gpu_pool_get_persist_tiles.argtypes = [vp, ctypes.POINTER(i32)]
         L.su2gpu_pool_get_persistent.argtypes = [vp, ctypes.POINTER(i32)]
         L.su2gpu_pool_check_wait_timeout.argtypes = [vp, i32, ctypes.POINTER(i32)]
         L.su2gpu_pool_enqueue_measure.argtypes = [vp, vp, i32, ctypes.POINTER(i32)]
@@ -601,6 +602,13 @@ class Pool:
         """True / False force the mode; None: automatic (the default,
         persistent from 8 chains on)."""
         check(lib().su2gpu_pool_set_persistent(self._h, -1 if on is None else (1 if on else 0)))
+
+    @property
+    def persist_tiles(self):
+        """Tiles of 128 sites per work item of the persistent sweep."""
+        n = ctypes.c_int32()
+        check(lib().su2gpu_pool_get_persist_tiles(self._h, ctypes.byref(n)))
+        return n.value
 
     def check_wait_timeout(self, spin_limit=2000):
         """Run the persistent kernel on a work list whose dependencies never

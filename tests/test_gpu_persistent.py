@@ -163,3 +163,37 @@ def test_persistent_automatic_mode(gpu):
         big.add(q, seed=seed, chain=chain)
     assert big.persistent  # the 384-chain ensemble: 43k tiles per pass
     big.close()
+
+
+def test_autotuner_picks_the_persistent_item_size(gpu):
+    """On the 384-chain ensemble the autotuner times the persistent sweep's
+    work-item sizes on a scratch copy (the chains do not advance) and keeps
+    one of them; sweeps with the pick equal one-launch-per-pass sweeps."""
+    from su2higgs_gb300 import workloads
+    specs = workloads.batched_ensemble(384)
+    need = sum(gpu.Pool.chain_bytes(q) for q, _, _ in specs)
+    pools = []
+    for persistent in (None, False):
+        pool = gpu.Pool(specs[0][0], arena_bytes=need, max_chains=384)
+        for q, seed, chain in specs:
+            s = pool.add(q, seed=seed, chain=chain)
+            if chain % 97 == 0:
+                pool.upload(s, **workloads.hot_fields(q, seed))
+        pool.persistent = persistent
+        pools.append(pool)
+    a, b = pools
+    assert a.persistent and not b.persistent
+    before = a.download(0)
+    a.autotune()
+    assert a.persist_tiles in (4, 6, 8, 12, 16)
+    for n in before:
+        if before[n] is not None:
+            assert np.array_equal(a.download(0)[n], before[n]), n
+    a.run(2)
+    b.run(2)
+    for s in (0, 97, 194, 291):
+        fa, fb = a.download(s), b.download(s)
+        for n in fa:
+            if fa[n] is not None:
+                assert np.array_equal(fa[n], fb[n]), (s, n)
+        assert np.array_equal(a.counters(s), b.counters(s)), s
