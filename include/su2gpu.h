@@ -166,6 +166,40 @@ int64_t su2gpu_footprint_bytes(const su2gpu_params* p);
  * order and copied back. */
 int su2gpu_layout_tables(su2gpu_ctx* ctx, int64_t* next, int64_t* prev, int64_t* coords, int32_t* parity);
 
+/* Per-site values of the deterministic parts of the sweep on the context's
+ * current fields (plain FP64 contexts only), computed by the same device
+ * functions the update kernels call, for checking them site by site against
+ * the reference; the fields are left unchanged.  `out` holds V rows in layout
+ * order, of the width given for each `what`:
+ *   SU2GPU_SITE_LINK_STAPLE      [3][4] su2link_staple, staples.c:134-193
+ *   SU2GPU_SITE_WILSON_STAPLE    [3][4] su2staple_wilson, staples.c:84-115
+ *   SU2GPU_SITE_LOCALACT_SU2LINK [3]    localact_su2link, su2u1.c:166-198
+ *   SU2GPU_SITE_LOCALACT_U1LINK  [3]    localact_u1link, su2u1.c:336-354
+ *   SU2GPU_SITE_STAPLE_DOUBLET   [4]    staple_doublet (doublet 0), staples.c:243-302
+ *   SU2GPU_SITE_LOCALACT_DOUBLET [1]    localact_doublet (doublet 0), su2u1.c:495-510
+ *   SU2GPU_SITE_LOCALACT_SINGLET [1]    localact_singlet, su2u1.c:688-705
+ *   SU2GPU_SITE_OR_DOUBLET       [4]    the overrelaxation proposal of doublet 0
+ *                                       (the value an accepted overrelax_doublet,
+ *                                       overrelax.c:54-128, or overrelax_higgs2,
+ *                                       295-417, writes)
+ *   SU2GPU_SITE_OR_DOUBLET1      [4]    the same for doublet 1 (two doublets)
+ *   SU2GPU_SITE_OR_TRIPLET       [3]    overrelax_triplet's, overrelax.c:137-236
+ *   SU2GPU_SITE_OR_SINGLET       [1]    overrelax_singlet's, overrelax.c:243-285
+ * SU2GPU_ERR_INVALID for a field the content lacks, SU2GPU_ERR_UNSUPPORTED
+ * for an FP32 context. */
+#define SU2GPU_SITE_LINK_STAPLE 1
+#define SU2GPU_SITE_WILSON_STAPLE 2
+#define SU2GPU_SITE_LOCALACT_SU2LINK 3
+#define SU2GPU_SITE_LOCALACT_U1LINK 4
+#define SU2GPU_SITE_STAPLE_DOUBLET 5
+#define SU2GPU_SITE_LOCALACT_DOUBLET 6
+#define SU2GPU_SITE_LOCALACT_SINGLET 7
+#define SU2GPU_SITE_OR_DOUBLET 8
+#define SU2GPU_SITE_OR_DOUBLET1 9
+#define SU2GPU_SITE_OR_TRIPLET 10
+#define SU2GPU_SITE_OR_SINGLET 11
+int su2gpu_site_values(su2gpu_ctx* ctx, int32_t what, double* out);
+
 /* Field transfer (FP64 AoS host arrays in layout order; NULL for absent
  * fields).  link: V*dim*4, u1: V*dim, doublet: V*4, triplet: V*3, singlet: V.
  * Page-locked arrays (su2gpu_host_register) are converted by the device in
@@ -400,7 +434,9 @@ int su2gpu_pool_run(su2gpu_pool* pool, int32_t nsweeps, int32_t use_graph);
 /* Persistent mode: 1 on, 0 off (one launch per pass), -1 automatic (the
  * default: persistent for 8 chains or more with at least 16 tiles of 128
  * sites per resident block in a pass, where it is the faster mode).  get:
- * the mode in effect for the current chains (1 / 0). */
+ * the mode in effect for the current chains (1 / 0).  A recipe of more than
+ * 64 passes per sweep always sweeps one launch per pass: setting 1 for it
+ * returns SU2GPU_ERR_INVALID. */
 int su2gpu_pool_set_persistent(su2gpu_pool* pool, int32_t on);
 int su2gpu_pool_get_persistent(su2gpu_pool* pool, int32_t* on);
 /* Tiles of 128 sites per work item of the persistent sweep: chosen from the
@@ -413,6 +449,14 @@ int su2gpu_pool_get_persist_tiles(su2gpu_pool* pool, int32_t* tiles);
  * counters are untouched.  *flags receives the kernel's error flags (bit 4:
  * a wait timed out), which are then cleared. */
 int su2gpu_pool_check_wait_timeout(su2gpu_pool* pool, int32_t spin_limit, int32_t* flags);
+/* Test hook: sets `flags` in the pool's device error word from the host, as
+ * a kernel that found a bad state would (1 NaN fields, 2 bad tile, 4 a
+ * dependency wait of the persistent sweep timed out).  The next call that
+ * checks the word (su2gpu_pool_run, _cycle, _measure, ...) returns
+ * SU2GPU_ERR_KERNEL and clears it; the call after that runs normally.  A
+ * call that returned SU2GPU_ERR_KERNEL leaves its chains partly swept (the
+ * passes that completed are in their fields, their sweep counters advanced). */
+int su2gpu_pool_raise_error(su2gpu_pool* pool, int32_t flags);
 /* measure() sums of every active chain, in slot order:
  * sums[k * SU2GPU_NMEAS + m] for the k-th active chain. */
 int su2gpu_pool_measure(su2gpu_pool* pool, double* sums, int32_t max_chains, int32_t* nchains);

@@ -42,7 +42,8 @@ static long last_key = -1;
 static int cur_check = 0;
 
 /* ---------------- RNG replacement for generic/mersenne.c ---------------- */
-double genrand64_real2(void) { return orc_stream_uniform(&S); }
+static int zero_uniforms = 0; /* ref_or_proposal: every uniform 0 */
+double genrand64_real2(void) { return zero_uniforms ? 0.0 : orc_stream_uniform(&S); }
 unsigned long long genrand64_int64(void) {
   /* only used by shuffle() for random sweep orders, which the harness never enables */
   double u = orc_stream_uniform(&S);
@@ -373,6 +374,59 @@ int ref_site_update(int kind, long i, int sub, unsigned int pass) {
   }
 }
 int ref_site_draws(void) { return (int)S.draw; }
+
+/* The overrelaxation proposal at site i: the value the reference's update
+ * writes when it accepts.  The update runs with every uniform 0, which it
+ * always accepts (|dV/dV'| >= 0, overrelax.c:116-125); the site's old value
+ * is put back afterwards.  kind 4: doublet `sub` (4 reals), 6: triplet (3),
+ * 8: singlet (1).  Returns the number of reals written to out, -1 if the
+ * kind is absent in this build. */
+int ref_or_proposal(int kind, long i, int sub, double* out) {
+  int n = -1;
+  zero_uniforms = 1;
+  switch (kind) {
+#if (NHIGGS > 0)
+    case 4: {
+      double old[4];
+      memcpy(old, F.su2doublet[sub][i], sizeof(old));
+#if (NHIGGS == 1)
+      __real_overrelax_doublet(&L, &F, &P, i);
+#else
+      __real_overrelax_higgs2(&L, &F, &P, i, sub);
+#endif
+      memcpy(out, F.su2doublet[sub][i], sizeof(old));
+      memcpy(F.su2doublet[sub][i], old, sizeof(old));
+      n = 4;
+      break;
+    }
+#endif
+#ifdef TRIPLET
+    case 6: {
+      double old[3];
+      memcpy(old, F.su2triplet[i], sizeof(old));
+      __real_overrelax_triplet(&L, &F, &P, i);
+      memcpy(out, F.su2triplet[i], sizeof(old));
+      memcpy(F.su2triplet[i], old, sizeof(old));
+      n = 3;
+      break;
+    }
+#endif
+#ifdef SINGLET
+    case 8: {
+      double old = F.singlet[i][0];
+      __real_overrelax_singlet(&L, &F, &P, i);
+      out[0] = F.singlet[i][0];
+      F.singlet[i][0] = old;
+      n = 1;
+      break;
+    }
+#endif
+    default: break;
+  }
+  zero_uniforms = 0;
+  (void)out; (void)sub;
+  return n;
+}
 
 /* ---- multicanonical ---- */
 /* main.c:212-221: load_weight, backups, order parameter of both parities */

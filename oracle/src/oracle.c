@@ -42,6 +42,7 @@ struct orc_ctx {
   uint32_t sweep, chain;
   int pass;
   int random_sweeps;
+  int zero_uniforms; /* orc_or_proposal: every uniform 0 */
   /* multicanonical */
   int muca_on;
   su2gpu_weight w;
@@ -82,7 +83,7 @@ static inline double* PHI(const orc_ctx* c, int h, long i) { return c->phi[h] + 
 static inline double* TRP(const orc_ctx* c, long i) { return c->trip + i * 3; }
 static inline double A1(const orc_ctx* c, long i, int d) { return c->u1[i * c->D + d]; }
 
-static inline double uni(orc_ctx* c) { return orc_stream_uniform(&c->rng); }
+static inline double uni(orc_ctx* c) { return c->zero_uniforms ? 0.0 : orc_stream_uniform(&c->rng); }
 
 /* ------------------------------------------------------------------ */
 /* layout: layout.c:657-756 (serial), paritymap layout.c:826-851       */
@@ -894,6 +895,27 @@ int orc_site_update(orc_ctx* c, int kind, long i, int sub, uint32_t pass) {
   return site_update(c, kind, i, sub);
 }
 int orc_site_draws(const orc_ctx* c) { return (int)c->rng.draw; }
+
+/* The overrelaxation proposal at site i (overrelax.c:54-417): the update
+ * run with every uniform 0, which it always accepts (|dV/dV'| >= 0), and
+ * the old value put back.  kind 4 doublet `sub`, 6 triplet, 8 singlet;
+ * returns the reals written to out (-1: absent field). */
+int orc_or_proposal(orc_ctx* c, int kind, long i, int sub, double* out) {
+  double* f = NULL;
+  int n = -1;
+  if (kind == 4 && sub < c->nh) { f = PHI(c, sub, i); n = 4; }
+  else if (kind == 6 && c->has_trip) { f = TRP(c, i); n = 3; }
+  else if (kind == 8 && c->has_sing) { f = c->sing + i; n = 1; }
+  if (!f) return -1;
+  double old[4];
+  memcpy(old, f, sizeof(double) * n);
+  c->zero_uniforms = 1;
+  site_update(c, kind, i, sub);
+  c->zero_uniforms = 0;
+  memcpy(out, f, sizeof(double) * n);
+  memcpy(f, old, sizeof(double) * n);
+  return n;
+}
 
 /* ------------------------------------------------------------------ */
 /* multicanonical (multicanonical.c)                                   */

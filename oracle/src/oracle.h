@@ -54,6 +54,7 @@ double orc_magcharge_cube(const orc_ctx* c, long i);
 double orc_polysolve3(double a, double b, double cc, double d);
 int orc_site_update(orc_ctx* c, int kind, long i, int sub, uint32_t pass);
 int orc_site_draws(const orc_ctx* c);
+int orc_or_proposal(orc_ctx* c, int kind, long i, int sub, double* out);
 
 /* multicanonical */
 int orc_muca_set(orc_ctx* c, const su2gpu_weight* w);

@@ -47,6 +47,7 @@ UNITS = [
     ("su2_noalloc", "su2_noalloc.cu", []),
     ("su2_pool", "su2_pool.cu", []),
     ("su2_correl", "su2_correl.cu", []),
+    ("su2_probe", "su2_probe.cu", []),
 ]
 EXTRA_SOURCES = []  # (name, source) of further host units, appended by later modules
 

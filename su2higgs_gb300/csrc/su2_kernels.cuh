@@ -338,8 +338,15 @@ __device__ inline R polysolve3(R a, R b, R c, R d, int* fallback) {
 }
 
 // ---------------------------------------------------------------------------
-// local updates
+// local updates.  The overrelaxation updates take their random-number source
+// as a template parameter: the sweep kernels pass the site's stream
+// (SiteRng), the per-site verification kernel ZeroRng, whose uniforms are
+// all 0, so that every proposal is accepted and can be read back.
 // ---------------------------------------------------------------------------
+template <typename R>
+struct ZeroRng {
+  __device__ R uni() { return (R)0; }
+};
 // heatbath_su2link (heatbath.c:15-124): Kennedy-Pendleton; the uniforms are
 // drawn in the reference's order (4 per trial, 3 per sphere trial, 1 for the
 // triplet accept/reject).
@@ -487,9 +494,9 @@ __device__ inline int metro_doublet(const Fields<R>& f, const Geom& g, const Cou
 }
 
 // overrelax_doublet (overrelax.c:54-128)
-template <typename R, int CC>
+template <typename R, int CC, typename RNG>
 __device__ inline int overrelax_doublet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
-                                        SiteRng<R>& rng, int* fallback) {
+                                        RNG& rng, int* fallback) {
   Q<R> s = staple_doublet<R, CC>(f, g, cp, c, i, 0);
   Q<R> p = ld4<R>(php(f, 0), i);
   R F = msqrt(s.a * s.a + s.b * s.b + s.c * s.c + s.d * s.d);
@@ -524,9 +531,9 @@ __device__ inline int overrelax_doublet(const Fields<R>& f, const Geom& g, const
 }
 
 // overrelax_higgs2 (overrelax.c:295-417)
-template <typename R, int CC>
+template <typename R, int CC, typename RNG>
 __device__ inline int overrelax_higgs2(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
-                                       int h, SiteRng<R>& rng, int* fallback) {
+                                       int h, RNG& rng, int* fallback) {
   Q<R> s = staple_doublet<R, CC>(f, g, cp, c, i, h);
   Q<R> fv = ld4<R>(php(f, h), i);
   Q<R> H;
@@ -602,9 +609,9 @@ __device__ inline V3<R> staple_triplet(const Fields<R>& f, const Geom& g, const 
   return s;
 }
 
-template <typename R, int CC>
+template <typename R, int CC, typename RNG>
 __device__ inline int overrelax_triplet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
-                                        SiteRng<R>& rng, int* fallback) {
+                                        RNG& rng, int* fallback) {
   V3<R> s = staple_triplet(f, g, c, i);
   V3<R> t = ld3(f, i);
   R F = msqrt(s.x * s.x + s.y * s.y + s.z * s.z);
@@ -670,9 +677,9 @@ __device__ inline R localact_singlet(const Fields<R>& f, const Geom& g, const Co
 }
 
 // overrelax_singlet (overrelax.c:243-285)
-template <typename R, int CC>
+template <typename R, int CC, typename RNG>
 __device__ inline int overrelax_singlet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
-                                        SiteRng<R>& rng, int* fallback) {
+                                        RNG& rng, int* fallback) {
   R S = f.sing[i];
   R c1 = (R)cp.b1s;
 #pragma unroll

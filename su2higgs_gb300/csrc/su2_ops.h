@@ -59,6 +59,16 @@ struct PrecOps {
                        cudaStream_t st);
 };
 
+// per-site values of su2gpu_site_values (su2_probe.cu): `what` is one of
+// SITE_*; out holds V rows of the value's width, in layout order
+enum : int {
+  SITE_LINK_STAPLE = 1, SITE_WILSON_STAPLE = 2, SITE_LOCALACT_SU2LINK = 3, SITE_LOCALACT_U1LINK = 4,
+  SITE_STAPLE_DOUBLET = 5, SITE_LOCALACT_DOUBLET = 6, SITE_LOCALACT_SINGLET = 7, SITE_OR_DOUBLET = 8,
+  SITE_OR_DOUBLET1 = 9, SITE_OR_TRIPLET = 10, SITE_OR_SINGLET = 11
+};
+void launch_site_probe(int what, int parity, const Fields<double>& f, const Geom& g, const Coup& cp, double* out,
+                       cudaStream_t st);
+
 // instantiations (su2_inst.cu)
 extern const Ops ops_f64_generic, ops_f64_fund, ops_f64_adj, ops_f64_su2u1s;
 extern const Ops ops_f32_generic, ops_f32_fund, ops_f32_adj, ops_f32_su2u1s;

@@ -122,6 +122,7 @@ struct su2gpu_pool {
   // its work items: segments of seg_tiles 128-site tiles of one chain, and
   // the first segment of each active chain (+ the end)
   int seg_tiles = 8, seg_env = 0, seg_tuned = 0;  // seg_tuned: the autotuner's pick (0: none)
+  int npasses = 0;  // passes per sweep of the recipe (set at the rebuild)
   Buf segs;
   std::vector<int4> h_segs;  // (slot, t0, the chain's segment count, 0)
   std::vector<int> h_sfirst;
@@ -268,8 +269,12 @@ int rebuild(su2gpu_pool* P, void* arena_base = nullptr, void* slot_base = nullpt
     std::vector<PassDesc> rec;
     int64_t counts[SU2GPU_NCOUNTERS] = {0};
     sweep_recipe(P->recipe, rec, counts);
-    P->persistent = P->persist_mode == 1 || (P->persist_mode < 0 && P->active.size() >= 8 && seg_auto >= 4 &&
-                                             (int)rec.size() <= PERSIST_MAX_PASSES);
+    P->npasses = (int)rec.size();
+    // a recipe of more passes than the work list holds always sweeps one
+    // launch per pass (forcing the persistent mode on is refused for it)
+    const bool fits = P->npasses <= PERSIST_MAX_PASSES;
+    P->persistent = fits && (P->persist_mode == 1 ||
+                             (P->persist_mode < 0 && P->active.size() >= 8 && seg_auto >= 4));
     P->h_segs.clear();
     P->h_sfirst.clear();
     for (int s : P->active) {
@@ -575,6 +580,7 @@ int su2gpu_pool_add(su2gpu_pool* P, const su2gpu_params* p, uint64_t seed, uint3
   PCK(cudaGetLastError());
   PCK(cudaStreamSynchronize(P->st));
   P->dirty = true;
+  P->seg_tuned = 0;  // a tuned work-item size holds for the membership it was tuned on
   *slot_out = s;
   return SU2GPU_OK;
 }
@@ -585,6 +591,7 @@ int su2gpu_pool_remove(su2gpu_pool* P, int32_t s) {
   arena_free(P, P->slots[s].off, P->slots[s].bytes);
   P->slots[s].active = false;
   P->dirty = true;
+  P->seg_tuned = 0;
   return SU2GPU_OK;
 }
 
@@ -976,9 +983,15 @@ static int pool_check(su2gpu_pool* P) {
   int herr = 0;
   PCK(cudaMemcpyAsync(&herr, P->err.p, sizeof(int), cudaMemcpyDeviceToHost, P->st));
   PCK(cudaStreamSynchronize(P->st));
-  if (herr)
+  if (herr) {
+    // the flags are reported once: cleared here, so that the next call on
+    // the pool runs again (the chains of a failed call are left partly
+    // swept: their fields hold whatever passes completed)
+    PCK(cudaMemsetAsync(P->err.p, 0, sizeof(int), P->st));
+    PCK(cudaStreamSynchronize(P->st));
     return fail(SU2GPU_ERR_KERNEL, "a pool kernel reported an invalid state (flags %d: 1 NaN fields, 2 bad tile, "
                 "4 persistent sweep dependency wait timed out)", herr);
+  }
   return SU2GPU_OK;
 }
 
@@ -996,6 +1009,7 @@ int su2gpu_pool_run(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
 // when forced, or in the automatic mode by the pool's rule applied to the
 // group alone (8 chains or more, 16 tiles or more per resident block)
 static bool group_persistent(const su2gpu_pool* P, int a0, int a1) {
+  if (P->npasses > PERSIST_MAX_PASSES) return false;
   if (P->persist_mode != -1) return P->persist_mode == 1;
   const int64_t tiles = P->h_tfirst[0][a1] - P->h_tfirst[0][a0];
   return a1 - a0 >= 8 && tiles >= 16 * (int64_t)std::max(1u, P->persist_grid);
@@ -1263,6 +1277,14 @@ int su2gpu_pool_enqueue(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
 
 int su2gpu_pool_set_persistent(su2gpu_pool* P, int32_t on) {
   if (!P) return SU2GPU_ERR_INVALID;
+  if (on > 0) {
+    std::vector<PassDesc> passes;
+    int64_t counts[SU2GPU_NCOUNTERS] = {0};
+    sweep_recipe(P->recipe, passes, counts);
+    if ((int)passes.size() > PERSIST_MAX_PASSES)
+      return fail(SU2GPU_ERR_INVALID, "the recipe has %d passes per sweep: the persistent sweep takes at most %d",
+                  (int)passes.size(), PERSIST_MAX_PASSES);
+  }
   PCK(cudaStreamSynchronize(P->st));
   P->persist_mode = on < 0 ? -1 : (on ? 1 : 0);
   P->dirty = true;  // the mode in effect and the segments are set at the rebuild
@@ -1307,6 +1329,16 @@ int su2gpu_pool_check_wait_timeout(su2gpu_pool* P, int32_t spin_limit, int32_t* 
   PCK(cudaMemcpy(&herr, P->err.p, sizeof(int), cudaMemcpyDeviceToHost));
   PCK(cudaMemset(P->err.p, 0, sizeof(int)));
   *flags = herr;
+  return SU2GPU_OK;
+}
+
+int su2gpu_pool_raise_error(su2gpu_pool* P, int32_t flags) {
+  if (!P || flags <= 0) return fail(SU2GPU_ERR_INVALID, "bad error flags");
+  PCK(cudaStreamSynchronize(P->st));
+  int herr = 0;
+  PCK(cudaMemcpy(&herr, P->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+  herr |= flags;
+  PCK(cudaMemcpy(P->err.p, &herr, sizeof(int), cudaMemcpyHostToDevice));
   return SU2GPU_OK;
 }
 
@@ -1515,6 +1547,15 @@ int su2gpu_pool_autotune(su2gpu_pool* P, int32_t* choices, float* best_ms) {
         if (r >= 0) ms += t;
       }
       if (rc) break;
+      // a candidate whose dependency wait gave up skipped its remaining
+      // items (and so finished early): its flags are cleared and it is not kept
+      int herr = 0;
+      PCK(cudaMemcpyAsync(&herr, P->err.p, sizeof(int), cudaMemcpyDeviceToHost, P->st));
+      PCK(cudaStreamSynchronize(P->st));
+      if (herr) {
+        PCK(cudaMemsetAsync(P->err.p, 0, sizeof(int), P->st));
+        continue;
+      }
       if (ms < best) { best = ms; bestseg = seg; }
     }
     segbuf.release();

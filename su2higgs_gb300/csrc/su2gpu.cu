@@ -348,6 +348,48 @@ int su2gpu_layout_tables(su2gpu_ctx* c, int64_t* next, int64_t* prev, int64_t* c
 // ---------------------------------------------------------------------------
 // field transfer
 // ---------------------------------------------------------------------------
+int su2gpu_site_values(su2gpu_ctx* c, int32_t what, double* out) {
+  if (!c || !out) return SU2GPU_ERR_INVALID;
+  if (c->prec != 64) {
+    set_err("per-site values are computed on FP64 contexts only");
+    return SU2GPU_ERR_UNSUPPORTED;
+  }
+  static_assert(SITE_OR_SINGLET == SU2GPU_SITE_OR_SINGLET, "site value codes differ");
+  int width = 0;
+  bool present = true;
+  switch (what) {
+    case SU2GPU_SITE_LINK_STAPLE: case SU2GPU_SITE_WILSON_STAPLE: width = 12; break;
+    case SU2GPU_SITE_LOCALACT_SU2LINK: width = 3; break;
+    case SU2GPU_SITE_LOCALACT_U1LINK: width = 3; present = c->has_u1; break;
+    case SU2GPU_SITE_STAPLE_DOUBLET: width = 4; present = c->nh > 0; break;
+    case SU2GPU_SITE_LOCALACT_DOUBLET: width = 1; present = c->nh > 0; break;
+    case SU2GPU_SITE_LOCALACT_SINGLET: width = 1; present = c->has_s; break;
+    case SU2GPU_SITE_OR_DOUBLET: width = 4; present = c->nh > 0; break;
+    case SU2GPU_SITE_OR_DOUBLET1: width = 4; present = c->nh > 1; break;
+    case SU2GPU_SITE_OR_TRIPLET: width = 3; present = c->has_t; break;
+    case SU2GPU_SITE_OR_SINGLET: width = 1; present = c->has_s; break;
+    default: set_err("unknown per-site value %d", what); return SU2GPU_ERR_INVALID;
+  }
+  if (!present) {
+    set_err("per-site value %d: the field content lacks its field", what);
+    return SU2GPU_ERR_INVALID;
+  }
+  const size_t bytes = (size_t)c->g.V * width * sizeof(double);
+  DevBuf buf;
+  int rc = buf.ensure(bytes);
+  if (rc) return rc;
+  for (int par = 0; par < 2; par++) launch_site_probe(what, par, c->f64, c->g, c->cp, (double*)buf.p, c->st);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, buf.p, bytes, cudaMemcpyDeviceToHost, c->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  buf.release();
+  if (e != cudaSuccess) {
+    set_err("per-site values: %s", cudaGetErrorString(e));
+    return SU2GPU_ERR_CUDA;
+  }
+  return SU2GPU_OK;
+}
+
 static int transfer(su2gpu_ctx* c, int upload, double* link, double* u1, double* d0, double* d1, double* trip,
                     double* sing) {
   int64_t V = c->g.V;

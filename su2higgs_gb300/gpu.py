@@ -41,6 +41,7 @@ def lib():
         L.su2gpu_footprint_bytes.restype = i64
         L.su2gpu_footprint_bytes.argtypes = [ctypes.POINTER(abi.Params)]
         L.su2gpu_layout_tables.argtypes = [vp, vp, vp, vp, vp]
+        L.su2gpu_site_values.argtypes = [vp, i32, vp]
         L.su2gpu_upload_fields.argtypes = [vp] + [vp] * 6
         L.su2gpu_download_fields.argtypes = [vp] + [vp] * 6
         L.su2gpu_set_seed.argtypes = [vp, u64, u32]
@@ -106,6 +107,7 @@ def lib():
         L.su2gpu_pool_get_persist_tiles.argtypes = [vp, ctypes.POINTER(i32)]
         L.su2gpu_pool_get_persistent.argtypes = [vp, ctypes.POINTER(i32)]
         L.su2gpu_pool_check_wait_timeout.argtypes = [vp, i32, ctypes.POINTER(i32)]
+        L.su2gpu_pool_raise_error.argtypes = [vp, i32]
         L.su2gpu_pool_enqueue_measure.argtypes = [vp, vp, i32, ctypes.POINTER(i32)]
         L.su2gpu_pool_set_stream.argtypes = [vp, vp]
         L.su2gpu_pool_launches_per_sweep.argtypes = [vp, ctypes.POINTER(i32)]
@@ -237,6 +239,19 @@ class Lattice:
         m = np.zeros(abi.NMEAS)
         check(lib().su2gpu_measure(self._h, _p(m)))
         return m
+
+    SITE_VALUES = {"link_staple": (1, (3, 4)), "wilson_staple": (2, (3, 4)), "localact_su2link": (3, (3,)),
+                   "localact_u1link": (4, (3,)), "staple_doublet": (5, (4,)), "localact_doublet": (6, ()),
+                   "localact_singlet": (7, ()), "or_doublet": (8, (4,)), "or_doublet1": (9, (4,)),
+                   "or_triplet": (10, (3,)), "or_singlet": (11, ())}
+
+    def site_values(self, name):
+        """Per-site values of a deterministic kernel (su2gpu_site_values),
+        named as the keys of SITE_VALUES; shape (V,) + the value's shape."""
+        what, shape = self.SITE_VALUES[name]
+        out = np.zeros((self.V,) + shape)
+        check(lib().su2gpu_site_values(self._h, what, _p(out)))
+        return out
 
     def layout_tables(self):
         V = self.V
@@ -616,6 +631,10 @@ class Pool:
         flags = ctypes.c_int32()
         check(lib().su2gpu_pool_check_wait_timeout(self._h, spin_limit, ctypes.byref(flags)))
         return flags.value
+
+    def raise_error(self, flags):
+        """Test hook: set error flags in the pool's device error word."""
+        check(lib().su2gpu_pool_raise_error(self._h, flags))
 
     def enqueue_measure(self, device_ptr, max_chains):
         """Measurement of every active chain into a device buffer of

@@ -3,7 +3,7 @@
 A request is one independent chain of the su2higgs update sweep: lattice side,
 field content, couplings, a number of sweeps and, optionally, a gradient-flow
 measurement at the end.  The reference runs one chain per process
-(su2higgs main loop, su2.c:1-200); here chains of many requests share the GPU:
+(su2higgs main loop, main.c:302-379); here chains of many requests share the GPU:
 
 * one pool (su2gpu_pool_*) per field content keeps the admitted chains
   resident in a device arena; a chain is admitted when its fields fit in the

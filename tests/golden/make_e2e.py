@@ -57,7 +57,8 @@ sys.path.insert(0, ROOT)
 
 from su2higgs_gb300 import abi, workloads  # noqa: E402
 
-REF_CONFIG = "/root/reference/config"
+# the reference checkout's example config (SU2HIGGS_REF overrides its location)
+REF_CONFIG = os.path.join(os.environ.get("SU2HIGGS_REF", "/root/reference"), "config")
 REF_BIN = os.path.join(ROOT, "oracle", "_ref")
 L = (6, 4, 8)
 

@@ -5,7 +5,11 @@ Needs the reference harness built from the reference sources
 Every fixture stores its inputs, so the tests never regenerate them:
 
   layout_<L>.npz         next/prev/coords/parity of layout() (layout.c:657-756)
-  sites_<content>.npz    per-site staples, local actions, alpha_proj on a hot lattice
+  tables_sha256.npz      SHA-256 of those tables for the larger sides (up to 128^3)
+  sites_<content>.npz    per-site staples, local actions, alpha_proj and
+                         overrelaxation proposals (the value an accepted
+                         overrelax_doublet / _higgs2 / _triplet / _singlet
+                         writes, overrelax.c:54-417) on a hot lattice
   sweep_<case>.npz       fields + counters + measure() sums after 1 and 3 calls of
                          update_lattice() (update.c:270) with the Philox stream
   muca_<case>.npz        the same with multicanonical global accept/reject
@@ -30,7 +34,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
-from native import Fields, Ref, hot_fields, ref_available, weight_from_state  # noqa: E402
+from native import Fields, Ref, hot_fields, layout_digest, ref_available, weight_from_state  # noqa: E402
 from su2higgs_gb300 import abi  # noqa: E402
 
 SEED = 20261203
@@ -69,8 +73,31 @@ def param_dict(p):
             if name != "reserved"}
 
 
+# sides whose layout tables are stored as SHA-256 digests only
+LAYOUT_HASHED = [(24, 24, 24), (48, 48, 48), (64, 64, 64), (96, 96, 96), (128, 128, 128), (32, 16, 24)]
+
+
+def layout_hash_of(L):
+    """The digest of one side's tables, each in a process of its own (the
+    reference keeps its lattice in globals; large sides need an unlimited
+    stack, as the reference's own runs do)."""
+    import subprocess
+    cmd = f"ulimit -s unlimited; {sys.executable} {os.path.abspath(__file__)} --layout-hash {L[0]} {L[1]} {L[2]}"
+    out = subprocess.run(["bash", "-c", cmd], check=True, capture_output=True, text=True).stdout
+    return out.strip().splitlines()[-1]
+
+
+def gen_layout_hashes():
+    Ls, digests = [], []
+    for L in LAYOUT_HASHED:
+        digests.append(layout_hash_of(L))
+        Ls.append(L)
+    np.savez_compressed(os.path.join(HERE, "tables_sha256.npz"), L=np.array(Ls, dtype=np.int32),
+                        sha256=np.array(digests))
+
+
 def gen_layout():
-    for L in [(4, 4, 4), (6, 4, 8), (8, 8, 8), (2, 6, 4), (10, 2, 2)]:
+    for L in [(4, 4, 4), (6, 4, 8), (8, 8, 8), (2, 6, 4), (10, 2, 2), (12, 12, 12), (16, 16, 16)]:
         p = abi.make_params("pure", L=L)
         r = Ref(p)
         nx, pv, co, par = r.tables()
@@ -114,6 +141,17 @@ def gen_sites(case):
         out["magcharge_cube"] = np.array([r.lib.ref_magcharge_cube(i) for i in range(V)])
     if p.content & abi.SINGLET:
         out["localact_singlet"] = np.array([r.lib.ref_localact_singlet(i) for i in range(V)])
+    # overrelaxation proposals (every site, from the input fields)
+    for key, kind, sub, n, present in (("or_doublet", 4, 0, 4, p.nhiggs() > 0),
+                                       ("or_doublet1", 4, 1, 4, p.nhiggs() > 1),
+                                       ("or_triplet", 6, 0, 3, bool(p.content & abi.TRIPLET)),
+                                       ("or_singlet", 8, 0, 1, bool(p.content & abi.SINGLET))):
+        if not present:
+            continue
+        a = np.zeros((V, n))
+        for i in range(V):
+            assert r.lib.ref_or_proposal(kind, i, sub, P(a[i])) == n
+        out[key] = a if n > 1 else a[:, 0]
     out["measure"] = r.measure()
     np.savez_compressed(os.path.join(HERE, f"sites_{case}.npz"), **out)
 
@@ -302,6 +340,11 @@ def main(only=None):
         for m in only:
             if m == "mpi_layout":
                 gen_mpi_layout()
+            elif m == "layout":
+                gen_layout()
+                gen_layout_hashes()
+            elif m.startswith("sites_"):
+                gen_sites(m[len("sites_"):])
             elif m in CORREL_CASES:
                 gen_correl(m)
             else:
@@ -310,6 +353,7 @@ def main(only=None):
     if not ref_available("fund"):
         sys.exit("reference harness not built: make -C oracle/ref REF=<su2higgs checkout>")
     gen_layout()
+    gen_layout_hashes()
     for c in ("pure", "fund", "adj", "su2u1s", "fundadj", "higgs2"):
         gen_sites(c)
     for c in CASES:
@@ -326,4 +370,8 @@ def main(only=None):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1:])
+    if len(sys.argv) == 5 and sys.argv[1] == "--layout-hash":
+        r = Ref(abi.make_params("pure", L=tuple(int(x) for x in sys.argv[2:5])))
+        print(layout_digest(*r.tables()))
+    else:
+        main(sys.argv[1:])

@@ -42,6 +42,7 @@ def oracle_lib():
         lib.orc_set_rng.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32]
         lib.orc_site_update.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_long, ctypes.c_int, ctypes.c_uint32]
         lib.orc_site_draws.argtypes = [ctypes.c_void_p]
+        lib.orc_or_proposal.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_long, ctypes.c_int, ctypes.c_void_p]
         for name in ("orc_localact_su2link", "orc_localact_u1link"):
             getattr(lib, name).restype = ctypes.c_double
             getattr(lib, name).argtypes = [ctypes.c_void_p, ctypes.c_long, ctypes.c_int]
@@ -382,6 +383,7 @@ class Ref:
         for name in ("ref_link_staple", "ref_wilson_staple", "ref_staple_doublet"):
             if hasattr(lib, name):
                 getattr(lib, name).argtypes = [ctypes.c_long, ctypes.c_int, ctypes.c_void_p]
+        lib.ref_or_proposal.argtypes = [ctypes.c_int, ctypes.c_long, ctypes.c_int, ctypes.c_void_p]
         lib.ref_polysolve3.restype = ctypes.c_double
         lib.ref_polysolve3.argtypes = [ctypes.c_double] * 4
         lib.ref_calc_orderparam.restype = ctypes.c_double
@@ -574,6 +576,17 @@ def ref_sums_to_layout(p, raw):
             m[abi.M_S2PHI2] = take()
     assert k == len(raw), (k, len(raw))
     return m
+
+
+def layout_digest(nx, pv, co, par):
+    """SHA-256 of the layout tables (next, prev, coords as little-endian
+    int64 [V][D], then parity as int32 [V])."""
+    import hashlib
+    h = hashlib.sha256()
+    for a in (nx, pv, co):
+        h.update(np.ascontiguousarray(a, dtype="<i8").tobytes())
+    h.update(np.ascontiguousarray(par, dtype="<i4").tobytes())
+    return h.hexdigest()
 
 
 def rel_err(a, b, floor=1e-300):

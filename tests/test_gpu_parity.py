@@ -55,6 +55,53 @@ def test_layout_tables(gpu, name):
     assert np.array_equal(par, d["parity"])
 
 
+def test_layout_table_digests(gpu):
+    """The device's closed-form layout of the larger sides (24^3 ... 128^3)
+    against the SHA-256 of the reference's own layout() tables."""
+    from native import layout_digest
+    d = load("tables_sha256.npz")
+    for L, digest in zip(d["L"], d["sha256"]):
+        lat = gpu.Lattice(abi.make_params("pure", L=tuple(int(x) for x in L)))
+        assert layout_digest(*lat.layout_tables()) == str(digest), tuple(L)
+        lat.close()
+
+
+# (fixture key, site_values name, relative-error floor): the staples can
+# cancel to small values, so their errors are taken against a floor of 1e-3
+SITE_KEYS = [("link_staple", "link_staple", 1e-3), ("wilson_staple", "wilson_staple", 1e-3),
+             ("localact_su2link", "localact_su2link", 1e-300), ("localact_u1link", "localact_u1link", 1e-300),
+             ("staple_doublet", "staple_doublet", 1e-3), ("localact_doublet", "localact_doublet", 1e-300),
+             ("localact_singlet", "localact_singlet", 1e-300), ("or_doublet", "or_doublet", 1e-3),
+             ("or_doublet1", "or_doublet1", 1e-3), ("or_triplet", "or_triplet", 1e-3),
+             ("or_singlet", "or_singlet", 1e-3)]
+
+
+@pytest.mark.parametrize("name", names("sites_"))
+def test_site_values_match_reference(gpu, name):
+    """Staples, local actions and overrelaxation proposals of every site,
+    computed on the device by the functions the update kernels call, on a
+    configuration of the reference's own run: within 1e-12 relative of the
+    reference's FP64 values (staples.c:84-302, su2u1.c:166-723,
+    overrelax.c:54-417)."""
+    from native import rel_err
+    d = load(name)
+    p = params_of(d)
+    lat = gpu.Lattice(p)
+    upload(lat, fields_of(d, p, "in_"))
+    checked = 0
+    for key, what, floor in SITE_KEYS:
+        if key not in d:
+            continue
+        got = lat.site_values(what)
+        err = rel_err(got, d[key], floor)
+        assert err < RTOL, (key, err)
+        checked += 1
+    assert checked >= 3
+    # the fields are unchanged by the overrelaxation probes
+    for k, v in max_diff(lat.download(), fields_of(d, p, "in_")).items():
+        assert v == 0.0, k
+
+
 def test_upload_download_roundtrip(gpu):
     p = abi.make_params("su2u1s", L=(6, 4, 8))
     f = hot_fields(p, seed=5)
@@ -131,7 +178,7 @@ def test_gradient_flow_matches_reference(gpu, name):
     ref = d["rows_raw"]
     assert rows.shape[0] == ref.shape[0]
     for r_g, r_r in zip(rows, ref):
-        ok, k, a, b = measure_close(r_g[1:], ref_sums_to_layout(p, r_r), 1e-11)
+        ok, k, a, b = measure_close(r_g[1:], ref_sums_to_layout(p, r_r), RTOL)
         assert ok, (k, a, b)
     # the flow works on a copy: the lattice itself is unchanged
     for k, v in max_diff(lat.download(), fields_of(d, p, "in_")).items():

@@ -197,3 +197,43 @@ def test_autotuner_picks_the_persistent_item_size(gpu):
             if fa[n] is not None:
                 assert np.array_equal(fa[n], fb[n]), (s, n)
         assert np.array_equal(a.counters(s), b.counters(s)), s
+
+
+def test_error_flags_reported_once(gpu):
+    """A kernel error flag (set here from the host, as a kernel that found a
+    bad state would) makes the next run fail with ERR_KERNEL and is cleared
+    by it: the run after that works."""
+    specs = specs_of("adj", 32)[:3]
+    inputs = [as_dict(hot_fields(p, seed=410 + k)) for k, (p, _, _) in enumerate(specs)]
+    pool, slots = make_pool(gpu, specs, True, inputs)
+    pool.raise_error(4)
+    with pytest.raises(gpu.SU2GPUError, match="flags 4"):
+        pool.run(1)
+    pool.run(2)
+    m = pool.measure()
+    assert all(np.all(np.isfinite(v)) for v in m.values())
+
+
+def test_long_recipe_sweeps_one_launch_per_pass(gpu):
+    """A recipe of more passes than the persistent work list holds (6 link
+    + 2 x 41 triplet passes = 88 > 64): forcing the persistent mode is
+    refused, the automatic mode sweeps one launch per pass, and the
+    pipelined cycle gives the same fields as upload + run + download."""
+    specs = [(abi.make_params("adj", L=(8, 8, 8), precision=32, scalar_sweeps=40, betasu2=6.0 + k), 20 + k, k)
+             for k in range(8)]
+    inputs = [as_dict(hot_fields(p, seed=430 + k)) for k, (p, _, _) in enumerate(specs)]
+    pool, slots = make_pool(gpu, specs, None, inputs)
+    with pytest.raises(gpu.SU2GPUError, match="passes per sweep"):
+        pool.persistent = True
+    assert not pool.persistent
+    assert pool.launches_per_sweep() == 6 + 82 + 1
+    fields = [{n: v.copy() for n, v in f.items() if v is not None} for f in inputs]
+    sums = pool.cycle(slots, fields, 2)
+    ref, rslots = make_pool(gpu, specs, False, inputs)
+    ref.run(2)
+    for s, f in zip(rslots, fields):
+        got = ref.download(s)
+        for n in f:
+            assert np.array_equal(got[n], f[n]), n
+    mref = ref.measure()
+    assert np.array_equal(np.array([mref[s] for s in rslots]), sums)

@@ -156,12 +156,16 @@ def test_observables_gpu64_gpu32_oracle(gpu):
             assert pv > 1e-3, (name, tag, pv)
 
 
+@pytest.mark.parametrize("content", ["fund", "su2u1s"])
 @pytest.mark.parametrize("precision", [64, 32])
-def test_multicanonical_orderparam_distribution(gpu, precision):
+def test_multicanonical_orderparam_distribution(gpu, precision, content):
     """READONLY multicanonical run (global accept/reject after each doublet
-    half-sweep): the order-parameter distribution of the GPU (FP64 fields, and
-    FP32 fields with the FP64 weight and decisions) and of the oracle."""
-    p = abi.make_params("fund", L=(6, 6, 6))
+    half-sweep, multicanonical.c:385-445 with the order parameter of
+    multicanonical.c:709-751): the order-parameter distribution of the GPU
+    (FP64 fields, and FP32 fields with the FP64 weight and decisions) and of
+    the oracle, for SU(2) + Higgs and for SU(2) x U(1) + Higgs + singlet
+    (the multicanonical workload's content)."""
+    p = abi.make_params(content, L=(6, 6, 6))
     f = hot_fields(p, seed=8, phi_mean=1.0)
     # warm up to equilibrium with the oracle, then centre a tilted weight there
     o0 = Oracle(p)
@@ -187,8 +191,8 @@ def test_multicanonical_orderparam_distribution(gpu, precision):
     s.param_value[0] = ph[:half].sum() / p.sites()
     s.param_value[1] = ph[half:].sum() / p.sites()
     nmeas = 3000
-    lat = gpu.Lattice(abi.make_params("fund", L=(6, 6, 6), precision=precision), seed=55)
-    lat.upload(link=f0.link, d0=f0.d0)
+    lat = gpu.Lattice(abi.make_params(content, L=(6, 6, 6), precision=precision), seed=55)
+    lat.upload(link=f0.link, u1=f0.u1, d0=f0.d0, sing=f0.sing)
     lat.muca_set(s)
     o = Oracle(p)
     o.put(f0)
@@ -212,3 +216,68 @@ def test_multicanonical_orderparam_distribution(gpu, precision):
     rate_g = cg[abi.C_ACC_MUCA] / cg[abi.C_TOTAL_MUCA]
     rate_o = co[abi.C_ACC_MUCA] / co[abi.C_TOTAL_MUCA]
     assert 0.05 < rate_g < 0.999 and abs(rate_g - rate_o) < 0.05, (rate_g, rate_o)
+
+
+def _starts(p, n, seed, broken=0.0, **kw):
+    out = []
+    for k in range(n):
+        f = hot_fields(p, seed=seed + k, **kw)
+        if broken and f.trip is not None:
+            f.trip[:, 0] += broken
+        out.append({n_: getattr(f, n_) for n_ in ("link", "u1", "d0", "d1", "trip", "sing")})
+    return out
+
+
+# SU(2) + adjoint Higgs at couplings of the batched ensemble (beta in [6, 12],
+# m^2_adj in [-0.3, 0.1], lambda_adj 0.005), one point on each side of the
+# transition on 8^3: beta 12, m^2 -0.3 started in the broken phase (Tr Sigma^2
+# ~ 23, no monopoles), beta 8, m^2 0.1 in the symmetric phase (Tr Sigma^2 ~
+# 0.3).  Observables of measure.c:110-174: plaquette, Tr Sigma^2,
+# hopping_Sigma, |magnetic charge| density.
+ADJ_POINTS = {
+    "broken": dict(betasu2=12.0, msq_triplet=-0.3, b4=0.005, broken=6.8),
+    "symmetric": dict(betasu2=8.0, msq_triplet=0.1, b4=0.005, broken=0.0),
+}
+
+
+@pytest.mark.parametrize("point", sorted(ADJ_POINTS))
+def test_adjoint_fp32_observables_match_oracle(gpu, point):
+    """The headline form's chains -- FP32 fields in a pool swept by the
+    persistent work-list kernel -- against FP64 GPU pool chains and the FP64
+    oracle from the same starts: every observable within 3 sigma of the
+    binned jackknife errors and equal histograms (heatbath.c:21-27,107-120,
+    overrelax.c:137-236, metropolis.c:113-143)."""
+    import chains
+    kw = dict(ADJ_POINTS[point])
+    broken = kw.pop("broken")
+    L = (8, 8, 8)
+    p32 = abi.make_params("adj", L=L, precision=32, **kw)
+    p64 = abi.make_params("adj", L=L, precision=64, **kw)
+    starts = _starts(p64, 8, 900, broken=broken, trip_sigma=0.3)
+    n_therm, n_gpu, n_orc = 400, 4000, 2000
+    orc = chains.oracle_chains("adj", L, kw, starts[:4], 303, n_therm, n_orc)
+    g32 = chains.pool_chains(gpu, p32, starts, 101, n_therm, n_gpu, persistent=True)
+    g64 = chains.pool_chains(gpu, p64, starts, 202, n_therm, n_gpu)
+    names = chains.CONTENT_OBSERVABLES["adj"]
+    rows, fails = chains.compare(names, {"fp32": g32, "fp64": g64, "oracle": orc})
+    print("\n" + chains.format_rows(f"adjoint 8^3 {point} {kw}", rows))
+    assert not fails, fails
+
+
+def test_su2u1s_fp32_observables_match_oracle(gpu):
+    """SU(2) x U(1) + doublet + singlet (the multicanonical workload's
+    content, beta_G 8, beta_U1 24) without multicanonical acceptance: FP32
+    GPU chains against FP64 GPU chains and the oracle."""
+    import chains
+    L = (8, 8, 8)
+    p32 = abi.make_params("su2u1s", L=L, precision=32)
+    p64 = abi.make_params("su2u1s", L=L, precision=64)
+    starts = _starts(p64, 8, 950, phi_mean=1.0)
+    n_therm, n_gpu, n_orc = 300, 4000, 2000
+    orc = chains.oracle_chains("su2u1s", L, {}, starts[:4], 313, n_therm, n_orc)
+    g32 = chains.pool_chains(gpu, p32, starts, 111, n_therm, n_gpu, persistent=True)
+    g64 = chains.pool_chains(gpu, p64, starts, 212, n_therm, n_gpu)
+    names = chains.CONTENT_OBSERVABLES["su2u1s"]
+    rows, fails = chains.compare(names, {"fp32": g32, "fp64": g64, "oracle": orc})
+    print("\n" + chains.format_rows("su2u1s 8^3", rows))
+    assert not fails, fails

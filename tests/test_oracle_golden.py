@@ -65,8 +65,25 @@ def test_site_kernels(name):
         assert np.max(np.abs(mc - d["magcharge_cube"])) < 1e-10
     if "localact_singlet" in d:
         assert rel_err([lib.orc_localact_singlet(h, i) for i in range(V)], d["localact_singlet"]) < RTOL_DET
+    for key, kind, sub, n in (("or_doublet", 4, 0, 4), ("or_doublet1", 4, 1, 4), ("or_triplet", 6, 0, 3),
+                              ("or_singlet", 8, 0, 1)):
+        if key in d:
+            got = np.zeros((V, n))
+            for i in range(V):
+                assert lib.orc_or_proposal(h, kind, i, sub, P(got[i])) == n
+            assert rel_err(got if n > 1 else got[:, 0], d[key], 1e-3) < RTOL_DET, key
     ok, k, a, b = measure_close(o.measure(), d["measure"], RTOL_DET)
     assert ok, (k, a, b)
+
+
+def test_layout_table_digests():
+    """The closed-form layout of the larger sides (up to 128^3) against the
+    SHA-256 of the reference's own layout() tables."""
+    from native import layout_digest
+    d = load("tables_sha256.npz")
+    for L, digest in zip(d["L"], d["sha256"]):
+        o = Oracle(abi.make_params("pure", L=tuple(int(x) for x in L)))
+        assert layout_digest(*o.tables()) == str(digest), tuple(L)
 
 
 @pytest.mark.parametrize("name", names("sweep_"))

@@ -7,8 +7,10 @@ result and uses only a file-scope scratch array.
 The test gives it fields laid out as the library keeps them, calls it twice in
 a row (the second call reuses the shared scratch), and checks both results
 against su2gpu_measure on the same fields, with the 1e-12 relative tolerance
-of the other measurement tests.  It also checks that a lattice beyond the
-scratch limit (128^3 sites) is refused.  This file is collected last.
+of the other measurement tests, and on configurations of the reference's own
+runs against the reference's measure() sums.  It also checks that a lattice
+beyond the scratch limit (128^3 sites) is refused.  This file is collected
+last.
 """
 import ctypes
 
@@ -98,3 +100,26 @@ def test_noalloc_rejects_lattices_beyond_its_scratch(env):
     rc = L.su2gpu_measure_noalloc(ctypes.byref(p), ctypes.byref(df), ctypes.c_void_p(out.data_ptr()), None)
     assert rc == abi.ERR_CAPACITY
     assert "2097152" in L.su2gpu_last_error().decode()
+
+
+@pytest.mark.parametrize("name", ["sites_fund.npz", "sites_adj.npz", "sites_su2u1s.npz", "sites_higgs2.npz",
+                                  "sites_fundadj.npz"])
+def test_noalloc_measure_matches_reference_sums(env, name):
+    """On a configuration of the reference's own run, two calls in a row give
+    the reference's measure() sums (measure.c:110-233) within 1e-12."""
+    from golden_io import fields_of, load, params_of
+    torch, gpu, L = env
+    d = load(name)
+    p = params_of(d)
+    f = fields_of(d, p, "in_")
+    df, keep = device_layout(torch, f, 64)
+    out = torch.full((2, abi.NMEAS), float("nan"), dtype=torch.float64, device="cuda")
+    for k in range(2):
+        rc = L.su2gpu_measure_noalloc(ctypes.byref(p), ctypes.byref(df), ctypes.c_void_p(out[k].data_ptr()), None)
+        assert rc == abi.OK, L.su2gpu_last_error().decode()
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    for k in range(2):
+        ok, idx, a, b = measure_close(got[k], d["measure"], RTOL)
+        assert ok, (k, idx, a, b)
+    del keep
