@@ -96,11 +96,14 @@ BATCHED = {
 # everywhere (1) and the doublet at the updated sites (2), writes half (0.5)
 # -> 3.5.
 REALS_PER_SITE = {"fund": {0: 16, 2: 18}, "adj": {0: 17, 3: 16.5}, "su2u1s": {0: 16.5, 1: 9.5, 2: 23.5, 4: 3.5}}
-# Compulsory reals per site-update of a whole sweep (6 link half-passes, 10
-# scalar half-passes, one measurement reading every field once)
-REALS_PER_SITE_UPDATE = {"fund": 6 * 16 + 10 * 18 + 16, "adj": 6 * 17 + 10 * 16.5 + 15,
-                         "su2u1s": 6 * 16.5 + 6 * 9.5 + 10 * 23.5 + 10 * 3.5 + 20}
-REALS_MEASURE = 16
+# Compulsory reals per site of the passes of one sweep (6 link half-passes,
+# 10 scalar half-passes) and of one measurement reading every field once; a
+# site-update counts the measurement at the workload's cadence (once per
+# sweep for the single lattices, once per step of S sweeps in the batched
+# form)
+REALS_PER_SWEEP = {"fund": 6 * 16 + 10 * 18, "adj": 6 * 17 + 10 * 16.5,
+                   "su2u1s": 6 * 16.5 + 6 * 9.5 + 10 * 23.5 + 10 * 3.5}
+REALS_MEASURE = {"fund": 16, "adj": 15, "su2u1s": 20}
 KIND_NAMES = {0: "link_heatbath", 1: "u1_metropolis", 2: "doublet_update", 3: "triplet_update",
               4: "singlet_update", 5: "reunitarize"}
 
@@ -247,6 +250,40 @@ def _cpu_chain_worker(args):
     return p.sites(), time.perf_counter() - t0, os.getpid()
 
 
+def batched_config(workload, specs):
+    """The workload's description, the same on both arms (the GPU arm's
+    launch details are reported beside it, under "step")."""
+    from su2higgs_gb300 import workloads
+    Ls = [int(p.L[0]) for p, _, _ in specs]
+    return {"workload": workload, "content": "SU(2) + adjoint Higgs", "chains": len(specs),
+            "sites_total": int(sum(p.sites() for p, _, _ in specs)),
+            "sides": {str(L): Ls.count(L) for L in sorted(set(Ls))},
+            "betasu2": list(workloads.ENSEMBLE_BETA), "msq_adj": list(workloads.ENSEMBLE_MSQ_ADJ),
+            "lambda_adj": workloads.ENSEMBLE_LAMBDA_ADJ, "sweeps_per_chain": 1000,
+            "recipe": "1 link heatbath (3 directions x 2 parities) + 4 triplet overrelax + 1 triplet Metropolis "
+                      "(x 2 parities) per sweep; every chain measured once per 10 sweeps",
+            "start": "seeded hot start (Haar links, triplet N(0, 0.1))"}
+
+
+def _cpu_ensemble_worker(args):
+    """One sweep (+ the measurement, when `measure`) of one ensemble chain
+    with the oracle (FP64), from its seeded start."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from native import Fields, Oracle
+    from su2higgs_gb300 import abi, workloads
+    L, beta, msq, b4, seed, chain, measure = args
+    p = abi.make_params("adj", L=(L, L, L), precision=64, betasu2=beta, msq_triplet=msq, b4=b4)
+    f = workloads.hot_fields(p, seed)
+    o = Oracle(p)
+    o.put(Fields(p, **f))
+    o.set_rng(seed, 0, chain)
+    t0 = time.perf_counter()
+    o.update()
+    if measure:
+        o.measure()
+    return p.sites(), time.perf_counter() - t0, os.getpid()
+
+
 def run_reference_batched(args):
     """The oracle's FP64 restatement of the reference's serial sweep on all
     host cores: each step sweeps 4 x cores chains of the ensemble (cycling
@@ -262,10 +299,7 @@ def run_reference_batched(args):
         jobs = [(r.content, r.L, r.betasu2, r.msq, r.seed, r.rid) for r in stream if r.L <= 32]
         nchains, what = len(jobs), "requests (L <= 32) of the served stream"
     else:
-        nchains, S = BATCHED[args.workload]
-        specs = workloads.batched_ensemble(nchains)
-        jobs = [("adj", int(p.L[0]), float(p.betasu2), float(p.msq_triplet), seed, chain) for p, seed, chain in specs]
-        what = "chains of the batched ensemble"
+        return run_reference_ensemble(args)
     cores = os.cpu_count() or 1
     ctx = mp.get_context("spawn")
     done, wall, nxt = 0, 0.0, 0
@@ -293,6 +327,49 @@ def run_reference_batched(args):
                          "sample": f"{per_step} {what} per step (one process per core, cycling through "
                                    f"{nchains} of them), 1 sweep + measure each; oracle C restatement of the "
                                    "reference's serial sweep"},
+        "e2e": {"value": value, "unit": "site-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_ensemble(args):
+    """The oracle's FP64 restatement of the reference's serial sweep on all
+    host cores over the whole ensemble: each step sweeps every one of its
+    chains once (one process per core, largest chains first, so that the
+    cores stay balanced), measuring each chain once per 10 steps as the GPU
+    arm measures once per 10 sweeps; a step lasts as long as the busiest
+    core's sweeps (lattice set-up excluded, as on the GPU)."""
+    from su2higgs_gb300 import workloads
+    import multiprocessing as mp
+    nchains, S = BATCHED[args.workload]
+    specs = workloads.batched_ensemble(nchains)
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    done, wall = 0, 0.0
+    with ctx.Pool(cores) as pool:
+        for s in range(args.warmup + args.steps):
+            jobs = sorted(((int(p.L[0]), float(p.betasu2), float(p.msq_triplet), float(p.b4), seed, chain,
+                            s % S == S - 1) for p, seed, chain in specs), key=lambda j: -j[0])
+            res = pool.map(_cpu_ensemble_worker, jobs, chunksize=1)
+            if s < args.warmup:
+                continue
+            per_pid = {}
+            for n, t, pid in res:
+                per_pid[pid] = per_pid.get(pid, 0.0) + t
+            done += sum(r[0] for r in res)
+            wall += max(per_pid.values())
+    value = done / wall
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "site-updates/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / max(args.steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": batched_config(args.workload, specs),
+        "step": {"sweeps_per_step": 1, "what": f"one sweep of all {nchains} chains, every 10th step with the "
+                                              "measurement of every chain"},
+        "cpu_baseline": {"value": value, "unit": "site-updates/s", "cores": cores, "kind": "port",
+                         "sample": f"every step: one sweep of each of the {nchains} chains of the ensemble "
+                                   f"(one process per core, {cores} processes), measured once per {S} steps; "
+                                   "oracle C restatement of the reference's serial sweep in FP64"},
         "e2e": {"value": value, "unit": "site-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -555,15 +632,17 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
-def sweep_roofline(site_updates_per_s, content, prec):
+def sweep_roofline(site_updates_per_s, content, prec, sweeps_per_measure=1):
     """The whole sweep against HBM: site-updates/s x compulsory bytes per
-    site-update over the measured copy bandwidth (one GPU)."""
+    site-update (the sweep's passes + the measurement at its cadence of one
+    per `sweeps_per_measure` sweeps) over the measured copy bandwidth (one
+    GPU)."""
     rsize = 4 if prec == 32 else 8
-    b = REALS_PER_SITE_UPDATE[content] * rsize
+    b = (REALS_PER_SWEEP[content] + REALS_MEASURE[content] / sweeps_per_measure) * rsize
     peak, kind = measured_peaks()
     achieved = site_updates_per_s * b / 1e9
-    return {"bytes_per_site_update": b, "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "peak_source": kind}
+    return {"bytes_per_site_update": b, "sweeps_per_measurement": sweeps_per_measure, "achieved": achieved,
+            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": kind}
 
 
 def roofline_of(kinds, ms, content, prec, sites, workload):
@@ -821,6 +900,68 @@ def run_gpu_batched(args):
                 "what": "every 4th chain of the ensemble as an FP64 single-lattice context (graph replay), "
                         "one after another"}
 
+    # the same ensemble in an FP64 pool, swept the same way (persistent
+    # work list where the pool's rule picks it): separates the precision
+    # gain from the batching gain
+    fp64_batched = None
+    if rank == 0 and not args.no_fp64:
+        specs64 = workloads.batched_ensemble(nchains, seed=replica_seed(20261203, rank), precision=64)
+        arena64 = sum(gpu.Pool.chain_bytes(p) for p, _, _ in specs64)
+        pool64 = gpu.Pool(specs64[0][0], arena_bytes=arena64, max_chains=nchains)
+        for p, seed, chain in specs64:
+            slot = pool64.add(p, seed=seed, chain=chain)
+            pool64.upload(slot, **workloads.hot_fields(p, seed))
+        pool64.autotune()
+        pool64.set_stream(stream.cuda_stream)
+        ms64 = []
+        with torch.cuda.stream(stream):
+            for k in range(5):
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                pool64.enqueue(S, graph=True)
+                pool64.enqueue_measure(sums[0].data_ptr(), nchains)
+                b.record(stream)
+                flush.zero_()
+                ms64.append((a, b))
+            torch.cuda.synchronize()
+        ms64 = [a.elapsed_time(b) for a, b in ms64][2:]
+        pool64.set_stream(None)
+        pool64.run(0)
+        v64b = sites * S * len(ms64) / (sum(ms64) * 1e-3)
+        fp64_batched = {"value": v64b, "unit": "site-updates/s", "steps": len(ms64), "sweeps_per_step": S,
+                        "persistent": pool64.persistent, "fp32_over_fp64_batched": value / world / v64b,
+                        "sweep_roofline": sweep_roofline(v64b, "adj", 64, sweeps_per_measure=S),
+                        "what": "the same 384 chains in one FP64 pool, S sweeps + measurement per step "
+                                "(CUDA events, L2 flushed between steps)"}
+        pool64.close()
+
+    # chain completion latency.  In the batched form every chain finishes
+    # its 1000 sweeps at the same time, one ensemble step time x 100; the
+    # served stream (continuous batching, requests of C5's mix arriving at
+    # 1 per second, which one GPU sustains) gives the latency distribution
+    latency = None
+    if rank == 0 and not args.no_latency:
+        from su2higgs_gb300 import serve
+        t_chain = float(np.median(step_ms)) * 1e-3 * (1000 // S)
+        stream_req = serve.make_stream(args.latency_rate, args.latency_window, seed=replica_seed(4242, rank))
+        srv = serve.Server(gpu.Pool, gpu.Pool.chain_bytes, arena_bytes=int(8 << 30), max_chains=256,
+                           quantum=args.serve_quantum)
+        t0 = time.perf_counter()
+        res = srv.serve(stream_req, deadline=args.latency_window + args.latency_drain)
+        wall_l = time.perf_counter() - t0
+        srv.close()
+        lat_s = np.array([r.latency for r in res.values()]) if res else np.array([np.nan])
+        latency = {"batched_chain_completion_s": t_chain,
+                   "batched_what": f"every chain of the ensemble completes its 1000 sweeps together: "
+                                   f"{1000 // S} steps x the median step time",
+                   "served": {"arrival_rate_per_s": args.latency_rate, "arrival_window_s": args.latency_window,
+                              "requests": len(stream_req), "completed": len(res), "unfinished": srv.unfinished,
+                              "p50_latency_s": float(np.percentile(lat_s, 50)),
+                              "p99_latency_s": float(np.percentile(lat_s, 99)),
+                              "site_updates_per_s": srv.site_updates / wall_l,
+                              "what": "served stream of the C5 request mix (L 16-128, fundamental / adjoint / "
+                                      "SU(2)xU(1)+singlet, 500-5000 sweeps, 30% with a gradient flow), FP32"}}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         n, tcpu, used = cpu_sample_chains(specs)
@@ -829,27 +970,22 @@ def run_gpu_batched(args):
                          f"oracle C restatement in FP64, 1 thread ({tcpu:.1f} s)"}
 
     if rank == 0:
-        Ls = [p.L[0] for p, _, _ in specs]
         line = {
             "metric": METRIC, "value": value, "unit": "site-updates/s", "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": dev_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": args.workload, "content": "SU(2) + adjoint Higgs", "chains": nchains,
-                       "sites_total": sites, "sweeps_per_step": S, "sweeps_per_chain": S * (K + W),
-                       "sides": {str(L): Ls.count(L) for L in sorted(set(Ls))},
-                       "betasu2": list(workloads.ENSEMBLE_BETA), "msq_adj": list(workloads.ENSEMBLE_MSQ_ADJ),
-                       "lambda_adj": workloads.ENSEMBLE_LAMBDA_ADJ,
-                       "precision": "FP32 fields, FP64 reductions",
-                       "recipe": "1 link heatbath (3 directions x 2 parities) + 4 triplet overrelax + "
-                                 "1 triplet Metropolis (x 2 parities) per sweep; measure every chain each step",
-                       "l2": "fields 660 MB > L2; 256 MiB write between steps outside the step events",
-                       "parallelism": f"replicas x{world}", "graph": True,
-                       "sweep_mode": "persistent work-list kernel, S sweeps per launch" if persistent
-                       else "one launch per pass",
-                       "persist_tiles_per_item": pool.persist_tiles if persistent else None,
-                       "launch_variants": [int(v) for v in variants]},
+            "config": batched_config(args.workload, specs),
+            "step": {"sweeps_per_step": S, "sweeps_per_chain_run": S * (K + W),
+                     "precision": "FP32 fields, FP64 reductions",
+                     "l2": "fields 660 MB > L2; 256 MiB write between steps outside the step events",
+                     "parallelism": f"replicas x{world}", "graph": True,
+                     "sweep_mode": "persistent work-list kernel, S sweeps per launch" if persistent
+                     else "one launch per pass",
+                     "persist_tiles_per_item": pool.persist_tiles if persistent else None,
+                     "launch_variants": [int(v) for v in variants]},
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "fp64_plain": fp64,
-            "sweep_roofline": sweep_roofline(value / world, "adj", 32),
+            "fp64_batched": fp64_batched, "latency": latency,
+            "sweep_roofline": sweep_roofline(value / world, "adj", 32, sweeps_per_measure=S),
             # per step: the sweeps (persistent: one work-list kernel + the
             # sweep-counter increment; otherwise S graph replays of one
             # launch per pass) + measure + per-chain reduction
@@ -948,6 +1084,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end host-buffer measurement")
+    ap.add_argument("--no-latency", action="store_true", help="batched: skip the served latency leg")
+    ap.add_argument("--latency-rate", type=float, default=1.0, help="batched latency leg: arrivals per second")
+    ap.add_argument("--latency-window", type=float, default=20.0, help="batched latency leg: seconds of arrivals")
+    ap.add_argument("--latency-drain", type=float, default=20.0,
+                    help="batched latency leg: seconds after the last arrival")
     ap.add_argument("--sweeps-per-step", type=int, default=None,
                     help="batched: sweeps per step (default: the workload's 10; 1 for a profiler capture of one sweep)")
     ap.add_argument("--variants", default=None,

@@ -307,11 +307,15 @@ __device__ inline R localact_u1link(const Fields<R>& f, const Geom& g, const Cou
 }
 
 // ---------------------------------------------------------------------------
-// real root of a x^3 + b x^2 + c x + d (polysolve3, overrelax.c:14-34).
-// FP64: Cardano's formula in double (the reference uses long double; the
-// difference is a rounding effect, far below 1e-12 for these cubics).
-// FP32: the same formula followed by two Newton steps on the cubic, which is
-// well conditioned near its root even where Cardano's form is not.
+// real root of a x^3 + b x^2 + c x + d (polysolve3, overrelax.c:14-34):
+// Cardano's formula followed by Newton steps on the cubic (one in FP64, two
+// in FP32).  The reference evaluates Cardano's formula in long double: the
+// leading coefficient of these cubics is lambda/4 (~5e-4), so the formula
+// cancels, and in double it lands up to ~1e-11 away (relative) from the
+// long-double root.  The cubic itself is well conditioned near its root
+// (the linear coefficient dominates), so a Newton step brings the double
+// result to the root within rounding, matching the reference's long-double
+// value to ~1e-15.
 // ---------------------------------------------------------------------------
 template <typename R>
 __device__ inline R polysolve3(R a, R b, R c, R d, int* fallback) {
@@ -322,13 +326,11 @@ __device__ inline R polysolve3(R a, R b, R c, R d, int* fallback) {
     R A = (R)0.5 * (del1 + a * msqrt((R)(-27) * discr));
     A = mcbrt(A);
     x = -(b + A + (b * b - (R)3 * a * c) / A) / ((R)3 * a);
-    if (sizeof(R) == 4) {
 #pragma unroll
-      for (int it = 0; it < 2; it++) {
-        R fx = ((a * x + b) * x + c) * x + d;
-        R dfx = ((R)3 * a * x + (R)2 * b) * x + c;
-        x -= fx / dfx;
-      }
+    for (int it = 0; it < (sizeof(R) == 4 ? 2 : 1); it++) {
+      R fx = ((a * x + b) * x + c) * x + d;
+      R dfx = ((R)3 * a * x + (R)2 * b) * x + c;
+      x -= fx / dfx;
     }
   } else {
     x = b / a;

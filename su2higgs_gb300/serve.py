@@ -21,9 +21,12 @@ measurement at the end.  The reference runs one chain per process
 A chain's results do not depend on the other chains or on the quanta: its
 random numbers are keyed by its seed, chain id, sweep and site.
 
-Chains start cold: unit links, zero U(1) angles and scalars (setfields,
+A chain starts cold -- unit links, zero U(1) angles and scalars (setfields,
 init.c:92-110, with the initial scalar values phi0 = sigma0 = singlet0 = 0),
-so no host field traffic is needed to admit one.
+so no host field traffic is needed to admit it -- unless its request carries
+a starting configuration (`start`: FP64 host fields in the reference's
+lattice-file layout, as a loaded checkpoint, load_lattice checkpoint.c:133-214),
+which is uploaded into the chain's slot when it is admitted.
 """
 import collections
 import concurrent.futures
@@ -56,6 +59,9 @@ class Request:
     betasu2: float
     msq: float
     seed: int
+    # optional starting configuration: {field name: FP64 host array} (names
+    # link, u1, d0, d1, trip, sing; absent fields start cold)
+    start: dict = None
 
     def params(self, precision=32):
         kw = dict(precision=precision, betasu2=self.betasu2)
@@ -160,11 +166,14 @@ class Server:
         while self.waiting:
             req = self.waiting.popleft()
             p = req.params(self.precision)
+            pool = self.pool(req.content)
             try:
-                slot = self.pool(req.content).add(p, seed=req.seed, chain=req.rid)
+                slot = pool.add(p, seed=req.seed, chain=req.rid)
             except CapacityError:
                 still.append(req)
                 continue
+            if req.start:
+                pool.upload(slot, **req.start)
             self.live[req.content][slot] = _Live(req, slot, t, p)
         self.waiting = still
 

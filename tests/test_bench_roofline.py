@@ -52,3 +52,21 @@ def test_per_pass_roofline_picks_the_largest_share(bench):
     assert r["algorithmic_bytes_per_launch"] == pytest.approx(16.5 * 4 * 1000)
     assert r["avg_launch_ms"] == pytest.approx(0.16)
     assert sum(r["shares"].values()) == pytest.approx(1.0)
+
+
+def test_sweep_roofline_counts_the_measurement_at_its_cadence(bench):
+    # adjoint FP32: 6 x 17 + 10 x 16.5 = 267 reals per sweep, 15 per measurement
+    peak, _ = bench.measured_peaks()
+    every = bench.sweep_roofline(1e9, "adj", 32)
+    per10 = bench.sweep_roofline(1e9, "adj", 32, sweeps_per_measure=10)
+    assert every["bytes_per_site_update"] == pytest.approx((267 + 15) * 4)
+    assert per10["bytes_per_site_update"] == pytest.approx((267 + 1.5) * 4)
+    assert per10["frac"] == pytest.approx(1e9 * 1074 / 1e9 / peak)
+
+
+def test_batched_config_is_the_same_on_both_arms(bench):
+    from su2higgs_gb300 import workloads
+    a = bench.batched_config("batched384_adj_f32", workloads.batched_ensemble(384))
+    b = bench.batched_config("batched384_adj_f32", workloads.batched_ensemble(384, precision=64))
+    assert a == b
+    assert a["chains"] == 384 and a["sites_total"] == 11011520

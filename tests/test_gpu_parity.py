@@ -66,14 +66,22 @@ def test_layout_table_digests(gpu):
         lat.close()
 
 
-# (fixture key, site_values name, relative-error floor): the staples can
-# cancel to small values, so their errors are taken against a floor of 1e-3
-SITE_KEYS = [("link_staple", "link_staple", 1e-3), ("wilson_staple", "wilson_staple", 1e-3),
-             ("localact_su2link", "localact_su2link", 1e-300), ("localact_u1link", "localact_u1link", 1e-300),
-             ("staple_doublet", "staple_doublet", 1e-3), ("localact_doublet", "localact_doublet", 1e-300),
-             ("localact_singlet", "localact_singlet", 1e-300), ("or_doublet", "or_doublet", 1e-3),
-             ("or_doublet1", "or_doublet1", 1e-3), ("or_triplet", "or_triplet", 1e-3),
-             ("or_singlet", "or_singlet", 1e-3)]
+# per-site values: (fixture key, vector width or 0 for a scalar).  A
+# vector value (a staple of one direction, a proposed doublet or triplet) is
+# compared relative to its own length at that site, a scalar relative to
+# itself.
+SITE_KEYS = [("link_staple", 4), ("wilson_staple", 4), ("localact_su2link", 0), ("localact_u1link", 0),
+             ("staple_doublet", 4), ("localact_doublet", 0), ("localact_singlet", 0), ("or_doublet", 4),
+             ("or_doublet1", 4), ("or_triplet", 3), ("or_singlet", 0)]
+
+
+def site_rel_err(got, want, width):
+    if not width:
+        from native import rel_err
+        return rel_err(got, want)
+    g = np.asarray(got).reshape(-1, width)
+    w = np.asarray(want).reshape(-1, width)
+    return float(np.max(np.max(np.abs(g - w), axis=1) / np.maximum(np.linalg.norm(w, axis=1), 1e-300)))
 
 
 @pytest.mark.parametrize("name", names("sites_"))
@@ -82,18 +90,23 @@ def test_site_values_match_reference(gpu, name):
     computed on the device by the functions the update kernels call, on a
     configuration of the reference's own run: within 1e-12 relative of the
     reference's FP64 values (staples.c:84-302, su2u1.c:166-723,
-    overrelax.c:54-417)."""
-    from native import rel_err
+    overrelax.c:54-417).  The proposals come from the cubic root of
+    polysolve3, which the reference takes by Cardano's formula in long
+    double and the device refines by a Newton step to the root itself: the
+    reference's own root is up to ~5e-12 (relative) from the exact one where
+    the formula cancels, which moves a proposed field by ~4e-13 of its length
+    at most on these configurations."""
     d = load(name)
     p = params_of(d)
     lat = gpu.Lattice(p)
     upload(lat, fields_of(d, p, "in_"))
     checked = 0
-    for key, what, floor in SITE_KEYS:
+    for key, width in SITE_KEYS:
         if key not in d:
             continue
-        got = lat.site_values(what)
-        err = rel_err(got, d[key], floor)
+        got = lat.site_values(key)
+        err = site_rel_err(got, d[key], width)
+        print(f"{name} {key}: max relative difference {err:.2e}")
         assert err < RTOL, (key, err)
         checked += 1
     assert checked >= 3

@@ -45,3 +45,31 @@ def test_served_results_alone_equal_in_mix():
         else:
             assert alone.flow_rows is None and m.flow_rows is None
         assert np.all(np.isfinite(m.sums)) and m.counters[0] == r.sweeps * 3 * r.L ** 3
+
+
+def test_served_request_with_a_starting_configuration():
+    """A request that carries its starting fields gives the same results as
+    a pool chain uploaded with them and run alone (and different results from
+    the cold start)."""
+    from native import hot_fields
+    from su2higgs_gb300 import gpu
+    gpu.lib()
+    r0 = serve.make_stream(rate=100, duration=0.2, seed=33, sides=(8,), sweeps=(30, 30), flow_fraction=0.0)[0]
+    p = r0.params(32)
+    f = hot_fields(p, seed=77, phi_mean=0.5)
+    start = {n: getattr(f, n) for n in ("link", "u1", "d0", "d1", "trip", "sing") if getattr(f, n) is not None}
+    req = serve.Request(**{**r0.__dict__, "arrival": 0.0, "start": start})
+    srv = make(gpu, quantum=8)
+    got = srv.serve([req])[req.rid]
+    srv.close()
+    pool = gpu.Pool(p, arena_bytes=16 << 20, max_chains=2)
+    slot = pool.add(p, seed=req.seed, chain=req.rid)
+    pool.upload(slot, **start)
+    pool.run(req.sweeps)
+    want = pool.measure()[slot]
+    pool.close()
+    assert np.array_equal(got.sums, want)
+    cold_srv = make(gpu, quantum=8)
+    cold = cold_srv.serve([serve.Request(**{**r0.__dict__, "arrival": 0.0})])[req.rid]
+    cold_srv.close()
+    assert not np.array_equal(cold.sums, got.sums)

@@ -219,10 +219,16 @@ def test_multicanonical_orderparam_distribution(gpu, precision, content):
 
 
 def _starts(p, n, seed, broken=0.0, **kw):
+    """Start configurations: hot (Haar links, normal scalars), or, with
+    `broken`, cold links and the triplet aligned at `broken` along its first
+    component (plus noise): a broken-phase start without monopoles, which a
+    hot start can trap in the Higgs phase as a frozen monopole pair."""
     out = []
     for k in range(n):
         f = hot_fields(p, seed=seed + k, **kw)
         if broken and f.trip is not None:
+            f.link[:] = 0.0
+            f.link[..., 0] = 1.0
             f.trip[:, 0] += broken
         out.append({n_: getattr(f, n_) for n_ in ("link", "u1", "d0", "d1", "trip", "sing")})
     return out
@@ -231,12 +237,12 @@ def _starts(p, n, seed, broken=0.0, **kw):
 # SU(2) + adjoint Higgs at couplings of the batched ensemble (beta in [6, 12],
 # m^2_adj in [-0.3, 0.1], lambda_adj 0.005), one point on each side of the
 # transition on 8^3: beta 12, m^2 -0.3 started in the broken phase (Tr Sigma^2
-# ~ 23, no monopoles), beta 8, m^2 0.1 in the symmetric phase (Tr Sigma^2 ~
+# ~ 23.5, no monopoles), beta 8, m^2 0.1 in the symmetric phase (Tr Sigma^2 ~
 # 0.3).  Observables of measure.c:110-174: plaquette, Tr Sigma^2,
 # hopping_Sigma, |magnetic charge| density.
 ADJ_POINTS = {
-    "broken": dict(betasu2=12.0, msq_triplet=-0.3, b4=0.005, broken=6.8),
-    "symmetric": dict(betasu2=8.0, msq_triplet=0.1, b4=0.005, broken=0.0),
+    "broken": dict(betasu2=12.0, msq_triplet=-0.3, b4=0.005, broken=6.8, trip_sigma=0.1),
+    "symmetric": dict(betasu2=8.0, msq_triplet=0.1, b4=0.005, broken=0.0, trip_sigma=0.3),
 }
 
 
@@ -250,10 +256,11 @@ def test_adjoint_fp32_observables_match_oracle(gpu, point):
     import chains
     kw = dict(ADJ_POINTS[point])
     broken = kw.pop("broken")
+    trip_sigma = kw.pop("trip_sigma")
     L = (8, 8, 8)
     p32 = abi.make_params("adj", L=L, precision=32, **kw)
     p64 = abi.make_params("adj", L=L, precision=64, **kw)
-    starts = _starts(p64, 8, 900, broken=broken, trip_sigma=0.3)
+    starts = _starts(p64, 8, 900, broken=broken, trip_sigma=trip_sigma)
     n_therm, n_gpu, n_orc = 400, 4000, 2000
     orc = chains.oracle_chains("adj", L, kw, starts[:4], 303, n_therm, n_orc)
     g32 = chains.pool_chains(gpu, p32, starts, 101, n_therm, n_gpu, persistent=True)

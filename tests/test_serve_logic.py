@@ -60,6 +60,9 @@ class FakePool:
         self.log.append(("add", chain, self.clock()))
         return slot
 
+    def upload(self, slot, **fields):
+        self.log.append(("upload", self.chains[slot][3], tuple(sorted(fields))))
+
     def remove(self, slot):
         self.log.append(("remove", self.chains[slot][3], self.clock()))
         del self.chains[slot]
@@ -166,3 +169,20 @@ def test_stream_statistics():
     assert set(r.L for r in s) == set(serve.SIDES)
     assert 0.27 < np.mean([r.flow for r in s]) < 0.33
     assert min(r.sweeps for r in s) >= 500 and max(r.sweeps for r in s) <= 5000
+
+
+def test_requests_with_a_starting_configuration_are_uploaded_at_admission():
+    stream = serve.make_stream(rate=20, duration=1.0, seed=9, sides=(8,), sweeps=(50, 60), flow_fraction=0.0)
+    start = {"link": np.zeros((512, 3, 4))}
+    stream = [serve.Request(**{**r.__dict__, "start": start if r.rid % 2 == 0 else None}) for r in stream]
+    srv, clock, log = make_server(arena=1 << 30)
+    res = srv.serve(stream)
+    srv.close()
+    assert sorted(res) == [r.rid for r in stream]
+    uploads = [e for e in log if e[0] == "upload"]
+    assert sorted(e[1] for e in uploads) == [r.rid for r in stream if r.rid % 2 == 0]
+    assert all(e[2] == ("link",) for e in uploads)
+    # each upload comes right after its chain's admission
+    for k, e in enumerate(log):
+        if e[0] == "upload":
+            assert log[k - 1][0] == "add" and log[k - 1][1] == e[1]
