@@ -94,7 +94,7 @@ static void p_orderparam(const void* f, const Geom& g, int parity, int op, doubl
 static void p_restore(int field, const void* f, const MucaDev* m, const void* backup, int h, int64_t lo, int64_t hi,
                       cudaStream_t st) {
   if (hi <= lo) return;
-  unsigned nb = nblk(hi - lo, 256);
+  unsigned nb = std::min<unsigned>(nblk(hi - lo, 256), 304);
   if (field == 0) k_muca_restore<R, 0><<<nb, 256, 0, st>>>(*(const Fields<R>*)f, m, backup, h, lo, hi);
   else k_muca_restore<R, 1><<<nb, 256, 0, st>>>(*(const Fields<R>*)f, m, backup, h, lo, hi);
 }

@@ -735,6 +735,9 @@ __device__ inline double orderparam_site(const Fields<R>& f, int op, int i) {
 // ---------------------------------------------------------------------------
 // half-sweep kernels
 // ---------------------------------------------------------------------------
+struct PassArgs;
+__device__ inline void muca_fused_finish(const PassArgs& a, double s);
+
 struct PassArgs {
   Geom g;
   CoupT<double> cpd;  // couplings for FP64 kernels
@@ -750,6 +753,13 @@ struct PassArgs {
   double* partials;         // per-block order-parameter sums (or null)
   unsigned long long* ctr;  // device counters
   int* err;                 // device error flag
+  // the multicanonical check decided inside the pass (muca_fused_finish):
+  // the weight (null: no decision in this launch), arrival counters, the
+  // check's number and the volume the order parameter is divided by
+  MucaDev* muca;
+  unsigned* arrive;
+  uint32_t check;
+  double vol;
 };
 
 template <typename R>
@@ -839,7 +849,8 @@ __global__ void __launch_bounds__(BS, MINB) k_scalar(Fields<R> f, PassArgs a) {
   warp_count(a.ctr + 23, fb);
   if (a.partials) {
     double s = block_sum(opv);
-    if (threadIdx.x == 0) a.partials[blockIdx.x] = s;
+    if (a.muca) muca_fused_finish(a, s);
+    else if (threadIdx.x == 0) a.partials[blockIdx.x] = s;
   }
 }
 
@@ -854,16 +865,19 @@ __global__ void __launch_bounds__(BLOCK) k_orderparam(Fields<R> f, Geom g, int p
 }
 
 // restore a block of the parity from the backup if the last check rejected
+// (a small grid striding over the block: when the check accepted, which is
+// the common case, the launch is over as soon as its few blocks have read
+// the flag)
 template <typename R, int FIELD>
 __global__ void k_muca_restore(Fields<R> f, const MucaDev* m, const void* backup, int h, int lo, int hi) {
   if (m->last_accept) return;
-  int i = lo + (int)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= hi) return;
-  if (FIELD == 0) {
-    php(f, h)[i] = ((const V4<R>*)backup)[i];
-  } else {
-    const R* b = (const R*)backup;
-    f.trip[0][i] = b[3 * i]; f.trip[1][i] = b[3 * i + 1]; f.trip[2][i] = b[3 * i + 2];
+  for (int i = lo + (int)blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += (int)(gridDim.x * blockDim.x)) {
+    if (FIELD == 0) {
+      php(f, h)[i] = ((const V4<R>*)backup)[i];
+    } else {
+      const R* b = (const R*)backup;
+      f.trip[0][i] = b[3 * i]; f.trip[1][i] = b[3 * i + 1]; f.trip[2][i] = b[3 * i + 2];
+    }
   }
 }
 
@@ -997,23 +1011,11 @@ __device__ inline void muca_update_slow(MucaDev* w) {
   for (int i = 0; i < n; i++) w->W[i] = wold[i];
 }
 
-#ifdef SU2_WITH_GLOBAL
-// muca_check (update.c:13-30): total of the parity sums, weight difference,
-// global draw (site 0xffffffff, block = check), accept/reject, hits and
-// weight recursion.  Partial sums are added in a fixed order.
-__global__ void k_muca_decide(MucaDev* w, const double* partials, int np, double vol, int parity, RngKey rk,
-                              uint32_t pass, uint32_t check, unsigned long long* ctr) {
-  __shared__ double red[256];
-  double v = 0.0;
-  for (int k = threadIdx.x; k < np; k += blockDim.x) v += partials[k];
-  red[threadIdx.x] = v;
-  __syncthreads();
-  for (int s = blockDim.x >> 1; s > 0; s >>= 1) {
-    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
-    __syncthreads();
-  }
-  if (threadIdx.x != 0) return;
-  double tot = red[0] / vol;
+// muca_check (update.c:13-30) once the parity's order parameter `tot` is
+// known: weight difference, global draw (site 0xffffffff, block = check),
+// accept/reject, hits and weight recursion.  One thread.
+__device__ inline void muca_decide_value(MucaDev* w, double tot, int parity, const RngKey& rk, uint32_t pass,
+                                         uint32_t check, unsigned long long* ctr) {
   double old = w->param_value[0] + w->param_value[1];
   w->param_value[parity] = tot;
   double nw = tot + w->param_value[1 - parity];
@@ -1035,6 +1037,85 @@ __global__ void k_muca_decide(MucaDev* w, const double* partials, int np, double
   w->last_accept = accept;
   ctr[20] += 1;
   ctr[21] += accept;
+}
+
+// sum of x[0..n) by the block's first 64 threads (blockDim.x >= 64) in a
+// fixed order -- lane l adds x[l], x[l + 64], ..., then a tree over the 64
+// lane sums -- valid in thread 0.  The loads bypass L1: the values were
+// written by other blocks of the same launch.
+__device__ inline double fixed_sum64(const double* x, int n) {
+  __shared__ double red[64];
+  if (threadIdx.x < 64) {
+    double v = 0.0;
+    for (int k = threadIdx.x; k < n; k += 64) v += __ldcg(x + k);
+    red[threadIdx.x] = v;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int h = 32; h > 0; h >>= 1) {
+    if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+    __syncthreads();
+  }
+  return red[0];
+}
+
+// The multicanonical check of a whole parity decided by the update launch
+// itself, without a kernel of its own: every block leaves its order-parameter
+// sum in partials[block]; the last block to finish in each chunk of
+// MUCA_CHUNK blocks adds the chunk's sums (fixed order) into
+// partials[blocks + chunk]; the last chunk to finish adds the chunk sums
+// (fixed order) and decides.  Arrival counts are atomic adds after a fence,
+// and each count is put back to 0 by the block that completes it, ready for
+// the next launch (and for graph replays).
+constexpr int MUCA_CHUNK = 64;
+constexpr int MUCA_MAX_CHUNKS = 3071;  // arrival counters after the chunk count (host buffer size)
+__device__ inline void muca_fused_finish(const PassArgs& a, double s) {
+  __shared__ int s_last;
+  const unsigned nb = gridDim.x, b = blockIdx.x;
+  const unsigned chunk = b / MUCA_CHUNK, c0 = chunk * MUCA_CHUNK;
+  const unsigned csize = min(nb - c0, (unsigned)MUCA_CHUNK);
+  const unsigned nchunks = (nb + MUCA_CHUNK - 1) / MUCA_CHUNK;
+  if (threadIdx.x == 0) {
+    a.partials[b] = s;
+    __threadfence();
+    s_last = atomicAdd(a.arrive + 1 + chunk, 1u) == csize - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  const double cs = fixed_sum64(a.partials + c0, (int)csize);
+  if (threadIdx.x == 0) {
+    a.arrive[1 + chunk] = 0;
+    a.partials[nb + chunk] = cs;
+    __threadfence();
+    s_last = atomicAdd(a.arrive, 1u) == nchunks - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  const double tot = fixed_sum64(a.partials + nb, (int)nchunks);
+  if (threadIdx.x == 0) {
+    a.arrive[0] = 0;
+    muca_decide_value(a.muca, tot / a.vol, a.parity, a.rk, a.pass, a.check, a.ctr);
+  }
+}
+
+#ifdef SU2_WITH_GLOBAL
+// muca_check (update.c:13-30) as a kernel of its own, for checks that cover
+// part of a parity: the partial sums added in a fixed order, then the
+// decision.  One block.
+__global__ void k_muca_decide(MucaDev* w, const double* partials, int np, double vol, int parity, RngKey rk,
+                              uint32_t pass, uint32_t check, unsigned long long* ctr) {
+  __shared__ double red[256];
+  double v = 0.0;
+  for (int k = threadIdx.x; k < np; k += blockDim.x) v += partials[k];
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int s = blockDim.x >> 1; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) muca_decide_value(w, red[0] / vol, parity, rk, pass, check, ctr);
 }
 
 // calc_orderparam for the host API: store the parity sum

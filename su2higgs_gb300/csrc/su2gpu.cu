@@ -99,6 +99,11 @@ struct DevBuf {
   }
 };
 
+// device words of a context: counters, error flag, sweep number, flow
+// marker, and from byte 4096 the arrival counts of a multicanonical check
+// decided inside its update launch (1 + MUCA_MAX_CHUNKS words)
+constexpr size_t CTRBUF_BYTES = 4096 + 4 * (1 + MUCA_MAX_CHUNKS) + 4;
+
 struct su2gpu_ctx {
   su2gpu_params p;
   int prec, nh, has_t, has_s, has_u1;
@@ -119,6 +124,7 @@ struct su2gpu_ctx {
   int* d_err = nullptr;
   uint32_t* d_sweep = nullptr;
   unsigned long long* d_fz = nullptr;
+  unsigned* d_arrive = nullptr;  // arrival counts of the multicanonical check decided in the pass
   int64_t host_tot[SU2GPU_NCOUNTERS] = {0};
   int var[5] = {0, 0, 0, 0, 0};  // launch-shape variant per kernel kind (link, U(1), doublet, triplet, singlet)
   int random_sweeps = 0;         // the reference's random_sweeps mode: the order changes every sweep
@@ -262,7 +268,7 @@ static int create_ctx(const su2gpu_params* p, void* borrowed, const void* copy_f
     c->borrowed = true;
   }
   if ((!borrowed && (rc = c->fields.ensure(field_bytes(p, V)))) ||
-      (rc = c->ctrbuf.ensure(4096)) ||
+      (rc = c->ctrbuf.ensure(CTRBUF_BYTES)) ||
       (rc = c->partials.ensure((size_t)(nblk(V, BLOCK) + 2) * NSUMS * 8)) ||
       (rc = c->sums.ensure(NSUMS * 8))) {
     su2gpu_destroy(c);
@@ -274,6 +280,7 @@ static int create_ctx(const su2gpu_params* p, void* borrowed, const void* copy_f
   c->d_err = (int*)((char*)c->ctrbuf.p + 512);
   c->d_sweep = (uint32_t*)((char*)c->ctrbuf.p + 1024);
   c->d_fz = (unsigned long long*)((char*)c->ctrbuf.p + 1536);
+  c->d_arrive = (unsigned*)((char*)c->ctrbuf.p + 4096);
   if ((!borrowed && !copy_from && cudaMemsetAsync(c->fields.p, 0, c->fields.n, c->st) != cudaSuccess) ||
       (copy_from && cudaMemcpyAsync(c->fields.p, copy_from, c->fields.n, cudaMemcpyDeviceToDevice, c->st) != cudaSuccess) ||
       cudaMemsetAsync(c->ctrbuf.p, 0, c->ctrbuf.n, c->st) != cudaSuccess) {
@@ -512,10 +519,19 @@ static int scalar_pass(su2gpu_ctx* c, const PassArgs& base, int field, int h, in
   RngKey rk = base.rk;
   a.backup = c->backup.p;
   a.op = op;
+  // a check over the whole parity is decided by the update launch itself
+  // (muca_fused_finish) when its blocks fit the arrival counters
+  const bool in_pass = fused && (N + 63) / 64 <= (int64_t)MUCA_CHUNK * MUCA_MAX_CHUNKS;
   for (int64_t k = 0; k < m; k++) {
     a.t_lo = k * interval;
     a.t_hi = (k + 1) * interval;
     a.partials = fused ? partials : nullptr;
+    if (in_pass) {
+      a.muca = c->d_muca;
+      a.arrive = c->d_arrive;
+      a.check = check++;
+      a.vol = vol;
+    }
     unsigned nb = c->ops->scalar(c->var[2 + field], field, c->F(), a, c->st);
     CKL();
     unsigned np = nb;
@@ -525,12 +541,16 @@ static int scalar_pass(su2gpu_ctx* c, const PassArgs& base, int field, int h, in
       c->launches++;
       CKL();
     }
-    launch_muca_decide(c->d_muca, partials, (int)np, vol, par, rk, pass, check++, c->d_ctr, c->st);
-    CKL();
+    if (!in_pass) {
+      launch_muca_decide(c->d_muca, partials, (int)np, vol, par, rk, pass, check++, c->d_ctr, c->st);
+      c->launches++;
+      CKL();
+    }
     c->pops->restore(field, c->F(), c->d_muca, c->backup.p, h, par * N + a.t_lo, par * N + a.t_hi, c->st);
-    c->launches += 3;
+    c->launches += 2;
     CKL();
   }
+  a.muca = nullptr;
   if (N % cps != 0) {
     int64_t lo = m * interval, hi = N, rlo = lo, rhi = hi;
     if (lo < hi) {
