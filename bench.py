@@ -982,6 +982,8 @@ def run_gpu_batched(args):
                      "sweep_mode": "persistent work-list kernel, S sweeps per launch" if persistent
                      else "one launch per pass",
                      "persist_tiles_per_item": pool.persist_tiles if persistent else None,
+                     "persist_shape": ({"shape": pool.persist_shape[0], "threads": pool.persist_shape[1],
+                                        "blocks_per_sm": pool.persist_shape[2]} if persistent else None),
                      "launch_variants": [int(v) for v in variants]},
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "fp64_plain": fp64,
             "fp64_batched": fp64_batched, "latency": latency,

@@ -443,6 +443,15 @@ int su2gpu_pool_get_persistent(su2gpu_pool* pool, int32_t* on);
  * tiles per pass, or timed by su2gpu_pool_autotune (4, 6, 8, 12 or 16) when
  * the pool sweeps persistently. */
 int su2gpu_pool_get_persist_tiles(su2gpu_pool* pool, int32_t* tiles);
+/* Launch shape of the persistent sweep: 0 (128 threads, the register budget
+ * of 8 resident blocks per SM in FP32, 4 in FP64) or 1 (128 threads, 5 / 3
+ * blocks: more registers per thread, fewer warps).  Both run the same
+ * compiled per-site code and give the same fields bit for bit;
+ * su2gpu_pool_autotune times both with every item size and keeps the
+ * fastest pair.  get: the shape in effect, its threads and resident blocks
+ * per SM (threads, blocks_per_sm may be NULL). */
+int su2gpu_pool_set_persist_shape(su2gpu_pool* pool, int32_t shape);
+int su2gpu_pool_get_persist_shape(su2gpu_pool* pool, int32_t* shape, int32_t* threads, int32_t* blocks_per_sm);
 /* Check of the persistent kernel's bounded dependency wait: runs it on a
  * work list whose dependencies are never met (pass 0 left out), so every
  * wait gives up after spin_limit polls; the chains' fields and sweep

@@ -351,10 +351,14 @@ struct ZeroRng {
 };
 // heatbath_su2link (heatbath.c:15-124): Kennedy-Pendleton; the uniforms are
 // drawn in the reference's order (4 per trial, 3 per sphere trial, 1 for the
-// triplet accept/reject).
+// triplet accept/reject).  The first trial's four are drawn before the staple
+// is gathered: the same values in the same order (each site's stream is
+// positional), with the generator's arithmetic free to run while the loads
+// are in flight.  The other local updates draw early in the same way.
 template <typename R, int CC>
 __device__ inline int heatbath(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i, int mu,
                                SiteRng<R>& rng, int* kpcap, int* err) {
+  R u0 = rng.uni(), u1 = rng.uni(), u2 = rng.uni(), u3 = rng.uni();  // the first trial's
   Q<R> old{};
   R oldact = 0;
   if (HAS(C_T)) {
@@ -368,12 +372,18 @@ __device__ inline int heatbath(const Fields<R>& f, const Geom& g, const CoupT<R>
   R a0, r1, r2, r3, d;
   int loop = 1;
   do {
-    r1 = -mlog((R)1 - rng.uni()) / a;
-    r2 = -mlog((R)1 - rng.uni()) / a;
-    r3 = mcos2pi(rng.uni());
+    if (loop > 1) {
+      u0 = rng.uni();
+      u1 = rng.uni();
+      u2 = rng.uni();
+      u3 = rng.uni();
+    }
+    r1 = -mlog((R)1 - u0) / a;
+    r2 = -mlog((R)1 - u1) / a;
+    r3 = mcos2pi(u2);
     r3 *= r3;
     d = r1 * r3 + r2;
-    r3 = (R)1 - rng.uni();
+    r3 = (R)1 - u3;
     loop++;
   } while (r3 * r3 > (R)1 - (R)0.5 * d && loop <= 200);
   R rad;
@@ -443,6 +453,15 @@ __device__ inline int metro_accept(R diff, SiteRng<R>& rng) {
   if (diff > (R)0 && mexp(-diff) > rng.uni()) return 1;
   return 0;
 }
+// the same with the decision's uniform u drawn beforehand (it is the site's
+// last draw of the pass, so drawing it whatever diff turns out to be changes
+// no other draw)
+template <typename R>
+__device__ inline int metro_accept_u(R diff, R u) {
+  if (diff < (R)0) return 1;
+  if (diff > (R)0 && mexp(-diff) > u) return 1;
+  return 0;
+}
 
 // metro_su2link (metropolis.c:15-41) with random_su2link (init.c:43-58)
 template <typename R, int CC>
@@ -481,13 +500,14 @@ __device__ inline int metro_u1(const Fields<R>& f, const Geom& g, const CoupT<R>
 template <typename R, int CC>
 __device__ inline int metro_doublet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
                                     int h, SiteRng<R>& rng) {
+  const R d0 = rng.uni() - (R)0.5, d1 = rng.uni() - (R)0.5, d2 = rng.uni() - (R)0.5, d3 = rng.uni() - (R)0.5;
   Q<R> old = ld4<R>(php(f, h), i);
   R a0 = localact_doublet<R, CC>(f, g, cp, c, i, h);
   Q<R> nw = old;
-  nw.a += (R)1 * (rng.uni() - (R)0.5);
-  nw.b += (R)1 * (rng.uni() - (R)0.5);
-  nw.c += (R)1 * (rng.uni() - (R)0.5);
-  nw.d += (R)1 * (rng.uni() - (R)0.5);
+  nw.a += (R)1 * d0;
+  nw.b += (R)1 * d1;
+  nw.c += (R)1 * d2;
+  nw.d += (R)1 * d3;
   st4<R>(php(f, h), i, nw);
   R a1 = localact_doublet<R, CC>(f, g, cp, c, i, h);
   if (metro_accept(a1 - a0, rng)) return 1;
@@ -499,6 +519,7 @@ __device__ inline int metro_doublet(const Fields<R>& f, const Geom& g, const Cou
 template <typename R, int CC, typename RNG>
 __device__ inline int overrelax_doublet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
                                         RNG& rng, int* fallback) {
+  const R u = rng.uni();
   Q<R> s = staple_doublet<R, CC>(f, g, cp, c, i, 0);
   Q<R> p = ld4<R>(php(f, 0), i);
   R F = msqrt(s.a * s.a + s.b * s.b + s.c * s.c + s.d * s.d);
@@ -523,7 +544,7 @@ __device__ inline int overrelax_doublet(const Fields<R>& f, const Geom& g, const
   R newX = polysolve3<R>(C, C * X, cc + C * X * X, F + cc * X + C * X * X * X, fallback);
   R dV = F + (R)2 * B * X + (R)4 * C * (X * X * X + Ysq * X);
   R dVn = F + (R)2 * B * newX + (R)4 * C * (newX * newX * newX + Ysq * newX);
-  if (mabs(dV / dVn) >= rng.uni()) {
+  if (mabs(dV / dVn) >= u) {
     R k = (newX + X);
     st4<R>(php(f, 0), i, f32 ? Q<R>{-p.a + k * s.a * iF, -p.b + k * s.b * iF, -p.c + k * s.c * iF, -p.d + k * s.d * iF}
                              : Q<R>{-p.a + k * s.a / F, -p.b + k * s.b / F, -p.c + k * s.c / F, -p.d + k * s.d / F});
@@ -536,6 +557,7 @@ __device__ inline int overrelax_doublet(const Fields<R>& f, const Geom& g, const
 template <typename R, int CC, typename RNG>
 __device__ inline int overrelax_higgs2(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
                                        int h, RNG& rng, int* fallback) {
+  const R u = rng.uni();
   Q<R> s = staple_doublet<R, CC>(f, g, cp, c, i, h);
   Q<R> fv = ld4<R>(php(f, h), i);
   Q<R> H;
@@ -583,7 +605,7 @@ __device__ inline int overrelax_higgs2(const Fields<R>& f, const Geom& g, const 
   R Xn = polysolve3<R>(b4, b3 + b4 * X, b2 + b3 * X + b4 * X * X, b1 + b2 * X + b3 * X * X + b4 * X * X * X, fallback);
   R dV = (R)4 * b4 * X * X * X + (R)3 * b3 * X * X + (R)2 * b2 * X + b1;
   R dVn = (R)4 * b4 * Xn * Xn * Xn + (R)3 * b3 * Xn * Xn + (R)2 * b2 * Xn + b1;
-  if (mabs(dV / dVn) >= rng.uni()) {
+  if (mabs(dV / dVn) >= u) {
     st4<R>(php(f, h), i, Q<R>{fr[0] + sv[0] * (Xn - X), fr[1] + sv[1] * (Xn - X), fr[2] + sv[2] * (Xn - X),
                              fr[3] + sv[3] * (Xn - X)});
     return 1;
@@ -614,6 +636,7 @@ __device__ inline V3<R> staple_triplet(const Fields<R>& f, const Geom& g, const 
 template <typename R, int CC, typename RNG>
 __device__ inline int overrelax_triplet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
                                         RNG& rng, int* fallback) {
+  const R u = rng.uni();
   V3<R> s = staple_triplet(f, g, c, i);
   V3<R> t = ld3(f, i);
   R F = msqrt(s.x * s.x + s.y * s.y + s.z * s.z);
@@ -632,7 +655,7 @@ __device__ inline int overrelax_triplet(const Fields<R>& f, const Geom& g, const
   R newX = polysolve3<R>(C, C * X, cc + C * X * X, F + cc * X + C * X * X * X, fallback);
   R dV = F + (R)2 * B * X + (R)4 * C * (X * X * X + Ysq * X);
   R dVn = F + (R)2 * B * newX + (R)4 * C * (newX * newX * newX + Ysq * newX);
-  if (mabs(dV / dVn) >= rng.uni()) {
+  if (mabs(dV / dVn) >= u) {
     R k = newX + X;
     st3(f, i, f32 ? V3<R>{-t.x + k * s.x * iF, -t.y + k * s.y * iF, -t.z + k * s.z * iF}
                   : V3<R>{-t.x + k * s.x / F, -t.y + k * s.y / F, -t.z + k * s.z / F});
@@ -649,19 +672,23 @@ __device__ inline int overrelax_triplet(const Fields<R>& f, const Geom& g, const
 template <typename R, int CC>
 __device__ inline int metro_triplet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
                                     SiteRng<R>& rng) {
+  const R e0 = rng.uni() - (R)0.5, e1 = rng.uni() - (R)0.5, e2 = rng.uni() - (R)0.5;
+  // FP32: the decision's uniform is the fourth word of the same generator
+  // block, drawn with the proposal; FP64 draws it only when it is needed
+  const R ua = sizeof(R) == 4 ? rng.uni() : (R)0;
   V3<R> s = staple_triplet(f, g, c, i);
   V3<R> old = ld3(f, i);
   V3<R> nw = old;
-  nw.x += (R)1 * (rng.uni() - (R)0.5);
-  nw.y += (R)1 * (rng.uni() - (R)0.5);
-  nw.z += (R)1 * (rng.uni() - (R)0.5);
+  nw.x += (R)1 * e0;
+  nw.y += (R)1 * e1;
+  nw.z += (R)1 * e2;
   const R dx = nw.x - old.x, dy = nw.y - old.y, dz = nw.z - old.z;
   const R dsq = dx * (nw.x + old.x) + dy * (nw.y + old.y) + dz * (nw.z + old.z);
   const R ssq = (nw.x * nw.x + nw.y * nw.y + nw.z * nw.z) + (old.x * old.x + old.y * old.y + old.z * old.z);
   R B = (R)0.5 * (R)cp.msqT + (R)3;
   if (NHIGGS > 0) B += (R)0.5 * (R)cp.a2 * doubletsq(ld4<R>(php(f, 0), i));
   const R dS = dx * s.x + dy * s.y + dz * s.z + dsq * (B + (R)0.25 * (R)cp.b4 * ssq);
-  if (metro_accept(dS, rng)) {
+  if (sizeof(R) == 4 ? metro_accept_u(dS, ua) : metro_accept(dS, rng)) {
     st3(f, i, nw);
     return 1;
   }
@@ -682,6 +709,7 @@ __device__ inline R localact_singlet(const Fields<R>& f, const Geom& g, const Co
 template <typename R, int CC, typename RNG>
 __device__ inline int overrelax_singlet(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
                                         RNG& rng, int* fallback) {
+  const R u = rng.uni();
   R S = f.sing[i];
   R c1 = (R)cp.b1s;
 #pragma unroll
@@ -700,7 +728,7 @@ __device__ inline int overrelax_singlet(const Fields<R>& f, const Geom& g, const
   R Y = polysolve3<R>(c4, d2, d1, d0, fallback);
   R dV = c1 + (R)2 * c2 * S + (R)3 * c3 * S * S + (R)4 * c4 * S * S * S;
   R dVn = c1 + (R)2 * c2 * Y + (R)3 * c3 * Y * Y + (R)4 * c4 * Y * Y * Y;
-  if (mabs(dV / dVn) >= rng.uni()) {
+  if (mabs(dV / dVn) >= u) {
     f.sing[i] = Y;
     return 1;
   }
@@ -1012,14 +1040,57 @@ __device__ inline void muca_update_slow(MucaDev* w) {
 }
 
 // muca_check (update.c:13-30) once the parity's order parameter `tot` is
-// known: weight difference, global draw (site 0xffffffff, block = check),
-// accept/reject, hits and weight recursion.  One thread.
-__device__ inline void muca_decide_value(MucaDev* w, double tot, int parity, const RngKey& rk, uint32_t pass,
+// known, by a whole block (every thread calls it; blockDim.x >= 2): weight
+// difference, global draw (site 0xffffffff, block = check), accept/reject,
+// hits and weight recursion.  The weights of the new and the old value
+// (get_weight, multicanonical.c:350-379) are looked up with the bins tested
+// by all threads at once -- one pass of independent loads instead of a
+// binary search of dependent ones, which on the critical path of every
+// check cost more than the update itself.  The bin found is the one the
+// reference's binary search (whichbin, multicanonical.c:671-704) returns:
+// the unique bin with pos[b] < val < pos[b+1]; a value within 1e-12 of a bin
+// edge (where the search may stop at either neighbour) or in no bin takes
+// the sequential search.
+__device__ inline void muca_decide_block(MucaDev* w, double tot, int parity, const RngKey& rk, uint32_t pass,
                                          uint32_t check, unsigned long long* ctr) {
-  double old = w->param_value[0] + w->param_value[1];
+  __shared__ int s_bin[2], s_fuzzy[2];
+  __shared__ double s_W[2];
+  const double pv0 = w->param_value[0], pv1 = w->param_value[1];
+  const int bins = w->bins;
+  const double* pos = w->pos;
+  const double old = pv0 + pv1;
+  const double nw = tot + (parity ? pv0 : pv1);
+  if (threadIdx.x < 2) {
+    s_bin[threadIdx.x] = -1;
+    s_fuzzy[threadIdx.x] = 0;
+  }
+  __syncthreads();
+  for (int k = 1 + (int)threadIdx.x; k <= bins; k += (int)blockDim.x) {
+    const double cur = pos[k], nxt = pos[k + 1];
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      const double v = j ? old : nw;
+      if (v < nxt && v > cur) s_bin[j] = k;
+      if (fabs(v - cur) < 1e-12 || fabs(v - nxt) < 1e-12) s_fuzzy[j] = 1;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 2) {
+    const int j = threadIdx.x;
+    const double v = j ? old : nw;
+    double W;
+    if (v >= w->max) W = w->b[bins + 1];
+    else if (v < w->min) W = w->b[0];
+    else {
+      const int bin = (s_bin[j] < 0 || s_fuzzy[j]) ? muca_whichbin(w, v) : s_bin[j];
+      W = bin >= bins + 1 ? w->b[bins + 1] : w->b[bin] + w->slope[bin] * v;
+    }
+    s_W[j] = W;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
   w->param_value[parity] = tot;
-  double nw = tot + w->param_value[1 - parity];
-  double Wn = muca_get_weight(w, nw), Wo = muca_get_weight(w, old);
+  const double Wn = s_W[0], Wo = s_W[1];
   double u = philox_uniform53(rk.k0, rk.k1, GLOBAL_SITE, pass, check, *rk.sweep, rk.chain, 0);
   int accept = exp(-(Wn - Wo)) > u ? 1 : 0;
   if (w->mode != 0) {
@@ -1093,11 +1164,9 @@ __device__ inline void muca_fused_finish(const PassArgs& a, double s) {
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  const double tot = fixed_sum64(a.partials + nb, (int)nchunks);
-  if (threadIdx.x == 0) {
-    a.arrive[0] = 0;
-    muca_decide_value(a.muca, tot / a.vol, a.parity, a.rk, a.pass, a.check, a.ctr);
-  }
+  const double tot = fixed_sum64(a.partials + nb, (int)nchunks);  // the same value in every thread
+  if (threadIdx.x == 0) a.arrive[0] = 0;
+  muca_decide_block(a.muca, tot / a.vol, a.parity, a.rk, a.pass, a.check, a.ctr);
 }
 
 #ifdef SU2_WITH_GLOBAL
@@ -1115,7 +1184,7 @@ __global__ void k_muca_decide(MucaDev* w, const double* partials, int np, double
     if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
     __syncthreads();
   }
-  if (threadIdx.x == 0) muca_decide_value(w, red[0] / vol, parity, rk, pass, check, ctr);
+  muca_decide_block(w, red[0] / vol, parity, rk, pass, check, ctr);
 }
 
 // calc_orderparam for the host API: store the parity sum

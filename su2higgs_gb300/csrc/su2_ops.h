@@ -88,10 +88,14 @@ void launch_pool_next_sweep(uint32_t* const* sweeps, int n, cudaStream_t st, uin
 // (a PersistArgs) on `grid` blocks of `threads`; blocks_per_sm: its resident
 // blocks per SM.  pool_*: one pass over the tile table (nblocks tiles, built
 // for the variant's block size).
+// The persistent kernel comes in PERSIST_SHAPES launch shapes of `threads`
+// threads (shape 0: the register budget of launch variant 0, shape 1: that
+// of variant 1), which call the same per-tile functions as those variants.
+constexpr int PERSIST_SHAPES = 2;
 struct PoolOps {
   int threads;
-  void (*launch)(const void* args, unsigned grid, cudaStream_t st);
-  int (*blocks_per_sm)();
+  void (*launch)(int shape, const void* args, unsigned grid, cudaStream_t st);
+  int (*blocks_per_sm)(int shape);
   void (*pool_link)(int variant, const PoolArgs& a, unsigned nblocks, cudaStream_t st);
   void (*pool_u1)(int variant, const PoolArgs& a, unsigned nblocks, cudaStream_t st);
   void (*pool_scalar)(int variant, int field, const PoolArgs& a, unsigned nblocks, cudaStream_t st);

@@ -12,9 +12,12 @@ namespace su2 {
 
 using R = SU2_R;
 constexpr int CCI = SU2_CC;
-// the shape of launch variant 0: 128 threads, 8 (FP32) / 4 (FP64) resident
-// blocks per SM asked of the compiler
+// the persistent kernel's shapes: those of launch variants 0 (128 threads,
+// 8 (FP32) / 4 (FP64) resident blocks per SM asked of the compiler) and 1
+// (128 threads, 5 / 3 blocks: more registers, fewer warps)
 constexpr int PBS = Variant<R, 0>::BS, PMB = Variant<R, 0>::MINB;
+constexpr int PMB1 = Variant<R, 1>::MINB;
+static_assert(Variant<R, 1>::BS == PBS, "persistent shapes share the tile size");
 
 template <int V>
 static void lp_link_v(const PoolArgs& a, unsigned nb, cudaStream_t st) {
@@ -64,15 +67,18 @@ static void lp_scalar(int v, int field, const PoolArgs& a, unsigned nb, cudaStre
     default: lp_scalar_v<0>(field, a, nb, st);
   }
 }
-static void persist_launch(const void* args, unsigned grid, cudaStream_t st) {
-  if (grid) k_pool_persist<R, CCI, PBS, PMB><<<grid, PBS, 0, st>>>(*(const PersistArgs*)args);
+static void persist_launch(int shape, const void* args, unsigned grid, cudaStream_t st) {
+  if (!grid) return;
+  if (shape == 1) k_pool_persist<R, CCI, PBS, PMB1><<<grid, PBS, 0, st>>>(*(const PersistArgs*)args);
+  else k_pool_persist<R, CCI, PBS, PMB><<<grid, PBS, 0, st>>>(*(const PersistArgs*)args);
 }
 
-static int persist_blocks_per_sm() {
+static int persist_blocks_per_sm(int shape) {
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_pool_persist<R, CCI, PBS, PMB>, PBS, 0) != cudaSuccess)
-    return 0;
-  return n;
+  cudaError_t e = shape == 1
+                      ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_pool_persist<R, CCI, PBS, PMB1>, PBS, 0)
+                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_pool_persist<R, CCI, PBS, PMB>, PBS, 0);
+  return e == cudaSuccess ? n : 0;
 }
 
 const PoolOps SU2_PERSIST = {PBS, persist_launch, persist_blocks_per_sm, lp_link, lp_u1, lp_scalar};

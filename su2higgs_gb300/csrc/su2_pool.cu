@@ -126,7 +126,9 @@ struct su2gpu_pool {
   Buf segs;
   std::vector<int4> h_segs;  // (slot, t0, the chain's segment count, 0)
   std::vector<int> h_sfirst;
-  unsigned persist_grid = 0;
+  unsigned persist_grid = 0;      // resident blocks of the persistent kernel in its current shape
+  int persist_shape = 0;          // launch shape of the persistent kernel (PERSIST_SHAPES)
+  unsigned persist_grids[PERSIST_SHAPES] = {0, 0};
   cudaGraphExec_t gexec_p = nullptr;
   int gexec_p_n = 0;
   int var[5] = {0, 0, 0, 0, 0};
@@ -433,7 +435,7 @@ int enqueue_persist(su2gpu_pool* P, const int4* tiles, int nt, uint32_t* const* 
     A.nsweeps = nsweeps > 0 ? n : 0;
     PCK(cudaMemsetAsync(P->qstate.p, 0, P->qstate.n, P->st));
     const unsigned grid = (unsigned)std::min<int64_t>(P->persist_grid, per_sweep * std::max(n, 1));
-    P->pers->launch(&A, grid, P->st);
+    P->pers->launch(P->persist_shape, &A, grid, P->st);
     PCK(cudaGetLastError());
     if (nsweeps > 0 && first_item == 0 && sweeps) launch_pool_next_sweep(sweeps, nchains, P->st, (uint32_t)n);
     PCK(cudaGetLastError());
@@ -505,7 +507,9 @@ int su2gpu_pool_create(const su2gpu_params* recipe, int64_t arena_bytes, int32_t
     int sms = 0, dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    P->persist_grid = (unsigned)std::max(0, sms * P->pers->blocks_per_sm());
+    for (int k = 0; k < PERSIST_SHAPES; k++)
+      P->persist_grids[k] = (unsigned)std::max(0, sms * P->pers->blocks_per_sm(k));
+    P->persist_grid = P->persist_grids[0];
   }
   cudaMemsetAsync(P->slotmem.p, 0, P->slotmem.n, P->st);
   cudaMemsetAsync(P->err.p, 0, P->err.n, P->st);
@@ -1300,6 +1304,26 @@ int su2gpu_pool_get_persist_tiles(su2gpu_pool* P, int32_t* tiles) {
   return SU2GPU_OK;
 }
 
+int su2gpu_pool_set_persist_shape(su2gpu_pool* P, int32_t shape) {
+  if (!P || shape < 0 || shape >= PERSIST_SHAPES || !P->persist_grids[shape])
+    return fail(SU2GPU_ERR_INVALID, "no such persistent launch shape");
+  PCK(cudaStreamSynchronize(P->st));
+  P->persist_shape = shape;
+  P->persist_grid = P->persist_grids[shape];
+  P->seg_tuned = 0;  // a tuned item size belongs to the shape it was timed with
+  P->dirty = true;
+  drop_graphs(P);
+  return SU2GPU_OK;
+}
+
+int su2gpu_pool_get_persist_shape(su2gpu_pool* P, int32_t* shape, int32_t* threads, int32_t* blocks_per_sm) {
+  if (!P || !shape) return SU2GPU_ERR_INVALID;
+  *shape = P->persist_shape;
+  if (threads) *threads = P->pers->threads;
+  if (blocks_per_sm) *blocks_per_sm = P->pers->blocks_per_sm(P->persist_shape);
+  return SU2GPU_OK;
+}
+
 int su2gpu_pool_get_persistent(su2gpu_pool* P, int32_t* on) {
   if (!P || !on) return SU2GPU_ERR_INVALID;
   int rc;
@@ -1524,10 +1548,15 @@ int su2gpu_pool_autotune(su2gpu_pool* P, int32_t* choices, float* best_ms) {
     for (int s : P->active) ntiles_all += (P->slots[s].g.half + kVariantBS[0] - 1) / kVariantBS[0];
     const int cand[5] = {4, 6, 8, 12, 16};
     float best = 1e30f;
-    int bestseg = P->seg_tiles;
+    int bestseg = P->seg_tiles, bestshape = P->persist_shape;
     Buf segbuf;
     std::vector<int4> tab;
+    // every launch shape of the persistent kernel with every item size
+    for (int shape = 0; shape < PERSIST_SHAPES && !rc; shape++)
     for (int seg : cand) {
+      if (!P->persist_grids[shape]) break;
+      P->persist_shape = shape;
+      P->persist_grid = P->persist_grids[shape];
       if (ntiles_all / seg < (int64_t)P->persist_grid) continue;  // at least one item per resident block and pass
       tab.clear();
       for (int s : P->active) append_segments(P, s, seg, tab);
@@ -1556,9 +1585,11 @@ int su2gpu_pool_autotune(su2gpu_pool* P, int32_t* choices, float* best_ms) {
         PCK(cudaMemsetAsync(P->err.p, 0, sizeof(int), P->st));
         continue;
       }
-      if (ms < best) { best = ms; bestseg = seg; }
+      if (ms < best) { best = ms; bestseg = seg; bestshape = shape; }
     }
     segbuf.release();
+    P->persist_shape = bestshape;
+    P->persist_grid = P->persist_grids[bestshape];
     if (!rc) {
       P->seg_tuned = bestseg;
       P->dirty = true;  // the segment table is rebuilt with the pick

@@ -105,6 +105,8 @@ def lib():
         L.su2gpu_pool_enqueue.argtypes = [vp, i32, i32]
         L.su2gpu_pool_set_persistent.argtypes = [vp, i32]
         L.su2gpu_pool_get_persist_tiles.argtypes = [vp, ctypes.POINTER(i32)]
+        L.su2gpu_pool_set_persist_shape.argtypes = [vp, i32]
+        L.su2gpu_pool_get_persist_shape.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(i32)]
         L.su2gpu_pool_get_persistent.argtypes = [vp, ctypes.POINTER(i32)]
         L.su2gpu_pool_check_wait_timeout.argtypes = [vp, i32, ctypes.POINTER(i32)]
         L.su2gpu_pool_raise_error.argtypes = [vp, i32]
@@ -624,6 +626,17 @@ class Pool:
         n = ctypes.c_int32()
         check(lib().su2gpu_pool_get_persist_tiles(self._h, ctypes.byref(n)))
         return n.value
+
+    @property
+    def persist_shape(self):
+        """(shape, threads, resident blocks per SM) of the persistent sweep."""
+        a, b, c = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        check(lib().su2gpu_pool_get_persist_shape(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    @persist_shape.setter
+    def persist_shape(self, shape):
+        check(lib().su2gpu_pool_set_persist_shape(self._h, int(shape)))
 
     def check_wait_timeout(self, spin_limit=2000):
         """Run the persistent kernel on a work list whose dependencies never

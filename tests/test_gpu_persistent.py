@@ -237,3 +237,19 @@ def test_long_recipe_sweeps_one_launch_per_pass(gpu):
             assert np.array_equal(got[n], f[n]), n
     mref = ref.measure()
     assert np.array_equal(np.array([mref[s] for s in rslots]), sums)
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_persistent_shapes_bit_identical(gpu, precision):
+    """Both launch shapes of the persistent sweep give the fields of one
+    launch per pass bit for bit."""
+    specs = specs_of("adj", precision)
+    inputs = [as_dict(hot_fields(p, seed=500 + k, phi_mean=0.5)) for k, (p, _, _) in enumerate(specs)]
+    ref, rslots = make_pool(gpu, specs, False, inputs)
+    ref.run(3)
+    for shape in (0, 1):
+        pool, slots = make_pool(gpu, specs, True, inputs)
+        pool.persist_shape = shape
+        assert pool.persist_shape[0] == shape and pool.persist_shape[1] == 128
+        pool.run(3)
+        assert_same(pool, slots, ref, rslots)
