@@ -440,7 +440,7 @@ int su2gpu_pool_run(su2gpu_pool* pool, int32_t nsweeps, int32_t use_graph);
 int su2gpu_pool_set_persistent(su2gpu_pool* pool, int32_t on);
 int su2gpu_pool_get_persistent(su2gpu_pool* pool, int32_t* on);
 /* Tiles of 128 sites per work item of the persistent sweep: chosen from the
- * tiles per pass, or timed by su2gpu_pool_autotune (4, 6, 8, 12 or 16) when
+ * tiles per pass, or timed by su2gpu_pool_autotune (4 to 32) when
  * the pool sweeps persistently. */
 int su2gpu_pool_get_persist_tiles(su2gpu_pool* pool, int32_t* tiles);
 /* Launch shape of the persistent sweep: 0 (128 threads, the register budget

@@ -1546,7 +1546,7 @@ int su2gpu_pool_autotune(su2gpu_pool* P, int32_t* choices, float* best_ms) {
   if (P->persistent && !P->seg_env) {
     int64_t ntiles_all = 0;
     for (int s : P->active) ntiles_all += (P->slots[s].g.half + kVariantBS[0] - 1) / kVariantBS[0];
-    const int cand[5] = {4, 6, 8, 12, 16};
+    const int cand[7] = {4, 6, 8, 12, 16, 24, 32};
     float best = 1e30f;
     int bestseg = P->seg_tiles, bestshape = P->persist_shape;
     Buf segbuf;
