@@ -3,7 +3,7 @@ large lattices, from one checkpoint.
 
 SU(2) + fundamental Higgs at beta 8, m^2 -0.1, lambda 0.002.  A seeded hot
 start is brought to equilibrium by the FP64 GPU path; from that checkpoint
-an FP32 chain and an FP64 chain run on the GPU (independent random streams)
+four FP32 and four FP64 chains run on the GPU (independent random streams)
 and, at 64^3, oracle chains (FP64, CPU) run in worker processes.  Plaquette,
 phi^2 and the hopping term must agree within 3 sigma of binned jackknife
 errors; each difference is printed with its error.  At 128^3 the GPU FP32
@@ -57,11 +57,11 @@ def test_fp32_against_fp64_and_oracle_at_scale(gpu, side):
     import chains
     L = (side,) * 3
     start = checkpoint(gpu, L, 400)
-    n = 1500 if side == 64 else 600
+    n = 2000 if side == 64 else 800
     sets = {"fp32": [gpu_series(gpu, abi.make_params("fund", L=L, precision=32), start, 32 + k, n)
-                     for k in range(2)],
+                     for k in range(4)],
             "fp64": [gpu_series(gpu, abi.make_params("fund", L=L, precision=64), start, 64 + k, n)
-                     for k in range(2)]}
+                     for k in range(4)]}
     if side == 64:
         # oracle chains of 60 sweeps from the checkpoint, the first 10 left
         # out (they still remember the common start)
