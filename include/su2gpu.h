@@ -343,12 +343,6 @@ int su2gpu_clone(su2gpu_ctx* ctx, uint64_t seed, uint32_t chain, su2gpu_ctx** ou
 /* Device-to-device copy of src's fields into dst (copy_fields,
  * hb_trajectory.c:61); both have the same lattice, content and precision. */
 int su2gpu_copy_fields(su2gpu_ctx* dst, su2gpu_ctx* src);
-/* With SU(2)xU(1) + one doublet + singlet, the singlet half-sweep of a
- * parity runs on a second stream beside the doublet half-sweep of the other
- * parity, which neither reads nor writes what it does (on by default; the
- * fields are the same bit for bit either way).  0 runs every pass on the
- * context's stream, one after another. */
-int su2gpu_set_concurrent_passes(su2gpu_ctx* ctx, int32_t on);
 /* The reference's random_sweeps mode (update.c:278-300, 338-344, used by the
  * heatbath trajectories, hb_trajectory.c:16-21): every sweep updates the
  * links in a random order of (direction, parity) and each scalar sweep starts

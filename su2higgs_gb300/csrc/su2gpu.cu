@@ -113,11 +113,6 @@ struct su2gpu_ctx {
   const PrecOps* pops;
   cudaStream_t st = nullptr;      // execution stream (the caller's, or own_st)
   cudaStream_t own_st = nullptr;  // the context's own stream; graphs are captured on it
-  // the singlet passes of SU(2)xU(1) + doublet + singlet run on a side stream
-  // beside the doublet passes they do not depend on (enqueue_sweep)
-  cudaStream_t side_st = nullptr;
-  cudaEvent_t ev_d[2] = {nullptr, nullptr}, ev_s[2] = {nullptr, nullptr};
-  int concurrent = 1;
   int launches = 0;               // kernel launches enqueued by the last sweep
   std::vector<cudaEvent_t>* prof = nullptr;  // per-pass events while profiling
   std::vector<int>* prof_kind = nullptr;
@@ -266,18 +261,6 @@ static int create_ctx(const su2gpu_params* p, void* borrowed, const void* copy_f
     return SU2GPU_ERR_CUDA;
   }
   c->st = c->own_st;
-  if (cudaStreamCreateWithFlags(&c->side_st, cudaStreamNonBlocking) != cudaSuccess) {
-    set_err("cudaStreamCreate failed");
-    su2gpu_destroy(c);
-    return SU2GPU_ERR_CUDA;
-  }
-  for (int k = 0; k < 2; k++)
-    if (cudaEventCreateWithFlags(&c->ev_d[k], cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->ev_s[k], cudaEventDisableTiming) != cudaSuccess) {
-      set_err("cudaEventCreate failed");
-      su2gpu_destroy(c);
-      return SU2GPU_ERR_CUDA;
-    }
   int64_t V = c->g.V;
   if (borrowed) {
     c->fields.p = borrowed;
@@ -342,14 +325,6 @@ int su2gpu_destroy(su2gpu_ctx* c) {
   c->fields.release(); c->stage.release(); c->ctrbuf.release(); c->partials.release(); c->sums.release();
   c->alpha.release(); c->backup.release(); c->muca.release(); c->flow.release(); c->rows.release();
   c->local.release(); c->correl.release();
-  if (c->side_st) {
-    cudaStreamSynchronize(c->side_st);
-    cudaStreamDestroy(c->side_st);
-  }
-  for (int k = 0; k < 2; k++) {
-    if (c->ev_d[k]) cudaEventDestroy(c->ev_d[k]);
-    if (c->ev_s[k]) cudaEventDestroy(c->ev_s[k]);
-  }
   if (c->own_st) cudaStreamDestroy(c->own_st);
   delete c;
   return SU2GPU_OK;
@@ -652,44 +627,8 @@ static int enqueue_sweep(su2gpu_ctx* c, int64_t* tot, uint32_t host_sweep) {
       }
   }
   int nsweeps = p.scalar_sweeps + 1;
-  // SU(2)xU(1) + one doublet + singlet: the singlet pass of a parity reads
-  // the doublet at its own sites and the singlet at the other parity's, and
-  // the doublet pass reads the singlet at its own sites only, so the singlet
-  // pass of parity p (after the doublet pass of p and its multicanonical
-  // check) runs on a side stream beside the doublet pass of the other
-  // parity, and the next doublet pass of p waits for it: the reads and
-  // writes are those of the sequential order, so are the results
-  const bool overlap = c->concurrent && c->side_st && c->has_s && c->nh == 1 && !c->has_t && !c->random_sweeps &&
-                       !c->prof && p.update_su2doublet == 1 && p.update_singlet == 1;
-  bool side_used[2] = {false, false};
   for (int s = 0; s < nsweeps; s++) {
     const int p0 = sfirst[s], pr[2] = {p0, 1 - p0};
-    if (overlap) {
-      const bool last = s >= nsweeps - 1;
-      const bool do_d = !last || p.algorithm_su2doublet == SU2GPU_OVERRELAX;
-      const bool do_s = !last || p.algorithm_singlet == SU2GPU_OVERRELAX;
-      const uint32_t pd = pass, ps = pass + (do_d ? 2u : 0u);
-      for (int j = 0; j <= 1; j++) {
-        const int par = pr[j];
-        if (do_d) {
-          if (side_used[par]) CK(cudaStreamWaitEvent(c->st, c->ev_s[par], 0));
-          if ((rc = scalar_pass(c, base, 0, 0, par, last ? 1 : 0, pd + j, tot))) return rc;
-          CK(cudaEventRecord(c->ev_d[par], c->st));
-        }
-        if (do_s) {
-          CK(cudaStreamWaitEvent(c->side_st, c->ev_d[par], 0));
-          cudaStream_t mainst = c->st;
-          c->st = c->side_st;
-          rc = scalar_pass(c, base, 2, 0, par, last ? 1 : 0, ps + j, tot);
-          c->st = mainst;
-          if (rc) return rc;
-          CK(cudaEventRecord(c->ev_s[par], c->side_st));
-          side_used[par] = true;
-        }
-      }
-      pass += (do_d ? 2u : 0u) + (do_s ? 2u : 0u);
-      continue;
-    }
     if (c->nh > 0)
       for (int k = 0; k < p.update_su2doublet; k++) {
         int force = 0;
@@ -722,9 +661,6 @@ static int enqueue_sweep(su2gpu_ctx* c, int64_t* tot, uint32_t host_sweep) {
           if ((rc = scalar_pass(c, base, 2, 0, pr[j], force, pass++, tot))) return rc;
       }
   }
-  // the side stream joins the main one before the sweep ends
-  for (int k = 0; k < 2; k++)
-    if (side_used[k]) CK(cudaStreamWaitEvent(c->st, c->ev_s[k], 0));
   // FP32: links are re-normalised where they are written (heatbath and
   // Metropolis kernels), which subsumes a periodic re-unitarisation pass
   mark(c, -1);
@@ -801,14 +737,6 @@ int su2gpu_run_sweeps(su2gpu_ctx* c, uint32_t first_sweep, int32_t nsweeps, int3
 int su2gpu_enqueue_sweeps(su2gpu_ctx* c, uint32_t first_sweep, int32_t nsweeps, int32_t use_graph) {
   if (!c || nsweeps < 0) return SU2GPU_ERR_INVALID;
   return enqueue_sweeps(c, first_sweep, nsweeps, use_graph);
-}
-
-int su2gpu_set_concurrent_passes(su2gpu_ctx* c, int32_t on) {
-  if (!c) return SU2GPU_ERR_INVALID;
-  CK(cudaStreamSynchronize(c->st));
-  c->concurrent = on ? 1 : 0;
-  if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
-  return SU2GPU_OK;
 }
 
 int su2gpu_set_random_sweeps(su2gpu_ctx* c, int32_t on) {

@@ -66,7 +66,6 @@ def lib():
         L.su2gpu_device_info.argtypes = [ctypes.POINTER(ctypes.c_int)] * 3 + [ctypes.POINTER(i64)]
         L.su2gpu_set_stream.argtypes = [vp, vp]
         L.su2gpu_set_random_sweeps.argtypes = [vp, i32]
-        L.su2gpu_set_concurrent_passes.argtypes = [vp, i32]
         L.su2gpu_clone.argtypes = [vp, u64, u32, ctypes.POINTER(vp)]
         L.su2gpu_measure_correlators.argtypes = [vp, i32, vp]
         L.su2gpu_measure_blocked_correlators.argtypes = [vp, i32, vp, i32, vp, ctypes.POINTER(i32)]
@@ -204,11 +203,6 @@ class Lattice:
         """Device copy of `other`'s fields into this chain (same lattice,
         content and precision)."""
         check(lib().su2gpu_copy_fields(self._h, other._h))
-
-    def set_concurrent_passes(self, on=True):
-        """Singlet half-sweeps on a second stream beside the doublet ones
-        (SU(2)xU(1) + doublet + singlet; on by default, same fields)."""
-        check(lib().su2gpu_set_concurrent_passes(self._h, 1 if on else 0))
 
     def set_random_sweeps(self, on=True):
         """The reference's random_sweeps mode: the pass order of every sweep

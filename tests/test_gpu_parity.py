@@ -298,46 +298,3 @@ def test_launch_variants_bit_identical(gpu, content, precision):
         if before[n] is not None:
             assert np.array_equal(before[n], after[n]), n
     assert not lat.counters().any()
-
-
-@pytest.mark.parametrize("precision", [64, 32])
-@pytest.mark.parametrize("muca", [False, True])
-def test_concurrent_singlet_passes_bit_identical(gpu, precision, muca):
-    """SU(2) x U(1) + doublet + singlet: the singlet half-sweeps on the side
-    stream beside the doublet ones give the fields, counters and
-    multicanonical state of the passes run one after another, bit for bit,
-    replayed from a graph and launched directly."""
-    from native import WeightBuf
-    p = abi.make_params("su2u1s", L=(8, 6, 10), precision=precision)
-    f = hot_fields(p, seed=61, phi_mean=0.8)
-    lats = []
-    for concurrent, graph in ((True, True), (True, False), (False, True)):
-        lat = gpu.Lattice(p, seed=4321)
-        upload(lat, f)
-        if muca:
-            w = WeightBuf(32, orderparam=abi.PHISQ, mode=abi.MUCA_READONLY)
-            w.pos[1:] = np.linspace(0.2, 1.0, 33)
-            w.pos[0] = -100.0
-            w.W[1:] = 30.0 * (w.pos[1:] - 0.6) ** 2
-            w.W[0] = w.W[1]
-            w.linearize()
-            s = w.struct
-            s.min, s.max, s.wrk_min, s.wrk_max = 0.2, 1.0, 0.2, 1.0
-            lat.muca_set(s)
-            lat.calc_orderparam(0)
-            lat.calc_orderparam(1)
-        lat.set_concurrent_passes(concurrent)
-        lat.run_sweeps(30, 6, graph=graph)
-        lats.append(lat)
-    ref = lats[2]
-    for lat in lats[:2]:
-        a, b = lat.download(), ref.download()
-        for n in a:
-            if a[n] is not None:
-                assert np.array_equal(a[n], b[n]), n
-        assert np.array_equal(lat.counters(), ref.counters())
-        if muca:
-            assert lat.calc_orderparam(0) == ref.calc_orderparam(0)
-    if muca:
-        c = ref.counters()
-        assert c[abi.C_TOTAL_MUCA] == 6 * 10
