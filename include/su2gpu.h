@@ -458,6 +458,21 @@ int su2gpu_pool_get_persist_shape(su2gpu_pool* pool, int32_t* shape, int32_t* th
  * counters are untouched.  *flags receives the kernel's error flags (bit 4:
  * a wait timed out), which are then cleared. */
 int su2gpu_pool_check_wait_timeout(su2gpu_pool* pool, int32_t spin_limit, int32_t* flags);
+/* Multicanonical chains in a pool (multicanonical.c, update.c:13-30): set
+ * the chain's weight (the fields of su2gpu_muca_set; checks_per_sweep must
+ * be 1, one global check after each checked half-sweep); the order
+ * parameter of both parities is taken from the chain's current fields.  In
+ * either sweep mode the block that completes a checked half-sweep of the
+ * chain sums the order parameter over the parity, decides and, on reject,
+ * restores the half; the persistent sweep does this before the chain's next
+ * pass may start, while the other chains' items run.  su2gpu_pool_upload
+ * recomputes the order parameter; the batch transfers (upload_many, cycle)
+ * refuse chains with a weight.  get: the chain's weight state, as
+ * su2gpu_muca_get.  calc_orderparam: recompute parity `parity`'s share and
+ * return the total (calc_orderparam, multicanonical.c:709). */
+int su2gpu_pool_muca_set(su2gpu_pool* pool, int32_t slot, const su2gpu_weight* w);
+int su2gpu_pool_muca_get(su2gpu_pool* pool, int32_t slot, su2gpu_weight* w);
+int su2gpu_pool_calc_orderparam(su2gpu_pool* pool, int32_t slot, int32_t parity, double* value);
 /* Test hook: sets `flags` in the pool's device error word from the host, as
  * a kernel that found a bad state would (1 NaN fields, 2 bad tile, 4 a
  * dependency wait of the persistent sweep timed out).  The next call that

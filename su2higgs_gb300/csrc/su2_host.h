@@ -124,6 +124,12 @@ SU2_HIDDEN void su2gpu_record_error(const char* msg);
 // pool (gradient flow).
 SU2_HIDDEN int su2gpu_attach(const su2gpu_params* p, void* fields, su2gpu_ctx** out);
 
+// The device state a context keeps for a multicanonical weight
+// (su2gpu_muca_set): its weight struct, the backup of the checked field, the
+// order parameter and the checks per sweep; *muca is null without a weight.
+SU2_HIDDEN int su2gpu_muca_device_state(su2gpu_ctx* c, void** muca, void** backup, int* orderparam, int* cps,
+                                        int* do_acceptance);
+
 // A context with its own copy of the fields at `fields` (device memory laid out
 // by carve() for p), seeded with (seed, chain); no cold start.
 SU2_HIDDEN int su2gpu_create_copy(const su2gpu_params* p, const void* fields, uint64_t seed, uint32_t chain,

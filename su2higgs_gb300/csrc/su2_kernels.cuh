@@ -1050,10 +1050,11 @@ __device__ inline void muca_update_slow(MucaDev* w) {
 // reference's binary search (whichbin, multicanonical.c:671-704) returns:
 // the unique bin with pos[b] < val < pos[b+1]; a value within 1e-12 of a bin
 // edge (where the search may stop at either neighbour) or in no bin takes
-// the sequential search.
-__device__ inline void muca_decide_block(MucaDev* w, double tot, int parity, const RngKey& rk, uint32_t pass,
-                                         uint32_t check, unsigned long long* ctr) {
-  __shared__ int s_bin[2], s_fuzzy[2];
+// the sequential search.  `sweep` is the chain's sweep number (the global
+// draw's counter); the decision (1 accept) is returned to every thread.
+__device__ inline int muca_decide_block(MucaDev* w, double tot, int parity, const RngKey& rk, uint32_t pass,
+                                        uint32_t check, uint32_t sweep, unsigned long long* ctr) {
+  __shared__ int s_bin[2], s_fuzzy[2], s_accept;
   __shared__ double s_W[2];
   const double pv0 = w->param_value[0], pv1 = w->param_value[1];
   const int bins = w->bins;
@@ -1088,26 +1089,30 @@ __device__ inline void muca_decide_block(MucaDev* w, double tot, int parity, con
     s_W[j] = W;
   }
   __syncthreads();
-  if (threadIdx.x != 0) return;
-  w->param_value[parity] = tot;
-  const double Wn = s_W[0], Wo = s_W[1];
-  double u = philox_uniform53(rk.k0, rk.k1, GLOBAL_SITE, pass, check, *rk.sweep, rk.chain, 0);
-  int accept = exp(-(Wn - Wo)) > u ? 1 : 0;
-  if (w->mode != 0) {
-    double val = accept ? nw : old;
-    muca_accumulate(w, val);
-    w->muca_count++;
-    if (w->muca_count % w->update_interval == 0) {
-      if (w->mode == 1) muca_update_fast(w);
-      else if (w->mode == 2) muca_update_slow(w);
-      w->muca_count = 0;
-      w->weight_updates++;
+  if (threadIdx.x == 0) {
+    w->param_value[parity] = tot;
+    const double Wn = s_W[0], Wo = s_W[1];
+    double u = philox_uniform53(rk.k0, rk.k1, GLOBAL_SITE, pass, check, sweep, rk.chain, 0);
+    int accept = exp(-(Wn - Wo)) > u ? 1 : 0;
+    if (w->mode != 0) {
+      double val = accept ? nw : old;
+      muca_accumulate(w, val);
+      w->muca_count++;
+      if (w->muca_count % w->update_interval == 0) {
+        if (w->mode == 1) muca_update_fast(w);
+        else if (w->mode == 2) muca_update_slow(w);
+        w->muca_count = 0;
+        w->weight_updates++;
+      }
     }
+    if (!accept) w->param_value[parity] = old - w->param_value[1 - parity];
+    w->last_accept = accept;
+    ctr[20] += 1;
+    ctr[21] += accept;
+    s_accept = accept;
   }
-  if (!accept) w->param_value[parity] = old - w->param_value[1 - parity];
-  w->last_accept = accept;
-  ctr[20] += 1;
-  ctr[21] += accept;
+  __syncthreads();
+  return s_accept;
 }
 
 // sum of x[0..n) by the block's first 64 threads (blockDim.x >= 64) in a
@@ -1166,7 +1171,7 @@ __device__ inline void muca_fused_finish(const PassArgs& a, double s) {
   __threadfence();
   const double tot = fixed_sum64(a.partials + nb, (int)nchunks);  // the same value in every thread
   if (threadIdx.x == 0) a.arrive[0] = 0;
-  muca_decide_block(a.muca, tot / a.vol, a.parity, a.rk, a.pass, a.check, a.ctr);
+  muca_decide_block(a.muca, tot / a.vol, a.parity, a.rk, a.pass, a.check, *a.rk.sweep, a.ctr);
 }
 
 #ifdef SU2_WITH_GLOBAL
@@ -1184,7 +1189,7 @@ __global__ void k_muca_decide(MucaDev* w, const double* partials, int np, double
     if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
     __syncthreads();
   }
-  muca_decide_block(w, red[0] / vol, parity, rk, pass, check, ctr);
+  muca_decide_block(w, red[0] / vol, parity, rk, pass, check, *rk.sweep, ctr);
 }
 
 // calc_orderparam for the host API: store the parity sum

@@ -80,6 +80,12 @@ struct Slot {
   uint64_t seed = 0;
   uint32_t chain = 0;
   int64_t tot[SU2GPU_NCOUNTERS] = {0};
+  // a multicanonical weight: a context attached to the chain's fields keeps
+  // its device state (su2gpu_pool_muca_set)
+  su2gpu_ctx* mctx = nullptr;
+  void* mdev = nullptr;
+  void* mbackup = nullptr;
+  int mop = 0;
 };
 
 }  // namespace
@@ -204,6 +210,14 @@ ChainDesc<R> make_desc(su2gpu_pool* P, int s, char* arena_base, char* slot_base)
   d.chain = sl.chain;
   d.sweep = (uint32_t*)(slot_base + (size_t)s * 256);
   d.ctr = (unsigned long long*)(slot_base + (size_t)s * 256 + 32);
+  d.mcount = (unsigned*)(slot_base + (size_t)s * 256 + 224);
+  // the weight only on the pool's own fields: the autotuner's scratch copy
+  // sweeps without checks, leaving the chain's multicanonical state alone
+  if (sl.mdev && arena_base == (char*)P->arena.p) {
+    d.muca = (MucaDev*)sl.mdev;
+    d.mbackup = sl.mbackup;
+    d.mop = sl.mop;
+  }
   return d;
 }
 
@@ -526,6 +540,8 @@ int su2gpu_pool_destroy(su2gpu_pool* P) {
   if (P->st) cudaStreamSynchronize(P->st);
   if (P->own_st) cudaStreamSynchronize(P->own_st);
   drop_graphs(P);
+  for (Slot& sl : P->slots)
+    if (sl.mctx) su2gpu_destroy(sl.mctx);
   P->qstate.release();
   P->segs.release();
   P->arena.release(); P->slotmem.release(); P->descs.release(); P->mtiles.release(); P->mfirst.release();
@@ -593,7 +609,8 @@ int su2gpu_pool_remove(su2gpu_pool* P, int32_t s) {
   if (!P || s < 0 || s >= P->max_slots || !P->slots[s].active) return fail(SU2GPU_ERR_INVALID, "no such chain slot");
   PCK(cudaStreamSynchronize(P->st));
   arena_free(P, P->slots[s].off, P->slots[s].bytes);
-  P->slots[s].active = false;
+  if (P->slots[s].mctx) su2gpu_destroy(P->slots[s].mctx);
+  P->slots[s] = Slot();
   P->dirty = true;
   P->seg_tuned = 0;
   return SU2GPU_OK;
@@ -675,6 +692,10 @@ int su2gpu_pool_upload(su2gpu_pool* P, int32_t s, const double* link, const doub
   int rc = slot_transfer(P, s, 1, h, 0);
   if (rc) return rc;
   PCK(cudaStreamSynchronize(P->st));
+  // a multicanonical chain takes the order parameter of its new fields
+  if (P->slots[s].mctx)
+    for (int par = 0; par < 2; par++)
+      if ((rc = su2gpu_calc_orderparam(P->slots[s].mctx, par, nullptr))) return rc;
   return SU2GPU_OK;
 }
 
@@ -894,7 +915,19 @@ static int many_transfer(su2gpu_pool* P, int32_t n, const int32_t* slots, int up
   return SU2GPU_OK;
 }
 
+// batch uploads leave a multicanonical chain's order parameter behind its
+// fields: they are refused for such chains (su2gpu_pool_upload recomputes it)
+static int refuse_muca_batch(const su2gpu_pool* P, int32_t n, const int32_t* slots) {
+  for (int j = 0; j < n; j++)
+    if (slots && slots[j] >= 0 && slots[j] < P->max_slots && P->slots[slots[j]].mctx)
+      return fail(SU2GPU_ERR_UNSUPPORTED, "chain slot %d has a multicanonical weight: upload it with "
+                  "su2gpu_pool_upload, which recomputes its order parameter", slots[j]);
+  return SU2GPU_OK;
+}
+
 int su2gpu_pool_upload_many(su2gpu_pool* P, int32_t n, const int32_t* slots, const double* const* const* fields) {
+  if (!P) return SU2GPU_ERR_INVALID;
+  if (int rc = refuse_muca_batch(P, n, slots)) return rc;
   return many_transfer(P, n, slots, 1, (double* const* const*)fields);
 }
 
@@ -1115,6 +1148,7 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
                       int32_t use_graph, double* sums, double* const* const* out) {
   if (!P || n < 0 || (n && !slots) || !in || !out || nsweeps < 0) return fail(SU2GPU_ERR_INVALID, "bad arguments");
   int rc;
+  if ((rc = refuse_muca_batch(P, n, slots))) return rc;
   if (P->dirty && (rc = rebuild(P))) return rc;
   const int na = (int)P->active.size();
   if (n != na) return fail(SU2GPU_ERR_INVALID, "a cycle lists every active chain once (%d listed, %d active)", n, na);
@@ -1354,6 +1388,46 @@ int su2gpu_pool_check_wait_timeout(su2gpu_pool* P, int32_t spin_limit, int32_t* 
   PCK(cudaMemset(P->err.p, 0, sizeof(int)));
   *flags = herr;
   return SU2GPU_OK;
+}
+
+int su2gpu_pool_muca_set(su2gpu_pool* P, int32_t s, const su2gpu_weight* w) {
+  if (!P || !w || s < 0 || s >= P->max_slots || !P->slots[s].active) return fail(SU2GPU_ERR_INVALID, "no such chain slot");
+  if (w->checks_per_sweep != 1)
+    return fail(SU2GPU_ERR_UNSUPPORTED, "pool chains take one multicanonical check per half-sweep (checks_per_sweep 1)");
+  const int op = w->orderparam, content = P->content;
+  const bool ok = (op == SU2GPU_PHISQ && (content & (SU2GPU_HIGGS1 | SU2GPU_HIGGS2))) ||
+                  (op == SU2GPU_SIGMASQ && (content & SU2GPU_TRIPLET)) ||
+                  (op == SU2GPU_PHI2MINUSSIGMA2 && (content & SU2GPU_HIGGS1) && (content & SU2GPU_TRIPLET)) ||
+                  (op == SU2GPU_PHI2SQ && (content & SU2GPU_HIGGS2));
+  if (!ok) return fail(SU2GPU_ERR_INVALID, "order parameter %d does not fit the pool's field content", op);
+  PCK(cudaStreamSynchronize(P->st));
+  Slot& sl = P->slots[s];
+  int rc;
+  if (!sl.mctx && (rc = su2gpu_attach(&sl.p, (char*)P->arena.p + sl.off, &sl.mctx))) return rc;
+  if ((rc = su2gpu_muca_set(sl.mctx, w))) return rc;
+  // the order parameter of both parities from the chain's current fields
+  for (int par = 0; par < 2; par++)
+    if ((rc = su2gpu_calc_orderparam(sl.mctx, par, nullptr))) return rc;
+  int mop = 0, cps = 0, acc = 0;
+  if ((rc = su2gpu_muca_device_state(sl.mctx, &sl.mdev, &sl.mbackup, &mop, &cps, &acc))) return rc;
+  sl.mop = acc ? mop : 0;
+  P->dirty = true;
+  drop_graphs(P);
+  return SU2GPU_OK;
+}
+
+int su2gpu_pool_muca_get(su2gpu_pool* P, int32_t s, su2gpu_weight* w) {
+  if (!P || !w || s < 0 || s >= P->max_slots || !P->slots[s].active || !P->slots[s].mctx)
+    return fail(SU2GPU_ERR_INVALID, "no multicanonical chain in that slot");
+  PCK(cudaStreamSynchronize(P->st));
+  return su2gpu_muca_get(P->slots[s].mctx, w);
+}
+
+int su2gpu_pool_calc_orderparam(su2gpu_pool* P, int32_t s, int32_t parity, double* value) {
+  if (!P || s < 0 || s >= P->max_slots || !P->slots[s].active || !P->slots[s].mctx || parity < 0 || parity > 1)
+    return fail(SU2GPU_ERR_INVALID, "no multicanonical chain in that slot");
+  PCK(cudaStreamSynchronize(P->st));
+  return su2gpu_calc_orderparam(P->slots[s].mctx, parity, value);
 }
 
 int su2gpu_pool_raise_error(su2gpu_pool* P, int32_t flags) {

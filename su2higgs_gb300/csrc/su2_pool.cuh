@@ -22,7 +22,98 @@ struct __align__(16) ChainDesc {
   uint32_t k0, k1, chain;
   uint32_t* sweep;          // this chain's sweep counter (device word)
   unsigned long long* ctr;  // this chain's counters [24]
+  // multicanonical chains (muca_pool_finish): the weight, the backup of the
+  // updated field (indexed like the field), the sites of the current checked
+  // half-sweep done so far (a slot word), the order parameter (0: no weight
+  // in this chain, or none checked in these passes)
+  MucaDev* muca;
+  void* mbackup;
+  unsigned* mcount;
+  int mop;
+  int mpad[3];
 };
+
+// whether a half-sweep of `field` (0 doublet `h`, 1 triplet) ends with a
+// global multicanonical check of order parameter op (update.c:82-229)
+__device__ inline bool muca_checked(int field, int h, int op) {
+  if (field == 0) return (h == 0 && (op == 1 || op == 3)) || (h == 1 && op == 4);
+  if (field == 1) return op == 2 || op == 3;
+  return false;
+}
+
+// a chain-wide quantity read while other blocks of the launch write: past L1
+template <typename R>
+__device__ inline Q<R> ldcg4(const V4<R>* p, int i) {
+  if constexpr (sizeof(R) == 4) {
+    const float4 v = __ldcg((const float4*)p + i);
+    return Q<R>{v.x, v.y, v.z, v.w};
+  } else {
+    const double2 a = __ldcg((const double2*)p + 2 * i), b = __ldcg((const double2*)p + 2 * i + 1);
+    return Q<R>{a.x, a.y, b.x, b.y};
+  }
+}
+template <typename R>
+__device__ inline double orderparam_site_cg(const Fields<R>& f, int op, int i) {
+  double phi = 0.0, sig = 0.0;
+  if (op == 1 || op == 3 || op == 4) phi = (double)doubletsq(ldcg4<R>(php(f, op == 4 ? 1 : 0), i));
+  if (op == 2 || op == 3)
+    sig = (double)tripletsq(V3<R>{__ldcg(f.trip[0] + i), __ldcg(f.trip[1] + i), __ldcg(f.trip[2] + i)});
+  return op == 2 ? sig : (op == 3 ? phi - sig : phi);
+}
+
+// The multicanonical check that ends a checked half-sweep of a pool chain
+// (muca_check, update.c:13-30, with one check per half-sweep): every block
+// that updated sites of the chain's parity adds their number to the chain's
+// count; the block that completes it sums the order parameter over the
+// parity in a fixed order (64 lanes over the sites, then a tree -- the same
+// value whatever the tiling or the launch), decides (muca_decide_block) and,
+// on reject, puts the backup back.  In the persistent sweep this happens
+// before the block publishes its item, so the chain's next pass sees the
+// decided fields; other chains' items keep the GPU busy meanwhile.
+template <typename R, int BS>
+__device__ inline void muca_pool_finish(const ChainDesc<R>& d, int field, int h, int parity, uint32_t pass,
+                                        uint32_t sweep, int t0) {
+  __shared__ int s_last;
+  __shared__ double red[64];
+  const int half = d.g.half;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned n = (unsigned)min(BS, half - t0);
+    __threadfence();
+    const unsigned prev = atomicAdd(d.mcount, n);
+    s_last = prev + n == (unsigned)half;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  if (threadIdx.x == 0) *d.mcount = 0;
+  if (threadIdx.x < 64) {
+    double v = 0.0;
+    for (int t = threadIdx.x; t < half; t += 64) v += orderparam_site_cg<R>(d.f, d.mop, parity * half + t);
+    red[threadIdx.x] = v;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 32; k > 0; k >>= 1) {
+    if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+    __syncthreads();
+  }
+  const double tot = red[0] / (double)d.g.V;
+  const RngKey rk{d.k0, d.k1, d.chain, nullptr};
+  const int accept = muca_decide_block(d.muca, tot, parity, rk, pass, 0u, sweep, d.ctr);
+  if (!accept) {
+    for (int t = threadIdx.x; t < half; t += BS) {
+      const int i = parity * half + t;
+      if (field == 0) {
+        st4<R>(php(d.f, h), i, ldcg4<R>((const V4<R>*)d.mbackup, i));
+      } else {
+        const R* b = (const R*)d.mbackup;
+        st3(d.f, i, V3<R>{__ldcg(b + 3 * i), __ldcg(b + 3 * i + 1), __ldcg(b + 3 * i + 2)});
+      }
+    }
+  }
+  __syncthreads();
+}
 
 struct PoolArgs {
   const void* descs;  // ChainDesc<R>[nslots]
@@ -105,10 +196,20 @@ __device__ __noinline__ void tile_scalar(const ChainDesc<R>& d, int parity, int 
   const CoupT<R>& cp = d.cp;
   int t = t0 + threadIdx.x;
   int acc = 0, fb = 0;
+  // a multicanonical chain keeps the old values of a checked half-sweep
+  const bool checked = FIELD != 2 && d.mop != 0 && muca_checked(FIELD, sub, d.mop);
   if (t < d.g.half) {
     int c[3];
     site_coords(d.g, parity, t, c);
     int i = parity * d.g.half + t;
+    if (checked) {
+      if (FIELD == 0) {
+        ((V4<R>*)d.mbackup)[i] = php(d.f, sub)[i];
+      } else {
+        R* b = (R*)d.mbackup;
+        b[3 * i] = d.f.trip[0][i]; b[3 * i + 1] = d.f.trip[1][i]; b[3 * i + 2] = d.f.trip[2][i];
+      }
+    }
     SiteRng<R> rng(RngKey{d.k0, d.k1, d.chain, d.sweep}, sweep, (uint32_t)i, pass);
     constexpr int CCx = CC;
     if (FIELD == 0) {
@@ -129,6 +230,7 @@ __device__ __noinline__ void tile_scalar(const ChainDesc<R>& d, int parity, int 
   bool any_or = (FIELD == 0 ? cp.alg_d : (FIELD == 1 ? cp.alg_t : cp.alg_s)) == ALG_OR && !force;
   warp_count(d.ctr + (any_or ? base_or : base_mt), acc);
   warp_count(d.ctr + 23, fb);
+  if (checked) muca_pool_finish<R, BS>(d, FIELD, sub, parity, pass, sweep, t0);
 }
 
 // one launch per pass: block b works on tile b of the table

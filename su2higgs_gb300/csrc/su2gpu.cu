@@ -1441,6 +1441,19 @@ int su2gpu_update_lattice_host(su2gpu_ctx* c, uint32_t sweep, double* link, doub
 
 }  // extern "C"
 
+// C++ linkage, not part of the ABI (declared in su2_host.h)
+int su2gpu_muca_device_state(su2gpu_ctx* c, void** muca, void** backup, int* orderparam, int* cps,
+                             int* do_acceptance) {
+  if (!c) return SU2GPU_ERR_INVALID;
+  *muca = c->muca_on ? (void*)c->d_muca : nullptr;
+  *backup = c->backup.p;
+  *orderparam = c->muca_orderparam;
+  *cps = c->muca_cps;
+  *do_acceptance = c->muca_do_acc;
+  return SU2GPU_OK;
+}
+
+
 int su2gpu_attach(const su2gpu_params* p, void* fields, su2gpu_ctx** out) {
   if (!fields) return SU2GPU_ERR_INVALID;
   return create_ctx(p, fields, nullptr, out);

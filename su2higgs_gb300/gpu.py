@@ -110,6 +110,9 @@ def lib():
         L.su2gpu_pool_get_persistent.argtypes = [vp, ctypes.POINTER(i32)]
         L.su2gpu_pool_check_wait_timeout.argtypes = [vp, i32, ctypes.POINTER(i32)]
         L.su2gpu_pool_raise_error.argtypes = [vp, i32]
+        L.su2gpu_pool_muca_set.argtypes = [vp, i32, ctypes.POINTER(abi.Weight)]
+        L.su2gpu_pool_muca_get.argtypes = [vp, i32, ctypes.POINTER(abi.Weight)]
+        L.su2gpu_pool_calc_orderparam.argtypes = [vp, i32, i32, ctypes.POINTER(ctypes.c_double)]
         L.su2gpu_pool_enqueue_measure.argtypes = [vp, vp, i32, ctypes.POINTER(i32)]
         L.su2gpu_pool_set_stream.argtypes = [vp, vp]
         L.su2gpu_pool_launches_per_sweep.argtypes = [vp, ctypes.POINTER(i32)]
@@ -644,6 +647,18 @@ class Pool:
         flags = ctypes.c_int32()
         check(lib().su2gpu_pool_check_wait_timeout(self._h, spin_limit, ctypes.byref(flags)))
         return flags.value
+
+    def muca_set(self, slot, weight_struct):
+        """Give chain `slot` a multicanonical weight (su2gpu_weight)."""
+        check(lib().su2gpu_pool_muca_set(self._h, slot, ctypes.byref(weight_struct)))
+
+    def muca_get(self, slot, weight_struct):
+        check(lib().su2gpu_pool_muca_get(self._h, slot, ctypes.byref(weight_struct)))
+
+    def calc_orderparam(self, slot, parity):
+        v = ctypes.c_double(0)
+        check(lib().su2gpu_pool_calc_orderparam(self._h, slot, parity, ctypes.byref(v)))
+        return v.value
 
     def raise_error(self, flags):
         """Test hook: set error flags in the pool's device error word."""
