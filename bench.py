@@ -381,7 +381,12 @@ def run_reference(args):
         return
     if args.workload in BATCHED or args.workload == "served":
         return run_reference_batched(args)
-    content, L, prec = WORKLOADS[args.workload]
+    if args.workload == "batched96_su2u1s_muca_f32":
+        # the chains' content and largest side; the CPU sample sweeps without
+        # the multicanonical checks (a small share of the reference's time)
+        content, L, prec = "su2u1s", (48, 48, 48), 32
+    else:
+        content, L, prec = WORKLOADS[args.workload]
     import multiprocessing as mp
     cores = os.cpu_count() or 1
     # each step: every core sweeps its own lattice once; the lattice side is
@@ -1001,6 +1006,85 @@ def run_gpu_batched(args):
         dist.destroy_process_group()
 
 
+def run_gpu_batched_muca(args):
+    """Multicanonical chains in the batched form: 96 SU(2)xU(1) + doublet +
+    singlet chains (sides 16..48, beta_G 8, beta_U1 24, FP32 fields), each
+    with the multicanonical workload's read-only weight (256 bins of phi^2
+    on [0, 3]) and a global check after every doublet half-sweep, in one
+    pool; a step is 10 sweeps of every chain (the persistent sweep decides
+    each chain's checks as its half-sweeps complete) + the measurement."""
+    import torch
+    from su2higgs_gb300 import abi, gpu, workloads
+    rank, world, local = env_rank()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    rng = np.random.default_rng(replica_seed(777, rank))
+    nchains, S = 96, 10
+    specs = []
+    for k in range(nchains):
+        L = int(rng.choice((16, 24, 32, 48)))
+        p = abi.make_params("su2u1s", L=(L, L, L), precision=32, betasu2=8.0, betau1=24.0)
+        specs.append((p, int(rng.integers(1, 2 ** 62)), k))
+    sites = sum(p.sites() for p, _, _ in specs)
+    arena = sum(gpu.Pool.chain_bytes(p) for p, _, _ in specs)
+    pool = gpu.Pool(specs[0][0], arena_bytes=arena, max_chains=nchains)
+    weight = workloads.muca_weight(replica_seed(20261203, rank))
+    slots = []
+    for p, seed, chain in specs:
+        s = pool.add(p, seed=seed, chain=chain)
+        pool.upload(s, **workloads.hot_fields(p, seed, phi_sigma=0.5, sing_sigma=0.3))
+        pool.muca_set(s, weight.struct)
+        slots.append(s)
+    variants, _ = pool.autotune()
+    stream = torch.cuda.Stream(device=dev)
+    pool.set_stream(stream.cuda_stream)
+    K, W = args.steps, args.warmup
+    sums = torch.zeros((nchains, abi.NMEAS), dtype=torch.float64, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    with torch.cuda.stream(stream):
+        for w in range(W):
+            pool.enqueue(S, graph=True)
+            pool.enqueue_measure(sums.data_ptr(), nchains)
+            flush.zero_()
+        torch.cuda.synchronize()
+        clocks = ClockSampler(local)
+        clocks.start()
+        for k in range(K):
+            starts[k].record(stream)
+            pool.enqueue(S, graph=True)
+            pool.enqueue_measure(sums.data_ptr(), nchains)
+            ends[k].record(stream)
+            flush.zero_()
+        torch.cuda.synchronize()
+        clk = clocks.stop()
+    pool.set_stream(None)
+    pool.run(0)
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    value = sites * S * K / (float(np.sum(step_ms)) * 1e-3)
+    cnt = [pool.counters(s) for s in slots]
+    checks = int(sum(c[abi.C_TOTAL_MUCA] for c in cnt))
+    accepted = int(sum(c[abi.C_ACC_MUCA] for c in cnt))
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "site-updates/s", "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": float(np.mean(step_ms)), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "content": "SU(2)xU(1) + doublet + singlet", "chains": nchains,
+                       "sites_total": sites, "sweeps_per_step": S, "betasu2": 8.0, "betau1": 24.0,
+                       "weight": "read-only, 256 bins of phi^2 on [0, 3], one check per doublet half-sweep",
+                       "persistent": pool.persistent, "launch_variants": [int(v) for v in variants]},
+            "multicanonical": {"checks": checks, "accepted": accepted},
+            "sweep_roofline": sweep_roofline(value / world, "su2u1s", 32),
+            "gpu_launches": int(K * (pool.launches_per_sweep() if pool.persistent else
+                                     S * pool.launches_per_sweep()) + 2 * K),
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    pool.close()
+
+
 def run_gpu_served(args):
     """The served stream: Poisson arrivals of single-chain requests (side L
     in {16,32,64,96,128}, content fundamental / adjoint / SU(2)xU(1)+singlet,
@@ -1082,7 +1166,8 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--workload", default="batched384_adj_f32", choices=sorted(WORKLOADS) + sorted(BATCHED) + ["served"])
+    ap.add_argument("--workload", default="batched384_adj_f32",
+                    choices=sorted(WORKLOADS) + sorted(BATCHED) + ["served", "batched96_su2u1s_muca_f32"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end host-buffer measurement")
@@ -1109,6 +1194,8 @@ def main():
         run_gpu_batched(args)
     elif args.workload == "served":
         run_gpu_served(args)
+    elif args.workload == "batched96_su2u1s_muca_f32":
+        run_gpu_batched_muca(args)
     else:
         run_gpu(args)
 

@@ -13,7 +13,6 @@ reject after every checked half-sweep of each chain with a weight
 * The autotuner's scratch sweeps leave the weight state alone; batch uploads
   and unsupported settings are refused.
 """
-import ctypes
 
 import numpy as np
 import pytest
