@@ -1122,8 +1122,18 @@ __device__ inline int muca_decide_block(MucaDev* w, double tot, int parity, cons
 __device__ inline double fixed_sum64(const double* x, int n) {
   __shared__ double red[64];
   if (threadIdx.x < 64) {
+    // lane k adds x[k], x[k + 64], ... in that order; the loads are issued
+    // eight at a time
     double v = 0.0;
-    for (int k = threadIdx.x; k < n; k += 64) v += __ldcg(x + k);
+    int k = threadIdx.x;
+    for (; k + 64 * 7 < n; k += 64 * 8) {
+      double t[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++) t[j] = __ldcg(x + k + 64 * j);
+#pragma unroll
+      for (int j = 0; j < 8; j++) v += t[j];
+    }
+    for (; k < n; k += 64) v += __ldcg(x + k);
     red[threadIdx.x] = v;
   }
   __syncthreads();

@@ -94,11 +94,15 @@ void launch_pool_next_sweep(uint32_t* const* sweeps, int n, cudaStream_t st, uin
 constexpr int PERSIST_SHAPES = 2;
 struct PoolOps {
   int threads;
-  void (*launch)(int shape, const void* args, unsigned grid, cudaStream_t st);
+  // muca: the instance for pools with multicanonical chains
+  void (*launch)(int shape, bool muca, const void* args, unsigned grid, cudaStream_t st);
   int (*blocks_per_sm)(int shape);
   void (*pool_link)(int variant, const PoolArgs& a, unsigned nblocks, cudaStream_t st);
   void (*pool_u1)(int variant, const PoolArgs& a, unsigned nblocks, cudaStream_t st);
   void (*pool_scalar)(int variant, int field, const PoolArgs& a, unsigned nblocks, cudaStream_t st);
+  // the multicanonical decide and restore passes over the chains mslots[0..n)
+  void (*pool_restore)(const PoolArgs& a, const int* mslots, int n, int kb, cudaStream_t st);
+  void (*pool_decide)(const PoolArgs& a, const int* mslots, int n, cudaStream_t st);
 };
 extern const PoolOps persist_f64_generic, persist_f64_fund, persist_f64_adj, persist_f64_su2u1s;
 extern const PoolOps persist_f32_generic, persist_f32_fund, persist_f32_adj, persist_f32_su2u1s;

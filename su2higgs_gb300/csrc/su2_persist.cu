@@ -67,20 +67,39 @@ static void lp_scalar(int v, int field, const PoolArgs& a, unsigned nb, cudaStre
     default: lp_scalar_v<0>(field, a, nb, st);
   }
 }
-static void persist_launch(int shape, const void* args, unsigned grid, cudaStream_t st) {
+static void lp_restore(const PoolArgs& a, const int* mslots, int n, int kb, cudaStream_t st) {
+  if (n > 0) k_pool_restore<R, PBS, PMB><<<(unsigned)(n * kb), PBS, 0, st>>>(a, mslots, kb);
+}
+static void lp_decide(const PoolArgs& a, const int* mslots, int n, cudaStream_t st) {
+  if (n > 0) k_pool_decide<R, PBS, PMB><<<(unsigned)n, PBS, 0, st>>>(a, mslots);
+}
+static void persist_launch(int shape, bool muca, const void* args, unsigned grid, cudaStream_t st) {
   if (!grid) return;
-  if (shape == 1) k_pool_persist<R, CCI, PBS, PMB1><<<grid, PBS, 0, st>>>(*(const PersistArgs*)args);
-  else k_pool_persist<R, CCI, PBS, PMB><<<grid, PBS, 0, st>>>(*(const PersistArgs*)args);
+  const PersistArgs& a = *(const PersistArgs*)args;
+  if (shape == 1) {
+    if (muca) k_pool_persist<R, CCI, PBS, PMB1, true><<<grid, PBS, 0, st>>>(a);
+    else k_pool_persist<R, CCI, PBS, PMB1, false><<<grid, PBS, 0, st>>>(a);
+  } else {
+    if (muca) k_pool_persist<R, CCI, PBS, PMB, true><<<grid, PBS, 0, st>>>(a);
+    else k_pool_persist<R, CCI, PBS, PMB, false><<<grid, PBS, 0, st>>>(a);
+  }
 }
 
+// resident blocks per SM of a shape: the smaller of its two instances
 static int persist_blocks_per_sm(int shape) {
-  int n = 0;
-  cudaError_t e = shape == 1
-                      ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_pool_persist<R, CCI, PBS, PMB1>, PBS, 0)
-                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_pool_persist<R, CCI, PBS, PMB>, PBS, 0);
-  return e == cudaSuccess ? n : 0;
+  int n0 = 0, n1 = 0;
+  cudaError_t e0, e1;
+  if (shape == 1) {
+    e0 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n0, k_pool_persist<R, CCI, PBS, PMB1, false>, PBS, 0);
+    e1 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k_pool_persist<R, CCI, PBS, PMB1, true>, PBS, 0);
+  } else {
+    e0 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n0, k_pool_persist<R, CCI, PBS, PMB, false>, PBS, 0);
+    e1 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k_pool_persist<R, CCI, PBS, PMB, true>, PBS, 0);
+  }
+  return e0 == cudaSuccess && e1 == cudaSuccess ? (n0 < n1 ? n0 : n1) : 0;
 }
 
-const PoolOps SU2_PERSIST = {PBS, persist_launch, persist_blocks_per_sm, lp_link, lp_u1, lp_scalar};
+const PoolOps SU2_PERSIST = {PBS, persist_launch, persist_blocks_per_sm, lp_link, lp_u1, lp_scalar, lp_restore,
+                               lp_decide};
 
 }  // namespace su2

@@ -85,6 +85,7 @@ struct Slot {
   su2gpu_ctx* mctx = nullptr;
   void* mdev = nullptr;
   void* mbackup = nullptr;
+  double* mpart = nullptr;  // the order parameter's 32-site warp sums (cudaMalloc)
   int mop = 0;
 };
 
@@ -106,6 +107,11 @@ struct su2gpu_pool {
   Buf slotmem;   // per slot: sweep counter word + 24 counters
   Buf descs;     // ChainDesc<R>[max_slots]
   Buf tiles[NVARIANTS], mtiles, mfirst, sweepptrs, partials, sums, stage, err;
+  // the active chains with a multicanonical weight (their slots), the
+  // restore launch's blocks per chain, and the half-sweeps that any of them
+  // checks (bit 0 / 1: doublet 0 / 1, bit 2: triplet)
+  Buf mslots;
+  int restore_kb = 1, mucamask = 0;
   int64_t stage_sites = 0;          // sites each staging half holds (STAGE_REALS doubles per site)
   cudaEvent_t stage_ev[2] = {nullptr, nullptr};
   // batch transfers (upload_many / download_many): a ring of staging memory
@@ -129,6 +135,7 @@ struct su2gpu_pool {
   // the first segment of each active chain (+ the end)
   int seg_tiles = 8, seg_env = 0, seg_tuned = 0;  // seg_tuned: the autotuner's pick (0: none)
   int npasses = 0;  // passes per sweep of the recipe (set at the rebuild)
+  int nmuca = 0;    // active chains with a multicanonical weight (set at the rebuild)
   Buf segs;
   std::vector<int4> h_segs;  // (slot, t0, the chain's segment count, 0)
   std::vector<int> h_sfirst;
@@ -210,18 +217,18 @@ ChainDesc<R> make_desc(su2gpu_pool* P, int s, char* arena_base, char* slot_base)
   d.chain = sl.chain;
   d.sweep = (uint32_t*)(slot_base + (size_t)s * 256);
   d.ctr = (unsigned long long*)(slot_base + (size_t)s * 256 + 32);
-  d.mcount = (unsigned*)(slot_base + (size_t)s * 256 + 224);
   // the weight only on the pool's own fields: the autotuner's scratch copy
   // sweeps without checks, leaving the chain's multicanonical state alone
   if (sl.mdev && arena_base == (char*)P->arena.p) {
     d.muca = (MucaDev*)sl.mdev;
     d.mbackup = sl.mbackup;
+    d.mpart = sl.mpart;
     d.mop = sl.mop;
   }
   return d;
 }
 
-void sweep_recipe(const su2gpu_params& p, std::vector<PassDesc>& out, int64_t* tot);
+void sweep_recipe(const su2gpu_params& p, std::vector<PassDesc>& out, int64_t* tot, int mucamask = 0);
 
 // the work-list segments of slot s: (slot, t0, the chain's segment count, 0)
 // for every `seg` tiles of 128 sites of one parity
@@ -284,7 +291,23 @@ int rebuild(su2gpu_pool* P, void* arena_base = nullptr, void* slot_base = nullpt
     P->seg_tiles = P->seg_env ? P->seg_env : (P->seg_tuned ? P->seg_tuned : seg_auto);
     std::vector<PassDesc> rec;
     int64_t counts[SU2GPU_NCOUNTERS] = {0};
-    sweep_recipe(P->recipe, rec, counts);
+    std::vector<int> ms;
+    int64_t mhalf = 1;
+    P->mucamask = 0;
+    for (int s : P->active)
+      if (P->slots[s].mdev && P->slots[s].mop) {
+        const int op = P->slots[s].mop;
+        ms.push_back(s);
+        mhalf = std::max<int64_t>(mhalf, P->slots[s].g.half);
+        P->mucamask |= (op == SU2GPU_PHISQ || op == SU2GPU_PHI2MINUSSIGMA2 ? 1 : 0) |
+                       (op == SU2GPU_PHI2SQ ? 2 : 0) | (op == SU2GPU_SIGMASQ || op == SU2GPU_PHI2MINUSSIGMA2 ? 4 : 0);
+      }
+    P->nmuca = (int)ms.size();
+    // restore blocks per chain: up to 8 sites per thread
+    P->restore_kb = (int)std::max<int64_t>(1, (mhalf + 8 * 128 - 1) / (8 * 128));
+    if (int rc = P->mslots.ensure(std::max<size_t>(ms.size(), 1) * sizeof(int))) return rc;
+    if (!ms.empty()) PCK(cudaMemcpyAsync(P->mslots.p, ms.data(), ms.size() * sizeof(int), cudaMemcpyHostToDevice, P->st));
+    sweep_recipe(P->recipe, rec, counts, P->mucamask);
     P->npasses = (int)rec.size();
     // a recipe of more passes than the work list holds always sweeps one
     // launch per pass (forcing the persistent mode on is refused for it)
@@ -343,7 +366,7 @@ void mark(su2gpu_pool* P, int kind) {
 
 // the passes of one sweep (update.c:270-430 order); `tot` receives the
 // per-chain half-site totals of one sweep
-void sweep_recipe(const su2gpu_params& p, std::vector<PassDesc>& out, int64_t* tot) {
+void sweep_recipe(const su2gpu_params& p, std::vector<PassDesc>& out, int64_t* tot, int mucamask) {
   out.clear();
   uint32_t pass = 0;
   const int nh = nhiggs_of(p.content);
@@ -376,7 +399,14 @@ void sweep_recipe(const su2gpu_params& p, std::vector<PassDesc>& out, int64_t* t
         int nrep = fd.field == 0 ? nh : 1;
         for (int h = 0; h < nrep; h++)
           for (int par = 0; par <= 1; par++) {
-            out.push_back(PassDesc{(uint8_t)(2 + fd.field), (uint8_t)par, (uint8_t)h, (uint8_t)force, pass++});
+            out.push_back(PassDesc{(uint8_t)(2 + fd.field), (uint8_t)par, (uint8_t)h, (uint8_t)force, pass});
+            // a half-sweep that a multicanonical chain of the pool checks is
+            // followed by the decision and the restore (with its pass number)
+            if (fd.field < 2 && (mucamask >> (fd.field == 0 ? h : 2) & 1)) {
+              out.push_back(PassDesc{6, (uint8_t)par, (uint8_t)h, (uint8_t)fd.field, pass});
+              out.push_back(PassDesc{5, (uint8_t)par, (uint8_t)h, (uint8_t)fd.field, pass});
+            }
+            pass++;
             bool orr = fd.alg == SU2GPU_OVERRELAX && !force;
             int idx = fd.field == 0 ? (orr ? SU2GPU_C_TOTAL_OR_DOUBLET : SU2GPU_C_TOTAL_DOUBLET) + h
                                     : (fd.field == 1 ? (orr ? SU2GPU_C_TOTAL_OR_TRIPLET : SU2GPU_C_TOTAL_TRIPLET)
@@ -392,19 +422,21 @@ int enqueue_pool_sweep(su2gpu_pool* P, const void* descs, const int2* const* til
                        int64_t* tot) {
   if (!nt) nt = P->ntiles;
   std::vector<PassDesc> passes;
-  sweep_recipe(P->recipe, passes, tot);
+  sweep_recipe(P->recipe, passes, tot, P->mucamask);
   PoolArgs a;
   memset(&a, 0, sizeof(a));
   a.descs = descs;
   a.nslots = P->max_slots;
   a.err = (int*)P->err.p;
   for (const PassDesc& q : passes) {
-    const int kind = q.kind, v = P->var[kind];
+    const int kind = q.kind, v = kind >= 5 ? 0 : P->var[kind];
     a.parity = q.parity; a.sub = q.sub; a.alg = q.alg; a.pass = q.pass;
     a.tiles = tiles[v];
     mark(P, kind);
     if (kind == 0) P->pers->pool_link(v, a, nt[v], P->st);
     else if (kind == 1) P->pers->pool_u1(v, a, nt[v], P->st);
+    else if (kind == 5) P->pers->pool_restore(a, (const int*)P->mslots.p, P->nmuca, P->restore_kb, P->st);
+    else if (kind == 6) P->pers->pool_decide(a, (const int*)P->mslots.p, P->nmuca, P->st);
     else P->pers->pool_scalar(v, kind - 2, a, nt[v], P->st);
   }
   mark(P, -1);
@@ -420,7 +452,7 @@ int enqueue_persist(su2gpu_pool* P, const int4* tiles, int nt, uint32_t* const* 
                     int64_t* tot, unsigned first_item = 0, int spin_limit = 1 << 18, const void* descs = nullptr,
                     int seg = 0) {
   std::vector<PassDesc> passes;
-  sweep_recipe(P->recipe, passes, tot);
+  sweep_recipe(P->recipe, passes, tot, P->mucamask);
   if ((int)passes.size() > PERSIST_MAX_PASSES)
     return fail(SU2GPU_ERR_INVALID, "%d passes per sweep: the persistent sweep takes at most %d", (int)passes.size(),
                 PERSIST_MAX_PASSES);
@@ -449,7 +481,7 @@ int enqueue_persist(su2gpu_pool* P, const int4* tiles, int nt, uint32_t* const* 
     A.nsweeps = nsweeps > 0 ? n : 0;
     PCK(cudaMemsetAsync(P->qstate.p, 0, P->qstate.n, P->st));
     const unsigned grid = (unsigned)std::min<int64_t>(P->persist_grid, per_sweep * std::max(n, 1));
-    P->pers->launch(P->persist_shape, &A, grid, P->st);
+    P->pers->launch(P->persist_shape, P->nmuca > 0, &A, grid, P->st);
     PCK(cudaGetLastError());
     if (nsweeps > 0 && first_item == 0 && sweeps) launch_pool_next_sweep(sweeps, nchains, P->st, (uint32_t)n);
     PCK(cudaGetLastError());
@@ -540,12 +572,15 @@ int su2gpu_pool_destroy(su2gpu_pool* P) {
   if (P->st) cudaStreamSynchronize(P->st);
   if (P->own_st) cudaStreamSynchronize(P->own_st);
   drop_graphs(P);
-  for (Slot& sl : P->slots)
+  for (Slot& sl : P->slots) {
     if (sl.mctx) su2gpu_destroy(sl.mctx);
+    if (sl.mpart) cudaFree(sl.mpart);
+  }
   P->qstate.release();
   P->segs.release();
   P->arena.release(); P->slotmem.release(); P->descs.release(); P->mtiles.release(); P->mfirst.release();
   P->sweepptrs.release(); P->partials.release(); P->sums.release(); P->stage.release(); P->err.release();
+  P->mslots.release();
   for (int v = 0; v < NVARIANTS; v++) P->tiles[v].release();
   for (int k = 0; k < 2; k++)
     if (P->stage_ev[k]) cudaEventDestroy(P->stage_ev[k]);
@@ -610,6 +645,7 @@ int su2gpu_pool_remove(su2gpu_pool* P, int32_t s) {
   PCK(cudaStreamSynchronize(P->st));
   arena_free(P, P->slots[s].off, P->slots[s].bytes);
   if (P->slots[s].mctx) su2gpu_destroy(P->slots[s].mctx);
+  if (P->slots[s].mpart) cudaFree(P->slots[s].mpart);
   P->slots[s] = Slot();
   P->dirty = true;
   P->seg_tuned = 0;
@@ -1318,7 +1354,7 @@ int su2gpu_pool_set_persistent(su2gpu_pool* P, int32_t on) {
   if (on > 0) {
     std::vector<PassDesc> passes;
     int64_t counts[SU2GPU_NCOUNTERS] = {0};
-    sweep_recipe(P->recipe, passes, counts);
+    sweep_recipe(P->recipe, passes, counts, P->mucamask);
     if ((int)passes.size() > PERSIST_MAX_PASSES)
       return fail(SU2GPU_ERR_INVALID, "the recipe has %d passes per sweep: the persistent sweep takes at most %d",
                   (int)passes.size(), PERSIST_MAX_PASSES);
@@ -1410,6 +1446,10 @@ int su2gpu_pool_muca_set(su2gpu_pool* P, int32_t s, const su2gpu_weight* w) {
     if ((rc = su2gpu_calc_orderparam(sl.mctx, par, nullptr))) return rc;
   int mop = 0, cps = 0, acc = 0;
   if ((rc = su2gpu_muca_device_state(sl.mctx, &sl.mdev, &sl.mbackup, &mop, &cps, &acc))) return rc;
+  if (!sl.mpart && cudaMalloc((void**)&sl.mpart, (size_t)((sl.g.half + 31) / 32) * sizeof(double)) != cudaSuccess) {
+    sl.mpart = nullptr;
+    return fail(SU2GPU_ERR_NOMEM, "cudaMalloc of the order parameter's partial sums failed");
+  }
   sl.mop = acc ? mop : 0;
   P->dirty = true;
   drop_graphs(P);
@@ -1472,6 +1512,10 @@ int su2gpu_pool_launches_per_sweep(su2gpu_pool* P, int32_t* n) {
   if (nh) passes += count(p.update_su2doublet, p.algorithm_su2doublet, nh);
   if (p.content & SU2GPU_TRIPLET) passes += count(p.update_su2triplet, p.algorithm_su2triplet, 1);
   if (p.content & SU2GPU_SINGLET) passes += count(p.update_singlet, p.algorithm_singlet, 1);
+  // a decide and a restore pass after every checked half-sweep
+  for (int h = 0; h < nh; h++)
+    if (P->mucamask >> h & 1) passes += 2 * count(p.update_su2doublet, p.algorithm_su2doublet, 1);
+  if ((p.content & SU2GPU_TRIPLET) && (P->mucamask & 4)) passes += 2 * count(p.update_su2triplet, p.algorithm_su2triplet, 1);
   *n = passes + 1;  // + the sweep-counter increment
   return SU2GPU_OK;
 }

@@ -22,13 +22,13 @@ struct __align__(16) ChainDesc {
   uint32_t k0, k1, chain;
   uint32_t* sweep;          // this chain's sweep counter (device word)
   unsigned long long* ctr;  // this chain's counters [24]
-  // multicanonical chains (muca_pool_finish): the weight, the backup of the
-  // updated field (indexed like the field), the sites of the current checked
-  // half-sweep done so far (a slot word), the order parameter (0: no weight
-  // in this chain, or none checked in these passes)
+  // multicanonical chains: the weight, the backup of the updated field
+  // (indexed like the field), the order parameter's sums over the 32-site
+  // warps of a checked half-sweep, the order parameter (0: no weight in
+  // this chain, or none checked in these passes)
   MucaDev* muca;
   void* mbackup;
-  unsigned* mcount;
+  double* mpart;
   int mop;
   int mpad[3];
 };
@@ -52,67 +52,51 @@ __device__ inline Q<R> ldcg4(const V4<R>* p, int i) {
     return Q<R>{a.x, a.y, b.x, b.y};
   }
 }
+// The multicanonical check of a pool chain's checked half-sweep
+// (muca_check, update.c:13-30, with one check per half-sweep) takes three
+// steps.  The update tiles keep the old values in the backup and leave the
+// order parameter's sum over each warp's 32 sites in mpart (a fixed-order
+// warp sum: the same values whatever the launch shape), with no barrier or
+// fence.  The decide pass sums the warp sums in a fixed order (fixed_sum64)
+// and decides (muca_decide_block), once per chain.  The restore pass puts a
+// rejected half back.
 template <typename R>
-__device__ inline double orderparam_site_cg(const Fields<R>& f, int op, int i) {
-  double phi = 0.0, sig = 0.0;
-  if (op == 1 || op == 3 || op == 4) phi = (double)doubletsq(ldcg4<R>(php(f, op == 4 ? 1 : 0), i));
-  if (op == 2 || op == 3)
-    sig = (double)tripletsq(V3<R>{__ldcg(f.trip[0] + i), __ldcg(f.trip[1] + i), __ldcg(f.trip[2] + i)});
-  return op == 2 ? sig : (op == 3 ? phi - sig : phi);
+__device__ inline void muca_warp_partial(const ChainDesc<R>& d, int t0, double opv) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) opv += __shfl_down_sync(0xffffffffu, opv, o);
+  const int w0 = t0 + (int)(threadIdx.x & ~31u);
+  if ((threadIdx.x & 31) == 0 && w0 < d.g.half) d.mpart[w0 >> 5] = opv;
 }
 
-// The multicanonical check that ends a checked half-sweep of a pool chain
-// (muca_check, update.c:13-30, with one check per half-sweep): every block
-// that updated sites of the chain's parity adds their number to the chain's
-// count; the block that completes it sums the order parameter over the
-// parity in a fixed order (64 lanes over the sites, then a tree -- the same
-// value whatever the tiling or the launch), decides (muca_decide_block) and,
-// on reject, puts the backup back.  In the persistent sweep this happens
-// before the block publishes its item, so the chain's next pass sees the
-// decided fields; other chains' items keep the GPU busy meanwhile.
+// the decision of a chain's checked half-sweep, made by the block that has
+// the chain's first tile (t0 == 0); fields, partial sums and weight are
+// read past L1
 template <typename R, int BS>
-__device__ inline void muca_pool_finish(const ChainDesc<R>& d, int field, int h, int parity, uint32_t pass,
-                                        uint32_t sweep, int t0) {
-  __shared__ int s_last;
-  __shared__ double red[64];
-  const int half = d.g.half;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const unsigned n = (unsigned)min(BS, half - t0);
-    __threadfence();
-    const unsigned prev = atomicAdd(d.mcount, n);
-    s_last = prev + n == (unsigned)half;
-  }
-  __syncthreads();
-  if (!s_last) return;
-  __threadfence();
-  if (threadIdx.x == 0) *d.mcount = 0;
-  if (threadIdx.x < 64) {
-    double v = 0.0;
-    for (int t = threadIdx.x; t < half; t += 64) v += orderparam_site_cg<R>(d.f, d.mop, parity * half + t);
-    red[threadIdx.x] = v;
-  }
-  __syncthreads();
-#pragma unroll
-  for (int k = 32; k > 0; k >>= 1) {
-    if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
-    __syncthreads();
-  }
-  const double tot = red[0] / (double)d.g.V;
+__device__ __noinline__ void tile_decide(const ChainDesc<R>& d, int field, int h, int parity, uint32_t pass,
+                                         uint32_t sweep, int t0) {
+  if (t0 != 0 || !d.mop || !muca_checked(field, h, d.mop)) return;
+  const double tot = fixed_sum64(d.mpart, (d.g.half + 31) / 32) / (double)d.g.V;
   const RngKey rk{d.k0, d.k1, d.chain, nullptr};
-  const int accept = muca_decide_block(d.muca, tot, parity, rk, pass, 0u, sweep, d.ctr);
-  if (!accept) {
-    for (int t = threadIdx.x; t < half; t += BS) {
-      const int i = parity * half + t;
-      if (field == 0) {
-        st4<R>(php(d.f, h), i, ldcg4<R>((const V4<R>*)d.mbackup, i));
-      } else {
-        const R* b = (const R*)d.mbackup;
-        st3(d.f, i, V3<R>{__ldcg(b + 3 * i), __ldcg(b + 3 * i + 1), __ldcg(b + 3 * i + 2)});
-      }
-    }
+  muca_decide_block(d.muca, tot, parity, rk, pass, 0u, sweep, d.ctr);
+}
+
+// site t of the parity back from the backup
+template <typename R>
+__device__ inline void restore_site(const ChainDesc<R>& d, int field, int h, int parity, int t) {
+  const int i = parity * d.g.half + t;
+  if (field == 0) {
+    st4<R>(php(d.f, h), i, ldcg4<R>((const V4<R>*)d.mbackup, i));
+  } else {
+    const R* b = (const R*)d.mbackup;
+    st3(d.f, i, V3<R>{__ldcg(b + 3 * i), __ldcg(b + 3 * i + 1), __ldcg(b + 3 * i + 2)});
   }
-  __syncthreads();
+}
+
+// whether chain d's check of this half-sweep rejected (the flag is read
+// past L1: the decide pass wrote it)
+template <typename R>
+__device__ inline bool muca_rejected(const ChainDesc<R>& d, int field, int h) {
+  return d.mop && muca_checked(field, h, d.mop) && !*(volatile const int*)&d.muca->last_accept;
 }
 
 struct PoolArgs {
@@ -146,6 +130,14 @@ __device__ inline const ChainDesc<R>& stage_desc_slot(const void* descs, int slo
 template <typename R>
 __device__ inline const ChainDesc<R>& stage_desc(const PoolArgs& a, int slot) {
   return stage_desc_slot<R>(a.descs, slot);
+}
+
+// the restore pass's tile in the persistent sweep
+template <typename R, int BS>
+__device__ __noinline__ void tile_restore(const ChainDesc<R>& d, int field, int h, int parity, int t0) {
+  if (!muca_rejected(d, field, h)) return;
+  const int t = t0 + threadIdx.x;
+  if (t < d.g.half) restore_site(d, field, h, parity, t);
 }
 
 // The per-tile work of the update passes: the sites [t0, t0 + blockDim.x)
@@ -189,15 +181,18 @@ __device__ __noinline__ void tile_u1(const ChainDesc<R>& d, int parity, uint32_t
 }
 
 // FIELD 0 doublet `sub`, 1 triplet, 2 singlet; force: the pass's forced
-// Metropolis flag (the last scalar sweep of an overrelaxation field)
-template <typename R, int CC, int FIELD, int BS, int MINB>
+// Metropolis flag (the last scalar sweep of an overrelaxation field).
+// CHECKED: a multicanonical chain's checked half-sweep, which keeps the old
+// values in the backup and sums the order parameter over the new ones (an
+// instance of its own, so the plain update carries none of it)
+template <typename R, int CC, int FIELD, int BS, int MINB, bool CHECKED>
 __device__ __noinline__ void tile_scalar(const ChainDesc<R>& d, int parity, int sub, int force, uint32_t pass,
                                    uint32_t sweep, int t0) {
   const CoupT<R>& cp = d.cp;
   int t = t0 + threadIdx.x;
   int acc = 0, fb = 0;
-  // a multicanonical chain keeps the old values of a checked half-sweep
-  const bool checked = FIELD != 2 && d.mop != 0 && muca_checked(FIELD, sub, d.mop);
+  constexpr bool checked = CHECKED && FIELD != 2;
+  double opv = 0.0;
   if (t < d.g.half) {
     int c[3];
     site_coords(d.g, parity, t, c);
@@ -224,13 +219,23 @@ __device__ __noinline__ void tile_scalar(const ChainDesc<R>& d, int parity, int 
       if (cp.alg_s == ALG_OR && !force) acc = overrelax_singlet<R, CC>(d.f, d.g, cp, c, i, rng, &fb);
       else acc = metro_singlet<R, CC>(d.f, d.g, cp, c, i, rng);
     }
+    if (checked) opv = orderparam_site<R>(d.f, d.mop, i);
   }
+  if (checked) muca_warp_partial(d, t0, opv);
   int base_or = FIELD == 0 ? 10 + sub : (FIELD == 1 ? 15 : 19);
   int base_mt = FIELD == 0 ? 6 + sub : (FIELD == 1 ? 13 : 17);
   bool any_or = (FIELD == 0 ? cp.alg_d : (FIELD == 1 ? cp.alg_t : cp.alg_s)) == ALG_OR && !force;
   warp_count(d.ctr + (any_or ? base_or : base_mt), acc);
   warp_count(d.ctr + 23, fb);
-  if (checked) muca_pool_finish<R, BS>(d, FIELD, sub, parity, pass, sweep, t0);
+}
+
+template <typename R, int CC, int FIELD, int BS, int MINB>
+__device__ __noinline__ void tile_scalar_any(const ChainDesc<R>& d, int parity, int sub, int force, uint32_t pass,
+                                       uint32_t sweep, int t0) {
+  if (FIELD != 2 && d.mop != 0 && muca_checked(FIELD, sub, d.mop))
+    tile_scalar<R, CC, FIELD, BS, MINB, FIELD != 2>(d, parity, sub, force, pass, sweep, t0);
+  else
+    tile_scalar<R, CC, FIELD, BS, MINB, false>(d, parity, sub, force, pass, sweep, t0);
 }
 
 // one launch per pass: block b works on tile b of the table
@@ -255,7 +260,36 @@ __global__ void __launch_bounds__(BS, MINB) k_pool_scalar(PoolArgs a) {
   int2 tile = a.tiles[blockIdx.x];
   if (bad_tile(a, tile)) return;
   const ChainDesc<R>& d = stage_desc<R>(a, tile.x);
-  tile_scalar<R, CC, FIELD, BS, MINB>(d, a.parity, a.sub, a.alg, a.pass, *d.sweep, tile.y);
+  tile_scalar_any<R, CC, FIELD, BS, MINB>(d, a.parity, a.sub, a.alg, a.pass, *d.sweep, tile.y);
+}
+
+// The decide and restore passes with one launch per pass, over the pool's
+// multicanonical chains (mslots, nmuca of them): sub = the doublet, alg = the
+// field (0 doublet, 1 triplet) of the checked half-sweep before them.
+// Decide: one block per chain.  Restore: `kb` blocks per chain, which read
+// the chain's flag in place and leave at once where the check accepted.
+template <typename R, int BS, int MINB>
+__global__ void __launch_bounds__(BS, MINB) k_pool_decide(PoolArgs a, const int* mslots) {
+  const int slot = mslots[blockIdx.x];
+  if ((unsigned)slot >= (unsigned)a.nslots) {
+    if (threadIdx.x == 0) atomicOr(a.err, 2);
+    return;
+  }
+  const ChainDesc<R>& d = stage_desc<R>(a, slot);
+  tile_decide<R, BS>(d, a.alg, a.sub, a.parity, a.pass, *d.sweep, 0);
+}
+
+template <typename R, int BS, int MINB>
+__global__ void __launch_bounds__(BS, MINB) k_pool_restore(PoolArgs a, const int* mslots, int kb) {
+  const int c = blockIdx.x / kb, b = blockIdx.x - c * kb;
+  const int slot = mslots[c];
+  if ((unsigned)slot >= (unsigned)a.nslots) {
+    if (threadIdx.x == 0 && b == 0) atomicOr(a.err, 2);
+    return;
+  }
+  const ChainDesc<R>& d = ((const ChainDesc<R>*)a.descs)[slot];
+  if (!muca_rejected(d, a.alg, a.sub)) return;
+  for (int t = b * BS + threadIdx.x; t < d.g.half; t += kb * BS) restore_site(d, a.alg, a.sub, a.parity, t);
 }
 
 // ---------------------------------------------------------------------------
@@ -282,9 +316,12 @@ __global__ void __launch_bounds__(BS, MINB) k_pool_scalar(PoolArgs a) {
 constexpr int PERSIST_MAX_PASSES = 64;
 
 // one pass of the sweep recipe: kind 0 links, 1 U(1), 2 doublet, 3 triplet,
-// 4 singlet; sub: the direction (links, U(1)) or the doublet; alg: the link
-// algorithm of a link pass, the forced Metropolis flag of a scalar pass (as
-// PoolArgs.alg); pass: the pass number within the sweep
+// 4 singlet; in pools with multicanonical chains a doublet / triplet pass is
+// followed by 6, the multicanonical decision, and 5, the restore; sub: the
+// direction (links, U(1)) or the doublet; alg: the link algorithm of a link
+// pass, the forced Metropolis flag of a scalar pass (as PoolArgs.alg), the
+// field (0 doublet, 1 triplet) of a decide / restore pass; pass: the pass
+// number within the sweep (that of the checked pass, for decide / restore)
 struct PassDesc {
   uint8_t kind, parity, sub, alg;
   uint32_t pass;
@@ -313,8 +350,10 @@ __device__ inline unsigned ld_acquire_gpu(const unsigned* p) {
 }
 
 // one tile of pass p (the tile functions are not inlined: each keeps the
-// kernel's register budget to itself)
-template <typename R, int CC, int BS, int MINB>
+// kernel's register budget to itself).  MUCA: the instance for pools with
+// multicanonical chains (checked half-sweeps and restore passes); the other
+// carries none of that code.
+template <typename R, int CC, int BS, int MINB, bool MUCA>
 __device__ inline void persist_tile(const ChainDesc<R>& d, PassDesc p, uint32_t sweep, int t0, int* errp) {
   switch (p.kind) {
     case 0:
@@ -330,18 +369,29 @@ __device__ inline void persist_tile(const ChainDesc<R>& d, PassDesc p, uint32_t 
       }
       break;
     case 2:
-      if (SU2_HAS(CC, d.cp.content, C_H1 | C_H2))
-        tile_scalar<R, CC, 0, BS, MINB>(d, p.parity, p.sub, p.alg, p.pass, sweep, t0);
+      if (SU2_HAS(CC, d.cp.content, C_H1 | C_H2)) {
+        if (MUCA) tile_scalar_any<R, CC, 0, BS, MINB>(d, p.parity, p.sub, p.alg, p.pass, sweep, t0);
+        else tile_scalar<R, CC, 0, BS, MINB, false>(d, p.parity, p.sub, p.alg, p.pass, sweep, t0);
+      }
       break;
     case 3:
-      if (SU2_HAS(CC, d.cp.content, C_T)) tile_scalar<R, CC, 1, BS, MINB>(d, p.parity, 0, p.alg, p.pass, sweep, t0);
+      if (SU2_HAS(CC, d.cp.content, C_T)) {
+        if (MUCA) tile_scalar_any<R, CC, 1, BS, MINB>(d, p.parity, 0, p.alg, p.pass, sweep, t0);
+        else tile_scalar<R, CC, 1, BS, MINB, false>(d, p.parity, 0, p.alg, p.pass, sweep, t0);
+      }
+      break;
+    case 5:
+      if (MUCA) tile_restore<R, BS>(d, p.alg, p.sub, p.parity, t0);
+      break;
+    case 6:
+      if (MUCA) tile_decide<R, BS>(d, p.alg, p.sub, p.parity, p.pass, sweep, t0);
       break;
     default:
-      if (SU2_HAS(CC, d.cp.content, C_S)) tile_scalar<R, CC, 2, BS, MINB>(d, p.parity, 0, p.alg, p.pass, sweep, t0);
+      if (SU2_HAS(CC, d.cp.content, C_S)) tile_scalar<R, CC, 2, BS, MINB, false>(d, p.parity, 0, p.alg, p.pass, sweep, t0);
   }
 }
 
-template <typename R, int CC, int BS, int MINB>
+template <typename R, int CC, int BS, int MINB, bool MUCA>
 __global__ void __launch_bounds__(BS, MINB) k_pool_persist(PersistArgs a) {
   __shared__ unsigned s_item;
   __shared__ int4 s_tile, s_next;
@@ -408,7 +458,7 @@ __global__ void __launch_bounds__(BS, MINB) k_pool_persist(PersistArgs a) {
       const PassDesc p = a.passes[k];
       const uint32_t sweep = *d.sweep + s;
       for (int j = 0, t0 = tile.y; j < a.seg && t0 < d.g.half; j++, t0 += BS)
-        persist_tile<R, CC, BS, MINB>(d, p, sweep, t0, a.err);
+        persist_tile<R, CC, BS, MINB, MUCA>(d, p, sweep, t0, a.err);
     }
     __syncthreads();
     if (threadIdx.x == 0 && !bad) {
