@@ -179,26 +179,24 @@ __device__ inline Q<double> clover(const PlainLat& p, const int* c, int d1, int 
   return cl;
 }
 
-// project_u1 (magfield.c:120-184): Pi(c) U_d(c) Pi(c+d), Pi = (1 + n.sigma)/2
-__device__ inline CM<double> plain_project_u1(const PlainLat& p, const int* c, int d) {
-  const int n = plain_index(p, c);
-  Q<double> u = plink(p, n, d);
-  CM<double> U;
-  U.re[0] = u.a; U.im[0] = u.d;
-  U.re[1] = u.c; U.im[1] = u.b;
-  U.re[2] = -u.c; U.im[2] = u.b;
-  U.re[3] = u.a; U.im[3] = -u.d;
-  return cm_mul(cm_mul(proj_mat(ptrip(p, n)), U), proj_mat(ptrip(p, plain_nb(p, c, d, 1))));
-}
-// alpha_proj (magfield.c:189-216)
+// alpha_proj (magfield.c:189-216) on the plain layout, from the spinors of
+// the projectors and the four link overlaps (the same angle as the
+// reference's product of projected link matrices; see alpha_proj)
 __device__ inline double plain_alpha_proj(const PlainLat& p, const int* c, int d1, int d2, double sqrt_beta) {
   int c1[3] = {c[0], c[1], c[2]}, c2[3] = {c[0], c[1], c[2]};
   c1[d1] = wrap(c1[d1] + 1, p.L[d1]);
   c2[d2] = wrap(c2[d2] + 1, p.L[d2]);
-  CM<double> t = cm_mul(cm_mul(cm_mul(plain_project_u1(p, c, d1), plain_project_u1(p, c1, d2)),
-                               cm_dag(plain_project_u1(p, c2, d1))),
-                        cm_dag(plain_project_u1(p, c, d2)));
-  return atan2(t.im[0] + t.im[3], t.re[0] + t.re[3]) * sqrt_beta;
+  const int n = plain_index(p, c), n1 = plain_index(p, c1), n2 = plain_index(p, c2), n12 = plain_nb(p, c1, d2, 1);
+  const Spinor<double> sx = proj_spinor(ptrip(p, n)), s1 = proj_spinor(ptrip(p, n1)), s2 = proj_spinor(ptrip(p, n2)),
+                       s12 = proj_spinor(ptrip(p, n12));
+  double z1r, z1i, z2r, z2i, z3r, z3i, z4r, z4i;
+  link_overlap(sx, plink(p, n, d1), s1, z1r, z1i);
+  link_overlap(s1, plink(p, n1, d2), s12, z2r, z2i);
+  link_overlap(s2, plink(p, n2, d1), s12, z3r, z3i);
+  link_overlap(sx, plink(p, n, d2), s2, z4r, z4i);
+  const double pr = z1r * z2r - z1i * z2i, pi = z1r * z2i + z1i * z2r;
+  const double qr = z3r * z4r - z3i * z4i, qi = z3r * z4i + z3i * z4r;
+  return atan2(pi * qr - pr * qi, pr * qr + pi * qi) * sqrt_beta;
 }
 
 // Per plane z (blockIdx.y) and chunk (blockIdx.x) of its sites: q = 0 the sum

@@ -1221,78 +1221,64 @@ __global__ void k_muca_set_param(MucaDev* w, const double* partials, int np, dou
 // ---------------------------------------------------------------------------
 // measurements (measure.c:71-243)
 // ---------------------------------------------------------------------------
-// complex 2x2 matrices for the projected U(1) links (magfield.c:32-184)
+// The projected U(1) links (magfield.c:32-184) and the plaquette angle
+// alpha_proj (magfield.c:189-216).  The reference forms each projected link
+// Pi(x) U_mu(x) Pi(x+mu), Pi = (1 + n.sigma)/2, n = Sigma/|Sigma| (projector(),
+// project_u1()), as a complex 2x2 matrix, multiplies the four of a plaquette
+// and takes the argument of the trace.  Pi is the rank-one projector |n><n|
+// onto the +1 eigenvector of n.sigma, so the product collapses to
+//   tr = z(x,d1) z(x+d1,d2) conj(z(x+d2,d1)) conj(z(x,d2)),
+//   z(a,mu) = <n_a| U_mu(a) |n_{a+mu}>,
+// the same number (the phase of each |n> cancels around the closed loop),
+// from 4 spinors and 4 overlaps instead of 8 projectors and 11 matrix
+// products.  Each site's spinor takes the chart that avoids the pole opposite
+// to Sigma: (|S| + S3, S1 + i S2) or (S1 - i S2, |S| - S3), normalised.
 template <typename R>
-struct CM {
-  R re[4], im[4];
+struct Spinor {
+  R r0, i0, r1, i1;
 };
 template <typename R>
-__device__ inline CM<R> cm_mul(const CM<R>& a, const CM<R>& b) {
-  CM<R> t;
-#pragma unroll
-  for (int i = 0; i < 2; i++)
-#pragma unroll
-    for (int j = 0; j < 2; j++) {
-      R sr = 0, si = 0;
-#pragma unroll
-      for (int k = 0; k < 2; k++) {
-        R ar = a.re[2 * i + k], ai = a.im[2 * i + k], br = b.re[2 * k + j], bi = b.im[2 * k + j];
-        sr += ar * br - ai * bi;
-        si += ar * bi + ai * br;
-      }
-      t.re[2 * i + j] = sr;
-      t.im[2 * i + j] = si;
-    }
-  return t;
+__device__ inline Spinor<R> proj_spinor(const V3<R>& a) {
+  const R m = msqrt(a.x * a.x + a.y * a.y + a.z * a.z);
+  Spinor<R> s;
+  if (a.z >= 0) {
+    const R k = (R)1 / msqrt((R)2 * m * (m + a.z));
+    s.r0 = (m + a.z) * k; s.i0 = 0; s.r1 = a.x * k; s.i1 = a.y * k;
+  } else {
+    const R k = (R)1 / msqrt((R)2 * m * (m - a.z));
+    s.r0 = a.x * k; s.i0 = -a.y * k; s.r1 = (m - a.z) * k; s.i1 = 0;
+  }
+  return s;
 }
+// z = <va| U |vb>, U = [[a + i d, c + i b], [-c + i b, a - i d]] (the SU(2)
+// matrix of the link quaternion, as project_u1 builds it)
 template <typename R>
-__device__ inline CM<R> cm_dag(const CM<R>& a) {
-  CM<R> t;
-#pragma unroll
-  for (int i = 0; i < 2; i++)
-#pragma unroll
-    for (int j = 0; j < 2; j++) {
-      t.re[2 * i + j] = a.re[2 * j + i];
-      t.im[2 * i + j] = -a.im[2 * j + i];
-    }
-  return t;
+__device__ inline void link_overlap(const Spinor<R>& va, const Q<R>& u, const Spinor<R>& vb, R& zr, R& zi) {
+  const R w0r = u.a * vb.r0 - u.d * vb.i0 + u.c * vb.r1 - u.b * vb.i1;
+  const R w0i = u.a * vb.i0 + u.d * vb.r0 + u.c * vb.i1 + u.b * vb.r1;
+  const R w1r = -u.c * vb.r0 - u.b * vb.i0 + u.a * vb.r1 + u.d * vb.i1;
+  const R w1i = -u.c * vb.i0 + u.b * vb.r0 + u.a * vb.i1 - u.d * vb.r1;
+  zr = va.r0 * w0r + va.i0 * w0i + va.r1 * w1r + va.i1 * w1i;
+  zi = va.r0 * w0i - va.i0 * w0r + va.r1 * w1i - va.i1 * w1r;
 }
-// projector() / project_u1(): Pi(x) U_mu(x) Pi(x+mu), Pi = (1 + n.sigma)/2
-template <typename R>
-__device__ inline CM<R> proj_mat(const V3<R>& a) {
-  R m = msqrt(a.x * a.x + a.y * a.y + a.z * a.z);
-  R n1 = a.x / m, n2 = a.y / m, n3 = a.z / m;
-  CM<R> P;
-  P.re[0] = (R)0.5 * ((R)1 + n3); P.im[0] = 0;
-  P.re[1] = (R)0.5 * n1;          P.im[1] = (R)-0.5 * n2;
-  P.re[2] = (R)0.5 * n1;          P.im[2] = (R)0.5 * n2;
-  P.re[3] = (R)0.5 * ((R)1 - n3); P.im[3] = 0;
-  return P;
-}
-template <typename R>
-__device__ inline CM<R> project_u1(const Fields<R>& f, const Geom& g, const int* c, int i, int d) {
-  Q<R> u = ld4<R>(lk(f, d), i);
-  CM<R> U;
-  U.re[0] = u.a; U.im[0] = u.d;
-  U.re[1] = u.c; U.im[1] = u.b;
-  U.re[2] = -u.c; U.im[2] = u.b;
-  U.re[3] = u.a; U.im[3] = -u.d;
-  return cm_mul(cm_mul(proj_mat(ld3(f, i)), U), proj_mat(ld3(f, shifted(g, c, d, 1))));
-}
-// alpha_proj (magfield.c:189-216)
 template <typename R>
 __device__ inline R alpha_proj(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i, int d1,
                                int d2) {
-  int c1[3], c2[3];
+  int c1[3];
   shift_coords(g, c, d1, 1, c1);
-  shift_coords(g, c, d2, 1, c2);
-  CM<R> u1 = project_u1(f, g, c, i, d1);
-  CM<R> u2 = project_u1(f, g, c1, shifted(g, c, d1, 1), d2);
-  CM<R> u3 = project_u1(f, g, c2, shifted(g, c, d2, 1), d1);
-  CM<R> u4 = project_u1(f, g, c, i, d2);
-  CM<R> t = cm_mul(cm_mul(cm_mul(u1, u2), cm_dag(u3)), cm_dag(u4));
-  R a = matan2(t.im[0] + t.im[3], t.re[0] + t.re[3]);
-  return a * msqrt((R)cp.beta);
+  const int i1 = shifted(g, c, d1, 1), i2 = shifted(g, c, d2, 1), i12 = shifted(g, c1, d2, 1);
+  const Spinor<R> sx = proj_spinor(ld3(f, i)), s1 = proj_spinor(ld3(f, i1)), s2 = proj_spinor(ld3(f, i2)),
+                  s12 = proj_spinor(ld3(f, i12));
+  R z1r, z1i, z2r, z2i, z3r, z3i, z4r, z4i;
+  link_overlap(sx, ld4<R>(lk(f, d1), i), s1, z1r, z1i);
+  link_overlap(s1, ld4<R>(lk(f, d2), i1), s12, z2r, z2i);
+  link_overlap(s2, ld4<R>(lk(f, d1), i2), s12, z3r, z3i);
+  link_overlap(sx, ld4<R>(lk(f, d2), i), s2, z4r, z4i);
+  // (z1 z2) conj(z3 z4)
+  const R pr = z1r * z2r - z1i * z2i, pi = z1r * z2i + z1i * z2r;
+  const R qr = z3r * z4r - z3i * z4i, qi = z3r * z4i + z3i * z4r;
+  const R tr = pr * qr + pi * qi, ti = pi * qr - pr * qi;
+  return matan2(ti, tr) * msqrt((R)cp.beta);
 }
 
 // alpha(x; 0,1), alpha(x; 0,2), alpha(x; 1,2) for every site
