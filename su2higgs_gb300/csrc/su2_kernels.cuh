@@ -1357,6 +1357,60 @@ __device__ inline double magcharge_site(const Fields<R>& f, const Geom& g, const
   return q;
 }
 
+// magcharge_cube with the projections computed here: the cube's 8 corner
+// spinors and 12 edge overlaps once each (each edge borders two of the six
+// faces), then the six face angles as alpha_proj forms them
+template <typename R>
+__device__ inline R face_angle(R ar, R ai, R br, R bi, R cr, R ci, R dr, R di, R sqrt_beta) {
+  const R pr = ar * br - ai * bi, pi = ar * bi + ai * br;
+  const R qr = cr * dr - ci * di, qi = cr * di + ci * dr;
+  return matan2(pi * qr - pr * qi, pr * qr + pi * qi) * sqrt_beta;
+}
+template <typename R>
+__device__ inline double magcharge_site(const Fields<R>& f, const Geom& g, const CoupT<R>& cp, const int* c, int i,
+                                        const AlphaOnTheFly&) {
+  int c0[3], c1[3], c01[3];
+  shift_coords(g, c, 0, 1, c0);
+  shift_coords(g, c, 1, 1, c1);
+  shift_coords(g, c0, 1, 1, c01);
+  const int i0 = shifted(g, c, 0, 1), i1 = shifted(g, c, 1, 1), i2 = shifted(g, c, 2, 1);
+  const int i01 = shifted(g, c0, 1, 1), i02 = shifted(g, c0, 2, 1), i12 = shifted(g, c1, 2, 1);
+  const int i012 = shifted(g, c01, 2, 1);
+  const Spinor<R> sx = proj_spinor(ld3(f, i)), s0 = proj_spinor(ld3(f, i0)), s1 = proj_spinor(ld3(f, i1)),
+                  s2 = proj_spinor(ld3(f, i2)), s01 = proj_spinor(ld3(f, i01)), s02 = proj_spinor(ld3(f, i02)),
+                  s12 = proj_spinor(ld3(f, i12)), s012 = proj_spinor(ld3(f, i012));
+  // z(y, mu) = <n_y| U_mu(y) |n_{y+mu}> on the cube's edges
+  R x0r, x0i, x1r, x1i, x2r, x2i, a1r, a1i, a2r, a2i, b0r, b0i, b2r, b2i, e0r, e0i, e1r, e1i, f2r, f2i, g1r, g1i,
+      h0r, h0i;
+  link_overlap(sx, ld4<R>(lk(f, 0), i), s0, x0r, x0i);       // (x, 0)
+  link_overlap(sx, ld4<R>(lk(f, 1), i), s1, x1r, x1i);       // (x, 1)
+  link_overlap(sx, ld4<R>(lk(f, 2), i), s2, x2r, x2i);       // (x, 2)
+  link_overlap(s0, ld4<R>(lk(f, 1), i0), s01, a1r, a1i);     // (x+0, 1)
+  link_overlap(s0, ld4<R>(lk(f, 2), i0), s02, a2r, a2i);     // (x+0, 2)
+  link_overlap(s1, ld4<R>(lk(f, 0), i1), s01, b0r, b0i);     // (x+1, 0)
+  link_overlap(s1, ld4<R>(lk(f, 2), i1), s12, b2r, b2i);     // (x+1, 2)
+  link_overlap(s2, ld4<R>(lk(f, 0), i2), s02, e0r, e0i);     // (x+2, 0)
+  link_overlap(s2, ld4<R>(lk(f, 1), i2), s12, e1r, e1i);     // (x+2, 1)
+  link_overlap(s01, ld4<R>(lk(f, 2), i01), s012, f2r, f2i);  // (x+0+1, 2)
+  link_overlap(s02, ld4<R>(lk(f, 1), i02), s012, g1r, g1i);  // (x+0+2, 1)
+  link_overlap(s12, ld4<R>(lk(f, 0), i12), s012, h0r, h0i);  // (x+1+2, 0)
+  const R sb = msqrt((R)cp.beta);
+  double q = 0.0;
+  // plane (1,2) at x + 0 minus at x
+  double B1 = (double)face_angle(x1r, x1i, b2r, b2i, e1r, e1i, x2r, x2i, sb);
+  double B2 = (double)face_angle(a1r, a1i, f2r, f2i, g1r, g1i, a2r, a2i, sb);
+  q += B2 - B1;
+  // plane (0,2): at x minus at x + 1
+  B1 = -(double)face_angle(x0r, x0i, a2r, a2i, e0r, e0i, x2r, x2i, sb);
+  B2 = -(double)face_angle(b0r, b0i, f2r, f2i, h0r, h0i, b2r, b2i, sb);
+  q += B2 - B1;
+  // plane (0,1) at x + 2 minus at x
+  B1 = (double)face_angle(x0r, x0i, a1r, a1i, b0r, b0i, x1r, x1i, sb);
+  B2 = (double)face_angle(e0r, e0i, g1r, g1i, h0r, h0i, e1r, e1i, sb);
+  q += B2 - B1;
+  return q;
+}
+
 // measure_local (measure.c:368-487): per site (storage order) Tr Sigma^2 and
 // the magnetic charge in units of 2 pi sqrt(beta) -- an integer up to rounding
 template <typename R>
