@@ -1395,20 +1395,22 @@ __device__ inline double magcharge_site(const Fields<R>& f, const Geom& g, const
   link_overlap(s02, ld4<R>(lk(f, 1), i02), s012, g1r, g1i);  // (x+0+2, 1)
   link_overlap(s12, ld4<R>(lk(f, 0), i12), s012, h0r, h0i);  // (x+1+2, 0)
   const R sb = msqrt((R)cp.beta);
-  double q = 0.0;
+  // the charge in the field precision (the angles are): a site's terms are
+  // combined in R, the volume sums are FP64
+  R q = 0;
   // plane (1,2) at x + 0 minus at x
-  double B1 = (double)face_angle(x1r, x1i, b2r, b2i, e1r, e1i, x2r, x2i, sb);
-  double B2 = (double)face_angle(a1r, a1i, f2r, f2i, g1r, g1i, a2r, a2i, sb);
+  R B1 = face_angle(x1r, x1i, b2r, b2i, e1r, e1i, x2r, x2i, sb);
+  R B2 = face_angle(a1r, a1i, f2r, f2i, g1r, g1i, a2r, a2i, sb);
   q += B2 - B1;
   // plane (0,2): at x minus at x + 1
-  B1 = -(double)face_angle(x0r, x0i, a2r, a2i, e0r, e0i, x2r, x2i, sb);
-  B2 = -(double)face_angle(b0r, b0i, f2r, f2i, h0r, h0i, b2r, b2i, sb);
+  B1 = -face_angle(x0r, x0i, a2r, a2i, e0r, e0i, x2r, x2i, sb);
+  B2 = -face_angle(b0r, b0i, f2r, f2i, h0r, h0i, b2r, b2i, sb);
   q += B2 - B1;
   // plane (0,1) at x + 2 minus at x
-  B1 = (double)face_angle(x0r, x0i, a1r, a1i, b0r, b0i, x1r, x1i, sb);
-  B2 = (double)face_angle(e0r, e0i, g1r, g1i, h0r, h0i, e1r, e1i, sb);
+  B1 = face_angle(x0r, x0i, a1r, a1i, b0r, b0i, x1r, x1i, sb);
+  B2 = face_angle(e0r, e0i, g1r, g1i, h0r, h0i, e1r, e1i, sb);
   q += B2 - B1;
-  return q;
+  return (double)q;
 }
 
 // measure_local (measure.c:368-487): per site (storage order) Tr Sigma^2 and
@@ -1483,26 +1485,27 @@ __device__ inline void measure_site(const Fields<R>& f, const Geom& g, const Cou
   wl += ((R)1 - (R)0.5 * ptrace(f, g, c, i, 0, 2));
   wl += ((R)1 - (R)0.5 * ptrace(f, g, c, i, 1, 2));
   wl = (R)cp.beta * wl;
-  double act = (double)wl;
+  // the site's action in the field precision (its terms are), summed in FP64
+  R act = wl;
   m[1] += (double)wl;
   if (SU2_HAS(CC, cp.content, C_U1)) {
     R u1w = local_u1wilson(f, g, cp, c, i);
-    act += (double)u1w;
+    act += u1w;
     m[2] += (double)u1w;
   }
-  act += (double)higgspotential<R, CC>(f, cp, i);
+  act += higgspotential<R, CC>(f, cp, i);
   const int nh = SU2_HAS(CC, cp.content, C_H2) ? 2 : (SU2_HAS(CC, cp.content, C_H1) ? 1 : 0);
   for (int h = 0; h < nh; h++) {
     R mod = doubletsq(ld4<R>(php(f, h), i));
     R cov = covariant_doublet<R, CC>(f, g, cp, c, i, h);
-    act += (double)cov;
+    act += cov;
     m[3 + 3 * h] += (double)cov;
     m[4 + 3 * h] += (double)mod;
     m[5 + 3 * h] += (double)(mod * mod);
   }
   if (SU2_HAS(CC, cp.content, C_T)) {
     R covt = covariant_triplet(f, g, c, i);
-    act += (double)covt;
+    act += covt;
     V3<R> tr = ld3(f, i);
     R tm = tripletsq(tr);
     if (nh > 0) m[14] += (double)(doubletsq(ld4<R>(php(f, 0), i)) * tm);
@@ -1531,7 +1534,7 @@ __device__ inline void measure_site(const Fields<R>& f, const Geom& g, const Cou
       kin -= S * Sn;
       scov += S * S - S * Sn;
     }
-    act += (double)kin;
+    act += kin;
     m[17] += (double)scov;
     m[18] += (double)S;
     m[19] += (double)(S * S);
@@ -1543,7 +1546,7 @@ __device__ inline void measure_site(const Fields<R>& f, const Geom& g, const Cou
       m[23] += (double)(mod * S * S);
     }
   }
-  m[0] += act;
+  m[0] += (double)act;
 }
 
 // sums of m[] over the block (blockDim.x == BLOCK) to partials[k * nblocks + block]
