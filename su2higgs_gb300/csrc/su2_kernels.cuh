@@ -1052,22 +1052,49 @@ __device__ inline void muca_update_slow(MucaDev* w) {
 // edge (where the search may stop at either neighbour) or in no bin takes
 // the sequential search.  `sweep` is the chain's sweep number (the global
 // draw's counter); the decision (1 accept) is returned to every thread.
-__device__ inline int muca_decide_block(MucaDev* w, double tot, int parity, const RngKey& rk, uint32_t pass,
-                                        uint32_t check, uint32_t sweep, unsigned long long* ctr) {
+// What the decision reads of the weight besides the bins it searches, and
+// this thread's first bin k = 1 + threadIdx.x (pos[k], pos[k + 1], b[k],
+// slope[k]) -- loaded by the deciding block while it still sums the order
+// parameter, so that the decision itself waits on no global load in the
+// common case (a value strictly inside a bin of the first blockDim.x)
+struct MucaPre {
+  double pv0, pv1, mn, mx;
+  int bins, mode;
+  double cur, nxt, bk, sk;
+};
+__device__ inline MucaPre muca_preload(const MucaDev* w) {
+  MucaPre p;
+  p.pv0 = w->param_value[0];
+  p.pv1 = w->param_value[1];
+  p.mn = w->min;
+  p.mx = w->max;
+  p.bins = w->bins;
+  p.mode = w->mode;
+  p.cur = p.nxt = p.bk = p.sk = 0.0;
+  const int k = 1 + (int)threadIdx.x;
+  if (k <= p.bins) {
+    p.cur = w->pos[k];
+    p.nxt = w->pos[k + 1];
+    p.bk = w->b[k];
+    p.sk = w->slope[k];
+  }
+  return p;
+}
+__device__ inline int muca_decide_block(MucaDev* w, const MucaPre& pre, double tot, int parity, const RngKey& rk,
+                                        uint32_t pass, uint32_t check, uint32_t sweep, unsigned long long* ctr) {
   __shared__ int s_bin[2], s_fuzzy[2], s_accept;
   __shared__ double s_W[2];
-  const double pv0 = w->param_value[0], pv1 = w->param_value[1];
-  const int bins = w->bins;
-  const double* pos = w->pos;
-  const double old = pv0 + pv1;
-  const double nw = tot + (parity ? pv0 : pv1);
+  const int bins = pre.bins;
+  const double old = pre.pv0 + pre.pv1;
+  const double nw = tot + (parity ? pre.pv0 : pre.pv1);
   if (threadIdx.x < 2) {
     s_bin[threadIdx.x] = -1;
     s_fuzzy[threadIdx.x] = 0;
   }
   __syncthreads();
   for (int k = 1 + (int)threadIdx.x; k <= bins; k += (int)blockDim.x) {
-    const double cur = pos[k], nxt = pos[k + 1];
+    const bool first = k == 1 + (int)threadIdx.x;
+    const double cur = first ? pre.cur : w->pos[k], nxt = first ? pre.nxt : w->pos[k + 1];
 #pragma unroll
     for (int j = 0; j < 2; j++) {
       const double v = j ? old : nw;
@@ -1076,17 +1103,24 @@ __device__ inline int muca_decide_block(MucaDev* w, double tot, int parity, cons
     }
   }
   __syncthreads();
-  if (threadIdx.x < 2) {
-    const int j = threadIdx.x;
+  // W = b[bin] + slope[bin] v (get_weight): by the thread that holds the bin,
+  // or with loads by thread j for the other cases
+#pragma unroll
+  for (int j = 0; j < 2; j++) {
     const double v = j ? old : nw;
-    double W;
-    if (v >= w->max) W = w->b[bins + 1];
-    else if (v < w->min) W = w->b[0];
-    else {
-      const int bin = (s_bin[j] < 0 || s_fuzzy[j]) ? muca_whichbin(w, v) : s_bin[j];
-      W = bin >= bins + 1 ? w->b[bins + 1] : w->b[bin] + w->slope[bin] * v;
+    const bool inside = !(v >= pre.mx) && !(v < pre.mn);
+    const bool direct = inside && s_bin[j] >= 1 && !s_fuzzy[j] && s_bin[j] <= (int)blockDim.x;
+    if (direct && s_bin[j] == 1 + (int)threadIdx.x) s_W[j] = pre.bk + pre.sk * v;
+    if (!direct && (int)threadIdx.x == j) {
+      double W;
+      if (v >= pre.mx) W = w->b[bins + 1];
+      else if (v < pre.mn) W = w->b[0];
+      else {
+        const int bin = (s_bin[j] < 0 || s_fuzzy[j]) ? muca_whichbin(w, v) : s_bin[j];
+        W = bin >= bins + 1 ? w->b[bins + 1] : w->b[bin] + w->slope[bin] * v;
+      }
+      s_W[j] = W;
     }
-    s_W[j] = W;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -1094,21 +1128,25 @@ __device__ inline int muca_decide_block(MucaDev* w, double tot, int parity, cons
     const double Wn = s_W[0], Wo = s_W[1];
     double u = philox_uniform53(rk.k0, rk.k1, GLOBAL_SITE, pass, check, sweep, rk.chain, 0);
     int accept = exp(-(Wn - Wo)) > u ? 1 : 0;
-    if (w->mode != 0) {
+    if (pre.mode != 0) {
       double val = accept ? nw : old;
       muca_accumulate(w, val);
       w->muca_count++;
       if (w->muca_count % w->update_interval == 0) {
-        if (w->mode == 1) muca_update_fast(w);
-        else if (w->mode == 2) muca_update_slow(w);
+        if (pre.mode == 1) muca_update_fast(w);
+        else if (pre.mode == 2) muca_update_slow(w);
         w->muca_count = 0;
         w->weight_updates++;
       }
+      // the recursion may have changed the other parity's value: read it back
+      if (!accept) w->param_value[parity] = old - w->param_value[1 - parity];
+    } else if (!accept) {
+      w->param_value[parity] = old - (parity ? pre.pv0 : pre.pv1);
     }
-    if (!accept) w->param_value[parity] = old - w->param_value[1 - parity];
     w->last_accept = accept;
-    ctr[20] += 1;
-    ctr[21] += accept;
+    // fire-and-forget adds: this thread alone writes the chain's counters here
+    atomicAdd(ctr + 20, 1ull);
+    atomicAdd(ctr + 21, (unsigned long long)accept);
     s_accept = accept;
   }
   __syncthreads();
@@ -1123,17 +1161,16 @@ __device__ inline double fixed_sum64(const double* x, int n) {
   __shared__ double red[64];
   if (threadIdx.x < 64) {
     // lane k adds x[k], x[k + 64], ... in that order; the loads are issued
-    // eight at a time
+    // sixteen at a time
     double v = 0.0;
-    int k = threadIdx.x;
-    for (; k + 64 * 7 < n; k += 64 * 8) {
-      double t[8];
+    for (int k = threadIdx.x; k < n; k += 64 * 16) {
+      double t[16];
 #pragma unroll
-      for (int j = 0; j < 8; j++) t[j] = __ldcg(x + k + 64 * j);
+      for (int j = 0; j < 16; j++) t[j] = k + 64 * j < n ? __ldcg(x + k + 64 * j) : 0.0;
 #pragma unroll
-      for (int j = 0; j < 8; j++) v += t[j];
+      for (int j = 0; j < 16; j++)
+        if (k + 64 * j < n) v += t[j];
     }
-    for (; k < n; k += 64) v += __ldcg(x + k);
     red[threadIdx.x] = v;
   }
   __syncthreads();
@@ -1169,6 +1206,8 @@ __device__ inline void muca_fused_finish(const PassArgs& a, double s) {
   __syncthreads();
   if (!s_last) return;
   __threadfence();
+  // the weight, loaded while the sums are formed (only the final block uses it)
+  const MucaPre pre = muca_preload(a.muca);
   const double cs = fixed_sum64(a.partials + c0, (int)csize);
   if (threadIdx.x == 0) {
     a.arrive[1 + chunk] = 0;
@@ -1181,7 +1220,7 @@ __device__ inline void muca_fused_finish(const PassArgs& a, double s) {
   __threadfence();
   const double tot = fixed_sum64(a.partials + nb, (int)nchunks);  // the same value in every thread
   if (threadIdx.x == 0) a.arrive[0] = 0;
-  muca_decide_block(a.muca, tot / a.vol, a.parity, a.rk, a.pass, a.check, *a.rk.sweep, a.ctr);
+  muca_decide_block(a.muca, pre, tot / a.vol, a.parity, a.rk, a.pass, a.check, *a.rk.sweep, a.ctr);
 }
 
 #ifdef SU2_WITH_GLOBAL
@@ -1191,6 +1230,7 @@ __device__ inline void muca_fused_finish(const PassArgs& a, double s) {
 __global__ void k_muca_decide(MucaDev* w, const double* partials, int np, double vol, int parity, RngKey rk,
                               uint32_t pass, uint32_t check, unsigned long long* ctr) {
   __shared__ double red[256];
+  const MucaPre pre = muca_preload(w);
   double v = 0.0;
   for (int k = threadIdx.x; k < np; k += blockDim.x) v += partials[k];
   red[threadIdx.x] = v;
@@ -1199,7 +1239,7 @@ __global__ void k_muca_decide(MucaDev* w, const double* partials, int np, double
     if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
     __syncthreads();
   }
-  muca_decide_block(w, red[0] / vol, parity, rk, pass, check, *rk.sweep, ctr);
+  muca_decide_block(w, pre, red[0] / vol, parity, rk, pass, check, *rk.sweep, ctr);
 }
 
 // calc_orderparam for the host API: store the parity sum

@@ -75,9 +75,10 @@ template <typename R, int BS>
 __device__ __noinline__ void tile_decide(const ChainDesc<R>& d, int field, int h, int parity, uint32_t pass,
                                          uint32_t sweep, int t0) {
   if (t0 != 0 || !d.mop || !muca_checked(field, h, d.mop)) return;
+  const MucaPre pre = muca_preload(d.muca);
   const double tot = fixed_sum64(d.mpart, (d.g.half + 31) / 32) / (double)d.g.V;
   const RngKey rk{d.k0, d.k1, d.chain, nullptr};
-  muca_decide_block(d.muca, tot, parity, rk, pass, 0u, sweep, d.ctr);
+  muca_decide_block(d.muca, pre, tot, parity, rk, pass, 0u, sweep, d.ctr);
 }
 
 // site t of the parity back from the backup
