@@ -675,11 +675,13 @@ def roofline_of(kinds, ms, content, prec, sites, workload):
             "time_share": shares[top] / tot, "shares": {KIND_NAMES[k]: v / tot for k, v in shares.items()}}
 
 
-def persistent_roofline(kinds, launch_ms, S, content, prec, sites, workload, step_ms):
+def persistent_roofline(kinds, launch_ms, S, content, prec, sites, workload, step_ms, groups=None):
     """The persistent sweep kernel (one launch of S sweeps): algorithmic
     bytes of the S sweeps (every pass: REALS_PER_SITE of its kind x sites;
     the passes of one sweep counted from a profiled per-pass sweep) over the
-    median launch time."""
+    median launch time.  groups = (G, NS): the grouped sweep instead, whose
+    per-pass kernels of G groups overlap on NS streams -- the same bytes
+    over the time of the S sweeps of all groups (fork to join)."""
     rsize = 4 if prec == 32 else 8
     kinds = np.asarray(kinds)
     nsw = max(1, int(np.sum(kinds == 0)) // 6)  # profiled sweeps (6 link passes each)
@@ -692,10 +694,19 @@ def persistent_roofline(kinds, launch_ms, S, content, prec, sites, workload, ste
     tr_path = os.path.join(ROOT, "profiles", f"traffic_{workload}.json")
     if os.path.exists(tr_path):
         with open(tr_path) as fh:
-            t = json.load(fh).get("pool_sweep_persistent_per_sweep")
-        traffic = None if t is None else t * S
+            tj = json.load(fh)
+        if groups:
+            # the same per-pass kernels over subsets of the chains: the DRAM
+            # bytes of one launch of each kind over all chains, per sweep
+            per = [tj.get(KIND_NAMES.get(int(k), "")) for k in kinds]
+            traffic = None if any(t is None for t in per) else sum(per) / nsw * S
+        else:
+            t = tj.get("pool_sweep_persistent_per_sweep")
+            traffic = None if t is None else t * S
+    kernel = ("pool_sweep_persistent (k_pool_persist)" if not groups else
+              f"pool sweep, grouped: k_pool_link / k_pool_scalar of {groups[0]} groups on {groups[1]} streams")
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": traffic, "kernel": "pool_sweep_persistent (k_pool_persist)", "peak_source": peak_kind,
+            "traffic": traffic, "kernel": kernel, "peak_source": peak_kind,
             "algorithmic_bytes_per_launch": alg_bytes, "sweeps_per_launch": S, "avg_launch_ms": avg_ms,
             "launches_profiled": len(launch_ms), "time_share": min(1.0, avg_ms / step_ms)}
 
@@ -805,8 +816,10 @@ def run_gpu_batched(args):
     assert np.all(np.isfinite(m_last)), "non-finite measurement"
 
     persistent = pool.persistent
+    groups = pool.sweep_groups
     # the sweep kernels alone: S sweeps per launch (persistent mode: one
-    # launch of the work-list kernel), CUDA events on the pool's stream,
+    # launch of the work-list kernel; grouped: the groups' graphs on several
+    # streams, forked from and joined back into the pool's), CUDA events on the pool's stream,
     # inputs (660 MB) larger than L2 and the L2 flushed between launches
     sweep_ms = []
     with torch.cuda.stream(stream):
@@ -828,9 +841,9 @@ def run_gpu_batched(args):
         ms_all.append(ms)
     kinds_all, ms_all = np.concatenate(kinds_all), np.concatenate(ms_all)
     per_pass = roofline_of(kinds_all, ms_all, "adj", 32, sites, args.workload)
-    if persistent:
+    if persistent or groups[0] > 1:
         roofline = persistent_roofline(kinds_all, sweep_ms, S, "adj", 32, sites, args.workload,
-                                       float(np.median(step_ms)))
+                                       float(np.median(step_ms)), groups=None if persistent else groups)
         roofline["per_pass_mode"] = per_pass
     else:
         roofline = per_pass
@@ -985,7 +998,10 @@ def run_gpu_batched(args):
                      "l2": "fields 660 MB > L2; 256 MiB write between steps outside the step events",
                      "parallelism": f"replicas x{world}", "graph": True,
                      "sweep_mode": "persistent work-list kernel, S sweeps per launch" if persistent
-                     else "one launch per pass",
+                     else (f"grouped: the chains in {groups[0]} groups of about equal sites, each group's "
+                           f"S sweeps one launch per pass (a CUDA graph per group), the groups on {groups[1]} "
+                           "streams in turn" if groups[0] > 1 else "one launch per pass"),
+                     "sweep_groups": {"groups": groups[0], "streams": groups[1]} if groups[0] > 1 else None,
                      "persist_tiles_per_item": pool.persist_tiles if persistent else None,
                      "persist_shape": ({"shape": pool.persist_shape[0], "threads": pool.persist_shape[1],
                                         "blocks_per_sm": pool.persist_shape[2]} if persistent else None),

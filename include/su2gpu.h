@@ -452,6 +452,19 @@ int su2gpu_pool_get_persist_tiles(su2gpu_pool* pool, int32_t* tiles);
  * per SM (threads, blocks_per_sm may be NULL). */
 int su2gpu_pool_set_persist_shape(su2gpu_pool* pool, int32_t shape);
 int su2gpu_pool_get_persist_shape(su2gpu_pool* pool, int32_t* shape, int32_t* threads, int32_t* blocks_per_sm);
+/* The grouped sweep mode: the chains split into `groups` groups of about
+ * equal sites (in slot order), each group's sweeps one launch per pass (a
+ * graph per group), the groups' sweeps on `streams` streams in turn (1 to 8),
+ * so that the passes of several groups run side by side on the GPU.  Same
+ * fields and counters as the other modes, bit for bit.  groups <= 1: off.
+ * It takes precedence over the automatic persistent choice, not over a
+ * forced one (su2gpu_pool_set_persistent(pool, 1)), and is not used for
+ * pools with multicanonical chains.  su2gpu_pool_autotune times a few
+ * (groups, streams) pairs against the pool's other mode and keeps the
+ * fastest when the mode is automatic.  get: the groups and streams in
+ * effect (0 and 1 when off). */
+int su2gpu_pool_set_sweep_groups(su2gpu_pool* pool, int32_t groups, int32_t streams);
+int su2gpu_pool_get_sweep_groups(su2gpu_pool* pool, int32_t* groups, int32_t* streams);
 /* Check of the persistent kernel's bounded dependency wait: runs it on a
  * work list whose dependencies are never met (pass 0 left out), so every
  * wait gives up after spin_limit polls; the chains' fields and sweep
@@ -493,9 +506,10 @@ int su2gpu_pool_enqueue_measure(su2gpu_pool* pool, double* device_sums, int32_t 
 /* Execution stream (a cudaStream_t; NULL = the pool's own stream). */
 int su2gpu_pool_set_stream(su2gpu_pool* pool, void* cuda_stream);
 /* Kernel launches of one pool sweep in the one-launch-per-pass mode (passes
- * + the sweep-counter increment); in the persistent mode, of one
- * su2gpu_pool_run call whatever its number of sweeps (the persistent kernel
- * + the sweep-counter increment). */
+ * + the sweep-counter increment; in the grouped mode that times the number
+ * of groups); in the persistent mode, of one su2gpu_pool_run call whatever
+ * its number of sweeps (the persistent kernel + the sweep-counter
+ * increment). */
 int su2gpu_pool_launches_per_sweep(su2gpu_pool* pool, int32_t* n);
 /* One sweep of every chain with CUDA events around every pass (the chains
  * advance): kinds / ms as su2gpu_profile_sweep. */
@@ -505,7 +519,9 @@ int su2gpu_pool_counters(su2gpu_pool* pool, int32_t slot, int64_t* out);
 /* Launch-shape autotuner over the pool's current chains (as su2gpu_autotune;
  * runs on a scratch copy, the chains do not advance).  In the persistent
  * mode it also times the persistent sweep's work-item sizes and keeps the
- * fastest (su2gpu_pool_get_persist_tiles). */
+ * fastest (su2gpu_pool_get_persist_tiles); in the automatic mode it then
+ * times the grouped sweep (su2gpu_pool_set_sweep_groups) for a few
+ * (groups, streams) pairs against that and keeps the fastest. */
 int su2gpu_pool_autotune(su2gpu_pool* pool, int32_t* choices, float* best_ms);
 int su2gpu_pool_set_variants(su2gpu_pool* pool, const int32_t* choices);
 /* Copy one chain out of the pool into a new single-lattice context (same

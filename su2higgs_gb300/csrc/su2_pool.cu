@@ -156,8 +156,23 @@ struct su2gpu_pool {
   // the download copy stream, and one sweep graph per group of chains
   Buf ring_down;
   cudaStream_t down_st = nullptr;
+  // update streams of the grouped sweep and the cycle, forked from and
+  // joined back into st: the sweeps of consecutive groups run side by side
+  // (highest priority, as own_st, whatever the caller's stream)
+  static constexpr int CYCLE_SWEEP_STREAMS = 8;
+  cudaStream_t sweep_st[CYCLE_SWEEP_STREAMS] = {};
+  std::vector<cudaEvent_t> grp_ev;
+  // the grouped sweep mode (one launch per pass, the chains split into
+  // grp_G groups of about equal sites whose sweeps run on grp_NS streams in
+  // turn; grp_G <= 1: off), its groups (active-chain ranges) and whether it
+  // is in effect for the current membership
+  int grp_G = 0, grp_NS = 1;
+  std::vector<int> h_groups;
+  bool grouped = false;
   std::vector<cudaEvent_t> cyc_ev;
-  struct GroupGraph { int a0, a1, n; cudaGraphExec_t exec; };  // n: sweeps per replay
+  // n: sweeps per replay; per_pass: one launch per pass even where the group
+  // would sweep persistently
+  struct GroupGraph { int a0, a1, n; bool per_pass; cudaGraphExec_t exec; };
   std::vector<GroupGraph> ggraphs;
   ConvItem* h_items = nullptr;  // page-locked conversion items of a cycle (2 per chain)
   size_t h_items_n = 0;
@@ -165,6 +180,14 @@ struct su2gpu_pool {
   std::vector<uint32_t*> h_sweeps;
   size_t rsize() const { return prec == 64 ? 8 : 4; }
 };
+
+// group helpers (defined with the C entry points below)
+extern "C" {
+static int group_graph(su2gpu_pool* P, int a0, int a1, int n, cudaGraphExec_t* out, bool per_pass);
+static int enqueue_group_sweep(su2gpu_pool* P, int a0, int a1, int n, int64_t* tot, bool per_pass);
+static std::vector<int> make_groups(const su2gpu_pool* P, int G, bool light_ends);
+static int sweep_streams(su2gpu_pool* P, int NS, std::vector<cudaStream_t>& ss);
+}
 
 namespace {
 
@@ -314,6 +337,15 @@ int rebuild(su2gpu_pool* P, void* arena_base = nullptr, void* slot_base = nullpt
     const bool fits = P->npasses <= PERSIST_MAX_PASSES;
     P->persistent = fits && (P->persist_mode == 1 ||
                              (P->persist_mode < 0 && P->active.size() >= 8 && seg_auto >= 4));
+    // the grouped mode (set by the autotuner or su2gpu_pool_set_sweep_groups)
+    // takes precedence over the automatic choice, not over a forced one
+    P->grouped = P->grp_G > 1 && (int)P->active.size() > 1 && P->persist_mode != 1 && P->nmuca == 0;
+    if (P->grouped) {
+      P->persistent = false;
+      P->h_groups = make_groups(P, P->grp_G, false);
+    } else {
+      P->h_groups.clear();
+    }
     P->h_segs.clear();
     P->h_sfirst.clear();
     for (int s : P->active) {
@@ -586,14 +618,19 @@ int su2gpu_pool_destroy(su2gpu_pool* P) {
     if (P->stage_ev[k]) cudaEventDestroy(P->stage_ev[k]);
   if (P->copy_st) cudaStreamSynchronize(P->copy_st);
   if (P->down_st) cudaStreamSynchronize(P->down_st);
+  for (cudaStream_t x : P->sweep_st)
+    if (x) cudaStreamSynchronize(x);
   P->ring.release();
   P->ring_down.release();
   for (cudaEvent_t e : P->ring_ev) cudaEventDestroy(e);
   for (cudaEvent_t e : P->cyc_ev) cudaEventDestroy(e);
+  for (cudaEvent_t e : P->grp_ev) cudaEventDestroy(e);
   if (P->h_items) cudaFreeHost(P->h_items);
   P->d_items.release();
   if (P->copy_st) cudaStreamDestroy(P->copy_st);
   if (P->down_st) cudaStreamDestroy(P->down_st);
+  for (cudaStream_t x : P->sweep_st)
+    if (x) cudaStreamDestroy(x);
   if (P->own_st) cudaStreamDestroy(P->own_st);
   delete P;
   return SU2GPU_OK;
@@ -978,6 +1015,7 @@ int su2gpu_pool_set_sweep(su2gpu_pool* P, int32_t s, uint32_t sweep) {
   return SU2GPU_OK;
 }
 
+
 static int pool_enqueue(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
   if (!P || nsweeps < 0) return fail(SU2GPU_ERR_INVALID, "bad pool run arguments");
   int rc;
@@ -1018,6 +1056,37 @@ static int pool_enqueue(su2gpu_pool* P, int32_t nsweeps, int32_t use_graph) {
                                      tot))) {
       return rc;
     }
+  } else if (P->grouped) {
+    // the groups' sweeps on grp_NS streams in turn, forked from and joined
+    // back into the pool's stream
+    const int Gn = (int)P->h_groups.size() - 1;
+    std::vector<cudaStream_t> ss;
+    if ((rc = sweep_streams(P, P->grp_NS, ss)) || (rc = ensure_events(P->grp_ev, ss.size() + 1))) return rc;
+    const int NS = (int)ss.size();
+    std::vector<cudaGraphExec_t> gex(Gn, nullptr);
+    if (use_graph)
+      for (int g = 0; g < Gn; g++)
+        if ((rc = group_graph(P, P->h_groups[g], P->h_groups[g + 1], nsweeps, &gex[g], true))) return rc;
+    PCK(cudaEventRecord(P->grp_ev[0], P->st));
+    for (int k = 0; k < NS; k++) PCK(cudaStreamWaitEvent(ss[k], P->grp_ev[0], 0));
+    for (int g = 0; g < Gn; g++) {
+      if (use_graph) {
+        PCK(cudaGraphLaunch(gex[g], ss[g % NS]));
+      } else {
+        cudaStream_t home = P->st;
+        P->st = ss[g % NS];
+        int64_t t1[SU2GPU_NCOUNTERS] = {0};
+        rc = enqueue_group_sweep(P, P->h_groups[g], P->h_groups[g + 1], nsweeps, t1, true);
+        P->st = home;
+        if (rc) return rc;
+      }
+    }
+    for (int k = 0; k < NS; k++) {
+      PCK(cudaEventRecord(P->grp_ev[k + 1], ss[k]));
+      PCK(cudaStreamWaitEvent(P->st, P->grp_ev[k + 1], 0));
+    }
+    std::vector<PassDesc> passes;
+    sweep_recipe(P->recipe, passes, tot);
   } else if (use_graph) {
     if (!P->gexec) {
       cudaGraph_t graph;
@@ -1090,9 +1159,9 @@ static bool group_persistent(const su2gpu_pool* P, int a0, int a1) {
 
 // `n` sweeps of the active chains [a0, a1): their tile ranges and sweep
 // counters (persistent: one launch; otherwise one launch per pass and sweep)
-static int enqueue_group_sweep(su2gpu_pool* P, int a0, int a1, int n, int64_t* tot) {
+static int enqueue_group_sweep(su2gpu_pool* P, int a0, int a1, int n, int64_t* tot, bool per_pass) {
   uint32_t* const* sweeps = (uint32_t* const*)P->sweepptrs.p + a0;
-  if (group_persistent(P, a0, a1)) {
+  if (!per_pass && group_persistent(P, a0, a1)) {
     const int4* sg = (const int4*)P->segs.p + P->h_sfirst[a0];
     return enqueue_persist(P, sg, P->h_sfirst[a1] - P->h_sfirst[a0], sweeps, a1 - a0, n, tot);
   }
@@ -1114,9 +1183,9 @@ static int enqueue_group_sweep(su2gpu_pool* P, int a0, int a1, int n, int64_t* t
 
 // the sweep graph of the group [a0, a1) (n sweeps per replay), captured on
 // the pool's own stream
-static int group_graph(su2gpu_pool* P, int a0, int a1, int n, cudaGraphExec_t* out) {
+static int group_graph(su2gpu_pool* P, int a0, int a1, int n, cudaGraphExec_t* out, bool per_pass) {
   for (auto& gg : P->ggraphs)
-    if (gg.a0 == a0 && gg.a1 == a1 && gg.n == n) {
+    if (gg.a0 == a0 && gg.a1 == a1 && gg.n == n && gg.per_pass == per_pass) {
       *out = gg.exec;
       return SU2GPU_OK;
     }
@@ -1127,7 +1196,7 @@ static int group_graph(su2gpu_pool* P, int a0, int a1, int n, cudaGraphExec_t* o
   cudaGraph_t graph;
   PCK(cudaStreamBeginCapture(P->st, cudaStreamCaptureModeThreadLocal));
   int64_t tot[SU2GPU_NCOUNTERS] = {0};
-  int rc = enqueue_group_sweep(P, a0, a1, n, tot);
+  int rc = enqueue_group_sweep(P, a0, a1, n, tot, per_pass);
   cudaError_t e = cudaStreamEndCapture(P->st, &graph);
   P->st = exec;
   if (rc) return rc;
@@ -1136,7 +1205,7 @@ static int group_graph(su2gpu_pool* P, int a0, int a1, int n, cudaGraphExec_t* o
   e = cudaGraphInstantiate(&ge, graph, 0);
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) return fail(SU2GPU_ERR_CUDA, "group graph instantiate: %s", cudaGetErrorString(e));
-  P->ggraphs.push_back({a0, a1, n, ge});
+  P->ggraphs.push_back({a0, a1, n, per_pass, ge});
   *out = ge;
   return SU2GPU_OK;
 }
@@ -1155,20 +1224,17 @@ static void enqueue_group_measure(su2gpu_pool* P, int a0, int a1, double* sums) 
   launch_pool_reduce(part, b1 - b0, (const int*)P->mfirst.p + a0, b0, a1 - a0, sums + (size_t)a0 * NSUMS, P->st);
 }
 
-// groups of consecutive active chains: the middle ones with about equal
-// numbers of sites, the first and the last a quarter of that (the first
-// group's upload and the last one's download are not hidden under sweeps)
-static std::vector<int> cycle_groups(const su2gpu_pool* P) {
+// groups of consecutive active chains, G of them with about equal numbers of
+// sites; light_ends: the first and the last a quarter of the others (the
+// first group's upload and the last one's download in a cycle are not hidden
+// under sweeps)
+static std::vector<int> make_groups(const su2gpu_pool* P, int G, bool light_ends) {
   const int na = (int)P->active.size();
   int64_t total = 0;
   for (int s : P->active) total += P->slots[s].g.V;
-  const int64_t bytes = total * STAGE_REALS * 8;
-  int G = (int)std::min<int64_t>(16, std::max<int64_t>(1, bytes / (64ll << 20)));
-  const char* e = getenv("SU2GPU_CYCLE_GROUPS");
-  if (e && *e) G = std::max(1, atoi(e));
-  G = std::min(G, na);
+  G = std::max(1, std::min(G, na));
   std::vector<double> edge(G + 1, 0.0);  // cumulative weight at each group's end
-  for (int g = 0; g < G; g++) edge[g + 1] = edge[g] + ((G > 2 && (g == 0 || g == G - 1)) ? 0.25 : 1.0);
+  for (int g = 0; g < G; g++) edge[g + 1] = edge[g] + ((light_ends && G > 2 && (g == 0 || g == G - 1)) ? 0.25 : 1.0);
   std::vector<int> b(1, 0);
   int64_t acc = 0;
   for (int a = 0; a < na; a++) {
@@ -1178,6 +1244,32 @@ static std::vector<int> cycle_groups(const su2gpu_pool* P) {
   }
   b.push_back(na);
   return b;
+}
+
+// the cycle's groups: about 64 MB of host arrays each, at most 32
+static std::vector<int> cycle_groups(const su2gpu_pool* P) {
+  int64_t total = 0;
+  for (int s : P->active) total += P->slots[s].g.V;
+  const int64_t bytes = total * STAGE_REALS * 8;
+  int G = (int)std::min<int64_t>(32, std::max<int64_t>(1, bytes / (64ll << 20)));
+  const char* e = getenv("SU2GPU_CYCLE_GROUPS");
+  if (e && *e) G = std::max(1, atoi(e));
+  return make_groups(P, G, true);
+}
+
+// NS of the pool's update streams (highest priority), created on first use
+static int sweep_streams(su2gpu_pool* P, int NS, std::vector<cudaStream_t>& ss) {
+  NS = std::max(1, std::min(NS, su2gpu_pool::CYCLE_SWEEP_STREAMS));
+  ss.assign(NS, nullptr);
+  for (int k = 0; k < NS; k++) {
+    if (!P->sweep_st[k]) {
+      int least = 0, greatest = 0;
+      cudaDeviceGetStreamPriorityRange(&least, &greatest);
+      PCK(cudaStreamCreateWithPriority(&P->sweep_st[k], cudaStreamNonBlocking, greatest));
+    }
+    ss[k] = P->sweep_st[k];
+  }
+  return SU2GPU_OK;
 }
 
 int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const double* const* const* in, int32_t nsweeps,
@@ -1207,11 +1299,24 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
   std::vector<cudaGraphExec_t> gex(G, nullptr);
   // sweeps per graph replay: all of them in one persistent launch, else one
   std::vector<int> per_replay(G, 1);
+  bool any_persistent = false;
   for (int g = 0; g < G; g++)
-    if (group_persistent(P, groups[g], groups[g + 1])) per_replay[g] = std::max(1, (int)nsweeps);
+    if (group_persistent(P, groups[g], groups[g + 1])) {
+      per_replay[g] = std::max(1, (int)nsweeps);
+      any_persistent = true;
+    }
+  // the groups' sweeps (one launch per pass: a group is a few waves of
+  // blocks, each pass with its ramp and tail) run on NS streams in turn, so
+  // that consecutive groups fill each other's gaps; persistent groups share
+  // the work counters and stay on one stream
+  int NS = any_persistent ? 1 : std::min(G, 3);
+  if (const char* e = getenv("SU2GPU_CYCLE_STREAMS"); e && *e && !any_persistent)
+    NS = std::max(1, std::min(std::min(G, su2gpu_pool::CYCLE_SWEEP_STREAMS), atoi(e)));
+  std::vector<cudaStream_t> ss;
+  if ((rc = sweep_streams(P, NS, ss))) return rc;
   if (use_graph && nsweeps > 0)
     for (int g = 0; g < G; g++)
-      if ((rc = group_graph(P, groups[g], groups[g + 1], per_replay[g], &gex[g]))) return rc;
+      if ((rc = group_graph(P, groups[g], groups[g + 1], per_replay[g], &gex[g], false))) return rc;
   // staging bytes of every group; a group's chains sit side by side in the
   // rings (a ring holds the largest group at least), so a chain only ever
   // overlaps chains of earlier groups, whose release events are recorded
@@ -1222,7 +1327,7 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
   Ring up, down;
   if ((rc = ensure_stream(&P->copy_st)) || (rc = ensure_stream(&P->down_st)) ||
       (rc = ensure_ring(P, P->ring, total, gmax, &up)) || (rc = ensure_ring(P, P->ring_down, total, gmax, &down)) ||
-      (rc = ensure_events(P->cyc_ev, 4 * (size_t)G + 1)) || (rc = P->d_items.ensure(2 * (size_t)na * sizeof(ConvItem))))
+      (rc = ensure_events(P->cyc_ev, 4 * (size_t)G + 1 + NS)) || (rc = P->d_items.ensure(2 * (size_t)na * sizeof(ConvItem))))
     return rc;
   if (P->h_items_n < 2 * (size_t)na) {
     if (P->h_items) cudaFreeHost(P->h_items);
@@ -1237,6 +1342,7 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
   PCK(cudaEventRecord(ev[4 * G], P->st));
   PCK(cudaStreamWaitEvent(P->copy_st, ev[4 * G], 0));
   PCK(cudaStreamWaitEvent(P->down_st, ev[4 * G], 0));
+  for (int k = 0; k < NS; k++) PCK(cudaStreamWaitEvent(ss[k], ev[4 * G], 0));
   int64_t tot[SU2GPU_NCOUNTERS] = {0};
   // one chain's host arrays and their staging layout
   auto layout = [&](int a, const double* const* const* tab, double** hp, ConvItem* it, size_t* bytes) {
@@ -1280,18 +1386,29 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
     PCK(cudaMemcpyAsync(dit + a0, P->h_items + a0, (a1 - a0) * sizeof(ConvItem), cudaMemcpyHostToDevice, P->copy_st));
     P->pops->pool_convert(P->descs.p, dit + a0, a1 - a0, vmax, (double*)up.base, 1, P->copy_st);
     PCK(cudaEventRecord(ev[4 * g + 1], P->copy_st));
-    // update stream: the group's sweeps and measurement
-    PCK(cudaStreamWaitEvent(P->st, ev[4 * g + 1], 0));
-    if (nsweeps > 0) {
-      if (use_graph) {
-        for (int k = 0; k < nsweeps; k += per_replay[g]) PCK(cudaGraphLaunch(gex[g], P->st));
-      } else {
-        int64_t t1[SU2GPU_NCOUNTERS] = {0};
-        if ((rc = enqueue_group_sweep(P, a0, a1, nsweeps, t1))) return rc;
-      }
+    // update stream of the group: its sweeps and measurement (the enqueue
+    // helpers launch on P->st, pointed at that stream meanwhile)
+    {
+      cudaStream_t home = P->st;
+      P->st = ss[g % NS];
+      auto group_work = [&]() -> int {
+        PCK(cudaStreamWaitEvent(P->st, ev[4 * g + 1], 0));
+        if (nsweeps > 0) {
+          if (use_graph) {
+            for (int k = 0; k < nsweeps; k += per_replay[g]) PCK(cudaGraphLaunch(gex[g], P->st));
+          } else {
+            int64_t t1[SU2GPU_NCOUNTERS] = {0};
+            if (int r = enqueue_group_sweep(P, a0, a1, nsweeps, t1, false)) return r;
+          }
+        }
+        if (sums) enqueue_group_measure(P, a0, a1, (double*)P->sums.p);
+        PCK(cudaEventRecord(ev[4 * g + 2], P->st));
+        return SU2GPU_OK;
+      };
+      rc = group_work();
+      P->st = home;
+      if (rc) return rc;
     }
-    if (sums) enqueue_group_measure(P, a0, a1, (double*)P->sums.p);
-    PCK(cudaEventRecord(ev[4 * g + 2], P->st));
     // download stream: one conversion launch into staging, then the copies
     // to the host arrays
     PCK(cudaStreamWaitEvent(P->down_st, ev[4 * g + 2], 0));
@@ -1327,6 +1444,11 @@ int su2gpu_pool_cycle(su2gpu_pool* P, int32_t n, const int32_t* slots, const dou
   {
     std::vector<PassDesc> passes;
     sweep_recipe(P->recipe, passes, tot);
+  }
+  // the pool's stream follows the other update streams
+  for (int k = 0; k < NS; k++) {
+    PCK(cudaEventRecord(ev[4 * G + 1 + k], ss[k]));
+    PCK(cudaStreamWaitEvent(P->st, ev[4 * G + 1 + k], 0));
   }
   std::vector<double> hs;
   if (sums) {
@@ -1495,6 +1617,7 @@ int su2gpu_pool_launches_per_sweep(su2gpu_pool* P, int32_t* n) {
     *n = 2;
     return SU2GPU_OK;
   }
+  const int ngroups = P->grouped ? (int)P->h_groups.size() - 1 : 1;
   // the recipe's passes per sweep, in the order of enqueue_pool_sweep
   const su2gpu_params& p = P->recipe;
   const int nh = nhiggs_of(p.content);
@@ -1516,7 +1639,27 @@ int su2gpu_pool_launches_per_sweep(su2gpu_pool* P, int32_t* n) {
   for (int h = 0; h < nh; h++)
     if (P->mucamask >> h & 1) passes += 2 * count(p.update_su2doublet, p.algorithm_su2doublet, 1);
   if ((p.content & SU2GPU_TRIPLET) && (P->mucamask & 4)) passes += 2 * count(p.update_su2triplet, p.algorithm_su2triplet, 1);
-  *n = passes + 1;  // + the sweep-counter increment
+  *n = ngroups * (passes + 1);  // + the sweep-counter increment (per group)
+  return SU2GPU_OK;
+}
+
+int su2gpu_pool_set_sweep_groups(su2gpu_pool* P, int32_t groups, int32_t streams) {
+  if (!P || streams < 1 || streams > su2gpu_pool::CYCLE_SWEEP_STREAMS)
+    return fail(SU2GPU_ERR_INVALID, "sweep groups: 1 to %d streams", su2gpu_pool::CYCLE_SWEEP_STREAMS);
+  PCK(cudaStreamSynchronize(P->st));
+  P->grp_G = groups > 1 ? groups : 0;
+  P->grp_NS = groups > 1 ? streams : 1;
+  P->dirty = true;
+  drop_graphs(P);
+  return SU2GPU_OK;
+}
+
+int su2gpu_pool_get_sweep_groups(su2gpu_pool* P, int32_t* groups, int32_t* streams) {
+  if (!P || !groups || !streams) return SU2GPU_ERR_INVALID;
+  int rc;
+  if (P->dirty && (rc = rebuild(P))) return rc;
+  *groups = P->grouped ? (int)P->h_groups.size() - 1 : 0;
+  *streams = P->grouped ? std::min(P->grp_NS, su2gpu_pool::CYCLE_SWEEP_STREAMS) : 1;
   return SU2GPU_OK;
 }
 
@@ -1607,6 +1750,74 @@ int su2gpu_pool_counters(su2gpu_pool* P, int32_t s, int64_t* out) {
 }
 
 // launch shapes for the pool's kernels, timed on a scratch copy of the arena
+// mean time of one sweep of every chain (no sweep-counter increment) with
+// the chains in G groups whose sweeps (one launch per pass, a graph per
+// group) run on NS streams in turn; G = 1: one stream, one graph
+static int time_grouped(su2gpu_pool* P, void* descs, int G, int NS, int reps, float* ms_out) {
+  const std::vector<int> groups = make_groups(P, G, false);
+  const int Gn = (int)groups.size() - 1;
+  std::vector<cudaGraphExec_t> gex(Gn, nullptr);
+  std::vector<cudaStream_t> ss;
+  int rc;
+  if ((rc = sweep_streams(P, NS, ss)) || (rc = ensure_events(P->grp_ev, ss.size() + 1))) return rc;
+  cudaStream_t exec = P->st;
+  PCK(cudaStreamSynchronize(exec));
+  PCK(cudaStreamSynchronize(P->own_st));
+  cudaEvent_t e0, e1;  // timing events (the pool's join events record no time)
+  PCK(cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return fail(SU2GPU_ERR_CUDA, "cudaEventCreate failed");
+  }
+  for (int g = 0; g < Gn && !rc; g++) {
+    const int2* tiles[NVARIANTS];
+    int nt[NVARIANTS];
+    for (int v = 0; v < NVARIANTS; v++) {
+      tiles[v] = (const int2*)P->tiles[v].p + P->h_tfirst[v][groups[g]];
+      nt[v] = P->h_tfirst[v][groups[g + 1]] - P->h_tfirst[v][groups[g]];
+    }
+    P->st = P->own_st;
+    cudaGraph_t graph;
+    int64_t t1[SU2GPU_NCOUNTERS] = {0};
+    cudaError_t e = cudaStreamBeginCapture(P->st, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      rc = enqueue_pool_sweep(P, descs, tiles, nt, t1);
+      e = cudaStreamEndCapture(P->st, &graph);
+      if (e == cudaSuccess) {
+        e = cudaGraphInstantiate(&gex[g], graph, 0);
+        cudaGraphDestroy(graph);
+      }
+    }
+    P->st = exec;
+    if (!rc && e != cudaSuccess) rc = fail(SU2GPU_ERR_CUDA, "grouped sweep timing: %s", cudaGetErrorString(e));
+  }
+  float ms = 0.f;
+  for (int r = -1; r < reps && !rc; r++) {
+    cudaEventRecord(e0, P->st);
+    for (int k = 0; k < (int)ss.size(); k++) cudaStreamWaitEvent(ss[k], e0, 0);
+    for (int g = 0; g < Gn; g++) cudaGraphLaunch(gex[g], ss[g % ss.size()]);
+    for (int k = 0; k < (int)ss.size(); k++) {
+      cudaEventRecord(P->grp_ev[k + 1], ss[k]);
+      cudaStreamWaitEvent(P->st, P->grp_ev[k + 1], 0);
+    }
+    cudaEventRecord(e1, P->st);
+    cudaError_t e = cudaEventSynchronize(e1);
+    if (e != cudaSuccess) {
+      rc = fail(SU2GPU_ERR_CUDA, "grouped sweep timing: %s", cudaGetErrorString(e));
+      break;
+    }
+    float t = 0.f;
+    cudaEventElapsedTime(&t, e0, e1);
+    if (r >= 0) ms += t;
+  }
+  for (cudaGraphExec_t g : gex)
+    if (g) cudaGraphExecDestroy(g);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms_out = ms / reps;
+  return rc;
+}
+
 int su2gpu_pool_autotune(su2gpu_pool* P, int32_t* choices, float* best_ms) {
   if (!P) return SU2GPU_ERR_INVALID;
   int rc;
@@ -1631,6 +1842,7 @@ int su2gpu_pool_autotune(su2gpu_pool* P, int32_t* choices, float* best_ms) {
   a.nslots = P->max_slots;
   a.err = (int*)P->err.p;
   const int reps = 3;
+  float base_ms = 0.f;  // one sweep in the mode the pool would use without groups
   for (int kind = 0; kind < 5; kind++) {
     if (!present[kind]) continue;
     float best = 1e30f;
@@ -1711,6 +1923,51 @@ int su2gpu_pool_autotune(su2gpu_pool* P, int32_t* choices, float* best_ms) {
     if (!rc) {
       P->seg_tuned = bestseg;
       P->dirty = true;  // the segment table is rebuilt with the pick
+      base_ms = best / reps;
+    }
+  }
+  // the grouped mode against the mode the pool would otherwise use (one
+  // persistent launch, or one launch per pass on one stream): one sweep of
+  // every chain per candidate (groups x streams), on the scratch copy
+  // SU2GPU_SWEEP_GROUPS="G,NS" fixes the pick (a profiler that serialises
+  // kernels cannot time the overlap the grouped mode is for)
+  const char* fixg = getenv("SU2GPU_SWEEP_GROUPS");
+  if (!rc && fixg && *fixg) {
+    int g = 0, ns = 1;
+    if (sscanf(fixg, "%d,%d", &g, &ns) >= 1) {
+      P->grp_G = g > 1 ? g : 0;
+      P->grp_NS = std::max(1, std::min(ns, su2gpu_pool::CYCLE_SWEEP_STREAMS));
+      P->dirty = true;
+    }
+  } else if (!rc && P->persist_mode == -1 && P->nmuca == 0 && P->active.size() >= 8) {
+    const int na = (int)P->active.size();
+    if (base_ms <= 0.f && (rc = time_grouped(P, desc2.p, 1, 1, reps, &base_ms))) {
+      // base_ms stays unset; rc is returned below
+    }
+    // (groups, streams): on the 384-chain ensemble 32-48 groups of ~0.3 M
+    // sites on 3-4 streams were fastest; small pools try a quarter, half and
+    // all of their chains as groups
+    std::vector<std::pair<int, int>> cand;
+    auto add = [&](int g, int ns) {
+      if (g < 3 || g > na) return;
+      for (auto& c : cand)
+        if (c.first == g && c.second == ns) return;
+      cand.push_back({g, ns});
+    };
+    for (int g : {24, 32, 48}) add(g, 3);
+    for (int g : {32, 48, 64}) add(g, 4);
+    for (int g : {na / 4, na / 2, na}) add(g, 3);
+    float bestg = base_ms;
+    int bg = 0, bns = 1;
+    for (size_t c = 0; c < cand.size() && !rc; c++) {
+      float ms = 0.f;
+      if ((rc = time_grouped(P, desc2.p, cand[c].first, cand[c].second, reps, &ms))) break;
+      if (ms < bestg) { bestg = ms; bg = cand[c].first; bns = cand[c].second; }
+    }
+    if (!rc) {
+      P->grp_G = bg;
+      P->grp_NS = bns;
+      P->dirty = true;
     }
   }
   cudaEventDestroy(e0);

@@ -108,6 +108,8 @@ def lib():
         L.su2gpu_pool_set_persist_shape.argtypes = [vp, i32]
         L.su2gpu_pool_get_persist_shape.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(i32)]
         L.su2gpu_pool_get_persistent.argtypes = [vp, ctypes.POINTER(i32)]
+        L.su2gpu_pool_set_sweep_groups.argtypes = [vp, i32, i32]
+        L.su2gpu_pool_get_sweep_groups.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(i32)]
         L.su2gpu_pool_check_wait_timeout.argtypes = [vp, i32, ctypes.POINTER(i32)]
         L.su2gpu_pool_raise_error.argtypes = [vp, i32]
         L.su2gpu_pool_muca_set.argtypes = [vp, i32, ctypes.POINTER(abi.Weight)]
@@ -640,6 +642,19 @@ class Pool:
     @persist_shape.setter
     def persist_shape(self, shape):
         check(lib().su2gpu_pool_set_persist_shape(self._h, int(shape)))
+
+    @property
+    def sweep_groups(self):
+        """(groups, streams) of the grouped sweep mode in effect ((0, 1): off)."""
+        g, n = ctypes.c_int32(), ctypes.c_int32()
+        check(lib().su2gpu_pool_get_sweep_groups(self._h, ctypes.byref(g), ctypes.byref(n)))
+        return g.value, n.value
+
+    @sweep_groups.setter
+    def sweep_groups(self, gs):
+        """(groups, streams); None or groups <= 1: off."""
+        g, n = (0, 1) if gs is None else gs
+        check(lib().su2gpu_pool_set_sweep_groups(self._h, int(g), int(n)))
 
     def check_wait_timeout(self, spin_limit=2000):
         """Run the persistent kernel on a work list whose dependencies never
