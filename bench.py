@@ -696,10 +696,14 @@ def persistent_roofline(kinds, launch_ms, S, content, prec, sites, workload, ste
         with open(tr_path) as fh:
             tj = json.load(fh)
         if groups:
-            # the same per-pass kernels over subsets of the chains: the DRAM
-            # bytes of one launch of each kind over all chains, per sweep
+            # one grouped sweep's launches captured by ncu (serialised), else
+            # the DRAM bytes of one launch of each kind over all chains
+            t = tj.get("pool_sweep_grouped_per_sweep")
             per = [tj.get(KIND_NAMES.get(int(k), "")) for k in kinds]
-            traffic = None if any(t is None for t in per) else sum(per) / nsw * S
+            if t is not None:
+                traffic = t * S
+            else:
+                traffic = None if any(x is None for x in per) else sum(per) / nsw * S
         else:
             t = tj.get("pool_sweep_persistent_per_sweep")
             traffic = None if t is None else t * S
