@@ -1750,9 +1750,13 @@ int su2gpu_pool_counters(su2gpu_pool* P, int32_t s, int64_t* out) {
 }
 
 // launch shapes for the pool's kernels, timed on a scratch copy of the arena
+// sweeps per timed launch when the autotuner compares sweep modes: several,
+// so that ramps, tails and the streams' drift weigh as in a run
+constexpr int TUNE_SWEEPS = 3;
+
 // mean time of one sweep of every chain (no sweep-counter increment) with
-// the chains in G groups whose sweeps (one launch per pass, a graph per
-// group) run on NS streams in turn; G = 1: one stream, one graph
+// the chains in G groups whose TUNE_SWEEPS sweeps (one launch per pass, a
+// graph per group) run on NS streams in turn; G = 1: one stream, one graph
 static int time_grouped(su2gpu_pool* P, void* descs, int G, int NS, int reps, float* ms_out) {
   const std::vector<int> groups = make_groups(P, G, false);
   const int Gn = (int)groups.size() - 1;
@@ -1781,7 +1785,7 @@ static int time_grouped(su2gpu_pool* P, void* descs, int G, int NS, int reps, fl
     int64_t t1[SU2GPU_NCOUNTERS] = {0};
     cudaError_t e = cudaStreamBeginCapture(P->st, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-      rc = enqueue_pool_sweep(P, descs, tiles, nt, t1);
+      for (int k = 0; k < TUNE_SWEEPS && !rc; k++) rc = enqueue_pool_sweep(P, descs, tiles, nt, t1);
       e = cudaStreamEndCapture(P->st, &graph);
       if (e == cudaSuccess) {
         e = cudaGraphInstantiate(&gex[g], graph, 0);
@@ -1814,7 +1818,7 @@ static int time_grouped(su2gpu_pool* P, void* descs, int G, int NS, int reps, fl
     if (g) cudaGraphExecDestroy(g);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  *ms_out = ms / reps;
+  *ms_out = ms / reps / TUNE_SWEEPS;
   return rc;
 }
 
@@ -1917,18 +1921,44 @@ int su2gpu_pool_autotune(su2gpu_pool* P, int32_t* choices, float* best_ms) {
       }
       if (ms < best) { best = ms; bestseg = seg; bestshape = shape; }
     }
-    segbuf.release();
     P->persist_shape = bestshape;
     P->persist_grid = P->persist_grids[bestshape];
     if (!rc) {
       P->seg_tuned = bestseg;
       P->dirty = true;  // the segment table is rebuilt with the pick
-      base_ms = best / reps;
+      // the pick with TUNE_SWEEPS sweeps per launch: the baseline of the
+      // grouped mode below
+      tab.clear();
+      for (int s : P->active) append_segments(P, s, bestseg, tab);
+      if (!(rc = segbuf.ensure(tab.size() * sizeof(int4)))) {
+        PCK(cudaMemcpyAsync(segbuf.p, tab.data(), tab.size() * sizeof(int4), cudaMemcpyHostToDevice, P->st));
+        float ms = 0.f;
+        for (int r = -1; r < reps && !rc; r++) {
+          int64_t t1[SU2GPU_NCOUNTERS] = {0};
+          cudaEventRecord(e0, P->st);
+          rc = enqueue_persist(P, (const int4*)segbuf.p, (int)tab.size(), nullptr, (int)P->active.size(),
+                               TUNE_SWEEPS, t1, 0, 1 << 18, desc2.p, bestseg);
+          cudaEventRecord(e1, P->st);
+          if (rc) break;
+          PCK(cudaEventSynchronize(e1));
+          float t = 0.f;
+          cudaEventElapsedTime(&t, e0, e1);
+          if (r >= 0) ms += t;
+        }
+        int herr = 0;
+        PCK(cudaMemcpyAsync(&herr, P->err.p, sizeof(int), cudaMemcpyDeviceToHost, P->st));
+        PCK(cudaStreamSynchronize(P->st));
+        if (herr) PCK(cudaMemsetAsync(P->err.p, 0, sizeof(int), P->st));
+        // a baseline whose wait gave up is not trusted: the grouped mode is
+        // then compared with one launch per pass
+        if (!rc && !herr) base_ms = ms / reps / TUNE_SWEEPS;
+      }
     }
+    segbuf.release();
   }
   // the grouped mode against the mode the pool would otherwise use (one
-  // persistent launch, or one launch per pass on one stream): one sweep of
-  // every chain per candidate (groups x streams), on the scratch copy
+  // persistent launch, or one launch per pass on one stream): TUNE_SWEEPS
+  // sweeps of every chain per candidate (groups x streams), on the scratch copy
   // SU2GPU_SWEEP_GROUPS="G,NS" fixes the pick (a profiler that serialises
   // kernels cannot time the overlap the grouped mode is for)
   const char* fixg = getenv("SU2GPU_SWEEP_GROUPS");
@@ -1944,9 +1974,9 @@ int su2gpu_pool_autotune(su2gpu_pool* P, int32_t* choices, float* best_ms) {
     if (base_ms <= 0.f && (rc = time_grouped(P, desc2.p, 1, 1, reps, &base_ms))) {
       // base_ms stays unset; rc is returned below
     }
-    // (groups, streams): on the 384-chain ensemble 32-48 groups of ~0.3 M
-    // sites on 3-4 streams were fastest; small pools try a quarter, half and
-    // all of their chains as groups
+    // (groups, streams): on the 384-chain ensemble (11 M sites) groups of
+    // about 0.23 M sites on 4 streams were fastest (48 groups); the
+    // candidates are around that group size, on 3 and 4 streams
     std::vector<std::pair<int, int>> cand;
     auto add = [&](int g, int ns) {
       if (g < 3 || g > na) return;
@@ -1954,9 +1984,16 @@ int su2gpu_pool_autotune(su2gpu_pool* P, int32_t* choices, float* best_ms) {
         if (c.first == g && c.second == ns) return;
       cand.push_back({g, ns});
     };
-    for (int g : {24, 32, 48}) add(g, 3);
-    for (int g : {32, 48, 64}) add(g, 4);
-    for (int g : {na / 4, na / 2, na}) add(g, 3);
+    int64_t total_sites = 0;
+    for (int s : P->active) total_sites += P->slots[s].g.V;
+    const int gt = (int)std::max<int64_t>(3, (total_sites + 115000) / 230000);
+    for (int ns : {4, 3}) {
+      add(gt, ns);
+      add(gt * 2 / 3, ns);
+      add(gt * 4 / 3, ns);
+    }
+    add(gt / 2, 3);
+    add(gt * 2, 4);
     float bestg = base_ms;
     int bg = 0, bns = 1;
     for (size_t c = 0; c < cand.size() && !rc; c++) {
