@@ -876,10 +876,19 @@ def run_gpu_batched(args):
         e2e_step()
         n_e2e = max(n_e2e, 20)
         tsteps = []
-        for k in range(n_e2e):
-            t0 = time.perf_counter()
-            e2e_step()
-            tsteps.append(time.perf_counter() - t0)
+        # the interpreter's cyclic garbage collector is held off while the
+        # steps are timed (a full collection over the harness's objects
+        # took 100-200 ms inside one step); it runs before and after
+        import gc
+        gc.collect()
+        gc.disable()
+        try:
+            for k in range(n_e2e):
+                t0 = time.perf_counter()
+                e2e_step()
+                tsteps.append(time.perf_counter() - t0)
+        finally:
+            gc.enable()
         for a in arrays:
             gpu.host_unregister(a)
         # the host and its memory are shared with other jobs: a step now and
