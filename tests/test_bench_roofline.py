@@ -44,6 +44,22 @@ def test_persistent_roofline_reads_traffic_per_sweep(bench):
     assert r["traffic"] is not None and r["traffic"] > 10 * 0.9 * (6 * 17 + 10 * 16.5) * 4 * 11011520
 
 
+def test_grouped_roofline_uses_the_grouped_traffic(bench):
+    # the grouped sweep: the same algorithmic bytes over the fork-to-join time,
+    # the DRAM traffic ncu measured for one grouped sweep (its groups' fields
+    # stay in L2 across their passes: far below the algorithmic bytes)
+    sites, S = 11011520, 10
+    r = bench.persistent_roofline(one_sweep_kinds(), [21.8], S, "adj", 32, sites, "batched384_adj_f32",
+                                  step_ms=22.5, groups=(48, 4))
+    per_sweep = (6 * 17 + 10 * 16.5) * 4 * sites
+    assert r["algorithmic_bytes_per_launch"] == pytest.approx(per_sweep * S)
+    assert "48 groups on 4 streams" in r["kernel"]
+    assert r["traffic"] is not None and r["traffic"] < 0.2 * per_sweep * S
+    p = bench.persistent_roofline(one_sweep_kinds(), [21.8], S, "adj", 32, sites, "batched384_adj_f32",
+                                  step_ms=22.5)
+    assert p["traffic"] > r["traffic"] and "k_pool_persist" in p["kernel"]
+
+
 def test_per_pass_roofline_picks_the_largest_share(bench):
     kinds = one_sweep_kinds(2)
     ms = np.where(kinds == 0, 0.18, 0.16)
