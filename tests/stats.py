@@ -102,14 +102,22 @@ def kp_a0_cdf(alpha):
 
 def chains_mean(chains):
     """Mean over independent chains and its error: the chains' binned
-    jackknife errors (each aware of its own autocorrelation) combined."""
+    jackknife errors (each aware of its own autocorrelation) combined, or,
+    with 8 chains or more, the spread of the chain means if that is larger.
+    The spread needs no autocorrelation estimate: repeated 64-chain runs of
+    slow observables (the adjoint Tr Sigma^2 and hopping term at 8^3) with
+    other seeds scattered about twice as far as the combined jackknife errors
+    said, so the per-chain windows can understate the error."""
     ms, es = [], []
     for x in chains:
         m, e, _ = jackknife_mean(x)
         ms.append(m)
         es.append(e)
     n = len(ms)
-    return float(np.mean(ms)), float(np.sqrt(np.sum(np.square(es))) / n)
+    err = float(np.sqrt(np.sum(np.square(es))) / n)
+    if n >= 8:
+        err = max(err, float(np.std(ms, ddof=1) / np.sqrt(n)))
+    return float(np.mean(ms)), err
 
 
 def compare_chain_means(a_chains, b_chains):
