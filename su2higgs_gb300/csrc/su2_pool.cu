@@ -2001,9 +2001,12 @@ int su2gpu_pool_autotune(su2gpu_pool* P, int32_t* choices, float* best_ms) {
       if ((rc = time_grouped(P, desc2.p, cand[c].first, cand[c].second, reps, &ms))) break;
       if (ms < bestg) { bestg = ms; bg = cand[c].first; bns = cand[c].second; }
     }
+    // the grouped mode only where it wins clearly (2 %): a near tie is left to
+    // the mode the pool would use anyway
+    if (bg && !(bestg < 0.98f * base_ms)) bg = 0;
     if (!rc) {
       P->grp_G = bg;
-      P->grp_NS = bns;
+      P->grp_NS = bg ? bns : 1;
       P->dirty = true;
     }
   }
